@@ -1,0 +1,370 @@
+"""GB300 sampling library with EigenRand's call surface.
+
+Python mirror of the ``Eigen::Rand`` API (bab2min/EigenRand v0.6.0) over the
+C ABI in include/gpurand.h.  Engines and generator caches live in HBM; outputs
+are CUDA tensors laid out column-major like Eigen arrays (shape (rows, cols),
+memory order = Eigen's linear index).  torch is used only for device memory
+and the current CUDA stream.
+
+    import eigenrand_gb300 as er
+    urng = er.Vmt19937_64(42)                       # Eigen::Rand::Vmt19937_64 urng{42};
+    x = er.normal(4096, 4096, urng)                 # Eigen::Rand::normal<ArrayXXf>(4096, 4096, urng)
+    g = er.GammaGen(0.5, 1.0, dtype=torch.float64)  # Eigen::Rand::GammaGen<double> g{0.5, 1.0};
+    y = g.generate(1024, 1024, urng)
+
+Values are bit-identical to EigenRand built for x86-64 AVX2 with Eigen 3.4
+(Vmt19937_64 = 4 lanes, float packets of 8, double 4, int32 4) wherever the
+reference's arithmetic is IEEE-exact; log/exp are this library's own <=1-ulp
+implementations (see csrc/gr_math.cuh).
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import GrError, KINDS, F32, F64, I32, U64
+
+__all__ = [
+    "GrError", "Vmt19937_64", "raw_u64", "version",
+    "uniformReal", "balanced", "normal", "lognormal", "exponential", "cauchy", "weibull", "extremeValue",
+    "gamma", "beta", "studentT", "chiSquared", "poisson", "binomial", "discrete", "randBits",
+    "StdUniformRealGen", "UniformRealGen", "BalancedGen", "Balanced2Gen", "StdNormalGen", "NormalGen",
+    "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
+    "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen",
+]
+
+_lib.load()
+_L = _lib._lib
+
+
+def version():
+    return _L.gr_version().decode()
+
+
+def _stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Vmt19937_64:
+    """Eigen::Rand::Vmt19937_64 (PacketRandomEngine.h:585-599), device resident.
+
+    streams=1: one 4-lane engine, lane l = std::mt19937_64(seed + l).
+    streams=K: K independent engines seeded seed + 4k; every call splits its
+    output into K contiguous slices, slice k drawn from engine k.
+    """
+
+    default_seed = 5489
+
+    def __init__(self, seed=default_seed, streams=1, lanes=4):
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_engine_create(ctypes.byref(h), ctypes.c_uint64(seed), lanes, streams))
+        self._h = h
+        self.streams = streams
+        self.lanes = lanes
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _L is not None:
+            _L.gr_engine_destroy(h)
+            self._h = None
+
+    def seed(self, seed, stream=None):
+        _lib.check(_L.gr_engine_seed(self._h, ctypes.c_uint64(seed), _stream_ptr(stream)))
+
+    def discard(self, npackets, stream=None):
+        _lib.check(_L.gr_engine_discard(self._h, ctypes.c_uint64(npackets), _stream_ptr(stream)))
+
+    def state_size(self):
+        return _L.gr_engine_state_size(self._h)
+
+    def save(self, stream=None):
+        buf = ctypes.create_string_buffer(self.state_size())
+        _lib.check(_L.gr_engine_save(self._h, buf, len(buf), _stream_ptr(stream)))
+        return bytes(buf.raw)
+
+    def restore(self, blob, stream=None):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        _lib.check(_L.gr_engine_restore(self._h, buf, len(blob), _stream_ptr(stream)))
+
+    def sync(self, stream=None):
+        _lib.check(_L.gr_engine_sync(self._h, _stream_ptr(stream)))
+
+
+def _empty(rows, cols, dtype, out):
+    if out is not None:
+        return out
+    return torch.empty((cols, rows), dtype=dtype, device="cuda").t()
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def raw_u64(urng, n, out=None, stream=None):
+    """makeUniversalRng<uint64_t>(urng)() repeated n times (PacketRandomEngine.h:468-475).
+
+    Returns an int64 tensor holding the uint64 bit patterns."""
+    o = out if out is not None else torch.empty(n, dtype=torch.int64, device="cuda")
+    _lib.check(_L.gr_raw_u64(urng._h, _ptr(o), n, _stream_ptr(stream)))
+    return o
+
+
+_DT = {torch.float32: F32, torch.float64: F64, torch.int32: I32}
+
+
+def _desc(kind, dtype, a=0.0, b=0.0, trials=0, weights=None):
+    d = _lib.DistDesc()
+    d.kind = KINDS[kind]
+    d.dtype = _DT[dtype]
+    d.a = float(a)
+    d.b = float(b)
+    d.trials = int(trials)
+    keep = None
+    if weights is not None:
+        keep = (ctypes.c_double * len(weights))(*[float(w) for w in weights])
+        d.nweights = len(weights)
+        d.weights = ctypes.cast(keep, ctypes.POINTER(ctypes.c_double))
+    return d, keep
+
+
+class _Gen:
+    """One generator object (mirrors a *Gen instance, caches included)."""
+
+    _kind = None
+
+    def __init__(self, dtype, a=0.0, b=0.0, trials=0, weights=None, kind=None):
+        self.dtype = dtype
+        self._desc, self._keep = _desc(kind or self._kind, dtype, a, b, trials, weights)
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_gen_create(ctypes.byref(h), ctypes.byref(self._desc)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _L is not None:
+            _L.gr_gen_destroy(h)
+            self._h = None
+
+    def generate(self, rows, cols, urng, out=None, stream=None):
+        o = _empty(rows, cols, self.dtype, out)
+        _lib.check(_L.gr_generate(self._h, urng._h, _ptr(o), rows * cols, _stream_ptr(stream)))
+        return o
+
+    def generateLike(self, o, urng, stream=None):
+        return self.generate(o.shape[0], o.shape[1], urng, stream=stream)
+
+
+def _sample(kind, rows, cols, urng, dtype, a=0.0, b=0.0, trials=0, weights=None, out=None, stream=None):
+    o = _empty(rows, cols, dtype, out)
+    d, keep = _desc(kind, dtype, a, b, trials, weights)
+    _lib.check(_L.gr_sample(urng._h, ctypes.byref(d), _ptr(o), rows * cols, _stream_ptr(stream)))
+    del keep
+    return o
+
+
+# ---- generator classes (Dists/*.h) --------------------------------------
+class StdUniformRealGen(_Gen):
+    _kind = "UNIFORM_REAL"
+
+    def __init__(self, dtype=torch.float32):
+        super().__init__(dtype)
+
+
+class UniformRealGen(_Gen):
+    _kind = "UNIFORM_REAL2"
+
+    def __init__(self, min=0.0, max=1.0, dtype=torch.float32):
+        super().__init__(dtype, min, max)
+
+
+class BalancedGen(_Gen):
+    _kind = "BALANCED"
+
+    def __init__(self, dtype=torch.float32):
+        super().__init__(dtype)
+
+
+class Balanced2Gen(_Gen):
+    _kind = "BALANCED2"
+
+    def __init__(self, a=-1.0, b=1.0, dtype=torch.float32):
+        super().__init__(dtype, a, b)
+
+
+class StdNormalGen(_Gen):
+    _kind = "NORMAL_STD"
+
+    def __init__(self, dtype=torch.float32):
+        super().__init__(dtype)
+
+
+class NormalGen(_Gen):
+    _kind = "NORMAL"
+
+    def __init__(self, mean=0.0, stdev=1.0, dtype=torch.float32):
+        super().__init__(dtype, mean, stdev)
+
+
+class LognormalGen(_Gen):
+    _kind = "LOGNORMAL"
+
+    def __init__(self, mean=0.0, stdev=1.0, dtype=torch.float32):
+        super().__init__(dtype, mean, stdev)
+
+
+class ExponentialGen(_Gen):
+    _kind = "EXPONENTIAL"
+
+    def __init__(self, lambda_=1.0, dtype=torch.float32):
+        super().__init__(dtype, lambda_)
+
+
+class CauchyGen(_Gen):
+    _kind = "CAUCHY"
+
+    def __init__(self, a=0.0, b=1.0, dtype=torch.float32):
+        super().__init__(dtype, a, b)
+
+
+class WeibullGen(_Gen):
+    _kind = "WEIBULL"
+
+    def __init__(self, a=1.0, b=1.0, dtype=torch.float32):
+        super().__init__(dtype, a, b)
+
+
+class ExtremeValueGen(_Gen):
+    _kind = "EXTREME_VALUE"
+
+    def __init__(self, a=0.0, b=1.0, dtype=torch.float32):
+        super().__init__(dtype, a, b)
+
+
+class GammaGen(_Gen):
+    _kind = "GAMMA"
+
+    def __init__(self, alpha=1.0, beta=1.0, dtype=torch.float32):
+        super().__init__(dtype, alpha, beta)
+
+
+class BetaGen(_Gen):
+    _kind = "BETA"
+
+    def __init__(self, a=1.0, b=1.0, dtype=torch.float32):
+        super().__init__(dtype, a, b)
+
+
+class StudentTGen(_Gen):
+    _kind = "STUDENT_T"
+
+    def __init__(self, n=1.0, dtype=torch.float32):
+        super().__init__(dtype, n)
+
+
+class ChiSquaredGen(_Gen):
+    _kind = "CHI_SQUARED"
+
+    def __init__(self, n=1.0, dtype=torch.float32):
+        super().__init__(dtype, n)
+
+
+class PoissonGen(_Gen):
+    _kind = "POISSON"
+
+    def __init__(self, mean=1.0):
+        super().__init__(torch.int32, mean)
+
+
+class BinomialGen(_Gen):
+    _kind = "BINOMIAL"
+
+    def __init__(self, trials=1, p=0.5):
+        super().__init__(torch.int32, p, trials=trials)
+
+
+class DiscreteGen(_Gen):
+    _kind = "DISCRETE"
+
+    def __init__(self, weights):
+        super().__init__(torch.int32, weights=list(weights))
+
+
+class RandbitsGen(_Gen):
+    _kind = "RANDBITS"
+
+    def __init__(self):
+        super().__init__(torch.int32)
+
+
+# ---- free functions (Dists/*.h tails) -----------------------------------
+def uniformReal(rows, cols, urng, min=None, max=None, dtype=torch.float32, out=None, stream=None):
+    if min is None and max is None:
+        return _sample("UNIFORM_REAL", rows, cols, urng, dtype, out=out, stream=stream)
+    return _sample("UNIFORM_REAL2", rows, cols, urng, dtype, 0.0 if min is None else min,
+                   1.0 if max is None else max, out=out, stream=stream)
+
+
+def balanced(rows, cols, urng, a=None, b=None, dtype=torch.float32, out=None, stream=None):
+    if a is None and b is None:
+        return _sample("BALANCED", rows, cols, urng, dtype, out=out, stream=stream)
+    return _sample("BALANCED2", rows, cols, urng, dtype, a, b, out=out, stream=stream)
+
+
+def normal(rows, cols, urng, mean=None, stdev=None, dtype=torch.float32, out=None, stream=None):
+    if mean is None and stdev is None:
+        return _sample("NORMAL_STD", rows, cols, urng, dtype, out=out, stream=stream)
+    return _sample("NORMAL", rows, cols, urng, dtype, 0.0 if mean is None else mean,
+                   1.0 if stdev is None else stdev, out=out, stream=stream)
+
+
+def lognormal(rows, cols, urng, mean=0.0, stdev=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("LOGNORMAL", rows, cols, urng, dtype, mean, stdev, out=out, stream=stream)
+
+
+def exponential(rows, cols, urng, lambda_=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("EXPONENTIAL", rows, cols, urng, dtype, lambda_, out=out, stream=stream)
+
+
+def cauchy(rows, cols, urng, a=0.0, b=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("CAUCHY", rows, cols, urng, dtype, a, b, out=out, stream=stream)
+
+
+def weibull(rows, cols, urng, a=1.0, b=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("WEIBULL", rows, cols, urng, dtype, a, b, out=out, stream=stream)
+
+
+def extremeValue(rows, cols, urng, a=0.0, b=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("EXTREME_VALUE", rows, cols, urng, dtype, a, b, out=out, stream=stream)
+
+
+def gamma(rows, cols, urng, alpha=1.0, beta=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("GAMMA", rows, cols, urng, dtype, alpha, beta, out=out, stream=stream)
+
+
+def beta(rows, cols, urng, a=1.0, b=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("BETA", rows, cols, urng, dtype, a, b, out=out, stream=stream)
+
+
+def studentT(rows, cols, urng, n=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("STUDENT_T", rows, cols, urng, dtype, n, out=out, stream=stream)
+
+
+def chiSquared(rows, cols, urng, n=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("CHI_SQUARED", rows, cols, urng, dtype, n, out=out, stream=stream)
+
+
+def poisson(rows, cols, urng, mean=1.0, out=None, stream=None):
+    return _sample("POISSON", rows, cols, urng, torch.int32, mean, out=out, stream=stream)
+
+
+def binomial(rows, cols, urng, trials=1, p=0.5, out=None, stream=None):
+    return _sample("BINOMIAL", rows, cols, urng, torch.int32, p, trials=trials, out=out, stream=stream)
+
+
+def discrete(rows, cols, urng, weights, out=None, stream=None):
+    return _sample("DISCRETE", rows, cols, urng, torch.int32, weights=list(weights), out=out, stream=stream)
+
+
+def randBits(rows, cols, urng, out=None, stream=None):
+    return _sample("RANDBITS", rows, cols, urng, torch.int32, out=out, stream=stream)

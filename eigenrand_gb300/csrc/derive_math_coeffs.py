@@ -1,0 +1,74 @@
+"""Derive the polynomial coefficients used by the library's own log/exp.
+
+The sampling kernels and the CPU oracle evaluate log/exp with the same
+operation sequence (explicit fused multiply-adds), so their results agree bit
+for bit.  The coefficients below are least-squares fits on Chebyshev nodes
+(near-minimax), computed in 60-digit arithmetic and rounded to the working
+precision.  Running this script prints the tables that are pasted into
+``gr_math.cuh`` (device) and ``oracle/ormath.c`` (oracle).
+
+Methods:
+  logf : x = 2^e * m, m in [sqrt(1/2), sqrt(2)), f = m - 1,
+         log(1+f) = f - f^2/2 + f^3 * P8(f)           (Cephes-style reduction)
+  expf : n = rint(x*log2(e)), r = x - n*ln2 (Cody-Waite split),
+         exp(r) = 1 + r + r^2 * P5(r)
+  log  : s = f/(2+f), log(1+f) = f - s*(f - T(s^2)),  T = 2*sum z^k/(2k+1)
+         (Taylor series of 2*atanh(s); coefficients are exact rationals)
+  exp  : exp(r) = sum_{k<=13} r^k/k!  (Taylor, |r| <= ln2/2)
+"""
+import mpmath as mp
+import numpy as np
+
+mp.mp.dps = 60
+
+
+def cheb_fit(func, a, b, deg, npts=400):
+    xs = [mp.mpf(a) + (mp.mpf(b) - mp.mpf(a)) * (1 - mp.cos(mp.pi * (k + 0.5) / npts)) / 2 for k in range(npts)]
+    A = mp.matrix(npts, deg + 1)
+    y = mp.matrix(npts, 1)
+    for i, x in enumerate(xs):
+        fx = func(x)
+        for j in range(deg + 1):
+            A[i, j] = x ** j
+        y[i] = fx
+    # weighted to relative error of the final result is handled by caller choice of func
+    coef = mp.lu_solve(A.T * A, A.T * y)
+    return [coef[j] for j in range(deg + 1)]
+
+
+def logf_coeffs():
+    a, b = mp.sqrt(0.5) - 1, mp.sqrt(2) - 1
+    g = lambda f: (mp.log1p(f) - f + f * f / 2) / f ** 3 if f != 0 else mp.mpf(1) / 3
+    c = cheb_fit(g, a, b, 8)
+    return [np.float32(float(v)) for v in c]
+
+
+def expf_coeffs():
+    h = mp.log(2) / 2
+    g = lambda r: (mp.exp(r) - 1 - r) / r ** 2 if r != 0 else mp.mpf(1) / 2
+    c = cheb_fit(g, -h, h, 5)
+    return [np.float32(float(v)) for v in c]
+
+
+if __name__ == "__main__":
+    print("logf P8 (ascending powers):")
+    for v in logf_coeffs():
+        print("  %.9ef" % v)
+    print("expf P5 (ascending powers):")
+    for v in expf_coeffs():
+        print("  %.9ef" % v)
+    ln2 = mp.log(2)
+    c1 = np.float32(0.693359375)        # 9 significant bits: n*c1 exact for |n| < 2^15
+    c2 = np.float32(float(ln2 - mp.mpf(float(c1))))
+    print("expf ln2 split: %.9ef %.9ef" % (c1, c2))
+    # double ln2 split with 32 trailing zero bits in the high part
+    hi = float(mp.floor(ln2 * 2 ** 32) / 2 ** 32)
+    lo = float(ln2 - hi)
+    print("double ln2 split: %.17g %.17g" % (hi, lo))
+    print("log2(e) float %.9ef double %.17g" % (np.float32(float(1 / ln2)), float(1 / ln2)))
+    print("atanh series T(z) = sum_k 2 z^k/(2k+1), k=1..12 (double):")
+    for k in range(1, 13):
+        print("  %.17g" % float(mp.mpf(2) / (2 * k + 1)))
+    print("exp Taylor 1/k!, k=2..13 (double):")
+    for k in range(2, 14):
+        print("  %.17g" % float(1 / mp.factorial(k)))

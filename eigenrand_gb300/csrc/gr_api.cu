@@ -1,0 +1,527 @@
+// C ABI of libgpurand.so (declared in include/gpurand.h).
+//
+// Host-side planning for one call: split the output over the engine's
+// sub-engines (streams), split a long single-engine call into jump-ahead
+// segments, compute the generator's constants exactly as the reference
+// constructor does, and launch the kernels.  Nothing here touches sample data.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gpurand.h"
+#include "gr_internal.h"
+#include "gr_kernels.cuh"
+#include "gr_poly.h"
+
+using namespace gr;
+
+namespace {
+
+thread_local std::string g_err;
+
+gr_status fail(gr_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+gr_status cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return GR_ERR_CUDA;
+}
+
+#define GR_CUDA(call)                                  \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// Jump polynomials x^(s*J) mod P for s = 1..count, per device, cached by J.
+struct JumpCache {
+  std::mutex mu;
+  struct Entry {
+    uint64_t* dev = nullptr;
+    int count = 0;
+  };
+  std::map<std::pair<int, int64_t>, Entry> tab;
+};
+JumpCache& jump_cache() {
+  static JumpCache c;
+  return c;
+}
+
+gr_status get_jump_polys(int dev, int64_t J, int need, const uint64_t** out) {
+  JumpCache& jc = jump_cache();
+  std::lock_guard<std::mutex> lk(jc.mu);
+  auto& ent = jc.tab[{dev, J}];
+  if (ent.count < need) {
+    const int cnt = std::max(need, 2 * ent.count);
+    std::vector<uint64_t> exps(cnt);
+    for (int s = 0; s < cnt; ++s) exps[s] = (uint64_t)(s + 1) * (uint64_t)J;
+    if (charpoly_terms().size() != 284) return fail(GR_ERR_CUDA, "MT19937-64 characteristic polynomial recovery failed");
+    std::vector<Poly> polys;
+    pow_x_mod_many(exps, polys);
+    uint64_t* d = nullptr;
+    GR_CUDA(cudaMalloc(&d, sizeof(uint64_t) * kPolyWords * (size_t)cnt));
+    GR_CUDA(cudaMemcpy(d, polys.data(), sizeof(uint64_t) * kPolyWords * (size_t)cnt, cudaMemcpyHostToDevice));
+    if (ent.dev) cudaFree(ent.dev);
+    ent.dev = d;
+    ent.count = cnt;
+  }
+  *out = ent.dev;
+  return GR_OK;
+}
+
+}  // namespace
+
+struct gr_engine {
+  int K = 1;
+  int device = 0;
+  uint64_t seed = 0;
+  EngState* st = nullptr;
+  // scratch for segmented (jump-ahead) calls
+  uint64_t* prefix = nullptr;
+  uint64_t* segwin = nullptr;
+  size_t segwin_words = 0;
+  CallSnap* snap = nullptr;
+  GenState* scratch_gen = nullptr;  // caches of temporary generators (gr_sample)
+};
+
+struct gr_gen {
+  gr_dist_desc desc{};
+  std::vector<double> weights;
+  DistParams dp{};
+  int32_t* table = nullptr;  // prob + alias (or cdf)
+  GenState* gst = nullptr;
+  int gst_K = 0;
+};
+
+extern "C" {
+
+const char* gr_last_error(void) { return g_err.c_str(); }
+const char* gr_version(void) { return "gpurand 0.1 (sm_103a; EigenRand 0.6.0 AVX2/Eigen-3.4 stream profile)"; }
+
+gr_status gr_engine_create(gr_engine** out, uint64_t seed, int32_t lanes, int32_t streams) {
+  if (!out) return fail(GR_ERR_INVALID, "out is NULL");
+  if (lanes != kLanes) return fail(GR_ERR_UNSUPPORTED, "only the 4-lane Vmt19937_64 (AVX2 profile) is implemented");
+  if (streams < 1 || streams > (1 << 20)) return fail(GR_ERR_INVALID, "streams must be in [1, 2^20]");
+  gr_engine* e = new gr_engine;
+  e->K = streams;
+  e->seed = seed;
+  cudaGetDevice(&e->device);
+  cudaError_t err = cudaMalloc(&e->st, sizeof(EngState) * (size_t)streams);
+  if (err != cudaSuccess) {
+    delete e;
+    return cuda_fail(err, "cudaMalloc(engine state)");
+  }
+  err = launch_seed(e->st, e->K, seed, nullptr);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(nullptr);
+  if (err != cudaSuccess) {
+    cudaFree(e->st);
+    delete e;
+    return cuda_fail(err, "seed kernel");
+  }
+  *out = e;
+  return GR_OK;
+}
+
+gr_status gr_engine_destroy(gr_engine* e) {
+  if (!e) return GR_OK;
+  cudaFree(e->st);
+  cudaFree(e->prefix);
+  cudaFree(e->segwin);
+  cudaFree(e->snap);
+  cudaFree(e->scratch_gen);
+  delete e;
+  return GR_OK;
+}
+
+gr_status gr_engine_seed(gr_engine* e, uint64_t seed, gr_stream_t stream) {
+  if (!e) return fail(GR_ERR_INVALID, "engine is NULL");
+  e->seed = seed;
+  GR_CUDA(launch_seed(e->st, e->K, seed, (cudaStream_t)stream));
+  return GR_OK;
+}
+
+int32_t gr_engine_streams(const gr_engine* e) { return e ? e->K : 0; }
+
+size_t gr_engine_state_size(const gr_engine* e) { return e ? sizeof(EngState) * (size_t)e->K : 0; }
+
+gr_status gr_engine_save(const gr_engine* e, void* host_buf, size_t size, gr_stream_t stream) {
+  if (!e || !host_buf) return fail(GR_ERR_INVALID, "NULL argument");
+  if (size < gr_engine_state_size(e)) return fail(GR_ERR_INVALID, "buffer too small");
+  GR_CUDA(cudaMemcpyAsync(host_buf, e->st, gr_engine_state_size(e), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  GR_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return GR_OK;
+}
+
+gr_status gr_engine_restore(gr_engine* e, const void* host_buf, size_t size, gr_stream_t stream) {
+  if (!e || !host_buf) return fail(GR_ERR_INVALID, "NULL argument");
+  if (size != gr_engine_state_size(e)) return fail(GR_ERR_INVALID, "state size does not match this engine");
+  GR_CUDA(cudaMemcpyAsync(e->st, host_buf, size, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  GR_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return GR_OK;
+}
+
+gr_status gr_engine_sync(gr_engine* e, gr_stream_t stream) {
+  if (!e) return fail(GR_ERR_INVALID, "engine is NULL");
+  GR_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  std::vector<int32_t> status(e->K);
+  GR_CUDA(cudaMemcpy2D(status.data(), sizeof(int32_t), &e->st[0].status, sizeof(EngState), sizeof(int32_t),
+                       (size_t)e->K, cudaMemcpyDeviceToHost));
+  int32_t any = 0;
+  for (int32_t s : status) any |= s;
+  if (any) {
+    GR_CUDA(cudaMemset2D(&e->st[0].status, sizeof(EngState), 0, sizeof(int32_t), (size_t)e->K));
+    if (any & GR_DEV_REJECT_LIMIT) return fail(GR_ERR_REJECT_LIMIT, "a rejection loop hit its iteration cap");
+    return fail(GR_ERR_INVALID, "device reported invalid input");
+  }
+  return GR_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Per-call constants, as the reference generators compute them.
+gr_status make_params(const gr_dist_desc& d, DistParams& p) {
+  std::memset(&p, 0, sizeof p);
+  p.kind = d.kind;
+  p.dtype = d.dtype;
+  const bool f = d.dtype == GR_F32;
+  const double a = d.a, b = d.b;
+  switch (d.kind) {
+    case kRawKind:
+    case GR_UNIFORM_REAL:
+    case GR_BALANCED:
+    case GR_NORMAL_STD:
+    case GR_RANDBITS:
+      break;
+    case GR_UNIFORM_REAL2:  // UniformRealGen(min, max): bias=min, slope=max-min (Scalar)
+    case GR_BALANCED2:      // Balanced2Gen(a, b): slope=b-a, bias=a
+      p.fa = (float)b - (float)a;
+      p.fb = (float)a;
+      p.da = b - a;
+      p.db = a;
+      break;
+    case GR_NORMAL:
+    case GR_LOGNORMAL:  // mean=a, stdev=b
+    case GR_CAUCHY:
+    case GR_EXTREME_VALUE:
+      p.fa = (float)a;
+      p.fb = (float)b;
+      p.da = a;
+      p.db = b;
+      break;
+    case GR_EXPONENTIAL:
+      p.fa = (float)a;
+      p.da = a;
+      break;
+    case GR_WEIBULL:  // pset1(1 / a) in the scalar type
+      p.fa = 1.0f / (float)a;
+      p.fb = (float)b;
+      p.da = 1.0 / a;
+      p.db = b;
+      break;
+    case GR_GAMMA:
+      p.fa = (float)a;
+      p.fb = (float)b;
+      p.da = a;
+      p.db = b;
+      p.ia = f ? ((float)a == 1.0f) : (a == 1.0);
+      break;
+    default:
+      return fail(GR_ERR_UNSUPPORTED, "distribution kind not implemented yet");
+  }
+  return GR_OK;
+}
+
+// AliasMethod::buildTable (Discrete.h:76-190) and the CDF of DiscreteGen
+// (Discrete.h:385-412), int32 precision; restated on the host.
+gr_status build_discrete(const std::vector<double>& w, std::vector<int32_t>& prob, std::vector<int32_t>& alias,
+                         int& ncdf, uint32_t& bitmask) {
+  const size_t n = w.size();
+  if (n == 0) return fail(GR_ERR_INVALID, "no weights");
+  if (n < 16) {
+    std::vector<double> cdf;
+    double acc = 0;
+    for (double x : w) cdf.push_back(acc += x);
+    prob.clear();
+    for (double x : cdf) prob.push_back((int32_t)(uint32_t)(x / cdf.back() * 0x80000000));
+    ncdf = (int)n;
+    bitmask = 0;
+    return GR_OK;
+  }
+  double sum = 0;
+  for (double x : w) sum += x;
+  if (!std::isfinite(sum)) return fail(GR_ERR_NAN_WEIGHT, "cannot build NaN value distribution");
+  const size_t nb = (size_t)std::ceil(std::log2((double)n));
+  const size_t ps = (size_t)1 << nb;
+  bitmask = (uint32_t)(((size_t)-1) >> (sizeof(size_t) * 8 - nb));
+  prob.assign(ps, 0);
+  alias.assign(ps, 0);
+  sum /= (double)ps;
+  std::vector<double> f(ps, 0.0);
+  for (size_t i = 0; i < n; ++i) f[i] = w[i] / sum;
+  size_t over = 0, under = 0, mm;
+  while (over < ps && f[over] < 1) ++over;
+  while (under < ps && f[under] >= 1) ++under;
+  mm = under + 1;
+  while (over < ps && under < ps) {
+    prob[under] = (int32_t)(f[under] * (2147483647 + 1.0));
+    alias[under] = (int32_t)over;
+    f[over] += f[under] - 1;
+    if (f[over] >= 1 || mm <= over) {
+      for (under = mm; under < ps && f[under] >= 1; ++under) {
+      }
+      mm = under + 1;
+    } else {
+      under = over;
+    }
+    while (over < ps && f[over] < 1) ++over;
+  }
+  for (; over < ps; ++over) {
+    if (f[over] >= 1) {
+      prob[over] = 2147483647;
+      alias[over] = (int32_t)over;
+    }
+  }
+  if (under < ps) {
+    prob[under] = 2147483647;
+    alias[under] = (int32_t)under;
+    for (under = mm; under < n; ++under) {
+      if (f[under] < 1) {
+        prob[under] = 2147483647;
+        alias[under] = (int32_t)under;
+      }
+    }
+  }
+  ncdf = 0;
+  return GR_OK;
+}
+
+gr_status ensure_gen_state(gr_gen* g, int K) {
+  if (g->gst && g->gst_K == K) return GR_OK;
+  cudaFree(g->gst);
+  g->gst = nullptr;
+  GR_CUDA(cudaMalloc(&g->gst, sizeof(GenState) * (size_t)K));
+  GR_CUDA(cudaMemset(g->gst, 0, sizeof(GenState) * (size_t)K));
+  g->gst_K = K;
+  return GR_OK;
+}
+
+// Choose the jump-ahead segmentation for a single-engine-per-slice call.
+void plan_segments(const gr_engine* e, int64_t packets_max, int ppu, int& S, int64_t& J) {
+  S = 1;
+  J = std::max<int64_t>(packets_max, 2);
+  if (e->K >= 16 || packets_max < (int64_t)1 << 17) return;
+  const int64_t target = std::max<int64_t>(1, 128 / e->K);
+  int64_t j = (int64_t)1 << 14;
+  while (j * target < packets_max) j <<= 1;
+  if (ppu == 2 && (j & 1)) ++j;
+  S = (int)((packets_max + j - 1) / j);
+  J = j;
+}
+
+gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream) {
+  const int gran = kind_granule(dp.kind, dp.dtype);
+  if (n % (size_t)gran) {
+    return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(gran) +
+                                    " (the reference packet width for this type)");
+  }
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  if (!kind_is_direct(dp.kind, dp.dtype, dp)) return fail(GR_ERR_UNSUPPORTED, "this parameter set is not implemented yet");
+  const int64_t granules = (int64_t)(n / (size_t)gran);
+  Plan p{};
+  p.eng = e->st;
+  p.gen = g ? g->gst : nullptr;
+  p.K = e->K;
+  p.gran = gran;
+  p.gran_per_k = granules / e->K;
+  p.gran_rem = granules % e->K;
+  p.out = out;
+  // packets per slice, upper bound (caches can only reduce it)
+  const int64_t nk_max = (p.gran_per_k + (p.gran_rem ? 1 : 0)) * gran;
+  int opp = 8;
+  if (dp.kind == kRawKind || (dp.dtype == GR_F64 && dp.kind != GR_BALANCED && dp.kind != GR_BALANCED2)) opp = 4;
+  const int ppu = kind_packets_per_unit(dp.kind, dp.dtype);
+  int64_t packets_max = (nk_max + opp - 1) / opp;
+  if (ppu == 2) packets_max += packets_max & 1;
+  int S;
+  int64_t J;
+  plan_segments(e, packets_max, ppu, S, J);
+  p.S = S;
+  p.J = J;
+  if (S > 1) {
+    if (!e->prefix) {
+      GR_CUDA(cudaMalloc(&e->prefix, sizeof(uint64_t) * (size_t)kPrefixLen * kLanes * (size_t)e->K));
+      GR_CUDA(cudaMalloc(&e->snap, sizeof(CallSnap) * (size_t)e->K));
+    }
+    const size_t need = (size_t)e->K * (S - 1) * kLanes * kN;
+    if (e->segwin_words < need) {
+      cudaFree(e->segwin);
+      e->segwin = nullptr;
+      GR_CUDA(cudaMalloc(&e->segwin, sizeof(uint64_t) * need));
+      e->segwin_words = need;
+    }
+    const uint64_t* polys = nullptr;
+    gr_status st = get_jump_polys(e->device, J, S - 1, &polys);
+    if (st != GR_OK) return st;
+    GR_CUDA(launch_prefix(e->st, p.gen, e->K, e->prefix, e->snap, stream));
+    GR_CUDA(launch_jump(e->prefix, polys, e->K, S, e->segwin, stream));
+    p.segwin = e->segwin;
+    p.prefix = e->prefix;
+  }
+  cudaError_t err = launch_direct(p, dp, e->snap, stream);
+  if (err != cudaSuccess) return cuda_fail(err, "sampling kernel");
+  return GR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gr_status gr_raw_u64(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stream) {
+  if (!e) return fail(GR_ERR_INVALID, "engine is NULL");
+  DistParams dp{};
+  dp.kind = kRawKind;
+  dp.dtype = GR_U64;
+  return run_call(e, nullptr, dp, dev_out, n, (cudaStream_t)stream);
+}
+
+gr_status gr_engine_discard(gr_engine* e, uint64_t npackets, gr_stream_t stream) {
+  if (!e) return fail(GR_ERR_INVALID, "engine is NULL");
+  if (npackets == 0) return GR_OK;
+  DistParams dp{};
+  dp.kind = kRawKind;
+  dp.dtype = GR_U64;
+  Plan p{};
+  p.eng = e->st;
+  p.K = e->K;
+  p.S = 1;
+  p.J = (int64_t)npackets;
+  p.gran = 4;
+  p.gran_per_k = (int64_t)npackets;
+  p.gran_rem = 0;
+  p.out = nullptr;  // every engine advances npackets; nothing is written
+  // slice offsets are irrelevant without output; each engine gets npackets
+  cudaError_t err = launch_direct(p, dp, nullptr, (cudaStream_t)stream);
+  if (err != cudaSuccess) return cuda_fail(err, "discard kernel");
+  return GR_OK;
+}
+
+gr_status gr_gen_create(gr_gen** out, const gr_dist_desc* desc) {
+  if (!out || !desc) return fail(GR_ERR_INVALID, "NULL argument");
+  gr_gen* g = new gr_gen;
+  g->desc = *desc;
+  gr_status st = GR_OK;
+  if (desc->kind == GR_DISCRETE) {
+    if (!desc->weights || desc->nweights <= 0) {
+      delete g;
+      return fail(GR_ERR_INVALID, "discrete needs weights");
+    }
+    g->weights.assign(desc->weights, desc->weights + desc->nweights);
+    g->desc.weights = nullptr;
+    std::vector<int32_t> prob, alias;
+    int ncdf = 0;
+    uint32_t mask = 0;
+    st = build_discrete(g->weights, prob, alias, ncdf, mask);
+    if (st == GR_OK) {
+      const size_t np = prob.size(), na = alias.size();
+      if (cudaMalloc(&g->table, sizeof(int32_t) * (np + na + 1)) != cudaSuccess) st = fail(GR_ERR_NOMEM, "table");
+      if (st == GR_OK) {
+        cudaMemcpy(g->table, prob.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice);
+        if (na) cudaMemcpy(g->table + np, alias.data(), sizeof(int32_t) * na, cudaMemcpyHostToDevice);
+      }
+      std::memset(&g->dp, 0, sizeof g->dp);
+      g->dp.kind = GR_DISCRETE;
+      g->dp.dtype = GR_I32;
+      g->dp.ncdf = ncdf;
+      g->dp.bitmask = mask;
+      g->dp.prob = g->table;
+      g->dp.alias = g->table + np;
+    }
+  } else {
+    st = make_params(g->desc, g->dp);
+  }
+  if (st != GR_OK) {
+    cudaFree(g->table);
+    delete g;
+    return st;
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_gen_destroy(gr_gen* g) {
+  if (!g) return GR_OK;
+  cudaFree(g->table);
+  cudaFree(g->gst);
+  delete g;
+  return GR_OK;
+}
+
+gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_stream_t stream) {
+  if (!g || !e) return fail(GR_ERR_INVALID, "NULL generator or engine");
+  gr_status st = ensure_gen_state(g, e->K);
+  if (st != GR_OK) return st;
+  return run_call(e, g, g->dp, dev_out, n, (cudaStream_t)stream);
+}
+
+gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream) {
+  if (!e || !desc) return fail(GR_ERR_INVALID, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  // A temporary *Gen: its caches start empty and die with the call.  They
+  // live in engine-owned scratch that is cleared in stream order, so the
+  // call stays asynchronous.
+  if (!e->scratch_gen) GR_CUDA(cudaMalloc(&e->scratch_gen, sizeof(GenState) * (size_t)e->K));
+  GR_CUDA(cudaMemsetAsync(e->scratch_gen, 0, sizeof(GenState) * (size_t)e->K, s));
+  gr_gen tmp;
+  tmp.desc = *desc;
+  gr_status st = GR_OK;
+  if (desc->kind == GR_DISCRETE) {
+    if (!desc->weights || desc->nweights <= 0) return fail(GR_ERR_INVALID, "discrete needs weights");
+    std::vector<double> w(desc->weights, desc->weights + desc->nweights);
+    std::vector<int32_t> prob, alias;
+    int ncdf = 0;
+    uint32_t mask = 0;
+    st = build_discrete(w, prob, alias, ncdf, mask);
+    if (st != GR_OK) return st;
+    const size_t np = prob.size(), na = alias.size();
+    std::vector<int32_t> both(prob);
+    both.insert(both.end(), alias.begin(), alias.end());
+    GR_CUDA(cudaMallocAsync(&tmp.table, sizeof(int32_t) * (np + na + 1), s));
+    GR_CUDA(cudaMemcpyAsync(tmp.table, both.data(), sizeof(int32_t) * (np + na), cudaMemcpyHostToDevice, s));
+    std::memset(&tmp.dp, 0, sizeof tmp.dp);
+    tmp.dp.kind = GR_DISCRETE;
+    tmp.dp.dtype = GR_I32;
+    tmp.dp.ncdf = ncdf;
+    tmp.dp.bitmask = mask;
+    tmp.dp.prob = tmp.table;
+    tmp.dp.alias = tmp.table + np;
+    tmp.gst = e->scratch_gen;
+    tmp.gst_K = e->K;
+    // pageable source: the table is staged before cudaMemcpyAsync returns
+    st = run_call(e, &tmp, tmp.dp, dev_out, n, s);
+    cudaFreeAsync(tmp.table, s);
+    tmp.table = nullptr;
+    tmp.gst = nullptr;
+    return st;
+  }
+  st = make_params(tmp.desc, tmp.dp);
+  if (st != GR_OK) return st;
+  tmp.gst = e->scratch_gen;
+  tmp.gst_K = e->K;
+  st = run_call(e, &tmp, tmp.dp, dev_out, n, s);
+  tmp.gst = nullptr;
+  return st;
+}
+
+}  // extern "C"

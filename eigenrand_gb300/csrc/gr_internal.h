@@ -1,0 +1,67 @@
+// Internal layouts shared by the host library code and the CUDA kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace gr {
+
+constexpr int kN = 312;      // MT19937-64 state words
+constexpr int kM = 156;      // MT19937-64 shift
+constexpr int kLanes = 4;    // Vmt19937_64 lanes under AVX2 (Pmt19937_64<Packet8i>)
+constexpr int kPrefix = 20280;  // 65 blocks: >= 19937 + 312 words for a jump
+
+constexpr uint64_t kMatA = 0xb5026f5aa96619e9ull;
+constexpr uint64_t kSeedF = 6364136223846793005ull;
+constexpr uint64_t kUpper = ~0ull << 31;
+constexpr uint64_t kLower = ~kUpper;
+
+// One Vmt19937_64 engine (4 MT19937-64 lanes) resident in HBM.
+//   win[l][i]  : the 312 raw (untempered) words of lane l that precede the
+//                next output; twisting them yields the next 312 outputs.
+//                After seeding these are the seed words x_0..x_311.
+//   half_*     : MersenneTwister::half() cache (the upper 128 bits of a split
+//                packet), PacketRandomEngine.h:325-336.
+struct EngState {
+  uint64_t win[kLanes][kN];
+  uint32_t half_cache[kLanes];
+  int32_t half_valid;
+  int32_t status;      // device-side error bits (GR_DEV_*), folded into the next sync
+  uint64_t consumed;   // packets drawn since seeding
+};
+static_assert(sizeof(EngState) % 16 == 0, "EngState must stay 16-byte aligned");
+
+// Caches that EigenRand keeps inside generator objects: the StdNormalGen /
+// DiscreteGen packet cache (valid + cache) and the CompressMask carry
+// (rest_cnt + rest).  Three slots: the generator itself and two nested ones
+// (BetaGen holds two GammaGens).
+struct GenSlot {
+  int32_t valid;
+  int32_t rest_cnt;
+  uint32_t cache[16];
+  uint32_t rest[16];
+};
+struct GenState {
+  GenSlot s[3];
+};
+
+// Jump-ahead prefix: the window plus 130 chunks of 156 words per lane
+// (20592 >= 19968 terms + 312 window words + register look-ahead).
+constexpr int kPrefixLen = kN + 130 * kM;
+constexpr int kRawKind = 100;  // internal kind id for the raw u64 stream
+
+// Caches as they were when a segmented call started (written by the prefix
+// kernel, read by every segment so that the last segment may update the live
+// state without racing the first).
+struct CallSnap {
+  int32_t half_valid;
+  int32_t gen_valid;
+  uint32_t half_cache[kLanes];
+  uint32_t gen_cache[16];
+};
+
+enum DevStatus : int32_t {
+  GR_DEV_REJECT_LIMIT = 1,  // a rejection loop hit its iteration cap
+  GR_DEV_BAD_INPUT = 2,
+};
+
+}  // namespace gr

@@ -1,0 +1,648 @@
+// MT19937-64 packet engine and fused engine+transform kernels for sm_103a.
+//
+// Engine: each Vmt19937_64 has 4 MT19937-64 lanes (lane l = std::mt19937_64
+// seeded seed+l), EigenRand/PacketRandomEngine.h:196-426.  One CTA owns one
+// engine (or one jump-ahead segment of it): the 4 x 312-word lane states sit
+// in shared memory, the twist runs in two phases of 156 independent words,
+// and each thread tempers the 4 lane words of one packet index and turns them
+// into output samples in registers, so raw bits never reach HBM.
+//
+// Jump-ahead: a segment starting e packets into the call gets its lane state
+// from  window(a+e) = sum_i c_i * window(a+i),  c = x^e mod P(x)  (P the
+// characteristic polynomial of MT19937-64), i.e. a GF(2) correlation of the
+// polynomial's coefficients with the lane's next 20k raw words (the "prefix").
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gr_internal.h"
+#include "gr_kernels.cuh"
+#include "gr_math.cuh"
+#include "../../include/gpurand.h"
+
+namespace gr {
+
+__device__ __forceinline__ uint64_t twist1(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t t = (a & kUpper) | (b & kLower);
+  return (t >> 1) ^ ((0ull - (t & 1ull)) & kMatA) ^ c;
+}
+
+__device__ __forceinline__ uint64_t temper(uint64_t r) {
+  r ^= (r >> 29) & 0x5555555555555555ull;
+  r ^= (r << 17) & 0x71d67fffeda60000ull;
+  r ^= (r << 37) & 0xfff7eee000000000ull;
+  r ^= r >> 43;
+  return r;
+}
+
+// ---------------------------------------------------------------- seeding
+// MersenneTwister::seed, PacketRandomEngine.h:256-265; engine k lane l is
+// seeded seed + 4k + l.
+__global__ void k_seed(EngState* st, int K, uint64_t seed) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= K * kLanes) return;
+  int k = t / kLanes, l = t % kLanes;
+  uint64_t prev = seed + (uint64_t)kLanes * (uint64_t)k + (uint64_t)l;
+  uint64_t* w = st[k].win[l];
+  w[0] = prev;
+  for (int i = 1; i < kN; ++i) {
+    prev = (prev ^ (prev >> 62)) * kSeedF + (uint64_t)i;
+    w[i] = prev;
+  }
+  if (l == 0) {
+    st[k].half_valid = 0;
+    st[k].status = 0;
+    st[k].consumed = 0;
+    for (int q = 0; q < kLanes; ++q) st[k].half_cache[q] = 0;
+  }
+}
+
+cudaError_t launch_seed(EngState* st, int K, uint64_t seed, cudaStream_t s) {
+  int n = K * kLanes;
+  k_seed<<<(n + 127) / 128, 128, 0, s>>>(st, K, seed);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- prefix
+// prefix[k][l][0..312) = current window, then the raw recurrence
+// x[i+312] = twist(x[i], x[i+1], x[i+156]) in chunks of 156 independent words.
+// Also snapshots the caches the call starts from (block lane 0).
+__global__ void __launch_bounds__(160) k_prefix(const EngState* st, uint64_t* prefix, CallSnap* snap,
+                                                const GenState* gen) {
+  __shared__ uint64_t ring[2 * kN];
+  const int k = blockIdx.x / kLanes, l = blockIdx.x % kLanes;
+  const int tid = threadIdx.x;
+  uint64_t* out = prefix + ((size_t)k * kLanes + l) * kPrefixLen;
+  for (int i = tid; i < kN; i += blockDim.x) {
+    uint64_t v = st[k].win[l][i];
+    ring[i] = v;
+    out[i] = v;
+  }
+  if (l == 0 && tid == 0) {
+    snap[k].half_valid = st[k].half_valid;
+    for (int q = 0; q < kLanes; ++q) snap[k].half_cache[q] = st[k].half_cache[q];
+    snap[k].gen_valid = gen ? gen[k].s[0].valid : 0;
+    for (int q = 0; q < 16; ++q) snap[k].gen_cache[q] = gen ? gen[k].s[0].cache[q] : 0u;
+  }
+  __syncthreads();
+  for (int base = 0; base + kN < kPrefixLen; base += kM) {
+    if (tid < kM) {
+      int i = base + tid;  // computes x[i+312]
+      uint64_t a = ring[i % (2 * kN)], b = ring[(i + 1) % (2 * kN)], c = ring[(i + kM) % (2 * kN)];
+      uint64_t v = twist1(a, b, c);
+      ring[(i + kN) % (2 * kN)] = v;
+      out[i + kN] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- jump
+// One CTA per (engine k, segment s >= 1, lane l).  16 warps; warp g covers
+// polynomial terms i in [1248 g, 1248 g + 1248), lane q of the warp covers
+// output words j in [10 q, 10 q + 10).  Per 8 terms a thread loads 8 new
+// prefix words into a sliding register window and XORs them into its 10
+// accumulators under the (warp-uniform) coefficient bits.
+constexpr int kJumpThreads = 512;
+constexpr int kJumpPer = 1248;  // terms per warp (16 * 1248 = 19968 >= 19937)
+
+__global__ void __launch_bounds__(kJumpThreads, 1)
+    k_jump(const uint64_t* prefix, const uint64_t* polys, int S, uint64_t* segwin) {
+  extern __shared__ uint64_t sm[];
+  uint64_t* px = sm;                  // kPrefixLen words
+  uint64_t* cf = sm + kPrefixLen;     // 312 coefficient words
+  const int nseg = S - 1;
+  const int l = blockIdx.x % kLanes;
+  const int s1 = (blockIdx.x / kLanes) % nseg;  // segment - 1
+  const int k = blockIdx.x / (kLanes * nseg);
+  const int tid = threadIdx.x;
+  const uint64_t* src = prefix + ((size_t)k * kLanes + l) * kPrefixLen;
+  for (int i = tid; i < kPrefixLen / 2; i += kJumpThreads)
+    reinterpret_cast<uint4*>(px)[i] = reinterpret_cast<const uint4*>(src)[i];
+  for (int i = tid; i < kN; i += kJumpThreads) cf[i] = polys[(size_t)s1 * kN + i];
+  __syncthreads();
+
+  const int g = tid >> 5, q = tid & 31;
+  const int j0 = 10 * q;
+  uint64_t acc[10];
+#pragma unroll
+  for (int jj = 0; jj < 10; ++jj) acc[jj] = 0;
+  uint64_t w[17];
+  const int ibeg = g * kJumpPer;
+#pragma unroll
+  for (int m = 0; m < 9; ++m) w[m] = px[ibeg + j0 + m];
+  for (int i0 = ibeg; i0 < ibeg + kJumpPer; i0 += 8) {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) w[9 + m] = px[i0 + j0 + 9 + m];
+    const uint32_t cb = (uint32_t)(cf[i0 >> 6] >> (i0 & 63)) & 0xffu;
+    if (cb) {
+#pragma unroll
+      for (int ii = 0; ii < 8; ++ii) {
+        if (cb & (1u << ii)) {
+#pragma unroll
+          for (int jj = 0; jj < 10; ++jj) acc[jj] ^= w[ii + jj];
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 9; ++m) w[m] = w[m + 8];
+  }
+  __syncthreads();
+  uint64_t* red = sm;  // reuse: [16][320]
+#pragma unroll
+  for (int jj = 0; jj < 10; ++jj) red[g * 320 + j0 + jj] = acc[jj];
+  __syncthreads();
+  uint64_t* dst = segwin + (((size_t)k * nseg + s1) * kLanes + l) * kN;
+  for (int j = tid; j < kN; j += kJumpThreads) {
+    uint64_t v = 0;
+#pragma unroll
+    for (int gg = 0; gg < 16; ++gg) v ^= red[gg * 320 + j];
+    dst[j] = v;
+  }
+}
+
+// ---------------------------------------------------------------- transforms
+__device__ __forceinline__ float ur_f(uint32_t x) { return u2f((x & 0x7fffffu) | (127u << 23)) - 1.0f; }
+__device__ __forceinline__ double ur_d(uint64_t x) {
+  return u2d((x & 0xfffffffffffffull) | (1023ull << 52)) - 1.0;
+}
+
+// float samples from one u32 word (one lane of a Packet8f), per kind.
+template <int KIND>
+__device__ __forceinline__ float tf32(uint32_t w, const DistParams& d) {
+  if (KIND == GR_UNIFORM_REAL) return ur_f(w);
+  if (KIND == GR_UNIFORM_REAL2) return ur_f(w) * d.fa + d.fb;
+  if (KIND == GR_BALANCED || KIND == GR_BALANCED2) {
+    float z = (float)(int32_t)(w & 0x7fffffffu) / (float)0x7FFFFFFF;
+    return KIND == GR_BALANCED ? z * 2.0f - 1.0f : z * d.fa + d.fb;
+  }
+  if (KIND == GR_EXPONENTIAL) return -(logf_(1.0f - ur_f(w)) / d.fa);
+  if (KIND == GR_GAMMA) return d.fb * (-(logf_(1.0f - ur_f(w)) / 1.0f));
+  if (KIND == GR_CAUCHY) {
+    float s, c;
+    sincosf_((float)3.1415926535897932 * (ur_f(w) - 0.5f), s, c);
+    return d.fa + d.fb * (s / c);
+  }
+  if (KIND == GR_WEIBULL) return expf_(logf_(-logf_(1.0f - ur_f(w))) * d.fa) * d.fb;
+  if (KIND == GR_EXTREME_VALUE) return d.fa - logf_(-logf_(ur_f(w) + 1.1920928955078125e-07f / 8)) * d.fb;
+  return 0.0f;
+}
+
+template <int KIND>
+__device__ __forceinline__ double tf64(uint64_t r, const DistParams& d) {
+  if (KIND == GR_UNIFORM_REAL) return ur_d(r);
+  if (KIND == GR_UNIFORM_REAL2) return ur_d(r) * d.da + d.db;
+  if (KIND == GR_EXPONENTIAL) return -(log_(1.0 - ur_d(r)) / d.da);
+  if (KIND == GR_GAMMA) return d.db * (-(log_(1.0 - ur_d(r)) / 1.0));
+  if (KIND == GR_CAUCHY) {
+    double s, c;
+    sincos_(3.1415926535897932 * (ur_d(r) - 0.5), s, c);
+    return d.da + d.db * (s / c);
+  }
+  if (KIND == GR_WEIBULL) return exp_(log_(-log_(1.0 - ur_d(r))) * d.da) * d.db;
+  if (KIND == GR_EXTREME_VALUE) return d.da - log_(-log_(ur_d(r) + 2.220446049250313e-16 / 8)) * d.db;
+  return 0.0;
+}
+
+// double balanced from one u32 word (rng.half() path)
+template <int KIND>
+__device__ __forceinline__ double tw64(uint32_t w, const DistParams& d) {
+  double z = (double)(int32_t)(w & 0x7fffffffu) / 2147483647.0;
+  return KIND == GR_BALANCED ? z * 2.0 - 1.0 : z * d.da + d.db;
+}
+
+template <int KIND>
+__device__ __forceinline__ int32_t tw32(uint32_t w, const DistParams& d) {
+  if (KIND == GR_RANDBITS) return (int32_t)w;
+  // DiscreteGen<int32_t,int32_t>, Discrete.h:455-470
+  if (d.ncdf > 0) {
+    int32_t r = d.ncdf - 1;
+    int32_t x = (int32_t)(w & 0x7fffffffu);
+    for (int i = 0; i < d.ncdf - 1; ++i) r += (x < __ldg(d.prob + i)) ? -1 : 0;
+    return r;
+  }
+  int32_t albit = (int32_t)(w & d.bitmask);
+  return ((int32_t)(w >> 1) < __ldg(d.prob + albit)) ? albit : __ldg(d.alias + albit);
+}
+
+template <int KIND>
+__device__ __forceinline__ float nscale32(float x, const DistParams& d) {
+  if (KIND == GR_NORMAL_STD) return x;
+  if (KIND == GR_NORMAL) return x * d.fb + d.fa;
+  return expf_(x * d.fb + d.fa);  // lognormal
+}
+template <int KIND>
+__device__ __forceinline__ double nscale64(double x, const DistParams& d) {
+  if (KIND == GR_NORMAL_STD) return x;
+  if (KIND == GR_NORMAL) return x * d.db + d.da;
+  return exp_(x * d.db + d.da);
+}
+
+// ---------------------------------------------------------------- direct kernel
+enum Mode { M_RAW, M_F32, M_F64, M_W32, M_W64, M_N32, M_N64 };
+
+template <int MODE>
+struct ModeInfo {
+  static constexpr int OPP = MODE == M_RAW ? 4 : MODE == M_F32 ? 8 : MODE == M_F64 ? 4 : MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : 8;
+  static constexpr bool kHalfCache = MODE == M_W64;  // randbits handled separately below
+  static constexpr int kCacheOut = MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : (MODE == M_W32 || MODE == M_W64) ? 4 : 0;
+};
+
+__device__ __forceinline__ void st16(void* p, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  *reinterpret_cast<uint4*>(p) = make_uint4(a, b, c, d);
+}
+
+template <int MODE, int KIND>
+__global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const CallSnap* snap) {
+  __shared__ uint64_t raw[2][kLanes][kN];
+  const int k = blockIdx.x / p.S, s = blockIdx.x % p.S;
+  const int tid = threadIdx.x;
+  EngState* st = p.eng + k;
+  GenState* gs = p.gen ? p.gen + k : nullptr;
+
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+
+  // --- caches the call starts from
+  constexpr bool kUsesHalf = (MODE == M_W64) || (MODE == M_W32 && KIND == GR_RANDBITS);
+  constexpr bool kUsesGen = (MODE == M_N32) || (MODE == M_N64) || (MODE == M_W32 && KIND == GR_DISCRETE);
+  int cvalid = 0;
+  const uint32_t* cwords = nullptr;
+  if (kUsesHalf) {
+    cvalid = p.S > 1 ? snap[k].half_valid : st->half_valid;
+    cwords = p.S > 1 ? snap[k].half_cache : st->half_cache;
+  } else if (kUsesGen) {
+    cvalid = p.S > 1 ? snap[k].gen_valid : gs->s[0].valid;
+    cwords = p.S > 1 ? snap[k].gen_cache : gs->s[0].cache;
+  }
+  constexpr int CO = ModeInfo<MODE>::kCacheOut;
+  const int64_t Q0 = (cvalid && CO) ? min((int64_t)CO, n) : 0;
+  const int64_t r = n - Q0;
+  constexpr int OPP = ModeInfo<MODE>::OPP;  // outputs per packet (N modes: per packet of a 2-packet unit)
+  const int64_t Np = (MODE == M_N32 || MODE == M_N64) ? 2 * ((r + 2 * OPP - 1) / (2 * OPP)) : (r + OPP - 1) / OPP;
+  const int64_t pbeg = (int64_t)s * p.J;
+  const int64_t pend = min(pbeg + p.J, Np);
+  const bool last = (pbeg < Np && Np <= pbeg + p.J) || (Np == 0 && s == 0);
+  if (pbeg >= Np && !(Np == 0 && s == 0)) return;
+
+  // --- prefix outputs served from the cache (segment 0 only)
+  if (s == 0 && tid < Q0) {
+    const int i = tid;
+    if (MODE == M_W64) reinterpret_cast<double*>(p.out)[off + i] = tw64<KIND>(cwords[i], d);
+    if (MODE == M_W32) {
+      if (KIND == GR_RANDBITS) reinterpret_cast<int32_t*>(p.out)[off + i] = (int32_t)cwords[i];
+      else reinterpret_cast<int32_t*>(p.out)[off + i] = (int32_t)cwords[i];
+    }
+    if (MODE == M_N32) reinterpret_cast<float*>(p.out)[off + i] = nscale32<KIND>(u2f(cwords[i]), d);
+    if (MODE == M_N64) {
+      uint64_t b = (uint64_t)cwords[2 * i] | ((uint64_t)cwords[2 * i + 1] << 32);
+      reinterpret_cast<double*>(p.out)[off + i] = nscale64<KIND>(u2d(b), d);
+    }
+  }
+
+  // --- lane windows.  With several segments the last one rewrites st->win,
+  // so segment 0 reads the copy the prefix kernel made at call start.
+  if (s == 0 && p.S > 1) {
+    for (int i = tid; i < kLanes * kN; i += blockDim.x)
+      (&raw[0][0][0])[i] = p.prefix[((size_t)k * kLanes + i / kN) * kPrefixLen + i % kN];
+  } else {
+    const uint64_t* w0 = (s == 0) ? &st->win[0][0] : p.segwin + ((size_t)k * (p.S - 1) + (s - 1)) * kLanes * kN;
+    for (int i = tid; i < kLanes * kN; i += blockDim.x) (&raw[0][0][0])[i] = w0[i];
+  }
+  __syncthreads();
+
+  const int64_t obase = off + Q0;
+  const int64_t oend = off + n;
+  int cur = 0;
+  int64_t base = pbeg;
+  for (; base < pend; base += kN) {
+    uint64_t(*old)[kN] = raw[cur];
+    uint64_t(*nw)[kN] = raw[cur ^ 1];
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ++ph) {
+      const int i = ph * kM + tid;
+      uint64_t pk[kLanes];
+      const bool act = tid < kM;
+      if (act) {
+#pragma unroll
+        for (int l = 0; l < kLanes; ++l) {
+          uint64_t b = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
+          uint64_t c = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
+          uint64_t v = twist1(old[l][i], b, c);
+          nw[l][i] = v;
+          pk[l] = temper(v);
+        }
+      } else {
+#pragma unroll
+        for (int l = 0; l < kLanes; ++l) pk[l] = 0;
+      }
+      const int64_t pidx = base + i;
+      const bool valid = act && pidx < pend;
+      // ---- emit
+      if (MODE == M_RAW) {
+        if (valid && p.out) {  // p.out == nullptr: discard
+          uint64_t* o = reinterpret_cast<uint64_t*>(p.out) + obase + pidx * 4;
+          reinterpret_cast<ulonglong2*>(o)[0] = make_ulonglong2(pk[0], pk[1]);
+          reinterpret_cast<ulonglong2*>(o)[1] = make_ulonglong2(pk[2], pk[3]);
+        }
+      } else if (MODE == M_F32) {
+        if (valid) {
+          float* o = reinterpret_cast<float*>(p.out) + obase + pidx * 8;
+          float v[8];
+#pragma unroll
+          for (int l = 0; l < kLanes; ++l) {
+            v[2 * l] = tf32<KIND>((uint32_t)pk[l], d);
+            v[2 * l + 1] = tf32<KIND>((uint32_t)(pk[l] >> 32), d);
+          }
+          reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
+          reinterpret_cast<float4*>(o)[1] = make_float4(v[4], v[5], v[6], v[7]);
+        }
+      } else if (MODE == M_F64) {
+        if (valid) {
+          double* o = reinterpret_cast<double*>(p.out) + obase + pidx * 4;
+          double v[4];
+#pragma unroll
+          for (int l = 0; l < kLanes; ++l) v[l] = tf64<KIND>(pk[l], d);
+          reinterpret_cast<double2*>(o)[0] = make_double2(v[0], v[1]);
+          reinterpret_cast<double2*>(o)[1] = make_double2(v[2], v[3]);
+        }
+      } else if (MODE == M_W32 || MODE == M_W64) {
+        if (valid) {
+          const int64_t ob = obase + pidx * 8;
+          uint32_t wd[8];
+#pragma unroll
+          for (int l = 0; l < kLanes; ++l) {
+            wd[2 * l] = (uint32_t)pk[l];
+            wd[2 * l + 1] = (uint32_t)(pk[l] >> 32);
+          }
+          const bool full = ob + 8 <= oend;
+          if (MODE == M_W32) {
+            int32_t v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = tw32<KIND>(wd[q], d);
+            int32_t* o = reinterpret_cast<int32_t*>(p.out) + ob;
+            st16(o, v[0], v[1], v[2], v[3]);
+            if (full) st16(o + 4, v[4], v[5], v[6], v[7]);
+            else if (gs || KIND == GR_RANDBITS) {
+              // leftover half: RandbitsGen leaves raw words in the engine's
+              // half() cache; DiscreteGen caches its computed upper 4 results
+              uint32_t* cdst = (KIND == GR_RANDBITS) ? st->half_cache : gs->s[0].cache;
+#pragma unroll
+              for (int q = 0; q < 4; ++q) cdst[q] = (KIND == GR_RANDBITS) ? wd[4 + q] : (uint32_t)v[4 + q];
+            }
+          } else {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = tw64<KIND>(wd[q], d);
+            double* o = reinterpret_cast<double*>(p.out) + ob;
+            reinterpret_cast<double2*>(o)[0] = make_double2(v[0], v[1]);
+            reinterpret_cast<double2*>(o)[1] = make_double2(v[2], v[3]);
+            if (full) {
+              reinterpret_cast<double2*>(o)[2] = make_double2(v[4], v[5]);
+              reinterpret_cast<double2*>(o)[3] = make_double2(v[6], v[7]);
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) st->half_cache[q] = wd[4 + q];
+            }
+          }
+        }
+      } else if (MODE == M_N32) {
+        // unit = packets (2j, 2j+1): u1 words in the even thread, u2 in the odd.
+        // Even thread handles lanes i = 0..3 of the unit, odd handles 4..7.
+        const bool odd = (tid & 1);
+        uint32_t wd[8];
+#pragma unroll
+        for (int l = 0; l < kLanes; ++l) {
+          wd[2 * l] = (uint32_t)pk[l];
+          wd[2 * l + 1] = (uint32_t)(pk[l] >> 32);
+        }
+        uint32_t other[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) other[q] = __shfl_xor_sync(0xffffffffu, odd ? wd[q] : wd[4 + q], 1);
+        if (valid) {
+          const int64_t unit = pidx >> 1;
+          const int i0 = odd ? 4 : 0;
+          float sv[4], cv[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float u1 = ur_f(odd ? other[q] : wd[q]);
+            const float u2 = ur_f(odd ? wd[4 + q] : other[q]);
+            const float radius = sqrtf((float)-2 * logf_(1.0f - u1));
+            const float theta = (float)(2 * 3.1415926535897932) * u2;
+            float sn, cs;
+            sincosf_(theta, sn, cs);
+            sv[q] = radius * sn;
+            cv[q] = radius * cs;
+          }
+          const int64_t ob = obase + unit * 16;
+          float* o = reinterpret_cast<float*>(p.out) + ob;
+          reinterpret_cast<float4*>(o + i0)[0] =
+              make_float4(nscale32<KIND>(sv[0], d), nscale32<KIND>(sv[1], d), nscale32<KIND>(sv[2], d),
+                          nscale32<KIND>(sv[3], d));
+          if (ob + 16 <= oend) {
+            reinterpret_cast<float4*>(o + 8 + i0)[0] =
+                make_float4(nscale32<KIND>(cv[0], d), nscale32<KIND>(cv[1], d), nscale32<KIND>(cv[2], d),
+                            nscale32<KIND>(cv[3], d));
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) gs->s[0].cache[i0 + q] = f2u(cv[q]);
+          }
+        }
+      } else if (MODE == M_N64) {
+        const bool odd = (tid & 1);
+        uint64_t other[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          uint64_t sendv = odd ? pk[q] : pk[2 + q];
+          other[q] = ((uint64_t)__shfl_xor_sync(0xffffffffu, (uint32_t)(sendv >> 32), 1) << 32) |
+                     (uint64_t)__shfl_xor_sync(0xffffffffu, (uint32_t)sendv, 1);
+        }
+        if (valid) {
+          const int64_t unit = pidx >> 1;
+          const int i0 = odd ? 2 : 0;
+          double sv[2], cv[2];
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const double u1 = ur_d(odd ? other[q] : pk[q]);
+            const double u2 = ur_d(odd ? pk[2 + q] : other[q]);
+            const double radius = sqrt(-2.0 * log_(1.0 - u1));
+            const double theta = (2 * 3.1415926535897932) * u2;
+            double sn, cs;
+            sincos_(theta, sn, cs);
+            sv[q] = radius * sn;
+            cv[q] = radius * cs;
+          }
+          const int64_t ob = obase + unit * 8;
+          double* o = reinterpret_cast<double*>(p.out) + ob;
+          reinterpret_cast<double2*>(o + i0)[0] = make_double2(nscale64<KIND>(sv[0], d), nscale64<KIND>(sv[1], d));
+          if (ob + 8 <= oend) {
+            reinterpret_cast<double2*>(o + 4 + i0)[0] =
+                make_double2(nscale64<KIND>(cv[0], d), nscale64<KIND>(cv[1], d));
+          } else {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              uint64_t b = d2u(cv[q]);
+              gs->s[0].cache[2 * (i0 + q)] = (uint32_t)b;
+              gs->s[0].cache[2 * (i0 + q) + 1] = (uint32_t)(b >> 32);
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    cur ^= 1;
+  }
+
+  // --- end-of-call state: new lane windows and cache flags
+  if (last) {
+    if (Np > 0) {
+      const int64_t nb = (pend - pbeg + kN - 1) / kN;
+      const int rr = (int)(pend - (pbeg + (nb - 1) * kN));  // packets used of the last block, 1..312
+      uint64_t(*lastb)[kN] = raw[cur];
+      uint64_t(*prevb)[kN] = raw[cur ^ 1];
+      for (int t = tid; t < kLanes * kN; t += blockDim.x) {
+        const int l = t / kN, i = t % kN;
+        st->win[l][i] = (i < kN - rr) ? prevb[l][rr + i] : lastb[l][i - (kN - rr)];
+      }
+    }
+    if (tid == 0) {
+      int64_t left = 0;  // leftover outputs cached for the next call
+      if (MODE == M_W32 || MODE == M_W64) left = (r % 8) ? 4 : 0;
+      if (MODE == M_N32) left = (r % 16) ? 8 : 0;
+      if (MODE == M_N64) left = (r % 8) ? 4 : 0;
+      if (kUsesHalf) st->half_valid = left ? 1 : (Q0 ? 0 : st->half_valid);
+      if (kUsesGen) gs->s[0].valid = left ? 1 : 0;
+      st->consumed += (uint64_t)Np;
+    }
+  }
+}
+
+template <int MODE, int KIND>
+static cudaError_t run_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s) {
+  k_direct<MODE, KIND><<<p.K * p.S, 160, 0, s>>>(p, d, snap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prefix(const EngState* st, const GenState* gen, int K, uint64_t* prefix, CallSnap* snap,
+                          cudaStream_t s) {
+  k_prefix<<<K * kLanes, 160, 0, s>>>(st, prefix, snap, gen);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, int S, uint64_t* segwin,
+                        cudaStream_t s) {
+  if (S <= 1) return cudaSuccess;
+  const size_t smem = (size_t)(kPrefixLen + kN) * sizeof(uint64_t);
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_jump, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_jump<<<K * (S - 1) * kLanes, kJumpThreads, smem, s>>>(prefix, polys, S, segwin);
+  return cudaGetLastError();
+}
+
+int kind_granule(int kind, int dtype) {
+  if (kind == kRawKind) return 4;
+  if (dtype == GR_F32) return 8;
+  return 4;  // double packets and int32 packets hold 4 lanes
+}
+
+int kind_packets_per_unit(int kind, int dtype) {
+  (void)dtype;
+  if (kind == GR_NORMAL_STD || kind == GR_NORMAL || kind == GR_LOGNORMAL) return 2;
+  return 1;
+}
+
+bool kind_is_direct(int kind, int dtype, const DistParams& d) {
+  switch (kind) {
+    case kRawKind:
+    case GR_UNIFORM_REAL:
+    case GR_UNIFORM_REAL2:
+    case GR_BALANCED:
+    case GR_BALANCED2:
+    case GR_NORMAL_STD:
+    case GR_NORMAL:
+    case GR_LOGNORMAL:
+    case GR_EXPONENTIAL:
+    case GR_CAUCHY:
+    case GR_WEIBULL:
+    case GR_EXTREME_VALUE:
+      return true;
+    case GR_GAMMA:
+      return d.ia == 1;  // alpha == 1: beta * exponential
+    case GR_RANDBITS:
+    case GR_DISCRETE:
+      return dtype == GR_I32;
+    default:
+      return false;
+  }
+}
+
+#define GR_F32_CASE(K) \
+  case K:              \
+    return run_direct<M_F32, K>(p, d, snap, s);
+#define GR_F64_CASE(K) \
+  case K:              \
+    return run_direct<M_F64, K>(p, d, snap, s);
+
+cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s) {
+  if (d.kind == kRawKind) return run_direct<M_RAW, kRawKind>(p, d, snap, s);
+  if (d.dtype == GR_F32) {
+    switch (d.kind) {
+      GR_F32_CASE(GR_UNIFORM_REAL)
+      GR_F32_CASE(GR_UNIFORM_REAL2)
+      GR_F32_CASE(GR_BALANCED)
+      GR_F32_CASE(GR_BALANCED2)
+      GR_F32_CASE(GR_EXPONENTIAL)
+      GR_F32_CASE(GR_CAUCHY)
+      GR_F32_CASE(GR_WEIBULL)
+      GR_F32_CASE(GR_EXTREME_VALUE)
+      GR_F32_CASE(GR_GAMMA)
+      case GR_NORMAL_STD:
+        return run_direct<M_N32, GR_NORMAL_STD>(p, d, snap, s);
+      case GR_NORMAL:
+        return run_direct<M_N32, GR_NORMAL>(p, d, snap, s);
+      case GR_LOGNORMAL:
+        return run_direct<M_N32, GR_LOGNORMAL>(p, d, snap, s);
+      default:
+        return cudaErrorNotSupported;
+    }
+  }
+  if (d.dtype == GR_F64) {
+    switch (d.kind) {
+      GR_F64_CASE(GR_UNIFORM_REAL)
+      GR_F64_CASE(GR_UNIFORM_REAL2)
+      GR_F64_CASE(GR_EXPONENTIAL)
+      GR_F64_CASE(GR_CAUCHY)
+      GR_F64_CASE(GR_WEIBULL)
+      GR_F64_CASE(GR_EXTREME_VALUE)
+      GR_F64_CASE(GR_GAMMA)
+      case GR_BALANCED:
+        return run_direct<M_W64, GR_BALANCED>(p, d, snap, s);
+      case GR_BALANCED2:
+        return run_direct<M_W64, GR_BALANCED2>(p, d, snap, s);
+      case GR_NORMAL_STD:
+        return run_direct<M_N64, GR_NORMAL_STD>(p, d, snap, s);
+      case GR_NORMAL:
+        return run_direct<M_N64, GR_NORMAL>(p, d, snap, s);
+      case GR_LOGNORMAL:
+        return run_direct<M_N64, GR_LOGNORMAL>(p, d, snap, s);
+      default:
+        return cudaErrorNotSupported;
+    }
+  }
+  if (d.dtype == GR_I32) {
+    if (d.kind == GR_RANDBITS) return run_direct<M_W32, GR_RANDBITS>(p, d, snap, s);
+    if (d.kind == GR_DISCRETE) return run_direct<M_W32, GR_DISCRETE>(p, d, snap, s);
+  }
+  return cudaErrorNotSupported;
+}
+
+}  // namespace gr

@@ -1,0 +1,56 @@
+// Launch interface between the host library (gr_api.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gr_internal.h"
+
+namespace gr {
+
+// Per-call distribution constants, computed on the host exactly as the
+// reference generator's constructor computes them.
+struct DistParams {
+  int32_t kind;   // gr_dist_kind
+  int32_t dtype;  // gr_dtype
+  float fa, fb, fc, fd, fe, ff, fg, fh;   // float-precision constants
+  double da, db, dc, dd, de, df, dg, dh;  // double-precision constants
+  int32_t ia, ib;                          // integer constants (trials, counts)
+  uint32_t bitmask;                        // alias table mask
+  int32_t ncdf;                            // CDF entries (discrete < 16 weights)
+  const int32_t* prob;                     // alias table / cdf (device)
+  const int32_t* alias;
+};
+
+// How one call is split over sub-engines and segments.
+struct Plan {
+  EngState* eng;          // K engines
+  GenState* gen;          // K generator states (may be null)
+  const uint64_t* segwin; // jump results: [(k*(S-1) + s-1)][4][312]
+  const uint64_t* prefix; // prefix buffer [k][4][kPrefixLen] (segmented calls)
+  int32_t K;              // sub-engines
+  int32_t S;              // segments per sub-engine
+  int64_t J;              // packets (or units for 2-packet kinds) per segment
+  int64_t gran_per_k;     // output granules per sub-engine ...
+  int64_t gran_rem;       // ... plus one for the first gran_rem engines
+  int32_t gran;           // outputs per granule
+  void* out;
+};
+
+// kernels (gr_kernels.cu)
+cudaError_t launch_seed(EngState* st, int K, uint64_t seed, cudaStream_t s);
+cudaError_t launch_prefix(const EngState* st, const GenState* gen, int K, uint64_t* prefix, CallSnap* snap,
+                          cudaStream_t s);
+cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, int S, uint64_t* segwin,
+                        cudaStream_t s);
+// Fused engine + transform for kinds whose draws per output are fixed and
+// packet aligned.  Returns cudaErrorNotSupported for other kinds.
+cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s);
+
+// Outputs per granule: the smallest output count a call (or a stream slice)
+// may have for the kind.  Packets per unit: 2 for the Box-Muller kinds.
+int kind_granule(int kind, int dtype);
+int kind_packets_per_unit(int kind, int dtype);
+bool kind_is_direct(int kind, int dtype, const DistParams& d);
+
+}  // namespace gr

@@ -1,0 +1,130 @@
+/*
+ * gpurand.h — C ABI of the GB300 sampling library (libgpurand.so).
+ *
+ * The drop-in boundary for EigenRand's sampling path (bab2min/EigenRand
+ * v0.6.0).  Every entry point takes plain pointers and sizes; device buffers
+ * are owned by the caller, engine and generator state lives in HBM and is
+ * owned by the library.  Calls are asynchronous on the given CUDA stream and
+ * never block, throw or abort; errors come back as gr_status, device-side
+ * error words are folded into the next gr_engine_sync().
+ *
+ * Engines and generators are externally synchronised: use one stream per
+ * engine, as EigenRand requires one engine per thread.
+ *
+ * Stream semantics (bit-exact with the reference, AVX2 + Eigen 3.4 profile):
+ *   - lane l of a Vmt19937_64 seeded s is std::mt19937_64(s + l), l < 4;
+ *   - raw u64 stream R[4k + l] = lane_l[k]  (packet k = 4 lanes);
+ *   - u32 word stream W[2i] = low32(R[i]), W[2i+1] = high32(R[i]);
+ *   - float outputs use one packet (8 words) per 8 samples, double outputs
+ *     one packet per 4 samples, int32 outputs half packets (4 words) per 4
+ *     samples, exactly as the reference's packetOp code consumes them.
+ * An engine created with streams = K > 1 holds K independent
+ * Vmt19937_64(seed + 4k) engines; a call then splits its output into K
+ * contiguous slices, slice k generated by engine k — identical to K host
+ * threads each running EigenRand on its own engine and slice.
+ */
+#ifndef GPURAND_H
+#define GPURAND_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gr_stream_t; /* == cudaStream_t; NULL = default stream */
+
+typedef enum {
+  GR_OK = 0,
+  GR_ERR_INVALID = 1,      /* bad argument (size not a multiple of the packet width, NULL, ...) */
+  GR_ERR_CUDA = 2,         /* a CUDA runtime call failed; see gr_last_error() */
+  GR_ERR_UNSUPPORTED = 3,  /* parameter combination not implemented */
+  GR_ERR_NOMEM = 4,        /* device allocation failed */
+  GR_ERR_REJECT_LIMIT = 5, /* a rejection loop hit its iteration cap (device word) */
+  GR_ERR_NOT_PD = 6,       /* covariance / scale matrix not positive definite */
+  GR_ERR_NAN_WEIGHT = 7    /* non-finite weight sum (AliasMethod, Discrete.h:88) */
+} gr_status;
+
+typedef enum { GR_F32 = 0, GR_F64 = 1, GR_I32 = 2, GR_U64 = 3 } gr_dtype;
+
+/* Distribution kinds.  Parameter meaning follows the reference generator's
+ * constructor (a, b in the order of the C++ arguments). */
+typedef enum {
+  GR_UNIFORM_REAL = 1,  /* StdUniformRealGen (a,b unused); Basic.h:525-591       */
+  GR_UNIFORM_REAL2 = 2, /* UniformRealGen(min=a, max=b); Basic.h:598-646          */
+  GR_BALANCED = 3,      /* BalancedGen; Basic.h:407-429                           */
+  GR_BALANCED2 = 4,     /* Balanced2Gen(a, b); Basic.h:436-467                    */
+  GR_NORMAL_STD = 5,    /* StdNormalGen; NormalExp.h:25-83                        */
+  GR_NORMAL = 6,        /* NormalGen(mean=a, stdev=b); NormalExp.h:92-136          */
+  GR_LOGNORMAL = 7,     /* LognormalGen(mean=a, stdev=b); NormalExp.h:170-210      */
+  GR_EXPONENTIAL = 8,   /* ExponentialGen(lambda=a); NormalExp.h:356-399           */
+  GR_CAUCHY = 9,        /* CauchyGen(a, b); NormalExp.h:809-856                   */
+  GR_WEIBULL = 10,      /* WeibullGen(a, b); NormalExp.h:613-656                  */
+  GR_EXTREME_VALUE = 11,/* ExtremeValueGen(a, b); NormalExp.h:689-733             */
+  GR_GAMMA = 12,        /* GammaGen(alpha=a, beta=b); NormalExp.h:434-606          */
+  GR_BETA = 13,         /* BetaGen(a, b); NormalExp.h:895-977                     */
+  GR_STUDENT_T = 14,    /* StudentTGen(n=a); NormalExp.h:241-300                  */
+  GR_CHI_SQUARED = 15,  /* ChiSquaredGen(n=a); NormalExp.h:767-802                */
+  GR_POISSON = 16,      /* PoissonGen(mean=a); Discrete.h:788-904                 */
+  GR_BINOMIAL = 17,     /* BinomialGen(trials, p=a); Discrete.h:911-1053          */
+  GR_DISCRETE = 18,     /* DiscreteGen<int32_t,int32_t>(weights); Discrete.h:352-486 */
+  GR_RANDBITS = 19      /* RandbitsGen<int32_t>; Basic.h:378-400                  */
+} gr_dist_kind;
+
+typedef struct {
+  int32_t kind;           /* gr_dist_kind */
+  int32_t dtype;          /* GR_F32 / GR_F64 for real kinds, GR_I32 for integer kinds */
+  double a, b;            /* scalar parameters */
+  int32_t trials;         /* binomial */
+  int32_t nweights;       /* discrete */
+  const double* weights;  /* discrete, host pointer, copied at gr_gen_create */
+} gr_dist_desc;
+
+typedef struct gr_engine gr_engine;
+typedef struct gr_gen gr_gen;
+
+/* ---- engines ------------------------------------------------------------
+ * Replaces Eigen::Rand::Vmt19937_64 (PacketRandomEngine.h:585-599, the
+ * MersenneTwister class :196-415).  lanes must be 4 (the AVX2 packet engine).
+ * streams = 1 gives one Vmt19937_64(seed); streams = K > 1 gives K engines
+ * seeded seed + 4k (the reference's one-engine-per-thread usage). */
+gr_status gr_engine_create(gr_engine** out, uint64_t seed, int32_t lanes, int32_t streams);
+gr_status gr_engine_destroy(gr_engine* e);
+/* MersenneTwister(x0) / seed(x0), PacketRandomEngine.h:230-265 */
+gr_status gr_engine_seed(gr_engine* e, uint64_t seed, gr_stream_t stream);
+/* Copy of the engine (AlignedArray deep copy, PacketRandomEngine.h:89-118).
+ * Host buffer layout: see gr_engine_state_size(). */
+size_t gr_engine_state_size(const gr_engine* e);
+gr_status gr_engine_save(const gr_engine* e, void* host_buf, size_t size, gr_stream_t stream);
+gr_status gr_engine_restore(gr_engine* e, const void* host_buf, size_t size, gr_stream_t stream);
+/* MersenneTwister::discard(num) (:317-323) — num packets, O(num). */
+gr_status gr_engine_discard(gr_engine* e, uint64_t npackets, gr_stream_t stream);
+/* Waits for the engine's stream work and folds device error words. */
+gr_status gr_engine_sync(gr_engine* e, gr_stream_t stream);
+int32_t gr_engine_streams(const gr_engine* e);
+
+/* Raw stream: makeUniversalRng<uint64_t>(Vmt19937_64) operator()
+ * (PacketRandomEngine.h:468-475, 577-583).  n must be a multiple of 4 per
+ * stream slice. */
+gr_status gr_raw_u64(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stream);
+
+/* ---- generators ---------------------------------------------------------
+ * A generator object mirrors one *Gen instance, including the caches it
+ * carries between calls (StdNormalGen::valid, GammaGen::cache_rest_cnt, ...).
+ * Weights / parameters are copied at creation. */
+gr_status gr_gen_create(gr_gen** out, const gr_dist_desc* desc);
+gr_status gr_gen_destroy(gr_gen* g);
+/* *Gen::generate(rows, cols, urng) with n = rows * cols, column-major. */
+gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_stream_t stream);
+/* Free-function form (Eigen::Rand::normal(rows, cols, urng, ...)): a fresh
+ * generator for one call. */
+gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream);
+
+const char* gr_last_error(void);
+const char* gr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

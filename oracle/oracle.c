@@ -1,0 +1,886 @@
+/*
+ * CPU ORACLE — engine and generators.  Test infrastructure only; see oracle.h.
+ *
+ * Restates, lane by lane, what EigenRand's packet code computes under the
+ * AVX2 + Eigen 3.4 profile.  File:line citations are into bab2min/EigenRand.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "oracle.h"
+
+static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static inline uint64_t d2u(double f) { uint64_t u; memcpy(&u, &f, 8); return u; }
+static inline double u2d(uint64_t u) { double f; memcpy(&f, &u, 8); return f; }
+
+#define PI_D 3.1415926535897932 /* Dists/Basic.h:23 */
+#define E_D 2.7182818284590452  /* Dists/Basic.h:24 */
+
+/* ======================================================================
+ * MT19937-64 lane: PacketRandomEngine.h:256-265 (seed), :295-310 (temper),
+ * :340-404 (refill_lower / refill_upper), constants :421-426.
+ * ====================================================================== */
+#define MT_N 312
+#define MT_M 156
+#define MT_A 0xb5026f5aa96619e9ull
+#define MT_F 6364136223846793005ull
+#define MT_HMASK (~0ull << 31)
+#define MT_LMASK (~MT_HMASK)
+
+static inline uint64_t mt_twist1(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t tmp = (a & MT_HMASK) | (b & MT_LMASK);
+  return (tmp >> 1) ^ ((tmp & 1) ? MT_A : 0) ^ c;
+}
+
+void or_mt64_seed(or_mt64* s, uint64_t seed) {
+  uint64_t prev = s->state[0] = seed;
+  for (int i = 1; i < MT_N; ++i) {
+    prev = s->state[i] = (prev ^ (prev >> 62)) * MT_F + (uint64_t)i;
+  }
+  for (int i = MT_N; i < 2 * MT_N; ++i) s->state[i] = 0;
+  s->idx = MT_N;
+}
+
+static void mt_refill_upper(or_mt64* s) {
+  for (int i = MT_N; i < 2 * MT_N; ++i)
+    s->state[i] = mt_twist1(s->state[i - MT_N], s->state[i - MT_N + 1], s->state[i - MT_N + MT_M]);
+}
+
+static void mt_refill_lower(or_mt64* s) {
+  int i;
+  for (i = 0; i < MT_N - MT_M; ++i)
+    s->state[i] = mt_twist1(s->state[i + MT_N], s->state[i + MT_N + 1], s->state[i + MT_N + MT_M]);
+  for (; i < MT_N - 1; ++i)
+    s->state[i] = mt_twist1(s->state[i + MT_N], s->state[i + MT_N + 1], s->state[i - MT_N + MT_M]);
+  s->state[i] = mt_twist1(s->state[i + MT_N], s->state[0], s->state[MT_M - 1]);
+  s->idx = 0;
+}
+
+uint64_t or_mt64_next(or_mt64* s) {
+  if (s->idx == MT_N)
+    mt_refill_upper(s);
+  else if (2 * MT_N <= s->idx)
+    mt_refill_lower(s);
+  uint64_t r = s->state[s->idx++];
+  r ^= (r >> 29) & 0x5555555555555555ull;
+  r ^= (r << 17) & 0x71d67fffeda60000ull;
+  r ^= (r << 37) & 0xfff7eee000000000ull;
+  r ^= r >> 43;
+  return r;
+}
+
+/* last 312 raw words produced (or the seed words before the first twist) */
+static void mt_window(const or_mt64* s, uint64_t* out) {
+  /* the 312 words preceding state[idx] in the cyclic double buffer */
+  for (int i = 0; i < MT_N; ++i) {
+    int j = s->idx - MT_N + i;
+    if (j < 0) j += 2 * MT_N;
+    out[i] = s->state[j];
+  }
+}
+
+/* ======================================================================
+ * Packet engine.  Lane l = MT19937-64 seeded seed+l (:230-239).
+ * ====================================================================== */
+or_vmt* or_vmt_new(uint64_t seed, int lanes) {
+  if (lanes < 1 || lanes > OR_MAXL) return NULL;
+  or_vmt* e = (or_vmt*)calloc(1, sizeof(or_vmt));
+  e->L = lanes;
+  for (int l = 0; l < lanes; ++l) or_mt64_seed(&e->lane[l], seed + (uint64_t)l);
+  return e;
+}
+void or_vmt_free(or_vmt* e) { free(e); }
+void or_vmt_copy(or_vmt* dst, const or_vmt* src) { memcpy(dst, src, sizeof(or_vmt)); }
+size_t or_vmt_sizeof(void) { return sizeof(or_vmt); }
+size_t or_gen_sizeof(void) { return sizeof(or_gen); }
+
+static void vmt_packet(or_vmt* e, uint64_t* r) {
+  for (int l = 0; l < e->L; ++l) r[l] = or_mt64_next(&e->lane[l]);
+}
+
+void or_vmt_raw(or_vmt* e, uint64_t* out, size_t npackets) {
+  for (size_t k = 0; k < npackets; ++k) vmt_packet(e, out + k * (size_t)e->L);
+}
+
+void or_vmt_discard(or_vmt* e, uint64_t npackets) {
+  uint64_t r[OR_MAXL];
+  for (uint64_t k = 0; k < npackets; ++k) vmt_packet(e, r);
+}
+
+void or_vmt_window(const or_vmt* e, uint64_t* out) {
+  for (int l = 0; l < e->L; ++l) mt_window(&e->lane[l], out + (size_t)l * MT_N);
+}
+
+/* one engine packet viewed as 2L u32 words (Packet8i for L=4) */
+static void draw_full(or_vmt* e, uint32_t* w) {
+  uint64_t r[OR_MAXL];
+  vmt_packet(e, r);
+  for (int l = 0; l < e->L; ++l) {
+    w[2 * l] = (uint32_t)r[l];
+    w[2 * l + 1] = (uint32_t)(r[l] >> 32);
+  }
+}
+
+/* MersenneTwister::half(), PacketRandomEngine.h:325-336: split_two gives the
+ * low 128 bits now and caches the high 128 bits. */
+static void draw_half(or_vmt* e, uint32_t* w) {
+  int hw = e->L; /* words in a half packet */
+  if (e->half_valid) {
+    e->half_valid = 0;
+    memcpy(w, e->half_cache, sizeof(uint32_t) * (size_t)hw);
+    return;
+  }
+  uint32_t full[2 * OR_MAXL];
+  draw_full(e, full);
+  memcpy(w, full, sizeof(uint32_t) * (size_t)hw);
+  memcpy(e->half_cache, full + hw, sizeof(uint32_t) * (size_t)hw);
+  e->half_valid = 1;
+}
+
+/* ======================================================================
+ * Uniform building blocks (AVX2 profile)
+ *   float  packet (P=8): rawbits_34 = rng()        arch/AVX/RandUtils.h:154-157
+ *   float  packet (P=4): rawbits_34 = rng.half()   arch/AVX/RandUtils.h:28-31
+ *   double packet (P=4): rawbits    = rng()        arch/AVX/RandUtils.h:149-152
+ *   bit_to_ur_float/double                         MorePacketMath.h:205-227
+ * ====================================================================== */
+static inline float bit_ur_f(uint32_t x) { return u2f((x & 0x7fffffu) | (127u << 23)) - 1.0f; }
+static inline double bit_ur_d(uint64_t x) {
+  return u2d((x & 0xfffffffffffffull) | (1023ull << 52)) - 1.0;
+}
+
+static void ur_f8(or_vmt* e, float* u) {
+  uint32_t w[8];
+  draw_full(e, w);
+  for (int j = 0; j < 8; ++j) u[j] = bit_ur_f(w[j]);
+}
+static void ur_f4(or_vmt* e, float* u) {
+  uint32_t w[4];
+  draw_half(e, w);
+  for (int j = 0; j < 4; ++j) u[j] = bit_ur_f(w[j]);
+}
+static void ur_d4(or_vmt* e, double* u) {
+  uint64_t r[4];
+  vmt_packet(e, r);
+  for (int j = 0; j < 4; ++j) u[j] = bit_ur_d(r[j]);
+}
+
+/* "packet of uniforms" for the generic real generators:
+ * width P (8 float / 4 double), stored as double for convenience but the
+ * float path keeps every operation in float below. */
+typedef struct {
+  int dbl;
+  float f[8];
+  double d[4];
+} upk;
+
+static int P_of(int dbl) { return dbl ? 4 : 8; }
+
+static void ur_pk(or_vmt* e, int dbl, upk* p) {
+  p->dbl = dbl;
+  if (dbl) ur_d4(e, p->d); else ur_f8(e, p->f);
+}
+
+/* nonzero_uniform_real = ur + epsilon/8, RandUtils.h:46-51 */
+static void nzur_pk(or_vmt* e, int dbl, upk* p) {
+  ur_pk(e, dbl, p);
+  if (dbl) for (int j = 0; j < 4; ++j) p->d[j] = p->d[j] + 2.220446049250313e-16 / 8;
+  else for (int j = 0; j < 8; ++j) p->f[j] = p->f[j] + 1.1920928955078125e-07f / 8;
+}
+
+/* zero_to_one (balanced): float: rng() words, cvtepi32_ps / 2^31 (the float
+ * constant 0x7FFFFFFF rounds to 2^31).  double: rng.half() words,
+ * cvtepi32_pd / 2147483647.  arch/AVX/RandUtils.h:200-204, 215-219 */
+static void z2o_pk(or_vmt* e, int dbl, upk* p) {
+  p->dbl = dbl;
+  if (dbl) {
+    uint32_t w[4];
+    draw_half(e, w);
+    for (int j = 0; j < 4; ++j) p->d[j] = (double)(int32_t)(w[j] & 0x7fffffffu) / 2147483647.0;
+  } else {
+    uint32_t w[8];
+    draw_full(e, w);
+    for (int j = 0; j < 8; ++j) p->f[j] = (float)(int32_t)(w[j] & 0x7fffffffu) / (float)0x7FFFFFFF;
+  }
+}
+
+/* ======================================================================
+ * CompressMask::compress_append, arch/AVX/PacketFilter.h:147-184, generic P.
+ * Fully accepted packets pass straight through; otherwise accepted lanes are
+ * appended, in order, to the carried lanes and a packet is emitted once P
+ * lanes are available.  `vals` are raw 32- or 64-bit lane bit patterns.
+ * ====================================================================== */
+static int compress_append(int P, int wide, void* value, const int* mask, void* rest, int rest_cnt,
+                           int* full) {
+  int m = 0;
+  for (int j = 0; j < P; ++j) m += mask[j] ? 1 : 0;
+  if (m == P) {
+    *full = 1;
+    return rest_cnt;
+  }
+  uint64_t acc[32];
+  int n = 0;
+  for (int j = 0; j < rest_cnt; ++j) acc[n++] = wide ? ((uint64_t*)rest)[j] : ((uint32_t*)rest)[j];
+  for (int j = 0; j < P; ++j)
+    if (mask[j]) acc[n++] = wide ? ((uint64_t*)value)[j] : ((uint32_t*)value)[j];
+  if (n >= P) {
+    for (int j = 0; j < P; ++j) {
+      if (wide) ((uint64_t*)value)[j] = acc[j]; else ((uint32_t*)value)[j] = (uint32_t)acc[j];
+    }
+    for (int j = P; j < n; ++j) {
+      if (wide) ((uint64_t*)rest)[j - P] = acc[j]; else ((uint32_t*)rest)[j - P] = (uint32_t)acc[j];
+    }
+    *full = 1;
+    return n - P;
+  }
+  for (int j = 0; j < n; ++j) {
+    if (wide) ((uint64_t*)rest)[j] = acc[j]; else ((uint32_t*)rest)[j] = (uint32_t)acc[j];
+  }
+  *full = 0;
+  return n;
+}
+
+/* ======================================================================
+ * Real-valued generators: one packet per call, as *Gen::packetOp does.
+ * ====================================================================== */
+
+/* StdNormalGen::packetOp, NormalExp.h:60-82 */
+static void stdnormal_pk(or_vmt* e, or_gen* g, int dbl, upk* out) {
+  int P = P_of(dbl);
+  out->dbl = dbl;
+  if (g->valid) {
+    g->valid = 0;
+    memcpy(dbl ? (void*)out->d : (void*)out->f, g->cache, (size_t)P * (dbl ? 8 : 4));
+    return;
+  }
+  g->valid = 1;
+  upk u1, u2;
+  ur_pk(e, dbl, &u1);
+  ur_pk(e, dbl, &u2);
+  if (dbl) {
+    double c[4];
+    for (int j = 0; j < 4; ++j) {
+      double a = 1.0 - u1.d[j];
+      double radius = sqrt(-2.0 * or_log(a));
+      double theta = (2 * PI_D) * u2.d[j];
+      double s, cc;
+      or_sincos(theta, &s, &cc);
+      c[j] = radius * cc;
+      out->d[j] = radius * s;
+    }
+    memcpy(g->cache, c, sizeof c);
+  } else {
+    float c[8];
+    for (int j = 0; j < 8; ++j) {
+      float a = 1.0f - u1.f[j];
+      float radius = sqrtf((float)-2 * or_logf(a));
+      float theta = (float)(2 * PI_D) * u2.f[j];
+      float s, cc;
+      or_sincosf(theta, &s, &cc);
+      c[j] = radius * cc;
+      out->f[j] = radius * s;
+    }
+    memcpy(g->cache, c, sizeof c);
+  }
+}
+
+/* GammaGen::packetOp, NormalExp.h:527-605 */
+static void gamma_pk(or_vmt* e, or_gen* g, int dbl, double alpha_in, double beta_in, upk* out) {
+  int P = P_of(dbl);
+  out->dbl = dbl;
+  if (dbl) {
+    double alpha = alpha_in, beta = beta_in;
+    double px = (double)(E_D / (alpha + E_D));
+    double sq = sqrt(2 * alpha - 1);
+    if (alpha < 1) {
+      for (;;) {
+        upk ux, vx;
+        ur_pk(e, 1, &ux);
+        nzur_pk(e, 1, &vx);
+        double cands[4];
+        int mask[4];
+        upk ux2;
+        double xx[4], qx[4];
+        for (int j = 0; j < 4; ++j) {
+          double lv = or_log(vx.d[j]);
+          double x1 = or_exp((1 / alpha) * lv);
+          double q1 = or_exp(-x1);
+          double x2 = 1.0 - lv;
+          double q2 = or_exp(or_log(x2) * (alpha - 1));
+          int c = ux.d[j] < px;
+          xx[j] = c ? x1 : x2;
+          qx[j] = c ? q1 : q2;
+        }
+        ur_pk(e, 1, &ux2);
+        for (int j = 0; j < 4; ++j) {
+          cands[j] = beta * xx[j];
+          mask[j] = ux2.d[j] < qx[j];
+        }
+        int full = 0;
+        g->rest_cnt = compress_append(4, 1, cands, mask, g->rest, g->rest_cnt, &full);
+        if (full) {
+          memcpy(out->d, cands, sizeof cands);
+          return;
+        }
+      }
+    }
+    if (alpha == 1) {
+      upk u;
+      ur_pk(e, 1, &u);
+      for (int j = 0; j < 4; ++j) out->d[j] = beta * (-(or_log(1.0 - u.d[j]) / 1.0));
+      return;
+    }
+    int count = (int)alpha;
+    if ((double)count == alpha && count < 20) {
+      upk y, t;
+      nzur_pk(e, 1, &y);
+      while (--count) {
+        nzur_pk(e, 1, &t);
+        for (int j = 0; j < 4; ++j) y.d[j] = y.d[j] * t.d[j];
+      }
+      for (int j = 0; j < 4; ++j) out->d[j] = -(beta * or_log(y.d[j]));
+      return;
+    }
+    for (;;) {
+      double alpha_1 = alpha - 1;
+      upk u, ux;
+      ur_pk(e, 1, &u);
+      double yx[4], xx[4];
+      int c[4];
+      for (int j = 0; j < 4; ++j) {
+        double s, cc;
+        or_sincos(PI_D * u.d[j], &s, &cc);
+        yx[j] = s / cc;
+        xx[j] = sq * yx[j] + alpha_1;
+        c[j] = 0 < xx[j];
+      }
+      ur_pk(e, 1, &ux);
+      double cands[4];
+      int mask[4];
+      for (int j = 0; j < 4; ++j) {
+        double ub = (yx[j] * yx[j] + 1) * or_exp(alpha_1 * or_log(xx[j] / alpha_1) - yx[j] * sq);
+        mask[j] = c[j] && (ux.d[j] <= ub);
+        cands[j] = beta * xx[j];
+      }
+      int full = 0;
+      g->rest_cnt = compress_append(4, 1, cands, mask, g->rest, g->rest_cnt, &full);
+      if (full) {
+        memcpy(out->d, cands, sizeof cands);
+        return;
+      }
+    }
+  } else {
+    float alpha = (float)alpha_in, beta = (float)beta_in;
+    float px = (float)(E_D / (alpha + E_D));
+    float sq = sqrtf(2 * alpha - 1);
+    (void)P;
+    if (alpha < 1) {
+      for (;;) {
+        upk ux, vx, ux2;
+        ur_pk(e, 0, &ux);
+        nzur_pk(e, 0, &vx);
+        float xx[8], qx[8];
+        for (int j = 0; j < 8; ++j) {
+          float lv = or_logf(vx.f[j]);
+          float x1 = or_expf((1 / alpha) * lv);
+          float q1 = or_expf(-x1);
+          float x2 = 1.0f - lv;
+          float q2 = or_expf(or_logf(x2) * (alpha - 1));
+          int c = ux.f[j] < px;
+          xx[j] = c ? x1 : x2;
+          qx[j] = c ? q1 : q2;
+        }
+        ur_pk(e, 0, &ux2);
+        float cands[8];
+        int mask[8];
+        for (int j = 0; j < 8; ++j) {
+          cands[j] = beta * xx[j];
+          mask[j] = ux2.f[j] < qx[j];
+        }
+        int full = 0;
+        g->rest_cnt = compress_append(8, 0, cands, mask, g->rest, g->rest_cnt, &full);
+        if (full) {
+          memcpy(out->f, cands, sizeof cands);
+          return;
+        }
+      }
+    }
+    if (alpha == 1) {
+      upk u;
+      ur_pk(e, 0, &u);
+      for (int j = 0; j < 8; ++j) out->f[j] = beta * (-(or_logf(1.0f - u.f[j]) / 1.0f));
+      return;
+    }
+    int count = (int)alpha;
+    if ((float)count == alpha && count < 20) {
+      upk y, t;
+      nzur_pk(e, 0, &y);
+      while (--count) {
+        nzur_pk(e, 0, &t);
+        for (int j = 0; j < 8; ++j) y.f[j] = y.f[j] * t.f[j];
+      }
+      for (int j = 0; j < 8; ++j) out->f[j] = -(beta * or_logf(y.f[j]));
+      return;
+    }
+    for (;;) {
+      float alpha_1 = alpha - 1;
+      upk u, ux;
+      ur_pk(e, 0, &u);
+      float yx[8], xx[8];
+      int c[8];
+      for (int j = 0; j < 8; ++j) {
+        float s, cc;
+        or_sincosf((float)PI_D * u.f[j], &s, &cc);
+        yx[j] = s / cc;
+        xx[j] = sq * yx[j] + alpha_1;
+        c[j] = 0 < xx[j];
+      }
+      ur_pk(e, 0, &ux);
+      float cands[8];
+      int mask[8];
+      for (int j = 0; j < 8; ++j) {
+        float ub = (yx[j] * yx[j] + 1) * or_expf(alpha_1 * or_logf(xx[j] / alpha_1) - yx[j] * sq);
+        mask[j] = c[j] && (ux.f[j] <= ub);
+        cands[j] = beta * xx[j];
+      }
+      int full = 0;
+      g->rest_cnt = compress_append(8, 0, cands, mask, g->rest, g->rest_cnt, &full);
+      if (full) {
+        memcpy(out->f, cands, sizeof cands);
+        return;
+      }
+    }
+  }
+}
+
+int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n) {
+  int dbl = dtype == 1;
+  int P = P_of(dbl);
+  if (n % (size_t)P) return 2;
+  if (e->L != 4) return 3; /* AVX2 profile only */
+  float* of = (float*)out;
+  double* od = (double*)out;
+  or_gen* g2 = g + 1; /* nested generators (beta: gd1, gd2) */
+  or_gen* g3 = g + 2;
+  for (size_t k = 0; k < n / (size_t)P; ++k) {
+    upk p;
+    switch (dist) {
+      case OR_UNIFORM: { /* UniformRealGen, Basic.h:638-645; std form :584-590 */
+        ur_pk(e, dbl, &p);
+        if (dbl) {
+          double slope = b - a, bias = a;
+          for (int j = 0; j < 4; ++j) p.d[j] = (a == 0 && b == 1) ? p.d[j] : p.d[j] * slope + bias;
+        } else {
+          float fa = (float)a, fb = (float)b;
+          float slope = fb - fa, bias = fa;
+          for (int j = 0; j < 8; ++j) p.f[j] = (a == 0 && b == 1) ? p.f[j] : p.f[j] * slope + bias;
+        }
+        break;
+      }
+      case OR_BALANCED: { /* RandUtils::balanced, RandUtils.h:36-45 */
+        z2o_pk(e, dbl, &p);
+        if (dbl) {
+          double slope = b - a, bias = a;
+          for (int j = 0; j < 4; ++j)
+            p.d[j] = (a == -1 && b == 1) ? p.d[j] * 2 - 1 : p.d[j] * slope + bias;
+        } else {
+          float fa = (float)a, fb = (float)b;
+          float slope = fb - fa, bias = fa;
+          for (int j = 0; j < 8; ++j)
+            p.f[j] = (a == -1 && b == 1) ? p.f[j] * 2.0f - 1.0f : p.f[j] * slope + bias;
+        }
+        break;
+      }
+      case OR_STDNORMAL: /* StdNormalGen::packetOp, NormalExp.h:60-82 */
+        stdnormal_pk(e, g, dbl, &p);
+        break;
+      case OR_NORMAL:    /* NormalGen::packetOp, NormalExp.h:127-135 */
+      case OR_LOGNORMAL: /* LognormalGen::packetOp, :204-209 */
+        stdnormal_pk(e, g, dbl, &p);
+        if (dbl) {
+          for (int j = 0; j < 4; ++j) {
+            p.d[j] = p.d[j] * b + a;
+            if (dist == OR_LOGNORMAL) p.d[j] = or_exp(p.d[j]);
+          }
+        } else {
+          for (int j = 0; j < 8; ++j) {
+            p.f[j] = p.f[j] * (float)b + (float)a;
+            if (dist == OR_LOGNORMAL) p.f[j] = or_expf(p.f[j]);
+          }
+        }
+        break;
+      case OR_EXPONENTIAL: /* ExponentialGen::packetOp, NormalExp.h:391-398 */
+        ur_pk(e, dbl, &p);
+        if (dbl) for (int j = 0; j < 4; ++j) p.d[j] = -(or_log(1.0 - p.d[j]) / a);
+        else for (int j = 0; j < 8; ++j) p.f[j] = -(or_logf(1.0f - p.f[j]) / (float)a);
+        break;
+      case OR_CAUCHY: /* CauchyGen::packetOp, NormalExp.h:844-855 */
+        ur_pk(e, dbl, &p);
+        if (dbl) {
+          for (int j = 0; j < 4; ++j) {
+            double s, c;
+            or_sincos(PI_D * (p.d[j] - 0.5), &s, &c);
+            p.d[j] = a + b * (s / c);
+          }
+        } else {
+          for (int j = 0; j < 8; ++j) {
+            float s, c;
+            or_sincosf((float)PI_D * (p.f[j] - 0.5f), &s, &c);
+            p.f[j] = (float)a + (float)b * (s / c);
+          }
+        }
+        break;
+      case OR_WEIBULL: /* WeibullGen::packetOp, NormalExp.h:648-655 */
+        ur_pk(e, dbl, &p);
+        if (dbl) {
+          double ia = 1 / a;
+          for (int j = 0; j < 4; ++j) p.d[j] = or_exp(or_log(-or_log(1.0 - p.d[j])) * ia) * b;
+        } else {
+          float ia = 1 / (float)a;
+          for (int j = 0; j < 8; ++j) p.f[j] = or_expf(or_logf(-or_logf(1.0f - p.f[j])) * ia) * (float)b;
+        }
+        break;
+      case OR_EXTREME: /* ExtremeValueGen::packetOp, NormalExp.h:724-732 */
+        nzur_pk(e, dbl, &p);
+        if (dbl) for (int j = 0; j < 4; ++j) p.d[j] = a - or_log(-or_log(p.d[j])) * b;
+        else for (int j = 0; j < 8; ++j) p.f[j] = (float)a - or_logf(-or_logf(p.f[j])) * (float)b;
+        break;
+      case OR_GAMMA:
+        gamma_pk(e, g, dbl, a, b, &p);
+        break;
+      case OR_CHI_SQUARED: /* ChiSquaredGen = GammaGen(n/2, 2), NormalExp.h:767-802 */
+        gamma_pk(e, g, dbl, dbl ? a * 0.5 : (double)((float)a * 0.5f), 2, &p);
+        break;
+      case OR_BETA: { /* BetaGen::packetOp, NormalExp.h:949-976 */
+        int both_small = dbl ? (a < 1 && b < 1) : ((float)a < 1 && (float)b < 1);
+        if (both_small) {
+          for (;;) {
+            upk u1, u2;
+            ur_pk(e, dbl, &u1);
+            ur_pk(e, dbl, &u2);
+            int mask[8];
+            if (dbl) {
+              double cands[4];
+              for (int j = 0; j < 4; ++j) {
+                double p1 = or_exp(or_log(u1.d[j]) * (1 / a));
+                double p2 = or_exp(or_log(u2.d[j]) * (1 / b));
+                double x = p1 + p2;
+                cands[j] = p1 / x;
+                mask[j] = x <= 1;
+              }
+              int full = 0;
+              g->rest_cnt = compress_append(4, 1, cands, mask, g->rest, g->rest_cnt, &full);
+              if (full) { memcpy(p.d, cands, sizeof cands); break; }
+            } else {
+              float cands[8];
+              float fa = (float)a, fb = (float)b;
+              for (int j = 0; j < 8; ++j) {
+                float p1 = or_expf(or_logf(u1.f[j]) * (1 / fa));
+                float p2 = or_expf(or_logf(u2.f[j]) * (1 / fb));
+                float x = p1 + p2;
+                cands[j] = p1 / x;
+                mask[j] = x <= 1;
+              }
+              int full = 0;
+              g->rest_cnt = compress_append(8, 0, cands, mask, g->rest, g->rest_cnt, &full);
+              if (full) { memcpy(p.f, cands, sizeof cands); break; }
+            }
+          }
+        } else {
+          upk p1, p2;
+          gamma_pk(e, g2, dbl, a, 1, &p1);
+          gamma_pk(e, g3, dbl, b, 1, &p2);
+          p.dbl = dbl;
+          if (dbl) for (int j = 0; j < 4; ++j) p.d[j] = p1.d[j] / (p1.d[j] + p2.d[j]);
+          else for (int j = 0; j < 8; ++j) p.f[j] = p1.f[j] / (p1.f[j] + p2.f[j]);
+        }
+        break;
+      }
+      case OR_STUDENT_T: { /* StudentTGen::packetOp, NormalExp.h:283-299 (psin) */
+        upk u1, u2;
+        ur_pk(e, dbl, &u1);
+        ur_pk(e, dbl, &u2);
+        p.dbl = dbl;
+        if (dbl) {
+          for (int j = 0; j < 4; ++j) {
+            double r = sqrt(a * (or_exp(or_log(1.0 - u1.d[j]) * (-2 / a)) - 1));
+            double s, c;
+            or_sincos((2 * PI_D) * u2.d[j], &s, &c);
+            p.d[j] = r * s;
+          }
+        } else {
+          float fa = (float)a;
+          for (int j = 0; j < 8; ++j) {
+            float r = sqrtf(fa * (or_expf(or_logf(1.0f - u1.f[j]) * (-2 / fa)) - 1));
+            float s, c;
+            or_sincosf((float)(2 * PI_D) * u2.f[j], &s, &c);
+            p.f[j] = r * s;
+          }
+        }
+        break;
+      }
+      default:
+        return 1;
+    }
+    if (dbl) memcpy(od + k * 4, p.d, 32);
+    else memcpy(of + k * 8, p.f, 32);
+  }
+  return 0;
+}
+
+/* ======================================================================
+ * Integer generators.  int32 packets are Packet4i; their float internals are
+ * Packet4f drawn through rng.half() (arch/AVX/RandUtils.h:28-31).
+ * ====================================================================== */
+
+/* PoissonGen::packetOp, Discrete.h:854-903 */
+static void poisson_pk(or_vmt* e, or_gen* g, double mean, int32_t* res) {
+  if (mean < 12) {
+    float pne = (float)exp(-mean);
+    float val[4] = {1, 1, 1, 1};
+    for (int j = 0; j < 4; ++j) res[j] = 0;
+    for (;;) {
+      float u[4];
+      ur_f4(e, u);
+      int any = 0;
+      int c[4];
+      for (int j = 0; j < 4; ++j) {
+        val[j] = val[j] * u[j];
+        c[j] = pne < val[j];
+        any |= c[j];
+      }
+      if (!any) break;
+      for (int j = 0; j < 4; ++j) res[j] += c[j];
+    }
+    return;
+  }
+  float ppi = (float)PI_D, psqrt_tmean = (float)sqrt(2 * mean), pmean = (float)mean;
+  float plog_mean = (float)log(mean);
+  float pg1 = (float)(mean * log(mean) - lgamma(mean + 1));
+  for (;;) {
+    float u[4], u2[4];
+    ur_f4(e, u);
+    float fres[4], p1[4];
+    for (int j = 0; j < 4; ++j) {
+      float s, c;
+      or_sincosf(ppi * u[j], &s, &c);
+      float yx = s / c;
+      fres[j] = truncf(psqrt_tmean * yx + pmean);
+      p1[j] = (yx * yx + 1.0f) * 0.9f;
+    }
+    ur_f4(e, u2);
+    uint32_t cands[4];
+    int mask[4];
+    for (int j = 0; j < 4; ++j) {
+      float p2 = or_expf((fres[j] * plog_mean - or_lgamma_approxf(fres[j] + 1.0f)) - pg1);
+      mask[j] = (0.0f <= fres[j]) && (u2[j] <= p1[j] * p2);
+      cands[j] = f2u(fres[j]);
+    }
+    int full = 0;
+    g->rest_cnt = compress_append(4, 0, cands, mask, g->rest, g->rest_cnt, &full);
+    if (full) {
+      for (int j = 0; j < 4; ++j) res[j] = (int32_t)u2f(cands[j]);
+      return;
+    }
+  }
+}
+
+int or_gen_poisson(or_vmt* e, or_gen* g, double mean, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  for (size_t k = 0; k < n / 4; ++k) poisson_pk(e, g, mean, out + 4 * k);
+  return 0;
+}
+
+/* BinomialGen::packetOp, Discrete.h:990-1052 */
+int or_gen_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  double small_p = p < 1 - p ? p : 1 - p;
+  double pmean_d = trials * small_p;
+  double g1 = 0, sqrt_v = 0, lsp = 0, lsq = 0;
+  if (!(trials < 25 || pmean_d < 1.0)) {
+    g1 = lgamma(trials + 1);
+    sqrt_v = sqrt(2 * pmean_d * (1 - small_p));
+    lsp = log(small_p);
+    lsq = log(1 - small_p);
+  }
+  for (size_t k = 0; k < n / 4; ++k) {
+    int32_t res[4];
+    if (trials < 25) {
+      float pp = (float)p;
+      for (int j = 0; j < 4; ++j) res[j] = trials;
+      for (int i = 0; i < trials; ++i) {
+        float u[4];
+        ur_f4(e, u);
+        for (int j = 0; j < 4; ++j) res[j] += (pp <= u[j]) ? -1 : 0;
+      }
+      memcpy(out + 4 * k, res, sizeof res);
+      continue;
+    } else if (pmean_d < 1.0) {
+      poisson_pk(e, g, pmean_d, res);
+    } else {
+      float ppi = (float)PI_D, ptrials = (float)trials, psqrt_v = (float)sqrt_v, pmean = (float)pmean_d;
+      float plsp = (float)lsp, plsq = (float)lsq, pg1 = (float)g1;
+      for (;;) {
+        float u[4], u2[4], fres[4], p1[4];
+        ur_f4(e, u);
+        for (int j = 0; j < 4; ++j) {
+          float s, c;
+          or_sincosf(ppi * u[j], &s, &c);
+          float ys = s / c;
+          fres[j] = truncf(psqrt_v * ys + pmean);
+          p1[j] = ((float)1.2 * psqrt_v) * (1.0f + ys * ys);
+        }
+        ur_f4(e, u2);
+        uint32_t cands[4];
+        int mask[4];
+        for (int j = 0; j < 4; ++j) {
+          float t = (pg1 - or_lgamma_approxf(fres[j] + 1.0f)) - or_lgamma_approxf((ptrials + 1.0f) - fres[j]);
+          t = t + fres[j] * plsp;
+          t = t + (ptrials - fres[j]) * plsq;
+          float p2 = or_expf(t);
+          mask[j] = (0.0f <= fres[j]) && (fres[j] <= ptrials) && (u2[j] <= p1[j] * p2);
+          cands[j] = f2u(fres[j]);
+        }
+        int full = 0;
+        g->rest_cnt = compress_append(4, 0, cands, mask, g->rest, g->rest_cnt, &full);
+        if (full) {
+          for (int j = 0; j < 4; ++j) res[j] = (int32_t)u2f(cands[j]);
+          break;
+        }
+      }
+    }
+    for (int j = 0; j < 4; ++j) out[4 * k + j] = (p == small_p) ? res[j] : trials - res[j];
+  }
+  return 0;
+}
+
+/* RandbitsGen::packetOp<Packet4i>: RawbitsMaker<Packet4i,..>::rawbits =
+ * rng.half(), Basic.h:393-399, arch/AVX/RandUtils.h:23-26 */
+int or_gen_randbits(or_vmt* e, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  for (size_t k = 0; k < n / 4; ++k) {
+    uint32_t w[4];
+    draw_half(e, w);
+    memcpy(out + 4 * k, w, 16);
+  }
+  return 0;
+}
+
+/* ======================================================================
+ * DiscreteGen<int32_t, int32_t>: CDF (<16 weights) or AliasMethod (>=16),
+ * Discrete.h:23-207 (table build), :385-412 (constructor), :443-485 (AVX2
+ * packetOp: 8 draws from one rng() packet, 4 returned and 4 cached).
+ * ====================================================================== */
+or_discrete* or_discrete_new(const double* w, int n) {
+  if (n < 1) return NULL;
+  or_discrete* d = (or_discrete*)calloc(1, sizeof(or_discrete));
+  d->n = n;
+  if (n < 16) {
+    d->use_cdf = 1;
+    double acc = 0, cdfd[64];
+    for (int i = 0; i < n; ++i) cdfd[i] = (acc += w[i]);
+    for (int i = 0; i < n; ++i) d->cdf[i] = (uint32_t)(cdfd[i] / cdfd[n - 1] * 0x80000000);
+    return d;
+  }
+  double sum = 0;
+  for (int i = 0; i < n; ++i) sum += w[i];
+  if (!isfinite(sum)) { free(d); return NULL; }
+  size_t nbsize = (size_t)ceil(log2((double)n));
+  size_t psize = (size_t)1 << nbsize;
+  d->bitsize = (int)nbsize;
+  d->bitmask = (uint32_t)(((size_t)-1) >> (sizeof(size_t) * 8 - nbsize));
+  d->prob = (int32_t*)calloc(psize, sizeof(int32_t));
+  d->alias = (int32_t*)calloc(psize, sizeof(int32_t));
+  sum /= (double)psize;
+  double* f = (double*)calloc(psize, sizeof(double));
+  for (int i = 0; i < n; ++i) f[i] = w[i] / sum;
+  size_t over = 0, under = 0, mm;
+  while (over < psize && f[over] < 1) ++over;
+  while (under < psize && f[under] >= 1) ++under;
+  mm = under + 1;
+  while (over < psize && under < psize) {
+    d->prob[under] = (int32_t)(f[under] * (2147483647 + 1.0));
+    d->alias[under] = (int32_t)over;
+    f[over] += f[under] - 1;
+    if (f[over] >= 1 || mm <= over) {
+      for (under = mm; under < psize && f[under] >= 1; ++under) {}
+      mm = under + 1;
+    } else {
+      under = over;
+    }
+    while (over < psize && f[over] < 1) ++over;
+  }
+  for (; over < psize; ++over) {
+    if (f[over] >= 1) {
+      d->prob[over] = 2147483647;
+      d->alias[over] = (int32_t)over;
+    }
+  }
+  if (under < psize) {
+    d->prob[under] = 2147483647;
+    d->alias[under] = (int32_t)under;
+    for (under = mm; under < (size_t)n; ++under) {
+      if (f[under] < 1) {
+        d->prob[under] = 2147483647;
+        d->alias[under] = (int32_t)under;
+      }
+    }
+  }
+  free(f);
+  return d;
+}
+
+void or_discrete_free(or_discrete* d) {
+  if (!d) return;
+  free(d->prob);
+  free(d->alias);
+  free(d);
+}
+
+int or_discrete_table(const or_discrete* d, int32_t* prob, int32_t* alias, int cap) {
+  if (d->use_cdf) {
+    for (int i = 0; i < d->n && i < cap; ++i) prob[i] = (int32_t)d->cdf[i];
+    return -d->n;
+  }
+  int ps = 1 << d->bitsize;
+  for (int i = 0; i < ps && i < cap; ++i) {
+    prob[i] = d->prob[i];
+    alias[i] = d->alias[i];
+  }
+  return ps;
+}
+
+int or_gen_discrete(or_vmt* e, or_gen* g, const or_discrete* d, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  for (size_t k = 0; k < n / 4; ++k) {
+    if (g->valid) {
+      g->valid = 0;
+      memcpy(out + 4 * k, g->cache, 16);
+      continue;
+    }
+    uint32_t rx[8];
+    int32_t ret[8];
+    draw_full(e, rx);
+    if (d->use_cdf) {
+      for (int j = 0; j < 8; ++j) {
+        int32_t r = d->n - 1;
+        int32_t x = (int32_t)(rx[j] & 0x7fffffffu);
+        for (int i = 0; i < d->n - 1; ++i) r += (x < (int32_t)d->cdf[i]) ? -1 : 0;
+        ret[j] = r;
+      }
+    } else {
+      for (int j = 0; j < 8; ++j) {
+        int32_t albit = (int32_t)(rx[j] & d->bitmask);
+        int32_t sh = (int32_t)(rx[j] >> 1);
+        ret[j] = (sh < d->prob[albit]) ? albit : d->alias[albit];
+      }
+    }
+    g->valid = 1;
+    memcpy(g->cache, ret + 4, 16);
+    memcpy(out + 4 * k, ret, 16);
+  }
+  return 0;
+}

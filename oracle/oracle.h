@@ -1,0 +1,125 @@
+/*
+ * CPU ORACLE — test infrastructure only.
+ *
+ * A plain-C restatement of EigenRand's sampling hot path (bab2min/EigenRand
+ * v0.6.0), used by tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline as the checker.  Nothing in the shipped library links or calls it.
+ *
+ * Reference profile that is emulated: x86-64 AVX2 with Eigen 3.4, i.e.
+ *   Vmt19937_64 = Pmt19937_64<Packet8i> (4 u64 lanes, lane l seeded seed+l),
+ *   float packets of 8, double packets of 4, int32 packets of 4 (Eigen 3.4
+ *   keeps integer packets on SSE when AVX2 is on).
+ *
+ * Transcendentals: log/exp are the library's own published-method
+ * implementations (Cody-Waite reduction + fitted polynomial, explicit fma),
+ * restated independently here; sin/cos are EigenRand's own psincos
+ * (EigenRand/MorePacketMath.h:297-491) restated; sqrt and division are IEEE.
+ * Every float operation is rounded individually (-ffp-contract=off).
+ */
+#ifndef GR_ORACLE_H
+#define GR_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- one MT19937-64 lane, literal restatement of MersenneTwister --------- */
+typedef struct {
+  uint64_t state[624]; /* double buffer, PacketRandomEngine.h:406 */
+  int idx;             /* stateIdx */
+} or_mt64;
+
+void or_mt64_seed(or_mt64* s, uint64_t seed);
+uint64_t or_mt64_next(or_mt64* s);
+
+/* ---- packet engine (Vmt19937_64 / P8 raw stream) ------------------------- */
+#define OR_MAXL 8
+typedef struct {
+  int L;
+  or_mt64 lane[OR_MAXL];
+  int half_valid;               /* MersenneTwister::half() cache, :325-336 */
+  uint32_t half_cache[OR_MAXL]; /* upper half of the last split packet      */
+} or_vmt;
+
+or_vmt* or_vmt_new(uint64_t seed, int lanes);
+void or_vmt_free(or_vmt* e);
+void or_vmt_copy(or_vmt* dst, const or_vmt* src);
+size_t or_vmt_sizeof(void);
+void or_vmt_raw(or_vmt* e, uint64_t* out, size_t npackets);
+void or_vmt_discard(or_vmt* e, uint64_t npackets);
+/* raw words of the last 312 outputs of each lane (untempered), for engine
+ * state comparison: out[l*312 + i] */
+void or_vmt_window(const or_vmt* e, uint64_t* out);
+
+/* ---- generator state (caches that EigenRand keeps inside *Gen objects) --- */
+typedef struct {
+  int valid;          /* StdNormalGen / DiscreteGen packet cache flag        */
+  uint32_t cache[16]; /* cached packet (up to 64 bytes)                      */
+  int rest_cnt;       /* CompressMask::compress_append carry count           */
+  uint32_t rest[16];  /* carried accepted lanes                              */
+} or_gen;
+size_t or_gen_sizeof(void);
+
+/* Distribution families.  n must be a multiple of the packet width
+ * (8 float / 4 double / 4 int32).  Returns 0 on success, nonzero on error.
+ * dtype: 0 = float32, 1 = float64. */
+enum {
+  OR_UNIFORM = 1,   /* a=min, b=max (UniformRealGen); std form when a=0,b=1 */
+  OR_BALANCED = 2,  /* a, b (Balanced2Gen); a=-1,b=1 is BalancedGen          */
+  OR_NORMAL = 3,    /* a=mean, b=stdev                                        */
+  OR_LOGNORMAL = 4, /* a=mean, b=stdev                                        */
+  OR_EXPONENTIAL = 5, /* a=lambda                                             */
+  OR_CAUCHY = 6,    /* a, b                                                   */
+  OR_WEIBULL = 7,   /* a=shape, b=scale                                       */
+  OR_EXTREME = 8,   /* a=location, b=scale                                    */
+  OR_GAMMA = 9,     /* a=alpha, b=beta                                        */
+  OR_BETA = 10,     /* a, b                                                   */
+  OR_STUDENT_T = 11,  /* a = n                                                */
+  OR_CHI_SQUARED = 12, /* a = n                                              */
+  OR_STDNORMAL = 13   /* StdNormalGen: no mean/stdev scaling                  */
+};
+int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b,
+                void* out, size_t n);
+
+/* int32 distributions */
+int or_gen_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out, size_t n);
+int or_gen_poisson(or_vmt* e, or_gen* g, double mean, int32_t* out, size_t n);
+int or_gen_randbits(or_vmt* e, int32_t* out, size_t n);
+
+/* discrete with int32 precision (DiscreteGen<int32_t, int32_t>) */
+typedef struct {
+  int use_cdf;
+  int n;             /* number of weights */
+  uint32_t cdf[64];  /* used when n < 16 */
+  int bitsize;       /* alias table: 2^bitsize entries */
+  uint32_t bitmask;
+  int32_t* prob;
+  int32_t* alias;
+} or_discrete;
+or_discrete* or_discrete_new(const double* w, int n);
+void or_discrete_free(or_discrete* d);
+int or_discrete_table(const or_discrete* d, int32_t* prob, int32_t* alias, int cap);
+int or_gen_discrete(or_vmt* e, or_gen* g, const or_discrete* d, int32_t* out, size_t n);
+
+/* ---- math (library's own log/exp; EigenRand psincos restated) ---------- */
+float or_logf(float x);
+float or_expf(float x);
+double or_log(double x);
+double or_exp(double x);
+void or_sincosf(float x, float* s, float* c);
+void or_sincos(double x, double* s, double* c);
+float or_lgamma_approxf(float x);
+double or_lgamma_approx(double x);
+void or_vec_logf(const float* x, float* y, size_t n);
+void or_vec_expf(const float* x, float* y, size_t n);
+void or_vec_log(const double* x, double* y, size_t n);
+void or_vec_exp(const double* x, double* y, size_t n);
+void or_vec_sincosf(const float* x, float* s, float* c, size_t n);
+void or_vec_sincos(const double* x, double* s, double* c, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

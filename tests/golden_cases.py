@@ -1,0 +1,60 @@
+"""Fixed small cases shared by the golden-fixture generator and the tests.
+
+Each case draws n samples from a fresh engine seeded `seed` (the reference's
+own test seeds and the configuration seeds: 42, 1234)."""
+import numpy as np
+
+W16 = [0.5488135, 0.71518937, 0.60276338, 0.54488318, 0.4236548, 0.64589411, 0.43758721, 0.891773,
+       0.96366276, 0.38344152, 0.79172504, 0.52889492, 0.56804456, 0.92559664, 0.07103606, 0.0871293]
+W5 = [1, 2, 3, 4, 5]
+
+CASES = {}
+
+
+def _add(name, kind, dtype, n, a=0.0, b=0.0, trials=0, weights=None, seed=1234):
+    CASES[name] = dict(kind=kind, dtype=dtype, n=n, a=a, b=b, trials=trials, weights=weights, seed=seed)
+
+
+for dt, tag, n in ((np.float32, "f32", 256), (np.float64, "f64", 128)):
+    _add(f"uniformReal_{tag}", "UNIFORM_REAL", dt, n)
+    _add(f"uniformReal2_{tag}", "UNIFORM_REAL2", dt, n, -2.0, 3.0)
+    _add(f"balanced_{tag}", "BALANCED", dt, n)
+    _add(f"balanced2_{tag}", "BALANCED2", dt, n, -3.0, 5.0)
+    _add(f"stdnormal_{tag}", "NORMAL_STD", dt, n)
+    _add(f"normal23_{tag}", "NORMAL", dt, n, 2.0, 3.0)
+    _add(f"lognormal_{tag}", "LOGNORMAL", dt, n, 0.0, 1.0)
+    _add(f"exponential_{tag}", "EXPONENTIAL", dt, n, 1.0)
+    _add(f"cauchy_{tag}", "CAUCHY", dt, n, 0.0, 1.0)
+    _add(f"weibull_{tag}", "WEIBULL", dt, n, 1.5, 1.0)
+    _add(f"extremeValue_{tag}", "EXTREME_VALUE", dt, n, 0.0, 1.0)
+    _add(f"gamma1_{tag}", "GAMMA", dt, n, 1.0, 1.0)
+    _add(f"gamma5_{tag}", "GAMMA", dt, n, 5.0, 1.0)
+    _add(f"gamma05_{tag}", "GAMMA", dt, n, 0.5, 1.0)
+    _add(f"beta_{tag}", "BETA", dt, n, 0.5, 2.0)
+_add("raw_42", "RAW", np.uint64, 256, seed=42)
+_add("binomial20", "BINOMIAL", np.int32, 256, 0.3, trials=20)
+_add("poisson4", "POISSON", np.int32, 256, 4.0)
+_add("discrete16", "DISCRETE", np.int32, 256, weights=W16)
+_add("discrete5", "DISCRETE", np.int32, 256, weights=W5)
+_add("randbits", "RANDBITS", np.int32, 256)
+
+
+def run_oracle(oracle, c):
+    e = oracle.Engine(c["seed"])
+    if c["kind"] == "RAW":
+        return e.raw(c["n"] // 4)
+    g = oracle.Gen()
+    return oracle.generate(e, g, c["kind"], c["n"], c["dtype"], c["a"], c["b"], c["trials"], c["weights"])
+
+
+def run_gpu(er, c):
+    import torch
+    u = er.Vmt19937_64(c["seed"])
+    if c["kind"] == "RAW":
+        return er.raw_u64(u, c["n"]).cpu().numpy().view(np.uint64)
+    tdt = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32}[c["dtype"]]
+    d, keep = er._desc(c["kind"], tdt, c["a"], c["b"], c["trials"], c["weights"])
+    o = torch.empty(c["n"], dtype=tdt, device="cuda")
+    er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), c["n"], er._stream_ptr()))
+    torch.cuda.synchronize()
+    return o.cpu().numpy()

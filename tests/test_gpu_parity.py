@@ -1,0 +1,201 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bit-exact comparisons throughout: the engine is integer work, the uniform
+transforms are exact, and the transcendental steps use the same operation
+sequence on both sides (csrc/gr_math.cuh, oracle/ormath.c)."""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import golden_cases  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def er(gpulib):
+    return gpulib
+
+
+def mem(t):
+    """Eigen linear (column-major) order of a (rows, cols) output."""
+    torch.cuda.synchronize()
+    if t.dim() == 2:
+        t = t.t()
+    return t.contiguous().reshape(-1).cpu().numpy()
+
+
+def npdt(tdt):
+    return {torch.float32: np.float32, torch.float64: np.float64, torch.int32: np.int32}[tdt]
+
+
+def assert_bits_equal(a, b, msg=""):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    ua = a.view(np.uint64 if a.itemsize == 8 else np.uint32)
+    ub = b.view(np.uint64 if b.itemsize == 8 else np.uint32)
+    bad = np.nonzero(ua != ub)[0]
+    assert bad.size == 0, f"{msg}: {bad.size} mismatches, first at {bad[:5]}: {a[bad[:5]]} vs {b[bad[:5]]}"
+
+
+# ---------------------------------------------------------------- engine
+def test_raw_stream_config1_2pow24(er, oracle):
+    """Vmt19937_64{42}, 2^24 raw uint64 draws: bit-exact (jump-ahead segments)."""
+    u = er.Vmt19937_64(42)
+    g = er.raw_u64(u, 1 << 24)
+    ref = oracle.Engine(42).raw(1 << 22)
+    assert_bits_equal(g.cpu().numpy().view(np.uint64), ref, "raw 2^24")
+
+
+def test_raw_stream_consecutive_calls(er, oracle):
+    u = er.Vmt19937_64(7)
+    e = oracle.Engine(7)
+    for n in (4, 1248, 100000, 4 * 312 * 3, 8, 1 << 20, 40):
+        g = er.raw_u64(u, n).cpu().numpy().view(np.uint64)
+        assert_bits_equal(g, e.raw(n // 4), f"raw n={n}")
+
+
+def test_engine_window_after_calls(er, oracle):
+    """Engine state in HBM equals the oracle's after mixed calls."""
+    u = er.Vmt19937_64(99)
+    e = oracle.Engine(99)
+    er.raw_u64(u, 4 * 1000)
+    e.raw(1000)
+    er.raw_u64(u, 1 << 21)
+    e.raw(1 << 19)
+    blob = u.save()
+    win = np.frombuffer(blob[:4 * 312 * 8], dtype=np.uint64).reshape(4, 312)
+    np.testing.assert_array_equal(win, e.window())
+
+
+def test_save_restore_roundtrip(er):
+    u = er.Vmt19937_64(5)
+    er.raw_u64(u, 4000)
+    blob = u.save()
+    a = er.raw_u64(u, 40000).cpu()
+    u.restore(blob)
+    b = er.raw_u64(u, 40000).cpu()
+    assert torch.equal(a, b)
+
+
+def test_discard_matches_draws(er, oracle):
+    u = er.Vmt19937_64(11)
+    u.discard(12345)
+    e = oracle.Engine(11)
+    e.discard(12345)
+    assert_bits_equal(er.raw_u64(u, 4096).cpu().numpy().view(np.uint64), e.raw(1024), "discard")
+
+
+def test_streams_are_independent_engines(er, oracle):
+    """streams=K: slice k comes from Vmt19937_64(seed + 4k)."""
+    K, per = 8, 8 * 1000
+    u = er.Vmt19937_64(1234, streams=K)
+    x = mem(er.uniformReal(K * per, 1, u))
+    for k in range(K):
+        e = oracle.Engine(1234 + 4 * k)
+        ref = oracle.generate(e, oracle.Gen(), "UNIFORM_REAL", per, np.float32)
+        assert_bits_equal(x[k * per:(k + 1) * per], ref, f"slice {k}")
+
+
+# ---------------------------------------------------------------- config 1
+def test_config1_uniform_and_normal_1024sq(er, oracle):
+    for fn, kind in ((er.uniformReal, "UNIFORM_REAL"), (er.normal, "NORMAL_STD")):
+        u = er.Vmt19937_64(42)
+        x = mem(fn(1024, 1024, u))
+        ref = oracle.generate(oracle.Engine(42), oracle.Gen(), kind, 1 << 20, np.float32)
+        assert_bits_equal(x, ref, kind)
+
+
+# ---------------------------------------------------------------- golden fixtures
+DIRECT = [name for name, c in golden_cases.CASES.items()
+          if c["kind"] not in ("GAMMA", "BETA", "POISSON", "BINOMIAL") or (c["kind"] == "GAMMA" and c["a"] == 1.0)]
+
+
+@pytest.mark.parametrize("name", DIRECT)
+def test_golden_fixture(er, name):
+    fx = np.load(os.path.join(ROOT, "tests", "golden", "oracle_fixtures.npz"))
+    got = golden_cases.run_gpu(er, golden_cases.CASES[name])
+    assert_bits_equal(got, fx[name], name)
+
+
+# ---------------------------------------------------------------- every direct kind, large (jump path)
+KINDS = [
+    ("UNIFORM_REAL", 0, 0), ("UNIFORM_REAL2", -2.0, 3.0), ("BALANCED", 0, 0), ("BALANCED2", -3.0, 5.0),
+    ("NORMAL_STD", 0, 0), ("NORMAL", 2.0, 3.0), ("LOGNORMAL", 0.0, 1.0), ("EXPONENTIAL", 1.5, 0),
+    ("CAUCHY", 0.0, 1.0), ("WEIBULL", 1.5, 1.0), ("EXTREME_VALUE", 0.0, 1.0), ("GAMMA", 1.0, 2.0),
+]
+
+
+@pytest.mark.parametrize("kind,a,b", KINDS)
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+def test_kind_bit_exact_large(er, oracle, kind, a, b, tdt):
+    n = 1 << 21  # long enough for jump-ahead segments
+    u = er.Vmt19937_64(1234)
+    d, keep = er._desc(kind, tdt, a, b)
+    o = torch.empty(n, dtype=tdt, device="cuda")
+    er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), n, er._stream_ptr()))
+    got = mem(o)
+    ref = oracle.generate(oracle.Engine(1234), oracle.Gen(), kind, n, npdt(tdt), a, b)
+    assert_bits_equal(got, ref, f"{kind} {tdt}")
+
+
+# ---------------------------------------------------------------- caches carried between calls
+def test_normal_gen_cache_carry(er, oracle):
+    """StdNormalGen caches the cos half across generate() calls."""
+    for tdt, P in ((torch.float32, 8), (torch.float64, 4)):
+        u = er.Vmt19937_64(3)
+        g = er.NormalGen(0.5, 2.0, dtype=tdt)
+        e = oracle.Engine(3)
+        og = oracle.Gen()
+        for n in (P, 3 * P, 5 * P, 2 * P, P, 7 * P, 1 << 18):
+            got = mem(g.generate(n, 1, u))
+            ref = oracle.generate(e, og, "NORMAL", n, npdt(tdt), 0.5, 2.0)
+            assert_bits_equal(got, ref, f"normal cache {tdt} n={n}")
+
+
+def test_half_packet_cache_between_kinds(er, oracle):
+    """rng.half() cache survives full-packet draws (PacketRandomEngine.h:325-336)."""
+    u = er.Vmt19937_64(8)
+    e = oracle.Engine(8)
+    seq = [("BALANCED", torch.float64, 4), ("UNIFORM_REAL", torch.float32, 16), ("RANDBITS", torch.int32, 4),
+           ("BALANCED", torch.float64, 12), ("RANDBITS", torch.int32, 8), ("BALANCED", torch.float64, 1 << 16),
+           ("RANDBITS", torch.int32, 4)]
+    for kind, tdt, n in seq:
+        d, keep = er._desc(kind, tdt)
+        o = torch.empty(n, dtype=tdt, device="cuda")
+        er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), n, er._stream_ptr()))
+        ref = oracle.generate(e, oracle.Gen(), kind, n, npdt(tdt), *((-1.0, 1.0) if kind == "BALANCED" else (0.0, 0.0)))
+        assert_bits_equal(mem(o), ref, f"{kind} n={n}")
+
+
+@pytest.mark.parametrize("weights", [golden_cases.W16, golden_cases.W5, list(range(1, 41))])
+def test_discrete_gen_cache(er, oracle, weights):
+    u = er.Vmt19937_64(21)
+    g = er.DiscreteGen(weights)
+    e = oracle.Engine(21)
+    og = oracle.Gen()
+    for n in (4, 8, 12, 4, 1 << 16, 4):
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, "DISCRETE", n, np.int32, weights=weights)
+        assert_bits_equal(got, ref, f"discrete n={n}")
+
+
+# ---------------------------------------------------------------- errors
+def test_size_not_multiple_of_packet_is_rejected(er):
+    u = er.Vmt19937_64(1)
+    with pytest.raises(er.GrError):
+        er.uniformReal(5, 3, u)
+
+
+def test_nan_weight_sum_is_rejected(er):
+    u = er.Vmt19937_64(1)
+    with pytest.raises(er.GrError):
+        er.discrete(16, 1, u, [float("nan")] + [1.0] * 20)

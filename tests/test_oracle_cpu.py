@@ -1,0 +1,118 @@
+"""CPU checks of the oracle and of the library's host-side logic (no GPU)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_engine_pinned_to_libstdcxx(oracle):
+    ok, out = oracle.pin_engine()
+    assert ok, out
+
+
+def test_packet_stream_interleave(oracle):
+    """R[4k + l] = lane_l[k]: the packet order of Vmt19937_64 under AVX2."""
+    e = oracle.Engine(42)
+    r = e.raw(300)
+    lanes = [oracle.Engine(42 + l, lanes=1).raw(300) for l in range(4)]
+    for l in range(4):
+        np.testing.assert_array_equal(r[l::4], lanes[l])
+
+
+@pytest.mark.parametrize("fn,lo,hi,n,maxulp", [
+    ("or_vec_logf", -80.0, 80.0, 400000, 1.0),
+    ("or_vec_expf", -87.0, 88.0, 400000, 1.0),
+])
+def test_float_math_ulp(oracle, fn, lo, hi, n, maxulp):
+    rng = np.random.default_rng(1)
+    if fn == "or_vec_logf":
+        x = np.exp(rng.uniform(lo, hi, n)).astype(np.float32)
+        ref = np.log(x.astype(np.float64))
+    else:
+        x = rng.uniform(lo, hi, n).astype(np.float32)
+        ref = np.exp(x.astype(np.float64))
+    y = oracle.vec_math(fn, x)
+    ulp = np.abs(y.astype(np.float64) - ref) / np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    assert ulp.max() <= maxulp
+
+
+def test_double_math_ulp(oracle):
+    mp = pytest.importorskip("mpmath")
+    rng = np.random.default_rng(2)
+    x = np.exp(rng.uniform(-700, 700, 3000))
+    y = oracle.vec_math("or_vec_log", x)
+    ref = np.array([float(mp.log(mp.mpf(float(v)))) for v in x])
+    assert (np.abs(y - ref) / np.spacing(np.abs(ref))).max() <= 1.0
+    x = rng.uniform(-700, 700, 3000)
+    y = oracle.vec_math("or_vec_exp", x)
+    ref = np.array([float(mp.exp(mp.mpf(float(v)))) for v in x])
+    assert (np.abs(y - ref) / np.spacing(np.abs(ref))).max() <= 1.0
+
+
+def test_sincos_restatement_accuracy(oracle):
+    """EigenRand's psincos is a float-grade Cephes polynomial: abs error ~1e-7."""
+    x = np.linspace(-2 * np.pi, 2 * np.pi, 100001).astype(np.float32)
+    s = np.empty_like(x)
+    c = np.empty_like(x)
+    L = oracle.lib()
+    L.or_vec_sincosf(oracle._p(x), oracle._p(s), oracle._p(c), x.size)
+    assert np.abs(s - np.sin(x.astype(np.float64))).max() < 3e-7
+    assert np.abs(c - np.cos(x.astype(np.float64))).max() < 3e-7
+
+
+def test_jump_algebra_host(tmp_path):
+    """GF(2) jump polynomials (library host code) reproduce sequential MT19937-64."""
+    exe = tmp_path / "jump_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-o", str(exe),
+                    os.path.join(ROOT, "tests", "cpp", "jump_check.cpp"),
+                    os.path.join(ROOT, "eigenrand_gb300", "csrc", "gr_poly.cpp")], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_abi_exports_every_declared_symbol(gpulib):
+    from eigenrand_gb300 import _lib
+    hdr = open(os.path.join(ROOT, "include", "gpurand.h")).read()
+    declared = sorted(set(re.findall(r"\b(gr_[a-z0-9_]+)\s*\(", hdr)))
+    lib = _lib.load()
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(declared) >= set(_lib.EXPORTS)
+
+
+def test_library_version_string(gpulib):
+    assert "sm_103a" in gpulib.version()
+
+
+def test_alias_table_matches_reference_rules(oracle):
+    """AliasMethod (Discrete.h:76-190): table reproduces the weights exactly in
+    expectation: P(k) = sum over slots of prob/2^31 and alias mass."""
+    rng = np.random.default_rng(3)
+    w = rng.uniform(0, 1, 16)
+    L = oracle.lib()
+    d = L.or_discrete_new(oracle._p(w), len(w))
+    prob = np.zeros(64, np.int32)
+    alias = np.zeros(64, np.int32)
+    ps = L.or_discrete_table(d, oracle._p(prob), oracle._p(alias), 64)
+    L.or_discrete_free(d)
+    assert ps == 16
+    mass = np.zeros(16)
+    for slot in range(ps):
+        p = prob[slot] / 2.0 ** 31
+        mass[slot] += p / ps
+        mass[alias[slot]] += (1 - p) / ps
+    np.testing.assert_allclose(mass, w / w.sum(), atol=1e-8)
+
+
+def test_oracle_golden_fixtures(oracle):
+    """The oracle reproduces the committed fixtures (regression pin)."""
+    import golden_cases
+    path = os.path.join(ROOT, "tests", "golden", "oracle_fixtures.npz")
+    fx = np.load(path)
+    for name, case in golden_cases.CASES.items():
+        got = golden_cases.run_oracle(oracle, case)
+        np.testing.assert_array_equal(got, fx[name], err_msg=name)
