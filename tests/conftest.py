@@ -25,7 +25,10 @@ def oracle():
 @pytest.fixture(scope="session")
 def gpulib():
     """Built and loaded sampling library (no GPU needed to load it)."""
-    from eigenrand_gb300 import build
-    build.build()
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_gr_build", os.path.join(ROOT, "eigenrand_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
     import eigenrand_gb300 as er
     return er
