@@ -62,7 +62,7 @@ def load(path=None):
     path = path or os.environ.get("GPURAND_LIB", LIB_PATH)
     if not os.path.exists(path):
         raise ImportError(
-            f"libgpurand.so not found at {path}; build it with `python -m eigenrand_gb300.build` "
+            f"libgpurand.so not found at {path}; build it with `python eigenrand_gb300/build.py` "
             "(the sampling library has no CPU fallback)")
     lib = ctypes.CDLL(path)
     vp, sz, i32, u64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_uint64
@@ -81,6 +81,7 @@ def load(path=None):
         "gr_gen_destroy": (i32, [vp]),
         "gr_generate": (i32, [vp, vp, vp, sz, vp]),
         "gr_sample": (i32, [vp, ctypes.POINTER(DistDesc), vp, sz, vp]),
+        "gr_raw_u64_noalloc": (i32, [vp, vp, sz, vp]),
         "gr_last_error": (ctypes.c_char_p, []),
         "gr_version": (ctypes.c_char_p, []),
     }

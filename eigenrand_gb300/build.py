@@ -1,7 +1,7 @@
 """Build libgpurand.so (the C-ABI sampling library) in-tree for sm_103a.
 
-    python -m eigenrand_gb300.build          # incremental
-    python -m eigenrand_gb300.build --force  # rebuild everything
+    python eigenrand_gb300/build.py          # incremental
+    python eigenrand_gb300/build.py --force  # rebuild everything
 
 Translation units are compiled in parallel with nvcc and linked into
 eigenrand_gb300/_build/libgpurand.so.  The kernels are compiled with
@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libgpurand.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-SOURCES = ["gr_kernels.cu", "gr_api.cu", "gr_poly.cpp"]
+SOURCES = ["gr_kernels.cu", "gr_api.cu", "gr_noalloc.cu", "gr_poly.cpp"]
 HEADERS = ["gr_internal.h", "gr_kernels.cuh", "gr_math.cuh", "gr_poly.h"]
 
 

@@ -102,6 +102,11 @@ struct gr_gen {
   int gst_K = 0;
 };
 
+namespace gr {
+EngState* engine_state_ptr(gr_engine* e) { return e ? e->st : nullptr; }
+gr_status set_last_error(gr_status s, const std::string& msg) { return fail(s, msg); }
+}  // namespace gr
+
 extern "C" {
 
 const char* gr_last_error(void) { return g_err.c_str(); }

@@ -5,6 +5,9 @@
 #include <cstdint>
 
 #include "gr_internal.h"
+#include "../../include/gpurand.h"
+
+#include <string>
 
 namespace gr {
 
@@ -52,5 +55,9 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
 int kind_granule(int kind, int dtype);
 int kind_packets_per_unit(int kind, int dtype);
 bool kind_is_direct(int kind, int dtype, const DistParams& d);
+
+// Host-side helpers shared by the C ABI translation units (gr_api.cu).
+EngState* engine_state_ptr(gr_engine* e);
+gr_status set_last_error(gr_status s, const std::string& msg);
 
 }  // namespace gr

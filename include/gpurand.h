@@ -124,6 +124,21 @@ gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_
 const char* gr_last_error(void);
 const char* gr_version(void);
 
+/* ---- allocation-free raw stream ------------------------------------------
+ * No counterpart in the reference (EigenRand runs on the host and never
+ * allocates device memory).  Same output and engine advance as gr_raw_u64,
+ * for callers that must not allocate device memory on their sampling path —
+ * for example a plugin whose host framework owns all device memory, or a
+ * thread with a real-time budget.  The engine is created once at set-up
+ * (streams = 1 only); the call then allocates nothing: its jump-ahead scratch
+ * is a file-scope __device__ array of about 1 MiB that every GPU loading the
+ * library keeps until process exit.  n <= GR_NOALLOC_MAX_DRAWS, else
+ * GR_ERR_INVALID.  Calls share that array, so calls that overlap on the GPU
+ * race and must be serialised by the caller.  The first call on a device
+ * performs one-time set-up; make it before any stream capture. */
+#define GR_NOALLOC_MAX_DRAWS 4294967296ull
+gr_status gr_raw_u64_noalloc(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
