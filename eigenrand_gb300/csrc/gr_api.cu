@@ -13,6 +13,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/gpurand.h"
@@ -42,28 +43,29 @@ gr_status cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
   } while (0)
 
-// Jump polynomials x^(s*J) mod P for s = 1..count, per device, cached by J.
+// Jump polynomials x^(s*J - delta) mod P for s = 1..count, per device,
+// cached by (J, delta).
 struct JumpCache {
   std::mutex mu;
   struct Entry {
     uint64_t* dev = nullptr;
     int count = 0;
   };
-  std::map<std::pair<int, int64_t>, Entry> tab;
+  std::map<std::tuple<int, int64_t, int>, Entry> tab;
 };
 JumpCache& jump_cache() {
   static JumpCache c;
   return c;
 }
 
-gr_status get_jump_polys(int dev, int64_t J, int need, const uint64_t** out) {
+gr_status get_jump_polys(int dev, int64_t J, int delta, int need, const uint64_t** out) {
   JumpCache& jc = jump_cache();
   std::lock_guard<std::mutex> lk(jc.mu);
-  auto& ent = jc.tab[{dev, J}];
+  auto& ent = jc.tab[std::make_tuple(dev, J, delta)];
   if (ent.count < need) {
     const int cnt = std::max(need, 2 * ent.count);
     std::vector<uint64_t> exps(cnt);
-    for (int s = 0; s < cnt; ++s) exps[s] = (uint64_t)(s + 1) * (uint64_t)J;
+    for (int s = 0; s < cnt; ++s) exps[s] = (uint64_t)(s + 1) * (uint64_t)J - (uint64_t)delta;
     if (charpoly_terms().size() != 284) return fail(GR_ERR_CUDA, "MT19937-64 characteristic polynomial recovery failed");
     std::vector<Poly> polys;
     pow_x_mod_many(exps, polys);
@@ -234,12 +236,34 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       p.da = 1.0 / a;
       p.db = b;
       break;
-    case GR_GAMMA:
+    case GR_CHI_SQUARED:  // ChiSquaredGen(n) = GammaGen(n * 0.5, 2) in the scalar type
+    case GR_GAMMA: {
+      const bool chi = d.kind == GR_CHI_SQUARED;
+      const float af = chi ? (float)a * 0.5f : (float)a;
+      const double ad = chi ? a * 0.5 : a;
+      const double bb = chi ? 2.0 : b;
+      p.kind = GR_GAMMA;
+      p.fa = af;
+      p.fb = (float)bb;
+      p.da = ad;
+      p.db = bb;
+      p.ia = f ? (af == 1.0f) : (ad == 1.0);
+      // integer alpha < 20: product of alpha uniforms (NormalExp.h:577-587)
+      const int cnt = f ? (int)af : (int)ad;
+      const bool integral = f ? ((float)cnt == af) : ((double)cnt == ad);
+      p.ib = (integral && cnt < 20 && cnt >= 2) ? cnt : 0;
+      break;
+    }
+    case GR_STUDENT_T:  // n = a; pset1(-2 / n) in the scalar type
       p.fa = (float)a;
-      p.fb = (float)b;
+      p.fc = -2 / (float)a;
       p.da = a;
-      p.db = b;
-      p.ia = f ? ((float)a == 1.0f) : (a == 1.0);
+      p.dc = -2 / a;
+      break;
+    case GR_BINOMIAL:  // BinomialGen(trials, p): a = p
+      p.fa = (float)a;
+      p.da = a;
+      p.ia = d.trials;
       break;
     default:
       return fail(GR_ERR_UNSUPPORTED, "distribution kind not implemented yet");
@@ -334,6 +358,43 @@ void plan_segments(const gr_engine* e, int64_t packets_max, int ppu, int& S, int
   J = j;
 }
 
+// How a kind's draws map onto the packet stream.
+enum class Family { Direct, Staged, Unsupported };
+
+Family family_of(const DistParams& dp) {
+  if (kind_is_direct(dp.kind, dp.dtype, dp)) return Family::Direct;
+  if (dp.kind == GR_GAMMA && dp.ib >= 2 && dp.dtype != GR_I32) return Family::Staged;
+  if (dp.kind == GR_STUDENT_T && dp.dtype != GR_I32) return Family::Staged;
+  if (dp.kind == GR_BINOMIAL && dp.dtype == GR_I32 && dp.ia < 25) return Family::Staged;
+  return Family::Unsupported;
+}
+
+// Sets up prefix / jump windows for an S-segment call; exponents s*J - delta.
+gr_status prepare_segments(gr_engine* e, Plan& p, int S, int64_t J, int delta, cudaStream_t stream) {
+  p.S = S;
+  p.J = J;
+  if (S <= 1) return GR_OK;
+  if (!e->prefix) {
+    GR_CUDA(cudaMalloc(&e->prefix, sizeof(uint64_t) * (size_t)kPrefixLen * kLanes * (size_t)e->K));
+    GR_CUDA(cudaMalloc(&e->snap, sizeof(CallSnap) * (size_t)e->K));
+  }
+  const size_t need = (size_t)e->K * (S - 1) * kLanes * kN;
+  if (e->segwin_words < need) {
+    cudaFree(e->segwin);
+    e->segwin = nullptr;
+    GR_CUDA(cudaMalloc(&e->segwin, sizeof(uint64_t) * need));
+    e->segwin_words = need;
+  }
+  const uint64_t* polys = nullptr;
+  gr_status st = get_jump_polys(e->device, J, delta, S - 1, &polys);
+  if (st != GR_OK) return st;
+  GR_CUDA(launch_prefix(e->st, p.gen, e->K, e->prefix, e->snap, stream));
+  GR_CUDA(launch_jump(e->prefix, polys, e->K, S, e->segwin, stream));
+  p.segwin = e->segwin;
+  p.prefix = e->prefix;
+  return GR_OK;
+}
+
 gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream) {
   const int gran = kind_granule(dp.kind, dp.dtype);
   if (n % (size_t)gran) {
@@ -342,7 +403,13 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
   }
   if (n == 0) return GR_OK;
   if (!out) return fail(GR_ERR_INVALID, "output is NULL");
-  if (!kind_is_direct(dp.kind, dp.dtype, dp)) return fail(GR_ERR_UNSUPPORTED, "this parameter set is not implemented yet");
+  const Family fam = family_of(dp);
+  if (fam == Family::Unsupported) return fail(GR_ERR_UNSUPPORTED, "this parameter set is not implemented yet");
+  if (dp.kind == GR_BINOMIAL && dp.ia <= 0) {
+    // BinomialGen with 0 trials draws nothing and returns 0 (Discrete.h:1000-1009)
+    GR_CUDA(cudaMemsetAsync(out, 0, n * sizeof(int32_t), stream));
+    return GR_OK;
+  }
   const int64_t granules = (int64_t)(n / (size_t)gran);
   Plan p{};
   p.eng = e->st;
@@ -352,40 +419,49 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
   p.gran_per_k = granules / e->K;
   p.gran_rem = granules % e->K;
   p.out = out;
-  // packets per slice, upper bound (caches can only reduce it)
   const int64_t nk_max = (p.gran_per_k + (p.gran_rem ? 1 : 0)) * gran;
-  int opp = 8;
-  if (dp.kind == kRawKind || (dp.dtype == GR_F64 && dp.kind != GR_BALANCED && dp.kind != GR_BALANCED2)) opp = 4;
-  const int ppu = kind_packets_per_unit(dp.kind, dp.dtype);
-  int64_t packets_max = (nk_max + opp - 1) / opp;
-  if (ppu == 2) packets_max += packets_max & 1;
-  int S;
-  int64_t J;
-  plan_segments(e, packets_max, ppu, S, J);
-  p.S = S;
-  p.J = J;
-  if (S > 1) {
-    if (!e->prefix) {
-      GR_CUDA(cudaMalloc(&e->prefix, sizeof(uint64_t) * (size_t)kPrefixLen * kLanes * (size_t)e->K));
-      GR_CUDA(cudaMalloc(&e->snap, sizeof(CallSnap) * (size_t)e->K));
-    }
-    const size_t need = (size_t)e->K * (S - 1) * kLanes * kN;
-    if (e->segwin_words < need) {
-      cudaFree(e->segwin);
-      e->segwin = nullptr;
-      GR_CUDA(cudaMalloc(&e->segwin, sizeof(uint64_t) * need));
-      e->segwin_words = need;
-    }
-    const uint64_t* polys = nullptr;
-    gr_status st = get_jump_polys(e->device, J, S - 1, &polys);
+
+  if (fam == Family::Direct) {
+    // packets per slice, upper bound (caches can only reduce it)
+    int opp = 8;
+    if (dp.kind == kRawKind || (dp.dtype == GR_F64 && dp.kind != GR_BALANCED && dp.kind != GR_BALANCED2)) opp = 4;
+    const int ppu = kind_packets_per_unit(dp.kind, dp.dtype);
+    int64_t packets_max = (nk_max + opp - 1) / opp;
+    if (ppu == 2) packets_max += packets_max & 1;
+    int S;
+    int64_t J;
+    plan_segments(e, packets_max, ppu, S, J);
+    gr_status st = prepare_segments(e, p, S, J, 0, stream);
     if (st != GR_OK) return st;
-    GR_CUDA(launch_prefix(e->st, p.gen, e->K, e->prefix, e->snap, stream));
-    GR_CUDA(launch_jump(e->prefix, polys, e->K, S, e->segwin, stream));
-    p.segwin = e->segwin;
-    p.prefix = e->prefix;
+    cudaError_t err = launch_direct(p, dp, e->snap, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "sampling kernel");
+    return GR_OK;
   }
-  cudaError_t err = launch_direct(p, dp, e->snap, stream);
-  if (err != cudaSuccess) return cuda_fail(err, "sampling kernel");
+
+  // staged: U packets (full kinds) or U half packets (int32) per unit of P outputs
+  const int P = (dp.dtype == GR_F32) ? 8 : 4;
+  const bool half = dp.dtype == GR_I32;
+  int U = 0;
+  if (dp.kind == GR_GAMMA) U = dp.ib;
+  if (dp.kind == GR_STUDENT_T) U = 2;
+  if (dp.kind == GR_BINOMIAL) U = dp.ia;
+  const int64_t units = nk_max / P;
+  const int64_t packets_max = half ? (units * U + 1) / 2 + 1 : units * U;
+  int S = 1;
+  int64_t Us = std::max<int64_t>(units, 1), J = packets_max;
+  if (e->K < 16 && packets_max >= ((int64_t)1 << 17)) {
+    const int64_t target = std::max<int64_t>(1, 128 / e->K);
+    int64_t us = 2;
+    while (us * target < units || (half ? us * U / 2 : us * U) < ((int64_t)1 << 14)) us <<= 1;
+    Us = us;
+    J = half ? us * U / 2 : us * U;
+    S = (int)((units + us - 1) / us);
+  }
+  const int delta = half ? 1 : 0;
+  gr_status st = prepare_segments(e, p, S, J, delta, stream);
+  if (st != GR_OK) return st;
+  cudaError_t err = launch_staged(p, dp, e->snap, U, Us, delta, stream);
+  if (err != cudaSuccess) return cuda_fail(err, "staged sampling kernel");
   return GR_OK;
 }
 

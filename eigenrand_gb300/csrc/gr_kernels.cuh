@@ -50,6 +50,12 @@ cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, in
 // packet aligned.  Returns cudaErrorNotSupported for other kinds.
 cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s);
 
+// Multi-packet fixed units (gr_samplers.cu): U packets (or half packets) per
+// unit of P outputs, Us units per jump segment; segment s starts at packet
+// s*J - delta.
+cudaError_t launch_staged(const Plan& p, const DistParams& d, const CallSnap* snap, int U, int64_t Us, int delta,
+                          cudaStream_t s);
+
 // Outputs per granule: the smallest output count a call (or a stream slice)
 // may have for the kind.  Packets per unit: 2 for the Box-Muller kinds.
 int kind_granule(int kind, int dtype);
