@@ -252,6 +252,41 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       const int cnt = f ? (int)af : (int)ad;
       const bool integral = f ? ((float)cnt == af) : ((double)cnt == ad);
       p.ib = (integral && cnt < 20 && cnt >= 2) ? cnt : 0;
+      // rejection branches (NormalExp.h:453-458, 535-604): 1/alpha, alpha-1,
+      // px = e/(alpha+e), sqrt(2 alpha - 1), all in the scalar type
+      p.fc = 1 / af;
+      p.fd = af - 1;
+      p.fe = (float)(2.7182818284590452 / (af + 2.7182818284590452));
+      p.ff = std::sqrt(2 * af - 1);
+      p.dc = 1 / ad;
+      p.dd = ad - 1;
+      p.de = 2.7182818284590452 / (ad + 2.7182818284590452);
+      p.df = std::sqrt(2 * ad - 1);
+      p.ic = f ? (af < 1.0f) : (ad < 1.0);  // GS branch
+      break;
+    }
+    case GR_BETA: {  // BetaGen(a, b), NormalExp.h:949-976
+      const float af = (float)a, bf = (float)b;
+      p.fa = af;
+      p.fb = bf;
+      p.fc = 1 / af;
+      p.fd = 1 / bf;
+      p.da = a;
+      p.db = b;
+      p.dc = 1 / a;
+      p.dd = 1 / b;
+      p.ic = f ? (af < 1 && bf < 1) : (a < 1 && b < 1);
+      break;
+    }
+    case GR_POISSON: {  // PoissonGen(mean), Discrete.h:806-812 (double), packet constants in float
+      const double mean = a;
+      p.da = mean;
+      p.fa = (float)std::sqrt(2 * mean);
+      p.fb = (float)mean;
+      p.fc = (float)std::log(mean);
+      p.fd = (float)(mean * std::log(mean) - std::lgamma(mean + 1));
+      p.fe = (float)std::exp(-mean);
+      p.ic = mean < 12;
       break;
     }
     case GR_STUDENT_T:  // n = a; pset1(-2 / n) in the scalar type
@@ -260,11 +295,28 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       p.da = a;
       p.dc = -2 / a;
       break;
-    case GR_BINOMIAL:  // BinomialGen(trials, p): a = p
-      p.fa = (float)a;
-      p.da = a;
+    case GR_BINOMIAL: {  // BinomialGen(trials, p): a = p, Discrete.h:926-938
+      const double pp = a, small_p = std::min(pp, 1 - pp), mean = d.trials * small_p;
+      p.da = pp;
       p.ia = d.trials;
+      p.db = mean;
+      p.ib = pp != small_p;  // return trials - res
+      if (d.trials < 25) {
+        p.fa = (float)pp;
+      } else if (mean < 1.0) {
+        p.fe = (float)std::exp(-mean);
+        p.ic = 1;  // poisson loop
+      } else {
+        const double sqrt_v = std::sqrt(2 * mean * (1 - small_p));
+        p.fa = (float)sqrt_v;
+        p.fb = (float)mean;
+        p.fc = (float)std::log(small_p);
+        p.fd = (float)std::log(1 - small_p);
+        p.fg = (float)std::lgamma(d.trials + 1);
+        p.fh = (float)d.trials;
+      }
       break;
+    }
     default:
       return fail(GR_ERR_UNSUPPORTED, "distribution kind not implemented yet");
   }
@@ -359,13 +411,26 @@ void plan_segments(const gr_engine* e, int64_t packets_max, int ppu, int& S, int
 }
 
 // How a kind's draws map onto the packet stream.
-enum class Family { Direct, Staged, Unsupported };
+enum class Family { Direct, Staged, Reject, Unsupported };
+
+// Rejection family code for launch_reject, or -1.
+int reject_code(const DistParams& dp) {
+  if (dp.dtype == GR_I32) {
+    if (dp.kind == GR_POISSON && !dp.ic) return 3;
+    if (dp.kind == GR_BINOMIAL && dp.ia >= 25 && !dp.ic) return 4;
+    return -1;
+  }
+  if (dp.kind == GR_GAMMA && dp.ia == 0 && dp.ib == 0) return dp.ic ? 0 : 1;
+  if (dp.kind == GR_BETA && dp.ic) return 2;
+  return -1;
+}
 
 Family family_of(const DistParams& dp) {
   if (kind_is_direct(dp.kind, dp.dtype, dp)) return Family::Direct;
   if (dp.kind == GR_GAMMA && dp.ib >= 2 && dp.dtype != GR_I32) return Family::Staged;
   if (dp.kind == GR_STUDENT_T && dp.dtype != GR_I32) return Family::Staged;
   if (dp.kind == GR_BINOMIAL && dp.dtype == GR_I32 && dp.ia < 25) return Family::Staged;
+  if (reject_code(dp) >= 0) return Family::Reject;
   return Family::Unsupported;
 }
 
@@ -435,6 +500,18 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
     if (st != GR_OK) return st;
     cudaError_t err = launch_direct(p, dp, e->snap, stream);
     if (err != cudaSuccess) return cuda_fail(err, "sampling kernel");
+    return GR_OK;
+  }
+
+  if (fam == Family::Reject) {
+    if (!p.gen) return fail(GR_ERR_INVALID, "rejection samplers need a generator state");
+    const int P = (dp.dtype == GR_F32) ? 8 : 4;
+    const int rk = reject_code(dp);
+    const int64_t wt = rk == 0 ? 24 : (rk >= 3 ? 8 : 16);  // words per trial
+    const int64_t npk = nk_max / P;
+    const int64_t max_blocks = ((16 * npk + 4096) * wt) / (kN * 8) + 64;
+    cudaError_t err = launch_reject(p, dp, rk, max_blocks, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "rejection sampling kernel");
     return GR_OK;
   }
 

@@ -18,7 +18,7 @@ struct DistParams {
   int32_t dtype;  // gr_dtype
   float fa, fb, fc, fd, fe, ff, fg, fh;   // float-precision constants
   double da, db, dc, dd, de, df, dg, dh;  // double-precision constants
-  int32_t ia, ib;                          // integer constants (trials, counts)
+  int32_t ia, ib, ic;                      // integer constants (trials, counts, flags)
   uint32_t bitmask;                        // alias table mask
   int32_t ncdf;                            // CDF entries (discrete < 16 weights)
   const int32_t* prob;                     // alias table / cdf (device)
@@ -55,6 +55,11 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
 // s*J - delta.
 cudaError_t launch_staged(const Plan& p, const DistParams& d, const CallSnap* snap, int U, int64_t Us, int delta,
                           cudaStream_t s);
+
+// Rejection samplers resolved with CompressMask semantics (gr_samplers.cu);
+// one CTA per stream.  rk: 0 gamma alpha<1 (GS), 1 gamma tan proposal,
+// 2 beta with a,b < 1, 3 poisson mean >= 12, 4 binomial tan proposal.
+cudaError_t launch_reject(const Plan& p, const DistParams& d, int rk, int64_t max_blocks, cudaStream_t s);
 
 // Outputs per granule: the smallest output count a call (or a stream slice)
 // may have for the kind.  Packets per unit: 2 for the Box-Muller kinds.

@@ -200,3 +200,409 @@ cudaError_t launch_staged(const Plan& p, const DistParams& d, const CallSnap* sn
 }
 
 }  // namespace gr
+
+namespace gr {
+
+// ===========================================================================
+// k_reject: rejection samplers driven by CompressMask::compress_append
+// (EigenRand/arch/AVX/PacketFilter.h:147-184).  Each trial consumes a fixed
+// run of Wt words and yields P candidates with an accept mask.  The
+// reference's packetOp loop is an automaton over trials: a fully accepted
+// trial is returned as is; otherwise its accepted lanes are appended, in lane
+// order, to a FIFO carried in the generator, and a packet is returned once
+// the FIFO holds P lanes.  With  NF_t = fully accepted trials before t  and
+// A_t = carried lanes + lanes appended before t,  trial t's emission (if any)
+// is packet  E + NF_t + floor(A_t / P),  so a batch of trials is resolved with
+// one block-wide prefix sum.  The call stops at the trial that completes its
+// last output packet; later trials are not consumed.
+// ===========================================================================
+namespace {
+
+enum RejKind { RK_GAMMA_GS = 0, RK_GAMMA_TAN = 1, RK_BETA_SMALL = 2, RK_POISSON = 3, RK_BINOMIAL = 4 };
+
+constexpr int kRejThreads = 160;
+constexpr int kMaxTrials = 320;  // trials resolved per block of packets (<= 2496 / 8 + 1)
+constexpr int kMaxCand = 1280;   // candidate lanes per block: <= 2496 words / Wt * P + P
+constexpr size_t kRejDynSmem = (size_t)(4 * kLanes * kN + kMaxCand) * sizeof(uint64_t);
+
+// inclusive block scan of one uint32 per thread (kRejThreads threads)
+__device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t* warp_tot) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t x = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += x;
+  }
+  if (lane == 31) warp_tot[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int i = 0; i < kRejThreads / 32; ++i) {
+      uint32_t t = warp_tot[i];
+      warp_tot[i] = acc;
+      acc += t;
+    }
+  }
+  __syncthreads();
+  return v + warp_tot[w];
+}
+
+}  // namespace
+
+template <int RK, int DT>  // DT: SD_F32 (P=8), SD_F64 (P=4), SD_I32H (P=4, float internals)
+__global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, int64_t max_blocks) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  constexpr bool kWide = DT == SD_F64;  // candidates are 64-bit
+  constexpr int Wt = (RK == RK_GAMMA_GS) ? 3 * 8 : (RK == RK_POISSON || RK == RK_BINOMIAL) ? 8 : 2 * 8;
+  extern __shared__ __align__(16) uint64_t rej_dyn[];
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(rej_dyn);
+  uint64_t(*tp)[kN][kLanes] = reinterpret_cast<uint64_t(*)[kN][kLanes]>(rej_dyn + 2 * kLanes * kN);
+  uint64_t* cand = rej_dyn + 4 * kLanes * kN;  // candidate bits per (trial, lane), kMaxCand
+  __shared__ uint32_t tmask[kMaxTrials];
+  __shared__ uint32_t tscan[kMaxTrials];      // exclusive: (fulls << 16) | lanes appended
+  __shared__ uint64_t fifo[2][16];            // carried lanes (ping-pong)
+  __shared__ int64_t emit_of_q[kMaxTrials + 2];
+  __shared__ uint32_t warp_tot[kRejThreads / 32];
+  __shared__ int s_tstar;
+  __shared__ int s_done;
+
+  const int k = blockIdx.x;
+  const int tid = threadIdx.x;
+  EngState* st = p.eng + k;
+  GenSlot* gs = &p.gen[k].s[0];
+
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  const int64_t Npk = n / P;  // packets of output to produce
+
+  constexpr bool kHalf = DT == SD_I32H;
+  const int c0w = (kHalf && st->half_valid) ? 4 : 0;
+  uint32_t cw[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) cw[q] = kHalf ? st->half_cache[q] : 0u;
+  int rcnt = gs->rest_cnt;  // carried lanes
+  if (tid < 16) fifo[0][tid] = kWide ? ((uint64_t)gs->rest[2 * (tid & 7)] | ((uint64_t)gs->rest[2 * (tid & 7) + 1] << 32))
+                                     : (uint64_t)gs->rest[tid];
+  load_window(raw[0], &st->win[0][0], kN);
+  if (tid == 0) s_done = 0;
+  __syncthreads();
+
+  auto word = [&](int64_t wq) -> uint32_t {
+    if (wq < c0w) return cw[wq];
+    const int64_t w = wq - c0w;
+    const int64_t rel = w >> 3;
+    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
+  };
+  // int32 result: BinomialGen returns trials - res when p > 1/2 (Discrete.h:1051)
+  auto iout = [&](uint32_t fbits) -> int32_t {
+    const int32_t r = (int32_t)u2f(fbits);
+    return (RK == RK_BINOMIAL && d.ib) ? (int32_t)d.fh - r : r;
+  };
+  auto rval = [&](int64_t r) -> uint64_t {  // u64 lane value (full-packet f64 kinds)
+    const int64_t rel = r >> 2;
+    return tp[(rel / kN) & 1][rel % kN][r & 3];
+  };
+
+  int64_t E = 0;        // output packets emitted so far
+  int64_t t_next = 0;   // next trial
+  int cur = 0, fsl = 0;
+  int64_t nb = 0;
+  int64_t end_word = -1;  // words consumed (cache-inclusive), set when done
+  for (; nb < max_blocks; ++nb) {
+    const int slot = (int)(nb & 1);
+    mt_block(raw[cur], raw[cur ^ 1], [&](int i, const uint64_t* pk) {
+#pragma unroll
+      for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
+    });
+    cur ^= 1;
+    const int64_t avail_words = (nb + 1) * kN * 8 + c0w;
+    int64_t t_end = avail_words / Wt;  // trials whose words all exist
+    int B = (int)min((int64_t)kMaxTrials, t_end - t_next);
+    if (B <= 0) continue;
+    // ---- candidates and accept masks
+    for (int base = 0; base < B * P; base += kRejThreads) {
+      const int e = base + tid;
+      const bool valid = e < B * P;
+      const int tl = e / P, j = e % P;
+      const int64_t t = t_next + tl;
+      bool acc = false;
+      uint64_t cbits = 0;
+      if (valid) {
+        const int64_t w0 = t * Wt;
+        if (DT == SD_F32) {
+          if (RK == RK_GAMMA_GS) {
+            const float ux = ur_f(word(w0 + j));
+            const float vx = ur_f(word(w0 + 8 + j)) + 1.1920928955078125e-07f / 8;
+            const float ux2 = ur_f(word(w0 + 16 + j));
+            const float lv = logf_(vx);
+            const float x1 = expf_(d.fc * lv);  // (1/alpha) * log(vx)
+            const float q1 = expf_(-x1);
+            const float x2 = 1.0f - lv;
+            const float q2 = expf_(logf_(x2) * d.fd);  // alpha - 1
+            const bool c = ux < d.fe;                 // px
+            const float xx = c ? x1 : x2, qx = c ? q1 : q2;
+            cbits = f2u(d.fb * xx);
+            acc = ux2 < qx;
+          } else if (RK == RK_GAMMA_TAN) {
+            const float u = ur_f(word(w0 + j));
+            const float ux = ur_f(word(w0 + 8 + j));
+            float ys, yc;
+            sincosf_((float)3.1415926535897932 * u, ys, yc);
+            const float yx = ys / yc;
+            const float xx = d.ff * yx + d.fd;  // sqrt * yx + (alpha - 1)
+            const bool c = 0.0f < xx;
+            const float ub = (yx * yx + 1.0f) * expf_(d.fd * logf_(xx / d.fd) - yx * d.ff);
+            acc = c && (ux <= ub);
+            cbits = f2u(d.fb * xx);
+          } else if (RK == RK_BETA_SMALL) {
+            const float u1 = ur_f(word(w0 + j));
+            const float u2 = ur_f(word(w0 + 8 + j));
+            const float p1 = expf_(logf_(u1) * d.fc);  // 1/a
+            const float p2 = expf_(logf_(u2) * d.fd);  // 1/b
+            const float x = p1 + p2;
+            cbits = f2u(p1 / x);
+            acc = x <= 1.0f;
+          }
+        } else if (DT == SD_F64) {
+          const int64_t r0 = (t * Wt / 8) * 4 + j;  // u64 lane index of the trial's first packet
+          if (RK == RK_GAMMA_GS) {
+            const double ux = ur_d(rval(r0));
+            const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
+            const double ux2 = ur_d(rval(r0 + 8));
+            const double lv = log_(vx);
+            const double x1 = exp_(d.dc * lv);
+            const double q1 = exp_(-x1);
+            const double x2 = 1.0 - lv;
+            const double q2 = exp_(log_(x2) * d.dd);
+            const bool c = ux < d.de;
+            const double xx = c ? x1 : x2, qx = c ? q1 : q2;
+            cbits = d2u(d.db * xx);
+            acc = ux2 < qx;
+          } else if (RK == RK_GAMMA_TAN) {
+            const double u = ur_d(rval(r0));
+            const double ux = ur_d(rval(r0 + 4));
+            double ys, yc;
+            sincos_(3.1415926535897932 * u, ys, yc);
+            const double yx = ys / yc;
+            const double xx = d.df * yx + d.dd;
+            const bool c = 0.0 < xx;
+            const double ub = (yx * yx + 1.0) * exp_(d.dd * log_(xx / d.dd) - yx * d.df);
+            acc = c && (ux <= ub);
+            cbits = d2u(d.db * xx);
+          } else if (RK == RK_BETA_SMALL) {
+            const double u1 = ur_d(rval(r0));
+            const double u2 = ur_d(rval(r0 + 4));
+            const double p1 = exp_(log_(u1) * d.dc);
+            const double p2 = exp_(log_(u2) * d.dd);
+            const double x = p1 + p2;
+            cbits = d2u(p1 / x);
+            acc = x <= 1.0;
+          }
+        } else {  // int32 kinds with Packet4f internals over half packets
+          const float u = ur_f(word(w0 + j));
+          const float u2 = ur_f(word(w0 + 4 + j));
+          float s, c;
+          sincosf_((float)3.1415926535897932 * u, s, c);
+          const float yx = s / c;
+          if (RK == RK_POISSON) {
+            const float fres = truncf(d.fa * yx + d.fb);  // sqrt(2 mean) * yx + mean
+            const float p1 = (yx * yx + 1.0f) * 0.9f;
+            const float p2 = expf_((fres * d.fc - lgamma_approxf_(fres + 1.0f)) - d.fd);
+            acc = (0.0f <= fres) && (u2 <= p1 * p2);
+            cbits = f2u(fres);
+          } else {  // binomial, BinomialGen::packetOp tan branch (Discrete.h:1014-1046)
+            const float fres = truncf(d.fa * yx + d.fb);  // sqrt_v * ys + mean
+            const float p1 = ((float)1.2 * d.fa) * (1.0f + yx * yx);
+            float tt = (d.fg - lgamma_approxf_(fres + 1.0f)) - lgamma_approxf_((d.fh + 1.0f) - fres);
+            tt = tt + fres * d.fc;
+            tt = tt + (d.fh - fres) * d.fd;
+            const float p2 = expf_(tt);
+            acc = (0.0f <= fres) && (fres <= d.fh) && (u2 <= p1 * p2);
+            cbits = f2u(fres);
+          }
+        }
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, acc);
+      if (valid) {
+        cand[tl * P + j] = cbits;
+        if (j == 0) tmask[tl] = (bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1);
+      }
+    }
+    __syncthreads();
+    // ---- prefix sums over trials: (fulls << 16) | appended lanes
+    uint32_t v0 = 0, v1 = 0;
+    const int ta = 2 * tid, tb = 2 * tid + 1;
+    if (ta < B) {
+      const int c = __popc(tmask[ta]);
+      v0 = (c == P) ? (1u << 16) : (uint32_t)c;
+    }
+    if (tb < B) {
+      const int c = __popc(tmask[tb]);
+      v1 = (c == P) ? (1u << 16) : (uint32_t)c;
+    }
+    const uint32_t incl = block_incl_scan(v0 + v1, warp_tot);
+    if (ta < B) tscan[ta] = incl - v0 - v1;
+    if (tb < B) tscan[tb] = incl - v1;
+    if (tid == 0) s_tstar = -1;
+    __syncthreads();
+    // ---- emissions of this batch; find the trial completing packet Npk-1
+    for (int tl = tid; tl < B; tl += kRejThreads) {
+      const uint32_t m = tmask[tl];
+      const int c = __popc(m);
+      const int64_t nf = tscan[tl] >> 16;
+      const int64_t at = (int64_t)rcnt + (tscan[tl] & 0xffffu);
+      const bool full = c == P;
+      const bool cross = !full && ((at + c) / P > at / P);
+      const int64_t eidx = E + nf + at / P;
+      if (cross) emit_of_q[at / P] = eidx;
+      if ((full || cross) && eidx == Npk - 1) s_tstar = tl;
+    }
+    __syncthreads();
+    const int tstar = s_tstar;
+    const int Bu = tstar >= 0 ? tstar + 1 : B;  // trials consumed in this batch
+    // FIFO level after the consumed trials
+    int64_t a_end;
+    int64_t nf_end;
+    {
+      const int tl = Bu - 1;
+      const int c = __popc(tmask[tl]);
+      nf_end = (tscan[tl] >> 16) + (c == P ? 1 : 0);
+      a_end = (int64_t)rcnt + (tscan[tl] & 0xffffu) + (c == P ? 0 : c);
+    }
+    const int64_t qe = a_end / P;  // FIFO packets emitted through the consumed trials
+    // ---- write outputs
+    for (int e = tid; e < Bu * P; e += kRejThreads) {
+      const int tl = e / P, j = e % P;
+      const uint32_t m = tmask[tl];
+      const int c = __popc(m);
+      const int64_t nf = tscan[tl] >> 16;
+      const int64_t at = (int64_t)rcnt + (tscan[tl] & 0xffffu);
+      uint64_t v = cand[tl * P + j];
+      if (c == P) {
+        const int64_t eidx = E + nf + at / P;
+        if (eidx < Npk) {
+          if (kWide) reinterpret_cast<uint64_t*>(p.out)[off + eidx * P + j] = v;
+          else if (DT == SD_I32H) reinterpret_cast<int32_t*>(p.out)[off + eidx * P + j] = iout((uint32_t)v);
+          else reinterpret_cast<uint32_t*>(p.out)[off + eidx * P + j] = (uint32_t)v;
+        }
+      } else if ((m >> j) & 1u) {
+        const int64_t f = at + __popc(m & ((1u << j) - 1));
+        const int64_t q = f / P;
+        if (q < qe) {
+          const int64_t eidx = emit_of_q[q];
+          if (eidx < Npk) {
+            if (kWide) reinterpret_cast<uint64_t*>(p.out)[off + eidx * P + f % P] = v;
+            else if (DT == SD_I32H) reinterpret_cast<int32_t*>(p.out)[off + eidx * P + f % P] = iout((uint32_t)v);
+            else reinterpret_cast<uint32_t*>(p.out)[off + eidx * P + f % P] = (uint32_t)v;
+          }
+        } else {
+          fifo[fsl ^ 1][f - qe * P] = v;
+        }
+      }
+    }
+    // carried lanes that were emitted in this batch's first FIFO packets
+    if (tid < rcnt) {
+      const int64_t f = tid;
+      if (f / P < qe) {
+        const int64_t eidx = emit_of_q[f / P];
+        const uint64_t v = fifo[fsl][tid];
+        if (eidx < Npk) {
+          if (kWide) reinterpret_cast<uint64_t*>(p.out)[off + eidx * P + f % P] = v;
+          else if (DT == SD_I32H) reinterpret_cast<int32_t*>(p.out)[off + eidx * P + f % P] = iout((uint32_t)v);
+          else reinterpret_cast<uint32_t*>(p.out)[off + eidx * P + f % P] = (uint32_t)v;
+        }
+      } else {
+        fifo[fsl ^ 1][f - qe * P] = fifo[fsl][tid];
+      }
+    }
+    __syncthreads();
+    E += nf_end + qe;
+    rcnt = (int)(a_end - qe * P);
+    fsl ^= 1;
+    t_next += Bu;
+    if (tstar >= 0) {
+      end_word = t_next * Wt;
+      break;
+    }
+  }
+
+  // ---- engine and generator state after the call
+  if (end_word < 0) {  // iteration cap: report, keep a consistent state
+    if (tid == 0) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+    end_word = t_next * Wt;
+  }
+  const int64_t w_pk = end_word - c0w;  // packet words consumed
+  const int64_t np = (w_pk + 7) / 8;    // packets consumed
+  if (np > 0) {
+    // the call ends inside the last generated block (block nb): its trials are
+    // the first whose words all exist, and every earlier trial was resolved
+    // one block earlier
+    const int rr = (int)(np - nb * kN);
+    store_window(st, raw[cur], raw[cur ^ 1], rr);
+  }
+  if (tid == 0) {
+    if (kHalf) {
+      if ((w_pk & 7) == 4) {  // ends mid-packet: upper half cached
+        const int64_t pl = np - 1;
+        const int sl = (int)((pl / kN) & 1);
+        const uint64_t a = tp[sl][pl % kN][2], b = tp[sl][pl % kN][3];
+        st->half_cache[0] = (uint32_t)a;
+        st->half_cache[1] = (uint32_t)(a >> 32);
+        st->half_cache[2] = (uint32_t)b;
+        st->half_cache[3] = (uint32_t)(b >> 32);
+        st->half_valid = 1;
+      } else {
+        st->half_valid = 0;
+      }
+    }
+    st->consumed += (uint64_t)max(np, (int64_t)0);
+    gs->rest_cnt = rcnt;
+  }
+  if (tid < 16) {
+    const uint64_t v = fifo[fsl][tid & 15];
+    if (kWide) {
+      if (tid < 8) {
+        gs->rest[2 * tid] = (uint32_t)fifo[fsl][tid];
+        gs->rest[2 * tid + 1] = (uint32_t)(fifo[fsl][tid] >> 32);
+      }
+    } else {
+      gs->rest[tid] = (uint32_t)v;
+    }
+  }
+}
+
+template <int RK, int DT>
+static cudaError_t run_reject(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_reject<RK, DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRejDynSmem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_reject<RK, DT><<<p.K, kRejThreads, kRejDynSmem, s>>>(p, d, max_blocks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reject(const Plan& p, const DistParams& d, int rk, int64_t max_blocks, cudaStream_t s) {
+  const int dt = d.dtype == GR_F32 ? SD_F32 : d.dtype == GR_F64 ? SD_F64 : SD_I32H;
+#define GR_RJ(R)                                                              \
+  if (rk == R) {                                                               \
+    if (dt == SD_F32) return run_reject<R, SD_F32>(p, d, max_blocks, s);       \
+    if (dt == SD_F64) return run_reject<R, SD_F64>(p, d, max_blocks, s);       \
+  }
+  GR_RJ(RK_GAMMA_GS)
+  GR_RJ(RK_GAMMA_TAN)
+  GR_RJ(RK_BETA_SMALL)
+#undef GR_RJ
+  if (rk == RK_POISSON && dt == SD_I32H) return run_reject<RK_POISSON, SD_I32H>(p, d, max_blocks, s);
+  if (rk == RK_BINOMIAL && dt == SD_I32H) return run_reject<RK_BINOMIAL, SD_I32H>(p, d, max_blocks, s);
+  return cudaErrorNotSupported;
+}
+
+}  // namespace gr

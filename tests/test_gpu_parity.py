@@ -116,12 +116,10 @@ def test_config1_uniform_and_normal_1024sq(er, oracle):
 
 # ---------------------------------------------------------------- golden fixtures
 def _gpu_has(c):
-    if c["kind"] in ("BETA", "POISSON"):
-        return False
-    if c["kind"] == "GAMMA":
-        return c["a"] == int(c["a"]) and c["a"] < 20
-    if c["kind"] == "BINOMIAL":
-        return c["trials"] < 25
+    if c["kind"] == "BETA":
+        return c["a"] < 1 and c["b"] < 1
+    if c["kind"] == "POISSON":
+        return c["a"] >= 12
     return True
 
 
@@ -201,6 +199,56 @@ def test_staged_on_many_streams(er, oracle):
     for k in range(K):
         ref = oracle.generate(oracle.Engine(1234 + 4 * k), oracle.Gen(), "GAMMA", per, np.float32, 5.0, 1.0)
         assert_bits_equal(x[k * per:(k + 1) * per], ref, f"gamma5 slice {k}")
+
+
+# ---------------------------------------------------------------- rejection samplers (CompressMask automaton)
+REJECT = [("GAMMA", 0.5, 1.0, 0), ("GAMMA", 0.2, 3.0, 0), ("GAMMA", 10.5, 1.0, 0), ("GAMMA", 25.0, 2.0, 0),
+          ("GAMMA", 1.7, 1.0, 0), ("CHI_SQUARED", 7.0, 0.0, 0), ("BETA", 0.5, 0.7, 0)]
+
+
+@pytest.mark.parametrize("kind,a,b,t", REJECT)
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+def test_rejection_kinds_bit_exact(er, oracle, kind, a, b, t, tdt):
+    """Consecutive calls with one generator: the carried lanes (rest) and the
+    engine position after the completing trial must match the reference."""
+    u = er.Vmt19937_64(31)
+    e = oracle.Engine(31)
+    g = er._Gen(tdt, a, b, kind=kind)
+    og = oracle.Gen()
+    P = 8 if tdt == torch.float32 else 4
+    for n in (P, 3 * P, 1 << 14, 5 * P, 1 << 16):
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, kind, n, npdt(tdt), a, b)
+        assert_bits_equal(got, ref, f"{kind}({a},{b}) {tdt} n={n}")
+    # the engine continues exactly: a raw draw after the rejection calls
+    assert_bits_equal(er.raw_u64(u, 64).cpu().numpy().view(np.uint64), e.raw(16), "engine after rejection")
+
+
+@pytest.mark.parametrize("kind,a,t", [("POISSON", 100.0, 0), ("POISSON", 12.0, 0), ("BINOMIAL", 0.75, 100),
+                                      ("BINOMIAL", 0.3, 1000), ("BINOMIAL", 0.1, 30)])
+def test_rejection_int_kinds_bit_exact(er, oracle, kind, a, t):
+    u = er.Vmt19937_64(32)
+    e = oracle.Engine(32)
+    g = er._Gen(torch.int32, a, 0.0, trials=t, kind=kind)
+    og = oracle.Gen()
+    for n in (4, 12, 1 << 14, 8, 1 << 16):
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, kind, n, np.int32, a, 0.0, t)
+        assert_bits_equal(got, ref, f"{kind}({a},{t}) n={n}")
+    # half-packet cache continues into the next half-packet kind
+    d, keep = er._desc("RANDBITS", torch.int32)
+    o = torch.empty(8, dtype=torch.int32, device="cuda")
+    er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), 8, er._stream_ptr()))
+    assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 8, np.int32), "randbits after")
+
+
+def test_rejection_on_many_streams(er, oracle):
+    K, per = 5, 8 * 512
+    u = er.Vmt19937_64(99, streams=K)
+    x = mem(er.gamma(K * per, 1, u, 0.5, 1.0))
+    for k in range(K):
+        ref = oracle.generate(oracle.Engine(99 + 4 * k), oracle.Gen(), "GAMMA", per, np.float32, 0.5, 1.0)
+        assert_bits_equal(x[k * per:(k + 1) * per], ref, f"gamma0.5 slice {k}")
 
 
 # ---------------------------------------------------------------- caches carried between calls
