@@ -411,7 +411,18 @@ void plan_segments(const gr_engine* e, int64_t packets_max, int ppu, int& S, int
 }
 
 // How a kind's draws map onto the packet stream.
-enum class Family { Direct, Staged, Reject, Unsupported };
+enum class Family { Direct, Staged, Reject, Walk, Unsupported };
+
+// GammaGen branch of a component with shape `alpha` in the generator's scalar
+// type: (branch << 8) | packets per draw or per trial (NormalExp.h:527-604).
+int gamma_branch(double alpha, bool f32) {
+  const double a = f32 ? (double)(float)alpha : alpha;
+  if (a < 1) return (2 << 8) | 3;  // GS rejection, 3 packets per trial
+  if (a == 1) return (0 << 8) | 1;  // exponential
+  const int cnt = (int)a;
+  if ((double)cnt == a && cnt < 20) return (1 << 8) | cnt;  // product of cnt uniforms
+  return (3 << 8) | 2;  // tan proposal, 2 packets per trial
+}
 
 // Rejection family code for launch_reject, or -1.
 int reject_code(const DistParams& dp) {
@@ -431,6 +442,9 @@ Family family_of(const DistParams& dp) {
   if (dp.kind == GR_STUDENT_T && dp.dtype != GR_I32) return Family::Staged;
   if (dp.kind == GR_BINOMIAL && dp.dtype == GR_I32 && dp.ia < 25) return Family::Staged;
   if (reject_code(dp) >= 0) return Family::Reject;
+  if (dp.dtype == GR_I32 && dp.kind == GR_POISSON && dp.ic) return Family::Walk;
+  if (dp.dtype == GR_I32 && dp.kind == GR_BINOMIAL && dp.ia >= 25 && dp.ic) return Family::Walk;
+  if (dp.dtype != GR_I32 && dp.kind == GR_BETA && !dp.ic) return Family::Walk;
   return Family::Unsupported;
 }
 
@@ -512,6 +526,32 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
     const int64_t max_blocks = ((16 * npk + 4096) * wt) / (kN * 8) + 64;
     cudaError_t err = launch_reject(p, dp, rk, max_blocks, stream);
     if (err != cudaSuccess) return cuda_fail(err, "rejection sampling kernel");
+    return GR_OK;
+  }
+
+  if (fam == Family::Walk) {
+    if (!p.gen) return fail(GR_ERR_INVALID, "these samplers need a generator state");
+    const int P = (dp.dtype == GR_F32) ? 8 : 4;
+    const int64_t npk = nk_max / P;
+    DistParams wd = dp;
+    int64_t max_blocks;
+    if (dp.dtype == GR_I32) {
+      // PoissonGen loop (mean < 12); BinomialGen with mean < 1 runs the same
+      // loop on its poisson member and returns trials - res when p > 1/2
+      wd.fe = dp.kind == GR_POISSON ? (float)std::exp(-dp.da) : dp.fe;
+      wd.ia = dp.kind == GR_BINOMIAL ? dp.ia : 0;
+      wd.ic = dp.kind == GR_BINOMIAL ? dp.ib : 0;
+      max_blocks = (npk * 64) / (2 * kN) + 64;
+    } else {
+      const bool f32 = dp.dtype == GR_F32;
+      wd.ia = gamma_branch(dp.da, f32);
+      wd.ib = gamma_branch(dp.db, f32);
+      wd.fa = (float)dp.da;
+      wd.fb = (float)dp.db;
+      max_blocks = (npk * 64) / kN + 64;
+    }
+    cudaError_t err = launch_walk(p, wd, max_blocks, stream);
+    if (err != cudaSuccess) return cuda_fail(err, "walk sampling kernel");
     return GR_OK;
   }
 

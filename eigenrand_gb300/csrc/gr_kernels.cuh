@@ -61,6 +61,11 @@ cudaError_t launch_staged(const Plan& p, const DistParams& d, const CallSnap* sn
 // 2 beta with a,b < 1, 3 poisson mean >= 12, 4 binomial tan proposal.
 cudaError_t launch_reject(const Plan& p, const DistParams& d, int rk, int64_t max_blocks, cudaStream_t s);
 
+// Data-dependent consumption (gr_samplers.cu), one CTA per stream: Poisson
+// mean < 12 (int32) and BetaGen with a or b >= 1 (f32/f64; d.ia / d.ib hold
+// (gamma branch << 8) | packets for the two GammaGens).
+cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s);
+
 // Outputs per granule: the smallest output count a call (or a stream slice)
 // may have for the kind.  Packets per unit: 2 for the Box-Muller kinds.
 int kind_granule(int kind, int dtype);

@@ -116,10 +116,6 @@ def test_config1_uniform_and_normal_1024sq(er, oracle):
 
 # ---------------------------------------------------------------- golden fixtures
 def _gpu_has(c):
-    if c["kind"] == "BETA":
-        return c["a"] < 1 and c["b"] < 1
-    if c["kind"] == "POISSON":
-        return c["a"] >= 12
     return True
 
 
@@ -240,6 +236,39 @@ def test_rejection_int_kinds_bit_exact(er, oracle, kind, a, t):
     o = torch.empty(8, dtype=torch.int32, device="cuda")
     er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), 8, er._stream_ptr()))
     assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 8, np.int32), "randbits after")
+
+
+# ---------------------------------------------------------------- data-dependent consumption (walk kernel)
+@pytest.mark.parametrize("kind,a,t", [("POISSON", 4.0, 0), ("POISSON", 0.3, 0), ("POISSON", 11.9, 0),
+                                      ("BINOMIAL", 0.01, 50), ("BINOMIAL", 0.995, 100)])
+def test_walk_int_kinds_bit_exact(er, oracle, kind, a, t):
+    u = er.Vmt19937_64(41)
+    e = oracle.Engine(41)
+    g = er._Gen(torch.int32, a, 0.0, trials=t, kind=kind)
+    og = oracle.Gen()
+    for n in (4, 8, 1 << 14, 12, 1 << 16):
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, kind, n, np.int32, a, 0.0, t)
+        assert_bits_equal(got, ref, f"{kind}({a},{t}) n={n}")
+    d, keep = er._desc("RANDBITS", torch.int32)
+    o = torch.empty(8, dtype=torch.int32, device="cuda")
+    er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), 8, er._stream_ptr()))
+    assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 8, np.int32), "randbits after")
+
+
+@pytest.mark.parametrize("a,b", [(0.5, 2.0), (2.0, 0.5), (1.0, 3.0), (2.5, 4.0), (0.3, 1.0), (22.0, 1.5)])
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+def test_beta_general_bit_exact(er, oracle, a, b, tdt):
+    u = er.Vmt19937_64(43)
+    e = oracle.Engine(43)
+    g = er.BetaGen(a, b, dtype=tdt)
+    og = oracle.Gen()
+    P = 8 if tdt == torch.float32 else 4
+    for n in (P, 3 * P, 1 << 13, 5 * P, 1 << 15):
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, "BETA", n, npdt(tdt), a, b)
+        assert_bits_equal(got, ref, f"beta({a},{b}) {tdt} n={n}")
+    assert_bits_equal(er.raw_u64(u, 64).cpu().numpy().view(np.uint64), e.raw(16), "engine after beta")
 
 
 def test_rejection_on_many_streams(er, oracle):
