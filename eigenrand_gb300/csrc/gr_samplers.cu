@@ -717,7 +717,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
   int64_t E = 0;     // output packets done
   int64_t done_pos = 0;  // positions evaluated up to (exclusive)
   // Beta FIFOs: carried lane sources are stored as values (bits)
-  uint64_t fifo[2][8];
+  uint64_t fifo[2][16];  // up to P-1 carried + P-1 appended lanes before an emission
   int fcnt[2] = {0, 0};
   if (!kPoisson && tid == 0) {
     for (int c = 0; c < 2; ++c) {
@@ -869,9 +869,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
           int64_t x = s;
           uint64_t outv[2][8];
           int fc[2] = {fcnt[0], fcnt[1]};
-          uint64_t ff[2][8];
+          uint64_t ff[2][16];
           for (int c = 0; c < 2; ++c)
-            for (int j = 0; j < 8; ++j) ff[c][j] = fifo[c][j];
+            for (int j = 0; j < 16; ++j) ff[c][j] = fifo[c][j];
           bool ok = true;
           for (int c = 0; c < 2 && ok; ++c) {
             if (comp[c].type <= 1) {
@@ -904,7 +904,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
           if (!ok) break;  // needs positions of the next block
           for (int c = 0; c < 2; ++c) {
             fcnt[c] = fc[c];
-            for (int j = 0; j < 8; ++j) fifo[c][j] = ff[c][j];
+            for (int j = 0; j < 16; ++j) fifo[c][j] = ff[c][j];
           }
           for (int c = 0; c < 2; ++c)
             for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)outv[c][j];
