@@ -337,13 +337,18 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
             const float ux = ur_f(word(w0 + j));
             const float vx = ur_f(word(w0 + 8 + j)) + 1.1920928955078125e-07f / 8;
             const float ux2 = ur_f(word(w0 + 16 + j));
+            // the reference evaluates both branches and blends (NormalExp.h:543-553);
+            // evaluating only the selected one gives the same bits
             const float lv = logf_(vx);
-            const float x1 = expf_(d.fc * lv);  // (1/alpha) * log(vx)
-            const float q1 = expf_(-x1);
-            const float x2 = 1.0f - lv;
-            const float q2 = expf_(logf_(x2) * d.fd);  // alpha - 1
-            const bool c = ux < d.fe;                 // px
-            const float xx = c ? x1 : x2, qx = c ? q1 : q2;
+            const bool c = ux < d.fe;  // px
+            float xx, qx;
+            if (c) {
+              xx = expf_(d.fc * lv);  // (1/alpha) * log(vx)
+              qx = expf_(-xx);
+            } else {
+              xx = 1.0f - lv;
+              qx = expf_(logf_(xx) * d.fd);  // alpha - 1
+            }
             cbits = f2u(d.fb * xx);
             acc = ux2 < qx;
           } else if (RK == RK_GAMMA_TAN) {
@@ -373,12 +378,15 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
             const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
             const double ux2 = ur_d(rval(r0 + 8));
             const double lv = log_(vx);
-            const double x1 = exp_(d.dc * lv);
-            const double q1 = exp_(-x1);
-            const double x2 = 1.0 - lv;
-            const double q2 = exp_(log_(x2) * d.dd);
             const bool c = ux < d.de;
-            const double xx = c ? x1 : x2, qx = c ? q1 : q2;
+            double xx, qx;
+            if (c) {
+              xx = exp_(d.dc * lv);
+              qx = exp_(-xx);
+            } else {
+              xx = 1.0 - lv;
+              qx = exp_(log_(xx) * d.dd);
+            }
             cbits = d2u(d.db * xx);
             acc = ux2 < qx;
           } else if (RK == RK_GAMMA_TAN) {
@@ -738,9 +746,6 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
     cur = nxt;
-    // the walk may lag the evaluated positions by at most one output packet;
-    // a lag beyond the ring would read overwritten slots, so it is an error
-    if (tid == 0 && done_pos - s > RING - 2 * kN) s_err = 1;
     // positions whose whole step lies in the generated packets
     int64_t lim;  // evaluate positions [done_pos, lim)
     if (kPoisson) {
@@ -750,6 +755,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
       const int umax = max(max(comp[0].U, comp[1].U), 3);
       lim = (nb + 1) * kN - umax + 1;
     }
+    // new positions overwrite ring slot x % RING; the walk (thread 0) must not
+    // still need a slot that is about to be overwritten
+    if (tid == 0 && lim - s > RING) s_err = 1;
     // ---- evaluate every start position in [done_pos, lim)
     for (int64_t x = done_pos + tid; x < lim; x += kWalkThreads) {
       if (kPoisson) {
@@ -793,13 +801,17 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
               } else if (comp[c].type == 2) {
                 const float ux = U(0), vx = U(1) + 1.1920928955078125e-07f / 8, ux2 = U(2);
                 const float lv = logf_(vx);
-                const float x1 = expf_((1 / af) * lv);
-                const float q1 = expf_(-x1);
-                const float x2 = 1.0f - lv;
-                const float q2 = expf_(logf_(x2) * (af - 1));
                 const bool cc = ux < (float)(2.7182818284590452 / (af + 2.7182818284590452));
-                vb = f2u(1.0f * (cc ? x1 : x2));
-                acc = ux2 < (cc ? q1 : q2);
+                float xx, qx;
+                if (cc) {
+                  xx = expf_((1 / af) * lv);
+                  qx = expf_(-xx);
+                } else {
+                  xx = 1.0f - lv;
+                  qx = expf_(logf_(xx) * (af - 1));
+                }
+                vb = f2u(1.0f * xx);
+                acc = ux2 < qx;
               } else {
                 const float a1 = af - 1, sq = sqrtf(2 * af - 1);
                 float ys, yc;
@@ -821,13 +833,17 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
               } else if (comp[c].type == 2) {
                 const double ux = U(0), vx = U(1) + 2.220446049250313e-16 / 8, ux2 = U(2);
                 const double lv = log_(vx);
-                const double x1 = exp_((1 / ad) * lv);
-                const double q1 = exp_(-x1);
-                const double x2 = 1.0 - lv;
-                const double q2 = exp_(log_(x2) * (ad - 1));
                 const bool cc = ux < (2.7182818284590452 / (ad + 2.7182818284590452));
-                vb = d2u(1.0 * (cc ? x1 : x2));
-                acc = ux2 < (cc ? q1 : q2);
+                double xx, qx;
+                if (cc) {
+                  xx = exp_((1 / ad) * lv);
+                  qx = exp_(-xx);
+                } else {
+                  xx = 1.0 - lv;
+                  qx = exp_(log_(xx) * (ad - 1));
+                }
+                vb = d2u(1.0 * xx);
+                acc = ux2 < qx;
               } else {
                 const double a1 = ad - 1, sq = sqrt(2 * ad - 1);
                 double ys, yc;
@@ -860,54 +876,47 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
           ++E;
         }
       } else {
-        // record layout per output packet: [src0 ... src(P-1)] for component 0 values
-        // (as raw bits, already resolved), then component 1's
+        // record per output packet: component 0's P lane values, then component 1's.
+        // Walk only while a generous margin of evaluated positions remains, so
+        // one output packet never runs past them (a longer run would need
+        // about 30 consecutive nearly-empty trials; it is reported as an error).
+        constexpr int64_t kMargin = 96;
         const int stride = 2 * P;
-        for (;;) {
-          if (E >= Npk || nrec >= kRecB) break;
-          // try to produce one output packet from position s without running past done_pos
+        while (E < Npk && nrec < kRecB && s + kMargin <= done_pos) {
           int64_t x = s;
-          uint64_t outv[2][8];
-          int fc[2] = {fcnt[0], fcnt[1]};
-          uint64_t ff[2][16];
-          for (int c = 0; c < 2; ++c)
-            for (int j = 0; j < 16; ++j) ff[c][j] = fifo[c][j];
-          bool ok = true;
-          for (int c = 0; c < 2 && ok; ++c) {
+          for (int c = 0; c < 2; ++c) {
             if (comp[c].type <= 1) {
-              if (x >= done_pos) { ok = false; break; }
               const int ri = (int)(x % RING);
-              for (int j = 0; j < P; ++j) outv[c][j] = pos_val[((size_t)c * RING + ri) * 8 + j];
+              for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)pos_val[((size_t)c * RING + ri) * 8 + j];
               x += comp[c].U;
-            } else {
-              for (;;) {
-                if (x >= done_pos) { ok = false; break; }
-                const int ri = (int)(x % RING);
-                const uint32_t m = pos_aux[c * RING + ri];
-                const uint64_t* cv = &pos_val[((size_t)c * RING + ri) * 8];
-                x += comp[c].U;
-                if (__popc(m) == P) {
-                  for (int j = 0; j < P; ++j) outv[c][j] = cv[j];
-                  break;
-                }
-                for (int j = 0; j < P; ++j)
-                  if ((m >> j) & 1u) ff[c][fc[c]++] = cv[j];
-                if (fc[c] >= P) {
-                  for (int j = 0; j < P; ++j) outv[c][j] = ff[c][j];
-                  for (int j = P; j < fc[c]; ++j) ff[c][j - P] = ff[c][j];
-                  fc[c] -= P;
-                  break;
-                }
+              continue;
+            }
+            for (;;) {
+              if (x >= done_pos) {
+                s_err = 1;
+                break;
               }
+              const int ri = (int)(x % RING);
+              const uint32_t m = pos_aux[c * RING + ri];
+              const uint64_t* cv = &pos_val[((size_t)c * RING + ri) * 8];
+              x += comp[c].U;
+              if (__popc(m) == P) {
+                for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)cv[j];
+                break;
+              }
+              int fc = fcnt[c];
+              for (int j = 0; j < P; ++j)
+                if ((m >> j) & 1u) fifo[c][fc++] = cv[j];
+              if (fc >= P) {
+                for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)fifo[c][j];
+                for (int j = P; j < fc; ++j) fifo[c][j - P] = fifo[c][j];
+                fc -= P;
+                fcnt[c] = fc;
+                break;
+              }
+              fcnt[c] = fc;
             }
           }
-          if (!ok) break;  // needs positions of the next block
-          for (int c = 0; c < 2; ++c) {
-            fcnt[c] = fc[c];
-            for (int j = 0; j < 16; ++j) fifo[c][j] = ff[c][j];
-          }
-          for (int c = 0; c < 2; ++c)
-            for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)outv[c][j];
           ++nrec;
           s = x;
           ++E;
