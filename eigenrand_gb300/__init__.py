@@ -31,6 +31,7 @@ __all__ = [
     "StdUniformRealGen", "UniformRealGen", "BalancedGen", "Balanced2Gen", "StdNormalGen", "NormalGen",
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
     "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen",
+    "sample_batched",
 ]
 
 _lib.load()
@@ -368,3 +369,53 @@ def discrete(rows, cols, urng, weights, out=None, stream=None):
 
 def randBits(rows, cols, urng, out=None, stream=None):
     return _sample("RANDBITS", rows, cols, urng, torch.int32, out=out, stream=stream)
+
+
+# ---- vectorize-over-params, many sets in one launch ------------------------
+def sample_batched(kind, counts, a, b=None, trials=None, seed=5489, urng=None, out=None, offsets=None,
+                   stream=None):
+    """Draw counts[i] samples for each parameter set i in one launch.
+
+    kind "GAMMA": GammaGen<float>(a[i], b[i]) -> float32.
+    kind "BINOMIAL_V": BinomialVGen<int32_t> with (trials[i], p = a[i]) -> int32.
+    Set i uses a fresh Vmt19937_64(seed + 4 i).  Returns (out, offsets)."""
+    counts = counts.to(device="cuda", dtype=torch.int32).contiguous()
+    a = a.to(device="cuda", dtype=torch.float32).contiguous()
+    if offsets is None:
+        offsets = torch.zeros(counts.numel(), dtype=torch.int64, device="cuda")
+        if counts.numel() > 1:
+            offsets[1:] = torch.cumsum(counts[:-1].to(torch.int64), 0)
+    total = int(offsets[-1].item() + counts[-1].item()) if counts.numel() else 0
+    if out is None:
+        out = torch.empty(max(total, 1), dtype=torch.float32 if kind == "GAMMA" else torch.int32, device="cuda")
+    bd = _lib.BatchDesc()
+    bd.kind = KINDS[kind]
+    bd.nsets = counts.numel()
+    bd.seed = seed
+    bd.a = a.data_ptr()
+    keep = [a, counts, offsets]
+    if b is not None:
+        b = b.to(device="cuda", dtype=torch.float32).contiguous()
+        bd.b = b.data_ptr()
+        keep.append(b)
+    if trials is not None:
+        trials = trials.to(device="cuda", dtype=torch.int32).contiguous()
+        bd.trials = trials.data_ptr()
+        keep.append(trials)
+    bd.counts = counts.data_ptr()
+    bd.offsets = offsets.data_ptr()
+    bd.out = out.data_ptr()
+    eng = urng if urng is not None else _status_engine()
+    _lib.check(_L.gr_sample_batched(eng._h, ctypes.byref(bd), _stream_ptr(stream)))
+    del keep
+    return out, offsets
+
+
+_status_eng = None
+
+
+def _status_engine():
+    global _status_eng
+    if _status_eng is None:
+        _status_eng = Vmt19937_64(0)
+    return _status_eng

@@ -22,15 +22,30 @@ F32, F64, I32, U64 = 0, 1, 2, 3
 KINDS = dict(
     UNIFORM_REAL=1, UNIFORM_REAL2=2, BALANCED=3, BALANCED2=4, NORMAL_STD=5, NORMAL=6, LOGNORMAL=7,
     EXPONENTIAL=8, CAUCHY=9, WEIBULL=10, EXTREME_VALUE=11, GAMMA=12, BETA=13, STUDENT_T=14,
-    CHI_SQUARED=15, POISSON=16, BINOMIAL=17, DISCRETE=18, RANDBITS=19,
+    CHI_SQUARED=15, POISSON=16, BINOMIAL=17, DISCRETE=18, RANDBITS=19, BINOMIAL_V=20,
 )
 
 # exported symbols, as declared in include/gpurand.h
 EXPORTS = [
     "gr_engine_create", "gr_engine_destroy", "gr_engine_seed", "gr_engine_state_size", "gr_engine_save",
     "gr_engine_restore", "gr_engine_discard", "gr_engine_sync", "gr_engine_streams", "gr_raw_u64",
-    "gr_gen_create", "gr_gen_destroy", "gr_generate", "gr_sample", "gr_last_error", "gr_version",
+    "gr_gen_create", "gr_gen_destroy", "gr_generate", "gr_sample", "gr_sample_batched", "gr_last_error",
+    "gr_version",
 ]
+
+
+class BatchDesc(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("nsets", ctypes.c_int64),
+        ("seed", ctypes.c_uint64),
+        ("a", ctypes.c_void_p),
+        ("b", ctypes.c_void_p),
+        ("trials", ctypes.c_void_p),
+        ("counts", ctypes.c_void_p),
+        ("offsets", ctypes.c_void_p),
+        ("out", ctypes.c_void_p),
+    ]
 
 
 class DistDesc(ctypes.Structure):
@@ -82,6 +97,7 @@ def load(path=None):
         "gr_generate": (i32, [vp, vp, vp, sz, vp]),
         "gr_sample": (i32, [vp, ctypes.POINTER(DistDesc), vp, sz, vp]),
         "gr_raw_u64_noalloc": (i32, [vp, vp, sz, vp]),
+        "gr_sample_batched": (i32, [vp, ctypes.POINTER(BatchDesc), vp]),
         "gr_last_error": (ctypes.c_char_p, []),
         "gr_version": (ctypes.c_char_p, []),
     }

@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "libgpurand.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-SOURCES = ["gr_kernels.cu", "gr_samplers.cu", "gr_api.cu", "gr_noalloc.cu", "gr_poly.cpp"]
+SOURCES = ["gr_kernels.cu", "gr_samplers.cu", "gr_vop.cu", "gr_api.cu", "gr_noalloc.cu", "gr_poly.cpp"]
 HEADERS = ["gr_internal.h", "gr_kernels.cuh", "gr_math.cuh", "gr_mt.cuh", "gr_poly.h"]
 
 

@@ -673,6 +673,83 @@ gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_strea
   return run_call(e, g, g->dp, dev_out, n, (cudaStream_t)stream);
 }
 
+// ---- batched sets + autotuner ------------------------------------------------
+// Candidates: CTA width 160 (the 156-thread twist plus 4) or 320 (twice the
+// threads for trial evaluation, half the CTAs per SM).  The first call for a
+// (kind, log2 nsets) class times each candidate on the call's own sets with
+// CUDA events (the results are deterministic, so the timed runs just rewrite
+// the same outputs) and caches the fastest.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tuned;
+}  // namespace
+
+static int tuned_threads(int kind, int64_t nsets) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  int b = 0;
+  while (((int64_t)1 << b) < nsets) ++b;
+  auto it = g_tuned.find({kind, b});
+  return it == g_tuned.end() ? 0 : it->second;
+}
+
+gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* bd, gr_stream_t stream) {
+  if (!e || !bd) return fail(GR_ERR_INVALID, "NULL argument");
+  if (bd->kind != GR_GAMMA && bd->kind != GR_BINOMIAL_V)
+    return fail(GR_ERR_UNSUPPORTED, "batched sets support GR_GAMMA and GR_BINOMIAL_V");
+  if (bd->nsets <= 0) return GR_OK;
+  if (!bd->a || !bd->counts || !bd->offsets || !bd->out || (bd->kind == GR_GAMMA && !bd->b) ||
+      (bd->kind == GR_BINOMIAL_V && !bd->trials))
+    return fail(GR_ERR_INVALID, "missing device array in gr_batch_desc");
+  cudaStream_t s = (cudaStream_t)stream;
+  VopArgs va{};
+  va.nsets = bd->nsets;
+  va.perm = nullptr;
+  va.seed = bd->seed;
+  va.a = bd->a;
+  va.b = bd->b;
+  va.trials = bd->trials;
+  va.counts = bd->counts;
+  va.offsets = bd->offsets;
+  va.out = bd->out;
+  va.status = &e->st[0].status;
+  int b = 0;
+  while (((int64_t)1 << b) < bd->nsets) ++b;
+  int threads = tuned_threads(bd->kind, bd->nsets);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cap);
+  if (threads == 0 && cap == cudaStreamCaptureStatusNone) {
+    const int cand[2] = {160, 320};
+    float best = 1e30f;
+    int best_t = 160;
+    cudaEvent_t e0, e1;
+    GR_CUDA(cudaEventCreate(&e0));
+    GR_CUDA(cudaEventCreate(&e1));
+    for (int c : cand) {
+      GR_CUDA(launch_vop(bd->kind, c, va, s));  // warm
+      GR_CUDA(cudaEventRecord(e0, s));
+      GR_CUDA(launch_vop(bd->kind, c, va, s));
+      GR_CUDA(cudaEventRecord(e1, s));
+      GR_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      GR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        best_t = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[{bd->kind, b}] = best_t;
+    threads = best_t;
+    // the timed runs already wrote the outputs; one more launch keeps the
+    // call's own semantics simple (identical values)
+  }
+  if (threads == 0) threads = 160;
+  GR_CUDA(launch_vop(bd->kind, threads, va, s));
+  return GR_OK;
+}
+
 gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream) {
   if (!e || !desc) return fail(GR_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;

@@ -66,6 +66,21 @@ cudaError_t launch_reject(const Plan& p, const DistParams& d, int rk, int64_t ma
 // (gamma branch << 8) | packets for the two GammaGens).
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s);
 
+// Batched vectorize-over-params sets (gr_vop.cu).
+struct VopArgs {
+  int64_t nsets;
+  const int32_t* perm;
+  uint64_t seed;
+  const float* a;
+  const float* b;
+  const int32_t* trials;
+  const int32_t* counts;
+  const int64_t* offsets;
+  void* out;
+  int32_t* status;
+};
+cudaError_t launch_vop(int kind, int threads, const VopArgs& va, cudaStream_t s);
+
 // Outputs per granule: the smallest output count a call (or a stream slice)
 // may have for the kind.  Packets per unit: 2 for the Box-Muller kinds.
 int kind_granule(int kind, int dtype);

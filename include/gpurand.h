@@ -69,7 +69,8 @@ typedef enum {
   GR_POISSON = 16,      /* PoissonGen(mean=a); Discrete.h:788-904                 */
   GR_BINOMIAL = 17,     /* BinomialGen(trials, p=a); Discrete.h:911-1053          */
   GR_DISCRETE = 18,     /* DiscreteGen<int32_t,int32_t>(weights); Discrete.h:352-486 */
-  GR_RANDBITS = 19      /* RandbitsGen<int32_t>; Basic.h:378-400                  */
+  GR_RANDBITS = 19,     /* RandbitsGen<int32_t>; Basic.h:378-400                  */
+  GR_BINOMIAL_V = 20    /* BinomialVGen<int32_t>, per-element (trials, p); Discrete.h:1061-1192 */
 } gr_dist_kind;
 
 typedef struct {
@@ -120,6 +121,33 @@ gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_strea
 /* Free-function form (Eigen::Rand::normal(rows, cols, urng, ...)): a fresh
  * generator for one call. */
 gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream);
+
+/* ---- vectorize-over-params, many parameter sets in one launch ----------
+ * Set i (0 <= i < nsets) is drawn from a fresh Vmt19937_64(seed + 4 i) with a
+ * fresh generator: exactly what seeding an engine and making one per-call
+ * sample of the set would give.  counts[i] samples land at
+ * out[offsets[i] .. offsets[i] + counts[i]); a set of c samples draws
+ * ceil(c / P) packets and keeps the first c values.
+ *   GR_GAMMA      : GammaGen<float>(a[i], b[i]) (NormalExp.h:434-606), float out
+ *   GR_BINOMIAL_V : BinomialVGen<int32_t> with (trials[i], a[i] = p)
+ *                   (Discrete.h:1124-1192; the reference's binomial(urng,
+ *                   ArrayXi, ArrayXf) over a set's repeated parameters), int32 out
+ * All arrays are device pointers.  Launch shape (threads per CTA) comes from
+ * the library's autotuner, which times the candidates on the first call for
+ * a (kind, size) class and caches the winner.  Device errors fold into the
+ * engine's status (gr_engine_sync). */
+typedef struct {
+  int32_t kind;
+  int64_t nsets;
+  uint64_t seed;
+  const float* a;
+  const float* b;
+  const int32_t* trials;
+  const int32_t* counts;
+  const int64_t* offsets;
+  void* out;
+} gr_batch_desc;
+gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* batch, gr_stream_t stream);
 
 const char* gr_last_error(void);
 const char* gr_version(void);

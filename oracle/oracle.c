@@ -884,3 +884,102 @@ int or_gen_discrete(or_vmt* e, or_gen* g, const or_discrete* d, int32_t* out, si
   }
   return 0;
 }
+
+/* ======================================================================
+ * BinomialVGen<int32_t>::packetOp (Discrete.h:1124-1192), one packet of 4
+ * lanes whose (trials, p) may differ per lane.  Lanes with mean < 1 run the
+ * multiplicative Poisson loop; the others a tan-proposal rejection with a
+ * per-lane accepted mask, iterating until every lane has a value.
+ * ====================================================================== */
+int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out) {
+  float small_p[4], ptrials[4], mean[4], g1[4], sqrt_v[4], lsp[4], lsq[4], ne[4];
+  int valid[4], any_valid = 0, all_valid = 1;
+  float valid_res[4] = {0, 0, 0, 0};
+  for (int j = 0; j < 4; ++j) {
+    small_p[j] = p[j] < 1.0f - p[j] ? p[j] : 1.0f - p[j]; /* pmin(p, 1 - p) */
+    ptrials[j] = (float)trials[j];
+    mean[j] = ptrials[j] * small_p[j];
+    g1[j] = or_lgamma_approxf(ptrials[j] + 1.0f);
+    sqrt_v[j] = sqrtf((2.0f * mean[j]) * (1.0f - small_p[j]));
+    lsp[j] = or_logf(small_p[j]);
+    lsq[j] = or_logf(1.0f - small_p[j]);
+    ne[j] = or_expf(-mean[j]);
+    valid[j] = mean[j] < 1.0f;
+    any_valid |= valid[j];
+    all_valid &= valid[j];
+  }
+  if (any_valid) {
+    int32_t res[4] = {0, 0, 0, 0};
+    float val[4] = {1, 1, 1, 1};
+    for (;;) {
+      float u[4];
+      ur_f4(e, u);
+      int any = 0, c[4];
+      for (int j = 0; j < 4; ++j) {
+        val[j] = val[j] * u[j];
+        c[j] = (ne[j] < val[j]) && valid[j];
+        any |= c[j];
+      }
+      if (!any) break;
+      for (int j = 0; j < 4; ++j) res[j] += c[j];
+    }
+    for (int j = 0; j < 4; ++j) valid_res[j] = (float)res[j];
+  }
+  if (!all_valid) {
+    for (;;) {
+      float u[4], u2[4], fres[4], ys[4];
+      ur_f4(e, u);
+      for (int j = 0; j < 4; ++j) {
+        float s, c;
+        or_sincosf((float)PI_D * u[j], &s, &c);
+        ys[j] = s / c;
+        fres[j] = truncf(sqrt_v[j] * ys[j] + mean[j]);
+      }
+      ur_f4(e, u2);
+      int all = 1;
+      for (int j = 0; j < 4; ++j) {
+        float p1 = ((float)1.2 * sqrt_v[j]) * (1.0f + ys[j] * ys[j]);
+        float t = (g1[j] - or_lgamma_approxf(fres[j] + 1.0f)) - or_lgamma_approxf((ptrials[j] + 1.0f) - fres[j]);
+        t = t + fres[j] * lsp[j];
+        t = t + (ptrials[j] - fres[j]) * lsq[j];
+        float p2 = or_expf(t);
+        int fvalid = (0.0f <= fres[j]) && (fres[j] <= ptrials[j]) && (u2[j] <= p1 * p2);
+        if (fvalid && !valid[j]) valid_res[j] = fres[j];
+        valid[j] |= fvalid;
+        all &= valid[j];
+      }
+      if (all) break;
+    }
+  }
+  for (int j = 0; j < 4; ++j) out[j] = (p[j] == small_p[j]) ? (int32_t)valid_res[j] : trials[j] - (int32_t)valid_res[j];
+  return 0;
+}
+
+/* One vectorize-over-params set, as the batched API defines it: a fresh
+ * Vmt19937_64(seed) and a fresh generator, count samples drawn with the
+ * packet algorithm, the last packet truncated.  kind: 0 = GammaGen<float>
+ * (a = alpha, b = beta), 1 = BinomialVGen<int32_t> with uniform (trials, p). */
+int or_vop_set(uint64_t seed, int kind, double a, double b, int32_t trials, void* out, size_t count) {
+  or_vmt* e = or_vmt_new(seed, 4);
+  or_gen g[3];
+  memset(g, 0, sizeof g);
+  int rc = 0;
+  if (kind == 0) {
+    size_t n8 = (count + 7) / 8 * 8;
+    float* tmp = (float*)malloc(sizeof(float) * (n8 ? n8 : 8));
+    rc = n8 ? or_gen_real(e, g, OR_GAMMA, 0, a, b, tmp, n8) : 0;
+    memcpy(out, tmp, sizeof(float) * count);
+    free(tmp);
+  } else {
+    int32_t tr[4] = {trials, trials, trials, trials};
+    float pp[4] = {(float)a, (float)a, (float)a, (float)a};
+    int32_t* o = (int32_t*)out;
+    for (size_t k = 0; k < count; k += 4) {
+      int32_t r[4];
+      or_binomial_v_packet(e, tr, pp, r);
+      for (size_t j = 0; j < 4 && k + j < count; ++j) o[k + j] = r[j];
+    }
+  }
+  or_vmt_free(e);
+  return rc;
+}

@@ -103,6 +103,10 @@ void or_discrete_free(or_discrete* d);
 int or_discrete_table(const or_discrete* d, int32_t* prob, int32_t* alias, int cap);
 int or_gen_discrete(or_vmt* e, or_gen* g, const or_discrete* d, int32_t* out, size_t n);
 
+/* vectorize-over-params */
+int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out);
+int or_vop_set(uint64_t seed, int kind, double a, double b, int32_t trials, void* out, size_t count);
+
 /* ---- math (library's own log/exp; EigenRand psincos restated) ---------- */
 float or_logf(float x);
 float or_expf(float x);

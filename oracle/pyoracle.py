@@ -56,6 +56,9 @@ def lib():
         L.or_discrete_table.restype = ctypes.c_int
         L.or_gen_discrete.argtypes = [vp, vp, vp, vp, sz]
         L.or_gen_discrete.restype = ctypes.c_int
+        L.or_vop_set.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                 vp, sz]
+        L.or_vop_set.restype = ctypes.c_int
         for name in ("or_vec_logf", "or_vec_expf", "or_vec_log", "or_vec_exp"):
             getattr(L, name).argtypes = [vp, vp, sz]
         L.or_vec_sincosf.argtypes = [vp, vp, vp, sz]
@@ -142,6 +145,15 @@ def generate(eng, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0, weight
     if rc != 0:
         raise RuntimeError(f"oracle error {rc} for {kind}")
     return out
+
+
+def vop_set(seed, kind, count, a=0.0, b=1.0, trials=0):
+    """One batched set: kind "GAMMA" (float32) or "BINOMIAL_V" (int32)."""
+    out = np.empty(max(count, 1), dtype=np.float32 if kind == "GAMMA" else np.int32)
+    rc = lib().or_vop_set(ctypes.c_uint64(seed), 0 if kind == "GAMMA" else 1, a, b, trials, _p(out), count)
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return out[:count]
 
 
 def vec_math(name, x):
