@@ -385,8 +385,8 @@ def sample_batched(kind, counts, a, b=None, trials=None, seed=5489, urng=None, o
         offsets = torch.zeros(counts.numel(), dtype=torch.int64, device="cuda")
         if counts.numel() > 1:
             offsets[1:] = torch.cumsum(counts[:-1].to(torch.int64), 0)
-    total = int(offsets[-1].item() + counts[-1].item()) if counts.numel() else 0
-    if out is None:
+    if out is None:  # sizing reads two values back; pass `out` to stay capturable
+        total = int(offsets[-1].item() + counts[-1].item()) if counts.numel() else 0
         out = torch.empty(max(total, 1), dtype=torch.float32 if kind == "GAMMA" else torch.int32, device="cuda")
     bd = _lib.BatchDesc()
     bd.kind = KINDS[kind]

@@ -61,17 +61,20 @@ def test_batched_equals_per_call_and_graph_replay(gpulib, kind):
                                   None if tt is None else tt[i:i + 1], seed=1234 + 4 * i)
         torch.cuda.synchronize()
         np.testing.assert_array_equal(o1.cpu().numpy()[:counts[i]], whole[off[i].item():off[i].item() + counts[i]])
-    # captured in a CUDA graph and replayed
+    # captured in a CUDA graph and replayed (inputs staged on the device first)
+    dc, da = tc.cuda(), ta.cuda()
+    db = None if tb is None else tb.cuda()
+    dt = None if tt is None else tt.cuda()
     out2 = torch.empty_like(out)
     s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
-        er.sample_batched(kind, tc, ta, tb, tt, seed=1234, out=out2, offsets=off, stream=s)  # tuned already
+        er.sample_batched(kind, dc, da, db, dt, seed=1234, out=out2, offsets=off, stream=s)  # tuned already
         s.synchronize()
         g = torch.cuda.CUDAGraph()
         out3 = torch.zeros_like(out)
         with torch.cuda.graph(g, stream=s):
-            er.sample_batched(kind, tc.cuda(), ta.cuda(), None if tb is None else tb.cuda(),
-                              None if tt is None else tt.cuda(), seed=1234, out=out3, offsets=off, stream=s)
+            er.sample_batched(kind, dc, da, db, dt, seed=1234, out=out3, offsets=off, stream=s)
     g.replay()
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out3.cpu().numpy(), whole)
