@@ -32,6 +32,9 @@ __all__ = [
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
     "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen",
     "sample_batched",
+    "MvNormalGen", "WishartGen", "InvWishartGen", "DirichletGen", "MultinomialGen", "makeMvNormalGen",
+    "makeMvNormalGenFromLt", "makeWishartGen", "makeWishartGenFromLt", "makeInvWishartGen",
+    "makeInvWishartGenFromIlt", "makeDirichletGen", "makeMultinomialGen",
 ]
 
 _lib.load()
@@ -419,3 +422,173 @@ def _status_engine():
     if _status_eng is None:
         _status_eng = Vmt19937_64(0)
     return _status_eng
+
+
+# ---- multivariate generators (MvDists/*.h) ---------------------------------
+def _host_f64(x, n=None):
+    """Column-major float64 host copy of a vector / square matrix (numpy, torch
+    or nested lists); returns (ctypes array, keep-alive)."""
+    if isinstance(x, torch.Tensor):
+        x = x.detach().to("cpu", torch.float64)
+        flat = x.t().contiguous().reshape(-1).tolist() if x.dim() == 2 else x.reshape(-1).tolist()
+    else:
+        import numpy as np
+
+        a = np.asarray(x, dtype=np.float64)
+        flat = a.reshape(-1, order="F").tolist()
+    if n is not None and len(flat) != n:
+        raise ValueError(f"expected {n} values, got {len(flat)}")
+    buf = (ctypes.c_double * len(flat))(*flat)
+    return buf
+
+
+class _MvGen:
+    _prefix = None
+
+    def _finish(self, h):
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _L is not None:
+            getattr(_L, self._prefix + "_destroy")(h)
+            self._h = None
+
+    def dims(self):
+        return self.dim
+
+
+class MvNormalGen(_MvGen):
+    """Eigen::Rand::MvNormalGen<float|double> (MvNormal.h:56-116).
+
+    MvNormalGen(mean, cov) factors cov by get_lt (FP64 Cholesky on the GPU, or
+    V sqrt(max(lambda, 0)) if not positive definite);
+    MvNormalGen(mean, lt, lower_triangular=True) takes the factor itself.
+    generate(urng, samples) -> (dim, samples) tensor, column-major like the
+    Eigen matrix (each sample a contiguous column)."""
+
+    _prefix = "gr_mvnormal"
+
+    def __init__(self, mean, cov, lower_triangular=False, dtype=torch.float32):
+        self.dim = len(mean) if not isinstance(mean, torch.Tensor) else mean.numel()
+        self.dtype = dtype
+        m = _host_f64(mean, self.dim)
+        c = _host_f64(cov, self.dim * self.dim)
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_mvnormal_create(ctypes.byref(h), _DT[dtype], self.dim, m, c, 1 if lower_triangular else 0))
+        self._finish(h)
+
+    def generate(self, urng, samples=1, out=None, stream=None):
+        o = out if out is not None else torch.empty((samples, self.dim), dtype=self.dtype, device="cuda").t()
+        _lib.check(_L.gr_mvnormal_sample(self._h, urng._h, _ptr(o), samples, _stream_ptr(stream)))
+        return o
+
+
+class WishartGen(_MvGen):
+    """Eigen::Rand::WishartGen (MvNormal.h:185-277): WishartGen(df, scale) or
+    WishartGen(df, lt, lower_triangular=True).  generate(urng, samples) ->
+    (dim, dim * samples) tensor, draw j in columns j*dim .. (j+1)*dim."""
+
+    _prefix = "gr_wishart"
+    _inverse = 0
+
+    def __init__(self, df, scale, lower_triangular=False, dtype=torch.float32):
+        import math
+
+        self.dim = int(round(math.sqrt(len(_host_f64(scale)))))
+        self.dtype = dtype
+        self.df = int(df)
+        c = _host_f64(scale, self.dim * self.dim)
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_wishart_create(ctypes.byref(h), _DT[dtype], self.dim, ctypes.c_int64(self.df), c,
+                                        1 if lower_triangular else 0, self._inverse))
+        self._finish(h)
+
+    def generate(self, urng, samples=1, out=None, stream=None):
+        d = self.dim
+        o = out if out is not None else torch.empty((d * samples, d), dtype=self.dtype, device="cuda").t()
+        _lib.check(_L.gr_wishart_sample(self._h, urng._h, _ptr(o), samples, _stream_ptr(stream)))
+        return o
+
+
+class InvWishartGen(WishartGen):
+    """Eigen::Rand::InvWishartGen (MvNormal.h:347-442): InvWishartGen(df, scale)
+    or InvWishartGen(df, ilt, inv_lower_triangular=True)."""
+
+    _inverse = 1
+
+    def __init__(self, df, scale, inv_lower_triangular=False, dtype=torch.float32):
+        super().__init__(df, scale, lower_triangular=inv_lower_triangular, dtype=dtype)
+
+
+class DirichletGen(_MvGen):
+    """Eigen::Rand::DirichletGen (Multinomial.h:160-204).  generate(urng,
+    samples) -> (dim, samples) tensor."""
+
+    _prefix = "gr_dirichlet"
+
+    def __init__(self, alpha, dtype=torch.float32):
+        a = _host_f64(alpha)
+        self.dim = len(a)
+        self.dtype = dtype
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_dirichlet_create(ctypes.byref(h), _DT[dtype], self.dim, a))
+        self._finish(h)
+
+    def generate(self, urng, samples=1, out=None, stream=None):
+        o = out if out is not None else torch.empty((samples, self.dim), dtype=self.dtype, device="cuda").t()
+        _lib.check(_L.gr_dirichlet_sample(self._h, urng._h, _ptr(o), samples, _stream_ptr(stream)))
+        return o
+
+
+class MultinomialGen(_MvGen):
+    """Eigen::Rand::MultinomialGen<int32_t> (Multinomial.h:25-118).
+    generate(urng, samples) -> int32 (dim, samples) tensor of counts."""
+
+    _prefix = "gr_multinomial"
+
+    def __init__(self, trials, weights):
+        w = _host_f64(weights)
+        self.dim = len(w)
+        self.trials = int(trials)
+        self.dtype = torch.int32
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_multinomial_create(ctypes.byref(h), self.dim, self.trials, w))
+        self._finish(h)
+
+    def generate(self, urng, samples=1, out=None, stream=None):
+        o = out if out is not None else torch.empty((samples, self.dim), dtype=torch.int32, device="cuda").t()
+        _lib.check(_L.gr_multinomial_sample(self._h, urng._h, _ptr(o), samples, _stream_ptr(stream)))
+        return o
+
+
+def makeMvNormalGen(mean, cov, dtype=torch.float32):
+    return MvNormalGen(mean, cov, dtype=dtype)
+
+
+def makeMvNormalGenFromLt(mean, lt, dtype=torch.float32):
+    return MvNormalGen(mean, lt, lower_triangular=True, dtype=dtype)
+
+
+def makeWishartGen(df, scale, dtype=torch.float32):
+    return WishartGen(df, scale, dtype=dtype)
+
+
+def makeWishartGenFromLt(df, lt, dtype=torch.float32):
+    return WishartGen(df, lt, lower_triangular=True, dtype=dtype)
+
+
+def makeInvWishartGen(df, scale, dtype=torch.float32):
+    return InvWishartGen(df, scale, dtype=dtype)
+
+
+def makeInvWishartGenFromIlt(df, ilt, dtype=torch.float32):
+    return InvWishartGen(df, ilt, inv_lower_triangular=True, dtype=dtype)
+
+
+def makeDirichletGen(alpha, dtype=torch.float32):
+    return DirichletGen(alpha, dtype=dtype)
+
+
+def makeMultinomialGen(trials, weights):
+    return MultinomialGen(trials, weights)

@@ -19,6 +19,7 @@
 #include "../../include/gpurand.h"
 #include "gr_internal.h"
 #include "gr_kernels.cuh"
+#include "gr_mv.cuh"
 #include "gr_poly.h"
 
 using namespace gr;
@@ -800,3 +801,50 @@ gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_
 }
 
 }  // extern "C"
+
+// ---- multinomial draws on an engine (k_multinomial, gr_mv.cu) ---------------
+namespace gr {
+
+gr_status build_discrete_table(const std::vector<double>& w, std::vector<int32_t>& prob, std::vector<int32_t>& alias,
+                               int& ncdf, uint32_t& bitmask) {
+  return build_discrete(w, prob, alias, ncdf, bitmask);
+}
+
+gr_status run_multinomial(gr_engine* e, GenState* gst, const MnArgs& a0, int64_t samples, cudaStream_t stream) {
+  if (samples <= 0) return GR_OK;
+  MnArgs a = a0;
+  // words per state period do not depend on the state the call starts in
+  const MnLayout L0 = mn_layout(a.trials, 0);
+  if (L0.W0 > kMnMaxSampleWords || L0.W1 > kMnMaxSampleWords)
+    return fail(GR_ERR_UNSUPPORTED, "multinomial draws per sample above the kernel's ring size");
+  const int64_t Wu = L0.spu == 2 ? L0.W0 + L0.W1 : L0.W0;
+  Plan p{};
+  p.eng = e->st;
+  p.gen = gst;
+  p.K = e->K;
+  p.gran = 1;
+  p.gran_per_k = samples / e->K;
+  p.gran_rem = samples % e->K;
+  p.out = a.out;
+  const int64_t ns_max = p.gran_per_k + (p.gran_rem ? 1 : 0);
+  const int64_t units = (ns_max + L0.spu - 1) / L0.spu;
+  const int64_t packets_max = units * Wu / 8;
+  int S = 1;
+  int64_t Us = std::max<int64_t>(units, 1), J = std::max<int64_t>(packets_max, 2);
+  if (e->K < 16 && packets_max >= ((int64_t)1 << 17)) {
+    const int64_t target = std::max<int64_t>(1, 128 / e->K);
+    int64_t us = 2;
+    while (us * target < units || us * Wu / 8 < ((int64_t)1 << 14)) us <<= 1;
+    Us = us;
+    J = us * Wu / 8;
+    S = (int)((units + us - 1) / us);
+  }
+  a.Us = Us;
+  gr_status st = prepare_segments(e, p, S, J, 0, stream);
+  if (st != GR_OK) return st;
+  cudaError_t err = launch_multinomial(p, a, e->snap, stream);
+  if (err != cudaSuccess) return cuda_fail(err, "multinomial kernel");
+  return GR_OK;
+}
+
+}  // namespace gr

@@ -1,0 +1,95 @@
+// Interface of the multivariate kernels (gr_mv.cu) for the host library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "gr_internal.h"
+#include "gr_kernels.cuh"
+
+namespace gr {
+
+constexpr int kWishTcMaxDim = 128;           // tensor-core Wishart products up to this dimension
+constexpr size_t kMvMaxSmem = 200 * 1024;    // shared memory cap of the SIMT fallbacks
+constexpr int kMvMaxDim = 2048;              // largest MvNormal dimension (in-place product)
+constexpr int kMnMaxSampleWords = 2464;      // multinomial sample must fit the two-block ring
+
+// Lower-triangular fragment count: sum over m-tiles of min(2mt + 2, KS).
+__host__ __device__ inline int64_t mv_tri_frags(int MT, int KS) {
+  int64_t t = 0;
+  for (int m = 0; m < MT; ++m) t += (2 * m + 2 < KS) ? 2 * m + 2 : KS;
+  return t;
+}
+
+// ---- multinomial word layout (MultinomialGen::generate, Multinomial.h:95-118)
+// Per sample: nP = trials / 4 DiscreteGen packet draws (16 at a time, then the
+// tail's whole packets) followed by ns = trials % 4 scalar draws.  State c =
+// DiscreteGen cache full (1) or empty (0) when the sample starts.
+struct MnLayout {
+  int nP, ns;  // packet draws, scalar draws
+  int spu;     // period of the state sequence in samples (1 or 2)
+  int c0;      // state of the first sample
+  int64_t W0, W1;  // u32 words consumed by a sample in state 0 / 1
+};
+
+__host__ __device__ inline MnLayout mn_layout(int trials, int c0) {
+  MnLayout L;
+  L.nP = trials >> 2;
+  L.ns = trials & 3;
+  L.c0 = c0;
+  L.W0 = 8 * (int64_t)((L.nP + 1) / 2 + L.ns);  // ceil(nP/2) packets + ns scalar packets
+  L.W1 = 8 * (int64_t)(L.nP / 2 + L.ns);        // first draw from the cache: ceil((nP-1)/2)
+  L.spu = (L.nP & 1) ? 2 : 1;                   // odd nP flips the cache every sample
+  return L;
+}
+__host__ __device__ inline int mn_state(const MnLayout& L, int64_t i) {
+  return L.spu == 2 ? (L.c0 ^ (int)(i & 1)) : L.c0;
+}
+// words before sample i (relative to the engine slice)
+__host__ __device__ inline int64_t mn_base(const MnLayout& L, int64_t i) {
+  if (L.spu == 1) return i * (L.c0 ? L.W1 : L.W0);
+  return (i >> 1) * (L.W0 + L.W1) + ((i & 1) ? (L.c0 ? L.W1 : L.W0) : 0);
+}
+// word offset (within a sample of state c) of the half packet it leaves cached
+__host__ __device__ inline int64_t mn_cache_off(const MnLayout& L, int c) {
+  return c == 0 ? 4 * (int64_t)L.nP : 4 * (int64_t)L.nP - 4;
+}
+// word offset of the first scalar draw's packet
+__host__ __device__ inline int64_t mn_scalar_off(const MnLayout& L, int c) {
+  return c == 0 ? 8 * (int64_t)((L.nP + 1) / 2) : 8 * (int64_t)(L.nP / 2);
+}
+
+struct MnArgs {
+  const int32_t* prob;   // alias probabilities, or the CDF when ncdf > 0
+  const int32_t* alias;
+  uint32_t bitmask;
+  int32_t ncdf;
+  int32_t dim;
+  int32_t trials;
+  int64_t Us;            // state periods per jump segment
+  int32_t* out;          // dim x samples, column-major
+};
+
+cudaError_t launch_inverse_f64(double* A, double* W, int d, int32_t* status, cudaStream_t s);
+cudaError_t launch_chol_f64(double* A, int d, int32_t* status, cudaStream_t s);
+cudaError_t launch_jacobi_f64(double* A, double* V, double* L, int d, int32_t* status, cudaStream_t s);
+cudaError_t launch_pack_lt(const double* L, float* out, int d, int tri, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
+cudaError_t launch_mvn(const float* Lf, int tri, const float* mean, float* X, int d, int64_t n, cudaStream_t s);
+cudaError_t launch_mvn_f64(const double* L, int tri, const double* mean, double* X, int d, int64_t n, cudaStream_t s);
+size_t wishart_smem(int d, int dtype);
+cudaError_t launch_wishart(const void* normals, const void* chis, const void* chol, void* out, int d, int64_t samples,
+                           int inverse, int dtype, cudaStream_t s);
+size_t dirichlet_smem(int K, int dtype);
+cudaError_t launch_dirichlet(const void* rows, void* out, int K, int64_t n, int dtype, cudaStream_t s);
+cudaError_t launch_multinomial(const Plan& p, const MnArgs& a, const CallSnap* snap, cudaStream_t s);
+
+// Host side (gr_api.cu): DiscreteGen's CDF / alias table (Discrete.h:23-207).
+gr_status build_discrete_table(const std::vector<double>& w, std::vector<int32_t>& prob, std::vector<int32_t>& alias,
+                               int& ncdf, uint32_t& bitmask);
+// Host side (gr_api.cu): plans and launches k_multinomial on an engine, with
+// the same slice / jump-segment split as the fixed-consumption samplers.
+gr_status run_multinomial(gr_engine* e, GenState* gst, const MnArgs& a, int64_t samples, cudaStream_t s);
+
+}  // namespace gr

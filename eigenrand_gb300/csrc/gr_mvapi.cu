@@ -1,0 +1,466 @@
+// C ABI of the multivariate generators (include/gpurand.h, EigenRand/MvDists).
+//
+// Each object owns the FP64 factor of its matrix (computed on the GPU at
+// creation), device copies of its parameters and the member generators whose
+// caches persist across calls.  A call issues the member generators' draws in
+// the reference's order (gr_generate on the caller's engine), then the
+// assembly kernels of gr_mv.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gpurand.h"
+#include "gr_internal.h"
+#include "gr_kernels.cuh"
+#include "gr_mv.cuh"
+
+using namespace gr;
+
+namespace {
+
+gr_status mv_fail(gr_status s, const std::string& m) { return set_last_error(s, m); }
+
+#define MV_CUDA(call)                                                                                 \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess) return set_last_error(GR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int packet_width(int dtype) { return dtype == GR_F32 ? 8 : 4; }
+size_t elem_size(int dtype) { return dtype == GR_F32 ? sizeof(float) : sizeof(double); }
+
+bool all_finite(const double* v, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+// RAII for the temporaries of one factorisation.
+struct DevBufs {
+  std::vector<void*> p;
+  cudaStream_t s = nullptr;
+  ~DevBufs() {
+    for (void* q : p) cudaFree(q);
+    if (s) cudaStreamDestroy(s);
+  }
+  template <class T>
+  cudaError_t alloc(T** out, size_t n) {
+    cudaError_t e = cudaMalloc((void**)out, sizeof(T) * n);
+    if (e == cudaSuccess) p.push_back(*out);
+    return e;
+  }
+};
+
+// The factor get_lt (MvNormal.h:21-38) computes, in FP64 on the GPU:
+// Cholesky of the lower triangle, else V diag(sqrt(max(lambda, 0))) of the
+// symmetric matrix the lower triangle defines.  invert: factor of matrix^-1
+// (InvWishartGen, MvNormal.h:387-391).  GR_MATRIX_LOWER: the matrix is the
+// factor.  *tri = 1 when the factor is lower triangular.
+gr_status factor_f64(int d, const double* host, int form, bool invert, double** out_dev, int* tri) {
+  const size_t dd = (size_t)d * d;
+  std::vector<double> h(host, host + dd);
+  double* L = nullptr;
+  MV_CUDA(cudaMalloc(&L, sizeof(double) * dd));
+  if (form == GR_MATRIX_LOWER) {
+    int is_tri = 1;
+    for (int c = 0; c < d; ++c)
+      for (int r = 0; r < c; ++r)
+        if (h[(size_t)c * d + r] != 0.0) is_tri = 0;
+    cudaError_t e = cudaMemcpy(L, h.data(), sizeof(double) * dd, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(L);
+      return mv_fail(GR_ERR_CUDA, std::string("factor upload: ") + cudaGetErrorString(e));
+    }
+    *out_dev = L;
+    *tri = is_tri;
+    return GR_OK;
+  }
+  DevBufs b;
+  b.p.push_back(L);  // freed on error; released below on success
+  double *A = nullptr, *W = nullptr;
+  int32_t* status = nullptr;
+  MV_CUDA(b.alloc(&A, dd));
+  MV_CUDA(b.alloc(&W, dd));
+  MV_CUDA(b.alloc(&status, 1));
+  MV_CUDA(cudaStreamCreateWithFlags(&b.s, cudaStreamNonBlocking));
+  int32_t hs = 0;
+  MV_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), b.s));
+  if (invert) {
+    MV_CUDA(cudaMemcpyAsync(A, h.data(), sizeof(double) * dd, cudaMemcpyHostToDevice, b.s));
+    MV_CUDA(launch_inverse_f64(A, W, d, status, b.s));
+    MV_CUDA(cudaMemcpyAsync(h.data(), A, sizeof(double) * dd, cudaMemcpyDeviceToHost, b.s));
+    MV_CUDA(cudaMemcpyAsync(&hs, status, sizeof(int32_t), cudaMemcpyDeviceToHost, b.s));
+    MV_CUDA(cudaStreamSynchronize(b.s));
+    if (hs & 1) return mv_fail(GR_ERR_NOT_PD, "the scale matrix is singular");
+  }
+  // LLT and SelfAdjointEigenSolver read the lower triangle only
+  for (int c = 0; c < d; ++c)
+    for (int r = 0; r < c; ++r) h[(size_t)c * d + r] = h[(size_t)r * d + c];
+  MV_CUDA(cudaMemcpyAsync(A, h.data(), sizeof(double) * dd, cudaMemcpyHostToDevice, b.s));
+  MV_CUDA(launch_chol_f64(A, d, status, b.s));
+  MV_CUDA(cudaMemcpyAsync(&hs, status, sizeof(int32_t), cudaMemcpyDeviceToHost, b.s));
+  MV_CUDA(cudaStreamSynchronize(b.s));
+  if (!(hs & 2)) {
+    MV_CUDA(cudaMemcpyAsync(L, A, sizeof(double) * dd, cudaMemcpyDeviceToDevice, b.s));
+    *tri = 1;
+  } else {
+    MV_CUDA(cudaMemsetAsync(status, 0, sizeof(int32_t), b.s));
+    MV_CUDA(cudaMemcpyAsync(A, h.data(), sizeof(double) * dd, cudaMemcpyHostToDevice, b.s));
+    MV_CUDA(launch_jacobi_f64(A, W, L, d, status, b.s));
+    MV_CUDA(cudaMemcpyAsync(&hs, status, sizeof(int32_t), cudaMemcpyDeviceToHost, b.s));
+    MV_CUDA(cudaStreamSynchronize(b.s));
+    if (hs & 4) return mv_fail(GR_ERR_NOT_PD, "The matrix cannot be solved! (eigen decomposition did not converge)");
+    *tri = 0;
+  }
+  MV_CUDA(cudaStreamSynchronize(b.s));
+  b.p.erase(b.p.begin());  // keep L
+  *out_dev = L;
+  return GR_OK;
+}
+
+gr_status make_gen(gr_gen** out, int kind, int dtype, double a, double b = 0.0) {
+  gr_dist_desc d{};
+  d.kind = kind;
+  d.dtype = dtype;
+  d.a = a;
+  d.b = b;
+  return gr_gen_create(out, &d);
+}
+
+// device scratch owned by an object, grown on demand
+struct Scratch {
+  void* p = nullptr;
+  size_t bytes = 0;
+  gr_status need(size_t n) {
+    if (n <= bytes) return GR_OK;
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) return mv_fail(GR_ERR_NOMEM, std::string("scratch: ") + cudaGetErrorString(e));
+    bytes = n;
+    return GR_OK;
+  }
+  ~Scratch() { cudaFree(p); }
+};
+
+}  // namespace
+
+struct gr_mvnormal {
+  int dim = 0, dtype = GR_F32, tri = 1;
+  double* L64 = nullptr;
+  float* Lf = nullptr;  // packed float fragments (float objects)
+  void* mean = nullptr;
+  gr_gen* normal = nullptr;
+};
+
+struct gr_wishart {
+  int dim = 0, dtype = GR_F32, inverse = 0;
+  int64_t df = 0;
+  double* L64 = nullptr;
+  void* chol = nullptr;  // factor in the object's type (aliases L64 for double)
+  gr_gen* normal = nullptr;
+  std::vector<gr_gen*> chis;
+  Scratch scratch;
+};
+
+struct gr_dirichlet {
+  int dim = 0, dtype = GR_F32;
+  std::vector<gr_gen*> gammas;
+  Scratch scratch;
+};
+
+struct gr_multinomial {
+  int dim = 0, trials = 0;
+  int32_t* table = nullptr;  // prob (or CDF) then alias
+  int32_t ncdf = 0;
+  uint32_t bitmask = 0;
+  size_t nprob = 0;
+  GenState* gst = nullptr;
+  int gst_K = 0;
+};
+
+extern "C" {
+
+// ---------------------------------------------------------------- MvNormalGen
+gr_status gr_mvnormal_destroy(gr_mvnormal* g) {
+  if (!g) return GR_OK;
+  cudaFree(g->L64);
+  cudaFree(g->Lf);
+  cudaFree(g->mean);
+  gr_gen_destroy(g->normal);
+  delete g;
+  return GR_OK;
+}
+
+gr_status gr_mvnormal_create(gr_mvnormal** out, int32_t dtype, int32_t dim, const double* mean, const double* matrix,
+                             int32_t matrix_form) {
+  if (!out || !mean || !matrix) return mv_fail(GR_ERR_INVALID, "NULL argument");
+  if (dtype != GR_F32 && dtype != GR_F64) return mv_fail(GR_ERR_INVALID, "MvNormalGen needs a float or double type");
+  if (matrix_form != GR_MATRIX_FULL && matrix_form != GR_MATRIX_LOWER) return mv_fail(GR_ERR_INVALID, "bad matrix form");
+  if (dim < 1) return mv_fail(GR_ERR_INVALID, "dim must be >= 1");
+  if (dtype == GR_F32 && dim > kMvMaxDim) return mv_fail(GR_ERR_UNSUPPORTED, "float MvNormalGen: dim <= 2048");
+  if (dtype == GR_F64 && (size_t)32 * dim * sizeof(double) > kMvMaxSmem)
+    return mv_fail(GR_ERR_UNSUPPORTED, "double MvNormalGen: dim <= 800");
+  if (!all_finite(mean, dim) || !all_finite(matrix, (size_t)dim * dim))
+    return mv_fail(GR_ERR_INVALID, "non-finite mean or matrix");
+  gr_mvnormal* g = new gr_mvnormal;
+  g->dim = dim;
+  g->dtype = dtype;
+  gr_status st = factor_f64(dim, matrix, matrix_form, false, &g->L64, &g->tri);
+  if (st == GR_OK) {
+    cudaError_t e = cudaSuccess;
+    if (dtype == GR_F32) {
+      const int MT = (dim + 15) / 16, KS = (dim + 7) / 8;
+      const int64_t nfr = g->tri ? mv_tri_frags(MT, KS) : (int64_t)MT * KS;
+      e = cudaMalloc(&g->Lf, sizeof(float) * (size_t)nfr * 128);
+      if (e == cudaSuccess) e = launch_pack_lt(g->L64, g->Lf, dim, g->tri, nullptr);
+      std::vector<float> mf(mean, mean + dim);
+      if (e == cudaSuccess) e = cudaMalloc(&g->mean, sizeof(float) * dim);
+      if (e == cudaSuccess) e = cudaMemcpy(g->mean, mf.data(), sizeof(float) * dim, cudaMemcpyHostToDevice);
+    } else {
+      e = cudaMalloc(&g->mean, sizeof(double) * dim);
+      if (e == cudaSuccess) e = cudaMemcpy(g->mean, mean, sizeof(double) * dim, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) st = mv_fail(GR_ERR_CUDA, std::string("MvNormalGen set-up: ") + cudaGetErrorString(e));
+  }
+  if (st == GR_OK) st = make_gen(&g->normal, GR_NORMAL_STD, dtype, 0.0);
+  if (st != GR_OK) {
+    gr_mvnormal_destroy(g);
+    return st;
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_mvnormal_sample(gr_mvnormal* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (samples == 0) return GR_OK;
+  if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  const size_t n = (size_t)g->dim * samples;
+  if (n % (size_t)packet_width(g->dtype))
+    return mv_fail(GR_ERR_INVALID, "dim * samples must be a multiple of the packet width");
+  cudaStream_t s = (cudaStream_t)stream;
+  // Z = StdNormalGen draws (dim x samples), then X = L Z + mean in place
+  gr_status st = gr_generate(g->normal, e, dev_out, n, stream);
+  if (st != GR_OK) return st;
+  cudaError_t err = g->dtype == GR_F32
+                        ? launch_mvn(g->Lf, g->tri, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples, s)
+                        : launch_mvn_f64(g->L64, g->tri, (const double*)g->mean, (double*)dev_out, g->dim,
+                                         (int64_t)samples, s);
+  if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("MvNormal product: ") + cudaGetErrorString(err));
+  return GR_OK;
+}
+
+// ---------------------------------------------------------------- Wishart / InvWishart
+gr_status gr_wishart_destroy(gr_wishart* g) {
+  if (!g) return GR_OK;
+  if (g->chol != g->L64) cudaFree(g->chol);
+  cudaFree(g->L64);
+  gr_gen_destroy(g->normal);
+  for (gr_gen* c : g->chis) gr_gen_destroy(c);
+  delete g;
+  return GR_OK;
+}
+
+gr_status gr_wishart_create(gr_wishart** out, int32_t dtype, int32_t dim, int64_t df, const double* matrix,
+                            int32_t matrix_form, int32_t inverse) {
+  if (!out || !matrix) return mv_fail(GR_ERR_INVALID, "NULL argument");
+  if (dtype != GR_F32 && dtype != GR_F64) return mv_fail(GR_ERR_INVALID, "WishartGen needs a float or double type");
+  if (matrix_form != GR_MATRIX_FULL && matrix_form != GR_MATRIX_LOWER) return mv_fail(GR_ERR_INVALID, "bad matrix form");
+  if (dim < 1) return mv_fail(GR_ERR_INVALID, "dim must be >= 1");
+  if (df <= dim - 1) return mv_fail(GR_ERR_INVALID, "df must be > dim - 1");
+  if (wishart_smem(dim, dtype) > kMvMaxSmem) return mv_fail(GR_ERR_UNSUPPORTED, "Wishart dimension too large");
+  if (!all_finite(matrix, (size_t)dim * dim)) return mv_fail(GR_ERR_INVALID, "non-finite matrix");
+  gr_wishart* g = new gr_wishart;
+  g->dim = dim;
+  g->dtype = dtype;
+  g->df = df;
+  g->inverse = inverse ? 1 : 0;
+  int tri = 0;
+  gr_status st = factor_f64(dim, matrix, matrix_form, g->inverse && matrix_form == GR_MATRIX_FULL, &g->L64, &tri);
+  if (st == GR_OK) {
+    if (dtype == GR_F64) {
+      g->chol = g->L64;
+    } else {
+      cudaError_t e = cudaMalloc(&g->chol, sizeof(float) * (size_t)dim * dim);
+      if (e == cudaSuccess) e = launch_f64_to_f32(g->L64, (float*)g->chol, (int64_t)dim * dim, nullptr);
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) st = mv_fail(GR_ERR_CUDA, std::string("WishartGen set-up: ") + cudaGetErrorString(e));
+    }
+  }
+  if (st == GR_OK) st = make_gen(&g->normal, GR_NORMAL_STD, dtype, 0.0);
+  for (int i = 0; st == GR_OK && i < dim; ++i) {  // ChiSquaredGen(df - i)
+    gr_gen* c = nullptr;
+    st = make_gen(&c, GR_CHI_SQUARED, dtype, (double)(df - i));
+    if (st == GR_OK) g->chis.push_back(c);
+  }
+  if (st != GR_OK) {
+    gr_wishart_destroy(g);
+    return st;
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_wishart_sample(gr_wishart* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (samples == 0) return GR_OK;
+  if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  const int d = g->dim;
+  const size_t P = (size_t)packet_width(g->dtype);
+  const size_t nnorm = samples * (size_t)d * (size_t)(d - 1) / 2;
+  if (samples % P || nnorm % P)
+    return mv_fail(GR_ERR_INVALID, "samples and samples * dim * (dim - 1) / 2 must be multiples of the packet width");
+  const size_t es = elem_size(g->dtype);
+  gr_status st = g->scratch.need((nnorm + (size_t)d * samples) * es);
+  if (st != GR_OK) return st;
+  char* normals = (char*)g->scratch.p;
+  char* chis = normals + nnorm * es;
+  // draw order of WishartGen::generate: all normals, then one chi^2 row per diagonal
+  if (nnorm) {
+    st = gr_generate(g->normal, e, normals, nnorm, stream);
+    if (st != GR_OK) return st;
+  }
+  for (int i = 0; i < d; ++i) {
+    st = gr_generate(g->chis[i], e, chis + (size_t)i * samples * es, samples, stream);
+    if (st != GR_OK) return st;
+  }
+  cudaError_t err = launch_wishart(normals, chis, g->chol, dev_out, d, (int64_t)samples, g->inverse, g->dtype,
+                                   (cudaStream_t)stream);
+  if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("Wishart products: ") + cudaGetErrorString(err));
+  return GR_OK;
+}
+
+// ---------------------------------------------------------------- DirichletGen
+gr_status gr_dirichlet_destroy(gr_dirichlet* g) {
+  if (!g) return GR_OK;
+  for (gr_gen* x : g->gammas) gr_gen_destroy(x);
+  delete g;
+  return GR_OK;
+}
+
+gr_status gr_dirichlet_create(gr_dirichlet** out, int32_t dtype, int32_t dim, const double* alpha) {
+  if (!out || !alpha) return mv_fail(GR_ERR_INVALID, "NULL argument");
+  if (dtype != GR_F32 && dtype != GR_F64) return mv_fail(GR_ERR_INVALID, "DirichletGen needs a float or double type");
+  if (dim < 1) return mv_fail(GR_ERR_INVALID, "dim must be >= 1");
+  if (dirichlet_smem(dim, dtype) > kMvMaxSmem) return mv_fail(GR_ERR_UNSUPPORTED, "Dirichlet dimension too large");
+  for (int i = 0; i < dim; ++i)
+    if (!(alpha[i] > 0) || !std::isfinite(alpha[i])) return mv_fail(GR_ERR_INVALID, "alpha must be > 0");
+  gr_dirichlet* g = new gr_dirichlet;
+  g->dim = dim;
+  g->dtype = dtype;
+  gr_status st = GR_OK;
+  for (int i = 0; st == GR_OK && i < dim; ++i) {  // GammaGen(alpha[i]) per category
+    gr_gen* x = nullptr;
+    st = make_gen(&x, GR_GAMMA, dtype, alpha[i], 1.0);
+    if (st == GR_OK) g->gammas.push_back(x);
+  }
+  if (st != GR_OK) {
+    gr_dirichlet_destroy(g);
+    return st;
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_dirichlet_sample(gr_dirichlet* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (samples == 0) return GR_OK;
+  if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  if (samples % (size_t)packet_width(g->dtype)) return mv_fail(GR_ERR_INVALID, "samples must be a multiple of the packet width");
+  const size_t es = elem_size(g->dtype);
+  gr_status st = g->scratch.need((size_t)g->dim * samples * es);
+  if (st != GR_OK) return st;
+  char* rows = (char*)g->scratch.p;
+  for (int i = 0; i < g->dim; ++i) {
+    st = gr_generate(g->gammas[i], e, rows + (size_t)i * samples * es, samples, stream);
+    if (st != GR_OK) return st;
+  }
+  cudaError_t err = launch_dirichlet(rows, dev_out, g->dim, (int64_t)samples, g->dtype, (cudaStream_t)stream);
+  if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("Dirichlet normalisation: ") + cudaGetErrorString(err));
+  return GR_OK;
+}
+
+// ---------------------------------------------------------------- MultinomialGen
+gr_status gr_multinomial_destroy(gr_multinomial* g) {
+  if (!g) return GR_OK;
+  cudaFree(g->table);
+  cudaFree(g->gst);
+  delete g;
+  return GR_OK;
+}
+
+gr_status gr_multinomial_create(gr_multinomial** out, int32_t dim, int32_t trials, const double* weights) {
+  if (!out || !weights) return mv_fail(GR_ERR_INVALID, "NULL argument");
+  if (dim < 1) return mv_fail(GR_ERR_INVALID, "dim must be >= 1");
+  if (trials < 0) return mv_fail(GR_ERR_INVALID, "trials must be >= 0");
+  for (int i = 0; i < dim; ++i)
+    if (!(weights[i] >= 0)) return mv_fail(GR_ERR_INVALID, "weights must be >= 0");
+  if ((int64_t)trials >= std::max<int64_t>(30 * (int64_t)(dim - 1), 100))
+    return mv_fail(GR_ERR_UNSUPPORTED, "the conditional-binomial multinomial path (trials >= max(30 (dim - 1), 100))");
+  const MnLayout L = mn_layout(trials, 0);
+  if (L.W0 > kMnMaxSampleWords || L.W1 > kMnMaxSampleWords)
+    return mv_fail(GR_ERR_UNSUPPORTED, "multinomial: trials above 2400");
+  if ((size_t)5 * dim * sizeof(int32_t) > 160 * 1024) return mv_fail(GR_ERR_UNSUPPORTED, "multinomial: dim too large");
+  std::vector<double> w(weights, weights + dim);
+  std::vector<int32_t> prob, alias;
+  int ncdf = 0;
+  uint32_t mask = 0;
+  gr_status st = build_discrete_table(w, prob, alias, ncdf, mask);
+  if (st != GR_OK) return st;
+  gr_multinomial* g = new gr_multinomial;
+  g->dim = dim;
+  g->trials = trials;
+  g->ncdf = ncdf;
+  g->bitmask = mask;
+  g->nprob = prob.size();
+  std::vector<int32_t> both(prob);
+  both.insert(both.end(), alias.begin(), alias.end());
+  both.push_back(0);
+  cudaError_t e = cudaMalloc(&g->table, sizeof(int32_t) * both.size());
+  if (e == cudaSuccess) e = cudaMemcpy(g->table, both.data(), sizeof(int32_t) * both.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    gr_multinomial_destroy(g);
+    return mv_fail(GR_ERR_CUDA, std::string("multinomial table: ") + cudaGetErrorString(e));
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_out, size_t samples,
+                                gr_stream_t stream) {
+  if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (samples == 0) return GR_OK;
+  if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (g->trials == 0) {  // no draws: every count is 0
+    MV_CUDA(cudaMemsetAsync(dev_out, 0, sizeof(int32_t) * (size_t)g->dim * samples, s));
+    return GR_OK;
+  }
+  const int K = gr_engine_streams(e);
+  if (g->gst_K != K) {  // DiscreteGen cache per engine stream
+    cudaFree(g->gst);
+    g->gst = nullptr;
+    g->gst_K = 0;
+    MV_CUDA(cudaMalloc(&g->gst, sizeof(GenState) * (size_t)K));
+    MV_CUDA(cudaMemset(g->gst, 0, sizeof(GenState) * (size_t)K));
+    g->gst_K = K;
+  }
+  MnArgs a{};
+  a.prob = g->table;
+  a.alias = g->table + g->nprob;
+  a.bitmask = g->bitmask;
+  a.ncdf = g->ncdf;
+  a.dim = g->dim;
+  a.trials = g->trials;
+  a.out = dev_out;
+  return run_multinomial(e, g->gst, a, (int64_t)samples, s);
+}
+
+}  // extern "C"

@@ -149,6 +149,67 @@ typedef struct {
 } gr_batch_desc;
 gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* batch, gr_stream_t stream);
 
+/* ---- multivariate generators (EigenRand/MvDists) -------------------------
+ * Each object mirrors one Mv*Gen instance: its parameters, the FP64 factor of
+ * its covariance / scale matrix (computed on the GPU at creation), and the
+ * member generators whose caches persist between calls (StdNormalGen,
+ * ChiSquaredGen per diagonal, GammaGen per category, DiscreteGen).  Host
+ * matrices are column-major dim x dim doubles; outputs are device buffers in
+ * the reference's layout:  *_sample(..., samples) == generate(urng, samples).
+ * The draws use the engine exactly as the reference's member generators do,
+ * so the normal / chi-squared / gamma / discrete streams are the reference's;
+ * the linear algebra after them is float (FP64 for GR_F64 objects).
+ * Creation synchronises the device; the first call of a given size may
+ * allocate scratch, so make it before any stream capture. */
+typedef struct gr_mvnormal gr_mvnormal;
+typedef struct gr_wishart gr_wishart;
+typedef struct gr_dirichlet gr_dirichlet;
+typedef struct gr_multinomial gr_multinomial;
+
+/* matrix_form: how `matrix` is given (MvNormal.h:42-46 tags) */
+typedef enum {
+  GR_MATRIX_FULL = 0,  /* covariance / scale matrix: factored by get_lt (MvNormal.h:21-38):
+                          Cholesky, or V sqrt(max(lambda, 0)) when it is not positive definite */
+  GR_MATRIX_LOWER = 1  /* already the factor: lower_triangular (MvNormalGen, WishartGen) or
+                          inv_lower_triangular (InvWishartGen: factor of the inverse scale) */
+} gr_matrix_form;
+
+/* MvNormalGen<float|double>(mean, matrix[, lower_triangular]) (MvNormal.h:56-116).
+ * sample: dev_out = dim x samples column-major, X = L Z + mean with Z the
+ * generator's StdNormalGen draws of dim * samples values (a multiple of the
+ * packet width: 8 for float, 4 for double).  Float: L Z on the tensor cores
+ * as 3xTF32 with FP32 accumulation; dim <= 2048 (float), <= 800 (double). */
+gr_status gr_mvnormal_create(gr_mvnormal** out, int32_t dtype, int32_t dim, const double* mean, const double* matrix,
+                             int32_t matrix_form);
+gr_status gr_mvnormal_sample(gr_mvnormal* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream);
+gr_status gr_mvnormal_destroy(gr_mvnormal* g);
+
+/* WishartGen (inverse = 0, MvNormal.h:185-277) / InvWishartGen (inverse = 1,
+ * :347-442) with df > dim - 1.  sample: dev_out = dim x (dim * samples)
+ * column-major (draw j in columns j*dim ..).  samples and
+ * samples * dim * (dim - 1) / 2 must be multiples of the packet width.
+ * Float and dim <= 128: Bartlett products on the tensor cores (3xTF32). */
+gr_status gr_wishart_create(gr_wishart** out, int32_t dtype, int32_t dim, int64_t df, const double* matrix,
+                            int32_t matrix_form, int32_t inverse);
+gr_status gr_wishart_sample(gr_wishart* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream);
+gr_status gr_wishart_destroy(gr_wishart* g);
+
+/* DirichletGen(alpha) (Multinomial.h:160-204), alpha[i] > 0.  sample:
+ * dev_out = dim x samples column-major; samples a multiple of the packet width. */
+gr_status gr_dirichlet_create(gr_dirichlet** out, int32_t dtype, int32_t dim, const double* alpha);
+gr_status gr_dirichlet_sample(gr_dirichlet* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream);
+gr_status gr_dirichlet_destroy(gr_dirichlet* g);
+
+/* MultinomialGen<int32_t>(trials, weights) (Multinomial.h:25-118), weights
+ * >= 0.  sample: dev_out = int32 dim x samples column-major, bit-exact with
+ * the reference.  Implemented for trials < max(30 (dim - 1), 100) (the
+ * reference's per-trial DiscreteGen path) with trials <= 2400; the
+ * conditional-binomial path above that returns GR_ERR_UNSUPPORTED. */
+gr_status gr_multinomial_create(gr_multinomial** out, int32_t dim, int32_t trials, const double* weights);
+gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_out, size_t samples,
+                                gr_stream_t stream);
+gr_status gr_multinomial_destroy(gr_multinomial* g);
+
 const char* gr_last_error(void);
 const char* gr_version(void);
 

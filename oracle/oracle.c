@@ -886,6 +886,55 @@ int or_gen_discrete(or_vmt* e, or_gen* g, const or_discrete* d, int32_t* out, si
 }
 
 /* ======================================================================
+ * MultinomialGen<int32_t>::generate(urng, samples) on the per-trial path
+ * (trials < max(30 (dim - 1), 100); Multinomial.h:62-71, 95-118).  Per
+ * sample, the DiscreteGen member draws 16 categories at a time through its
+ * packet operator (a Matrix<int32_t, 16, 1> assignment), then the trials % 16
+ * tail: its whole packets of 4 first, then trials % 4 draws through the
+ * scalar operator() (Discrete.h:420-441).  A scalar draw takes one full
+ * rng() packet, uses its first 32-bit word and leaves the packet cache alone.
+ * Counts go to out[s * dim + category].
+ * ====================================================================== */
+static int32_t discrete_scalar(or_vmt* e, const or_discrete* d) {
+  uint32_t rx[8];
+  draw_full(e, rx);
+  const int32_t x = (int32_t)rx[0];
+  if (d->use_cdf) { /* std::lower_bound over the uint32 cdf[0 .. n-2] */
+    const uint32_t v = (uint32_t)(x & 0x7fffffff);
+    int32_t r = 0;
+    for (int i = 0; i < d->n - 1; ++i) r += (d->cdf[i] < v) ? 1 : 0;
+    return r;
+  }
+  const int32_t albit = x & (int32_t)d->bitmask;
+  const uint32_t alx = (uint32_t)(x >> 1); /* arithmetic shift of the signed draw */
+  return alx < (uint32_t)d->prob[albit] ? albit : d->alias[albit];
+}
+
+int or_gen_multinomial(or_vmt* e, or_gen* g, const or_discrete* d, int32_t trials, int32_t dim, int32_t* out,
+                       size_t samples) {
+  if (e->L != 4 || trials < 0) return 2;
+  int32_t buf[16];
+  for (size_t s = 0; s < samples; ++s) {
+    int32_t* h = out + s * (size_t)dim;
+    memset(h, 0, sizeof(int32_t) * (size_t)dim);
+    int32_t i = 0;
+    for (; i + 16 <= trials; i += 16) {
+      int rc = or_gen_discrete(e, g, d, buf, 16);
+      if (rc) return rc;
+      for (int j = 0; j < 16; ++j) h[buf[j]] += 1;
+    }
+    const int32_t r = trials - i, q = r / 4;
+    if (q) {
+      int rc = or_gen_discrete(e, g, d, buf, (size_t)(4 * q));
+      if (rc) return rc;
+      for (int j = 0; j < 4 * q; ++j) h[buf[j]] += 1;
+    }
+    for (int j = 4 * q; j < r; ++j) h[discrete_scalar(e, d)] += 1;
+  }
+  return 0;
+}
+
+/* ======================================================================
  * BinomialVGen<int32_t>::packetOp (Discrete.h:1124-1192), one packet of 4
  * lanes whose (trials, p) may differ per lane.  Lanes with mean < 1 run the
  * multiplicative Poisson loop; the others a tan-proposal rejection with a

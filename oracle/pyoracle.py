@@ -56,6 +56,8 @@ def lib():
         L.or_discrete_table.restype = ctypes.c_int
         L.or_gen_discrete.argtypes = [vp, vp, vp, vp, sz]
         L.or_gen_discrete.restype = ctypes.c_int
+        L.or_gen_multinomial.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
+        L.or_gen_multinomial.restype = ctypes.c_int
         L.or_vop_set.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                  vp, sz]
         L.or_vop_set.restype = ctypes.c_int
@@ -145,6 +147,89 @@ def generate(eng, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0, weight
     if rc != 0:
         raise RuntimeError(f"oracle error {rc} for {kind}")
     return out
+
+
+def multinomial(eng, gen, weights, trials, samples):
+    """MultinomialGen<int32_t>(trials, weights).generate(urng, samples) on the
+    per-trial path (Multinomial.h:62-71, 95-118).  Returns (samples, dim):
+    row s = column s of the reference's (dim, samples) matrix."""
+    L = lib()
+    w = np.asarray(weights, dtype=np.float64)
+    d = L.or_discrete_new(_p(w), len(w))
+    out = np.empty((samples, len(w)), dtype=np.int32)
+    rc = L.or_gen_multinomial(eng.h, gen.ptr, d, int(trials), len(w), _p(out), samples)
+    L.or_discrete_free(d)
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return out
+
+
+def discrete_table(weights):
+    """DiscreteGen's table (Discrete.h:23-207): ("cdf", cdf) or ("alias", prob, alias, bitmask)."""
+    L = lib()
+    w = np.asarray(weights, dtype=np.float64)
+    d = L.or_discrete_new(_p(w), len(w))
+    prob = np.zeros(1 << 16, np.int32)
+    alias = np.zeros(1 << 16, np.int32)
+    ps = L.or_discrete_table(d, _p(prob), _p(alias), len(prob))
+    L.or_discrete_free(d)
+    if ps < 0:
+        return ("cdf", prob[:-ps].astype(np.uint32))
+    return ("alias", prob[:ps].copy(), alias[:ps].copy(), ps - 1)
+
+
+# ---- FP64 restatements of the multivariate assembly (the error oracle) ----
+def get_lt(matrix):
+    """MvNormal.h:21-38 in FP64: Cholesky of the matrix the lower triangle
+    defines, else eigenvectors * sqrt(max(eigenvalues, 0))."""
+    a = np.asarray(matrix, dtype=np.float64)
+    a = np.tril(a) + np.tril(a, -1).T
+    try:
+        return np.linalg.cholesky(a)
+    except np.linalg.LinAlgError:
+        w, v = np.linalg.eigh(a)
+        return v * np.sqrt(np.maximum(w, 0.0))
+
+
+def mvnormal_f64(lt, z, mean):
+    """MvNormalGen::generate (MvNormal.h:103-108): lt @ Z + mean, Z (dim, samples)."""
+    return np.asarray(lt, np.float64) @ np.asarray(z, np.float64) + np.asarray(mean, np.float64)[:, None]
+
+
+def bartlett(normals, chis, dim, samples):
+    """The per-draw Bartlett matrices of WishartGen::generate (MvNormal.h:236-262):
+    strictly-lower normals column by column, sqrt(chi^2) on the diagonal.
+    normals: samples * dim (dim-1) / 2 values; chis: (dim, samples)."""
+    nper = dim * (dim - 1) // 2
+    A = np.zeros((samples, dim, dim))
+    nz = np.asarray(normals, np.float64).reshape(samples, nper)
+    ptr = 0
+    for i in range(dim - 1):
+        A[:, i + 1:, i] = nz[:, ptr:ptr + dim - 1 - i]
+        ptr += dim - 1 - i
+    ch = np.sqrt(np.asarray(chis, np.float64))
+    for i in range(dim):
+        A[:, i, i] = ch[i]
+    return A
+
+
+def wishart_f64(chol, normals, chis, dim, samples, inverse=False):
+    """WishartGen (MvNormal.h:263-276) / InvWishartGen (:427-440) in FP64.
+    Returns (dim, dim * samples) like the reference."""
+    A = bartlett(normals, chis, dim, samples)
+    T = np.asarray(chol, np.float64)[None] @ A
+    if inverse:
+        U = np.linalg.inv(np.tril(T))
+        W = np.transpose(U, (0, 2, 1)) @ U
+    else:
+        W = T @ np.transpose(T, (0, 2, 1))
+    return np.concatenate(list(W), axis=1)
+
+
+def dirichlet_f64(rows):
+    """DirichletGen::generate (Multinomial.h:190-203): column-normalised gamma rows."""
+    r = np.asarray(rows, np.float64)
+    return r / r.sum(axis=0, keepdims=True)
 
 
 def vop_set(seed, kind, count, a=0.0, b=1.0, trials=0):
