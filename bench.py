@@ -288,8 +288,150 @@ def run_ours(args, rank, world):
         "gpu_launches": launches_per_call * len(items) * args.steps,
         "clocks": clk,
     }
+    if not args.no_extras:
+        del outs, host
+        torch.cuda.empty_cache()
+        res["workloads"] = {"batched_vop": bench_batched(er), "multivariate": bench_multivariate(er)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
+    return res
+
+
+# --------------------------------------------------------------------------- other workloads
+def _median_ms(fn, reps=3, warm=1):
+    """Median device time of fn() in ms (CUDA events on the current stream)."""
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    st = torch.cuda.current_stream()
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn()
+        e1.record(st)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def bench_batched(er, nsets=1_000_000, percall_sets=2048):
+    """Batched vectorize-over-params: 10^6 sets in one launch (captured in a
+    CUDA graph, CTA width from the library's autotuner) against the plain
+    per-call path (one gr_sample_batched call per set, the same values)."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(7)
+    counts = rng.integers(1, 4097, nsets).astype(np.int32)
+    res = {}
+    for kind in ("GAMMA", "BINOMIAL_V"):
+        if kind == "GAMMA":
+            a = (10.0 ** rng.uniform(-1, 2, nsets)).astype(np.float32)
+            b = np.ones(nsets, np.float32)
+            t = None
+        else:
+            a = rng.uniform(0, 1, nsets).astype(np.float32)
+            b = None
+            t = rng.integers(1, 1001, nsets).astype(np.int32)
+        tc = torch.from_numpy(counts).cuda()
+        ta = torch.from_numpy(a).cuda()
+        tb = torch.from_numpy(b).cuda() if b is not None else None
+        tt = torch.from_numpy(t).cuda() if t is not None else None
+        out, off = er.sample_batched(kind, tc, ta, tb, tt, seed=7)  # first call autotunes
+        torch.cuda.synchronize()
+        total = int(counts.astype(np.int64).sum())
+        s = torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            er.sample_batched(kind, tc, ta, tb, tt, seed=7, out=out, offsets=off, stream=s)
+            s.synchronize()
+            with torch.cuda.graph(g, stream=s):
+                er.sample_batched(kind, tc, ta, tb, tt, seed=7, out=out, offsets=off, stream=s)
+        torch.cuda.synchronize()
+        ms = _median_ms(g.replay)
+        # plain per-call path on the first sets
+        M = percall_sets
+        outs1 = torch.empty(4096 + 8, dtype=out.dtype, device="cuda")
+        off1 = torch.zeros(1, dtype=torch.int64, device="cuda")
+        one = [(tc[i:i + 1], ta[i:i + 1], None if tb is None else tb[i:i + 1], None if tt is None else tt[i:i + 1])
+               for i in range(M)]
+
+        def percall():
+            for i in range(M):
+                c, aa, bb, trr = one[i]
+                er.sample_batched(kind, c, aa, bb, trr, seed=7 + 4 * i, out=outs1, offsets=off1)
+        ms1 = _median_ms(percall, reps=2)
+        m_samples = int(counts[:M].astype(np.int64).sum())
+        res[kind.lower()] = {
+            "sets": nsets, "samples": total, "batched_ms": round(ms, 3),
+            "batched_gsamples_s": round(total / (ms / 1e3) / 1e9, 3),
+            "batched_gbs_out": round(total * 4 / (ms / 1e3) / 1e9, 1),
+            "percall_sets_timed": M, "percall_ms": round(ms1, 3),
+            "percall_gsamples_s": round(m_samples / (ms1 / 1e3) / 1e9, 4),
+            "speedup_batched_vs_percall": round((total / ms) / (m_samples / ms1), 1),
+        }
+        del out, g
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return res
+
+
+def bench_multivariate(er, streams=608):
+    """MvNormal d in {16, 64, 256} (N = 10^6), Wishart d=32 df=40 (10^5 draws),
+    Dirichlet K=64 (10^6), Multinomial K=100 trials=1000 (10^6); float32."""
+    import numpy as np
+    import torch
+    urng = er.Vmt19937_64(99, streams=streams)
+    res = {}
+    N = 1_000_000
+    for d in (16, 64, 256):
+        rng = np.random.default_rng(99)
+        A = rng.standard_normal((d, d))
+        cov = A @ A.T + d * np.eye(d)
+        mean = rng.standard_normal(d)
+        g = er.MvNormalGen(mean, cov)
+        out = torch.empty((N, d), dtype=torch.float32, device="cuda").t()
+        ms = _median_ms(lambda: g.generate(urng, N, out=out))
+        z = er.StdNormalGen()
+        ms_z = _median_ms(lambda: z.generate(d, N, urng, out=out))
+        gemm = max(ms - ms_z, 1e-6)
+        res[f"mvnormal_d{d}"] = {
+            "samples": N, "ms": round(ms, 3), "msamples_s": round(N / ms / 1e3, 1),
+            "gbs_out": round(4 * d * N / (ms / 1e3) / 1e9, 1),
+            "normals_ms": round(ms_z, 3), "lz_ms": round(gemm, 3),
+            "lz_tflops_full": round(2 * d * d * N / (gemm / 1e3) / 1e12, 2),
+            "lz_bytes_gbs": round(8 * d * N / (gemm / 1e3) / 1e9, 1)}
+        del out
+    d, df, n = 32, 40, 100_000
+    rng = np.random.default_rng(99)
+    A = rng.standard_normal((d, d))
+    w = er.WishartGen(df, A @ A.T + d * np.eye(d))
+    out = torch.empty((d * n, d), dtype=torch.float32, device="cuda").t()
+    ms = _median_ms(lambda: w.generate(urng, n, out=out))
+    res["wishart_d32"] = {"draws": n, "ms": round(ms, 3), "kdraws_s": round(n / ms, 1),
+                          "gbs_out": round(4 * d * d * n / (ms / 1e3) / 1e9, 1)}
+    del out
+    K, n = 64, 1_000_000
+    alpha = np.random.default_rng(99).uniform(0.1, 2.0, K)
+    dg = er.DirichletGen(alpha)
+    out = torch.empty((n, K), dtype=torch.float32, device="cuda").t()
+    ms = _median_ms(lambda: dg.generate(urng, n, out=out))
+    res["dirichlet_k64"] = {"draws": n, "ms": round(ms, 3), "mdraws_s": round(n / ms / 1e3, 2),
+                            "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
+    del out
+    K, trials, n = 100, 1000, 1_000_000
+    p = np.random.default_rng(99).dirichlet(np.ones(K))
+    mg = er.MultinomialGen(trials, p)
+    out = torch.empty((n, K), dtype=torch.int32, device="cuda").t()
+    ms = _median_ms(lambda: mg.generate(urng, n, out=out))
+    res["multinomial_k100_t1000"] = {"draws": n, "ms": round(ms, 3), "mdraws_s": round(n / ms / 1e3, 2),
+                                     "alias_draws_g_s": round(n * trials / (ms / 1e3) / 1e9, 1),
+                                     "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
+    del out
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     return res
 
 
@@ -375,6 +517,8 @@ def main():
     ap.add_argument("--mode", default="streams", choices=["compat", "streams"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched, multivariate and serving workloads (extra keys of the JSON line)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))

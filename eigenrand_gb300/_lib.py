@@ -34,7 +34,38 @@ EXPORTS = [
     "gr_mvnormal_create", "gr_mvnormal_sample", "gr_mvnormal_destroy", "gr_wishart_create", "gr_wishart_sample",
     "gr_wishart_destroy", "gr_dirichlet_create", "gr_dirichlet_sample", "gr_dirichlet_destroy",
     "gr_multinomial_create", "gr_multinomial_sample", "gr_multinomial_destroy",
+    "gr_server_create", "gr_server_set_mvnormal", "gr_server_submit", "gr_server_progress", "gr_server_read",
+    "gr_server_release", "gr_server_pending", "gr_server_now", "gr_server_destroy",
 ]
+
+GR_SERVE_MVNORMAL = 64
+
+
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("client", ctypes.c_int32),
+        ("kind", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("trials", ctypes.c_int32),
+        ("a", ctypes.c_double),
+        ("b", ctypes.c_double),
+        ("count", ctypes.c_uint64),
+        ("arrival", ctypes.c_double),
+    ]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [
+        ("ticket", ctypes.c_uint64),
+        ("status", ctypes.c_int32),
+        ("client", ctypes.c_int32),
+        ("dev_out", ctypes.c_void_p),
+        ("count", ctypes.c_uint64),
+        ("bytes", ctypes.c_size_t),
+        ("arrival", ctypes.c_double),
+        ("admitted", ctypes.c_double),
+        ("completed", ctypes.c_double),
+    ]
 
 
 class BatchDesc(ctypes.Structure):
@@ -113,6 +144,15 @@ def load(path=None):
         "gr_multinomial_create": (i32, [ctypes.POINTER(vp), i32, i32, vp]),
         "gr_multinomial_sample": (i32, [vp, vp, vp, sz, vp]),
         "gr_multinomial_destroy": (i32, [vp]),
+        "gr_server_create": (i32, [ctypes.POINTER(vp), i32, vp, sz, i32]),
+        "gr_server_set_mvnormal": (i32, [vp, i32, vp, vp]),
+        "gr_server_submit": (i32, [vp, ctypes.POINTER(Request), ctypes.POINTER(u64)]),
+        "gr_server_progress": (i32, [vp, vp, sz, ctypes.POINTER(sz)]),
+        "gr_server_read": (i32, [vp, u64, vp, sz]),
+        "gr_server_release": (i32, [vp, u64]),
+        "gr_server_pending": (i32, [vp, ctypes.POINTER(sz), ctypes.POINTER(sz), ctypes.POINTER(sz)]),
+        "gr_server_now": (ctypes.c_double, []),
+        "gr_server_destroy": (i32, [vp]),
         "gr_last_error": (ctypes.c_char_p, []),
         "gr_version": (ctypes.c_char_p, []),
     }

@@ -64,7 +64,9 @@ gr_status get_jump_polys(int dev, int64_t J, int delta, int need, const uint64_t
   std::lock_guard<std::mutex> lk(jc.mu);
   auto& ent = jc.tab[std::make_tuple(dev, J, delta)];
   if (ent.count < need) {
-    const int cnt = std::max(need, 2 * ent.count);
+    // every entry is made at full size (127 = the most segments a call uses)
+    // so a buffer that running kernels may read is never replaced
+    const int cnt = std::max({need, 2 * ent.count, 127});
     std::vector<uint64_t> exps(cnt);
     for (int s = 0; s < cnt; ++s) exps[s] = (uint64_t)(s + 1) * (uint64_t)J - (uint64_t)delta;
     if (charpoly_terms().size() != 284) return fail(GR_ERR_CUDA, "MT19937-64 characteristic polynomial recovery failed");
@@ -844,6 +846,30 @@ gr_status run_multinomial(gr_engine* e, GenState* gst, const MnArgs& a0, int64_t
   if (st != GR_OK) return st;
   cudaError_t err = launch_multinomial(p, a, e->snap, stream);
   if (err != cudaSuccess) return cuda_fail(err, "multinomial kernel");
+  return GR_OK;
+}
+
+}  // namespace gr
+
+// ---- engine scratch reservation (serving loop) -------------------------------
+namespace gr {
+
+// Allocates the scratch a segmented call may need (prefix, call snapshot,
+// windows for up to max_segments segments, the temporary-generator caches), so
+// that later calls on this engine allocate nothing.
+gr_status engine_reserve(gr_engine* e, int max_segments) {
+  if (!e->prefix) {
+    GR_CUDA(cudaMalloc(&e->prefix, sizeof(uint64_t) * (size_t)kPrefixLen * kLanes * (size_t)e->K));
+    GR_CUDA(cudaMalloc(&e->snap, sizeof(CallSnap) * (size_t)e->K));
+  }
+  const size_t need = (size_t)e->K * (size_t)std::max(max_segments - 1, 1) * kLanes * kN;
+  if (e->segwin_words < need) {
+    cudaFree(e->segwin);
+    e->segwin = nullptr;
+    GR_CUDA(cudaMalloc(&e->segwin, sizeof(uint64_t) * need));
+    e->segwin_words = need;
+  }
+  if (!e->scratch_gen) GR_CUDA(cudaMalloc(&e->scratch_gen, sizeof(GenState) * (size_t)e->K));
   return GR_OK;
 }
 

@@ -91,5 +91,11 @@ gr_status build_discrete_table(const std::vector<double>& w, std::vector<int32_t
 // Host side (gr_api.cu): plans and launches k_multinomial on an engine, with
 // the same slice / jump-segment split as the fixed-consumption samplers.
 gr_status run_multinomial(gr_engine* e, GenState* gst, const MnArgs& a, int64_t samples, cudaStream_t s);
+// Host side (gr_api.cu): pre-allocates an engine's segmented-call scratch.
+gr_status engine_reserve(gr_engine* e, int max_segments);
+// Host side (gr_mvapi.cu): a second MvNormalGen with the same mean and factor
+// (no refactorisation) and its own StdNormalGen.
+gr_status mvnormal_clone(const gr_mvnormal* src, gr_mvnormal** out);
+int mvnormal_dim(const gr_mvnormal* g);
 
 }  // namespace gr

@@ -184,6 +184,40 @@ struct gr_multinomial {
   int gst_K = 0;
 };
 
+namespace gr {
+
+int mvnormal_dim(const gr_mvnormal* g) { return g ? g->dim : 0; }
+
+gr_status mvnormal_clone(const gr_mvnormal* src, gr_mvnormal** out) {
+  if (!src || !out) return mv_fail(GR_ERR_INVALID, "NULL argument");
+  gr_mvnormal* g = new gr_mvnormal;
+  g->dim = src->dim;
+  g->dtype = src->dtype;
+  g->tri = src->tri;
+  const size_t dd = (size_t)src->dim * src->dim;
+  const size_t es = elem_size(src->dtype);
+  cudaError_t e = cudaMalloc(&g->L64, sizeof(double) * dd);
+  if (e == cudaSuccess) e = cudaMemcpy(g->L64, src->L64, sizeof(double) * dd, cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess && src->Lf) {
+    const int MT = (src->dim + 15) / 16, KS = (src->dim + 7) / 8;
+    const int64_t nfr = src->tri ? mv_tri_frags(MT, KS) : (int64_t)MT * KS;
+    e = cudaMalloc(&g->Lf, sizeof(float) * (size_t)nfr * 128);
+    if (e == cudaSuccess) e = cudaMemcpy(g->Lf, src->Lf, sizeof(float) * (size_t)nfr * 128, cudaMemcpyDeviceToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&g->mean, es * src->dim);
+  if (e == cudaSuccess) e = cudaMemcpy(g->mean, src->mean, es * src->dim, cudaMemcpyDeviceToDevice);
+  gr_status st = e == cudaSuccess ? GR_OK : mv_fail(GR_ERR_CUDA, std::string("MvNormalGen copy: ") + cudaGetErrorString(e));
+  if (st == GR_OK) st = make_gen(&g->normal, GR_NORMAL_STD, g->dtype, 0.0);
+  if (st != GR_OK) {
+    gr_mvnormal_destroy(g);
+    return st;
+  }
+  *out = g;
+  return GR_OK;
+}
+
+}  // namespace gr
+
 extern "C" {
 
 // ---------------------------------------------------------------- MvNormalGen

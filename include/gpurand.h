@@ -210,6 +210,55 @@ gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_ou
                                 gr_stream_t stream);
 gr_status gr_multinomial_destroy(gr_multinomial* g);
 
+/* ---- serving loop ----------------------------------------------------------
+ * No counterpart in the reference (EigenRand is a library called in-process);
+ * this is the request loop the sampling path is deployed behind.  Each client
+ * owns a device-resident Vmt19937_64 (streams = 1) seeded by the caller.
+ * Requests of mixed kinds and sizes queue in arrival order and are admitted
+ * while stream slots are free and their output fits the device-memory budget;
+ * admitted requests run concurrently on the GPU and complete out of order.  A
+ * client's requests run one at a time, in submission order, so every result
+ * equals that client's plain call sequence run alone: gr_sample (a fresh
+ * generator per request, the free-function form) or, for GR_SERVE_MVNORMAL,
+ * the client's own MvNormalGen.  Results stay in budgeted device memory until
+ * gr_server_release().  Not thread-safe: drive a server from one thread. */
+#define GR_SERVE_MVNORMAL 64 /* gr_request.kind: MvNormalGen set by gr_server_set_mvnormal */
+typedef struct gr_server gr_server;
+typedef struct {
+  int32_t client;   /* 0 <= client < nclients */
+  int32_t kind;     /* a univariate gr_dist_kind value except GR_DISCRETE and GR_BINOMIAL_V, or GR_SERVE_MVNORMAL */
+  int32_t dtype;    /* GR_F32 / GR_F64 (GR_I32 for the integer kinds) */
+  int32_t trials;   /* binomial */
+  double a, b;      /* as gr_dist_desc */
+  uint64_t count;   /* output scalars; rounded up to the packet width (MvNormal: to whole samples) */
+  double arrival;   /* gr_server_now() time the request arrived; < 0 means now */
+} gr_request;
+typedef struct {
+  uint64_t ticket;
+  int32_t status;   /* gr_status of the request */
+  int32_t client;
+  void* dev_out;    /* the result in device memory, valid until gr_server_release */
+  uint64_t count;   /* scalars written */
+  size_t bytes;
+  double arrival, admitted, completed; /* gr_server_now() seconds */
+} gr_completion;
+gr_status gr_server_create(gr_server** out, int32_t nclients, const uint64_t* seeds, size_t budget_bytes,
+                           int32_t slots);
+/* the MvNormalGen<float>(mean, cov) every client uses for GR_SERVE_MVNORMAL (one factorisation, a
+ * StdNormalGen per client) */
+gr_status gr_server_set_mvnormal(gr_server* s, int32_t dim, const double* mean, const double* cov);
+/* queues a request; GR_ERR_NOMEM if its output can never fit the budget */
+gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* ticket);
+/* non-blocking: harvests finished requests, admits queued ones, reports up to cap completions */
+gr_status gr_server_progress(gr_server* s, gr_completion* done, size_t cap, size_t* ndone);
+/* copies a finished result to host memory (synchronous) */
+gr_status gr_server_read(gr_server* s, uint64_t ticket, void* host_dst, size_t bytes);
+/* gives a finished result's memory back to the budget */
+gr_status gr_server_release(gr_server* s, uint64_t ticket);
+gr_status gr_server_pending(const gr_server* s, size_t* queued, size_t* running, size_t* bytes_held);
+double gr_server_now(void);
+gr_status gr_server_destroy(gr_server* s);
+
 const char* gr_last_error(void);
 const char* gr_version(void);
 

@@ -1,0 +1,123 @@
+"""GPU checks of the serving loop: every result served in a concurrent mix is
+bit-identical to the same client's plain call sequence run alone."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def er(gpulib):
+    return gpulib
+
+
+def make_trace(nreq, nclients, seed, lo=3, hi=5):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(nreq):
+        kind = ["NORMAL", "GAMMA", "BINOMIAL", "MVNORMAL"][rng.integers(4)]
+        count = int(10 ** rng.uniform(lo, hi))
+        c = int(rng.integers(nclients))
+        if kind == "NORMAL":
+            r = dict(kind=kind, dtype=[torch.float32, torch.float64][rng.integers(2)], a=0.0, b=1.0, trials=0)
+        elif kind == "GAMMA":
+            r = dict(kind=kind, dtype=[torch.float32, torch.float64][rng.integers(2)], a=float(10 ** rng.uniform(-1, 1)),
+                     b=1.0, trials=0)
+        elif kind == "BINOMIAL":
+            r = dict(kind=kind, dtype=torch.int32, a=float(rng.uniform()), b=0.0, trials=int(rng.integers(1, 1001)))
+        else:
+            r = dict(kind=kind, dtype=torch.float32, a=0.0, b=0.0, trials=0)
+        r.update(client=c, count=count)
+        reqs.append(r)
+    return reqs
+
+
+def run_served(er, reqs, nclients, seeds, budget, slots, mv):
+    from eigenrand_gb300.serving import Server
+    srv = Server(nclients, seeds, budget, slots=slots)
+    srv.set_mvnormal(*mv)
+    tickets = [srv.submit(r["client"], r["kind"], r["dtype"], r["count"], r["a"], r["b"], r["trials"]) for r in reqs]
+    results, done = {}, 0
+    max_running, max_held = 0, 0
+    while done < len(reqs):
+        for c in srv.progress():
+            assert c["status"] == 0, c
+            results[c["ticket"]] = srv.read(c["ticket"], c["count"])
+            srv.release(c["ticket"])
+            done += 1
+        q, r, b = srv.pending()
+        max_running = max(max_running, r)
+        max_held = max(max_held, b)
+    return [results[t] for t in tickets], max_running, max_held
+
+
+def run_alone(er, reqs, nclients, seeds, mv):
+    """Each client's requests in order, plain calls on its own engine."""
+    out = [None] * len(reqs)
+    for c in range(nclients):
+        u = er.Vmt19937_64(seeds[c])
+        g = er.MvNormalGen(mv[0], mv[1])
+        for i, r in enumerate(reqs):
+            if r["client"] != c:
+                continue
+            if r["kind"] == "MVNORMAL":
+                d = len(mv[0])
+                s = -(-r["count"] // d)
+                while (s * d) % 8:
+                    s += 1
+                x = g.generate(u, s)
+                torch.cuda.synchronize()
+                out[i] = x.t().contiguous().reshape(-1).cpu().numpy()
+            else:
+                P = 8 if r["dtype"] == torch.float32 else 4
+                n = -(-r["count"] // P) * P
+                x = er._sample(r["kind"], n, 1, u, r["dtype"], r["a"], r["b"], r["trials"])
+                torch.cuda.synchronize()
+                out[i] = x.reshape(-1).cpu().numpy()
+    return out
+
+
+def mv_params(d=64, seed=3):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((d, d))
+    return rng.standard_normal(d), a @ a.T + d * np.eye(d)
+
+
+def test_served_equals_alone(er):
+    nclients = 6
+    seeds = [1000 + c for c in range(nclients)]
+    reqs = make_trace(90, nclients, 1)
+    mv = mv_params()
+    served, max_running, max_held = run_served(er, reqs, nclients, seeds, budget=1 << 30, slots=8, mv=mv)
+    alone = run_alone(er, reqs, nclients, seeds, mv)
+    for i, (a, b) in enumerate(zip(served, alone)):
+        assert a.dtype == b.dtype and a.shape == b.shape, (i, reqs[i])
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), (i, reqs[i])
+    assert max_running > 1  # requests overlapped on the GPU
+
+
+def test_budget_limits_memory_and_still_completes(er):
+    nclients = 4
+    seeds = [7 + c for c in range(nclients)]
+    reqs = make_trace(40, nclients, 2, lo=4, hi=6)
+    mv = mv_params()
+    budget = 6 << 20  # 6 MiB: large requests have to wait for memory
+    big = max(r["count"] * (8 if r["dtype"] == torch.float64 else 4) for r in reqs)
+    if big > budget:
+        reqs = [r for r in reqs if r["count"] * (8 if r["dtype"] == torch.float64 else 4) + 1024 <= budget]
+    served, _, max_held = run_served(er, reqs, nclients, seeds, budget=budget, slots=16, mv=mv)
+    assert max_held <= budget
+    alone = run_alone(er, reqs, nclients, seeds, mv)
+    for a, b in zip(served, alone):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_oversized_request_is_refused(er):
+    from eigenrand_gb300.serving import Server
+    srv = Server(2, [1, 2], 1 << 20, slots=2)
+    with pytest.raises(er.GrError, match="NOMEM"):
+        srv.submit(0, "NORMAL", torch.float32, 1 << 20)
