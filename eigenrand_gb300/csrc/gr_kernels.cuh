@@ -61,6 +61,23 @@ cudaError_t launch_staged(const Plan& p, const DistParams& d, const CallSnap* sn
 // 2 beta with a,b < 1, 3 poisson mean >= 12, 4 binomial tan proposal.
 cudaError_t launch_reject(const Plan& p, const DistParams& d, int rk, int64_t max_blocks, cudaStream_t s);
 
+// Segmented form of launch_reject for long calls on few engines (see
+// gr_samplers.cu): p.S segments of a.Ts trials per engine, windows from
+// prepare_segments with J = Ts * packets per trial (one packet earlier for the
+// int32 kinds).  gather_n bounds the FIFO lanes of one engine.
+struct RsArgs {
+  int64_t Ts;
+  int64_t* cnt;    // [K * S][2]
+  int64_t* start;  // [K * S][2]
+  int64_t* fin;    // [K][4]
+  uint64_t* lanes; // [K][lane_cap] lanes of 8 bytes (double) or 4 bytes (float / int32)
+  int64_t* pos;    // [K][pos_cap]
+  int64_t lane_cap, pos_cap;
+  int64_t max_blocks;
+};
+cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, const CallSnap* snap, const RsArgs& a,
+                                    int64_t gather_n, cudaStream_t s);
+
 // Data-dependent consumption (gr_samplers.cu), one CTA per stream: Poisson
 // mean < 12 (int32) and BetaGen with a or b >= 1 (f32/f64; d.ia / d.ib hold
 // (gamma branch << 8) | packets for the two GammaGens).

@@ -9,6 +9,7 @@
 // exists.  Fixed consumption means jump-ahead segments still apply.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/gpurand.h"
@@ -249,6 +250,120 @@ __device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t* warp_t
 
 }  // namespace
 
+// One rejection trial, lane j: candidate bits and accept flag.  Trial t
+// reads words [t * Wt, (t + 1) * Wt) of the cache-inclusive word stream
+// (word(w)); full-packet double kinds read u64 lane values (rval(r)).
+template <int RK, int DT, class WF, class RF>
+__device__ __forceinline__ bool rej_trial(const DistParams& d, int64_t t, int j, WF&& word, RF&& rval,
+                                          uint64_t& cbits) {
+  constexpr int Wt = (RK == RK_GAMMA_GS) ? 3 * 8 : (RK == RK_POISSON || RK == RK_BINOMIAL) ? 8 : 2 * 8;
+  bool acc = false;
+  cbits = 0;
+
+  const int64_t w0 = t * Wt;
+  if (DT == SD_F32) {
+    if (RK == RK_GAMMA_GS) {
+      const float ux = ur_f(word(w0 + j));
+      const float vx = ur_f(word(w0 + 8 + j)) + 1.1920928955078125e-07f / 8;
+      const float ux2 = ur_f(word(w0 + 16 + j));
+      // the reference evaluates both branches and blends (NormalExp.h:543-553);
+      // evaluating only the selected one gives the same bits
+      const float lv = logf_(vx);
+      const bool c = ux < d.fe;  // px
+      float xx, qx;
+      if (c) {
+        xx = expf_(d.fc * lv);  // (1/alpha) * log(vx)
+        qx = expf_(-xx);
+      } else {
+        xx = 1.0f - lv;
+        qx = expf_(logf_(xx) * d.fd);  // alpha - 1
+      }
+      cbits = f2u(d.fb * xx);
+      acc = ux2 < qx;
+    } else if (RK == RK_GAMMA_TAN) {
+      const float u = ur_f(word(w0 + j));
+      const float ux = ur_f(word(w0 + 8 + j));
+      float ys, yc;
+      sincosf_((float)3.1415926535897932 * u, ys, yc);
+      const float yx = ys / yc;
+      const float xx = d.ff * yx + d.fd;  // sqrt * yx + (alpha - 1)
+      const bool c = 0.0f < xx;
+      const float ub = (yx * yx + 1.0f) * expf_(d.fd * logf_(xx / d.fd) - yx * d.ff);
+      acc = c && (ux <= ub);
+      cbits = f2u(d.fb * xx);
+    } else if (RK == RK_BETA_SMALL) {
+      const float u1 = ur_f(word(w0 + j));
+      const float u2 = ur_f(word(w0 + 8 + j));
+      const float p1 = expf_(logf_(u1) * d.fc);  // 1/a
+      const float p2 = expf_(logf_(u2) * d.fd);  // 1/b
+      const float x = p1 + p2;
+      cbits = f2u(p1 / x);
+      acc = x <= 1.0f;
+    }
+  } else if (DT == SD_F64) {
+    const int64_t r0 = (t * Wt / 8) * 4 + j;  // u64 lane index of the trial's first packet
+    if (RK == RK_GAMMA_GS) {
+      const double ux = ur_d(rval(r0));
+      const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
+      const double ux2 = ur_d(rval(r0 + 8));
+      const double lv = log_(vx);
+      const bool c = ux < d.de;
+      double xx, qx;
+      if (c) {
+        xx = exp_(d.dc * lv);
+        qx = exp_(-xx);
+      } else {
+        xx = 1.0 - lv;
+        qx = exp_(log_(xx) * d.dd);
+      }
+      cbits = d2u(d.db * xx);
+      acc = ux2 < qx;
+    } else if (RK == RK_GAMMA_TAN) {
+      const double u = ur_d(rval(r0));
+      const double ux = ur_d(rval(r0 + 4));
+      double ys, yc;
+      sincos_(3.1415926535897932 * u, ys, yc);
+      const double yx = ys / yc;
+      const double xx = d.df * yx + d.dd;
+      const bool c = 0.0 < xx;
+      const double ub = (yx * yx + 1.0) * exp_(d.dd * log_(xx / d.dd) - yx * d.df);
+      acc = c && (ux <= ub);
+      cbits = d2u(d.db * xx);
+    } else if (RK == RK_BETA_SMALL) {
+      const double u1 = ur_d(rval(r0));
+      const double u2 = ur_d(rval(r0 + 4));
+      const double p1 = exp_(log_(u1) * d.dc);
+      const double p2 = exp_(log_(u2) * d.dd);
+      const double x = p1 + p2;
+      cbits = d2u(p1 / x);
+      acc = x <= 1.0;
+    }
+  } else {  // int32 kinds with Packet4f internals over half packets
+    const float u = ur_f(word(w0 + j));
+    const float u2 = ur_f(word(w0 + 4 + j));
+    float s, c;
+    sincosf_((float)3.1415926535897932 * u, s, c);
+    const float yx = s / c;
+    if (RK == RK_POISSON) {
+      const float fres = truncf(d.fa * yx + d.fb);  // sqrt(2 mean) * yx + mean
+      const float p1 = (yx * yx + 1.0f) * 0.9f;
+      const float p2 = expf_((fres * d.fc - lgamma_approxf_(fres + 1.0f)) - d.fd);
+      acc = (0.0f <= fres) && (u2 <= p1 * p2);
+      cbits = f2u(fres);
+    } else {  // binomial, BinomialGen::packetOp tan branch (Discrete.h:1014-1046)
+      const float fres = truncf(d.fa * yx + d.fb);  // sqrt_v * ys + mean
+      const float p1 = ((float)1.2 * d.fa) * (1.0f + yx * yx);
+      float tt = (d.fg - lgamma_approxf_(fres + 1.0f)) - lgamma_approxf_((d.fh + 1.0f) - fres);
+      tt = tt + fres * d.fc;
+      tt = tt + (d.fh - fres) * d.fd;
+      const float p2 = expf_(tt);
+      acc = (0.0f <= fres) && (fres <= d.fh) && (u2 <= p1 * p2);
+      cbits = f2u(fres);
+    }
+  }
+        return acc;
+}
+
 template <int RK, int DT>  // DT: SD_F32 (P=8), SD_F64 (P=4), SD_I32H (P=4, float internals)
 __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, int64_t max_blocks) {
   constexpr int P = DT == SD_F32 ? 8 : 4;
@@ -330,109 +445,7 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
       const int64_t t = t_next + tl;
       bool acc = false;
       uint64_t cbits = 0;
-      if (valid) {
-        const int64_t w0 = t * Wt;
-        if (DT == SD_F32) {
-          if (RK == RK_GAMMA_GS) {
-            const float ux = ur_f(word(w0 + j));
-            const float vx = ur_f(word(w0 + 8 + j)) + 1.1920928955078125e-07f / 8;
-            const float ux2 = ur_f(word(w0 + 16 + j));
-            // the reference evaluates both branches and blends (NormalExp.h:543-553);
-            // evaluating only the selected one gives the same bits
-            const float lv = logf_(vx);
-            const bool c = ux < d.fe;  // px
-            float xx, qx;
-            if (c) {
-              xx = expf_(d.fc * lv);  // (1/alpha) * log(vx)
-              qx = expf_(-xx);
-            } else {
-              xx = 1.0f - lv;
-              qx = expf_(logf_(xx) * d.fd);  // alpha - 1
-            }
-            cbits = f2u(d.fb * xx);
-            acc = ux2 < qx;
-          } else if (RK == RK_GAMMA_TAN) {
-            const float u = ur_f(word(w0 + j));
-            const float ux = ur_f(word(w0 + 8 + j));
-            float ys, yc;
-            sincosf_((float)3.1415926535897932 * u, ys, yc);
-            const float yx = ys / yc;
-            const float xx = d.ff * yx + d.fd;  // sqrt * yx + (alpha - 1)
-            const bool c = 0.0f < xx;
-            const float ub = (yx * yx + 1.0f) * expf_(d.fd * logf_(xx / d.fd) - yx * d.ff);
-            acc = c && (ux <= ub);
-            cbits = f2u(d.fb * xx);
-          } else if (RK == RK_BETA_SMALL) {
-            const float u1 = ur_f(word(w0 + j));
-            const float u2 = ur_f(word(w0 + 8 + j));
-            const float p1 = expf_(logf_(u1) * d.fc);  // 1/a
-            const float p2 = expf_(logf_(u2) * d.fd);  // 1/b
-            const float x = p1 + p2;
-            cbits = f2u(p1 / x);
-            acc = x <= 1.0f;
-          }
-        } else if (DT == SD_F64) {
-          const int64_t r0 = (t * Wt / 8) * 4 + j;  // u64 lane index of the trial's first packet
-          if (RK == RK_GAMMA_GS) {
-            const double ux = ur_d(rval(r0));
-            const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
-            const double ux2 = ur_d(rval(r0 + 8));
-            const double lv = log_(vx);
-            const bool c = ux < d.de;
-            double xx, qx;
-            if (c) {
-              xx = exp_(d.dc * lv);
-              qx = exp_(-xx);
-            } else {
-              xx = 1.0 - lv;
-              qx = exp_(log_(xx) * d.dd);
-            }
-            cbits = d2u(d.db * xx);
-            acc = ux2 < qx;
-          } else if (RK == RK_GAMMA_TAN) {
-            const double u = ur_d(rval(r0));
-            const double ux = ur_d(rval(r0 + 4));
-            double ys, yc;
-            sincos_(3.1415926535897932 * u, ys, yc);
-            const double yx = ys / yc;
-            const double xx = d.df * yx + d.dd;
-            const bool c = 0.0 < xx;
-            const double ub = (yx * yx + 1.0) * exp_(d.dd * log_(xx / d.dd) - yx * d.df);
-            acc = c && (ux <= ub);
-            cbits = d2u(d.db * xx);
-          } else if (RK == RK_BETA_SMALL) {
-            const double u1 = ur_d(rval(r0));
-            const double u2 = ur_d(rval(r0 + 4));
-            const double p1 = exp_(log_(u1) * d.dc);
-            const double p2 = exp_(log_(u2) * d.dd);
-            const double x = p1 + p2;
-            cbits = d2u(p1 / x);
-            acc = x <= 1.0;
-          }
-        } else {  // int32 kinds with Packet4f internals over half packets
-          const float u = ur_f(word(w0 + j));
-          const float u2 = ur_f(word(w0 + 4 + j));
-          float s, c;
-          sincosf_((float)3.1415926535897932 * u, s, c);
-          const float yx = s / c;
-          if (RK == RK_POISSON) {
-            const float fres = truncf(d.fa * yx + d.fb);  // sqrt(2 mean) * yx + mean
-            const float p1 = (yx * yx + 1.0f) * 0.9f;
-            const float p2 = expf_((fres * d.fc - lgamma_approxf_(fres + 1.0f)) - d.fd);
-            acc = (0.0f <= fres) && (u2 <= p1 * p2);
-            cbits = f2u(fres);
-          } else {  // binomial, BinomialGen::packetOp tan branch (Discrete.h:1014-1046)
-            const float fres = truncf(d.fa * yx + d.fb);  // sqrt_v * ys + mean
-            const float p1 = ((float)1.2 * d.fa) * (1.0f + yx * yx);
-            float tt = (d.fg - lgamma_approxf_(fres + 1.0f)) - lgamma_approxf_((d.fh + 1.0f) - fres);
-            tt = tt + fres * d.fc;
-            tt = tt + (d.fh - fres) * d.fd;
-            const float p2 = expf_(tt);
-            acc = (0.0f <= fres) && (fres <= d.fh) && (u2 <= p1 * p2);
-            cbits = f2u(fres);
-          }
-        }
-      }
+      if (valid) acc = rej_trial<RK, DT>(d, t, j, word, rval, cbits);
       const uint32_t bal = __ballot_sync(0xffffffffu, acc);
       if (valid) {
         cand[tl * P + j] = cbits;
@@ -611,6 +624,444 @@ cudaError_t launch_reject(const Plan& p, const DistParams& d, int rk, int64_t ma
 #undef GR_RJ
   if (rk == RK_POISSON && dt == SD_I32H) return run_reject<RK_POISSON, SD_I32H>(p, d, max_blocks, s);
   if (rk == RK_BINOMIAL && dt == SD_I32H) return run_reject<RK_BINOMIAL, SD_I32H>(p, d, max_blocks, s);
+  return cudaErrorNotSupported;
+}
+
+// ===========================================================================
+// Segmented rejection for long calls on few engines.  The trial stream of a
+// call is cut into S segments of Ts trials; segment s starts at packet s*J
+// (J = Ts * packets per trial; half-packet kinds one packet earlier) from a
+// jump-ahead window, so the segments run on separate SMs.
+//   k_rs_count   per segment: fully accepted trials F and lanes of partially
+//                accepted trials L.
+//   k_rs_scan    per engine: prefix of (F, L) after the carried lanes, and
+//                the segment s* whose trials complete the last output packet
+//                (the last segment when the planned trials fall short: it
+//                then runs on past its end, one CTA, until done).
+//   k_rs_write   segments s <= s*: the automaton of k_reject from the
+//                segment's starting (NF, A).  Full trials go straight to the
+//                output; lanes of partial trials go to a lane buffer at their
+//                FIFO position; the trial completing FIFO packet q records
+//                its output index pos[q].  Segment s* stops at the trial that
+//                completes the last packet and stores the engine state there.
+//   k_rs_gather  FIFO packets to their output index (carried lanes from the
+//                generator), then k_rs_finish carries the leftover lanes.
+// The result is identical to k_reject's: the same trials, the same automaton.
+// ===========================================================================
+namespace {
+
+template <int RK>
+struct RejTraits {
+  static constexpr int Wt = (RK == RK_GAMMA_GS) ? 3 * 8 : (RK == RK_POISSON || RK == RK_BINOMIAL) ? 8 : 2 * 8;
+};
+
+// Common per-CTA set-up of the segmented kernels.
+template <int RK, int DT>
+struct RsSeg {
+  static constexpr int P = DT == SD_F32 ? 8 : 4;
+  static constexpr bool kHalf = DT == SD_I32H;
+  static constexpr int Wt = RejTraits<RK>::Wt;
+  int k, s;
+  int64_t off, Npk;
+  int64_t seg_p0;  // first packet generated by this CTA
+  int c0w;
+  uint32_t cw[4];
+  __device__ bool init(const Plan& p, const CallSnap* snap) {
+    k = blockIdx.x / p.S;
+    s = blockIdx.x % p.S;
+    const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+    const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+    off = g0 * p.gran;
+    Npk = ng * p.gran / P;
+    c0w = (kHalf && snap[k].half_valid) ? 4 : 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cw[q] = kHalf ? snap[k].half_cache[q] : 0u;
+    seg_p0 = s == 0 ? 0 : (int64_t)s * p.J - (kHalf ? 1 : 0);
+    return Npk > 0;
+  }
+};
+
+__device__ __forceinline__ void rs_load_window(uint64_t (*raw)[kN], const Plan& p, int k, int s) {
+  if (s == 0) load_window(raw, p.prefix + (size_t)k * kLanes * kPrefixLen, kPrefixLen);
+  else load_window(raw, p.segwin + ((size_t)k * (p.S - 1) + (s - 1)) * kLanes * kN, kN);
+}
+
+}  // namespace
+
+template <int RK, int DT>
+__global__ void __launch_bounds__(kRejThreads) k_rs_count(Plan p, DistParams d, const CallSnap* snap, RsArgs a) {
+  using G = RsSeg<RK, DT>;
+  constexpr int P = G::P, Wt = G::Wt;
+  extern __shared__ __align__(16) uint64_t rej_dyn[];
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(rej_dyn);
+  uint64_t(*tp)[kN][kLanes] = reinterpret_cast<uint64_t(*)[kN][kLanes]>(rej_dyn + 2 * kLanes * kN);
+  __shared__ uint32_t tmask[kMaxTrials];
+  __shared__ unsigned long long red[2];
+  G g;
+  if (!g.init(p, snap)) return;
+  const int tid = threadIdx.x;
+  rs_load_window(raw[0], p, g.k, g.s);
+  if (tid < 2) red[tid] = 0;
+  __syncthreads();
+  auto word = [&](int64_t wq) -> uint32_t {
+    if (wq < g.c0w) return g.cw[wq];
+    const int64_t w = wq - g.c0w;
+    const int64_t rel = (w >> 3) - g.seg_p0;
+    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
+  };
+  auto rval = [&](int64_t r) -> uint64_t {
+    const int64_t rel = (r >> 2) - g.seg_p0;
+    return tp[(rel / kN) & 1][rel % kN][r & 3];
+  };
+  const int64_t t_beg = (int64_t)g.s * a.Ts, t_end = t_beg + a.Ts;
+  int64_t t_next = t_beg;
+  uint64_t nfull = 0, nlanes = 0;
+  int cur = 0;
+  for (int64_t nb = 0; t_next < t_end; ++nb) {
+    const int slot = (int)(nb & 1);
+    mt_block(raw[cur], raw[cur ^ 1], [&](int i, const uint64_t* pk) {
+#pragma unroll
+      for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
+    });
+    cur ^= 1;
+    const int64_t t_av = ((g.seg_p0 + (nb + 1) * kN) * 8 + g.c0w) / Wt;
+    const int B = (int)(min(t_av, t_end) - t_next);
+    if (B <= 0) continue;
+    for (int base = 0; base < B * P; base += kRejThreads) {
+      const int e = base + tid;
+      const bool valid = e < B * P;
+      const int tl = e / P, j = e % P;
+      uint64_t cbits = 0;
+      bool acc = false;
+      if (valid) acc = rej_trial<RK, DT>(d, t_next + tl, j, word, rval, cbits);
+      const uint32_t bal = __ballot_sync(0xffffffffu, acc);
+      if (valid && j == 0) tmask[tl] = (bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1);
+    }
+    __syncthreads();
+    for (int tl = tid; tl < B; tl += kRejThreads) {
+      const int c = __popc(tmask[tl]);
+      if (c == P) ++nfull;
+      else nlanes += (uint64_t)c;
+    }
+    t_next += B;
+    __syncthreads();
+  }
+  atomicAdd(&red[0], (unsigned long long)nfull);
+  atomicAdd(&red[1], (unsigned long long)nlanes);
+  __syncthreads();
+  if (tid == 0) {
+    a.cnt[((size_t)g.k * p.S + g.s) * 2] = (int64_t)red[0];
+    a.cnt[((size_t)g.k * p.S + g.s) * 2 + 1] = (int64_t)red[1];
+  }
+}
+
+template <int P>
+__global__ void k_rs_scan(Plan p, RsArgs a) {
+  const int k = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t Npk = ng * p.gran / P;
+  int64_t NF = 0, A = p.gen[k].s[0].rest_cnt;
+  int sstar = p.S - 1;
+  for (int s = 0; s < p.S; ++s) {
+    a.start[((size_t)k * p.S + s) * 2] = NF;
+    a.start[((size_t)k * p.S + s) * 2 + 1] = A;
+    NF += a.cnt[((size_t)k * p.S + s) * 2];
+    A += a.cnt[((size_t)k * p.S + s) * 2 + 1];
+    if (NF + A / P >= Npk) {
+      sstar = s;
+      break;
+    }
+  }
+  a.fin[(size_t)k * 4] = Npk > 0 ? sstar : -1;
+  a.fin[(size_t)k * 4 + 1] = 0;  // A and NF at the end, written by segment s*
+  a.fin[(size_t)k * 4 + 2] = 0;
+}
+
+template <int RK, int DT>
+__global__ void __launch_bounds__(kRejThreads) k_rs_write(Plan p, DistParams d, const CallSnap* snap, RsArgs a) {
+  using G = RsSeg<RK, DT>;
+  constexpr int P = G::P, Wt = G::Wt;
+  constexpr bool kWide = DT == SD_F64;
+  extern __shared__ __align__(16) uint64_t rej_dyn[];
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(rej_dyn);
+  uint64_t(*tp)[kN][kLanes] = reinterpret_cast<uint64_t(*)[kN][kLanes]>(rej_dyn + 2 * kLanes * kN);
+  uint64_t* cand = rej_dyn + 4 * kLanes * kN;
+  __shared__ uint32_t tmask[kMaxTrials];
+  __shared__ uint32_t tscan[kMaxTrials];
+  __shared__ uint32_t warp_tot[kRejThreads / 32];
+  __shared__ int s_tstar;
+  G g;
+  if (!g.init(p, snap)) return;
+  const int sstar = (int)a.fin[(size_t)g.k * 4];
+  if (g.s > sstar) return;
+  const int tid = threadIdx.x;
+  EngState* st = p.eng + g.k;
+  rs_load_window(raw[0], p, g.k, g.s);
+  __syncthreads();
+  auto word = [&](int64_t wq) -> uint32_t {
+    if (wq < g.c0w) return g.cw[wq];
+    const int64_t w = wq - g.c0w;
+    const int64_t rel = (w >> 3) - g.seg_p0;
+    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
+  };
+  auto rval = [&](int64_t r) -> uint64_t {
+    const int64_t rel = (r >> 2) - g.seg_p0;
+    return tp[(rel / kN) & 1][rel % kN][r & 3];
+  };
+  auto iout = [&](uint32_t fbits) -> int32_t {
+    const int32_t r = (int32_t)u2f(fbits);
+    return (RK == RK_BINOMIAL && d.ib) ? (int32_t)d.fh - r : r;
+  };
+  auto put = [&](int64_t idx, uint64_t v) {
+    if (kWide) reinterpret_cast<uint64_t*>(p.out)[g.off + idx] = v;
+    else if (DT == SD_I32H) reinterpret_cast<int32_t*>(p.out)[g.off + idx] = iout((uint32_t)v);
+    else reinterpret_cast<uint32_t*>(p.out)[g.off + idx] = (uint32_t)v;
+  };
+  const bool last = g.s == sstar;
+  const bool open = last && g.s == p.S - 1;  // may run past the planned trials
+  const int64_t t_beg = (int64_t)g.s * a.Ts;
+  const int64_t t_lim = open ? INT64_MAX : t_beg + a.Ts;
+  // lane buffer of engine k: 64-bit lanes for double, 32-bit otherwise
+  uint64_t* lanes64 = a.lanes + (size_t)g.k * a.lane_cap;
+  uint32_t* lanes32 = reinterpret_cast<uint32_t*>(a.lanes) + (size_t)g.k * a.lane_cap;
+  int64_t* pos = a.pos + (size_t)g.k * a.pos_cap;
+  int64_t NF = a.start[((size_t)g.k * p.S + g.s) * 2];
+  int64_t A = a.start[((size_t)g.k * p.S + g.s) * 2 + 1];
+  int64_t t_next = t_beg;
+  int cur = 0;
+  int64_t nb = 0;
+  bool stopped = false;
+  const int64_t nb_cap = open ? a.max_blocks : INT64_MAX;
+  for (; nb < nb_cap && t_next < t_lim; ++nb) {
+    const int slot = (int)(nb & 1);
+    mt_block(raw[cur], raw[cur ^ 1], [&](int i, const uint64_t* pk) {
+#pragma unroll
+      for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
+    });
+    cur ^= 1;
+    const int64_t t_av = ((g.seg_p0 + (nb + 1) * kN) * 8 + g.c0w) / Wt;
+    const int B = (int)(min(t_av, t_lim) - t_next);
+    if (B <= 0) continue;
+    for (int base = 0; base < B * P; base += kRejThreads) {
+      const int e = base + tid;
+      const bool valid = e < B * P;
+      const int tl = e / P, j = e % P;
+      uint64_t cbits = 0;
+      bool acc = false;
+      if (valid) acc = rej_trial<RK, DT>(d, t_next + tl, j, word, rval, cbits);
+      const uint32_t bal = __ballot_sync(0xffffffffu, acc);
+      if (valid) {
+        cand[tl * P + j] = cbits;
+        if (j == 0) tmask[tl] = (bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1);
+      }
+    }
+    __syncthreads();
+    uint32_t v0 = 0, v1 = 0;
+    const int ta = 2 * tid, tb = 2 * tid + 1;
+    if (ta < B) {
+      const int c = __popc(tmask[ta]);
+      v0 = (c == P) ? (1u << 16) : (uint32_t)c;
+    }
+    if (tb < B) {
+      const int c = __popc(tmask[tb]);
+      v1 = (c == P) ? (1u << 16) : (uint32_t)c;
+    }
+    const uint32_t incl = block_incl_scan(v0 + v1, warp_tot);
+    if (ta < B) tscan[ta] = incl - v0 - v1;
+    if (tb < B) tscan[tb] = incl - v1;
+    if (tid == 0) s_tstar = -1;
+    __syncthreads();
+    if (last) {
+      for (int tl = tid; tl < B; tl += kRejThreads) {
+        const int c = __popc(tmask[tl]);
+        const int64_t at = A + (tscan[tl] & 0xffffu);
+        const bool full = c == P;
+        const bool cross = !full && ((at + c) / P > at / P);
+        const int64_t eidx = NF + (tscan[tl] >> 16) + at / P;
+        if ((full || cross) && eidx == g.Npk - 1) s_tstar = tl;
+      }
+      __syncthreads();
+    }
+    const int tstar = s_tstar;
+    const int Bu = tstar >= 0 ? tstar + 1 : B;
+    for (int e = tid; e < Bu * P; e += kRejThreads) {
+      const int tl = e / P, j = e % P;
+      const uint32_t m = tmask[tl];
+      const int c = __popc(m);
+      const int64_t nf = NF + (tscan[tl] >> 16);
+      const int64_t at = A + (tscan[tl] & 0xffffu);
+      const uint64_t v = cand[tl * P + j];
+      if (c == P) {
+        const int64_t eidx = nf + at / P;
+        if (eidx < g.Npk) put(eidx * P + j, v);
+      } else {
+        if ((m >> j) & 1u) {
+          const int64_t f = at + __popc(m & ((1u << j) - 1));
+          if (f < a.lane_cap) {
+            if (kWide) lanes64[f] = v;
+            else lanes32[f] = (uint32_t)v;
+          }
+          else atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+        }
+        if (j == 0 && (at + c) / P > at / P) {  // this trial completes FIFO packet at / P
+          const int64_t q = at / P;
+          if (q < a.pos_cap) pos[q] = nf + q;
+          else atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+        }
+      }
+    }
+    {  // advance (NF, A) past the consumed trials
+      const int tl = Bu - 1;
+      const int c = __popc(tmask[tl]);
+      NF += (tscan[tl] >> 16) + (c == P ? 1 : 0);
+      A += (tscan[tl] & 0xffffu) + (c == P ? 0 : c);
+    }
+    t_next += Bu;
+    __syncthreads();
+    if (tstar >= 0) {
+      stopped = true;
+      break;
+    }
+  }
+  if (!last) return;
+  if (!stopped && tid == 0) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+  // engine state after the call: packets through the end of trial t_next - 1
+  const int64_t w_pk = t_next * Wt - g.c0w;  // packet-stream words consumed
+  const int64_t np = (w_pk + 7) / 8;
+  const int64_t np_rel = np - g.seg_p0;  // generated by this CTA
+  if (np_rel > 0) {
+    const int64_t rr = np_rel - nb * kN;
+    if (rr >= 1 && rr <= kN) store_window(st, raw[cur], raw[cur ^ 1], (int)rr);
+    else if (tid == 0) atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+  }
+  if (tid == 0) {
+    if (G::kHalf) {
+      if ((w_pk & 7) == 4) {
+        const int64_t rel = np - 1 - g.seg_p0;
+        const int sl = (int)((rel / kN) & 1);
+        const uint64_t x = tp[sl][rel % kN][2], y = tp[sl][rel % kN][3];
+        st->half_cache[0] = (uint32_t)x;
+        st->half_cache[1] = (uint32_t)(x >> 32);
+        st->half_cache[2] = (uint32_t)y;
+        st->half_cache[3] = (uint32_t)(y >> 32);
+        st->half_valid = 1;
+      } else {
+        st->half_valid = 0;
+      }
+    }
+    st->consumed += (uint64_t)max(np, (int64_t)0);
+    a.fin[(size_t)g.k * 4 + 1] = A;
+    a.fin[(size_t)g.k * 4 + 2] = NF;
+  }
+}
+
+// u64 value of carried lane f (the generator's rest, float or double lanes)
+template <int DT>
+__device__ __forceinline__ uint64_t rs_rest(const GenSlot* gs, int64_t f) {
+  if (DT == SD_F64) return (uint64_t)gs->rest[2 * f] | ((uint64_t)gs->rest[2 * f + 1] << 32);
+  return (uint64_t)gs->rest[f];
+}
+
+template <int DT>
+__device__ __forceinline__ uint64_t rs_lane(const RsArgs& a, int k, int64_t f) {
+  if (DT == SD_F64) return a.lanes[(size_t)k * a.lane_cap + f];
+  return reinterpret_cast<const uint32_t*>(a.lanes)[(size_t)k * a.lane_cap + f];
+}
+
+template <int RK, int DT>
+__global__ void k_rs_gather(Plan p, DistParams d, RsArgs a) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  const int k = blockIdx.y;
+  if (a.fin[(size_t)k * 4] < 0) return;
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, Npk = ng * p.gran / P;
+  const int64_t Qend = min(a.fin[(size_t)k * 4 + 1] / P, min(a.pos_cap, a.lane_cap / P));
+  const GenSlot* gs = &p.gen[k].s[0];
+  const int64_t rc0 = gs->rest_cnt;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Qend * P; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = i / P, f = i;
+    const int64_t eidx = a.pos[(size_t)k * a.pos_cap + q];
+    if (eidx < 0 || eidx >= Npk) continue;
+    const uint64_t v = f < rc0 ? rs_rest<DT>(gs, f) : rs_lane<DT>(a, k, f);
+    const int64_t o = off + eidx * P + (f - q * P);
+    if (DT == SD_F64) {
+      reinterpret_cast<uint64_t*>(p.out)[o] = v;
+    } else if (DT == SD_I32H) {
+      const int32_t r = (int32_t)u2f((uint32_t)v);
+      reinterpret_cast<int32_t*>(p.out)[o] = (RK == RK_BINOMIAL && d.ib) ? (int32_t)d.fh - r : r;
+    } else {
+      reinterpret_cast<uint32_t*>(p.out)[o] = (uint32_t)v;
+    }
+  }
+}
+
+template <int DT>
+__global__ void k_rs_finish(Plan p, RsArgs a) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  const int k = blockIdx.x;
+  if (a.fin[(size_t)k * 4] < 0) return;
+  GenSlot* gs = &p.gen[k].s[0];
+  const int64_t Aend = min(a.fin[(size_t)k * 4 + 1], a.lane_cap);
+  const int64_t q0 = (Aend / P) * P;
+  const int64_t rc0 = gs->rest_cnt;
+  const int l = threadIdx.x;  // 32 threads
+  uint64_t v = 0;
+  const int64_t f = q0 + l;
+  if (l < P && f < Aend) v = f < rc0 ? rs_rest<DT>(gs, f) : rs_lane<DT>(a, k, f);
+  __syncwarp();
+  if (l < P && f < Aend) {
+    if (DT == SD_F64) {
+      gs->rest[2 * l] = (uint32_t)v;
+      gs->rest[2 * l + 1] = (uint32_t)(v >> 32);
+    } else {
+      gs->rest[l] = (uint32_t)v;
+    }
+  }
+  if (l == 0) gs->rest_cnt = (int32_t)(Aend - q0);
+}
+
+template <int RK, int DT>
+static cudaError_t run_rs(const Plan& p, const DistParams& d, const CallSnap* snap, const RsArgs& a, int64_t gather_n,
+                          cudaStream_t s) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_rs_count<RK, DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRejDynSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_rs_write<RK, DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRejDynSmem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_rs_count<RK, DT><<<p.K * p.S, kRejThreads, kRejDynSmem, s>>>(p, d, snap, a);
+  k_rs_scan<P><<<p.K, 32, 0, s>>>(p, a);
+  k_rs_write<RK, DT><<<p.K * p.S, kRejThreads, kRejDynSmem, s>>>(p, d, snap, a);
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((gather_n + 255) / 256, 4096));
+  k_rs_gather<RK, DT><<<dim3((unsigned)blocks, (unsigned)p.K), 256, 0, s>>>(p, d, a);
+  k_rs_finish<DT><<<p.K, 32, 0, s>>>(p, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, const CallSnap* snap, const RsArgs& a,
+                                    int64_t gather_n, cudaStream_t s) {
+  const int dt = d.dtype == GR_F32 ? SD_F32 : d.dtype == GR_F64 ? SD_F64 : SD_I32H;
+#define GR_RS(R)                                                           \
+  if (rk == R) {                                                            \
+    if (dt == SD_F32) return run_rs<R, SD_F32>(p, d, snap, a, gather_n, s); \
+    if (dt == SD_F64) return run_rs<R, SD_F64>(p, d, snap, a, gather_n, s); \
+  }
+  GR_RS(RK_GAMMA_GS)
+  GR_RS(RK_GAMMA_TAN)
+  GR_RS(RK_BETA_SMALL)
+#undef GR_RS
+  if (rk == RK_POISSON && dt == SD_I32H) return run_rs<RK_POISSON, SD_I32H>(p, d, snap, a, gather_n, s);
+  if (rk == RK_BINOMIAL && dt == SD_I32H) return run_rs<RK_BINOMIAL, SD_I32H>(p, d, snap, a, gather_n, s);
   return cudaErrorNotSupported;
 }
 

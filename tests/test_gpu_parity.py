@@ -271,6 +271,40 @@ def test_beta_general_bit_exact(er, oracle, a, b, tdt):
     assert_bits_equal(er.raw_u64(u, 64).cpu().numpy().view(np.uint64), e.raw(16), "engine after beta")
 
 
+@pytest.mark.parametrize("kind,a,b,t,tdt", [
+    ("GAMMA", 0.5, 1.0, 0, torch.float32), ("GAMMA", 3.3, 2.0, 0, torch.float64), ("BETA", 0.4, 0.6, 0, torch.float32),
+    ("POISSON", 50.0, 0.0, 0, torch.int32), ("BINOMIAL", 0.4, 0.0, 500, torch.int32),
+    ("BINOMIAL", 0.8, 0.0, 60, torch.int32), ("GAMMA", 25.0, 1.0, 0, torch.float32)])
+def test_segmented_rejection_large_and_short_plan(er, oracle, kind, a, b, t, tdt, monkeypatch):
+    """Long single-engine calls run as jump-ahead segments (count, scan,
+    write, gather).  A plan scaled down to 30% of the needed trials makes the
+    last segment run on past its end; both must equal the single stream."""
+    u = er.Vmt19937_64(2718)
+    e = oracle.Engine(2718)
+    g = er._Gen(tdt, a, b, trials=t, kind=kind)
+    og = oracle.Gen()
+    for n, scale in ((1 << 21, None), (24, None), (1 << 19, "0.3"), (1 << 18, None)):
+        if scale:
+            monkeypatch.setenv("GR_REJECT_PLAN_SCALE", scale)
+        else:
+            monkeypatch.delenv("GR_REJECT_PLAN_SCALE", raising=False)
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, kind, n, npdt(tdt), a, b, t)
+        assert_bits_equal(got, ref, f"{kind}({a},{b},{t}) {tdt} n={n} scale={scale}")
+    monkeypatch.delenv("GR_REJECT_PLAN_SCALE", raising=False)
+    u.sync()
+    assert_bits_equal(er.raw_u64(u, 64).cpu().numpy().view(np.uint64), e.raw(16), "engine after segmented calls")
+
+
+def test_segmented_rejection_few_streams(er, oracle):
+    K, per = 3, 8 * 40000
+    u = er.Vmt19937_64(55, streams=K)
+    x = mem(er.gamma(K * per, 1, u, 0.7, 1.0))
+    for k in range(K):
+        ref = oracle.generate(oracle.Engine(55 + 4 * k), oracle.Gen(), "GAMMA", per, np.float32, 0.7, 1.0)
+        assert_bits_equal(x[k * per:(k + 1) * per], ref, f"gamma0.7 slice {k}")
+
+
 def test_rejection_on_many_streams(er, oracle):
     K, per = 5, 8 * 512
     u = er.Vmt19937_64(99, streams=K)
