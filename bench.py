@@ -291,7 +291,8 @@ def run_ours(args, rank, world):
     if not args.no_extras:
         del outs, host
         torch.cuda.empty_cache()
-        res["workloads"] = {"batched_vop": bench_batched(er), "multivariate": bench_multivariate(er)}
+        res["workloads"] = {"batched_vop": bench_batched(er), "multivariate": bench_multivariate(er),
+                            "serving": bench_serving(er, seconds=args.serve_seconds)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
     return res
@@ -435,6 +436,136 @@ def bench_multivariate(er, streams=608):
     return res
 
 
+def make_serving_trace(seconds, rate=2000.0, nclients=256, seed=5):
+    """Poisson arrivals (exponential gaps, mean 1/rate); kind uniform over
+    {normal, gamma(alpha = 10^U(-1,1)), binomial(n ~ U{1..1000}, p ~ U(0,1)),
+    MvNormal d=64}; output scalars log-uniform in [10^3, 10^8]; float32 /
+    float64 half and half (MvNormal float32, binomial int32)."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        kind = ("NORMAL", "GAMMA", "BINOMIAL", "MVNORMAL")[rng.integers(4)]
+        count = int(10 ** rng.uniform(3, 8))
+        f64 = bool(rng.integers(2))
+        r = dict(t=t, client=int(rng.integers(nclients)), kind=kind, count=count, a=0.0, b=0.0, trials=0,
+                 dtype=torch.float64 if f64 else torch.float32)
+        if kind == "NORMAL":
+            r.update(b=1.0)
+        elif kind == "GAMMA":
+            r.update(a=float(10 ** rng.uniform(-1, 1)), b=1.0)
+        elif kind == "BINOMIAL":
+            r.update(trials=int(rng.integers(1, 1001)), a=float(rng.uniform()), dtype=torch.int32)
+        else:
+            r.update(dtype=torch.float32)
+        out.append(r)
+    return out
+
+
+def _pct(v, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(v), q)) if v else None
+
+
+def bench_serving(er, seconds=6.0, rates=(2000.0, 500.0), nclients=256, budget=40 << 30, slots=64, serial_cap=1.5):
+    """Trace-driven serving runs (per arrival rate) against the serial
+    plain-call path on the same trace."""
+    import numpy as np
+    import torch
+    from eigenrand_gb300.serving import Server, now
+    rng = np.random.default_rng(99)
+    A = rng.standard_normal((64, 64))
+    cov, mean = A @ A.T + 64 * np.eye(64), rng.standard_normal(64)
+    seeds = [1000 + c for c in range(nclients)]
+    out = {"config": {"clients": nclients, "trace_s": seconds, "budget_gb": budget / 2**30, "slots": slots,
+                      "counts": "log-uniform [1e3, 1e8]",
+                      "kinds": "normal, gamma(10^U(-1,1)), binomial(U{1..1000}, U(0,1)), MvNormal d=64; "
+                               "f32/f64 half and half (MvNormal f32, binomial int32)",
+                      "engines": "one Vmt19937_64(1000 + c) per client (single stream, bit-exact)"}}
+    for rate in rates:
+        trace = make_serving_trace(seconds, rate=rate, nclients=nclients)
+        warm = make_serving_trace(0.5, rate=rate, nclients=nclients, seed=6)
+        srv = Server(nclients, seeds, budget, slots=slots)
+        srv.set_mvnormal(mean, cov)
+
+        def replay(reqs):
+            t0 = now()
+            i, done, lat, nbytes, last = 0, 0, [], 0, t0
+            while done < len(reqs):
+                tn = now() - t0
+                while i < len(reqs) and reqs[i]["t"] <= tn:
+                    r = reqs[i]
+                    srv.submit(r["client"], r["kind"], r["dtype"], r["count"], r["a"], r["b"], r["trials"],
+                               arrival=t0 + r["t"])
+                    i += 1
+                comp = srv.progress()
+                for c in comp:
+                    srv.release(c["ticket"])
+                    if c["status"] != 0:
+                        raise RuntimeError(f"request failed: {c}")
+                    lat.append(c["completed"] - c["arrival"])
+                    nbytes += c["bytes"]
+                    last = max(last, c["completed"])
+                    done += 1
+                if not comp:
+                    time.sleep(20e-6)
+            return lat, nbytes, last - t0
+
+        replay(warm)
+        lat, nbytes, span = replay(trace)
+        served = {"requests": len(trace), "p50_ms": round(_pct(lat, 50) * 1e3, 2),
+                  "p99_ms": round(_pct(lat, 99) * 1e3, 2), "mean_ms": round(float(np.mean(lat)) * 1e3, 2),
+                  "span_s": round(span, 3), "gbs_out": round(nbytes / span / 1e9, 2),
+                  "req_s": round(len(trace) / span, 1)}
+        del srv
+        torch.cuda.synchronize()
+        # serial plain calls: one stream, arrival order, one call at a time on
+        # the same per-client engines (fresh, same seeds); stops after
+        # serial_cap x the trace duration and reports how far it got
+        engines = [er.Vmt19937_64(s) for s in seeds]
+        mv = [None] * nclients
+        lat_s, nbytes_s, ndone = [], 0, 0
+        st = torch.cuda.current_stream()
+        t0 = now()
+        for r in trace:
+            while now() - t0 < r["t"]:
+                time.sleep(20e-6)
+            c = r["client"]
+            if r["kind"] == "MVNORMAL":
+                if mv[c] is None:
+                    mv[c] = er.MvNormalGen(mean, cov)
+                s = -(-r["count"] // 64)
+                o = torch.empty((s, 64), dtype=torch.float32, device="cuda").t()
+                mv[c].generate(engines[c], s, out=o)
+            else:
+                P = 8 if r["dtype"] == torch.float32 else 4
+                n = -(-r["count"] // P) * P
+                o = torch.empty((1, n), dtype=r["dtype"], device="cuda").t()
+                er._sample(r["kind"], n, 1, engines[c], r["dtype"], r["a"], r["b"], r["trials"], out=o)
+            st.synchronize()
+            tdone = now()
+            lat_s.append(tdone - (t0 + r["t"]))
+            nbytes_s += o.numel() * o.element_size()
+            ndone += 1
+            del o
+            if tdone - t0 > serial_cap * seconds:
+                break
+        span_s = now() - t0
+        serial = {"requests_done": ndone, "of": len(trace), "p50_ms": round(_pct(lat_s, 50) * 1e3, 2),
+                  "p99_ms": round(_pct(lat_s, 99) * 1e3, 2), "span_s": round(span_s, 3),
+                  "gbs_out": round(nbytes_s / span_s / 1e9, 2), "req_s": round(ndone / span_s, 1),
+                  "stopped_early": ndone < len(trace)}
+        del engines, mv
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        out[f"rate_{int(rate)}"] = {"served": served, "serial_plain": serial}
+    return out
+
+
 # --------------------------------------------------------------------------- reference arm
 def cpu_run(per_dist_samples, threads=1):
     """The reference's CPU path over a bounded sample of the sweep.  The
@@ -508,6 +639,52 @@ def run_reference(args, rank, world):
             "e2e": {"value": round(v, 5), "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_case(args):
+    """One named workload, repeated (small cases for profiler captures)."""
+    import numpy as np
+    import torch
+    import eigenrand_gb300 as er
+    name = args.case
+    urng = er.Vmt19937_64(1234, streams=608)
+    if name == "uniform_f32":
+        out = torch.empty((4096, 4096), dtype=torch.float32, device="cuda")
+        fn = lambda: er.uniformReal(4096, 4096, urng, out=out)
+    elif name.startswith("mvnormal_d"):
+        d = int(name[len("mvnormal_d"):])
+        rng = np.random.default_rng(99)
+        A = rng.standard_normal((d, d))
+        g = er.MvNormalGen(rng.standard_normal(d), A @ A.T + d * np.eye(d))
+        n = (1 << 26) // (4 * d)  # 64 MiB of output: above L2 with the normals
+        out = torch.empty((n, d), dtype=torch.float32, device="cuda").t()
+        fn = lambda: g.generate(urng, n, out=out)
+    elif name == "multinomial":
+        g = er.MultinomialGen(1000, np.random.default_rng(99).dirichlet(np.ones(100)))
+        n = 1 << 16
+        out = torch.empty((n, 100), dtype=torch.int32, device="cuda").t()
+        fn = lambda: g.generate(urng, n, out=out)
+    elif name == "wishart_d32":
+        rng = np.random.default_rng(99)
+        A = rng.standard_normal((32, 32))
+        g = er.WishartGen(40, A @ A.T + 32 * np.eye(32))
+        n = 1 << 14
+        out = torch.empty((32 * n, 32), dtype=torch.float32, device="cuda").t()
+        fn = lambda: g.generate(urng, n, out=out)
+    elif name in ("beta_f32", "beta_f64"):
+        dt = torch.float32 if name == "beta_f32" else torch.float64
+        g = er.BetaGen(0.5, 2.0, dtype=dt)
+        out = torch.empty((2048, 2048), dtype=dt, device="cuda")
+        fn = lambda: g.generate(2048, 2048, urng, out=out)
+    elif name == "gamma_compat":
+        u1 = er.Vmt19937_64(1234)
+        g = er.GammaGen(0.5, 1.0)
+        out = torch.empty((4096, 4096), dtype=torch.float32, device="cuda")
+        fn = lambda: g.generate(4096, 4096, u1, out=out)
+    else:
+        raise SystemExit(f"unknown case {name}")
+    ms = _median_ms(fn, reps=args.steps, warm=args.warmup)
+    print(json.dumps({"case": name, "ms": round(ms, 4)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -517,9 +694,16 @@ def main():
     ap.add_argument("--mode", default="streams", choices=["compat", "streams"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=6.0, help="length of each serving trace")
+    ap.add_argument("--case", default=None,
+                    help="run one named small workload instead (uniform_f32, mvnormal_dD, multinomial, wishart_d32, "
+                         "beta_f32, beta_f64, gamma_compat), for profiler captures")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, multivariate and serving workloads (extra keys of the JSON line)")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if world != args.gpus and "RANK" not in os.environ:

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "../../include/gpurand.h"
 #include "gr_internal.h"
@@ -1464,6 +1465,392 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
   }
 }
 
+// ===========================================================================
+// k_beta: BetaGen with a >= 1 or b >= 1 (NormalExp.h:970-975).  Each output
+// packet draws one packet from GammaGen(a), then one from GammaGen(b); a
+// component is closed form (alpha == 1: 1 packet; integer alpha < 20: alpha
+// packets) or a rejection sampler (GS trials of 3 packets, tan trials of 2)
+// with its own CompressMask carry.
+// Per block of 312 packets:
+//   masks  every start position of a rejection component gets its P-lane
+//          accept mask (all threads; ballot per P lanes);
+//   walk   thread 0 follows the reference automaton over the masks only:
+//          output packet sources (closed form / full trial at x, or FIFO
+//          packet at a lane offset) and the partial trials it consumed;
+//   write  all threads recompute the values of the consumed trials only, put
+//          partial-trial lanes into a per-component lane buffer at their FIFO
+//          position, and write p1 / (p1 + p2); lanes still carried move to
+//          the front of the lane buffer.
+// ===========================================================================
+namespace {
+
+constexpr int kBetaThreads = 160;
+constexpr int kBetaRing = 640;              // positions whose masks are kept
+constexpr int kBetaRec = 160;               // output packets per block step
+constexpr int kBetaPT = 128;                // partial trials per component per block step
+constexpr int kBetaLB = 8 + kBetaPT * 8;    // lane buffer per component
+constexpr int64_t kBetaMargin = 96;         // evaluated positions kept ahead of an output packet
+
+template <int DT>
+__host__ __device__ constexpr size_t beta_smem_bytes() {
+  return (size_t)5 * kLanes * kN * 8 +                       // raw x3, tp x2
+         (size_t)kBetaRec * 2 * 8 +                          // rec
+         (size_t)2 * kBetaPT * 8 +                           // partial trial positions
+         (size_t)2 * kBetaLB * (DT == SD_F64 ? 8 : 4) +      // lane buffers
+         (size_t)2 * kBetaPT * 4 * 2 +                       // lane offsets, masks
+         (size_t)2 * kBetaRing;                              // masks per position
+}
+
+// Value (closed form) or candidate (rejection trial) of one GammaGen
+// component at packet position x, lane j, with the accept flag of a trial.
+template <int DT, class WF, class RF>
+__device__ __forceinline__ uint64_t beta_comp(int type, int U, float af, double ad, int64_t x, int j, WF&& word,
+                                              RF&& rval, bool& acc) {
+  acc = true;
+  if (DT == SD_F32) {
+    auto Uf = [&](int q) { return ur_f(word((x + q) * 8 + j)); };
+    if (type == 0) return f2u(1.0f * (-(logf_(1.0f - Uf(0)) / 1.0f)));
+    if (type == 1) {
+      float y = Uf(0) + 1.1920928955078125e-07f / 8;
+      for (int t = 1; t < U; ++t) y = y * (Uf(t) + 1.1920928955078125e-07f / 8);
+      return f2u(-(1.0f * logf_(y)));
+    }
+    if (type == 2) {
+      const float ux = Uf(0), vx = Uf(1) + 1.1920928955078125e-07f / 8, ux2 = Uf(2);
+      const float lv = logf_(vx);
+      const bool cc = ux < (float)(2.7182818284590452 / (af + 2.7182818284590452));
+      float xx, qx;
+      if (cc) {
+        xx = expf_((1 / af) * lv);
+        qx = expf_(-xx);
+      } else {
+        xx = 1.0f - lv;
+        qx = expf_(logf_(xx) * (af - 1));
+      }
+      acc = ux2 < qx;
+      return f2u(1.0f * xx);
+    }
+    const float a1 = af - 1, sq = sqrtf(2 * af - 1);
+    float ys, yc;
+    sincosf_((float)3.1415926535897932 * Uf(0), ys, yc);
+    const float yx = ys / yc;
+    const float xx = sq * yx + a1;
+    const float ub = (yx * yx + 1.0f) * expf_(a1 * logf_(xx / a1) - yx * sq);
+    acc = (0.0f < xx) && (Uf(1) <= ub);
+    return f2u(1.0f * xx);
+  } else {
+    auto Ud = [&](int q) { return ur_d(rval((x + q) * 4 + j)); };
+    if (type == 0) return d2u(1.0 * (-(log_(1.0 - Ud(0)) / 1.0)));
+    if (type == 1) {
+      double y = Ud(0) + 2.220446049250313e-16 / 8;
+      for (int t = 1; t < U; ++t) y = y * (Ud(t) + 2.220446049250313e-16 / 8);
+      return d2u(-(1.0 * log_(y)));
+    }
+    if (type == 2) {
+      const double ux = Ud(0), vx = Ud(1) + 2.220446049250313e-16 / 8, ux2 = Ud(2);
+      const double lv = log_(vx);
+      const bool cc = ux < (2.7182818284590452 / (ad + 2.7182818284590452));
+      double xx, qx;
+      if (cc) {
+        xx = exp_((1 / ad) * lv);
+        qx = exp_(-xx);
+      } else {
+        xx = 1.0 - lv;
+        qx = exp_(log_(xx) * (ad - 1));
+      }
+      acc = ux2 < qx;
+      return d2u(1.0 * xx);
+    }
+    const double a1 = ad - 1, sq = sqrt(2 * ad - 1);
+    double ys, yc;
+    sincos_(3.1415926535897932 * Ud(0), ys, yc);
+    const double yx = ys / yc;
+    const double xx = sq * yx + a1;
+    const double ub = (yx * yx + 1.0) * exp_(a1 * log_(xx / a1) - yx * sq);
+    acc = (0.0 < xx) && (Ud(1) <= ub);
+    return d2u(1.0 * xx);
+  }
+}
+
+}  // namespace
+
+template <int DT>  // SD_F32 or SD_F64
+__global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int64_t max_blocks) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  using V = typename std::conditional<DT == SD_F64, uint64_t, uint32_t>::type;
+  extern __shared__ __align__(16) uint64_t beta_dyn[];
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(beta_dyn);
+  uint64_t(*tp)[kN][kLanes] = reinterpret_cast<uint64_t(*)[kN][kLanes]>(beta_dyn + 3 * kLanes * kN);
+  int64_t* rec = reinterpret_cast<int64_t*>(beta_dyn + 5 * kLanes * kN);   // [kBetaRec][2]
+  int64_t* ptx = rec + kBetaRec * 2;                                         // [2][kBetaPT]
+  V* lanebuf = reinterpret_cast<V*>(ptx + 2 * kBetaPT);                      // [2][kBetaLB]
+  int32_t* pA = reinterpret_cast<int32_t*>(lanebuf + 2 * kBetaLB);           // [2][kBetaPT]
+  uint32_t* pm = reinterpret_cast<uint32_t*>(pA + 2 * kBetaPT);              // [2][kBetaPT]
+  uint8_t* pmask = reinterpret_cast<uint8_t*>(pm + 2 * kBetaPT);             // [2][kBetaRing]
+  __shared__ int s_nrec, s_np[2], s_fc[2], s_A[2];
+  __shared__ int s_stop, s_err, s_more;
+  __shared__ int64_t s_ebase, s_end;
+
+  const int k = blockIdx.x;
+  const int tid = threadIdx.x;
+  EngState* st = p.eng + k;
+  GenState* gs = p.gen + k;
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  const int64_t Npk = n / P;
+
+  const int type0 = d.ia >> 8, U0 = d.ia & 0xff, type1 = d.ib >> 8, U1 = d.ib & 0xff;
+  const int umax = max(max(U0, U1), 3);
+  load_window(raw[0], &st->win[0][0], kN);
+  // carried lanes of the two GammaGens (generator slots 1 and 2)
+  if (tid < 2 * 8) {
+    const int c = tid / 8, j = tid % 8;
+    const GenSlot& g = gs->s[1 + c];
+    if (j < g.rest_cnt)
+      lanebuf[c * kBetaLB + j] = (V)(DT == SD_F64 ? ((uint64_t)g.rest[2 * j] | ((uint64_t)g.rest[2 * j + 1] << 32))
+                                                  : (uint64_t)g.rest[j]);
+  }
+  if (tid == 0) {
+    s_err = 0;
+    s_stop = 0;
+    s_fc[0] = gs->s[1].rest_cnt;
+    s_fc[1] = gs->s[2].rest_cnt;
+  }
+  __syncthreads();
+  auto word = [&](int64_t w) -> uint32_t {
+    const int64_t rel = w >> 3;
+    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
+  };
+  auto rval = [&](int64_t r) -> uint64_t {
+    const int64_t rel = r >> 2;
+    return tp[(rel / kN) & 1][rel % kN][r & 3];
+  };
+  auto comp = [&](int c, int64_t x, int j, bool& acc) -> uint64_t {
+    return c == 0 ? beta_comp<DT>(type0, U0, d.fa, d.da, x, j, word, rval, acc)
+                  : beta_comp<DT>(type1, U1, d.fb, d.db, x, j, word, rval, acc);
+  };
+  // rejection components evaluated at every position
+  const int nrej = (type0 >= 2 ? 1 : 0) + (type1 >= 2 ? 1 : 0);
+  const int rej0 = type0 >= 2 ? 0 : 1;  // first rejection component
+
+  int64_t s = 0, E = 0, done_pos = 0;  // walk state (thread 0 reads / writes s and E)
+  int fc[2] = {0, 0};
+  if (tid == 0) {
+    fc[0] = s_fc[0];
+    fc[1] = s_fc[1];
+  }
+  int cur = 0;
+  int64_t nb = 0;
+  for (; nb < max_blocks; ++nb) {
+    const int slot = (int)(nb & 1);
+    const int nxt = cur == 2 ? 0 : cur + 1;
+    mt_block(raw[cur], raw[nxt], [&](int i, const uint64_t* pk) {
+#pragma unroll
+      for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
+    });
+    cur = nxt;
+    const int64_t lim = (nb + 1) * kN - umax + 1;  // positions whose packets all exist
+    if (tid == 0 && lim - s > kBetaRing) s_err = 1;
+    // ---- masks of the rejection components at positions [done_pos, lim)
+    if (nrej > 0) {
+      const int64_t cnt = (lim - done_pos) * nrej * P;
+      for (int64_t base = 0; base < cnt; base += kBetaThreads) {
+        const int64_t e = base + tid;
+        const bool valid = e < cnt;
+        bool acc = false;
+        int c = 0;
+        int64_t x = 0;
+        if (valid) {
+          const int64_t xi = e / (nrej * P);
+          const int ci = (int)((e / P) % nrej);
+          c = nrej == 2 ? ci : rej0;
+          x = done_pos + xi;
+          comp(c, x, (int)(e % P), acc);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, acc);
+        if (valid && (e % P) == 0)
+          pmask[c * kBetaRing + (int)(x % kBetaRing)] = (uint8_t)((bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1));
+      }
+    }
+    done_pos = max(done_pos, lim);
+    __syncthreads();
+    // walk, then write, until the evaluated positions are used up (a walk
+    // step stops early when its record buffers fill)
+    for (;;) {
+      // ---- walk (thread 0): sources of the next output packets
+      if (tid == 0) {
+        s_ebase = E;
+        s_more = 0;
+        int nrec = 0, np[2] = {0, 0}, A[2] = {fc[0], fc[1]};
+        const int64_t pk_end = (nb + 1) * kN;  // packets generated so far
+        if (s < nb * kN - kN) s_err = 1;       // packets before s left the ring
+        while (E < Npk && s + kBetaMargin <= done_pos) {
+          if (nrec >= kBetaRec || np[0] > kBetaPT - 48 || np[1] > kBetaPT - 48) {
+            s_more = 1;
+            break;
+          }
+          int64_t x = s;
+          bool bad = false;
+          for (int c = 0; c < 2 && !bad; ++c) {
+            const int ty = c == 0 ? type0 : type1, U = c == 0 ? U0 : U1;
+            if (ty <= 1) {
+              if (x + U > pk_end) bad = true;
+              rec[nrec * 2 + c] = x;
+              x += U;
+              continue;
+            }
+            for (;;) {
+              if (x >= done_pos || np[c] >= kBetaPT) {
+                bad = true;
+                break;
+              }
+              const uint32_t m = pmask[c * kBetaRing + (int)(x % kBetaRing)];
+              const int cn = __popc(m);
+              if (cn == P) {
+                rec[nrec * 2 + c] = x;
+                x += U;
+                break;
+              }
+              ptx[c * kBetaPT + np[c]] = x;
+              pA[c * kBetaPT + np[c]] = A[c];
+              pm[c * kBetaPT + np[c]] = m;
+              ++np[c];
+              A[c] += cn;
+              fc[c] += cn;
+              x += U;
+              if (fc[c] >= P) {
+                rec[nrec * 2 + c] = -(int64_t)(1 + (A[c] - fc[c]));
+                fc[c] -= P;
+                break;
+              }
+            }
+          }
+          if (bad) {
+            s_err = 1;
+            break;
+          }
+          ++nrec;
+          s = x;
+          ++E;
+        }
+        s_nrec = nrec;
+        s_np[0] = np[0];
+        s_np[1] = np[1];
+        s_A[0] = A[0];
+        s_A[1] = A[1];
+        s_fc[0] = fc[0];
+        s_fc[1] = fc[1];
+        if (E >= Npk) {
+          s_stop = 1;
+          s_end = s;
+        }
+      }
+      __syncthreads();
+      // ---- values of the consumed partial trials into the lane buffers
+      const int np0 = s_np[0], np1 = s_np[1];
+      for (int e = tid; e < (np0 + np1) * P; e += kBetaThreads) {
+        const int c = e < np0 * P ? 0 : 1;
+        const int kk = (c == 0 ? e : e - np0 * P) / P, j = e % P;
+        const uint32_t m = pm[c * kBetaPT + kk];
+        if ((m >> j) & 1u) {
+          bool acc;
+          const uint64_t v = comp(c, ptx[c * kBetaPT + kk], j, acc);
+          lanebuf[c * kBetaLB + pA[c * kBetaPT + kk] + __popc(m & ((1u << j) - 1))] = (V)v;
+        }
+      }
+      __syncthreads();
+      // ---- output packets
+      const int nrec = s_nrec;
+      const int64_t e_first = s_ebase;
+      for (int e = tid; e < nrec * P; e += kBetaThreads) {
+        const int i = e / P, j = e % P;
+        uint64_t v[2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const int64_t src = rec[i * 2 + c];
+          if (src >= 0) {
+            bool acc;
+            v[c] = comp(c, src, j, acc);
+          } else {
+            v[c] = (uint64_t)lanebuf[c * kBetaLB + (int)(-src - 1) + j];
+          }
+        }
+        if (DT == SD_F32) {
+          const float p1 = u2f((uint32_t)v[0]), p2 = u2f((uint32_t)v[1]);
+          reinterpret_cast<float*>(p.out)[off + (e_first + i) * P + j] = p1 / (p1 + p2);
+        } else {
+          const double p1 = u2d(v[0]), p2 = u2d(v[1]);
+          reinterpret_cast<double*>(p.out)[off + (e_first + i) * P + j] = p1 / (p1 + p2);
+        }
+      }
+      __syncthreads();
+      // ---- lanes still carried move to the front of each lane buffer
+      V carry = 0;
+      const int cc = tid / 8, cj = tid % 8;
+      const bool mover = tid < 16 && cj < s_fc[cc];
+      if (mover) carry = lanebuf[cc * kBetaLB + s_A[cc] - s_fc[cc] + cj];
+      __syncthreads();
+      if (mover) lanebuf[cc * kBetaLB + cj] = carry;
+      __syncthreads();
+      if (!s_more || s_stop || s_err) break;
+    }
+    if (s_stop || s_err) break;
+  }
+
+  // ---- state after the call
+  if (tid == 0) {
+    if (!s_stop) s_end = s;
+    if (!s_stop || s_err) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+  }
+  __syncthreads();
+  const int64_t np = s_end;  // packets consumed
+  if (np > 0) {
+    const int64_t nblk = min(nb + 1, max_blocks);  // blocks generated
+    const int64_t lastb = (np - 1) / kN;
+    const int prv = cur == 0 ? 2 : cur - 1, prv2 = prv == 0 ? 2 : prv - 1;
+    const int64_t rr = np - lastb * kN;  // in [1, 312]
+    if (lastb == nblk - 1) store_window(st, raw[cur], raw[prv], (int)rr);
+    else if (lastb == nblk - 2) store_window(st, raw[prv], raw[prv2], (int)rr);
+    else if (tid == 0) atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+  }
+  if (tid < 2 * 8) {
+    const int c = tid / 8, j = tid % 8;
+    GenSlot& g = gs->s[1 + c];
+    const uint64_t v = j < s_fc[c] ? (uint64_t)lanebuf[c * kBetaLB + j] : 0;
+    if (DT == SD_F64) {
+      g.rest[2 * j] = (uint32_t)v;
+      g.rest[2 * j + 1] = (uint32_t)(v >> 32);
+    } else {
+      g.rest[j] = (uint32_t)v;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    gs->s[1].rest_cnt = s_fc[0];
+    gs->s[2].rest_cnt = s_fc[1];
+    st->consumed += (uint64_t)max(np, (int64_t)0);
+  }
+}
+
+template <int DT>
+static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  constexpr size_t smem = beta_smem_bytes<DT>();
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_beta<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_beta<DT><<<p.K, kBetaThreads, smem, s>>>(p, d, max_blocks);
+  return cudaGetLastError();
+}
+
 template <int DT>
 static cudaError_t run_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
   const size_t smem = walk_smem_bytes<DT>();
@@ -1482,8 +1869,8 @@ static cudaError_t run_walk(const Plan& p, const DistParams& d, int64_t max_bloc
 
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
   if (d.dtype == GR_I32) return run_walk<SD_I32H>(p, d, max_blocks, s);
-  if (d.dtype == GR_F32) return run_walk<SD_F32>(p, d, max_blocks, s);
-  if (d.dtype == GR_F64) return run_walk<SD_F64>(p, d, max_blocks, s);
+  if (d.dtype == GR_F32) return run_beta<SD_F32>(p, d, max_blocks, s);
+  if (d.dtype == GR_F64) return run_beta<SD_F64>(p, d, max_blocks, s);
   return cudaErrorNotSupported;
 }
 

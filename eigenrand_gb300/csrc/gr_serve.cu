@@ -192,6 +192,12 @@ gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* ticket) 
     q.gen = (r->count + P - 1) / P * P;
     q.units = q.gen;
     q.bytes = q.gen * elem_bytes(r->dtype);
+    // data-dependent samplers also take transient scratch (the FIFO lane
+    // buffer and packet positions of a segmented call): budget 1.5x more
+    const int k = r->kind;
+    if (k == GR_GAMMA || k == GR_BETA || k == GR_POISSON || k == GR_BINOMIAL || k == GR_CHI_SQUARED ||
+        k == GR_STUDENT_T)
+      q.bytes += q.bytes + q.bytes / 2;
   }
   q.ticket = s->next_ticket++;
   if (!s->adm->submit(AdmitReq{q.ticket, r->client, q.bytes, q.r.arrival}))
