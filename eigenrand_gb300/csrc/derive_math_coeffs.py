@@ -1,4 +1,4 @@
-"""Derive the polynomial coefficients used by the library's own log/exp.
+"""Derive the polynomial coefficients used by the library's own float log/exp.
 
 The sampling kernels and the CPU oracle evaluate log/exp with the same
 operation sequence (explicit fused multiply-adds), so their results agree bit
@@ -12,9 +12,8 @@ Methods:
          log(1+f) = f - f^2/2 + f^3 * P8(f)           (Cephes-style reduction)
   expf : n = rint(x*log2(e)), r = x - n*ln2 (Cody-Waite split),
          exp(r) = 1 + r + r^2 * P5(r)
-  log  : s = f/(2+f), log(1+f) = f - s*(f - T(s^2)),  T = 2*sum z^k/(2k+1)
-         (Taylor series of 2*atanh(s); coefficients are exact rationals)
-  exp  : exp(r) = sum_{k<=13} r^k/k!  (Taylor, |r| <= ln2/2)
+The double-precision log/exp are table-driven; their tables come from
+derive_math_tables.py.
 """
 import mpmath as mp
 import numpy as np
@@ -61,14 +60,4 @@ if __name__ == "__main__":
     c1 = np.float32(0.693359375)        # 9 significant bits: n*c1 exact for |n| < 2^15
     c2 = np.float32(float(ln2 - mp.mpf(float(c1))))
     print("expf ln2 split: %.9ef %.9ef" % (c1, c2))
-    # double ln2 split with 32 trailing zero bits in the high part
-    hi = float(mp.floor(ln2 * 2 ** 32) / 2 ** 32)
-    lo = float(ln2 - hi)
-    print("double ln2 split: %.17g %.17g" % (hi, lo))
-    print("log2(e) float %.9ef double %.17g" % (np.float32(float(1 / ln2)), float(1 / ln2)))
-    print("atanh series T(z) = sum_k 2 z^k/(2k+1), k=1..12 (double):")
-    for k in range(1, 13):
-        print("  %.17g" % float(mp.mpf(2) / (2 * k + 1)))
-    print("exp Taylor 1/k!, k=2..13 (double):")
-    for k in range(2, 14):
-        print("  %.17g" % float(1 / mp.factorial(k)))
+    print("log2(e) float %.9ef" % np.float32(float(1 / ln2)))

@@ -2,7 +2,8 @@
  * CPU ORACLE — math.  Test infrastructure only; see oracle.h.
  *
  * log/exp: the library's own published-method implementations, restated here
- * independently of the device code.  Same operation order, explicit fma() /
+ * independently of the device code (double: table-driven, tables from
+ * ormath_tables.h).  Same operation order, explicit fma() /
  * fmaf() (correctly rounded), every other operation rounded on its own, so
  * the oracle and the CUDA kernels agree bit for bit.  Coefficients come from
  * eigenrand_gb300/csrc/derive_math_coeffs.py.
@@ -18,6 +19,7 @@
 #include <string.h>
 
 #include "oracle.h"
+#include "ormath_tables.h"
 
 static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
@@ -94,15 +96,15 @@ float or_expf(float x) {
   return y * u2f((uint32_t)(ni + 127) << 23);
 }
 
-/* ------------------------------------------------------------------- log */
-static const double LN2_HI = 0.69314718036912382;    /* 32 significant bits */
-static const double LN2_LO = 1.9082149292705877e-10;
-
+/* ------------------------------------------------------------- log, exp
+ * Table-driven (P. T. P. Tang, ACM TOMS 1989 and 1990); tables and the
+ * method notes in eigenrand_gb300/csrc/derive_math_tables.py.
+ */
 double or_log(double x) {
   uint64_t ux = d2u(x);
-  if (x != x) return x;
-  if (x < 0.0) return u2d(0x7ff8000000000000ull);
-  if (x == 0.0) return -INFINITY;
+  if ((ux & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return x; /* NaN */
+  if (ux >> 63) return (ux << 1) == 0 ? -INFINITY : u2d(0x7ff8000000000000ull);
+  if (ux == 0) return -INFINITY;
   if (ux == 0x7ff0000000000000ull) return x;
   int e = 0;
   if (ux < 0x0010000000000000ull) {
@@ -110,68 +112,55 @@ double or_log(double x) {
     ux = d2u(x);
     e = -54;
   }
-  e += (int)((ux >> 52) & 0x7ff) - 1022;
-  double m = u2d((ux & 0x000fffffffffffffull) | 0x3fe0000000000000ull); /* [0.5,1) */
-  double f;
-  if (m < 0.70710678118654752) {
-    e -= 1;
-    f = (m + m) - 1.0;
-  } else {
-    f = m - 1.0;
-  }
-  double s = f / (2.0 + f);
-  double z = s * s;
-  double t = 0.080000000000000002;
-  t = fma(t, z, 0.086956521739130432);
-  t = fma(t, z, 0.095238095238095233);
-  t = fma(t, z, 0.10526315789473684);
-  t = fma(t, z, 0.11764705882352941);
-  t = fma(t, z, 0.13333333333333333);
-  t = fma(t, z, 0.15384615384615385);
-  t = fma(t, z, 0.18181818181818182);
-  t = fma(t, z, 0.22222222222222221);
-  t = fma(t, z, 0.2857142857142857);
-  t = fma(t, z, 0.40000000000000002);
-  t = fma(t, z, 0.66666666666666663);
-  t = t * z; /* T(z) = sum_{k>=1} 2 z^k/(2k+1) */
-  double de = (double)e;
-  double l1p = f - s * (f - t);
-  double r = fma(de, LN2_LO, l1p);
-  return fma(de, LN2_HI, r);
+  e += (int)(ux >> 52) - 1023;
+  const int i = (int)((ux >> 45) & 127);
+  const double m = u2d((ux & 0x000fffffffffffffull) | 0x3ff0000000000000ull); /* [1, 2) */
+  const double r = fma(m, GRT_LOG_INVC[i], -1.0);
+  const double de = (double)e;
+  const double hi = fma(de, GRT_LOG_LN2_HI, GRT_LOG_C_HI[i]); /* exact: both on the 2^-42 grid */
+  const double lo = fma(de, GRT_LOG_LN2_LO, GRT_LOG_C_LO[i]);
+  const double r2 = r * r;
+  double q = GRT_LOG_Q6;
+  q = fma(q, r, GRT_LOG_Q5);
+  q = fma(q, r, GRT_LOG_Q4);
+  q = fma(q, r, GRT_LOG_Q3);
+  q = fma(q, r, GRT_LOG_Q2);
+  q = fma(q, r, GRT_LOG_Q1);
+  q = fma(q, r, GRT_LOG_Q0);
+  const double t = (r2 * r) * q; /* r^3 Q(r) */
+  double s = lo + t;
+  s = s - 0.5 * r2;
+  s = s + r;
+  return hi + s;
 }
 
-/* ------------------------------------------------------------------- exp */
 double or_exp(double x) {
-  if (x != x) return x;
-  if (x > 709.782712893383973) return INFINITY;
-  if (x < -745.1332191019412) return 0.0;
-  double n = rint(x * 1.4426950408889634);
-  double r = fma(-n, LN2_HI, x);
-  r = fma(-n, LN2_LO, r);
-  double p = 1.6059043836821613e-10;
-  p = fma(p, r, 2.08767569878681e-09);
-  p = fma(p, r, 2.505210838544172e-08);
-  p = fma(p, r, 2.7557319223985888e-07);
-  p = fma(p, r, 2.7557319223985893e-06);
-  p = fma(p, r, 2.4801587301587302e-05);
-  p = fma(p, r, 0.00019841269841269841);
-  p = fma(p, r, 0.0013888888888888889);
-  p = fma(p, r, 0.0083333333333333332);
-  p = fma(p, r, 0.041666666666666664);
-  p = fma(p, r, 0.16666666666666666);
-  p = fma(p, r, 0.5);
-  double r2 = r * r;
-  double y = fma(r2, p, r) + 1.0;
-  int ni = (int)n;
-  if (ni > 1023) {
-    y = y * 2.0;
-    ni -= 1;
+  const uint64_t ax = d2u(x) & 0x7fffffffffffffffull;
+  if (ax >= 0x4086200000000000ull) { /* |x| >= 708, inf or NaN */
+    if (ax > 0x7ff0000000000000ull) return x;
+    if (x > 709.782712893383973) return INFINITY;
+    if (x < -745.1332191019412) return 0.0;
   }
-  if (ni < -1022) {
-    y = y * u2d((uint64_t)(ni + 1022 + 1023) << 52);
+  const double z = fma(x, GRT_EXP_INV_L, 6755399441055744.0); /* 1.5 * 2^52 + n */
+  const double n = z - 6755399441055744.0;
+  const int32_t ni = (int32_t)(uint32_t)d2u(z);
+  const int j = ni & 63;
+  int mm = (ni - j) / 64;
+  double r = fma(-n, GRT_EXP_L_HI, x);
+  r = fma(-n, GRT_EXP_L_LO, r);
+  double q = GRT_EXP_C6;
+  q = fma(q, r, GRT_EXP_C5);
+  q = fma(q, r, GRT_EXP_C4);
+  q = fma(q, r, GRT_EXP_C3);
+  q = fma(q, r, GRT_EXP_C2);
+  const double p = fma(r * r, q, r); /* exp(r) - 1 */
+  const double th = GRT_EXP_T_HI[j];
+  double y = th + fma(th, p, GRT_EXP_T_LO[j]);
+  if (mm < -1022) {
+    y = y * u2d((uint64_t)(mm + 1022 + 1023) << 52);
     return y * u2d(0x0010000000000000ull); /* 2^-1022 */
   }
-  return y * u2d((uint64_t)(ni + 1023) << 52);
+  return y * u2d((uint64_t)(mm + 1023) << 52);
 }
 
 /* --------------------------------------------------------------- sincosf */

@@ -27,7 +27,7 @@ def main():
     out = {name: golden_cases.run_oracle(pyoracle, c) for name, c in golden_cases.CASES.items()}
     np.savez_compressed(os.path.join(HERE, "oracle_fixtures.npz"), **out)
     h = hashlib.sha256()
-    for f in ("oracle.c", "ormath.c", "oracle.h"):
+    for f in ("oracle.c", "ormath.c", "oracle.h", "ormath_tables.h"):
         h.update(open(os.path.join(ROOT, "oracle", f), "rb").read())
     json.dump({"oracle_sha256": h.hexdigest(), "cases": sorted(out)}, open(os.path.join(HERE, "manifest.json"), "w"),
               indent=1)

