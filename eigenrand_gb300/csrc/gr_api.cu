@@ -268,6 +268,8 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       p.de = 2.7182818284590452 / (ad + 2.7182818284590452);
       p.df = std::sqrt(2 * ad - 1);
       p.ic = f ? (af < 1.0f) : (ad < 1.0);  // GS branch
+      // relative band of the float pre-test of double GS trials (gs_filter_f64)
+      p.fh = (float)(std::ldexp(1.0, -18) * (1.0 + 40.0 / ad));
       break;
     }
     case GR_BETA: {  // BetaGen(a, b), NormalExp.h:949-976

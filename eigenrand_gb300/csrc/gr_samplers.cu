@@ -251,6 +251,35 @@ __device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t* warp_t
 
 }  // namespace
 
+// Accept test of a double GS trial (GammaGen, alpha < 1, NormalExp.h:535-556)
+// decided in float arithmetic where the float result lies clearly on one side
+// of both comparisons: 1 accept, 0 reject, -1 undecided (evaluate in double).
+// Bounds: the uniforms convert to float with relative error <= 2^-24, float
+// log / exp are within 1 ulp and |log vx| <= 38.2, so the float qx is within
+// 7e-6 (1 + 1/alpha) of the double qx, relatively; the band used is
+// 2^-18 (1 + 40/alpha), over 20 times wider.  The branch test ux < px is
+// trusted outside |ux - px| <= 2^-21 (float ux is within 2^-23 of ux).
+__device__ __forceinline__ int gs_filter_f64(uint64_t bux, uint64_t bvx, uint64_t bux2, float pxf, float inv_a,
+                                             float am1, float band) {
+  constexpr uint64_t M = 0xfffffffffffffull;
+  const float ux = __ull2float_rn(bux & M) * 0x1p-52f;
+  if (fabsf(ux - pxf) <= 0x1p-21f) return -1;
+  const float vx = __ull2float_rn(bvx & M) * 0x1p-52f + 0x1p-55f;
+  const float ux2 = __ull2float_rn(bux2 & M) * 0x1p-52f;
+  const float lv = logf_(vx);
+  float qx;
+  if (ux < pxf) {
+    const float xx = expf_(inv_a * lv);
+    qx = expf_(-xx);
+  } else {
+    const float xx = 1.0f - lv;
+    qx = expf_(logf_(xx) * am1);
+  }
+  if (ux2 < qx * (1.0f - band)) return 1;
+  if (ux2 > qx * (1.0f + band)) return 0;
+  return -1;
+}
+
 // One rejection trial, lane j: candidate bits and accept flag.  Trial t
 // reads words [t * Wt, (t + 1) * Wt) of the cache-inclusive word stream
 // (word(w)); full-packet double kinds read u64 lane values (rval(r)).
@@ -304,21 +333,35 @@ __device__ __forceinline__ bool rej_trial(const DistParams& d, int64_t t, int j,
   } else if (DT == SD_F64) {
     const int64_t r0 = (t * Wt / 8) * 4 + j;  // u64 lane index of the trial's first packet
     if (RK == RK_GAMMA_GS) {
-      const double ux = ur_d(rval(r0));
-      const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
-      const double ux2 = ur_d(rval(r0 + 8));
-      const double lv = log_(vx);
-      const bool c = ux < d.de;
-      double xx, qx;
-      if (c) {
-        xx = exp_(d.dc * lv);
-        qx = exp_(-xx);
+      // float filter first: rejected lanes need nothing more, accepted ones
+      // only the candidate (the exact branch is known)
+      const int f = gs_filter_f64(rval(r0), rval(r0 + 4), rval(r0 + 8), d.fe, d.fc, d.fd, d.fh);
+      if (f == 0) {
+        acc = false;
+      } else if (f == 1) {
+        const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
+        const double lv = log_(vx);
+        const double ux = ur_d(rval(r0));
+        const double xx = (ux < d.de) ? exp_(d.dc * lv) : 1.0 - lv;
+        cbits = d2u(d.db * xx);
+        acc = true;
       } else {
-        xx = 1.0 - lv;
-        qx = exp_(log_(xx) * d.dd);
+        const double ux = ur_d(rval(r0));
+        const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
+        const double ux2 = ur_d(rval(r0 + 8));
+        const double lv = log_(vx);
+        const bool c = ux < d.de;
+        double xx, qx;
+        if (c) {
+          xx = exp_(d.dc * lv);
+          qx = exp_(-xx);
+        } else {
+          xx = 1.0 - lv;
+          qx = exp_(log_(xx) * d.dd);
+        }
+        cbits = d2u(d.db * xx);
+        acc = ux2 < qx;
       }
-      cbits = d2u(d.db * xx);
-      acc = ux2 < qx;
     } else if (RK == RK_GAMMA_TAN) {
       const double u = ur_d(rval(r0));
       const double ux = ur_d(rval(r0 + 4));
@@ -1632,6 +1675,16 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
     return c == 0 ? beta_comp<DT>(type0, U0, d.fa, d.da, x, j, word, rval, acc)
                   : beta_comp<DT>(type1, U1, d.fb, d.db, x, j, word, rval, acc);
   };
+  // float constants of the double GS pre-test: px, 1/alpha, alpha - 1, band
+  float gsf[2][4];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const double ad = c == 0 ? d.da : d.db;
+    gsf[c][0] = (float)(2.7182818284590452 / (ad + 2.7182818284590452));
+    gsf[c][1] = (float)(1.0 / ad);
+    gsf[c][2] = (float)(ad - 1.0);
+    gsf[c][3] = (float)(0x1p-18 * (1.0 + 40.0 / ad));
+  }
   // rejection components evaluated at every position
   const int nrej = (type0 >= 2 ? 1 : 0) + (type1 >= 2 ? 1 : 0);
   const int rej0 = type0 >= 2 ? 0 : 1;  // first rejection component
@@ -1668,7 +1721,13 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
           const int ci = (int)((e / P) % nrej);
           c = nrej == 2 ? ci : rej0;
           x = done_pos + xi;
-          comp(c, x, (int)(e % P), acc);
+          const int j = (int)(e % P);
+          int f = -1;
+          if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)  // float pre-test of a double GS trial
+            f = gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), gsf[c][0], gsf[c][1],
+                              gsf[c][2], gsf[c][3]);
+          if (f >= 0) acc = f == 1;
+          else comp(c, x, j, acc);
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, acc);
         if (valid && (e % P) == 0)
