@@ -11,10 +11,17 @@
  *   keeps integer packets on SSE when AVX2 is on).
  *
  * Transcendentals: log/exp are the library's own published-method
- * implementations (Cody-Waite reduction + fitted polynomial, explicit fma),
- * restated independently here; sin/cos are EigenRand's own psincos
+ * implementations (float: Cody-Waite reduction + fitted polynomial; double:
+ * Tang's table-driven methods, tables in ormath_tables.h), restated
+ * independently here; sin/cos are EigenRand's own psincos
  * (EigenRand/MorePacketMath.h:297-491) restated; sqrt and division are IEEE.
  * Every float operation is rounded individually (-ffp-contract=off).
+ *
+ * Pins: the MT19937-64 lane against libstdc++ std::mt19937_64 and the C++
+ * standard's known answer (pin_mt.cpp).  Beyond the engine, parity with the
+ * reference is unpinned: the reference needs Eigen (absent here) and ships
+ * no golden vectors, so the transforms are checked as restatements of its
+ * source (file:line at each function) and by distribution tests.
  */
 #ifndef GR_ORACLE_H
 #define GR_ORACLE_H
