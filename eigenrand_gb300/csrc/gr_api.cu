@@ -268,8 +268,13 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       p.de = 2.7182818284590452 / (ad + 2.7182818284590452);
       p.df = std::sqrt(2 * ad - 1);
       p.ic = f ? (af < 1.0f) : (ad < 1.0);  // GS branch
-      // relative band of the float pre-test of double GS trials (gs_filter_f64)
+      // relative band of the float pre-test of double GS trials (gs_filter_f64),
+      // and ceil(px * 2^52) for the integer branch test, as the bits of dg
       p.fh = (float)(std::ldexp(1.0, -18) * (1.0 + 40.0 / ad));
+      {
+        const uint64_t tpx = (uint64_t)std::ceil(p.de * 0x1p52);
+        std::memcpy(&p.dg, &tpx, sizeof tpx);
+      }
       break;
     }
     case GR_BETA: {  // BetaGen(a, b), NormalExp.h:949-976

@@ -254,18 +254,23 @@ __device__ __forceinline__ uint32_t block_incl_scan(uint32_t v, uint32_t* warp_t
 // Accept test of a double GS trial (GammaGen, alpha < 1, NormalExp.h:535-556)
 // decided in float arithmetic where the float result lies clearly on one side
 // of both comparisons: 1 accept, 0 reject, -1 undecided (evaluate in double).
-// Bounds: the uniforms convert to float with relative error <= 2^-24, float
-// log / exp are within 1 ulp and |log vx| <= 38.2, so the float qx is within
-// 7e-6 (1 + 1/alpha) of the double qx, relatively; the band used is
-// 2^-18 (1 + 40/alpha), over 20 times wider.  The branch test ux < px is
-// trusted outside |ux - px| <= 2^-21 (float ux is within 2^-23 of ux).
+// Bounds: vx converts with relative error < 2^-19 (vx >= 2^-12 here), ux2
+// with absolute error < 2^-24, float log / exp are within 1 ulp and
+// |log vx| <= 8.4, so the float qx is within 1e-5 (1 + 1/alpha) of the double
+// qx, relatively (qx >= 0.027); the band used is 2^-18 (1 + 40/alpha), over
+// 14 times wider.  The branch test ux < px is trusted outside
+// |ux - px| <= 2^-21 (float ux is within 2^-24 of ux).
 __device__ __forceinline__ int gs_filter_f64(uint64_t bux, uint64_t bvx, uint64_t bux2, float pxf, float inv_a,
                                              float am1, float band) {
   constexpr uint64_t M = 0xfffffffffffffull;
-  const float ux = __ull2float_rn(bux & M) * 0x1p-52f;
+  // top 32 of the 52 fraction bits (absolute error < 2^-32); vx below 2^-12
+  // is left to the double test, so vx keeps a relative error below 2^-19
+  const float ux = __uint2float_rn((uint32_t)((bux & M) >> 20)) * 0x1p-32f;
   if (fabsf(ux - pxf) <= 0x1p-21f) return -1;
-  const float vx = __ull2float_rn(bvx & M) * 0x1p-52f + 0x1p-55f;
-  const float ux2 = __ull2float_rn(bux2 & M) * 0x1p-52f;
+  const uint64_t mv = bvx & M;
+  if ((mv >> 40) == 0) return -1;
+  const float vx = __uint2float_rn((uint32_t)(mv >> 20)) * 0x1p-32f;
+  const float ux2 = __uint2float_rn((uint32_t)((bux2 & M) >> 20)) * 0x1p-32f;
   const float lv = logf_(vx);
   float qx;
   if (ux < pxf) {
@@ -278,6 +283,15 @@ __device__ __forceinline__ int gs_filter_f64(uint64_t bux, uint64_t bvx, uint64_
   if (ux2 < qx * (1.0f - band)) return 1;
   if (ux2 > qx * (1.0f + band)) return 0;
   return -1;
+}
+
+// Candidate of a double GS trial already known to be accepted: xx only
+// (no acceptance bound); ux < px is decided on the integer fraction against
+// tpx = ceil(px * 2^52).
+__device__ __forceinline__ double gs_value_f64(uint64_t bux, uint64_t bvx, uint64_t tpx, double inv_a) {
+  const double vx = ur_d(bvx) + 2.220446049250313e-16 / 8;
+  const double lv = log_(vx);
+  return ((bux & 0xfffffffffffffull) < tpx) ? exp_(inv_a * lv) : 1.0 - lv;
 }
 
 // One rejection trial, lane j: candidate bits and accept flag.  Trial t
@@ -339,11 +353,7 @@ __device__ __forceinline__ bool rej_trial(const DistParams& d, int64_t t, int j,
       if (f == 0) {
         acc = false;
       } else if (f == 1) {
-        const double vx = ur_d(rval(r0 + 4)) + 2.220446049250313e-16 / 8;
-        const double lv = log_(vx);
-        const double ux = ur_d(rval(r0));
-        const double xx = (ux < d.de) ? exp_(d.dc * lv) : 1.0 - lv;
-        cbits = d2u(d.db * xx);
+        cbits = d2u(d.db * gs_value_f64(rval(r0), rval(r0 + 4), d2u(d.dg), d.dc));  // dg holds tpx as bits
         acc = true;
       } else {
         const double ux = ur_d(rval(r0));
@@ -1675,6 +1685,22 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
     return c == 0 ? beta_comp<DT>(type0, U0, d.fa, d.da, x, j, word, rval, acc)
                   : beta_comp<DT>(type1, U1, d.fb, d.db, x, j, word, rval, acc);
   };
+  // value of an accepted trial lane (or a closed-form draw): double GS lanes
+  // skip the acceptance bound
+  uint64_t gtpx[2];
+  double ginv[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const double ad = c == 0 ? d.da : d.db;
+    gtpx[c] = (uint64_t)ceil((2.7182818284590452 / (ad + 2.7182818284590452)) * 0x1p52);
+    ginv[c] = 1 / ad;
+  }
+  auto value = [&](int c, int64_t x, int j) -> uint64_t {
+    if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)
+      return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), gtpx[c], ginv[c]));
+    bool acc;
+    return comp(c, x, j, acc);
+  };
   // float constants of the double GS pre-test: px, 1/alpha, alpha - 1, band
   float gsf[2][4];
 #pragma unroll
@@ -1815,8 +1841,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
         const int kk = (c == 0 ? e : e - np0 * P) / P, j = e % P;
         const uint32_t m = pm[c * kBetaPT + kk];
         if ((m >> j) & 1u) {
-          bool acc;
-          const uint64_t v = comp(c, ptx[c * kBetaPT + kk], j, acc);
+          const uint64_t v = value(c, ptx[c * kBetaPT + kk], j);
           lanebuf[c * kBetaLB + pA[c * kBetaPT + kk] + __popc(m & ((1u << j) - 1))] = (V)v;
         }
       }
@@ -1831,8 +1856,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
         for (int c = 0; c < 2; ++c) {
           const int64_t src = rec[i * 2 + c];
           if (src >= 0) {
-            bool acc;
-            v[c] = comp(c, src, j, acc);
+            v[c] = value(c, src, j);
           } else {
             v[c] = (uint64_t)lanebuf[c * kBetaLB + (int)(-src - 1) + j];
           }
