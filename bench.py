@@ -674,6 +674,10 @@ def run_case(args):
         g = er.BetaGen(0.5, 2.0, dtype=dt)
         out = torch.empty((2048, 2048), dtype=dt, device="cuda")
         fn = lambda: g.generate(2048, 2048, urng, out=out)
+    elif name == "poisson4":
+        g = er.PoissonGen(4.0)
+        out = torch.empty((2048, 2048), dtype=torch.int32, device="cuda")
+        fn = lambda: g.generate(2048, 2048, urng, out=out)
     elif name == "gamma_compat":
         u1 = er.Vmt19937_64(1234)
         g = er.GammaGen(0.5, 1.0)
@@ -697,7 +701,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="length of each serving trace")
     ap.add_argument("--case", default=None,
                     help="run one named small workload instead (uniform_f32, mvnormal_dD, multinomial, wishart_d32, "
-                         "beta_f32, beta_f64, gamma_compat), for profiler captures")
+                         "beta_f32, beta_f64, poisson4, gamma_compat), for profiler captures")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, multivariate and serving workloads (extra keys of the JSON line)")
     args = ap.parse_args()

@@ -55,6 +55,22 @@ __device__ __forceinline__ void mt_block(uint64_t (*old)[kN], uint64_t (*nw)[kN]
   }
 }
 
+// Packet `rel` of the two-block ring tp (blocks go to slots 0, 1, 0, ... in
+// order): ring_new is the number of the newest block's first packet and
+// ring_slot its slot.  Valid for ring_new - kN <= rel < ring_new + kN; a
+// compare replaces the 64-bit division by 312.
+template <class TP>
+__device__ __forceinline__ const uint64_t* ring_packet(TP tp, int64_t rel, int64_t ring_new, int ring_slot) {
+  int d = (int)(rel - ring_new);
+  int sl = ring_slot;
+  if (d < 0) {
+    d += kN;
+    sl ^= 1;
+  }
+  if ((unsigned)d >= (unsigned)kN) d = 0;  // outside the ring: never read past the buffers
+  return tp[sl][d];
+}
+
 // Load the 4 lane windows of engine/segment into raw[0].
 __device__ __forceinline__ void load_window(uint64_t (*raw)[kN], const uint64_t* src, size_t lane_stride) {
   for (int i = threadIdx.x; i < kLanes * kN; i += blockDim.x)

@@ -734,9 +734,11 @@ __global__ void __launch_bounds__(kMnThreads) k_multinomial(Plan p, MnArgs a, co
   }
   __syncthreads();
 
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t w) -> uint32_t {  // slice word w, present in the ring
     const int64_t rel = (w >> 3) - seg_p0;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   int32_t* h = hist + warp * a.dim;
@@ -777,7 +779,7 @@ __global__ void __launch_bounds__(kMnThreads) k_multinomial(Plan p, MnArgs a, co
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur ^= 1;
+    cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     const int64_t wavail = (seg_p0 + (nb + 1) * kN) * 8;  // words [.., wavail) exist
     int64_t i_ready = i_next;
     while (i_ready < i_end && mn_base(L, i_ready + 1) <= wavail) ++i_ready;

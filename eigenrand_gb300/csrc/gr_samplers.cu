@@ -67,18 +67,20 @@ __global__ void __launch_bounds__(160)
   else load_window(raw[0], p.segwin + ((size_t)k * (p.S - 1) + (s - 1)) * kLanes * kN, kN);
   __syncthreads();
 
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t wq) -> uint32_t {  // cache-inclusive u32 word
     if (wq < c0w) return cw[wq];
     const int64_t w = wq - c0w;
     const int64_t pp = w >> 3;
     const int64_t rel = pp - seg_p0;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   auto rword = [&](int64_t r) -> uint64_t {  // u64 lane value r of the packet stream (full kinds)
     const int64_t pp = r >> 2;
     const int64_t rel = pp - seg_p0;
-    return tp[(rel / kN) & 1][rel % kN][r & 3];
+    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
   };
 
   int64_t u_next = u_beg;
@@ -93,7 +95,7 @@ __global__ void __launch_bounds__(160)
 #pragma unroll
         for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
       });
-      cur ^= 1;
+      cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     }
     // units whose last packet is now available
     const int64_t avail = seg_p0 + base + kN;  // packets [.., avail) exist
@@ -458,11 +460,13 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
   if (tid == 0) s_done = 0;
   __syncthreads();
 
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t wq) -> uint32_t {
     if (wq < c0w) return cw[wq];
     const int64_t w = wq - c0w;
     const int64_t rel = w >> 3;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   // int32 result: BinomialGen returns trials - res when p > 1/2 (Discrete.h:1051)
@@ -472,7 +476,7 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
   };
   auto rval = [&](int64_t r) -> uint64_t {  // u64 lane value (full-packet f64 kinds)
     const int64_t rel = r >> 2;
-    return tp[(rel / kN) & 1][rel % kN][r & 3];
+    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
   };
 
   int64_t E = 0;        // output packets emitted so far
@@ -486,7 +490,7 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur ^= 1;
+    cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     const int64_t avail_words = (nb + 1) * kN * 8 + c0w;
     int64_t t_end = avail_words / Wt;  // trials whose words all exist
     int B = (int)min((int64_t)kMaxTrials, t_end - t_next);
@@ -757,16 +761,18 @@ __global__ void __launch_bounds__(kRejThreads) k_rs_count(Plan p, DistParams d, 
   rs_load_window(raw[0], p, g.k, g.s);
   if (tid < 2) red[tid] = 0;
   __syncthreads();
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t wq) -> uint32_t {
     if (wq < g.c0w) return g.cw[wq];
     const int64_t w = wq - g.c0w;
     const int64_t rel = (w >> 3) - g.seg_p0;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   auto rval = [&](int64_t r) -> uint64_t {
     const int64_t rel = (r >> 2) - g.seg_p0;
-    return tp[(rel / kN) & 1][rel % kN][r & 3];
+    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
   };
   const int64_t t_beg = (int64_t)g.s * a.Ts, t_end = t_beg + a.Ts;
   int64_t t_next = t_beg;
@@ -778,7 +784,7 @@ __global__ void __launch_bounds__(kRejThreads) k_rs_count(Plan p, DistParams d, 
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur ^= 1;
+    cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     const int64_t t_av = ((g.seg_p0 + (nb + 1) * kN) * 8 + g.c0w) / Wt;
     const int B = (int)(min(t_av, t_end) - t_next);
     if (B <= 0) continue;
@@ -854,16 +860,18 @@ __global__ void __launch_bounds__(kRejThreads) k_rs_write(Plan p, DistParams d, 
   EngState* st = p.eng + g.k;
   rs_load_window(raw[0], p, g.k, g.s);
   __syncthreads();
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t wq) -> uint32_t {
     if (wq < g.c0w) return g.cw[wq];
     const int64_t w = wq - g.c0w;
     const int64_t rel = (w >> 3) - g.seg_p0;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   auto rval = [&](int64_t r) -> uint64_t {
     const int64_t rel = (r >> 2) - g.seg_p0;
-    return tp[(rel / kN) & 1][rel % kN][r & 3];
+    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
   };
   auto iout = [&](uint32_t fbits) -> int32_t {
     const int32_t r = (int32_t)u2f(fbits);
@@ -895,7 +903,7 @@ __global__ void __launch_bounds__(kRejThreads) k_rs_write(Plan p, DistParams d, 
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur ^= 1;
+    cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     const int64_t t_av = ((g.seg_p0 + (nb + 1) * kN) * 8 + g.c0w) / Wt;
     const int B = (int)(min(t_av, t_lim) - t_next);
     if (B <= 0) continue;
@@ -1207,16 +1215,18 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
   }
   __syncthreads();
 
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t wq) -> uint32_t {  // cache-inclusive u32 word
     if (wq < c0w) return cw[wq];
     const int64_t w = wq - c0w;
     const int64_t rel = w >> 3;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   auto rval = [&](int64_t r) -> uint64_t {
     const int64_t rel = r >> 2;
-    return tp[(rel / kN) & 1][rel % kN][r & 3];
+    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
   };
 
   // Beta components (types per GammaGen branch) -------------------------
@@ -1250,7 +1260,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur = nxt;
+    cur = nxt; ring_new = nb * kN; ring_slot = slot;
     // positions whose whole step lies in the generated packets
     int64_t lim;  // evaluate positions [done_pos, lim)
     if (kPoisson) {
@@ -1672,14 +1682,16 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
     s_fc[1] = gs->s[2].rest_cnt;
   }
   __syncthreads();
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t w) -> uint32_t {
     const int64_t rel = w >> 3;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   auto rval = [&](int64_t r) -> uint64_t {
     const int64_t rel = r >> 2;
-    return tp[(rel / kN) & 1][rel % kN][r & 3];
+    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
   };
   auto comp = [&](int c, int64_t x, int j, bool& acc) -> uint64_t {
     return c == 0 ? beta_comp<DT>(type0, U0, d.fa, d.da, x, j, word, rval, acc)
@@ -1730,7 +1742,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur = nxt;
+    cur = nxt; ring_new = nb * kN; ring_slot = slot;
     const int64_t lim = (nb + 1) * kN - umax + 1;  // positions whose packets all exist
     if (tid == 0 && lim - s > kBetaRing) s_err = 1;
     // ---- masks of the rejection components at positions [done_pos, lim)

@@ -106,9 +106,11 @@ __global__ void __launch_bounds__(kT) k_vop_gamma(VopArgs va, int64_t set0) {
 
   seed_engine(raw[0], va.seed + 4ull * (uint64_t)set);
   __syncthreads();
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t w) -> uint32_t {
     const int64_t rel = w >> 3;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   int64_t E = 0, t_next = 0;
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(kT) k_vop_gamma(VopArgs va, int64_t set0) {
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur ^= 1;
+    cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     const int64_t t_end = ((nb + 1) * kN * 8) / Wt;
     const int B = (int)min((int64_t)kMaxTr, t_end - t_next);
     if (B <= 0) continue;
@@ -294,9 +296,11 @@ __global__ void __launch_bounds__(kT) k_vop_binomial(VopArgs va, int64_t set0) {
     s_err = 0;
   }
   __syncthreads();
+  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
+  int ring_slot = 0;
   auto word = [&](int64_t w) -> uint32_t {
     const int64_t rel = w >> 3;
-    const uint64_t v = tp[(rel / kN) & 1][rel % kN][(w & 7) >> 1];
+    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
   int64_t s = 0, E = 0, done_pos = 0;
@@ -309,7 +313,7 @@ __global__ void __launch_bounds__(kT) k_vop_binomial(VopArgs va, int64_t set0) {
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
     });
-    cur ^= 1;
+    cur ^= 1; ring_new = nb * kN; ring_slot = slot;
     const int64_t lim = 2 * (nb + 1) * kN - kLookB;  // half packets whose lookahead exists
     if (tid == 0 && lim - s > kBRing) s_err = 1;
     for (int64_t x = done_pos + tid; x < lim; x += kT) {
