@@ -78,9 +78,10 @@ struct RsArgs {
 cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, const CallSnap* snap, const RsArgs& a,
                                     int64_t gather_n, cudaStream_t s);
 
-// Data-dependent consumption (gr_samplers.cu), one CTA per stream: Poisson
-// mean < 12 (int32) and BetaGen with a or b >= 1 (f32/f64; d.ia / d.ib hold
-// (gamma branch << 8) | packets for the two GammaGens).
+// Data-dependent consumption (gr_samplers.cu), one CTA per stream: k_poisson
+// for PoissonGen mean < 12 and BinomialGen mean < 1 (int32), k_beta for
+// BetaGen with a or b >= 1 (f32/f64; d.ia / d.ib hold (gamma branch << 8) |
+// packets for the two GammaGens).
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s);
 
 // Batched vectorize-over-params sets (gr_vop.cu).

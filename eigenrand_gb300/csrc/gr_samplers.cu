@@ -1132,125 +1132,56 @@ cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, 
 namespace gr {
 
 // ===========================================================================
-// k_walk: samplers whose packet consumption depends on the data in a way that
-// is not a fixed run of trials.
-//  * PoissonGen, mean < 12 (Discrete.h:870-882), also BinomialGen with
-//    trials*min(p,1-p) < 1: one packetOp multiplies half packets of uniforms
-//    until every lane's product is <= exp(-mean); it consumes L(h) half
-//    packets when it starts at half packet h.
-//  * BetaGen with a >= 1 or b >= 1 (NormalExp.h:970-975): each packetOp draws
-//    one packet from GammaGen(a) and then one from GammaGen(b); either may be
-//    a rejection sampler with its own CompressMask carry.
-// For every start position of the newly generated block the CTA evaluates the
-// step in parallel (L and the counts for Poisson; trial masks / candidates or
-// closed-form values for the gammas).  Thread 0 then walks the reference
-// automaton through those precomputed results and records, per output packet,
-// where its lanes come from; all threads then write the outputs.
+// k_poisson: PoissonGen with mean < 12 (Discrete.h:870-882), also BinomialGen
+// with trials * min(p, 1-p) < 1 (its PoissonGen member).  One packetOp
+// multiplies half packets of uniforms until every lane's product is
+// <= exp(-mean) and returns, per lane, how many products stayed above it; the
+// step from half packet s consumes L(s) half packets and the next starts at
+// s + L(s).  Per block of 312 packets: the uniforms go to a float ring as the
+// packets are made; every new start position gets its step (L and the four
+// counts, packed in one word) in parallel; thread 0 follows s += L(s); all
+// threads write the visited steps' counts.
 // ===========================================================================
 namespace {
-
-constexpr int kWalkThreads = 160;
-constexpr int kLook = 64;          // Poisson: max half packets one packetOp may read
-constexpr int kPosRingP = 1280;    // Poisson: start positions (half packets) kept
-constexpr int kPosRingB = 640;     // Beta: start positions (packets) kept
-constexpr int kRecP = 704;         // Poisson: output packets recorded per block (<= 624 + kLook)
-constexpr int kRecB = 160;         // Beta: output packets recorded per block (each uses >= 2 packets)
-
-template <int DT>
-__host__ __device__ constexpr size_t walk_smem_bytes() {
-  return (size_t)(3 * kLanes * kN + 2 * kLanes * kN) * 8 +                               // raw x3, tp x2
-         (DT == SD_I32H ? (size_t)kPosRingP * 8 + (size_t)kPosRingP * 4 + (size_t)kRecP * 8
-                        : (size_t)2 * kPosRingB * 8 * 8 + (size_t)2 * kPosRingB * 4 + (size_t)kRecB * 16 * 8);
-}
-
-// one gamma component of BetaGen: closed form or rejection
-struct GammaComp {
-  int type;  // 0: alpha == 1 (exponential, 1 packet); 1: integer alpha (U packets); 2: GS trial (3 packets); 3: tan trial (2)
-  int U;     // packets per draw (types 0,1) or per trial (2,3)
-};
-
+constexpr int kPoisThreads = 160;
+constexpr int kPoisLook = 64;    // half packets one step may read; a longer step is reported
+constexpr int kPoisRing = 1024;  // start positions kept (>= 2 * 312 + kPoisLook)
+constexpr int kPoisRec = 704;    // steps recorded per block (<= 624 + kPoisLook)
+constexpr size_t kPoisSmem = (size_t)3 * kLanes * kN * 8 +  // raw x3
+                             (size_t)2 * kN * 8 * 4 +       // uniforms of the two newest blocks
+                             (size_t)kPoisRing * 4 +        // per position: L << 24 | counts (6 bits each)
+                             (size_t)kPoisRec * 2;          // visited positions (ring index)
 }  // namespace
 
-template <int DT>  // SD_I32H: Poisson; SD_F32 / SD_F64: Beta
-__global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int64_t max_blocks) {
-  constexpr int P = DT == SD_F32 ? 8 : 4;
-  constexpr bool kPoisson = DT == SD_I32H;
-  constexpr int RING = kPoisson ? kPosRingP : kPosRingB;
-  extern __shared__ __align__(16) uint64_t walk_dyn[];
-  // raw: three block buffers so the window before any packet of the last two
-  // generated blocks is still in shared memory when the call ends
-  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(walk_dyn);
-  uint64_t(*tp)[kN][kLanes] = reinterpret_cast<uint64_t(*)[kN][kLanes]>(walk_dyn + 3 * kLanes * kN);
-  // per start position (ring index x % RING): Poisson: packed counts + L;
-  // Beta: per component P candidate lanes (bits) + accept mask
-  uint64_t* pos_val = walk_dyn + 5 * kLanes * kN;
-  uint32_t* pos_aux = reinterpret_cast<uint32_t*>(pos_val + (kPoisson ? RING : 2 * RING * 8));
-  int64_t* rec = reinterpret_cast<int64_t*>(pos_aux + (kPoisson ? RING : 2 * RING));
-  __shared__ int s_nrec;
-  __shared__ int s_stop;
-  __shared__ int s_err;
-  __shared__ int64_t s_ebase;   // first output packet recorded in this block
-  __shared__ int64_t s_endpos;  // walk position after the last output packet
-  __shared__ int64_t s_end;
-
+__global__ void __launch_bounds__(kPoisThreads) k_poisson(Plan p, DistParams d, int64_t max_blocks) {
+  extern __shared__ __align__(16) uint64_t pois_dyn[];
+  // raw: three block buffers so the window before the end of the call is
+  // still in shared memory when the call ends in the previous block
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(pois_dyn);
+  float(*uf)[kN][8] = reinterpret_cast<float(*)[kN][8]>(pois_dyn + 3 * kLanes * kN);
+  uint32_t* pos = reinterpret_cast<uint32_t*>(pois_dyn + 3 * kLanes * kN + kN * 8);
+  uint16_t* rec = reinterpret_cast<uint16_t*>(pos + kPoisRing);
+  __shared__ int s_nrec, s_stop, s_err;
+  __shared__ int64_t s_ebase, s_end;
+  __shared__ float4 s_cache;  // uniforms of the engine's cached half packet
   const int k = blockIdx.x;
   const int tid = threadIdx.x;
   EngState* st = p.eng + k;
-  GenState* gs = p.gen + k;
-
   const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
   const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
   const int64_t off = g0 * p.gran, n = ng * p.gran;
   if (n == 0) return;
-  const int64_t Npk = n / P;
-
-  const int c0w = (kPoisson && st->half_valid) ? 4 : 0;
-  uint32_t cw[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) cw[q] = kPoisson ? st->half_cache[q] : 0u;
+  const int64_t Npk = n / 4;
+  const int c0w = st->half_valid ? 4 : 0;  // the first half packet comes from the engine's cache
   load_window(raw[0], &st->win[0][0], kN);
   if (tid == 0) {
     s_err = 0;
     s_stop = 0;
+    s_cache = make_float4(ur_f(st->half_cache[0]), ur_f(st->half_cache[1]), ur_f(st->half_cache[2]),
+                          ur_f(st->half_cache[3]));
   }
   __syncthreads();
-
-  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
-  int ring_slot = 0;
-  auto word = [&](int64_t wq) -> uint32_t {  // cache-inclusive u32 word
-    if (wq < c0w) return cw[wq];
-    const int64_t w = wq - c0w;
-    const int64_t rel = w >> 3;
-    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
-    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
-  };
-  auto rval = [&](int64_t r) -> uint64_t {
-    const int64_t rel = r >> 2;
-    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
-  };
-
-  // Beta components (types per GammaGen branch) -------------------------
-  GammaComp comp[2];
-  comp[0].type = d.ia >> 8;
-  comp[0].U = d.ia & 0xff;
-  comp[1].type = d.ib >> 8;
-  comp[1].U = d.ib & 0xff;
-  // walk state (thread 0)
-  int64_t s = 0;     // next start position: half packets (Poisson) / packets (Beta)
-  int64_t E = 0;     // output packets done
-  int64_t done_pos = 0;  // positions evaluated up to (exclusive)
-  // Beta FIFOs: carried lane sources are stored as values (bits)
-  uint64_t fifo[2][16];  // up to P-1 carried + P-1 appended lanes before an emission
-  int fcnt[2] = {0, 0};
-  if (!kPoisson && tid == 0) {
-    for (int c = 0; c < 2; ++c) {
-      fcnt[c] = gs->s[1 + c].rest_cnt;
-      for (int j = 0; j < 8; ++j)
-        fifo[c][j] = (DT == SD_F64) ? ((uint64_t)gs->s[1 + c].rest[2 * j] | ((uint64_t)gs->s[1 + c].rest[2 * j + 1] << 32))
-                                    : (uint64_t)gs->s[1 + c].rest[j];
-    }
-  }
-
+  int64_t s = 0, E = 0, done_pos = 0;  // walk (thread 0); positions evaluated up to done_pos
   int cur = 0;
   int64_t nb = 0;
   for (; nb < max_blocks; ++nb) {
@@ -1258,274 +1189,129 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(Plan p, DistParams d, int
     const int nxt = cur == 2 ? 0 : cur + 1;
     mt_block(raw[cur], raw[nxt], [&](int i, const uint64_t* pk) {
 #pragma unroll
-      for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
-    });
-    cur = nxt; ring_new = nb * kN; ring_slot = slot;
-    // positions whose whole step lies in the generated packets
-    int64_t lim;  // evaluate positions [done_pos, lim)
-    if (kPoisson) {
-      const int64_t avail_h = (c0w / 4) + 2 * (nb + 1) * kN;
-      lim = avail_h - kLook;
-    } else {
-      const int umax = max(max(comp[0].U, comp[1].U), 3);
-      lim = (nb + 1) * kN - umax + 1;
-    }
-    // new positions overwrite ring slot x % RING; the walk (thread 0) must not
-    // still need a slot that is about to be overwritten
-    if (tid == 0 && lim - s > RING) s_err = 1;
-    // ---- evaluate every start position in [done_pos, lim)
-    for (int64_t x = done_pos + tid; x < lim; x += kWalkThreads) {
-      if (kPoisson) {
-        const int ri = (int)(x % RING);
-        float val[4] = {1.0f, 1.0f, 1.0f, 1.0f};
-        int kk[4] = {0, 0, 0, 0};
-        int L = 0;
-        bool any = true;
-        for (int it = 0; it < kLook && any; ++it) {
-          any = false;
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            val[j] = val[j] * ur_f(word((x + it) * 4 + j));
-            const bool c = d.fe < val[j];  // exp(-mean) < val
-            kk[j] += c ? 1 : 0;
-            any |= c;
-          }
-          L = it + 1;
-        }
-        if (any) atomicOr(&s_err, 1);
-        pos_aux[ri] = (uint32_t)L;
-        pos_val[ri] = (uint64_t)(kk[0] & 0xff) | ((uint64_t)(kk[1] & 0xff) << 8) | ((uint64_t)(kk[2] & 0xff) << 16) |
-                      ((uint64_t)(kk[3] & 0xff) << 24);
-      } else {
-        const int ri = (int)(x % RING);
-        for (int c = 0; c < 2; ++c) {
-          const float af = c == 0 ? d.fa : d.fb;
-          const double ad = c == 0 ? d.da : d.db;
-          uint32_t mask = 0;
-          for (int j = 0; j < P; ++j) {
-            uint64_t vb = 0;
-            bool acc = true;
-            if (DT == SD_F32) {
-              auto U = [&](int q) { return ur_f(word((x + q) * 8 + j)); };
-              if (comp[c].type == 0) {
-                vb = f2u(1.0f * (-(logf_(1.0f - U(0)) / 1.0f)));
-              } else if (comp[c].type == 1) {
-                float y = U(0) + 1.1920928955078125e-07f / 8;
-                for (int t = 1; t < comp[c].U; ++t) y = y * (U(t) + 1.1920928955078125e-07f / 8);
-                vb = f2u(-(1.0f * logf_(y)));
-              } else if (comp[c].type == 2) {
-                const float ux = U(0), vx = U(1) + 1.1920928955078125e-07f / 8, ux2 = U(2);
-                const float lv = logf_(vx);
-                const bool cc = ux < (float)(2.7182818284590452 / (af + 2.7182818284590452));
-                float xx, qx;
-                if (cc) {
-                  xx = expf_((1 / af) * lv);
-                  qx = expf_(-xx);
-                } else {
-                  xx = 1.0f - lv;
-                  qx = expf_(logf_(xx) * (af - 1));
-                }
-                vb = f2u(1.0f * xx);
-                acc = ux2 < qx;
-              } else {
-                const float a1 = af - 1, sq = sqrtf(2 * af - 1);
-                float ys, yc;
-                sincosf_((float)3.1415926535897932 * U(0), ys, yc);
-                const float yx = ys / yc;
-                const float xx = sq * yx + a1;
-                const float ub = (yx * yx + 1.0f) * expf_(a1 * logf_(xx / a1) - yx * sq);
-                acc = (0.0f < xx) && (U(1) <= ub);
-                vb = f2u(1.0f * xx);
-              }
-            } else {
-              auto U = [&](int q) { return ur_d(rval((x + q) * 4 + j)); };
-              if (comp[c].type == 0) {
-                vb = d2u(1.0 * (-(log_(1.0 - U(0)) / 1.0)));
-              } else if (comp[c].type == 1) {
-                double y = U(0) + 2.220446049250313e-16 / 8;
-                for (int t = 1; t < comp[c].U; ++t) y = y * (U(t) + 2.220446049250313e-16 / 8);
-                vb = d2u(-(1.0 * log_(y)));
-              } else if (comp[c].type == 2) {
-                const double ux = U(0), vx = U(1) + 2.220446049250313e-16 / 8, ux2 = U(2);
-                const double lv = log_(vx);
-                const bool cc = ux < (2.7182818284590452 / (ad + 2.7182818284590452));
-                double xx, qx;
-                if (cc) {
-                  xx = exp_((1 / ad) * lv);
-                  qx = exp_(-xx);
-                } else {
-                  xx = 1.0 - lv;
-                  qx = exp_(log_(xx) * (ad - 1));
-                }
-                vb = d2u(1.0 * xx);
-                acc = ux2 < qx;
-              } else {
-                const double a1 = ad - 1, sq = sqrt(2 * ad - 1);
-                double ys, yc;
-                sincos_(3.1415926535897932 * U(0), ys, yc);
-                const double yx = ys / yc;
-                const double xx = sq * yx + a1;
-                const double ub = (yx * yx + 1.0) * exp_(a1 * log_(xx / a1) - yx * sq);
-                acc = (0.0 < xx) && (U(1) <= ub);
-                vb = d2u(1.0 * xx);
-              }
-            }
-            pos_val[((size_t)c * RING + ri) * 8 + j] = vb;
-            mask |= acc ? (1u << j) : 0u;
-          }
-          pos_aux[c * RING + ri] = mask;
-        }
+      for (int l = 0; l < kLanes; ++l) {
+        uf[slot][i][2 * l] = ur_f((uint32_t)pk[l]);
+        uf[slot][i][2 * l + 1] = ur_f((uint32_t)(pk[l] >> 32));
       }
+    });
+    cur = nxt;
+    // positions whose whole step (<= kPoisLook half packets) exists
+    const int64_t lim = c0w / 4 + 2 * (nb + 1) * kN - kPoisLook;
+    if (tid == 0 && lim - s > kPoisRing) s_err = 1;
+    // ---- steps of the new start positions
+    for (int64_t x = done_pos + tid; x < lim; x += kPoisThreads) {
+      // half packet x starts at packet-stream word 4x - c0w (negative: the
+      // engine's cached half packet); w = offset from the newest block's first word
+      const bool cached = 4 * x < c0w;
+      int w = (int)(4 * x - c0w - 8 * nb * (int64_t)kN);
+      float val[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+      int kk[4] = {0, 0, 0, 0};
+      int L = 0;
+      bool any = true;
+      for (int it = 0; it < kPoisLook && any; ++it, w += 4) {
+        float4 u;
+        if (it == 0 && cached) {
+          u = s_cache;
+        } else {
+          int pk = w >> 3, sl = slot;
+          if (pk < 0) {
+            pk += kN;
+            sl ^= 1;
+          }
+          u = *reinterpret_cast<const float4*>(&uf[sl][pk][w & 7]);
+        }
+        const float uu[4] = {u.x, u.y, u.z, u.w};
+        any = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          val[j] = val[j] * uu[j];
+          const bool c = d.fe < val[j];  // exp(-mean) < val
+          kk[j] += c ? 1 : 0;
+          any |= c;
+        }
+        L = it + 1;
+      }
+      if (any) atomicOr(&s_err, 1);
+      pos[(int)(x & (kPoisRing - 1))] =
+          ((uint32_t)L << 24) | (uint32_t)kk[0] | ((uint32_t)kk[1] << 6) | ((uint32_t)kk[2] << 12) | ((uint32_t)kk[3] << 18);
     }
     done_pos = max(done_pos, lim);
     __syncthreads();
-    // ---- walk (thread 0): record output packets
+    // ---- walk (thread 0)
     if (tid == 0) {
       s_ebase = E;
       int nrec = 0;
-      if (kPoisson) {
-        while (s < done_pos && E < Npk && nrec < kRecP) {
-          const int ri = (int)(s % RING);
-          rec[nrec++] = s;
-          s += pos_aux[ri];
-          ++E;
-        }
-      } else {
-        // record per output packet: component 0's P lane values, then component 1's.
-        // Walk only while a generous margin of evaluated positions remains, so
-        // one output packet never runs past them (a longer run would need
-        // about 30 consecutive nearly-empty trials; it is reported as an error).
-        constexpr int64_t kMargin = 96;
-        const int stride = 2 * P;
-        while (E < Npk && nrec < kRecB && s + kMargin <= done_pos) {
-          int64_t x = s;
-          for (int c = 0; c < 2; ++c) {
-            if (comp[c].type <= 1) {
-              const int ri = (int)(x % RING);
-              for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)pos_val[((size_t)c * RING + ri) * 8 + j];
-              x += comp[c].U;
-              continue;
-            }
-            for (;;) {
-              if (x >= done_pos) {
-                s_err = 1;
-                break;
-              }
-              const int ri = (int)(x % RING);
-              const uint32_t m = pos_aux[c * RING + ri];
-              const uint64_t* cv = &pos_val[((size_t)c * RING + ri) * 8];
-              x += comp[c].U;
-              if (__popc(m) == P) {
-                for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)cv[j];
-                break;
-              }
-              int fc = fcnt[c];
-              for (int j = 0; j < P; ++j)
-                if ((m >> j) & 1u) fifo[c][fc++] = cv[j];
-              if (fc >= P) {
-                for (int j = 0; j < P; ++j) rec[(size_t)nrec * stride + c * P + j] = (int64_t)fifo[c][j];
-                for (int j = P; j < fc; ++j) fifo[c][j - P] = fifo[c][j];
-                fc -= P;
-                fcnt[c] = fc;
-                break;
-              }
-              fcnt[c] = fc;
-            }
-          }
-          ++nrec;
-          s = x;
-          ++E;
-        }
+      while (s < done_pos && E < Npk && nrec < kPoisRec) {
+        const int ri = (int)(s & (kPoisRing - 1));
+        rec[nrec++] = (uint16_t)ri;
+        s += pos[ri] >> 24;
+        ++E;
       }
       s_nrec = nrec;
       if (E >= Npk) {
         s_stop = 1;
-        s_endpos = s;
+        s_end = s;
       }
     }
     __syncthreads();
-    // ---- write the recorded output packets (indices e_first .. e_first+nrec-1)
+    // ---- write the visited steps
     const int nrec = s_nrec;
     const int64_t e_first = s_ebase;
-    if (kPoisson) {
-      for (int e = tid; e < nrec * 4; e += kWalkThreads) {
-        const int i = e / 4, j = e % 4;
-        const int ri = (int)(rec[i] % RING);
-        int32_t v = (int32_t)((pos_val[ri] >> (8 * j)) & 0xff);
-        if (d.ic) v = d.ia - v;  // BinomialGen: trials - res when p > 1/2
-        reinterpret_cast<int32_t*>(p.out)[off + (e_first + i) * 4 + j] = v;
-      }
-    } else {
-      for (int e = tid; e < nrec * P; e += kWalkThreads) {
-        const int i = e / P, j = e % P;
-        const uint64_t a = (uint64_t)rec[(size_t)i * 2 * P + j], b = (uint64_t)rec[(size_t)i * 2 * P + P + j];
-        if (DT == SD_F32) {
-          const float p1 = u2f((uint32_t)a), p2 = u2f((uint32_t)b);
-          reinterpret_cast<float*>(p.out)[off + (e_first + i) * P + j] = p1 / (p1 + p2);
-        } else {
-          const double p1 = u2d(a), p2 = u2d(b);
-          reinterpret_cast<double*>(p.out)[off + (e_first + i) * P + j] = p1 / (p1 + p2);
-        }
-      }
+    for (int e = tid; e < nrec * 4; e += kPoisThreads) {
+      const int i = e >> 2, j = e & 3;
+      int32_t v = (int32_t)((pos[rec[i]] >> (6 * j)) & 63);
+      if (d.ic) v = d.ia - v;  // BinomialGen: trials - res when p > 1/2
+      reinterpret_cast<int32_t*>(p.out)[off + (e_first + i) * 4 + j] = v;
     }
     __syncthreads();
-    if (s_stop) break;
+    if (s_stop || s_err) break;
   }
-
   // ---- state after the call
-  if (tid == 0) {
-    s_end = s_stop ? s_endpos : s;
-    if (!s_stop || s_err) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+  if (tid == 0 && (!s_stop || s_err)) {
+    if (!s_stop) s_end = s;
+    atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
   }
   __syncthreads();
-  const int64_t endp = s_end;
-  // packets consumed
-  int64_t np;
-  if (kPoisson) {
-    const int64_t fresh = endp - c0w / 4;  // half packets drawn fresh
-    np = (fresh + 1) / 2;
-  } else {
-    np = endp;
-  }
+  const int64_t fresh = s_end - c0w / 4;  // half packets drawn fresh
+  const int64_t np = (fresh + 1) / 2;     // packets consumed
+  const int prv = cur == 0 ? 2 : cur - 1, prv2 = prv == 0 ? 2 : prv - 1;
+  const int64_t nblk = min(nb + 1, max_blocks);  // blocks generated
   if (np > 0) {
-    // the last consumed packet lies in the last or second-to-last generated block
-    const int64_t nblk = nb + (s_stop ? 1 : 0);
     const int64_t lastb = (np - 1) / kN;
-    const int prv = cur == 0 ? 2 : cur - 1, prv2 = prv == 0 ? 2 : prv - 1;
-    const int64_t rr = np - lastb * kN;  // in [1, 312] by construction
+    const int64_t rr = np - lastb * kN;  // in [1, 312]
     if (lastb == nblk - 1) store_window(st, raw[cur], raw[prv], (int)rr);
     else if (lastb == nblk - 2) store_window(st, raw[prv], raw[prv2], (int)rr);
     else if (tid == 0) atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
   }
   if (tid == 0) {
-    if (kPoisson) {
-      const int64_t fresh = endp - c0w / 4;
-      if (fresh & 1) {
-        const int64_t pl = np - 1;
-        const uint64_t a = tp[(pl / kN) & 1][pl % kN][2], b = tp[(pl / kN) & 1][pl % kN][3];
-        st->half_cache[0] = (uint32_t)a;
-        st->half_cache[1] = (uint32_t)(a >> 32);
-        st->half_cache[2] = (uint32_t)b;
-        st->half_cache[3] = (uint32_t)(b >> 32);
-        st->half_valid = 1;
-      } else {
-        st->half_valid = 0;
-      }
+    if (fresh & 1) {  // the last packet's upper half stays in the engine's half cache
+      const int64_t pl = np - 1;
+      const int buf = (pl / kN == nblk - 1) ? cur : prv;
+      const uint64_t a = mt_temper(raw[buf][2][pl % kN]), b = mt_temper(raw[buf][3][pl % kN]);
+      st->half_cache[0] = (uint32_t)a;
+      st->half_cache[1] = (uint32_t)(a >> 32);
+      st->half_cache[2] = (uint32_t)b;
+      st->half_cache[3] = (uint32_t)(b >> 32);
+      st->half_valid = 1;
     } else {
-      for (int c = 0; c < 2; ++c) {
-        gs->s[1 + c].rest_cnt = fcnt[c];
-        for (int j = 0; j < 8; ++j) {
-          if (DT == SD_F64) {
-            gs->s[1 + c].rest[2 * j] = (uint32_t)fifo[c][j];
-            gs->s[1 + c].rest[2 * j + 1] = (uint32_t)(fifo[c][j] >> 32);
-          } else {
-            gs->s[1 + c].rest[j] = (uint32_t)fifo[c][j];
-          }
-        }
-      }
+      st->half_valid = 0;
     }
     st->consumed += (uint64_t)max(np, (int64_t)0);
   }
+}
+
+static cudaError_t run_poisson(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_poisson, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPoisSmem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_poisson<<<p.K, kPoisThreads, kPoisSmem, s>>>(p, d, max_blocks);
+  return cudaGetLastError();
 }
 
 // ===========================================================================
@@ -1946,24 +1732,9 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
   return cudaGetLastError();
 }
 
-template <int DT>
-static cudaError_t run_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
-  const size_t smem = walk_smem_bytes<DT>();
-  static bool attr[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_walk<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr[dev] = true;
-  }
-  k_walk<DT><<<p.K, kWalkThreads, smem, s>>>(p, d, max_blocks);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
-  if (d.dtype == GR_I32) return run_walk<SD_I32H>(p, d, max_blocks, s);
+  if (d.dtype == GR_I32) return run_poisson(p, d, max_blocks, s);
   if (d.dtype == GR_F32) return run_beta<SD_F32>(p, d, max_blocks, s);
   if (d.dtype == GR_F64) return run_beta<SD_F64>(p, d, max_blocks, s);
   return cudaErrorNotSupported;
