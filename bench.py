@@ -649,6 +649,9 @@ def run_case(args):
     if name == "uniform_f32":
         out = torch.empty((4096, 4096), dtype=torch.float32, device="cuda")
         fn = lambda: er.uniformReal(4096, 4096, urng, out=out)
+    elif name == "uniform_f32_big":  # 256 MiB output, twice the L2: DRAM traffic of the sweep's kernel
+        out = torch.empty((8192, 8192), dtype=torch.float32, device="cuda")
+        fn = lambda: er.uniformReal(8192, 8192, urng, out=out)
     elif name.startswith("mvnormal_d"):
         d = int(name[len("mvnormal_d"):])
         rng = np.random.default_rng(99)
@@ -700,7 +703,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="length of each serving trace")
     ap.add_argument("--case", default=None,
-                    help="run one named small workload instead (uniform_f32, mvnormal_dD, multinomial, wishart_d32, "
+                    help="run one named small workload instead (uniform_f32, uniform_f32_big, mvnormal_dD, multinomial, wishart_d32, "
                          "beta_f32, beta_f64, poisson4, gamma_compat), for profiler captures")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, multivariate and serving workloads (extra keys of the JSON line)")

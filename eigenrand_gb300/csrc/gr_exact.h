@@ -1,0 +1,51 @@
+// Exact integer forms of floating-point expressions of the reference, shared
+// by the kernels and the host-side checks (compiles as plain C++).
+#pragma once
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define GR_HD __host__ __device__ __forceinline__
+#else
+#define GR_HD inline
+#endif
+
+namespace gr {
+
+GR_HD int clz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
+GR_HD double bits_to_double(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// (double)k / 2147483647.0 (BalancedGen<double>'s quotient, round to
+// nearest), 0 <= k <= 2^31 - 1, with no division.  1 / (2^31 - 1) =
+// 2^-31 (1 + 2^-31 + 2^-62 + ...), so for 0 < k < 2^31 - 1 the quotient is
+// X 2^-62 + t with X = k (2^31 + 1) < 2^62 and 0 < t < 2^-62.  t never
+// vanishes, so no quotient lies on a midpoint: rounding to nearest keeps the
+// leading 53 bits of X and adds the bit after them (a carry out of the
+// significand moves into the exponent).
+GR_HD double div_2p31m1(uint32_t k) {
+  if (k == 0u) return 0.0;
+  if (k == 0x7fffffffu) return 1.0;
+  const uint64_t X = (uint64_t)k * 0x80000001ull;
+  const int lz = clz64(X);                 // 2 .. 32
+  const uint64_t N = X << lz;              // leading bit at 63; value N 2^(-62-lz)
+  const uint64_t sig = N >> 11;            // 53 bits with the leading one at bit 52
+  const uint64_t rnd = (N >> 10) & 1ull;
+  return bits_to_double(((uint64_t)(1023 - lz) << 52) + sig + rnd);
+}
+
+}  // namespace gr

@@ -15,6 +15,7 @@
 
 #include <cstdint>
 
+#include "gr_exact.h"
 #include "gr_internal.h"
 #include "gr_kernels.cuh"
 #include "gr_math.cuh"
@@ -204,10 +205,11 @@ __device__ __forceinline__ double tf64(uint64_t r, const DistParams& d) {
   return 0.0;
 }
 
-// double balanced from one u32 word (rng.half() path)
+// double balanced from one u32 word (rng.half() path); the quotient by
+// 2^31 - 1 in integer form (gr_exact.h), bit-identical to the division
 template <int KIND>
 __device__ __forceinline__ double tw64(uint32_t w, const DistParams& d) {
-  double z = (double)(int32_t)(w & 0x7fffffffu) / 2147483647.0;
+  double z = div_2p31m1(w & 0x7fffffffu);
   return KIND == GR_BALANCED ? z * 2.0 - 1.0 : z * d.da + d.db;
 }
 

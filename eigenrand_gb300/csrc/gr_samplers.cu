@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <type_traits>
 
@@ -1320,42 +1321,94 @@ static cudaError_t run_poisson(const Plan& p, const DistParams& d, int64_t max_b
 // component is closed form (alpha == 1: 1 packet; integer alpha < 20: alpha
 // packets) or a rejection sampler (GS trials of 3 packets, tan trials of 2)
 // with its own CompressMask carry.
-// Per block of 312 packets:
+// The ring of packets is the newest two raw engine blocks in shared memory,
+// tempered where read (no tempered copy), so four CTAs fit on an SM and all
+// engines run in one wave.  Per block of 312 packets:
 //   masks  every start position of a rejection component gets its P-lane
 //          accept mask (all threads; ballot per P lanes);
 //   walk   thread 0 follows the reference automaton over the masks only:
 //          output packet sources (closed form / full trial at x, or FIFO
 //          packet at a lane offset) and the partial trials it consumed;
-//   write  all threads recompute the values of the consumed trials only, put
-//          partial-trial lanes into a per-component lane buffer at their FIFO
-//          position, and write p1 / (p1 + p2); lanes still carried move to
-//          the front of the lane buffer.
+//   values the accepted lanes of the consumed partial trials are listed by
+//          FIFO slot; then one thread per lane, with no idle lanes, computes
+//          them into the lane buffer and the full-trial lanes of the
+//          rejection component into a value buffer (a value-only evaluation:
+//          acceptance is already known);
+//   write  p1 / (p1 + p2) per output lane, the other component computed in
+//          place; lanes still carried move to the front of the lane buffer.
 // ===========================================================================
 namespace {
 
 constexpr int kBetaThreads = 160;
 constexpr int kBetaRing = 640;              // positions whose masks are kept
-constexpr int kBetaRec = 160;               // output packets per block step
-constexpr int kBetaPT = 128;                // partial trials per component per block step
-constexpr int kBetaLB = 8 + kBetaPT * 8;    // lane buffer per component
+constexpr int kBetaRec = 160;               // output packets per walk step
+constexpr int kBetaPT = 128;                // partial trials per component per walk step
 constexpr int64_t kBetaMargin = 96;         // evaluated positions kept ahead of an output packet
 
 template <int DT>
+__host__ __device__ constexpr int beta_lanes() {
+  return DT == SD_F64 ? 4 : 8;
+}
+template <int DT>
+__host__ __device__ constexpr int beta_lb() {  // lane buffer per component: carried lanes + partial-trial lanes
+  return 8 + kBetaPT * beta_lanes<DT>();
+}
+
+template <int DT>
 __host__ __device__ constexpr size_t beta_smem_bytes() {
-  return (size_t)5 * kLanes * kN * 8 +                       // raw x3, tp x2
-         (size_t)kBetaRec * 2 * 8 +                          // rec
-         (size_t)2 * kBetaPT * 8 +                           // partial trial positions
-         (size_t)2 * kBetaLB * (DT == SD_F64 ? 8 : 4) +      // lane buffers
-         (size_t)2 * kBetaPT * 4 * 2 +                       // lane offsets, masks
-         (size_t)2 * kBetaRing;                              // masks per position
+  return (size_t)3 * kLanes * kN * 8 +                                             // raw windows
+         (size_t)kBetaRec * 2 * 8 +                                                // rec
+         (size_t)2 * kBetaPT * 8 +                                                 // partial trial positions
+         ((size_t)2 * beta_lb<DT>() + (size_t)kBetaRec * beta_lanes<DT>()) *       // lane buffers, values of
+             (DT == SD_F64 ? 8 : 4) +                                              //   full trials
+         (size_t)2 * kBetaPT * 4 * 2 +                                             // lane offsets, masks
+         (size_t)kBetaRec * 2 +                                                    // full-trial records
+         (size_t)2 * kBetaPT * beta_lanes<DT>() * 2 +                              // partial-lane tasks
+         (size_t)2 * kBetaRing;                                                    // masks per position
+}
+
+// Constants of one GammaGen component of a BetaGen, computed on the host
+// with the same IEEE expressions the generator uses (so with the same bits),
+// and passed as a kernel parameter: in the sampling loops they cost a
+// constant-bank load, never a division.
+struct BetaComp {
+  int type, U;                      // gamma_branch: type << 8 | packets
+  float af, f_px, f_inv, f_am1, f_sq;
+  float f_band;                     // band of the float pre-test of a double GS trial
+  double ad, d_px, d_inv, d_am1, d_sq;
+  uint64_t tpx;                     // ceil(px * 2^52): double GS branch on the integer fraction
+};
+struct BetaConsts {
+  BetaComp c[2];
+};
+
+BetaComp beta_component(int branch, float af, double ad) {
+  BetaComp b;
+  b.type = branch >> 8;
+  b.U = branch & 0xff;
+  b.af = af;
+  b.f_px = (float)(2.7182818284590452 / ((double)af + 2.7182818284590452));
+  b.f_inv = 1 / af;
+  b.f_am1 = af - 1;
+  b.f_sq = std::sqrt(2 * af - 1);
+  b.f_band = (float)(0x1p-18 * (1.0 + 40.0 / ad));
+  b.ad = ad;
+  b.d_px = 2.7182818284590452 / (ad + 2.7182818284590452);
+  b.d_inv = 1 / ad;
+  b.d_am1 = ad - 1;
+  b.d_sq = std::sqrt(2 * ad - 1);
+  b.tpx = (uint64_t)std::ceil(b.d_px * 0x1p52);
+  return b;
 }
 
 // Value (closed form) or candidate (rejection trial) of one GammaGen
-// component at packet position x, lane j, with the accept flag of a trial.
-template <int DT, class WF, class RF>
-__device__ __forceinline__ uint64_t beta_comp(int type, int U, float af, double ad, int64_t x, int j, WF&& word,
-                                              RF&& rval, bool& acc) {
+// component at packet position x, lane j.  ACC: also decide acceptance (the
+// rejection types); without it only the candidate is computed, for lanes
+// already known to be accepted (the same expressions, so the same bits).
+template <int DT, bool ACC, class WF, class RF>
+__device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j, WF&& word, RF&& rval, bool& acc) {
   acc = true;
+  const int type = g.type, U = g.U;
   if (DT == SD_F32) {
     auto Uf = [&](int q) { return ur_f(word((x + q) * 8 + j)); };
     if (type == 0) return f2u(1.0f * (-(logf_(1.0f - Uf(0)) / 1.0f)));
@@ -1365,27 +1418,27 @@ __device__ __forceinline__ uint64_t beta_comp(int type, int U, float af, double 
       return f2u(-(1.0f * logf_(y)));
     }
     if (type == 2) {
-      const float ux = Uf(0), vx = Uf(1) + 1.1920928955078125e-07f / 8, ux2 = Uf(2);
+      const float ux = Uf(0), vx = Uf(1) + 1.1920928955078125e-07f / 8;
       const float lv = logf_(vx);
-      const bool cc = ux < (float)(2.7182818284590452 / (af + 2.7182818284590452));
-      float xx, qx;
-      if (cc) {
-        xx = expf_((1 / af) * lv);
-        qx = expf_(-xx);
+      float xx;
+      if (ux < g.f_px) {
+        xx = expf_(g.f_inv * lv);
+        if (ACC) acc = Uf(2) < expf_(-xx);
       } else {
         xx = 1.0f - lv;
-        qx = expf_(logf_(xx) * (af - 1));
+        if (ACC) acc = Uf(2) < expf_(logf_(xx) * g.f_am1);
       }
-      acc = ux2 < qx;
       return f2u(1.0f * xx);
     }
-    const float a1 = af - 1, sq = sqrtf(2 * af - 1);
+    const float a1 = g.f_am1, sq = g.f_sq;
     float ys, yc;
     sincosf_((float)3.1415926535897932 * Uf(0), ys, yc);
     const float yx = ys / yc;
     const float xx = sq * yx + a1;
-    const float ub = (yx * yx + 1.0f) * expf_(a1 * logf_(xx / a1) - yx * sq);
-    acc = (0.0f < xx) && (Uf(1) <= ub);
+    if (ACC) {
+      const float ub = (yx * yx + 1.0f) * expf_(a1 * logf_(xx / a1) - yx * sq);
+      acc = (0.0f < xx) && (Uf(1) <= ub);
+    }
     return f2u(1.0f * xx);
   } else {
     auto Ud = [&](int q) { return ur_d(rval((x + q) * 4 + j)); };
@@ -1396,27 +1449,27 @@ __device__ __forceinline__ uint64_t beta_comp(int type, int U, float af, double 
       return d2u(-(1.0 * log_(y)));
     }
     if (type == 2) {
-      const double ux = Ud(0), vx = Ud(1) + 2.220446049250313e-16 / 8, ux2 = Ud(2);
+      const double ux = Ud(0), vx = Ud(1) + 2.220446049250313e-16 / 8;
       const double lv = log_(vx);
-      const bool cc = ux < (2.7182818284590452 / (ad + 2.7182818284590452));
-      double xx, qx;
-      if (cc) {
-        xx = exp_((1 / ad) * lv);
-        qx = exp_(-xx);
+      double xx;
+      if (ux < g.d_px) {
+        xx = exp_(g.d_inv * lv);
+        if (ACC) acc = Ud(2) < exp_(-xx);
       } else {
         xx = 1.0 - lv;
-        qx = exp_(log_(xx) * (ad - 1));
+        if (ACC) acc = Ud(2) < exp_(log_(xx) * g.d_am1);
       }
-      acc = ux2 < qx;
       return d2u(1.0 * xx);
     }
-    const double a1 = ad - 1, sq = sqrt(2 * ad - 1);
+    const double a1 = g.d_am1, sq = g.d_sq;
     double ys, yc;
     sincos_(3.1415926535897932 * Ud(0), ys, yc);
     const double yx = ys / yc;
     const double xx = sq * yx + a1;
-    const double ub = (yx * yx + 1.0) * exp_(a1 * log_(xx / a1) - yx * sq);
-    acc = (0.0 < xx) && (Ud(1) <= ub);
+    if (ACC) {
+      const double ub = (yx * yx + 1.0) * exp_(a1 * log_(xx / a1) - yx * sq);
+      acc = (0.0 < xx) && (Ud(1) <= ub);
+    }
     return d2u(1.0 * xx);
   }
 }
@@ -1424,19 +1477,22 @@ __device__ __forceinline__ uint64_t beta_comp(int type, int U, float af, double 
 }  // namespace
 
 template <int DT>  // SD_F32 or SD_F64
-__global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int64_t max_blocks) {
-  constexpr int P = DT == SD_F32 ? 8 : 4;
+__global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, int64_t max_blocks) {
+  constexpr int P = beta_lanes<DT>();
+  constexpr int LB = beta_lb<DT>();
   using V = typename std::conditional<DT == SD_F64, uint64_t, uint32_t>::type;
   extern __shared__ __align__(16) uint64_t beta_dyn[];
   uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(beta_dyn);
-  uint64_t(*tp)[kN][kLanes] = reinterpret_cast<uint64_t(*)[kN][kLanes]>(beta_dyn + 3 * kLanes * kN);
-  int64_t* rec = reinterpret_cast<int64_t*>(beta_dyn + 5 * kLanes * kN);   // [kBetaRec][2]
+  int64_t* rec = reinterpret_cast<int64_t*>(beta_dyn + 3 * kLanes * kN);   // [kBetaRec][2]
   int64_t* ptx = rec + kBetaRec * 2;                                         // [2][kBetaPT]
-  V* lanebuf = reinterpret_cast<V*>(ptx + 2 * kBetaPT);                      // [2][kBetaLB]
-  int32_t* pA = reinterpret_cast<int32_t*>(lanebuf + 2 * kBetaLB);           // [2][kBetaPT]
+  V* lanebuf = reinterpret_cast<V*>(ptx + 2 * kBetaPT);                      // [2][LB]
+  V* fullval = lanebuf + 2 * LB;                                             // [kBetaRec][P]
+  int32_t* pA = reinterpret_cast<int32_t*>(fullval + kBetaRec * P);          // [2][kBetaPT]
   uint32_t* pm = reinterpret_cast<uint32_t*>(pA + 2 * kBetaPT);              // [2][kBetaPT]
-  uint8_t* pmask = reinterpret_cast<uint8_t*>(pm + 2 * kBetaPT);             // [2][kBetaRing]
-  __shared__ int s_nrec, s_np[2], s_fc[2], s_A[2];
+  uint16_t* fr = reinterpret_cast<uint16_t*>(pm + 2 * kBetaPT);              // [kBetaRec]
+  uint16_t* ptask = fr + kBetaRec;                                           // [2][kBetaPT * P]
+  uint8_t* pmask = reinterpret_cast<uint8_t*>(ptask + 2 * kBetaPT * P);      // [2][kBetaRing]
+  __shared__ int s_nrec, s_nf, s_np[2], s_fc[2], s_A[2], s_A0[2];
   __shared__ int s_stop, s_err, s_more;
   __shared__ int64_t s_ebase, s_end;
 
@@ -1450,16 +1506,19 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
   if (n == 0) return;
   const int64_t Npk = n / P;
 
-  const int type0 = d.ia >> 8, U0 = d.ia & 0xff, type1 = d.ib >> 8, U1 = d.ib & 0xff;
+  const int type0 = bk.c[0].type, U0 = bk.c[0].U, type1 = bk.c[1].type, U1 = bk.c[1].U;
   const int umax = max(max(U0, U1), 3);
+  // the component whose full-trial values are computed ahead of the outputs
+  // (a rejection one); the other is computed where its output is written
+  const int bc = type0 >= 2 ? 0 : (type1 >= 2 ? 1 : -1);
   load_window(raw[0], &st->win[0][0], kN);
   // carried lanes of the two GammaGens (generator slots 1 and 2)
   if (tid < 2 * 8) {
     const int c = tid / 8, j = tid % 8;
     const GenSlot& g = gs->s[1 + c];
     if (j < g.rest_cnt)
-      lanebuf[c * kBetaLB + j] = (V)(DT == SD_F64 ? ((uint64_t)g.rest[2 * j] | ((uint64_t)g.rest[2 * j + 1] << 32))
-                                                  : (uint64_t)g.rest[j]);
+      lanebuf[c * LB + j] = (V)(DT == SD_F64 ? ((uint64_t)g.rest[2 * j] | ((uint64_t)g.rest[2 * j + 1] << 32))
+                                             : (uint64_t)g.rest[j]);
   }
   if (tid == 0) {
     s_err = 0;
@@ -1468,47 +1527,42 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
     s_fc[1] = gs->s[2].rest_cnt;
   }
   __syncthreads();
-  int64_t ring_new = 0;  // newest ring block's first packet (ring_packet)
-  int ring_slot = 0;
+  // The newest two raw blocks are the ring of packets; words are tempered
+  // where they are read.
+  int64_t ring_new = 0;  // first packet of the newest block
+  int wn = 0, wp = 0;    // raw windows of the newest block and of the one before
+  auto tword = [&](int64_t rel, int l) -> uint64_t {
+    int dd = (int)(rel - ring_new);
+    int w = wn;
+    if (dd < 0) {
+      dd += kN;
+      w = wp;
+    }
+    if ((unsigned)dd >= (unsigned)kN) dd = 0;  // outside the ring: never read past the buffers
+    return mt_temper(raw[w][l][dd]);
+  };
   auto word = [&](int64_t w) -> uint32_t {
-    const int64_t rel = w >> 3;
-    const uint64_t v = ring_packet(tp, rel, ring_new, ring_slot)[(w & 7) >> 1];
+    const uint64_t v = tword(w >> 3, (int)((w & 7) >> 1));
     return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
   };
-  auto rval = [&](int64_t r) -> uint64_t {
-    const int64_t rel = r >> 2;
-    return ring_packet(tp, rel, ring_new, ring_slot)[r & 3];
+  auto rval = [&](int64_t r) -> uint64_t { return tword(r >> 2, (int)(r & 3)); };
+  auto trial = [&](int c, int64_t x, int j, bool& acc) -> uint64_t {
+    return c == 0 ? beta_comp<DT, true>(bk.c[0], x, j, word, rval, acc)
+                  : beta_comp<DT, true>(bk.c[1], x, j, word, rval, acc);
   };
-  auto comp = [&](int c, int64_t x, int j, bool& acc) -> uint64_t {
-    return c == 0 ? beta_comp<DT>(type0, U0, d.fa, d.da, x, j, word, rval, acc)
-                  : beta_comp<DT>(type1, U1, d.fb, d.db, x, j, word, rval, acc);
-  };
-  // value of an accepted trial lane (or a closed-form draw): double GS lanes
-  // skip the acceptance bound
-  uint64_t gtpx[2];
-  double ginv[2];
-#pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    const double ad = c == 0 ? d.da : d.db;
-    gtpx[c] = (uint64_t)ceil((2.7182818284590452 / (ad + 2.7182818284590452)) * 0x1p52);
-    ginv[c] = 1 / ad;
-  }
+  // value of an accepted trial lane or a closed-form draw; double GS lanes
+  // use the branch threshold in integer form
   auto value = [&](int c, int64_t x, int j) -> uint64_t {
-    if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)
-      return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), gtpx[c], ginv[c]));
     bool acc;
-    return comp(c, x, j, acc);
+    if (c == 0) {
+      if (DT == SD_F64 && type0 == 2)
+        return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[0].tpx, bk.c[0].d_inv));
+      return beta_comp<DT, false>(bk.c[0], x, j, word, rval, acc);
+    }
+    if (DT == SD_F64 && type1 == 2)
+      return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[1].tpx, bk.c[1].d_inv));
+    return beta_comp<DT, false>(bk.c[1], x, j, word, rval, acc);
   };
-  // float constants of the double GS pre-test: px, 1/alpha, alpha - 1, band
-  float gsf[2][4];
-#pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    const double ad = c == 0 ? d.da : d.db;
-    gsf[c][0] = (float)(2.7182818284590452 / (ad + 2.7182818284590452));
-    gsf[c][1] = (float)(1.0 / ad);
-    gsf[c][2] = (float)(ad - 1.0);
-    gsf[c][3] = (float)(0x1p-18 * (1.0 + 40.0 / ad));
-  }
   // rejection components evaluated at every position
   const int nrej = (type0 >= 2 ? 1 : 0) + (type1 >= 2 ? 1 : 0);
   const int rej0 = type0 >= 2 ? 0 : 1;  // first rejection component
@@ -1522,36 +1576,41 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
   int cur = 0;
   int64_t nb = 0;
   for (; nb < max_blocks; ++nb) {
-    const int slot = (int)(nb & 1);
     const int nxt = cur == 2 ? 0 : cur + 1;
-    mt_block(raw[cur], raw[nxt], [&](int i, const uint64_t* pk) {
-#pragma unroll
-      for (int l = 0; l < kLanes; ++l) tp[slot][i][l] = pk[l];
-    });
-    cur = nxt; ring_new = nb * kN; ring_slot = slot;
+    mt_block(raw[cur], raw[nxt], [&](int, const uint64_t*) {});
+    wp = cur;
+    cur = nxt;
+    wn = cur;
+    ring_new = nb * kN;
     const int64_t lim = (nb + 1) * kN - umax + 1;  // positions whose packets all exist
     if (tid == 0 && lim - s > kBetaRing) s_err = 1;
     // ---- masks of the rejection components at positions [done_pos, lim)
+    // (32-bit index arithmetic with shifts: a 64-bit division by a runtime
+    // value would run on the FP64 pipe)
     if (nrej > 0) {
-      const int64_t cnt = (lim - done_pos) * nrej * P;
-      for (int64_t base = 0; base < cnt; base += kBetaThreads) {
-        const int64_t e = base + tid;
+      constexpr int LP = P == 8 ? 3 : 2;
+      const int sh = LP + nrej - 1;  // log2(nrej * P)
+      const int cnt = (int)(lim - done_pos) << sh;
+      for (int base = 0; base < cnt; base += kBetaThreads) {
+        const int e = base + tid;
         const bool valid = e < cnt;
         bool acc = false;
         int c = 0;
         int64_t x = 0;
         if (valid) {
-          const int64_t xi = e / (nrej * P);
-          const int ci = (int)((e / P) % nrej);
+          const int xi = e >> sh;
+          const int ci = (e >> LP) & (nrej - 1);
           c = nrej == 2 ? ci : rej0;
           x = done_pos + xi;
-          const int j = (int)(e % P);
+          const int j = e & (P - 1);
           int f = -1;
           if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)  // float pre-test of a double GS trial
-            f = gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), gsf[c][0], gsf[c][1],
-                              gsf[c][2], gsf[c][3]);
+            f = c == 0 ? gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[0].f_px,
+                                       bk.c[0].f_inv, bk.c[0].f_am1, bk.c[0].f_band)
+                       : gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[1].f_px,
+                                       bk.c[1].f_inv, bk.c[1].f_am1, bk.c[1].f_band);
           if (f >= 0) acc = f == 1;
-          else comp(c, x, j, acc);
+          else trial(c, x, j, acc);
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, acc);
         if (valid && (e % P) == 0)
@@ -1560,14 +1619,16 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
     }
     done_pos = max(done_pos, lim);
     __syncthreads();
-    // walk, then write, until the evaluated positions are used up (a walk
-    // step stops early when its record buffers fill)
+    // walk, then values, then outputs, until the evaluated positions are used
+    // up (a walk step stops early when its record buffers fill)
     for (;;) {
       // ---- walk (thread 0): sources of the next output packets
       if (tid == 0) {
         s_ebase = E;
         s_more = 0;
-        int nrec = 0, np[2] = {0, 0}, A[2] = {fc[0], fc[1]};
+        s_A0[0] = fc[0];
+        s_A0[1] = fc[1];
+        int nrec = 0, nf = 0, np[2] = {0, 0}, A[2] = {fc[0], fc[1]};
         const int64_t pk_end = (nb + 1) * kN;  // packets generated so far
         if (s < nb * kN - kN) s_err = 1;       // packets before s left the ring
         while (E < Npk && s + kBetaMargin <= done_pos) {
@@ -1576,7 +1637,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
             break;
           }
           int64_t x = s;
-          bool bad = false;
+          bool bad = false, full_bc = false;
           for (int c = 0; c < 2 && !bad; ++c) {
             const int ty = c == 0 ? type0 : type1, U = c == 0 ? U0 : U1;
             if (ty <= 1) {
@@ -1594,6 +1655,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
               const int cn = __popc(m);
               if (cn == P) {
                 rec[nrec * 2 + c] = x;
+                if (c == bc) full_bc = true;
                 x += U;
                 break;
               }
@@ -1615,11 +1677,13 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
             s_err = 1;
             break;
           }
+          if (full_bc) fr[nf++] = (uint16_t)nrec;
           ++nrec;
           s = x;
           ++E;
         }
         s_nrec = nrec;
+        s_nf = nf;
         s_np[0] = np[0];
         s_np[1] = np[1];
         s_A[0] = A[0];
@@ -1632,15 +1696,30 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
         }
       }
       __syncthreads();
-      // ---- values of the consumed partial trials into the lane buffers
+      // ---- accepted lanes of the partial trials, listed by their FIFO slot
       const int np0 = s_np[0], np1 = s_np[1];
+      const int a00 = s_A0[0], a01 = s_A0[1];
       for (int e = tid; e < (np0 + np1) * P; e += kBetaThreads) {
         const int c = e < np0 * P ? 0 : 1;
         const int kk = (c == 0 ? e : e - np0 * P) / P, j = e % P;
         const uint32_t m = pm[c * kBetaPT + kk];
-        if ((m >> j) & 1u) {
-          const uint64_t v = value(c, ptx[c * kBetaPT + kk], j);
-          lanebuf[c * kBetaLB + pA[c * kBetaPT + kk] + __popc(m & ((1u << j) - 1))] = (V)v;
+        if ((m >> j) & 1u)
+          ptask[c * kBetaPT * P + pA[c * kBetaPT + kk] - (c == 0 ? a00 : a01) + __popc(m & ((1u << j) - 1))] =
+              (uint16_t)(kk * 8 + j);
+      }
+      __syncthreads();
+      // ---- values, one lane per thread with no idle lanes: full trials of
+      // the buffered component, then the accepted partial-trial lanes
+      const int t0 = s_nf * P, tp0 = s_A[0] - a00, tp1 = s_A[1] - a01;
+      for (int t = tid; t < t0 + tp0 + tp1; t += kBetaThreads) {
+        if (t < t0) {
+          const int i = fr[t / P], j = t % P;
+          fullval[i * P + j] = (V)value(bc, rec[i * 2 + bc], j);
+        } else {
+          const int c = t < t0 + tp0 ? 0 : 1;
+          const int q = c == 0 ? t - t0 : t - t0 - tp0;
+          const int tk = ptask[c * kBetaPT * P + q];
+          lanebuf[c * LB + (c == 0 ? a00 : a01) + q] = (V)value(c, ptx[c * kBetaPT + (tk >> 3)], tk & 7);
         }
       }
       __syncthreads();
@@ -1653,11 +1732,9 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
           const int64_t src = rec[i * 2 + c];
-          if (src >= 0) {
-            v[c] = value(c, src, j);
-          } else {
-            v[c] = (uint64_t)lanebuf[c * kBetaLB + (int)(-src - 1) + j];
-          }
+          if (src < 0) v[c] = (uint64_t)lanebuf[c * LB + (int)(-src - 1) + j];
+          else if (c == bc) v[c] = (uint64_t)fullval[i * P + j];
+          else v[c] = value(c, src, j);
         }
         if (DT == SD_F32) {
           const float p1 = u2f((uint32_t)v[0]), p2 = u2f((uint32_t)v[1]);
@@ -1672,9 +1749,9 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
       V carry = 0;
       const int cc = tid / 8, cj = tid % 8;
       const bool mover = tid < 16 && cj < s_fc[cc];
-      if (mover) carry = lanebuf[cc * kBetaLB + s_A[cc] - s_fc[cc] + cj];
+      if (mover) carry = lanebuf[cc * LB + s_A[cc] - s_fc[cc] + cj];
       __syncthreads();
-      if (mover) lanebuf[cc * kBetaLB + cj] = carry;
+      if (mover) lanebuf[cc * LB + cj] = carry;
       __syncthreads();
       if (!s_more || s_stop || s_err) break;
     }
@@ -1700,7 +1777,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
   if (tid < 2 * 8) {
     const int c = tid / 8, j = tid % 8;
     GenSlot& g = gs->s[1 + c];
-    const uint64_t v = j < s_fc[c] ? (uint64_t)lanebuf[c * kBetaLB + j] : 0;
+    const uint64_t v = j < s_fc[c] ? (uint64_t)lanebuf[c * LB + j] : 0;
     if (DT == SD_F64) {
       g.rest[2 * j] = (uint32_t)v;
       g.rest[2 * j + 1] = (uint32_t)(v >> 32);
@@ -1718,6 +1795,9 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, DistParams d, int
 
 template <int DT>
 static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  BetaConsts bk;
+  bk.c[0] = beta_component(d.ia, d.fa, d.da);
+  bk.c[1] = beta_component(d.ib, d.fb, d.db);
   constexpr size_t smem = beta_smem_bytes<DT>();
   static bool attr[64] = {};
   int dev = 0;
@@ -1728,7 +1808,7 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  k_beta<DT><<<p.K, kBetaThreads, smem, s>>>(p, d, max_blocks);
+  k_beta<DT><<<p.K, kBetaThreads, smem, s>>>(p, bk, max_blocks);
   return cudaGetLastError();
 }
 
