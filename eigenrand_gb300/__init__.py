@@ -27,10 +27,12 @@ from ._lib import GrError, KINDS, F32, F64, I32, U64
 __all__ = [
     "GrError", "Vmt19937_64", "raw_u64", "version",
     "uniformReal", "balanced", "normal", "lognormal", "exponential", "cauchy", "weibull", "extremeValue",
-    "gamma", "beta", "studentT", "chiSquared", "poisson", "binomial", "discrete", "randBits",
+    "gamma", "beta", "studentT", "chiSquared", "poisson", "binomial", "discrete", "randBits", "bernoulli",
+    "geometric", "fisherF",
     "StdUniformRealGen", "UniformRealGen", "BalancedGen", "Balanced2Gen", "StdNormalGen", "NormalGen",
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
-    "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen",
+    "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen", "BernoulliGen",
+    "GeometricGen", "FisherFGen",
     "sample_batched",
     "MvNormalGen", "WishartGen", "InvWishartGen", "DirichletGen", "MultinomialGen", "makeMvNormalGen",
     "makeMvNormalGenFromLt", "makeWishartGen", "makeWishartGenFromLt", "makeInvWishartGen",
@@ -301,6 +303,30 @@ class RandbitsGen(_Gen):
         super().__init__(torch.int32)
 
 
+class BernoulliGen(_Gen):
+    """BernoulliGen<Scalar>(p): 1 or 0 in float32, float64 or int32 (Basic.h:669-708)."""
+    _kind = "BERNOULLI"
+
+    def __init__(self, p=0.5, dtype=torch.float32):
+        super().__init__(dtype, p)
+
+
+class FisherFGen(_Gen):
+    """FisherFGen(m, n) = BetaGen(m/2, n/2) mapped to (n/m) x / (1 - x) (NormalExp.h:984-1023)."""
+    _kind = "FISHER_F"
+
+    def __init__(self, m=1.0, n=1.0, dtype=torch.float32):
+        super().__init__(dtype, m, n)
+
+
+class GeometricGen(_Gen):
+    """GeometricGen<int32_t>(p) (Discrete.h:1338-1376)."""
+    _kind = "GEOMETRIC"
+
+    def __init__(self, p=0.5):
+        super().__init__(torch.int32, p)
+
+
 # ---- free functions (Dists/*.h tails) -----------------------------------
 def uniformReal(rows, cols, urng, min=None, max=None, dtype=torch.float32, out=None, stream=None):
     if min is None and max is None:
@@ -372,6 +398,18 @@ def discrete(rows, cols, urng, weights, out=None, stream=None):
 
 def randBits(rows, cols, urng, out=None, stream=None):
     return _sample("RANDBITS", rows, cols, urng, torch.int32, out=out, stream=stream)
+
+
+def bernoulli(rows, cols, urng, p=0.5, dtype=torch.float32, out=None, stream=None):
+    return _sample("BERNOULLI", rows, cols, urng, dtype, p, out=out, stream=stream)
+
+
+def fisherF(rows, cols, urng, m=1.0, n=1.0, dtype=torch.float32, out=None, stream=None):
+    return _sample("FISHER_F", rows, cols, urng, dtype, m, n, out=out, stream=stream)
+
+
+def geometric(rows, cols, urng, p=0.5, out=None, stream=None):
+    return _sample("GEOMETRIC", rows, cols, urng, torch.int32, p, out=out, stream=stream)
 
 
 # ---- vectorize-over-params, many sets in one launch ------------------------

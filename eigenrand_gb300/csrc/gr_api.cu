@@ -235,6 +235,13 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       p.fa = (float)a;
       p.da = a;
       break;
+    case GR_BERNOULLI:  // BernoulliGen(p): (uint32_t)(p * 0x80000000), compared as int32 (Basic.h:680-684)
+      if (!(a >= 0 && a <= 1)) return fail(GR_ERR_INVALID, "bernoulli needs 0 <= p <= 1");
+      p.ia = (int32_t)(uint32_t)(a * 2147483648.0);
+      break;
+    case GR_GEOMETRIC:  // GeometricGen(p): rlog_q = 1 / log(1 - p), set as a float packet (Discrete.h:1353-1374)
+      p.fa = (float)(1 / std::log(1 - a));
+      break;
     case GR_WEIBULL:  // pset1(1 / a) in the scalar type
       p.fa = 1.0f / (float)a;
       p.fb = (float)b;
@@ -277,17 +284,32 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
       }
       break;
     }
-    case GR_BETA: {  // BetaGen(a, b), NormalExp.h:949-976
-      const float af = (float)a, bf = (float)b;
+    case GR_FISHER_F:  // FisherFGen(m, n): BetaGen(m/2, n/2) in the scalar type, NormalExp.h:997-1000
+    case GR_BETA: {    // BetaGen(a, b), NormalExp.h:949-976
+      double ba = a, bb = b;
+      if (d.kind == GR_FISHER_F) {
+        if (f) {
+          ba = (double)((float)a * 0.5f);
+          bb = (double)((float)b * 0.5f);
+        } else {
+          ba = a * 0.5;
+          bb = b * 0.5;
+        }
+        p.kind = GR_BETA;
+        p.post = 1;  // (b/a) x / (1 - x), NormalExp.h:1016-1021
+        p.fh = (float)bb / (float)ba;
+        p.dh = bb / ba;
+      }
+      const float af = (float)ba, bf = (float)bb;
       p.fa = af;
       p.fb = bf;
       p.fc = 1 / af;
       p.fd = 1 / bf;
-      p.da = a;
-      p.db = b;
-      p.dc = 1 / a;
-      p.dd = 1 / b;
-      p.ic = f ? (af < 1 && bf < 1) : (a < 1 && b < 1);
+      p.da = ba;
+      p.db = bb;
+      p.dc = 1 / ba;
+      p.dd = 1 / bb;
+      p.ic = f ? (af < 1 && bf < 1) : (ba < 1 && bb < 1);
       break;
     }
     case GR_POISSON: {  // PoissonGen(mean), Discrete.h:806-812 (double), packet constants in float

@@ -186,6 +186,8 @@ __device__ __forceinline__ float tf32(uint32_t w, const DistParams& d) {
   }
   if (KIND == GR_WEIBULL) return expf_(logf_(-logf_(1.0f - ur_f(w))) * d.fa) * d.fb;
   if (KIND == GR_EXTREME_VALUE) return d.fa - logf_(-logf_(ur_f(w) + 1.1920928955078125e-07f / 8)) * d.fb;
+  // BernoulliGen<float>: the word of the lane, masked, compared signed
+  if (KIND == GR_BERNOULLI) return ((int32_t)(w & 0x7fffffffu) < d.ia) ? 1.0f : 0.0f;
   return 0.0f;
 }
 
@@ -202,6 +204,9 @@ __device__ __forceinline__ double tf64(uint64_t r, const DistParams& d) {
   }
   if (KIND == GR_WEIBULL) return exp_(log_(-log_(1.0 - ur_d(r))) * d.da) * d.db;
   if (KIND == GR_EXTREME_VALUE) return d.da - log_(-log_(ur_d(r) + 2.220446049250313e-16 / 8)) * d.db;
+  // BernoulliGen<double>: the compare runs on the eight 32-bit words and the
+  // blend reads each 64-bit element's sign, the compare of its high word
+  if (KIND == GR_BERNOULLI) return ((int32_t)((uint32_t)(r >> 32) & 0x7fffffffu) < d.ia) ? 1.0 : 0.0;
   return 0.0;
 }
 
@@ -213,9 +218,17 @@ __device__ __forceinline__ double tw64(uint32_t w, const DistParams& d) {
   return KIND == GR_BALANCED ? z * 2.0 - 1.0 : z * d.da + d.db;
 }
 
+// _mm_cvttps_epi32 of one lane: truncation; NaN and out of range give INT_MIN
+__device__ __forceinline__ int32_t cvtt_f32(float x) {
+  return (x >= -2147483648.0f && x < 2147483648.0f) ? (int32_t)x : (int32_t)0x80000000u;
+}
+
 template <int KIND>
 __device__ __forceinline__ int32_t tw32(uint32_t w, const DistParams& d) {
   if (KIND == GR_RANDBITS) return (int32_t)w;
+  if (KIND == GR_BERNOULLI) return ((int32_t)(w & 0x7fffffffu) < d.ia) ? 1 : 0;
+  // GeometricGen<int32_t>: pcast(ptruncate(plog(1 - u) * rlog_q)), Discrete.h:1368-1374
+  if (KIND == GR_GEOMETRIC) return cvtt_f32(truncf(logf_(1.0f - ur_f(w)) * d.fa));
   // DiscreteGen<int32_t,int32_t>, Discrete.h:455-470
   if (d.ncdf > 0) {
     int32_t r = d.ncdf - 1;
@@ -268,7 +281,10 @@ __global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const Call
   if (n == 0) return;
 
   // --- caches the call starts from
-  constexpr bool kUsesHalf = (MODE == M_W64) || (MODE == M_W32 && KIND == GR_RANDBITS);
+  // int32 kinds whose packets are rng.half() words leave raw words in the
+  // engine's half cache; DiscreteGen caches its own computed results
+  constexpr bool kHalfKind = KIND == GR_RANDBITS || KIND == GR_BERNOULLI || KIND == GR_GEOMETRIC;
+  constexpr bool kUsesHalf = (MODE == M_W64) || (MODE == M_W32 && kHalfKind);
   constexpr bool kUsesGen = (MODE == M_N32) || (MODE == M_N64) || (MODE == M_W32 && KIND == GR_DISCRETE);
   int cvalid = 0;
   const uint32_t* cwords = nullptr;
@@ -293,10 +309,8 @@ __global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const Call
   if (s == 0 && tid < Q0) {
     const int i = tid;
     if (MODE == M_W64) reinterpret_cast<double*>(p.out)[off + i] = tw64<KIND>(cwords[i], d);
-    if (MODE == M_W32) {
-      if (KIND == GR_RANDBITS) reinterpret_cast<int32_t*>(p.out)[off + i] = (int32_t)cwords[i];
-      else reinterpret_cast<int32_t*>(p.out)[off + i] = (int32_t)cwords[i];
-    }
+    if (MODE == M_W32)
+      reinterpret_cast<int32_t*>(p.out)[off + i] = kHalfKind ? tw32<KIND>(cwords[i], d) : (int32_t)cwords[i];
     if (MODE == M_N32) reinterpret_cast<float*>(p.out)[off + i] = nscale32<KIND>(u2f(cwords[i]), d);
     if (MODE == M_N64) {
       uint64_t b = (uint64_t)cwords[2 * i] | ((uint64_t)cwords[2 * i + 1] << 32);
@@ -387,12 +401,12 @@ __global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const Call
             int32_t* o = reinterpret_cast<int32_t*>(p.out) + ob;
             st16(o, v[0], v[1], v[2], v[3]);
             if (full) st16(o + 4, v[4], v[5], v[6], v[7]);
-            else if (gs || KIND == GR_RANDBITS) {
-              // leftover half: RandbitsGen leaves raw words in the engine's
+            else if (gs || kHalfKind) {
+              // leftover half: rng.half() kinds leave raw words in the engine's
               // half() cache; DiscreteGen caches its computed upper 4 results
-              uint32_t* cdst = (KIND == GR_RANDBITS) ? st->half_cache : gs->s[0].cache;
+              uint32_t* cdst = kHalfKind ? st->half_cache : gs->s[0].cache;
 #pragma unroll
-              for (int q = 0; q < 4; ++q) cdst[q] = (KIND == GR_RANDBITS) ? wd[4 + q] : (uint32_t)v[4 + q];
+              for (int q = 0; q < 4; ++q) cdst[q] = kHalfKind ? wd[4 + q] : (uint32_t)v[4 + q];
             }
           } else {
             double v[8];
@@ -579,8 +593,11 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
       return true;
     case GR_GAMMA:
       return d.ia == 1;  // alpha == 1: beta * exponential
+    case GR_BERNOULLI:
+      return true;
     case GR_RANDBITS:
     case GR_DISCRETE:
+    case GR_GEOMETRIC:
       return dtype == GR_I32;
     default:
       return false;
@@ -607,6 +624,7 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F32_CASE(GR_WEIBULL)
       GR_F32_CASE(GR_EXTREME_VALUE)
       GR_F32_CASE(GR_GAMMA)
+      GR_F32_CASE(GR_BERNOULLI)
       case GR_NORMAL_STD:
         return run_direct<M_N32, GR_NORMAL_STD>(p, d, snap, s);
       case GR_NORMAL:
@@ -626,6 +644,7 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F64_CASE(GR_WEIBULL)
       GR_F64_CASE(GR_EXTREME_VALUE)
       GR_F64_CASE(GR_GAMMA)
+      GR_F64_CASE(GR_BERNOULLI)
       case GR_BALANCED:
         return run_direct<M_W64, GR_BALANCED>(p, d, snap, s);
       case GR_BALANCED2:
@@ -643,6 +662,8 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
   if (d.dtype == GR_I32) {
     if (d.kind == GR_RANDBITS) return run_direct<M_W32, GR_RANDBITS>(p, d, snap, s);
     if (d.kind == GR_DISCRETE) return run_direct<M_W32, GR_DISCRETE>(p, d, snap, s);
+    if (d.kind == GR_BERNOULLI) return run_direct<M_W32, GR_BERNOULLI>(p, d, snap, s);
+    if (d.kind == GR_GEOMETRIC) return run_direct<M_W32, GR_GEOMETRIC>(p, d, snap, s);
   }
   return cudaErrorNotSupported;
 }

@@ -21,9 +21,24 @@ struct DistParams {
   int32_t ia, ib, ic;                      // integer constants (trials, counts, flags)
   uint32_t bitmask;                        // alias table mask
   int32_t ncdf;                            // CDF entries (discrete < 16 weights)
+  int32_t post;                            // output transform of a beta draw: 1 = FisherFGen (fh / dh = b/a)
   const int32_t* prob;                     // alias table / cdf (device)
   const int32_t* alias;
 };
+
+// Output transform of generators built on a BetaGen draw x (bits v):
+// FisherFGen writes (b/a) x / (1 - x), b/a in the scalar type
+// (NormalExp.h:1016-1021).
+template <bool WIDE>
+__device__ __forceinline__ uint64_t beta_post(uint64_t v, const DistParams& d) {
+  if (d.post != 1) return v;
+  if (WIDE) {
+    const double x = __longlong_as_double((long long)v);
+    return (uint64_t)__double_as_longlong((d.dh * x) / (1.0 - x));
+  }
+  const float x = __uint_as_float((uint32_t)v);
+  return (uint64_t)__float_as_uint((d.fh * x) / (1.0f - x));
+}
 
 // How one call is split over sub-engines and segments.
 struct Plan {

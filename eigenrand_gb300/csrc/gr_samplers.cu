@@ -561,6 +561,7 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
       const int64_t nf = tscan[tl] >> 16;
       const int64_t at = (int64_t)rcnt + (tscan[tl] & 0xffffu);
       uint64_t v = cand[tl * P + j];
+      if (RK == RK_BETA_SMALL) v = beta_post<kWide>(v, d);
       if (c == P) {
         const int64_t eidx = E + nf + at / P;
         if (eidx < Npk) {
@@ -579,7 +580,7 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
             else reinterpret_cast<uint32_t*>(p.out)[off + eidx * P + f % P] = (uint32_t)v;
           }
         } else {
-          fifo[fsl ^ 1][f - qe * P] = v;
+          fifo[fsl ^ 1][f - qe * P] = cand[tl * P + j];  // the FIFO keeps beta draws
         }
       }
     }
@@ -588,7 +589,7 @@ __global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, in
       const int64_t f = tid;
       if (f / P < qe) {
         const int64_t eidx = emit_of_q[f / P];
-        const uint64_t v = fifo[fsl][tid];
+        const uint64_t v = RK == RK_BETA_SMALL ? beta_post<kWide>(fifo[fsl][tid], d) : fifo[fsl][tid];
         if (eidx < Npk) {
           if (kWide) reinterpret_cast<uint64_t*>(p.out)[off + eidx * P + f % P] = v;
           else if (DT == SD_I32H) reinterpret_cast<int32_t*>(p.out)[off + eidx * P + f % P] = iout((uint32_t)v);
@@ -879,6 +880,7 @@ __global__ void __launch_bounds__(kRejThreads) k_rs_write(Plan p, DistParams d, 
     return (RK == RK_BINOMIAL && d.ib) ? (int32_t)d.fh - r : r;
   };
   auto put = [&](int64_t idx, uint64_t v) {
+    if (RK == RK_BETA_SMALL) v = beta_post<kWide>(v, d);
     if (kWide) reinterpret_cast<uint64_t*>(p.out)[g.off + idx] = v;
     else if (DT == SD_I32H) reinterpret_cast<int32_t*>(p.out)[g.off + idx] = iout((uint32_t)v);
     else reinterpret_cast<uint32_t*>(p.out)[g.off + idx] = (uint32_t)v;
@@ -1049,7 +1051,8 @@ __global__ void k_rs_gather(Plan p, DistParams d, RsArgs a) {
     const int64_t q = i / P, f = i;
     const int64_t eidx = a.pos[(size_t)k * a.pos_cap + q];
     if (eidx < 0 || eidx >= Npk) continue;
-    const uint64_t v = f < rc0 ? rs_rest<DT>(gs, f) : rs_lane<DT>(a, k, f);
+    uint64_t v = f < rc0 ? rs_rest<DT>(gs, f) : rs_lane<DT>(a, k, f);
+    if (RK == RK_BETA_SMALL) v = beta_post<DT == SD_F64>(v, d);
     const int64_t o = off + eidx * P + (f - q * P);
     if (DT == SD_F64) {
       reinterpret_cast<uint64_t*>(p.out)[o] = v;
@@ -1380,6 +1383,9 @@ struct BetaComp {
 };
 struct BetaConsts {
   BetaComp c[2];
+  int post;              // FisherFGen: write (b/a) x / (1 - x)
+  float fpost;           // b/a in the scalar type
+  double dpost;
 };
 
 BetaComp beta_component(int branch, float af, double ad) {
@@ -1507,6 +1513,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
   const int64_t Npk = n / P;
 
   const int type0 = bk.c[0].type, U0 = bk.c[0].U, type1 = bk.c[1].type, U1 = bk.c[1].U;
+  const bool post = bk.post == 1;
   const int umax = max(max(U0, U1), 3);
   // the component whose full-trial values are computed ahead of the outputs
   // (a rejection one); the other is computed where its output is written
@@ -1738,10 +1745,12 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
         }
         if (DT == SD_F32) {
           const float p1 = u2f((uint32_t)v[0]), p2 = u2f((uint32_t)v[1]);
-          reinterpret_cast<float*>(p.out)[off + (e_first + i) * P + j] = p1 / (p1 + p2);
+          const float x = p1 / (p1 + p2);
+          reinterpret_cast<float*>(p.out)[off + (e_first + i) * P + j] = post ? (bk.fpost * x) / (1.0f - x) : x;
         } else {
           const double p1 = u2d(v[0]), p2 = u2d(v[1]);
-          reinterpret_cast<double*>(p.out)[off + (e_first + i) * P + j] = p1 / (p1 + p2);
+          const double x = p1 / (p1 + p2);
+          reinterpret_cast<double*>(p.out)[off + (e_first + i) * P + j] = post ? (bk.dpost * x) / (1.0 - x) : x;
         }
       }
       __syncthreads();
@@ -1798,6 +1807,9 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
   BetaConsts bk;
   bk.c[0] = beta_component(d.ia, d.fa, d.da);
   bk.c[1] = beta_component(d.ib, d.fb, d.db);
+  bk.post = d.post;
+  bk.fpost = d.fh;
+  bk.dpost = d.dh;
   constexpr size_t smem = beta_smem_bytes<DT>();
   static bool attr[64] = {};
   int dev = 0;

@@ -70,7 +70,10 @@ typedef enum {
   GR_BINOMIAL = 17,     /* BinomialGen(trials, p=a); Discrete.h:911-1053          */
   GR_DISCRETE = 18,     /* DiscreteGen<int32_t,int32_t>(weights); Discrete.h:352-486 */
   GR_RANDBITS = 19,     /* RandbitsGen<int32_t>; Basic.h:378-400                  */
-  GR_BINOMIAL_V = 20    /* BinomialVGen<int32_t>, per-element (trials, p); Discrete.h:1061-1192 */
+  GR_BINOMIAL_V = 20,   /* BinomialVGen<int32_t>, per-element (trials, p); Discrete.h:1061-1192 */
+  GR_BERNOULLI = 21,    /* BernoulliGen(p=a), f32 / f64 / int32; Basic.h:669-708    */
+  GR_GEOMETRIC = 22,    /* GeometricGen<int32_t>(p=a); Discrete.h:1338-1376         */
+  GR_FISHER_F = 23      /* FisherFGen(m=a, n=b); NormalExp.h:984-1023             */
 } gr_dist_kind;
 
 typedef struct {

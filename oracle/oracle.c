@@ -456,6 +456,55 @@ static void gamma_pk(or_vmt* e, or_gen* g, int dbl, double alpha_in, double beta
   }
 }
 
+/* BetaGen::packetOp, NormalExp.h:949-976 (g: its own cache for the a, b < 1
+ * branch; g2, g3: the two GammaGens) */
+static void beta_pk(or_vmt* e, or_gen* g, or_gen* g2, or_gen* g3, int dbl, double a, double b, upk* pp) {
+  upk p;
+  int both_small = dbl ? (a < 1 && b < 1) : ((float)a < 1 && (float)b < 1);
+  if (both_small) {
+    for (;;) {
+      upk u1, u2;
+      ur_pk(e, dbl, &u1);
+      ur_pk(e, dbl, &u2);
+      int mask[8];
+      if (dbl) {
+        double cands[4];
+        for (int j = 0; j < 4; ++j) {
+          double p1 = or_exp(or_log(u1.d[j]) * (1 / a));
+          double p2 = or_exp(or_log(u2.d[j]) * (1 / b));
+          double x = p1 + p2;
+          cands[j] = p1 / x;
+          mask[j] = x <= 1;
+        }
+        int full = 0;
+        g->rest_cnt = compress_append(4, 1, cands, mask, g->rest, g->rest_cnt, &full);
+        if (full) { memcpy(p.d, cands, sizeof cands); break; }
+      } else {
+        float cands[8];
+        float fa = (float)a, fb = (float)b;
+        for (int j = 0; j < 8; ++j) {
+          float p1 = or_expf(or_logf(u1.f[j]) * (1 / fa));
+          float p2 = or_expf(or_logf(u2.f[j]) * (1 / fb));
+          float x = p1 + p2;
+          cands[j] = p1 / x;
+          mask[j] = x <= 1;
+        }
+        int full = 0;
+        g->rest_cnt = compress_append(8, 0, cands, mask, g->rest, g->rest_cnt, &full);
+        if (full) { memcpy(p.f, cands, sizeof cands); break; }
+      }
+    }
+  } else {
+    upk p1, p2;
+    gamma_pk(e, g2, dbl, a, 1, &p1);
+    gamma_pk(e, g3, dbl, b, 1, &p2);
+    p.dbl = dbl;
+    if (dbl) for (int j = 0; j < 4; ++j) p.d[j] = p1.d[j] / (p1.d[j] + p2.d[j]);
+    else for (int j = 0; j < 8; ++j) p.f[j] = p1.f[j] / (p1.f[j] + p2.f[j]);
+  }
+  *pp = p;
+}
+
 int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n) {
   int dbl = dtype == 1;
   int P = P_of(dbl);
@@ -551,51 +600,35 @@ int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, v
       case OR_GAMMA:
         gamma_pk(e, g, dbl, a, b, &p);
         break;
+      case OR_BERNOULLI: { /* BernoulliGen::packetOp, Basic.h:695-707: Packet8i rawbits
+                            * = rng() (arch/AVX/RandUtils.h:147-152), masked, compared
+                            * signed with (int32)(uint32)(p * 2^31); for double the
+                            * blend reads the sign of each 64-bit element, i.e. the
+                            * compare of its high word (arch/AVX/MorePacketMath.h:583-586) */
+        uint32_t w[8];
+        draw_full(e, w);
+        const int32_t pt = (int32_t)(uint32_t)(a * 2147483648.0);
+        p.dbl = dbl;
+        if (dbl) for (int j = 0; j < 4; ++j) p.d[j] = ((int32_t)(w[2 * j + 1] & 0x7fffffffu) < pt) ? 1.0 : 0.0;
+        else for (int j = 0; j < 8; ++j) p.f[j] = ((int32_t)(w[j] & 0x7fffffffu) < pt) ? 1.0f : 0.0f;
+        break;
+      }
       case OR_CHI_SQUARED: /* ChiSquaredGen = GammaGen(n/2, 2), NormalExp.h:767-802 */
         gamma_pk(e, g, dbl, dbl ? a * 0.5 : (double)((float)a * 0.5f), 2, &p);
         break;
-      case OR_BETA: { /* BetaGen::packetOp, NormalExp.h:949-976 */
-        int both_small = dbl ? (a < 1 && b < 1) : ((float)a < 1 && (float)b < 1);
-        if (both_small) {
-          for (;;) {
-            upk u1, u2;
-            ur_pk(e, dbl, &u1);
-            ur_pk(e, dbl, &u2);
-            int mask[8];
-            if (dbl) {
-              double cands[4];
-              for (int j = 0; j < 4; ++j) {
-                double p1 = or_exp(or_log(u1.d[j]) * (1 / a));
-                double p2 = or_exp(or_log(u2.d[j]) * (1 / b));
-                double x = p1 + p2;
-                cands[j] = p1 / x;
-                mask[j] = x <= 1;
-              }
-              int full = 0;
-              g->rest_cnt = compress_append(4, 1, cands, mask, g->rest, g->rest_cnt, &full);
-              if (full) { memcpy(p.d, cands, sizeof cands); break; }
-            } else {
-              float cands[8];
-              float fa = (float)a, fb = (float)b;
-              for (int j = 0; j < 8; ++j) {
-                float p1 = or_expf(or_logf(u1.f[j]) * (1 / fa));
-                float p2 = or_expf(or_logf(u2.f[j]) * (1 / fb));
-                float x = p1 + p2;
-                cands[j] = p1 / x;
-                mask[j] = x <= 1;
-              }
-              int full = 0;
-              g->rest_cnt = compress_append(8, 0, cands, mask, g->rest, g->rest_cnt, &full);
-              if (full) { memcpy(p.f, cands, sizeof cands); break; }
-            }
-          }
+      case OR_BETA:
+        beta_pk(e, g, g2, g3, dbl, a, b, &p);
+        break;
+      case OR_FISHER_F: { /* FisherFGen: BetaGen(m/2, n/2) in the scalar type, then
+                           * (b/a) x / (1 - x), NormalExp.h:997-1021 */
+        if (dbl) {
+          const double ba = a * 0.5, bb = b * 0.5, c = bb / ba;
+          beta_pk(e, g, g2, g3, dbl, ba, bb, &p);
+          for (int j = 0; j < 4; ++j) p.d[j] = (c * p.d[j]) / (1.0 - p.d[j]);
         } else {
-          upk p1, p2;
-          gamma_pk(e, g2, dbl, a, 1, &p1);
-          gamma_pk(e, g3, dbl, b, 1, &p2);
-          p.dbl = dbl;
-          if (dbl) for (int j = 0; j < 4; ++j) p.d[j] = p1.d[j] / (p1.d[j] + p2.d[j]);
-          else for (int j = 0; j < 8; ++j) p.f[j] = p1.f[j] / (p1.f[j] + p2.f[j]);
+          const float ba = (float)a * 0.5f, bb = (float)b * 0.5f, c = bb / ba;
+          beta_pk(e, g, g2, g3, dbl, ba, bb, &p);
+          for (int j = 0; j < 8; ++j) p.f[j] = (c * p.f[j]) / (1.0f - p.f[j]);
         }
         break;
       }
@@ -765,6 +798,41 @@ int or_gen_randbits(or_vmt* e, int32_t* out, size_t n) {
     uint32_t w[4];
     draw_half(e, w);
     memcpy(out + 4 * k, w, 16);
+  }
+  return 0;
+}
+
+/* BernoulliGen<int32_t>::packetOp<Packet4i>, Basic.h:695-707: rawbits of a
+ * Packet4i = rng.half() (arch/AVX/RandUtils.h:23-26), (w & 0x7FFFFFFF)
+ * compared signed with (int32)(uint32)(p * 2^31) (so p = 1 gives 0) */
+int or_gen_bernoulli_i32(or_vmt* e, double p, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  const int32_t pt = (int32_t)(uint32_t)(p * 2147483648.0);
+  for (size_t k = 0; k < n / 4; ++k) {
+    uint32_t w[4];
+    draw_half(e, w);
+    for (int j = 0; j < 4; ++j) out[4 * k + j] = ((int32_t)(w[j] & 0x7fffffffu) < pt) ? 1 : 0;
+  }
+  return 0;
+}
+
+/* _mm_cvttps_epi32 of one lane: truncation; NaN and out-of-range give
+ * 0x80000000 */
+static int32_t cvtt_f32(float x) {
+  return (x >= -2147483648.0f && x < 2147483648.0f) ? (int32_t)x : INT32_MIN;
+}
+
+/* GeometricGen<int32_t>::packetOp<Packet4i>, Discrete.h:1355-1375:
+ * rlog_q = 1 / log(1 - p) in double, set as a float packet; u from
+ * StdUniformRealGen<float> over Packet4f (rng.half() words);
+ * pcast(ptruncate(plog(1 - u) * rlog_q)) */
+int or_gen_geometric(or_vmt* e, double p, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  const float rlq = (float)(1 / log(1 - p));
+  for (size_t k = 0; k < n / 4; ++k) {
+    float u[4];
+    ur_f4(e, u);
+    for (int j = 0; j < 4; ++j) out[4 * k + j] = cvtt_f32(truncf(or_logf(1.0f - u[j]) * rlq));
   }
   return 0;
 }

@@ -85,7 +85,9 @@ enum {
   OR_BETA = 10,     /* a, b                                                   */
   OR_STUDENT_T = 11,  /* a = n                                                */
   OR_CHI_SQUARED = 12, /* a = n                                              */
-  OR_STDNORMAL = 13   /* StdNormalGen: no mean/stdev scaling                  */
+  OR_STDNORMAL = 13,  /* StdNormalGen: no mean/stdev scaling                  */
+  OR_BERNOULLI = 14,  /* a = p; BernoulliGen<float/double>                    */
+  OR_FISHER_F = 15    /* a = m, b = n; FisherFGen                             */
 };
 int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b,
                 void* out, size_t n);
@@ -94,6 +96,8 @@ int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b,
 int or_gen_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out, size_t n);
 int or_gen_poisson(or_vmt* e, or_gen* g, double mean, int32_t* out, size_t n);
 int or_gen_randbits(or_vmt* e, int32_t* out, size_t n);
+int or_gen_bernoulli_i32(or_vmt* e, double p, int32_t* out, size_t n);
+int or_gen_geometric(or_vmt* e, double p, int32_t* out, size_t n);
 
 /* discrete with int32 precision (DiscreteGen<int32_t, int32_t>) */
 typedef struct {

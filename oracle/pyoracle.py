@@ -15,6 +15,7 @@ PIN = os.path.join(HERE, "_build", "pin_mt")
 
 OR_UNIFORM, OR_BALANCED, OR_NORMAL, OR_LOGNORMAL, OR_EXPONENTIAL, OR_CAUCHY = 1, 2, 3, 4, 5, 6
 OR_WEIBULL, OR_EXTREME, OR_GAMMA, OR_BETA, OR_STUDENT_T, OR_CHI_SQUARED, OR_STDNORMAL = 7, 8, 9, 10, 11, 12, 13
+OR_BERNOULLI, OR_FISHER_F = 14, 15
 
 
 def build():
@@ -49,6 +50,9 @@ def lib():
         L.or_gen_poisson.restype = ctypes.c_int
         L.or_gen_randbits.argtypes = [vp, vp, sz]
         L.or_gen_randbits.restype = ctypes.c_int
+        for fn in ("or_gen_bernoulli_i32", "or_gen_geometric"):
+            getattr(L, fn).argtypes = [vp, ctypes.c_double, vp, sz]
+            getattr(L, fn).restype = ctypes.c_int
         L.or_discrete_new.restype = vp
         L.or_discrete_new.argtypes = [vp, ctypes.c_int]
         L.or_discrete_free.argtypes = [vp]
@@ -115,15 +119,22 @@ REAL = {
     "UNIFORM_REAL": OR_UNIFORM, "UNIFORM_REAL2": OR_UNIFORM, "BALANCED": OR_BALANCED, "BALANCED2": OR_BALANCED,
     "NORMAL_STD": OR_STDNORMAL, "NORMAL": OR_NORMAL, "LOGNORMAL": OR_LOGNORMAL, "EXPONENTIAL": OR_EXPONENTIAL,
     "CAUCHY": OR_CAUCHY, "WEIBULL": OR_WEIBULL, "EXTREME_VALUE": OR_EXTREME, "GAMMA": OR_GAMMA, "BETA": OR_BETA,
-    "STUDENT_T": OR_STUDENT_T, "CHI_SQUARED": OR_CHI_SQUARED,
+    "STUDENT_T": OR_STUDENT_T, "CHI_SQUARED": OR_CHI_SQUARED, "FISHER_F": OR_FISHER_F,
 }
+INT_ONE_PARAM = {"BERNOULLI": "or_gen_bernoulli_i32", "GEOMETRIC": "or_gen_geometric"}
 DEFAULT_AB = {"UNIFORM_REAL": (0.0, 1.0), "BALANCED": (-1.0, 1.0)}
 
 
 def generate(eng, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0, weights=None):
     """Draw n samples of a distribution kind (names as in eigenrand_gb300._lib.KINDS)."""
     L = lib()
-    if kind in REAL:
+    if kind == "BERNOULLI" and dtype != np.int32:
+        out = np.empty(n, dtype=dtype)
+        rc = L.or_gen_real(eng.h, gen.ptr, OR_BERNOULLI, 1 if dtype == np.float64 else 0, a, 0.0, _p(out), n)
+    elif kind in INT_ONE_PARAM:
+        out = np.empty(n, dtype=np.int32)
+        rc = getattr(L, INT_ONE_PARAM[kind])(eng.h, a, _p(out), n)
+    elif kind in REAL:
         a, b = DEFAULT_AB.get(kind, (a, b))
         out = np.empty(n, dtype=dtype)
         rc = L.or_gen_real(eng.h, gen.ptr, REAL[kind], 1 if dtype == np.float64 else 0, a, b, _p(out), n)

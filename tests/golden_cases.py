@@ -31,12 +31,18 @@ for dt, tag, n in ((np.float32, "f32", 256), (np.float64, "f64", 128)):
     _add(f"gamma5_{tag}", "GAMMA", dt, n, 5.0, 1.0)
     _add(f"gamma05_{tag}", "GAMMA", dt, n, 0.5, 1.0)
     _add(f"beta_{tag}", "BETA", dt, n, 0.5, 2.0)
+    _add(f"fisherF11_{tag}", "FISHER_F", dt, n, 1.0, 1.0)
+    _add(f"fisherF55_{tag}", "FISHER_F", dt, n, 5.0, 5.0)
 _add("raw_42", "RAW", np.uint64, 256, seed=42)
 _add("binomial20", "BINOMIAL", np.int32, 256, 0.3, trials=20)
 _add("poisson4", "POISSON", np.int32, 256, 4.0)
 _add("discrete16", "DISCRETE", np.int32, 256, weights=W16)
 _add("discrete5", "DISCRETE", np.int32, 256, weights=W5)
 _add("randbits", "RANDBITS", np.int32, 256)
+_add("bernoulli_f32", "BERNOULLI", np.float32, 256, 0.3)
+_add("bernoulli_f64", "BERNOULLI", np.float64, 128, 0.3)
+_add("bernoulli_i32", "BERNOULLI", np.int32, 256, 0.7)
+_add("geometric", "GEOMETRIC", np.int32, 256, 0.25)
 
 
 def run_oracle(oracle, c):

@@ -134,6 +134,7 @@ KINDS = [
     ("UNIFORM_REAL", 0, 0), ("UNIFORM_REAL2", -2.0, 3.0), ("BALANCED", 0, 0), ("BALANCED2", -3.0, 5.0),
     ("NORMAL_STD", 0, 0), ("NORMAL", 2.0, 3.0), ("LOGNORMAL", 0.0, 1.0), ("EXPONENTIAL", 1.5, 0),
     ("CAUCHY", 0.0, 1.0), ("WEIBULL", 1.5, 1.0), ("EXTREME_VALUE", 0.0, 1.0), ("GAMMA", 1.0, 2.0),
+    ("BERNOULLI", 0.3, 0),
 ]
 
 
@@ -341,6 +342,68 @@ def test_half_packet_cache_between_kinds(er, oracle):
         er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), n, er._stream_ptr()))
         ref = oracle.generate(e, oracle.Gen(), kind, n, npdt(tdt), *((-1.0, 1.0) if kind == "BALANCED" else (0.0, 0.0)))
         assert_bits_equal(mem(o), ref, f"{kind} n={n}")
+
+
+@pytest.mark.parametrize("m,n", [(1.0, 1.0), (1.0, 1.6), (5.0, 5.0), (1.0, 5.0), (4.0, 2.0), (10.0, 3.0)])
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+def test_fisher_f_bit_exact(er, oracle, m, n, tdt):
+    """FisherFGen = BetaGen(m/2, n/2) (both branches: a, b < 1 rejection with
+    its segmented form on one engine, and the two-gamma walk) followed by
+    (b/a) x / (1 - x) on every output, including lanes carried between calls."""
+    P = 8 if tdt == torch.float32 else 4
+    u = er.Vmt19937_64(44)
+    e = oracle.Engine(44)
+    g = er.FisherFGen(m, n, dtype=tdt)
+    og = oracle.Gen()
+    for cnt in (P, 3 * P, 1 << 20, 5 * P, 1 << 14):
+        ref = oracle.generate(e, og, "FISHER_F", cnt, npdt(tdt), m, n)
+        assert_bits_equal(mem(g.generate(cnt, 1, u)), ref, f"fisherF({m},{n}) {tdt} n={cnt}")
+
+
+@pytest.mark.parametrize("kind,a", [("BERNOULLI", 0.7), ("BERNOULLI", 1.0), ("BERNOULLI", 0.0),
+                                    ("GEOMETRIC", 0.25), ("GEOMETRIC", 0.9), ("GEOMETRIC", 0.0),
+                                    ("GEOMETRIC", 1.0)])
+def test_half_word_int_kinds_bit_exact(er, oracle, kind, a):
+    """int32 BernoulliGen / GeometricGen over rng.half() words, large calls
+    (jump segments) and odd half-packet counts that leave the half() cache
+    full; p = 1 gives 0 on the packet path (signed compare with 2^31), and
+    GeometricGen(0) converts NaN / inf lanes to INT_MIN like cvttps2dq."""
+    u = er.Vmt19937_64(31)
+    e = oracle.Engine(31)
+    for n in (4, 12, 1 << 21, 8, 4 + (1 << 20)):
+        d, keep = er._desc(kind, torch.int32, a)
+        o = torch.empty(n, dtype=torch.int32, device="cuda")
+        er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), n, er._stream_ptr()))
+        ref = oracle.generate(e, oracle.Gen(), kind, n, np.int32, a)
+        assert_bits_equal(mem(o), ref, f"{kind}({a}) n={n}")
+
+
+def test_half_cache_shared_by_int_kinds(er, oracle):
+    """RandbitsGen, BernoulliGen<int32_t> and GeometricGen all draw through
+    rng.half(): a cached half left by one is used by the next."""
+    u = er.Vmt19937_64(12)
+    e = oracle.Engine(12)
+    seq = [("BERNOULLI", 0.4, 4), ("GEOMETRIC", 0.3, 12), ("RANDBITS", 0.0, 4), ("BERNOULLI", 0.4, 1 << 16 | 4),
+           ("GEOMETRIC", 0.3, 4), ("UNIFORM_REAL", 0.0, 8), ("GEOMETRIC", 0.3, 4), ("BERNOULLI", 0.9, 8)]
+    for kind, a, n in seq:
+        tdt = torch.float32 if kind == "UNIFORM_REAL" else torch.int32
+        d, keep = er._desc(kind, tdt, a)
+        o = torch.empty(n, dtype=tdt, device="cuda")
+        er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), n, er._stream_ptr()))
+        ref = oracle.generate(e, oracle.Gen(), kind, n, npdt(tdt), a)
+        assert_bits_equal(mem(o), ref, f"{kind} n={n}")
+
+
+def test_bernoulli_real_generator_and_invalid_p(er, oracle):
+    for tdt in (torch.float32, torch.float64):
+        u = er.Vmt19937_64(3)
+        e = oracle.Engine(3)
+        g = er.BernoulliGen(0.25, dtype=tdt)
+        for n in (8, 1 << 20, 16):
+            ref = oracle.generate(e, oracle.Gen(), "BERNOULLI", n, npdt(tdt), 0.25)
+            assert_bits_equal(mem(g.generate(n, 1, u)), ref, f"bernoulli {tdt} n={n}")
+    with pytest.raises(er.GrError):
+        er.bernoulli(8, 1, er.Vmt19937_64(1), p=1.5)
 
 
 @pytest.mark.parametrize("weights", [golden_cases.W16, golden_cases.W5, list(range(1, 41))])

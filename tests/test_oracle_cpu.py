@@ -139,3 +139,48 @@ def test_oracle_golden_fixtures(oracle):
     for name, case in golden_cases.CASES.items():
         got = golden_cases.run_oracle(oracle, case)
         np.testing.assert_array_equal(got, fx[name], err_msg=name)
+
+
+@pytest.mark.parametrize("p", [0.05, 0.3, 0.7])
+def test_oracle_bernoulli_and_geometric_moments(oracle, p):
+    """The reference's own tests only run these generators (test/test.cpp:189-209):
+    the oracle is checked against the distributions' moments.  Bernoulli:
+    P(1) = p (to 2^-31).  Geometric (failures before the first success):
+    mean (1 - p) / p, P(0) = p."""
+    n = 1 << 16
+    for dt in (np.float32, np.float64, np.int32):
+        x = oracle.generate(oracle.Engine(11), oracle.Gen(), "BERNOULLI", n, dt, p)
+        assert set(np.unique(x)) <= {0, 1}
+        assert abs(x.mean() - p) < 5 * np.sqrt(p * (1 - p) / n)
+    g = oracle.generate(oracle.Engine(12), oracle.Gen(), "GEOMETRIC", n, np.int32, p)
+    assert g.min() >= 0
+    sd = np.sqrt(1 - p) / p
+    assert abs(g.mean() - (1 - p) / p) < 5 * sd / np.sqrt(n)
+    assert abs((g == 0).mean() - p) < 5 * np.sqrt(p * (1 - p) / n)
+
+
+def test_oracle_bernoulli_packet_quirks(oracle):
+    """p = 1 sets the threshold 2^31, which the packet path compares as the
+    signed int32 -2^31: every lane gives 0 (Basic.h:680-684, 702-706)."""
+    for dt in (np.float32, np.float64, np.int32):
+        x = oracle.generate(oracle.Engine(1), oracle.Gen(), "BERNOULLI", 64, dt, 1.0)
+        assert not x.any()
+
+
+@pytest.mark.parametrize("m,n", [(1.0, 1.0), (5.0, 5.0), (4.0, 9.0)])
+def test_oracle_fisher_f_is_mapped_beta(oracle, m, n):
+    """FisherFGen(m, n) draws BetaGen(m/2, n/2) from the same stream and maps
+    x to (b/a) x / (1 - x) in the scalar type (NormalExp.h:997-1021); its mean
+    is n / (n - 2) for n > 2."""
+    for dt in (np.float32, np.float64):
+        f = oracle.generate(oracle.Engine(5), oracle.Gen(), "FISHER_F", 4096, dt, m, n)
+        half = dt(0.5)
+        a, b = dt(m) * half, dt(n) * half
+        x = oracle.generate(oracle.Engine(5), oracle.Gen(), "BETA", 4096, dt, float(a), float(b))
+        c = dt(b / a)
+        np.testing.assert_array_equal(f, (c * x) / (dt(1) - x))
+    if n > 2:
+        big = oracle.generate(oracle.Engine(6), oracle.Gen(), "FISHER_F", 1 << 18, np.float64, m, n)
+        var = 2 * n * n * (m + n - 2) / (m * (n - 2) ** 2 * (n - 4)) if n > 4 else None
+        tol = 5 * np.sqrt(var / big.size) if var else 0.05
+        assert abs(big.mean() - n / (n - 2)) < tol
