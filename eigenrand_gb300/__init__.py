@@ -28,11 +28,11 @@ __all__ = [
     "GrError", "Vmt19937_64", "raw_u64", "version",
     "uniformReal", "balanced", "normal", "lognormal", "exponential", "cauchy", "weibull", "extremeValue",
     "gamma", "beta", "studentT", "chiSquared", "poisson", "binomial", "discrete", "randBits", "bernoulli",
-    "geometric", "fisherF",
+    "geometric", "fisherF", "uniformInt",
     "StdUniformRealGen", "UniformRealGen", "BalancedGen", "Balanced2Gen", "StdNormalGen", "NormalGen",
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
     "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen", "BernoulliGen",
-    "GeometricGen", "FisherFGen",
+    "GeometricGen", "FisherFGen", "UniformIntGen",
     "sample_batched",
     "MvNormalGen", "WishartGen", "InvWishartGen", "DirichletGen", "MultinomialGen", "makeMvNormalGen",
     "makeMvNormalGenFromLt", "makeWishartGen", "makeWishartGenFromLt", "makeInvWishartGen",
@@ -319,6 +319,14 @@ class FisherFGen(_Gen):
         super().__init__(dtype, m, n)
 
 
+class UniformIntGen(_Gen):
+    """UniformIntGen<int32_t>(min, max), both ends included (Discrete.h:214-336)."""
+    _kind = "UNIFORM_INT"
+
+    def __init__(self, min=0, max=0):
+        super().__init__(torch.int32, float(min), float(max))
+
+
 class GeometricGen(_Gen):
     """GeometricGen<int32_t>(p) (Discrete.h:1338-1376)."""
     _kind = "GEOMETRIC"
@@ -406,6 +414,10 @@ def bernoulli(rows, cols, urng, p=0.5, dtype=torch.float32, out=None, stream=Non
 
 def fisherF(rows, cols, urng, m=1.0, n=1.0, dtype=torch.float32, out=None, stream=None):
     return _sample("FISHER_F", rows, cols, urng, dtype, m, n, out=out, stream=stream)
+
+
+def uniformInt(rows, cols, urng, min, max, out=None, stream=None):
+    return _sample("UNIFORM_INT", rows, cols, urng, torch.int32, float(min), float(max), out=out, stream=stream)
 
 
 def geometric(rows, cols, urng, p=0.5, out=None, stream=None):

@@ -242,6 +242,21 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
     case GR_GEOMETRIC:  // GeometricGen(p): rlog_q = 1 / log(1 - p), set as a float packet (Discrete.h:1353-1374)
       p.fa = (float)(1 / std::log(1 - a));
       break;
+    case GR_UNIFORM_INT: {  // UniformIntGen<int32_t>(min, max), Discrete.h:230-245 (size_t arithmetic)
+      const int32_t mn = (int32_t)a, mx = (int32_t)b;
+      // pdiff = (size_t)(_max - _min): the int32 difference, sign-extended
+      const uint64_t pdiff = (uint64_t)(int64_t)(int32_t)((uint32_t)mx - (uint32_t)mn);
+      uint64_t bits = 0;
+      if (pdiff != 0) bits = (uint64_t)std::ceil(std::log2((double)(pdiff + 1 > pdiff ? pdiff + 1 : pdiff)));
+      // bitmask = (_Scalar)(~0 >> (64 - bitsize)), stored back into a size_t
+      const uint64_t bitmask = bits == 0 ? ~0ull : (uint64_t)(int64_t)(int32_t)(uint32_t)(~0ull >> (64 - bits));
+      p.ia = mn;                                  // pmin
+      p.bitmask = (uint32_t)bitmask;              // pset1<Packet4i>(bitmask)
+      p.ic = (int32_t)(uint32_t)(pdiff + 1);      // plen = pset1<Packet4i>(pdiff + 1)
+      p.ncdf = bits < 32 ? (int32_t)bits : 32;    // slice width (shifts only happen below 16)
+      p.ib = pdiff == 0 ? 0 : (pdiff == bitmask ? 1 : 2);  // constant / masked bits / rejection
+      break;
+    }
     case GR_WEIBULL:  // pset1(1 / a) in the scalar type
       p.fa = 1.0f / (float)a;
       p.fb = (float)b;
@@ -479,6 +494,7 @@ Family family_of(const DistParams& dp) {
   if (dp.dtype == GR_I32 && dp.kind == GR_POISSON && dp.ic) return Family::Walk;
   if (dp.dtype == GR_I32 && dp.kind == GR_BINOMIAL && dp.ia >= 25 && dp.ic) return Family::Walk;
   if (dp.dtype != GR_I32 && dp.kind == GR_BETA && !dp.ic) return Family::Walk;
+  if (dp.dtype == GR_I32 && dp.kind == GR_UNIFORM_INT) return Family::Walk;  // constant or rejection
   return Family::Unsupported;
 }
 
@@ -668,7 +684,10 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
     const int64_t npk = nk_max / P;
     DistParams wd = dp;
     int64_t max_blocks;
-    if (dp.dtype == GR_I32) {
+    if (dp.kind == GR_UNIFORM_INT) {
+      // every draw accepts each lane with probability > 1/2
+      max_blocks = (npk * 16) / (2 * kN) + 64;
+    } else if (dp.dtype == GR_I32) {
       // PoissonGen loop (mean < 12); BinomialGen with mean < 1 runs the same
       // loop on its poisson member and returns trials - res when p > 1/2
       wd.fe = dp.kind == GR_POISSON ? (float)std::exp(-dp.da) : dp.fe;

@@ -227,6 +227,8 @@ template <int KIND>
 __device__ __forceinline__ int32_t tw32(uint32_t w, const DistParams& d) {
   if (KIND == GR_RANDBITS) return (int32_t)w;
   if (KIND == GR_BERNOULLI) return ((int32_t)(w & 0x7fffffffu) < d.ia) ? 1 : 0;
+  // UniformIntGen<int32_t> over a power-of-two range: (rx & bitmask) + pmin (Discrete.h:302-305)
+  if (KIND == GR_UNIFORM_INT) return (int32_t)((w & d.bitmask) + (uint32_t)d.ia);
   // GeometricGen<int32_t>: pcast(ptruncate(plog(1 - u) * rlog_q)), Discrete.h:1368-1374
   if (KIND == GR_GEOMETRIC) return cvtt_f32(truncf(logf_(1.0f - ur_f(w)) * d.fa));
   // DiscreteGen<int32_t,int32_t>, Discrete.h:455-470
@@ -283,7 +285,8 @@ __global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const Call
   // --- caches the call starts from
   // int32 kinds whose packets are rng.half() words leave raw words in the
   // engine's half cache; DiscreteGen caches its own computed results
-  constexpr bool kHalfKind = KIND == GR_RANDBITS || KIND == GR_BERNOULLI || KIND == GR_GEOMETRIC;
+  constexpr bool kHalfKind =
+      KIND == GR_RANDBITS || KIND == GR_BERNOULLI || KIND == GR_GEOMETRIC || KIND == GR_UNIFORM_INT;
   constexpr bool kUsesHalf = (MODE == M_W64) || (MODE == M_W32 && kHalfKind);
   constexpr bool kUsesGen = (MODE == M_N32) || (MODE == M_N64) || (MODE == M_W32 && KIND == GR_DISCRETE);
   int cvalid = 0;
@@ -599,6 +602,8 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
     case GR_DISCRETE:
     case GR_GEOMETRIC:
       return dtype == GR_I32;
+    case GR_UNIFORM_INT:
+      return dtype == GR_I32 && d.ib == 1;
     default:
       return false;
   }
@@ -664,6 +669,7 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
     if (d.kind == GR_DISCRETE) return run_direct<M_W32, GR_DISCRETE>(p, d, snap, s);
     if (d.kind == GR_BERNOULLI) return run_direct<M_W32, GR_BERNOULLI>(p, d, snap, s);
     if (d.kind == GR_GEOMETRIC) return run_direct<M_W32, GR_GEOMETRIC>(p, d, snap, s);
+    if (d.kind == GR_UNIFORM_INT) return run_direct<M_W32, GR_UNIFORM_INT>(p, d, snap, s);
   }
   return cudaErrorNotSupported;
 }

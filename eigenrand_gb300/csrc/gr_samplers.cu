@@ -1825,7 +1825,166 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
 }
 
 
+// ===========================================================================
+// k_uniform_int: UniformIntGen<int32_t>(min, max) whose range is not a power
+// of two (Discrete.h:296-331).  Each output packet starts a fresh
+// rx = rng.half(), tries its bit slices (the low `bits` bits, then rx >> bits
+// while bitcnt + bits < 32) through CompressMask, and draws again until a
+// packet is full; a packet with all four lanes accepted is returned as is and
+// leaves the carried lanes alone.  One CTA per engine: all threads twist and
+// temper a block into its 624 half-packet draws, then thread 0 runs the
+// automaton over them (a few integer operations per slice).  A range of one
+// value draws nothing and writes the constant.
+// ===========================================================================
+namespace {
+constexpr int kUiThreads = 160;
+}
+
+__global__ void __launch_bounds__(kUiThreads) k_uniform_int(Plan p, DistParams d, int64_t max_blocks) {
+  __shared__ uint64_t raw[2][kLanes][kN];
+  __shared__ uint32_t hw[2 * kN][4];  // draw 2i: low half of packet i, 2i + 1: high half
+  __shared__ int s_done;
+  __shared__ int s_last;              // last draw consumed in the newest block, or -1
+  const int k = blockIdx.x;
+  const int tid = threadIdx.x;
+  EngState* st = p.eng + k;
+  GenSlot* gsl = &p.gen[k].s[0];
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  int32_t* out = reinterpret_cast<int32_t*>(p.out) + off;
+  const int32_t pmin = d.ia;
+  if (d.ib == 0) {  // pdiff == 0: pset1(pmin), no draws
+    for (int64_t i = tid; i < n; i += kUiThreads) out[i] = pmin;
+    return;
+  }
+  const uint32_t mask = d.bitmask;
+  const int32_t plen = d.ic;
+  const int bits = d.ncdf;
+  const int64_t Npk = n / 4;
+
+  // thread-0 automaton state: carried lanes and packets written
+  uint32_t cache[8];
+  int fc = 0;
+  int64_t e = 0;
+  auto put = [&](int64_t pk, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3) {
+    int32_t* o = out + pk * 4;
+    o[0] = (int32_t)(a0 + (uint32_t)pmin);
+    o[1] = (int32_t)(a1 + (uint32_t)pmin);
+    o[2] = (int32_t)(a2 + (uint32_t)pmin);
+    o[3] = (int32_t)(a3 + (uint32_t)pmin);
+  };
+  // one rng.half() draw; true when it completed an output packet
+  auto draw = [&](const uint32_t* w) -> bool {
+    uint32_t rx[4] = {w[0], w[1], w[2], w[3]};
+    int bitcnt = bits;
+    for (;;) {
+      uint32_t c[4];
+      unsigned m = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        c[j] = rx[j] & mask;
+        if ((int32_t)c[j] < plen) m |= 1u << j;
+      }
+      if (m == 15u) {
+        put(e++, c[0], c[1], c[2], c[3]);
+        return true;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if ((m >> j) & 1u) cache[fc++] = c[j];
+      if (fc >= 4) {
+        put(e++, cache[0], cache[1], cache[2], cache[3]);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) cache[j] = cache[j + 4];
+        fc -= 4;
+        return true;
+      }
+      if (bitcnt + bits < 32) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) rx[j] >>= bits;
+        bitcnt += bits;
+      } else {
+        return false;
+      }
+    }
+  };
+
+  load_window(raw[0], &st->win[0][0], kN);
+  const int hv = st->half_valid;
+  if (tid == 0) {
+    fc = min(max(gsl->rest_cnt, 0), 3);  // at most P - 1 lanes are ever carried
+    for (int j = 0; j < fc; ++j) cache[j] = gsl->rest[j];
+    s_done = 0;
+    s_last = -1;
+    if (hv) {  // the engine's cached half is the first draw
+      uint32_t w[4];
+      for (int j = 0; j < 4; ++j) w[j] = st->half_cache[j];
+      draw(w);
+      if (e >= Npk) s_done = 1;
+    }
+  }
+  __syncthreads();
+  int cur = 0;
+  int64_t nb = 0;
+  for (; nb < max_blocks && !s_done; ++nb) {
+    mt_block(raw[cur], raw[cur ^ 1], [&](int i, const uint64_t* pk) {
+      hw[2 * i][0] = (uint32_t)pk[0];
+      hw[2 * i][1] = (uint32_t)(pk[0] >> 32);
+      hw[2 * i][2] = (uint32_t)pk[1];
+      hw[2 * i][3] = (uint32_t)(pk[1] >> 32);
+      hw[2 * i + 1][0] = (uint32_t)pk[2];
+      hw[2 * i + 1][1] = (uint32_t)(pk[2] >> 32);
+      hw[2 * i + 1][2] = (uint32_t)pk[3];
+      hw[2 * i + 1][3] = (uint32_t)(pk[3] >> 32);
+    });
+    cur ^= 1;
+    if (tid == 0) {
+      for (int h = 0; h < 2 * kN; ++h) {
+        draw(hw[h]);
+        if (e >= Npk) {
+          s_last = h;
+          s_done = 1;
+          break;
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- state after the call
+  const int last = s_last;
+  if (last >= 0) {  // draws of the newest block were consumed: packets up to last / 2
+    const int rr = last / 2 + 1;
+    store_window(st, raw[cur], raw[cur ^ 1], rr);
+  }
+  if (tid == 0) {
+    if (!s_done) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+    if (last >= 0) {
+      const int64_t np = (nb - 1) * kN + last / 2 + 1;
+      st->consumed += (uint64_t)np;
+      if ((last & 1) == 0) {  // the high half of the last packet stays in the half() cache
+        for (int j = 0; j < 4; ++j) st->half_cache[j] = hw[last + 1][j];
+        st->half_valid = 1;
+      } else {
+        st->half_valid = 0;
+      }
+    } else if (hv) {
+      st->half_valid = 0;  // only the cached half was drawn
+    }
+    gsl->rest_cnt = fc;
+    for (int j = 0; j < fc; ++j) gsl->rest[j] = cache[j];
+  }
+}
+
+static cudaError_t run_uniform_int(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  k_uniform_int<<<p.K, kUiThreads, 0, s>>>(p, d, max_blocks);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  if (d.kind == GR_UNIFORM_INT) return run_uniform_int(p, d, max_blocks, s);
   if (d.dtype == GR_I32) return run_poisson(p, d, max_blocks, s);
   if (d.dtype == GR_F32) return run_beta<SD_F32>(p, d, max_blocks, s);
   if (d.dtype == GR_F64) return run_beta<SD_F64>(p, d, max_blocks, s);

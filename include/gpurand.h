@@ -73,7 +73,8 @@ typedef enum {
   GR_BINOMIAL_V = 20,   /* BinomialVGen<int32_t>, per-element (trials, p); Discrete.h:1061-1192 */
   GR_BERNOULLI = 21,    /* BernoulliGen(p=a), f32 / f64 / int32; Basic.h:669-708    */
   GR_GEOMETRIC = 22,    /* GeometricGen<int32_t>(p=a); Discrete.h:1338-1376         */
-  GR_FISHER_F = 23      /* FisherFGen(m=a, n=b); NormalExp.h:984-1023             */
+  GR_FISHER_F = 23,     /* FisherFGen(m=a, n=b); NormalExp.h:984-1023             */
+  GR_UNIFORM_INT = 24   /* UniformIntGen<int32_t>(min=a, max=b); Discrete.h:214-336 */
 } gr_dist_kind;
 
 typedef struct {

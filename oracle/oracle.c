@@ -837,6 +837,57 @@ int or_gen_geometric(or_vmt* e, double p, int32_t* out, size_t n) {
   return 0;
 }
 
+/* UniformIntGen<int32_t>(min, max), Discrete.h:230-245 (constructor, size_t
+ * arithmetic) and :287-331 (packetOp<Packet4i>): rx = randbits = rng.half();
+ * a power-of-two range masks; otherwise bit slices of rx go through
+ * compress_append until a packet is full, rx shifting by bitsize while
+ * bitcnt + bitsize < 32 and redrawn after that. */
+int or_gen_uniform_int(or_vmt* e, or_gen* g, int32_t mn, int32_t mx, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  const uint64_t pdiff = (uint64_t)(int64_t)(int32_t)((uint32_t)mx - (uint32_t)mn);
+  uint64_t bitsize = 0, bitmask;
+  if (pdiff == 0) bitsize = 0;
+  else if (pdiff + 1 > pdiff) bitsize = (uint64_t)ceil(log2((double)(pdiff + 1)));
+  else bitsize = (uint64_t)ceil(log2((double)pdiff));
+  bitmask = bitsize == 0 ? ~0ull : (uint64_t)(int64_t)(int32_t)(uint32_t)(~0ull >> (64 - bitsize));
+  const uint32_t pmask = (uint32_t)bitmask;
+  const int32_t plen = (int32_t)(uint32_t)(pdiff + 1);
+  for (size_t k = 0; k < n / 4; ++k) {
+    if (pdiff == 0) {
+      for (int j = 0; j < 4; ++j) out[4 * k + j] = mn;
+      continue;
+    }
+    uint32_t rx[4];
+    draw_half(e, rx);
+    if (pdiff == bitmask) {
+      for (int j = 0; j < 4; ++j) out[4 * k + j] = (int32_t)((rx[j] & pmask) + (uint32_t)mn);
+      continue;
+    }
+    uint64_t bitcnt = bitsize;
+    for (;;) {
+      uint32_t cands[4];
+      int mask[4], full = 0;
+      for (int j = 0; j < 4; ++j) {
+        cands[j] = rx[j] & pmask;
+        mask[j] = (int32_t)cands[j] < plen;
+      }
+      g->rest_cnt = compress_append(4, 0, cands, mask, g->rest, g->rest_cnt, &full);
+      if (full) {
+        for (int j = 0; j < 4; ++j) out[4 * k + j] = (int32_t)(cands[j] + (uint32_t)mn);
+        break;
+      }
+      if (bitcnt + bitsize < 32) {
+        for (int j = 0; j < 4; ++j) rx[j] >>= bitsize;
+        bitcnt += bitsize;
+      } else {
+        draw_half(e, rx);
+        bitcnt = bitsize;
+      }
+    }
+  }
+  return 0;
+}
+
 /* ======================================================================
  * DiscreteGen<int32_t, int32_t>: CDF (<16 weights) or AliasMethod (>=16),
  * Discrete.h:23-207 (table build), :385-412 (constructor), :443-485 (AVX2

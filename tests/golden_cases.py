@@ -43,6 +43,10 @@ _add("bernoulli_f32", "BERNOULLI", np.float32, 256, 0.3)
 _add("bernoulli_f64", "BERNOULLI", np.float64, 128, 0.3)
 _add("bernoulli_i32", "BERNOULLI", np.int32, 256, 0.7)
 _add("geometric", "GEOMETRIC", np.int32, 256, 0.25)
+_add("uniformInt_0_9", "UNIFORM_INT", np.int32, 256, 0, 9)
+_add("uniformInt_m5_5", "UNIFORM_INT", np.int32, 256, -5, 5)
+_add("uniformInt_0_7", "UNIFORM_INT", np.int32, 256, 0, 7)
+_add("uniformInt_big", "UNIFORM_INT", np.int32, 256, -1000, 100000)
 
 
 def run_oracle(oracle, c):

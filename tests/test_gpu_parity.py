@@ -378,6 +378,39 @@ def test_half_word_int_kinds_bit_exact(er, oracle, kind, a):
         assert_bits_equal(mem(o), ref, f"{kind}({a}) n={n}")
 
 
+UNIFORM_INT_RANGES = [(0, 9), (-5, 5), (1, 6), (0, 2), (0, 7), (7, 7), (-1000, 100000), (0, 65536),
+                      (-2 ** 31, 2 ** 31 - 1), (0, 2 ** 31 - 2), (10, 5)]
+
+
+@pytest.mark.parametrize("lo,hi", UNIFORM_INT_RANGES)
+def test_uniform_int_bit_exact(er, oracle, lo, hi):
+    """UniformIntGen<int32_t>: bit-slice rejection through CompressMask with
+    the carried lanes and the half() cache continuing across calls; power-of-two
+    ranges mask; a one-value range draws nothing; min > max follows the
+    reference's size_t arithmetic."""
+    u = er.Vmt19937_64(17)
+    e = oracle.Engine(17)
+    g = er.UniformIntGen(lo, hi)
+    og = oracle.Gen()
+    for n in (4, 8, 12, 1 << 20, 4, (1 << 16) + 4, 8):
+        ref = oracle.generate(e, og, "UNIFORM_INT", n, np.int32, lo, hi)
+        assert_bits_equal(mem(g.generate(n, 1, u)), ref, f"uniformInt[{lo},{hi}] n={n}")
+    # the engine continues exactly where the oracle's does
+    d, keep = er._desc("RANDBITS", torch.int32)
+    o = torch.empty(12, dtype=torch.int32, device="cuda")
+    er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), 12, er._stream_ptr()))
+    assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 12, np.int32), "randbits after")
+
+
+def test_uniform_int_many_streams(er, oracle):
+    K, per = 6, 4 * 3000
+    u = er.Vmt19937_64(23, streams=K)
+    x = mem(er.uniformInt(K * per, 1, u, -3, 20))
+    for k in range(K):
+        ref = oracle.generate(oracle.Engine(23 + 4 * k), oracle.Gen(), "UNIFORM_INT", per, np.int32, -3, 20)
+        assert_bits_equal(x[k * per:(k + 1) * per], ref, f"uniformInt slice {k}")
+
+
 def test_half_cache_shared_by_int_kinds(er, oracle):
     """RandbitsGen, BernoulliGen<int32_t> and GeometricGen all draw through
     rng.half(): a cached half left by one is used by the next."""

@@ -184,3 +184,19 @@ def test_oracle_fisher_f_is_mapped_beta(oracle, m, n):
         var = 2 * n * n * (m + n - 2) / (m * (n - 2) ** 2 * (n - 4)) if n > 4 else None
         tol = 5 * np.sqrt(var / big.size) if var else 0.05
         assert abs(big.mean() - n / (n - 2)) < tol
+
+
+@pytest.mark.parametrize("lo,hi", [(0, 9), (-5, 5), (1, 6), (-1000, 100000), (0, 7)])
+def test_oracle_uniform_int_is_uniform(oracle, lo, hi):
+    """The reference checks uniformInt with a chi-square test over its range
+    (test/test.cpp:598-634); the oracle passes the same test."""
+    from scipy import stats
+    n = 1 << 17
+    x = oracle.generate(oracle.Engine(9), oracle.Gen(), "UNIFORM_INT", n, np.int32, lo, hi)
+    assert x.min() >= lo and x.max() <= hi
+    k = hi - lo + 1
+    if k <= 64:
+        cnt = np.bincount(x - lo, minlength=k)
+        assert stats.chisquare(cnt).pvalue > 1e-4
+    else:
+        assert stats.kstest((x - lo + 0.5) / k, "uniform").pvalue > 1e-4
