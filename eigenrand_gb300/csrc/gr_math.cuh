@@ -18,6 +18,7 @@
 #pragma once
 #include <cstdint>
 
+#include "gr_dmath.h"
 #include "gr_math_tables.h"
 
 namespace gr {
@@ -94,73 +95,10 @@ __device__ __forceinline__ float expf_(float x) {
   return y * u2f((uint32_t)(ni + 127) << 23);
 }
 
-// Double log / exp: table-driven (P. T. P. Tang, ACM TOMS 1989 and 1990),
-// tables from derive_math_tables.py.  Max error measured against 40-digit
-// references: log 0.80 ulp, exp 0.51 ulp (0.75 ulp for subnormal results).
-// Special cases are decided on the bit pattern so the FP64 pipe only does
-// the arithmetic.
-__device__ __forceinline__ double log_(double x) {
-  uint64_t ux = d2u(x);
-  if ((ux & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return x;  // NaN
-  if (ux >> 63) return (ux << 1) == 0 ? -u2d(0x7ff0000000000000ull) : u2d(0x7ff8000000000000ull);
-  if (ux == 0) return -u2d(0x7ff0000000000000ull);
-  if (ux == 0x7ff0000000000000ull) return x;
-  int e = 0;
-  if (ux < 0x0010000000000000ull) {
-    x = x * 18014398509481984.0;  // 2^54
-    ux = d2u(x);
-    e = -54;
-  }
-  e += (int)(ux >> 52) - 1023;
-  const int i = (int)((ux >> 45) & 127);
-  const double m = u2d((ux & 0x000fffffffffffffull) | 0x3ff0000000000000ull);  // [1, 2)
-  const double r = fma(m, __ldg(&GRT_LOG_INVC[i]), -1.0);
-  const double de = (double)e;
-  const double hi = fma(de, GRT_LOG_LN2_HI, __ldg(&GRT_LOG_C_HI[i]));  // exact: both on the 2^-42 grid
-  const double lo = fma(de, GRT_LOG_LN2_LO, __ldg(&GRT_LOG_C_LO[i]));
-  const double r2 = r * r;
-  double q = GRT_LOG_Q6;
-  q = fma(q, r, GRT_LOG_Q5);
-  q = fma(q, r, GRT_LOG_Q4);
-  q = fma(q, r, GRT_LOG_Q3);
-  q = fma(q, r, GRT_LOG_Q2);
-  q = fma(q, r, GRT_LOG_Q1);
-  q = fma(q, r, GRT_LOG_Q0);
-  const double t = (r2 * r) * q;  // r^3 Q(r)
-  double s = lo + t;
-  s = s - 0.5 * r2;
-  s = s + r;
-  return hi + s;
-}
-
-__device__ __forceinline__ double exp_(double x) {
-  const uint64_t ax = d2u(x) & 0x7fffffffffffffffull;
-  if (ax >= 0x4086200000000000ull) {  // |x| >= 708, inf or NaN
-    if (ax > 0x7ff0000000000000ull) return x;
-    if (x > 709.782712893383973) return u2d(0x7ff0000000000000ull);
-    if (x < -745.1332191019412) return 0.0;
-  }
-  const double z = fma(x, GRT_EXP_INV_L, 6755399441055744.0);  // 1.5 * 2^52 + n
-  const double n = z - 6755399441055744.0;
-  const int32_t ni = (int32_t)(uint32_t)d2u(z);
-  const int j = ni & 63;
-  const int mm = (ni - j) / 64;
-  double r = fma(-n, GRT_EXP_L_HI, x);
-  r = fma(-n, GRT_EXP_L_LO, r);
-  double q = GRT_EXP_C6;
-  q = fma(q, r, GRT_EXP_C5);
-  q = fma(q, r, GRT_EXP_C4);
-  q = fma(q, r, GRT_EXP_C3);
-  q = fma(q, r, GRT_EXP_C2);
-  const double p = fma(r * r, q, r);  // exp(r) - 1
-  const double th = __ldg(&GRT_EXP_T_HI[j]);
-  double y = th + fma(th, p, __ldg(&GRT_EXP_T_LO[j]));
-  if (mm < -1022) {
-    y = y * u2d((uint64_t)(mm + 1022 + 1023) << 52);
-    return y * u2d(0x0010000000000000ull);  // 2^-1022
-  }
-  return y * u2d((uint64_t)(mm + 1023) << 52);
-}
+// Double log / exp in integer arithmetic (gr_dmath.h): no FP64 instruction,
+// about 0.5 ulp.
+__device__ __forceinline__ double log_(double x) { return grd_log(x); }
+__device__ __forceinline__ double exp_(double x) { return grd_exp(x); }
 
 // EigenRand psincos, float lanes (MorePacketMath.h:297-393).
 __device__ __forceinline__ void sincosf_(float x, float& s, float& c) {

@@ -1,12 +1,13 @@
 /*
  * CPU ORACLE — math.  Test infrastructure only; see oracle.h.
  *
- * log/exp: the library's own published-method implementations, restated here
- * independently of the device code (double: table-driven, tables from
- * ormath_tables.h).  Same operation order, explicit fma() /
- * fmaf() (correctly rounded), every other operation rounded on its own, so
- * the oracle and the CUDA kernels agree bit for bit.  Coefficients come from
- * eigenrand_gb300/csrc/derive_math_coeffs.py.
+ * log/exp: the library's own implementations, restated here independently of
+ * the device code.  Float: Cephes-style polynomials with the same operation
+ * order, explicit fmaf() (correctly rounded), every other operation rounded
+ * on its own (coefficients from eigenrand_gb300/csrc/derive_math_coeffs.py).
+ * Double: integer fixed-point arithmetic with one final rounding (tables
+ * from ormath_tables.h).  Either way the oracle and the CUDA kernels agree
+ * bit for bit.
  *
  * sincos: EigenRand's psincos (Cephes single-precision sin/cos with the
  * "extended precision modular arithmetic" reduction), restated lane-wise
@@ -97,70 +98,117 @@ float or_expf(float x) {
 }
 
 /* ------------------------------------------------------------- log, exp
- * Table-driven (P. T. P. Tang, ACM TOMS 1989 and 1990); tables and the
- * method notes in eigenrand_gb300/csrc/derive_math_tables.py.
+ * Integer arithmetic: fixed-point reductions and series in 64- and 128-bit
+ * integers, one final rounding to double (the method notes and tables are
+ * in eigenrand_gb300/csrc/derive_math_tables.py).  Restated here in C; the
+ * integer steps are exact, so the oracle and the kernels agree bit for bit.
  */
+typedef unsigned __int128 u128;
+typedef __int128 i128;
+
+static inline u128 u128_of(uint64_t hi, uint64_t lo) { return ((u128)hi << 64) | lo; }
+static inline int clz64(uint64_t x) { return __builtin_clzll(x); }
+static inline int64_t mulhi64(int64_t a, int64_t b) { return (int64_t)(((i128)a * b) >> 64); }
+
+/* A 2^-q (A > 0) rounded to nearest even, signed by `neg`: 53 significant
+ * bits, or down to 2^-1074 below the normal range; overflow gives infinity */
+static double round_fixed(u128 A, int q, int neg) {
+  const uint64_t hi = (uint64_t)(A >> 64), lo = (uint64_t)A;
+  const int p = hi ? 127 - clz64(hi) : 63 - clz64(lo);
+  int E = p - q;
+  const uint64_t sgn = (uint64_t)neg << 63;
+  if (E > 1023) return u2d(sgn | 0x7ff0000000000000ull);
+  const int sh = E >= -1022 ? p - 52 : q - 1074;
+  uint64_t sig;
+  if (sh <= 0) {
+    sig = (uint64_t)A << -sh;
+  } else if (sh >= 128) {
+    sig = 0;
+  } else {
+    sig = (uint64_t)(A >> sh);
+    const u128 rem = A & (((u128)1 << sh) - 1), half = (u128)1 << (sh - 1);
+    if (rem > half || (rem == half && (sig & 1))) ++sig;
+  }
+  if (E >= -1022) {
+    if (sig >> 53) {
+      sig >>= 1;
+      if (++E > 1023) return u2d(sgn | 0x7ff0000000000000ull);
+    }
+    return u2d(sgn | ((uint64_t)(E + 1023) << 52) | (sig & 0xfffffffffffffull));
+  }
+  return u2d(sgn | sig);
+}
+
+/* log x = e ln2 + L1_i + L2_j + r2 S(r2): two reciprocal reductions
+ * (y1 = M K1_i = (1 + r1) 2^60, y2 = y1 K2_j = (1 + r2) 2^80, exact),
+ * S(r) = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 in Q62, the sum in Q116 */
 double or_log(double x) {
-  uint64_t ux = d2u(x);
+  const uint64_t ux = d2u(x);
   if ((ux & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return x; /* NaN */
   if (ux >> 63) return (ux << 1) == 0 ? -INFINITY : u2d(0x7ff8000000000000ull);
   if (ux == 0) return -INFINITY;
   if (ux == 0x7ff0000000000000ull) return x;
-  int e = 0;
-  if (ux < 0x0010000000000000ull) {
-    x = x * 18014398509481984.0; /* 2^54 */
-    ux = d2u(x);
-    e = -54;
+  int e;
+  uint64_t M;
+  if (ux < 0x0010000000000000ull) { /* subnormal */
+    const int s = clz64(ux) - 11;
+    M = ux << s;
+    e = -1022 - s;
+  } else {
+    e = (int)(ux >> 52) - 1023;
+    M = (ux & 0xfffffffffffffull) | 0x10000000000000ull;
   }
-  e += (int)(ux >> 52) - 1023;
-  const int i = (int)((ux >> 45) & 127);
-  const double m = u2d((ux & 0x000fffffffffffffull) | 0x3ff0000000000000ull); /* [1, 2) */
-  const double r = fma(m, GRT_LOG_INVC[i], -1.0);
-  const double de = (double)e;
-  const double hi = fma(de, GRT_LOG_LN2_HI, GRT_LOG_C_HI[i]); /* exact: both on the 2^-42 grid */
-  const double lo = fma(de, GRT_LOG_LN2_LO, GRT_LOG_C_LO[i]);
-  const double r2 = r * r;
-  double q = GRT_LOG_Q6;
-  q = fma(q, r, GRT_LOG_Q5);
-  q = fma(q, r, GRT_LOG_Q4);
-  q = fma(q, r, GRT_LOG_Q3);
-  q = fma(q, r, GRT_LOG_Q2);
-  q = fma(q, r, GRT_LOG_Q1);
-  q = fma(q, r, GRT_LOG_Q0);
-  const double t = (r2 * r) * q; /* r^3 Q(r) */
-  double s = lo + t;
-  s = s - 0.5 * r2;
-  s = s + r;
-  return hi + s;
+  const int i = (int)((M >> 45) & 127);
+  const uint64_t y1 = M * (uint64_t)GRT_ILOG_K1[i];
+  const int64_t r1 = (int64_t)(y1 - (1ull << 60));
+  int j = (int)((r1 + (1ll << 45)) >> 46) + GRT_ILOG_J0;
+  if (j < 0) j = 0;
+  if (j > GRT_ILOG_JN - 1) j = GRT_ILOG_JN - 1;
+  const u128 y2 = (u128)y1 * GRT_ILOG_K2[j];
+  const int64_t r = (int64_t)((i128)(y2 - ((u128)1 << 80)) >> 4); /* Q76 */
+  int64_t s = GRT_ILOG_S0;
+  s = GRT_ILOG_S1 + (mulhi64(s, r) >> 12);
+  s = GRT_ILOG_S2 + (mulhi64(s, r) >> 12);
+  s = GRT_ILOG_S3 + (mulhi64(s, r) >> 12);
+  s = GRT_ILOG_S4 + (mulhi64(s, r) >> 12);
+  i128 v = (i128)e * (i128)u128_of(GRT_ILOG_LN2_HI, GRT_ILOG_LN2_LO);
+  v += (i128)u128_of(GRT_ILOG_L1[2 * i], GRT_ILOG_L1[2 * i + 1]);
+  v += (i128)u128_of(GRT_ILOG_L2[2 * j], GRT_ILOG_L2[2 * j + 1]);
+  v += ((i128)r * s) >> 22;
+  if (v == 0) return 0.0;
+  return v < 0 ? round_fixed((u128)(-v), 116, 1) : round_fixed((u128)v, 116, 0);
 }
 
+/* exp x = 2^(n div 64) 2^((n mod 64)/64) exp(r), n = round(64 x / ln2)
+ * estimated from x in Q20, r = x - n ln2/64 exact in Q100, exp(r) by its
+ * Taylor series to degree 7 in Q62, 2^(j/64) in Q63 */
 double or_exp(double x) {
-  const uint64_t ax = d2u(x) & 0x7fffffffffffffffull;
-  if (ax >= 0x4086200000000000ull) { /* |x| >= 708, inf or NaN */
-    if (ax > 0x7ff0000000000000ull) return x;
-    if (x > 709.782712893383973) return INFINITY;
-    if (x < -745.1332191019412) return 0.0;
+  const uint64_t ux = d2u(x), ax = ux & 0x7fffffffffffffffull;
+  if (ax > 0x7ff0000000000000ull) return x;
+  if (ax >= 0x4086200000000000ull) { /* |x| >= 708 */
+    if (!(ux >> 63) && ax > 0x40862e42fefa39efull) return INFINITY; /* > 709.782712893384 */
+    if ((ux >> 63) && ax > 0x40874910d52d3052ull) return 0.0;       /* < -745.1332191019412 */
   }
-  const double z = fma(x, GRT_EXP_INV_L, 6755399441055744.0); /* 1.5 * 2^52 + n */
-  const double n = z - 6755399441055744.0;
-  const int32_t ni = (int32_t)(uint32_t)d2u(z);
-  const int j = ni & 63;
-  int mm = (ni - j) / 64;
-  double r = fma(-n, GRT_EXP_L_HI, x);
-  r = fma(-n, GRT_EXP_L_LO, r);
-  double q = GRT_EXP_C6;
-  q = fma(q, r, GRT_EXP_C5);
-  q = fma(q, r, GRT_EXP_C4);
-  q = fma(q, r, GRT_EXP_C3);
-  q = fma(q, r, GRT_EXP_C2);
-  const double p = fma(r * r, q, r); /* exp(r) - 1 */
-  const double th = GRT_EXP_T_HI[j];
-  double y = th + fma(th, p, GRT_EXP_T_LO[j]);
-  if (mm < -1022) {
-    y = y * u2d((uint64_t)(mm + 1022 + 1023) << 52);
-    return y * u2d(0x0010000000000000ull); /* 2^-1022 */
-  }
-  return y * u2d((uint64_t)(mm + 1023) << 52);
+  if (ax < 0x3c90000000000000ull) return 1.0; /* |x| < 2^-54 */
+  const int ex = (int)(ax >> 52) - 1023;
+  const uint64_t M = (ax & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int sx = ex + 48;
+  i128 xv = sx >= 0 ? (i128)((u128)M << sx) : (i128)(M >> -sx);
+  if (ux >> 63) xv = -xv;
+  const int64_t xq = (int64_t)(xv >> 80);
+  const int64_t n = (xq * GRT_IEXP_INVL + (1ll << 39)) >> 40;
+  const i128 rv = xv - (i128)n * (i128)u128_of(GRT_IEXP_LN2_64_HI, GRT_IEXP_LN2_64_LO);
+  const int64_t r = (int64_t)(rv >> 36);
+  int64_t c = GRT_IEXP_C0;
+  c = GRT_IEXP_C1 + mulhi64(c, r);
+  c = GRT_IEXP_C2 + mulhi64(c, r);
+  c = GRT_IEXP_C3 + mulhi64(c, r);
+  c = GRT_IEXP_C4 + mulhi64(c, r);
+  c = GRT_IEXP_C5 + mulhi64(c, r);
+  c = GRT_IEXP_C6 + mulhi64(c, r);
+  c = GRT_IEXP_C7 + mulhi64(c, r);
+  const int jj = (int)(n & 63), m = (int)(n >> 6);
+  return round_fixed((u128)GRT_IEXP_T[jj] * (uint64_t)c, 125 - m, 0);
 }
 
 /* --------------------------------------------------------------- sincosf */
