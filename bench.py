@@ -713,11 +713,12 @@ def run_case(args):
         n = 1 << 14
         out = torch.empty((32 * n, 32), dtype=torch.float32, device="cuda").t()
         fn = lambda: g.generate(urng, n, out=out)
-    elif name in ("beta_f32", "beta_f64"):
+    elif name in ("beta_f32", "beta_f64", "beta_f64_4096"):
         dt = torch.float32 if name == "beta_f32" else torch.float64
         g = er.BetaGen(0.5, 2.0, dtype=dt)
-        out = torch.empty((2048, 2048), dtype=dt, device="cuda")
-        fn = lambda: g.generate(2048, 2048, urng, out=out)
+        side = 4096 if name.endswith("4096") else 2048  # 4096: the sweep's launch
+        out = torch.empty((side, side), dtype=dt, device="cuda")
+        fn = lambda: g.generate(side, side, urng, out=out)
     elif name == "poisson4":
         g = er.PoissonGen(4.0)
         out = torch.empty((2048, 2048), dtype=torch.int32, device="cuda")

@@ -369,6 +369,9 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
     default:
       return fail(GR_ERR_UNSUPPORTED, "distribution kind not implemented yet");
   }
+  // divisors and scales that are exactly 1 in the scalar type
+  if (p.kind == GR_EXPONENTIAL && (f ? p.fa == 1.0f : p.da == 1.0)) p.flags |= kParamUnitDiv;
+  if ((p.kind == GR_GAMMA || p.kind == GR_WEIBULL) && (f ? p.fb == 1.0f : p.db == 1.0)) p.flags |= kParamUnitScale;
   return GR_OK;
 }
 

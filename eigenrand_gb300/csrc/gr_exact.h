@@ -48,4 +48,35 @@ GR_HD double div_2p31m1(uint32_t k) {
   return bits_to_double(((uint64_t)(1023 - lz) << 52) + sig + rnd);
 }
 
+// 1 - u for u = asdouble((x & (2^52 - 1)) | 1.0) - 1 (the reference's
+// uniform double, then 1 - u): both steps are exact, and the result is
+// 2 - m = (2^52 - F) 2^-52 for the fraction F, built here from the integer.
+GR_HD double one_minus_ur_d(uint64_t x) {
+  const uint64_t F = x & 0xfffffffffffffull;
+  if (F == 0) return 1.0;
+  const uint64_t D = 0x10000000000000ull - F;  // 1 .. 2^52 - 1
+  const int p = 63 - clz64(D);                 // leading bit, 0 .. 51
+  return bits_to_double(((uint64_t)(p + 1023 - 52) << 52) | ((D << (52 - p)) & 0xfffffffffffffull));
+}
+
+// MT19937-64 tempering (PacketRandomEngine.h:295-310) and its inverse:
+// each step y ^= (y >> s) & m or y ^= (y << s) & m is undone by iterating
+// x = y ^ ((x >> s) & m) (or <<) until s (k + 1) >= 64.
+GR_HD uint64_t mt_temper64(uint64_t r) {
+  r ^= (r >> 29) & 0x5555555555555555ull;
+  r ^= (r << 17) & 0x71d67fffeda60000ull;
+  r ^= (r << 37) & 0xfff7eee000000000ull;
+  r ^= r >> 43;
+  return r;
+}
+GR_HD uint64_t mt_untemper64(uint64_t y) {
+  y ^= y >> 43;
+  y ^= (y << 37) & 0xfff7eee000000000ull;
+  uint64_t x = y;
+  for (int k = 0; k < 3; ++k) x = y ^ ((x << 17) & 0x71d67fffeda60000ull);
+  y = x;
+  for (int k = 0; k < 2; ++k) x = y ^ ((x >> 29) & 0x5555555555555555ull);
+  return x;
+}
+
 }  // namespace gr

@@ -195,14 +195,23 @@ template <int KIND>
 __device__ __forceinline__ double tf64(uint64_t r, const DistParams& d) {
   if (KIND == GR_UNIFORM_REAL) return ur_d(r);
   if (KIND == GR_UNIFORM_REAL2) return ur_d(r) * d.da + d.db;
-  if (KIND == GR_EXPONENTIAL) return -(log_(1.0 - ur_d(r)) / d.da);
-  if (KIND == GR_GAMMA) return d.db * (-(log_(1.0 - ur_d(r)) / 1.0));
+  if (KIND == GR_EXPONENTIAL) {
+    const double l = log_(one_minus_ur_d(r));
+    return (d.flags & kParamUnitDiv) ? -l : -(l / d.da);
+  }
+  if (KIND == GR_GAMMA) {
+    const double l = -(log_(one_minus_ur_d(r)) / 1.0);
+    return (d.flags & kParamUnitScale) ? l : d.db * l;
+  }
   if (KIND == GR_CAUCHY) {
     double s, c;
     sincos_(3.1415926535897932 * (ur_d(r) - 0.5), s, c);
     return d.da + d.db * (s / c);
   }
-  if (KIND == GR_WEIBULL) return exp_(log_(-log_(1.0 - ur_d(r))) * d.da) * d.db;
+  if (KIND == GR_WEIBULL) {
+    const double w = exp_(log_(-log_(one_minus_ur_d(r))) * d.da);
+    return (d.flags & kParamUnitScale) ? w : w * d.db;
+  }
   if (KIND == GR_EXTREME_VALUE) return d.da - log_(-log_(ur_d(r) + 2.220446049250313e-16 / 8)) * d.db;
   // BernoulliGen<double>: the compare runs on the eight 32-bit words and the
   // blend reads each 64-bit element's sign, the compare of its high word
@@ -484,9 +493,8 @@ __global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const Call
           double sv[2], cv[2];
 #pragma unroll
           for (int q = 0; q < 2; ++q) {
-            const double u1 = ur_d(odd ? other[q] : pk[q]);
             const double u2 = ur_d(odd ? pk[2 + q] : other[q]);
-            const double radius = sqrt(-2.0 * log_(1.0 - u1));
+            const double radius = sqrt(-2.0 * log_(one_minus_ur_d(odd ? other[q] : pk[q])));
             const double theta = (2 * 3.1415926535897932) * u2;
             double sn, cs;
             sincos_(theta, sn, cs);

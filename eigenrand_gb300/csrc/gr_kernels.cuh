@@ -22,9 +22,15 @@ struct DistParams {
   uint32_t bitmask;                        // alias table mask
   int32_t ncdf;                            // CDF entries (discrete < 16 weights)
   int32_t post;                            // output transform of a beta draw: 1 = FisherFGen (fh / dh = b/a)
+  int32_t flags;                           // kParamUnit*: a divisor or scale that is exactly 1 in the scalar type
   const int32_t* prob;                     // alias table / cdf (device)
   const int32_t* alias;
 };
+
+// x / 1 and x * 1 are x in IEEE arithmetic, so a parameter that is exactly 1
+// skips its division or multiplication without changing a bit.
+constexpr int32_t kParamUnitDiv = 1;    // ExponentialGen: lambda == 1
+constexpr int32_t kParamUnitScale = 2;  // GammaGen beta, WeibullGen b == 1
 
 // Output transform of generators built on a BetaGen draw x (bits v):
 // FisherFGen writes (b/a) x / (1 - x), b/a in the scalar type

@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "../../include/gpurand.h"
+#include "gr_exact.h"
 #include "gr_internal.h"
 #include "gr_kernels.cuh"
 #include "gr_math.cuh"
@@ -131,9 +132,10 @@ __global__ void __launch_bounds__(160)
         if (KIND == GR_GAMMA || KIND == GR_CHI_SQUARED) {
           double y = ur_d(rword(r0)) + 2.220446049250313e-16 / 8;
           for (int t = 1; t < U; ++t) y = y * (ur_d(rword(r0 + 4 * t)) + 2.220446049250313e-16 / 8);
-          reinterpret_cast<double*>(p.out)[o] = -(d.db * log_(y));
+          const double l = log_(y);
+          reinterpret_cast<double*>(p.out)[o] = (d.flags & kParamUnitScale) ? -l : -(d.db * l);
         } else if (KIND == GR_STUDENT_T) {
-          const double u1 = 1.0 - ur_d(rword(r0));
+          const double u1 = one_minus_ur_d(rword(r0));
           const double u2 = ur_d(rword(r0 + 4));
           const double radius = sqrt(d.da * (exp_(log_(u1) * d.dc) - 1.0));
           double sn, cs;
@@ -1346,7 +1348,6 @@ constexpr int kBetaThreads = 160;
 constexpr int kBetaRing = 640;              // positions whose masks are kept
 constexpr int kBetaRec = 160;               // output packets per walk step
 constexpr int kBetaPT = 128;                // partial trials per component per walk step
-constexpr int64_t kBetaMargin = 96;         // evaluated positions kept ahead of an output packet
 
 template <int DT>
 __host__ __device__ constexpr int beta_lanes() {
@@ -1638,33 +1639,35 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
         int nrec = 0, nf = 0, np[2] = {0, 0}, A[2] = {fc[0], fc[1]};
         const int64_t pk_end = (nb + 1) * kN;  // packets generated so far
         if (s < nb * kN - kN) s_err = 1;       // packets before s left the ring
-        while (E < Npk && s + kBetaMargin <= done_pos) {
-          if (nrec >= kBetaRec || np[0] > kBetaPT - 48 || np[1] > kBetaPT - 48) {
+        while (E < Npk) {
+          if (nrec >= kBetaRec) {
             s_more = 1;
             break;
           }
           int64_t x = s;
-          bool bad = false, full_bc = false;
-          for (int c = 0; c < 2 && !bad; ++c) {
+          bool full_bc = false;
+          // one component of output record nrec: 0 done, 1 partial-trial
+          // buffer full, 2 positions not evaluated yet (component index a
+          // compile-time constant, so the walk state stays in registers)
+          auto step = [&](auto cc) -> int {
+            constexpr int c = decltype(cc)::value;
             const int ty = c == 0 ? type0 : type1, U = c == 0 ? U0 : U1;
             if (ty <= 1) {
-              if (x + U > pk_end) bad = true;
+              if (x + U > pk_end) return 2;
               rec[nrec * 2 + c] = x;
               x += U;
-              continue;
+              return 0;
             }
             for (;;) {
-              if (x >= done_pos || np[c] >= kBetaPT) {
-                bad = true;
-                break;
-              }
+              if (x >= done_pos) return 2;
+              if (np[c] >= kBetaPT) return 1;
               const uint32_t m = pmask[c * kBetaRing + (int)(x % kBetaRing)];
               const int cn = __popc(m);
               if (cn == P) {
                 rec[nrec * 2 + c] = x;
                 if (c == bc) full_bc = true;
                 x += U;
-                break;
+                return 0;
               }
               ptx[c * kBetaPT + np[c]] = x;
               pA[c * kBetaPT + np[c]] = A[c];
@@ -1676,12 +1679,26 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
               if (fc[c] >= P) {
                 rec[nrec * 2 + c] = -(int64_t)(1 + (A[c] - fc[c]));
                 fc[c] -= P;
-                break;
+                return 0;
               }
             }
-          }
-          if (bad) {
-            s_err = 1;
+          };
+          // a record that does not fit rolls back: it waits for the next
+          // step (buffer full) or the next block (positions not evaluated)
+          const int np0 = np[0], np1 = np[1], a0 = A[0], a1 = A[1], f0 = fc[0], f1 = fc[1];
+          int stall = step(std::integral_constant<int, 0>{});
+          if (!stall) stall = step(std::integral_constant<int, 1>{});
+          if (stall) {
+            np[0] = np0;
+            np[1] = np1;
+            A[0] = a0;
+            A[1] = a1;
+            fc[0] = f0;
+            fc[1] = f1;
+            if (stall == 1) {
+              if (nrec == 0) s_err = 1;  // one record needs more partial trials than the buffer holds
+              else s_more = 1;
+            }
             break;
           }
           if (full_bc) fr[nf++] = (uint16_t)nrec;

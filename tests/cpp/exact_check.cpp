@@ -2,6 +2,7 @@
 // IEEE double division they replace.
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 
 #include "gr_exact.h"
 
@@ -15,5 +16,33 @@ int main() {
     }
   }
   std::printf("div_2p31m1 mismatches %llu of 2^31\n", bad);
-  return bad != 0;
+  // one_minus_ur_d: every fraction near both ends, and a stride through the rest
+  unsigned long long bad2 = 0, cnt = 0;
+  auto check = [&](uint64_t F) {
+    for (uint64_t hi : {0ull, 0x3ff0000000000000ull, 0xfff0000000000000ull}) {
+      const uint64_t x = hi | F;
+      const double u = gr::bits_to_double((x & 0xfffffffffffffull) | 0x3ff0000000000000ull) - 1.0;
+      const double want = 1.0 - u, got = gr::one_minus_ur_d(x);
+      ++cnt;
+      if (std::memcmp(&want, &got, sizeof want) != 0) {
+        if (bad2 < 5) std::printf("F=%llx want %a got %a\n", (unsigned long long)F, want, got);
+        ++bad2;
+      }
+    }
+  };
+  for (uint64_t F = 0; F < (1ull << 22); ++F) check(F);
+  for (uint64_t F = (1ull << 52) - (1ull << 22); F < (1ull << 52); ++F) check(F);
+  for (uint64_t F = 0; F < (1ull << 52); F += 0x3b9aca07ull) check(F);
+  std::printf("one_minus_ur_d mismatches %llu of %llu\n", bad2, cnt);
+  // untempering inverts tempering (xorshift-64 sequence of inputs)
+  unsigned long long bad3 = 0;
+  uint64_t s = 0x9e3779b97f4a7c15ull;
+  for (int i = 0; i < (1 << 24); ++i) {
+    s ^= s << 13;
+    s ^= s >> 7;
+    s ^= s << 17;
+    if (gr::mt_untemper64(gr::mt_temper64(s)) != s || gr::mt_temper64(gr::mt_untemper64(s)) != s) ++bad3;
+  }
+  std::printf("untemper mismatches %llu\n", bad3);
+  return bad != 0 || bad2 != 0 || bad3 != 0;
 }
