@@ -618,6 +618,7 @@ def cpu_run(per_dist_samples, threads=1):
     import pyoracle
     from concurrent.futures import ThreadPoolExecutor
     pyoracle.build()
+    pyoracle.set_fp_math(True)  # FP64 log / exp, the reference's speed class on a CPU
     items = sweep_items()
     dt = {"f32": np.float32, "f64": np.float64, "i32": np.int32}
     per_thread = max(8, (per_dist_samples // threads) // 8 * 8)
@@ -648,7 +649,8 @@ def cpu_baseline(seconds=15.0):
     return {"value": round(s / t / 1e9, 5), "unit": "Gsamples/s", "cores": threads, "kind": "port",
             "sample": f"{s // len(sweep_items())} samples per distribution x {len(sweep_items())} distributions "
                       f"({t:.1f} s), {threads} threads each with its own Vmt19937_64(1234+4k); the reference needs "
-                      "Eigen (absent), so its plain-C restatement in oracle/ runs"}
+                      "Eigen (absent), so its plain-C restatement in oracle/ runs, with the C library's FP64 "
+                      "log / exp standing in for Eigen's plog / pexp"}
 
 
 def run_reference(args, rank, world):

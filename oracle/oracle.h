@@ -127,6 +127,9 @@ float or_logf(float x);
 float or_expf(float x);
 double or_log(double x);
 double or_exp(double x);
+/* CPU-baseline timing mode: or_log / or_exp become the C library's FP64
+ * log / exp (never used for parity) */
+void or_set_fp_math(int on);
 void or_sincosf(float x, float* s, float* c);
 void or_sincos(double x, double* s, double* c);
 float or_lgamma_approxf(float x);

@@ -142,7 +142,15 @@ static double round_fixed(u128 A, int q, int neg) {
 /* log x = e ln2 + L1_i + L2_j + r2 S(r2): two reciprocal reductions
  * (y1 = M K1_i = (1 + r1) 2^60, y2 = y1 K2_j = (1 + r2) 2^80, exact),
  * S(r) = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 in Q62, the sum in Q116 */
+/* Timing mode for the CPU baseline: the integer arithmetic above is exact
+ * and portable but slow on a CPU, whose FP64 units are fast, while the
+ * reference calls Eigen's FP64 plog / pexp.  With it on, or_log / or_exp are
+ * the C library's FP64 log / exp (within an ulp; never used for parity). */
+static int g_fp_math = 0;
+void or_set_fp_math(int on) { g_fp_math = on; }
+
 double or_log(double x) {
+  if (g_fp_math) return log(x);
   const uint64_t ux = d2u(x);
   if ((ux & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return x; /* NaN */
   if (ux >> 63) return (ux << 1) == 0 ? -INFINITY : u2d(0x7ff8000000000000ull);
@@ -183,6 +191,7 @@ double or_log(double x) {
  * estimated from x in Q20, r = x - n ln2/64 exact in Q100, exp(r) by its
  * Taylor series to degree 7 in Q62, 2^(j/64) in Q63 */
 double or_exp(double x) {
+  if (g_fp_math) return exp(x);
   const uint64_t ux = d2u(x), ax = ux & 0x7fffffffffffffffull;
   if (ax > 0x7ff0000000000000ull) return x;
   if (ax >= 0x4086200000000000ull) { /* |x| >= 708 */

@@ -50,6 +50,8 @@ def lib():
         L.or_gen_poisson.restype = ctypes.c_int
         L.or_gen_randbits.argtypes = [vp, vp, sz]
         L.or_gen_randbits.restype = ctypes.c_int
+        L.or_set_fp_math.argtypes = [ctypes.c_int]
+        L.or_set_fp_math.restype = None
         L.or_gen_uniform_int.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
         L.or_gen_uniform_int.restype = ctypes.c_int
         for fn in ("or_gen_bernoulli_i32", "or_gen_geometric"):
@@ -269,3 +271,10 @@ def pin_engine():
         build()
     r = subprocess.run([PIN], capture_output=True, text=True)
     return r.returncode == 0, r.stdout
+
+
+def set_fp_math(on):
+    """CPU-baseline timing mode: double log / exp through the C library's FP64
+    functions, the speed class of the reference's Eigen plog / pexp (values
+    within an ulp of the exact integer versions; never used for parity)."""
+    lib().or_set_fp_math(1 if on else 0)
