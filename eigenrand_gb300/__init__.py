@@ -28,11 +28,11 @@ __all__ = [
     "GrError", "Vmt19937_64", "raw_u64", "version",
     "uniformReal", "balanced", "normal", "lognormal", "exponential", "cauchy", "weibull", "extremeValue",
     "gamma", "beta", "studentT", "chiSquared", "poisson", "binomial", "discrete", "randBits", "bernoulli",
-    "geometric", "fisherF", "uniformInt",
+    "geometric", "fisherF", "uniformInt", "negativeBinomial",
     "StdUniformRealGen", "UniformRealGen", "BalancedGen", "Balanced2Gen", "StdNormalGen", "NormalGen",
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
     "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen", "BernoulliGen",
-    "GeometricGen", "FisherFGen", "UniformIntGen",
+    "GeometricGen", "FisherFGen", "UniformIntGen", "NegativeBinomialGen",
     "sample_batched",
     "MvNormalGen", "WishartGen", "InvWishartGen", "DirichletGen", "MultinomialGen", "makeMvNormalGen",
     "makeMvNormalGenFromLt", "makeWishartGen", "makeWishartGenFromLt", "makeInvWishartGen",
@@ -327,6 +327,14 @@ class UniformIntGen(_Gen):
         super().__init__(torch.int32, float(min), float(max))
 
 
+class NegativeBinomialGen(_Gen):
+    """NegativeBinomialGen<int32_t>(trials, p) (GammaPoisson.h:28-98)."""
+    _kind = "NEGATIVE_BINOMIAL"
+
+    def __init__(self, trials=1, p=0.5):
+        super().__init__(torch.int32, p, trials=trials)
+
+
 class GeometricGen(_Gen):
     """GeometricGen<int32_t>(p) (Discrete.h:1338-1376)."""
     _kind = "GEOMETRIC"
@@ -418,6 +426,10 @@ def fisherF(rows, cols, urng, m=1.0, n=1.0, dtype=torch.float32, out=None, strea
 
 def uniformInt(rows, cols, urng, min, max, out=None, stream=None):
     return _sample("UNIFORM_INT", rows, cols, urng, torch.int32, float(min), float(max), out=out, stream=stream)
+
+
+def negativeBinomial(rows, cols, urng, trials=1, p=0.5, out=None, stream=None):
+    return _sample("NEGATIVE_BINOMIAL", rows, cols, urng, torch.int32, p, trials=trials, out=out, stream=stream)
 
 
 def geometric(rows, cols, urng, p=0.5, out=None, stream=None):

@@ -23,7 +23,7 @@ KINDS = dict(
     UNIFORM_REAL=1, UNIFORM_REAL2=2, BALANCED=3, BALANCED2=4, NORMAL_STD=5, NORMAL=6, LOGNORMAL=7,
     EXPONENTIAL=8, CAUCHY=9, WEIBULL=10, EXTREME_VALUE=11, GAMMA=12, BETA=13, STUDENT_T=14,
     CHI_SQUARED=15, POISSON=16, BINOMIAL=17, DISCRETE=18, RANDBITS=19, BINOMIAL_V=20, BERNOULLI=21,
-    GEOMETRIC=22, FISHER_F=23, UNIFORM_INT=24,
+    GEOMETRIC=22, FISHER_F=23, UNIFORM_INT=24, NEGATIVE_BINOMIAL=25,
 )
 
 # exported symbols, as declared in include/gpurand.h

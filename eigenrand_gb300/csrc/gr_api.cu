@@ -242,6 +242,18 @@ gr_status make_params(const gr_dist_desc& d, DistParams& p) {
     case GR_GEOMETRIC:  // GeometricGen(p): rlog_q = 1 / log(1 - p), set as a float packet (Discrete.h:1353-1374)
       p.fa = (float)(1 / std::log(1 - a));
       break;
+    case GR_NEGATIVE_BINOMIAL: {  // GammaGen<float>((float)trials, (float)((1 - p) / p)), GammaPoisson.h:42-45
+      if (d.trials < 1 || !(a > 0 && a <= 1)) return fail(GR_ERR_INVALID, "negativeBinomial needs trials >= 1, 0 < p <= 1");
+      const float af = (float)d.trials, bf = (float)((1 - a) / a);
+      p.fa = af;
+      p.fb = bf;
+      p.fc = std::sqrt(2 * af - 1);  // GammaGen::sqrt, NormalExp.h:455-459
+      p.fd = af - 1;
+      const int cnt = (int)af;
+      p.ia = cnt;
+      p.ic = af == 1.0f ? 0 : (((float)cnt == af && cnt < 20) ? 1 : 2);  // exponential / product / tan
+      break;
+    }
     case GR_UNIFORM_INT: {  // UniformIntGen<int32_t>(min, max), Discrete.h:230-245 (size_t arithmetic)
       const int32_t mn = (int32_t)a, mx = (int32_t)b;
       // pdiff = (size_t)(_max - _min): the int32 difference, sign-extended
@@ -498,6 +510,7 @@ Family family_of(const DistParams& dp) {
   if (dp.dtype == GR_I32 && dp.kind == GR_BINOMIAL && dp.ia >= 25 && dp.ic) return Family::Walk;
   if (dp.dtype != GR_I32 && dp.kind == GR_BETA && !dp.ic) return Family::Walk;
   if (dp.dtype == GR_I32 && dp.kind == GR_UNIFORM_INT) return Family::Walk;  // constant or rejection
+  if (dp.dtype == GR_I32 && dp.kind == GR_NEGATIVE_BINOMIAL) return Family::Walk;
   return Family::Unsupported;
 }
 
@@ -690,6 +703,9 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
     if (dp.kind == GR_UNIFORM_INT) {
       // every draw accepts each lane with probability > 1/2
       max_blocks = (npk * 16) / (2 * kN) + 64;
+    } else if (dp.kind == GR_NEGATIVE_BINOMIAL) {
+      // gamma draws (< 20 or ~2.5 per trial) plus the Poisson loop or trials
+      max_blocks = (npk * 160) / (2 * kN) + 64;
     } else if (dp.dtype == GR_I32) {
       // PoissonGen loop (mean < 12); BinomialGen with mean < 1 runs the same
       // loop on its poisson member and returns trials - res when p > 1/2

@@ -227,11 +227,6 @@ __device__ __forceinline__ double tw64(uint32_t w, const DistParams& d) {
   return KIND == GR_BALANCED ? z * 2.0 - 1.0 : z * d.da + d.db;
 }
 
-// _mm_cvttps_epi32 of one lane: truncation; NaN and out of range give INT_MIN
-__device__ __forceinline__ int32_t cvtt_f32(float x) {
-  return (x >= -2147483648.0f && x < 2147483648.0f) ? (int32_t)x : (int32_t)0x80000000u;
-}
-
 template <int KIND>
 __device__ __forceinline__ int32_t tw32(uint32_t w, const DistParams& d) {
   if (KIND == GR_RANDBITS) return (int32_t)w;

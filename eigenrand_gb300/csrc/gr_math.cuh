@@ -95,6 +95,11 @@ __device__ __forceinline__ float expf_(float x) {
   return y * u2f((uint32_t)(ni + 127) << 23);
 }
 
+// _mm_cvttps_epi32 of one lane: truncation; NaN and out of range give INT_MIN
+__device__ __forceinline__ int32_t cvtt_f32(float x) {
+  return (x >= -2147483648.0f && x < 2147483648.0f) ? (int32_t)x : (int32_t)0x80000000u;
+}
+
 // Double log / exp in integer arithmetic (gr_dmath.h): no FP64 instruction,
 // about 0.5 ulp.
 __device__ __forceinline__ double log_(double x) { return grd_log(x); }

@@ -2000,7 +2000,222 @@ static cudaError_t run_uniform_int(const Plan& p, const DistParams& d, int64_t m
   return cudaGetLastError();
 }
 
+// ===========================================================================
+// k_negbin: NegativeBinomialGen<int32_t>(trials, p) (GammaPoisson.h:42-98).
+// Per output packet: a Packet4f GammaGen((float)trials, (float)((1-p)/p))
+// draw over rng.half() words (NormalExp.h:568-604), then a Poisson draw with
+// those per-lane means: the multiplicative loop while no lane's mean exceeds
+// 12, else tan rejection whose CompressMask carry is the GammaGen's.  One
+// warp per engine: the warp twists its own engine blocks into 624
+// half-packet draws, and lanes 0-3 run the packet code in lock step (one
+// lane per packet lane, decisions by ballot).
+// ===========================================================================
+namespace {
+constexpr int kNbWarps = 4;                                         // engines per CTA
+constexpr size_t kNbWarpBytes = (size_t)2 * kLanes * kN * 8 + (size_t)2 * kN * 16 + 64;  // windows, draws, carry
+}
+
+__global__ void __launch_bounds__(32 * kNbWarps) k_negbin(Plan p, DistParams d, int64_t max_blocks) {
+  extern __shared__ __align__(16) uint64_t nb_dyn[];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kNbWarps + wi;
+  if (k >= p.K) return;  // the whole warp
+  uint8_t* base = reinterpret_cast<uint8_t*>(nb_dyn) + (size_t)wi * kNbWarpBytes;
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(base);
+  uint32_t(*hw)[4] = reinterpret_cast<uint32_t(*)[4]>(base + (size_t)2 * kLanes * kN * 8);
+  uint32_t* carry = reinterpret_cast<uint32_t*>(base + (size_t)2 * kLanes * kN * 8 + (size_t)2 * kN * 16);
+  EngState* st = p.eng + k;
+  GenSlot* gsl = &p.gen[k].s[0];
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  int32_t* out = reinterpret_cast<int32_t*>(p.out) + off;
+  const int64_t Npk = n / 4;
+  const float alpha = d.fa, beta = d.fb, gsq = d.fc, a1 = d.fd;
+  const int count = d.ia, mode = d.ic;  // mode 0: alpha == 1, 1: product of count uniforms, 2: tan rejection
+  const float eps8 = 1.1920928955078125e-07f / 8;
+  const float fpi = (float)3.1415926535897932;
+  (void)alpha;
+
+  for (int i = lane; i < kLanes * kN; i += 32) raw[0][i / kN][i % kN] = st->win[i / kN][i % kN];
+  int fc = min(max(gsl->rest_cnt, 0), 3);
+  if (lane < fc) carry[lane] = gsl->rest[lane];
+  __syncwarp();
+
+  // draws: the engine's cached half first, then the halves of new blocks
+  bool pending = st->half_valid != 0, abort = false;
+  int h = 2 * kN, cur = 0;
+  int64_t nb = 0;
+  auto next = [&]() -> uint32_t {
+    if (pending) {
+      pending = false;
+      return lane < 4 ? st->half_cache[lane] : 0u;
+    }
+    if (h == 2 * kN) {
+      if (nb >= max_blocks) {
+        abort = true;
+        return 0u;
+      }
+      __syncwarp();
+      uint64_t(*old)[kN] = raw[cur];
+      uint64_t(*nw)[kN] = raw[cur ^ 1];
+#pragma unroll 1
+      for (int ph = 0; ph < 2; ++ph) {
+        for (int ii = lane; ii < kM; ii += 32) {
+          const int i = ph * kM + ii;
+          uint64_t pk[kLanes];
+#pragma unroll
+          for (int l = 0; l < kLanes; ++l) {
+            const uint64_t b = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
+            const uint64_t c = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
+            const uint64_t v = mt_twist(old[l][i], b, c);
+            nw[l][i] = v;
+            pk[l] = mt_temper(v);
+          }
+          hw[2 * i][0] = (uint32_t)pk[0];
+          hw[2 * i][1] = (uint32_t)(pk[0] >> 32);
+          hw[2 * i][2] = (uint32_t)pk[1];
+          hw[2 * i][3] = (uint32_t)(pk[1] >> 32);
+          hw[2 * i + 1][0] = (uint32_t)pk[2];
+          hw[2 * i + 1][1] = (uint32_t)(pk[2] >> 32);
+          hw[2 * i + 1][2] = (uint32_t)pk[3];
+          hw[2 * i + 1][3] = (uint32_t)(pk[3] >> 32);
+        }
+        __syncwarp();
+      }
+      cur ^= 1;
+      ++nb;
+      h = 0;
+    }
+    const uint32_t v = lane < 4 ? hw[h][lane] : 0u;
+    ++h;
+    return v;
+  };
+  auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
+  // CompressMask::compress_append over lanes 0-3 (arch/AVX/PacketFilter.h:147-184)
+  auto compress = [&](uint32_t bits, bool acc, uint32_t& res) -> bool {
+    const unsigned m = mask4(acc);
+    if (m == 0xfu) {
+      res = bits;
+      return true;
+    }
+    if (lane < 4 && ((m >> lane) & 1u)) carry[fc + __popc(m & ((1u << lane) - 1))] = bits;
+    fc += __popc(m);
+    __syncwarp();
+    if (fc < 4) return false;
+    res = lane < 4 ? carry[lane] : 0u;
+    const uint32_t mv = lane < fc - 4 ? carry[4 + lane] : 0u;
+    __syncwarp();
+    if (lane < fc - 4) carry[lane] = mv;
+    fc -= 4;
+    __syncwarp();
+    return true;
+  };
+
+  int64_t e = 0;
+  for (; e < Npk && !abort; ++e) {
+    float mean = 0.0f;
+    if (mode == 0) {
+      mean = beta * (-(logf_(1.0f - ur_f(next())) / 1.0f));
+    } else if (mode == 1) {
+      float y = ur_f(next()) + eps8;
+      for (int c = 1; c < count; ++c) y = y * (ur_f(next()) + eps8);
+      mean = -(beta * logf_(y));
+    } else {
+      for (;;) {
+        float ys, yc;
+        sincosf_(fpi * ur_f(next()), ys, yc);
+        const float ux = ur_f(next());
+        if (abort) break;
+        const float yx = ys / yc;
+        const float xx = gsq * yx + a1;
+        const float ub = (yx * yx + 1.0f) * expf_(a1 * logf_(xx / a1) - yx * gsq);
+        uint32_t r;
+        if (compress(f2u(beta * xx), (0.0f < xx) && (ux <= ub), r)) {
+          mean = u2f(r);
+          break;
+        }
+      }
+    }
+    if (abort) break;
+    const float pne = expf_(-mean);
+    if (mask4(12.0f < mean) == 0) {
+      float val = 1.0f;
+      int32_t res = 0;
+      for (;;) {
+        val = val * ur_f(next());
+        if (abort) break;
+        const bool c = pne < val;
+        if (mask4(c) == 0) break;
+        res += c ? 1 : 0;
+      }
+      if (abort) break;
+      if (lane < 4) out[e * 4 + lane] = res;
+    } else {
+      const float sq = sqrtf(2.0f * mean), lm = logf_(mean), g1 = mean * lm - lgamma_approxf_(mean + 1.0f);
+      for (;;) {
+        float s, c;
+        sincosf_(fpi * ur_f(next()), s, c);
+        const float yx = s / c;
+        const float fres = truncf(sq * yx + mean);
+        const float p1 = (yx * yx + 1.0f) * 0.9f;
+        const float u2 = ur_f(next());
+        if (abort) break;
+        const float p2 = expf_((fres * lm - lgamma_approxf_(fres + 1.0f)) - g1);
+        uint32_t r;
+        if (compress(f2u(fres), (0.0f <= fres) && (u2 <= p1 * p2), r)) {
+          if (lane < 4) out[e * 4 + lane] = cvtt_f32(u2f(r));
+          break;
+        }
+      }
+    }
+  }
+
+  // ---- state after the call
+  if (abort) {
+    if (lane == 0) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+    return;
+  }
+  const bool used_block = nb > 0;  // the last draw came from the newest block (h >= 1)
+  if (used_block) {
+    const int last = h - 1;          // last draw consumed in the newest block
+    const int rr = last / 2 + 1;     // packets used of it
+    uint64_t(*lastb)[kN] = raw[cur];
+    uint64_t(*prevb)[kN] = raw[cur ^ 1];
+    for (int t = lane; t < kLanes * kN; t += 32) {
+      const int l = t / kN, i = t % kN;
+      st->win[l][i] = (i < kN - rr) ? prevb[l][rr + i] : lastb[l][i - (kN - rr)];
+    }
+    if (lane < 4) st->half_cache[lane] = (last & 1) == 0 ? hw[last + 1][lane] : 0u;
+    if (lane == 0) {
+      st->half_valid = (last & 1) == 0 ? 1 : 0;
+      st->consumed += (uint64_t)((nb - 1) * kN + rr);
+    }
+  } else if (lane == 0 && st->half_valid && Npk > 0) {
+    st->half_valid = 0;  // only the cached half was drawn
+  }
+  if (lane < fc) gsl->rest[lane] = carry[lane];
+  if (lane == 0) gsl->rest_cnt = fc;
+}
+
+static cudaError_t run_negbin(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  constexpr size_t smem = kNbWarpBytes * kNbWarps;
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_negbin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_negbin<<<(p.K + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, smem, s>>>(p, d, max_blocks);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
+  if (d.kind == GR_NEGATIVE_BINOMIAL) return run_negbin(p, d, max_blocks, s);
   if (d.kind == GR_UNIFORM_INT) return run_uniform_int(p, d, max_blocks, s);
   if (d.dtype == GR_I32) return run_poisson(p, d, max_blocks, s);
   if (d.dtype == GR_F32) return run_beta<SD_F32>(p, d, max_blocks, s);

@@ -74,7 +74,8 @@ typedef enum {
   GR_BERNOULLI = 21,    /* BernoulliGen(p=a), f32 / f64 / int32; Basic.h:669-708    */
   GR_GEOMETRIC = 22,    /* GeometricGen<int32_t>(p=a); Discrete.h:1338-1376         */
   GR_FISHER_F = 23,     /* FisherFGen(m=a, n=b); NormalExp.h:984-1023             */
-  GR_UNIFORM_INT = 24   /* UniformIntGen<int32_t>(min=a, max=b); Discrete.h:214-336 */
+  GR_UNIFORM_INT = 24,  /* UniformIntGen<int32_t>(min=a, max=b); Discrete.h:214-336 */
+  GR_NEGATIVE_BINOMIAL = 25 /* NegativeBinomialGen<int32_t>(trials, p=a); GammaPoisson.h:28-98 */
 } gr_dist_kind;
 
 typedef struct {

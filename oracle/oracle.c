@@ -888,6 +888,114 @@ int or_gen_uniform_int(or_vmt* e, or_gen* g, int32_t mn, int32_t mx, int32_t* ou
   return 0;
 }
 
+/* NegativeBinomialGen<int32_t>(trials, p), GammaPoisson.h:42-98: a Packet4f
+ * GammaGen<float>((float)trials, (float)((1 - p) / p)) draw (NormalExp.h:
+ * 568-604 over rng.half() words), then a Poisson draw with those per-lane
+ * means: the multiplicative loop when no lane's mean exceeds 12, else tan
+ * rejection whose CompressMask carry is the GammaGen's own. */
+int or_gen_negative_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out, size_t n) {
+  if (n % 4 || e->L != 4) return 2;
+  const float alpha = (float)trials, beta = (float)((1 - p) / p);
+  const float gsq = sqrtf(2 * alpha - 1);
+  const int count0 = (int)alpha;
+  const float eps8 = 1.1920928955078125e-07f / 8;
+  for (size_t k = 0; k < n / 4; ++k) {
+    float mean[4];
+    if (alpha == 1) { /* beta * ExponentialGen(1) */
+      float u[4];
+      ur_f4(e, u);
+      for (int j = 0; j < 4; ++j) mean[j] = beta * (-(or_logf(1.0f - u[j]) / 1.0f));
+    } else if ((float)count0 == alpha && count0 < 20) { /* product of count uniforms */
+      float y[4], u[4];
+      ur_f4(e, u);
+      for (int j = 0; j < 4; ++j) y[j] = u[j] + eps8;
+      for (int c = 1; c < count0; ++c) {
+        ur_f4(e, u);
+        for (int j = 0; j < 4; ++j) y[j] = y[j] * (u[j] + eps8);
+      }
+      for (int j = 0; j < 4; ++j) mean[j] = -(beta * or_logf(y[j]));
+    } else { /* tan rejection, NormalExp.h:589-603 */
+      const float a1 = alpha - 1;
+      for (;;) {
+        float u[4], ux[4];
+        ur_f4(e, u);
+        float xx[4], ys[4], yc[4];
+        int mask[4];
+        for (int j = 0; j < 4; ++j) or_sincosf((float)PI_D * u[j], &ys[j], &yc[j]);
+        ur_f4(e, ux);
+        float cands[4];
+        for (int j = 0; j < 4; ++j) {
+          const float yx = ys[j] / yc[j];
+          xx[j] = gsq * yx + a1;
+          const float ub = (yx * yx + 1.0f) * or_expf(a1 * or_logf(xx[j] / a1) - yx * gsq);
+          mask[j] = (0.0f < xx[j]) && (ux[j] <= ub);
+          cands[j] = beta * xx[j];
+        }
+        int full = 0;
+        g->rest_cnt = compress_append(4, 0, cands, mask, g->rest, g->rest_cnt, &full);
+        if (full) {
+          memcpy(mean, cands, sizeof mean);
+          break;
+        }
+      }
+    }
+    float pne[4];
+    int big = 0;
+    for (int j = 0; j < 4; ++j) {
+      pne[j] = or_expf(-mean[j]);
+      big |= 12.0f < mean[j];
+    }
+    if (!big) {
+      float val[4] = {1, 1, 1, 1};
+      int32_t res[4] = {0, 0, 0, 0};
+      for (;;) {
+        float u[4];
+        ur_f4(e, u);
+        int any = 0, c[4];
+        for (int j = 0; j < 4; ++j) {
+          val[j] = val[j] * u[j];
+          c[j] = pne[j] < val[j];
+          any |= c[j];
+        }
+        if (!any) break;
+        for (int j = 0; j < 4; ++j) res[j] += c[j];
+      }
+      memcpy(out + 4 * k, res, sizeof res);
+      continue;
+    }
+    float st[4], lm[4], g1[4];
+    for (int j = 0; j < 4; ++j) {
+      st[j] = sqrtf(2.0f * mean[j]);
+      lm[j] = or_logf(mean[j]);
+      g1[j] = mean[j] * lm[j] - or_lgamma_approxf(mean[j] + 1.0f);
+    }
+    for (;;) {
+      float u[4], u2[4], fres[4], p1[4];
+      ur_f4(e, u);
+      for (int j = 0; j < 4; ++j) {
+        float s, c;
+        or_sincosf((float)PI_D * u[j], &s, &c);
+        const float yx = s / c;
+        fres[j] = truncf(st[j] * yx + mean[j]);
+        p1[j] = (yx * yx + 1.0f) * 0.9f;
+      }
+      ur_f4(e, u2);
+      int mask[4];
+      for (int j = 0; j < 4; ++j) {
+        const float p2 = or_expf((fres[j] * lm[j] - or_lgamma_approxf(fres[j] + 1.0f)) - g1[j]);
+        mask[j] = (0.0f <= fres[j]) && (u2[j] <= p1[j] * p2);
+      }
+      int full = 0;
+      g->rest_cnt = compress_append(4, 0, fres, mask, g->rest, g->rest_cnt, &full);
+      if (full) {
+        for (int j = 0; j < 4; ++j) out[4 * k + j] = cvtt_f32(fres[j]);
+        break;
+      }
+    }
+  }
+  return 0;
+}
+
 /* ======================================================================
  * DiscreteGen<int32_t, int32_t>: CDF (<16 weights) or AliasMethod (>=16),
  * Discrete.h:23-207 (table build), :385-412 (constructor), :443-485 (AVX2

@@ -50,6 +50,8 @@ def lib():
         L.or_gen_poisson.restype = ctypes.c_int
         L.or_gen_randbits.argtypes = [vp, vp, sz]
         L.or_gen_randbits.restype = ctypes.c_int
+        L.or_gen_negative_binomial.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_double, vp, sz]
+        L.or_gen_negative_binomial.restype = ctypes.c_int
         L.or_set_fp_math.argtypes = [ctypes.c_int]
         L.or_set_fp_math.restype = None
         L.or_gen_uniform_int.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
@@ -135,6 +137,9 @@ def generate(eng, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0, weight
     if kind == "BERNOULLI" and dtype != np.int32:
         out = np.empty(n, dtype=dtype)
         rc = L.or_gen_real(eng.h, gen.ptr, OR_BERNOULLI, 1 if dtype == np.float64 else 0, a, 0.0, _p(out), n)
+    elif kind == "NEGATIVE_BINOMIAL":
+        out = np.empty(n, dtype=np.int32)
+        rc = L.or_gen_negative_binomial(eng.h, gen.ptr, int(trials), a, _p(out), n)
     elif kind == "UNIFORM_INT":
         out = np.empty(n, dtype=np.int32)
         rc = L.or_gen_uniform_int(eng.h, gen.ptr, int(a), int(b), _p(out), n)

@@ -47,6 +47,9 @@ _add("uniformInt_0_9", "UNIFORM_INT", np.int32, 256, 0, 9)
 _add("uniformInt_m5_5", "UNIFORM_INT", np.int32, 256, -5, 5)
 _add("uniformInt_0_7", "UNIFORM_INT", np.int32, 256, 0, 7)
 _add("uniformInt_big", "UNIFORM_INT", np.int32, 256, -1000, 100000)
+_add("negbin_5_03", "NEGATIVE_BINOMIAL", np.int32, 256, 0.3, trials=5)
+_add("negbin_1_05", "NEGATIVE_BINOMIAL", np.int32, 256, 0.5, trials=1)
+_add("negbin_25_05", "NEGATIVE_BINOMIAL", np.int32, 256, 0.5, trials=25)
 
 
 def run_oracle(oracle, c):

@@ -402,6 +402,34 @@ def test_uniform_int_bit_exact(er, oracle, lo, hi):
     assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 12, np.int32), "randbits after")
 
 
+@pytest.mark.parametrize("trials,p", [(5, 0.3), (1, 0.5), (3, 0.9), (25, 0.5), (2, 0.05), (19, 0.6), (40, 0.2)])
+def test_negative_binomial_bit_exact(er, oracle, trials, p):
+    """NegativeBinomialGen<int32_t>: gamma draw (exponential, product or tan
+    rejection), then the Poisson loop or tan rejection through the shared
+    CompressMask carry; the carry and the half() cache continue across calls."""
+    u = er.Vmt19937_64(19)
+    e = oracle.Engine(19)
+    g = er.NegativeBinomialGen(trials, p)
+    og = oracle.Gen()
+    for n in (4, 8, 1 << 17, 12, (1 << 14) + 4):
+        ref = oracle.generate(e, og, "NEGATIVE_BINOMIAL", n, np.int32, p, trials=trials)
+        assert_bits_equal(mem(g.generate(n, 1, u)), ref, f"negbin({trials},{p}) n={n}")
+    d, keep = er._desc("RANDBITS", torch.int32)
+    o = torch.empty(12, dtype=torch.int32, device="cuda")
+    er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), 12, er._stream_ptr()))
+    assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 12, np.int32), "randbits after")
+
+
+def test_negative_binomial_many_streams(er, oracle):
+    K, per = 9, 4 * 1500
+    u = er.Vmt19937_64(29, streams=K)
+    x = mem(er.negativeBinomial(K * per, 1, u, 4, 0.35))
+    for k in range(K):
+        ref = oracle.generate(oracle.Engine(29 + 4 * k), oracle.Gen(), "NEGATIVE_BINOMIAL", per, np.int32, 0.35,
+                              trials=4)
+        assert_bits_equal(x[k * per:(k + 1) * per], ref, f"negbin slice {k}")
+
+
 def test_uniform_int_many_streams(er, oracle):
     K, per = 6, 4 * 3000
     u = er.Vmt19937_64(23, streams=K)

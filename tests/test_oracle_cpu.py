@@ -218,3 +218,15 @@ def test_oracle_uniform_int_is_uniform(oracle, lo, hi):
         assert stats.chisquare(cnt).pvalue > 1e-4
     else:
         assert stats.kstest((x - lo + 0.5) / k, "uniform").pvalue > 1e-4
+
+
+@pytest.mark.parametrize("trials,p", [(5, 0.3), (1, 0.5), (3, 0.9), (2, 0.05)])
+def test_oracle_negative_binomial_moments(oracle, trials, p):
+    """NegativeBinomialGen: mean r(1-p)/p and variance r(1-p)/p^2 (the
+    reference's tests only run it)."""
+    n = 1 << 16
+    x = oracle.generate(oracle.Engine(13), oracle.Gen(), "NEGATIVE_BINOMIAL", n, np.int32, p, trials=trials)
+    m, v = trials * (1 - p) / p, trials * (1 - p) / p ** 2
+    assert x.min() >= 0
+    assert abs(x.mean() - m) < 5 * np.sqrt(v / n)
+    assert abs(x.var() / v - 1) < 0.08
