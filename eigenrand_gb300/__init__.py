@@ -416,7 +416,20 @@ def randBits(rows, cols, urng, out=None, stream=None):
     return _sample("RANDBITS", rows, cols, urng, torch.int32, out=out, stream=stream)
 
 
-def bernoulli(rows, cols, urng, p=0.5, dtype=torch.float32, out=None, stream=None):
+def bernoulli(*args, p=0.5, dtype=torch.float32, out=None, stream=None):
+    """bernoulli(rows, cols, urng, p=0.5) -> BernoulliGen; bernoulli(urng, p_tensor)
+    -> BernoulliVGen<float>, one probability per element (Basic.h:1105-1153)."""
+    if args and isinstance(args[0], Vmt19937_64):
+        urng, pv = args[0], args[1]
+        pv = pv.to(device="cuda", dtype=torch.float32).contiguous()
+        o = torch.empty_like(pv) if out is None else out
+        d, keep = _desc("BERNOULLI", torch.float32)
+        _lib.check(_L.gr_sample_v(urng._h, ctypes.byref(d), _ptr(pv), _ptr(o), pv.numel(), _stream_ptr(stream)))
+        del keep
+        return o
+    rows, cols, urng = args[:3]
+    if len(args) > 3:
+        p = args[3]
     return _sample("BERNOULLI", rows, cols, urng, dtype, p, out=out, stream=stream)
 
 

@@ -970,6 +970,20 @@ gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_
   return st;
 }
 
+gr_status gr_sample_v(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, void* dev_out, size_t n,
+                      gr_stream_t stream) {
+  if (!e || !desc || (n && (!dev_a || !dev_out))) return fail(GR_ERR_INVALID, "NULL argument");
+  if (desc->kind != GR_BERNOULLI || desc->dtype != GR_F32)
+    return fail(GR_ERR_UNSUPPORTED, "per-element parameters: BernoulliVGen<float> only");
+  if (((uintptr_t)dev_a | (uintptr_t)dev_out) % 16)
+    return fail(GR_ERR_INVALID, "parameter and output arrays must be 16-byte aligned");
+  DistParams dp{};
+  dp.kind = kBernoulliVKind;
+  dp.dtype = GR_F32;
+  dp.vparam = dev_a;
+  return run_call(e, nullptr, dp, dev_out, n, (cudaStream_t)stream);
+}
+
 }  // extern "C"
 
 // ---- multinomial draws on an engine (k_multinomial, gr_mv.cu) ---------------

@@ -48,6 +48,7 @@ struct GenState {
 // (20592 >= 19968 terms + 312 window words + register look-ahead).
 constexpr int kPrefixLen = kN + 130 * kM;
 constexpr int kRawKind = 100;  // internal kind id for the raw u64 stream
+constexpr int kBernoulliVKind = 101;  // BernoulliVGen<float>: per-element probability (DistParams::vparam)
 
 // Caches as they were when a segmented call started (written by the prefix
 // kernel, read by every segment so that the last segment may update the live

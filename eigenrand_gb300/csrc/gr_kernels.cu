@@ -374,10 +374,23 @@ __global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const Call
         if (valid) {
           float* o = reinterpret_cast<float*>(p.out) + obase + pidx * 8;
           float v[8];
+          if (KIND == kBernoulliVKind) {
+            // BernoulliVGen<float>: p = cvttps(a * 2^31), compared signed with
+            // the masked word (Basic.h:735-745)
+            const float4* pv = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(d.vparam) + obase + pidx * 8);
+            const float4 q0 = pv[0], q1 = pv[1];
+            const float pa[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
 #pragma unroll
-          for (int l = 0; l < kLanes; ++l) {
-            v[2 * l] = tf32<KIND>((uint32_t)pk[l], d);
-            v[2 * l + 1] = tf32<KIND>((uint32_t)(pk[l] >> 32), d);
+            for (int q = 0; q < 8; ++q) {
+              const uint32_t w = (q & 1) ? (uint32_t)(pk[q >> 1] >> 32) : (uint32_t)pk[q >> 1];
+              v[q] = ((int32_t)(w & 0x7fffffffu) < cvtt_f32(pa[q] * 2147483648.0f)) ? 1.0f : 0.0f;
+            }
+          } else {
+#pragma unroll
+            for (int l = 0; l < kLanes; ++l) {
+              v[2 * l] = tf32<KIND>((uint32_t)pk[l], d);
+              v[2 * l + 1] = tf32<KIND>((uint32_t)(pk[l] >> 32), d);
+            }
           }
           reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
           reinterpret_cast<float4*>(o)[1] = make_float4(v[4], v[5], v[6], v[7]);
@@ -601,6 +614,8 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
       return d.ia == 1;  // alpha == 1: beta * exponential
     case GR_BERNOULLI:
       return true;
+    case kBernoulliVKind:
+      return dtype == GR_F32;
     case GR_RANDBITS:
     case GR_DISCRETE:
     case GR_GEOMETRIC:
@@ -633,6 +648,7 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F32_CASE(GR_EXTREME_VALUE)
       GR_F32_CASE(GR_GAMMA)
       GR_F32_CASE(GR_BERNOULLI)
+      GR_F32_CASE(kBernoulliVKind)
       case GR_NORMAL_STD:
         return run_direct<M_N32, GR_NORMAL_STD>(p, d, snap, s);
       case GR_NORMAL:

@@ -23,6 +23,7 @@ struct DistParams {
   int32_t ncdf;                            // CDF entries (discrete < 16 weights)
   int32_t post;                            // output transform of a beta draw: 1 = FisherFGen (fh / dh = b/a)
   int32_t flags;                           // kParamUnit*: a divisor or scale that is exactly 1 in the scalar type
+  const void* vparam;                      // per-element parameter array (device), aligned with the output
   const int32_t* prob;                     // alias table / cdf (device)
   const int32_t* alias;
 };

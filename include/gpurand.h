@@ -154,6 +154,17 @@ typedef struct {
 } gr_batch_desc;
 gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* batch, gr_stream_t stream);
 
+/* ---- per-element parameters ---------------------------------------------
+ * The reference's vectorized forms that take a parameter array of the
+ * output's shape: out[i] drawn with parameter a[i] (device arrays of n
+ * elements, 16-byte aligned).  Supported: GR_BERNOULLI with GR_F32 --
+ * BernoulliVGen<float> (Basic.h:711-747, bernoulli(urng, ArrayXf p),
+ * :1146-1153).  The double form goes through a packet cast the reference
+ * leaves to Eigen's generic pcast, which cannot be pinned here: it returns
+ * GR_ERR_UNSUPPORTED. */
+gr_status gr_sample_v(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, void* dev_out, size_t n,
+                      gr_stream_t stream);
+
 /* ---- multivariate generators (EigenRand/MvDists) -------------------------
  * Each object mirrors one Mv*Gen instance: its parameters, the FP64 factor of
  * its covariance / scale matrix (computed on the GPU at creation), and the

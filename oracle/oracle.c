@@ -822,6 +822,20 @@ static int32_t cvtt_f32(float x) {
   return (x >= -2147483648.0f && x < 2147483648.0f) ? (int32_t)x : INT32_MIN;
 }
 
+/* BernoulliVGen<float>::packetOp, Basic.h:735-745: one Packet8i rawbits
+ * packet (rng()), p = pcast<Packet8f, Packet8i>(a * 2^31) (cvttps2dq),
+ * compared signed with the masked words */
+int or_gen_bernoulli_v_f32(or_vmt* e, const float* pv, float* out, size_t n) {
+  if (n % 8 || e->L != 4) return 2;
+  for (size_t k = 0; k < n / 8; ++k) {
+    uint32_t w[8];
+    draw_full(e, w);
+    for (int j = 0; j < 8; ++j)
+      out[8 * k + j] = ((int32_t)(w[j] & 0x7fffffffu) < cvtt_f32(pv[8 * k + j] * 2147483648.0f)) ? 1.0f : 0.0f;
+  }
+  return 0;
+}
+
 /* GeometricGen<int32_t>::packetOp<Packet4i>, Discrete.h:1355-1375:
  * rlog_q = 1 / log(1 - p) in double, set as a float packet; u from
  * StdUniformRealGen<float> over Packet4f (rng.half() words);

@@ -100,6 +100,7 @@ int or_gen_bernoulli_i32(or_vmt* e, double p, int32_t* out, size_t n);
 int or_gen_geometric(or_vmt* e, double p, int32_t* out, size_t n);
 int or_gen_uniform_int(or_vmt* e, or_gen* g, int32_t mn, int32_t mx, int32_t* out, size_t n);
 int or_gen_negative_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out, size_t n);
+int or_gen_bernoulli_v_f32(or_vmt* e, const float* pv, float* out, size_t n);
 
 /* discrete with int32 precision (DiscreteGen<int32_t, int32_t>) */
 typedef struct {

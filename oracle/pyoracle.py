@@ -52,6 +52,8 @@ def lib():
         L.or_gen_randbits.restype = ctypes.c_int
         L.or_gen_negative_binomial.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_double, vp, sz]
         L.or_gen_negative_binomial.restype = ctypes.c_int
+        L.or_gen_bernoulli_v_f32.argtypes = [vp, vp, vp, sz]
+        L.or_gen_bernoulli_v_f32.restype = ctypes.c_int
         L.or_set_fp_math.argtypes = [ctypes.c_int]
         L.or_set_fp_math.restype = None
         L.or_gen_uniform_int.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
@@ -283,3 +285,13 @@ def set_fp_math(on):
     functions, the speed class of the reference's Eigen plog / pexp (values
     within an ulp of the exact integer versions; never used for parity)."""
     lib().or_set_fp_math(1 if on else 0)
+
+
+def bernoulli_v(eng, p):
+    """BernoulliVGen<float>: one probability per element (float32 array)."""
+    p = np.ascontiguousarray(p, dtype=np.float32)
+    out = np.empty_like(p)
+    rc = lib().or_gen_bernoulli_v_f32(eng.h, _p(p), _p(out), p.size)
+    if rc != 0:
+        raise RuntimeError(f"oracle error {rc} for bernoulli_v")
+    return out

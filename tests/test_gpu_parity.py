@@ -455,6 +455,35 @@ def test_half_cache_shared_by_int_kinds(er, oracle):
         assert_bits_equal(mem(o), ref, f"{kind} n={n}")
 
 
+def test_bernoulli_per_element(er, oracle):
+    """BernoulliVGen<float> (bernoulli(urng, ArrayXf p)): one probability per
+    element, including 0, 1 (which the packet path turns into 0) and tiny
+    values; long calls run as jump segments; K streams split the array."""
+    rng = np.random.default_rng(5)
+    pv = rng.uniform(0, 1, 1 << 20).astype(np.float32)
+    pv[:8] = [0.0, 1.0, 1e-9, 0.5, 0.999999, 2 ** -31, 0.25, 0.75]
+    for streams in (1, 5):
+        u = er.Vmt19937_64(61, streams=streams)
+        got = er.bernoulli(u, torch.from_numpy(pv)).cpu().numpy()
+        # slices of whole packets, the first (granules mod K) one packet longer
+        g, r = divmod(pv.size // 8, streams)
+        lo = 0
+        for k in range(streams):
+            hi = lo + 8 * (g + (1 if k < r else 0))
+            ref = oracle.bernoulli_v(oracle.Engine(61 + 4 * k), pv[lo:hi])
+            assert_bits_equal(got[lo:hi], ref, f"bernoulliV streams={streams} slice {k}")
+            lo = hi
+    u = er.Vmt19937_64(62)
+    e = oracle.Engine(62)
+    for n in (8, 64, 8):  # consecutive calls continue the stream
+        q = rng.uniform(0, 1, n).astype(np.float32)
+        assert_bits_equal(er.bernoulli(u, torch.from_numpy(q)).cpu().numpy(), oracle.bernoulli_v(e, q), f"n={n}")
+    with pytest.raises(er.GrError):
+        d, keep = er._desc("BERNOULLI", torch.float64)
+        t = torch.zeros(8, dtype=torch.float64, device="cuda")
+        er._lib.check(er._L.gr_sample_v(u._h, er.ctypes.byref(d), er._ptr(t), er._ptr(t), 8, er._stream_ptr()))
+
+
 def test_bernoulli_real_generator_and_invalid_p(er, oracle):
     for tdt in (torch.float32, torch.float64):
         u = er.Vmt19937_64(3)

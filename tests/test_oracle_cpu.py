@@ -230,3 +230,13 @@ def test_oracle_negative_binomial_moments(oracle, trials, p):
     assert x.min() >= 0
     assert abs(x.mean() - m) < 5 * np.sqrt(v / n)
     assert abs(x.var() / v - 1) < 0.08
+
+
+def test_oracle_bernoulli_per_element(oracle):
+    """BernoulliVGen<float>: P(1) = p per element (to 2^-31 and float
+    rounding); p = 1 gives 0 on the packet path."""
+    p = np.repeat(np.array([0.05, 0.3, 0.5, 0.9, 1.0], dtype=np.float32), 1 << 14)
+    x = oracle.bernoulli_v(oracle.Engine(4), p).reshape(5, -1)
+    for k, pk in enumerate([0.05, 0.3, 0.5, 0.9]):
+        assert abs(x[k].mean() - pk) < 5 * np.sqrt(pk * (1 - pk) / x.shape[1])
+    assert not x[4].any()
