@@ -721,6 +721,13 @@ def run_case(args):
         side = 4096 if name.endswith("4096") else 2048  # 4096: the sweep's launch
         out = torch.empty((side, side), dtype=dt, device="cuda")
         fn = lambda: g.generate(side, side, urng, out=out)
+    elif name in ("weibull_f64", "exponential_f64", "gamma05_f64", "normal_f64"):  # 2048x2048 f64
+        kind = {"weibull_f64": ("WEIBULL", 1.5, 1.0), "exponential_f64": ("EXPONENTIAL", 1.0, 0.0),
+                "gamma05_f64": ("GAMMA", 0.5, 1.0), "normal_f64": ("NORMAL_STD", 0.0, 0.0)}[name]
+        d, keep = er._desc(kind[0], torch.float64, kind[1], kind[2])
+        out = torch.empty((2048, 2048), dtype=torch.float64, device="cuda")
+        fn = lambda: er._lib.check(er._L.gr_sample(urng._h, er.ctypes.byref(d), er._ptr(out), out.numel(),
+                                                   er._stream_ptr()))
     elif name == "poisson4":
         g = er.PoissonGen(4.0)
         out = torch.empty((2048, 2048), dtype=torch.int32, device="cuda")

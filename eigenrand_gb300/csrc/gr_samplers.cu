@@ -1484,7 +1484,7 @@ __device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j
 }  // namespace
 
 template <int DT>  // SD_F32 or SD_F64
-__global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, int64_t max_blocks) {
+__global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks) {
   constexpr int P = beta_lanes<DT>();
   constexpr int LB = beta_lb<DT>();
   using V = typename std::conditional<DT == SD_F64, uint64_t, uint32_t>::type;
@@ -1576,6 +1576,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
   const int rej0 = type0 >= 2 ? 0 : 1;  // first rejection component
 
   int64_t s = 0, E = 0, done_pos = 0;  // walk state (thread 0 reads / writes s and E)
+  int sr = 0;                           // s mod kBetaRing
   int fc[2] = {0, 0};
   if (tid == 0) {
     fc[0] = s_fc[0];
@@ -1645,7 +1646,13 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
             break;
           }
           int64_t x = s;
+          int xr = sr;  // x mod kBetaRing, advanced with x
           bool full_bc = false;
+          auto adv = [&](int U) {
+            x += U;
+            xr += U;
+            if (xr >= kBetaRing) xr -= kBetaRing;
+          };
           // one component of output record nrec: 0 done, 1 partial-trial
           // buffer full, 2 positions not evaluated yet (component index a
           // compile-time constant, so the walk state stays in registers)
@@ -1655,18 +1662,18 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
             if (ty <= 1) {
               if (x + U > pk_end) return 2;
               rec[nrec * 2 + c] = x;
-              x += U;
+              adv(U);
               return 0;
             }
             for (;;) {
               if (x >= done_pos) return 2;
               if (np[c] >= kBetaPT) return 1;
-              const uint32_t m = pmask[c * kBetaRing + (int)(x % kBetaRing)];
+              const uint32_t m = pmask[c * kBetaRing + xr];
               const int cn = __popc(m);
               if (cn == P) {
                 rec[nrec * 2 + c] = x;
                 if (c == bc) full_bc = true;
-                x += U;
+                adv(U);
                 return 0;
               }
               ptx[c * kBetaPT + np[c]] = x;
@@ -1675,7 +1682,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
               ++np[c];
               A[c] += cn;
               fc[c] += cn;
-              x += U;
+              adv(U);
               if (fc[c] >= P) {
                 rec[nrec * 2 + c] = -(int64_t)(1 + (A[c] - fc[c]));
                 fc[c] -= P;
@@ -1704,6 +1711,7 @@ __global__ void __launch_bounds__(kBetaThreads) k_beta(Plan p, BetaConsts bk, in
           if (full_bc) fr[nf++] = (uint16_t)nrec;
           ++nrec;
           s = x;
+          sr = xr;
           ++E;
         }
         s_nrec = nrec;
