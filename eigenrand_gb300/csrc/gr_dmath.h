@@ -86,6 +86,53 @@ GRD_HD int64_t grd_mulhi(int64_t a, int64_t b) {
 
 GRD_HD grd_u128 grd_u128_of(uint64_t hi, uint64_t lo) { return ((grd_u128)hi << 64) | lo; }
 
+GRD_HD uint64_t grd_umulhi(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((grd_u128)a * b) >> 64);
+#endif
+}
+
+// k (hi:lo) for a small signed k (|k| < 2^20), modulo 2^128: two 64-bit
+// products instead of a general 128-bit one
+GRD_HD grd_i128 grd_mul_small(int64_t k, uint64_t hi, uint64_t lo) {
+  const uint64_t a = (uint64_t)(k < 0 ? -k : k);
+  const uint64_t rl = a * lo;
+  const uint64_t rh = grd_umulhi(a, lo) + a * hi;
+  const grd_u128 r = grd_u128_of(rh, rl);
+  return k < 0 ? -(grd_i128)r : (grd_i128)r;
+}
+
+// Round a normalized magnitude h:l (leading bit at 127) to 53 bits, nearest
+// even, with binary exponent E of the leading bit; E within the normal range.
+GRD_HD double grd_round_norm(uint64_t h, uint64_t l, int E, int neg) {
+  uint64_t sig = h >> 11;  // 53 bits
+  const uint64_t rest = h & 0x7ffull;
+  if ((rest > 0x400ull) || (rest == 0x400ull && (l != 0 || (sig & 1)))) ++sig;
+  if (sig >> 53) {
+    sig >>= 1;
+    ++E;
+  }
+  if (E > 1023) return grd_double(((uint64_t)neg << 63) | 0x7ff0000000000000ull);
+  return grd_double(((uint64_t)neg << 63) | ((uint64_t)(E + 1023) << 52) | (sig & 0xfffffffffffffull));
+}
+
+// leading-bit normalization of A > 0: h:l = A << lz, returns lz
+GRD_HD int grd_normalize(grd_u128 A, uint64_t& h, uint64_t& l) {
+  const uint64_t hi = (uint64_t)(A >> 64), lo = (uint64_t)A;
+  if (hi) {
+    const int lz = grd_clz64(hi);
+    h = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    l = lo << lz;
+    return lz;
+  }
+  const int lz = grd_clz64(lo);
+  h = lo << lz;
+  l = 0;
+  return 64 + lz;
+}
+
 // A 2^-q rounded to nearest even (A > 0), with the sign bit `neg`; results
 // below the normal range round once to a subnormal, above it to infinity.
 GRD_HD double grd_round(grd_u128 A, int q, int neg) {
@@ -148,14 +195,15 @@ GRD_HD double grd_log(double x) {
   s = GRT_ILOG_S3 + (grd_mulhi(s, r) >> 12);
   s = GRT_ILOG_S4 + (grd_mulhi(s, r) >> 12);
   // e ln2 + L1_i + L2_j + r2 S(r2), Q116
-  const grd_u128 ln2 = grd_u128_of(GRT_ILOG_LN2_HI, GRT_ILOG_LN2_LO);
-  grd_i128 v = (grd_i128)e * (grd_i128)ln2;
+  grd_i128 v = grd_mul_small(e, GRT_ILOG_LN2_HI, GRT_ILOG_LN2_LO);
   v += (grd_i128)grd_u128_of(GRD_LD(GRT_ILOG_L1[2 * i]), GRD_LD(GRT_ILOG_L1[2 * i + 1]));
   v += (grd_i128)grd_u128_of(GRD_LD(GRT_ILOG_L2[2 * j]), GRD_LD(GRT_ILOG_L2[2 * j + 1]));
   v += ((grd_i128)r * s) >> 22;  // Q138 -> Q116
   if (v == 0) return 0.0;
   const int neg = v < 0;
-  return grd_round(neg ? (grd_u128)(-v) : (grd_u128)v, 116, neg);
+  uint64_t h, l;
+  const int lz = grd_normalize(neg ? (grd_u128)(-v) : (grd_u128)v, h, l);
+  return grd_round_norm(h, l, 127 - lz - 116, neg);  // |log x| is within [2^-53, 745]: normal
 }
 
 GRD_HD double grd_exp(double x) {
@@ -175,8 +223,7 @@ GRD_HD double grd_exp(double x) {
   // n = round(64 x / ln2) from x in Q20 (floor) times 64/ln2 in Q20
   const int64_t xq = (int64_t)(xv >> 80);
   const int64_t n = (xq * GRT_IEXP_INVL + (1ll << 39)) >> 40;
-  const grd_u128 l64 = grd_u128_of(GRT_IEXP_LN2_64_HI, GRT_IEXP_LN2_64_LO);
-  const grd_i128 rv = xv - (grd_i128)n * (grd_i128)l64;  // Q100
+  const grd_i128 rv = xv - grd_mul_small(n, GRT_IEXP_LN2_64_HI, GRT_IEXP_LN2_64_LO);  // Q100
   const int64_t r = (int64_t)(rv >> 36);                              // Q64
   int64_t c = GRT_IEXP_C0;  // Q62 x Q64 >> 64 is Q62
   c = GRT_IEXP_C1 + grd_mulhi(c, r);
@@ -188,8 +235,14 @@ GRD_HD double grd_exp(double x) {
   c = GRT_IEXP_C7 + grd_mulhi(c, r);  // exp(r) in Q62
   const int jj = (int)(n & 63);
   const int m = (int)(n >> 6);
-  const grd_u128 P = (grd_u128)GRD_LD(GRT_IEXP_T[jj]) * (uint64_t)c;  // Q125
-  return grd_round(P, 125 - m, 0);
+  const grd_u128 P = (grd_u128)GRD_LD(GRT_IEXP_T[jj]) * (uint64_t)c;  // Q125, in [2^124, 2^126)
+  const int top = (int)(P >> 125);                                   // leading bit at 125 or 124
+  const int E = m + top - 1;
+  if (E < -1022) return grd_round(P, 125 - m, 0);                    // subnormal result
+  const uint64_t hi = (uint64_t)(P >> 64), lo = (uint64_t)P;
+  const uint64_t h = top ? (hi << 2) | (lo >> 62) : (hi << 3) | (lo >> 61);
+  const uint64_t l = top ? lo << 2 : lo << 3;
+  return grd_round_norm(h, l, E, 0);
 }
 
 }  // namespace gr

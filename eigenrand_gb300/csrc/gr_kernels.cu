@@ -274,7 +274,7 @@ __device__ __forceinline__ void st16(void* p, uint32_t a, uint32_t b, uint32_t c
 }
 
 template <int MODE, int KIND>
-__global__ void __launch_bounds__(160) k_direct(Plan p, DistParams d, const CallSnap* snap) {
+__global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* snap) {
   __shared__ uint64_t raw[2][kLanes][kN];
   const int k = blockIdx.x / p.S, s = blockIdx.x % p.S;
   const int tid = threadIdx.x;

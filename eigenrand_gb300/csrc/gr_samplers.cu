@@ -424,7 +424,7 @@ __device__ __forceinline__ bool rej_trial(const DistParams& d, int64_t t, int j,
 }
 
 template <int RK, int DT>  // DT: SD_F32 (P=8), SD_F64 (P=4), SD_I32H (P=4, float internals)
-__global__ void __launch_bounds__(kRejThreads) k_reject(Plan p, DistParams d, int64_t max_blocks) {
+__global__ void __maxnreg__(64) k_reject(Plan p, DistParams d, int64_t max_blocks) {
   constexpr int P = DT == SD_F32 ? 8 : 4;
   constexpr bool kWide = DT == SD_F64;  // candidates are 64-bit
   constexpr int Wt = (RK == RK_GAMMA_GS) ? 3 * 8 : (RK == RK_POISSON || RK == RK_BINOMIAL) ? 8 : 2 * 8;
