@@ -79,4 +79,43 @@ GR_HD uint64_t mt_untemper64(uint64_t y) {
   return x;
 }
 
+// Inverse of one MT19937-64 block twist (PacketRandomEngine.h:340-404): from
+// the 312 words nw of a block recover the 312 words of the block before.
+// nw[i] = c_i ^ f(y_i) with y_i = (old[i] & upper) | (old[i + 1] & lower)
+// (old[312] read as nw[0]), c_i = old[i + 156] below 156 and nw[i - 156]
+// from 156 on, and f(y) = (y >> 1) ^ (y & 1 ? MATRIX_A : 0); since the top
+// bit of MATRIX_A is set, the top bit of f(y) is y & 1, so f inverts.  The
+// y_i of the upper half come from nw alone, those of the lower half from the
+// recovered upper half, and old[0]'s lower bits from the twist that made
+// old[311] (old[311] = old[155] ^ f((older & upper) | (old[0] & lower))).
+// `idx` gives the element of a lane window (stride for lane-major layouts).
+GR_HD uint64_t mt_finv(uint64_t t) {
+  const uint64_t b = t >> 63;
+  return ((t ^ (b ? 0xb5026f5aa96619e9ull : 0ull)) << 1) | b;
+}
+template <class NW, class OLD>
+GR_HD void mt_untwist_block(NW&& nw, OLD&& old) {
+  constexpr uint64_t U = 0x8000000000000000ull, L = 0x7fffffffffffffffull;
+  // upper half: y_i for i in [156, 312) from nw only
+  for (int i = 156; i < 312; ++i) {
+    const uint64_t y = mt_finv(nw(i) ^ nw(i - 156));
+    const uint64_t hi = y & U;
+    old(i) = hi | (i > 156 ? (old(i) & L) : 0);  // lower bits of old[i] come from y_(i-1)
+    if (i + 1 < 312) old(i + 1) = (old(i + 1) & U) | (y & L);
+  }
+  // y_155 = (old[155] & U) | (old[156] & L): nw[155] = old[311] ^ f(y_155)
+  {
+    const uint64_t y = mt_finv(nw(155) ^ old(311));
+    old(156) = (old(156) & U) | (y & L);
+    old(155) = y & U;
+  }
+  for (int i = 154; i >= 0; --i) {
+    const uint64_t y = mt_finv(nw(i) ^ old(i + 156));
+    old(i + 1) = (old(i + 1) & U) | (y & L);
+    old(i) = y & U;
+  }
+  // lower bits of old[0]: old[311] = old[155] ^ f((older & U) | (old[0] & L))
+  old(0) = (old(0) & U) | (mt_finv(old(311) ^ old(155)) & L);
+}
+
 }  // namespace gr

@@ -1345,7 +1345,7 @@ static cudaError_t run_poisson(const Plan& p, const DistParams& d, int64_t max_b
 namespace {
 
 constexpr int kBetaThreads = 160;
-constexpr int kBetaRing = 640;              // positions whose masks are kept
+constexpr int kBetaRing = 1024;             // positions whose masks are kept (a power of two)
 constexpr int kBetaRec = 160;               // output packets per walk step
 constexpr int kBetaPT = 128;                // partial trials per component per walk step
 
@@ -1519,7 +1519,7 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
   // the component whose full-trial values are computed ahead of the outputs
   // (a rejection one); the other is computed where its output is written
   const int bc = type0 >= 2 ? 0 : (type1 >= 2 ? 1 : -1);
-  load_window(raw[0], &st->win[0][0], kN);
+  load_window(raw[2], &st->win[0][0], kN);  // block -1; block b lives in window b mod 3
   // carried lanes of the two GammaGens (generator slots 1 and 2)
   if (tid < 2 * 8) {
     const int c = tid / 8, j = tid % 8;
@@ -1535,16 +1535,26 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
     s_fc[1] = gs->s[2].rest_cnt;
   }
   __syncthreads();
-  // The newest two raw blocks are the ring of packets; words are tempered
-  // where they are read.
-  int64_t ring_new = 0;  // first packet of the newest block
-  int wn = 0, wp = 0;    // raw windows of the newest block and of the one before
+  // The newest three raw blocks are the ring of packets; words are tempered
+  // where they are read.  Each thread keeps its own view of the newest block.
+  int64_t ring_new = 0;         // first packet of the newest block
+  int wb0 = 0, wb1 = 2, wb2 = 1;  // windows of the newest block and the two before
+  auto set_ring = [&](int64_t B) {
+    ring_new = B * kN;
+    wb0 = (int)(B % 3);
+    wb1 = (int)((B + 2) % 3);
+    wb2 = (int)((B + 1) % 3);
+  };
   auto tword = [&](int64_t rel, int l) -> uint64_t {
     int dd = (int)(rel - ring_new);
-    int w = wn;
+    int w = wb0;
     if (dd < 0) {
       dd += kN;
-      w = wp;
+      w = wb1;
+      if (dd < 0) {
+        dd += kN;
+        w = wb2;
+      }
     }
     if ((unsigned)dd >= (unsigned)kN) dd = 0;  // outside the ring: never read past the buffers
     return mt_temper(raw[w][l][dd]);
@@ -1582,55 +1592,82 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
     fc[0] = s_fc[0];
     fc[1] = s_fc[1];
   }
-  int cur = 0;
-  int64_t nb = 0;
-  for (; nb < max_blocks; ++nb) {
-    const int nxt = cur == 2 ? 0 : cur + 1;
-    mt_block(raw[cur], raw[nxt], [&](int, const uint64_t*) {});
-    wp = cur;
-    cur = nxt;
-    wn = cur;
-    ring_new = nb * kN;
-    const int64_t lim = (nb + 1) * kN - umax + 1;  // positions whose packets all exist
-    if (tid == 0 && lim - s > kBetaRing) s_err = 1;
-    // ---- masks of the rejection components at positions [done_pos, lim)
+  // accept masks of the rejection components at positions [from, to), by
+  // threads t = 0 .. T-1 of whole warps
+  auto masks = [&](int64_t from, int64_t to, int t, int T) {
+    if (nrej == 0) return;
     // (32-bit index arithmetic with shifts: a 64-bit division by a runtime
     // value would run on the FP64 pipe)
-    if (nrej > 0) {
-      constexpr int LP = P == 8 ? 3 : 2;
-      const int sh = LP + nrej - 1;  // log2(nrej * P)
-      const int cnt = (int)(lim - done_pos) << sh;
-      for (int base = 0; base < cnt; base += kBetaThreads) {
-        const int e = base + tid;
-        const bool valid = e < cnt;
-        bool acc = false;
-        int c = 0;
-        int64_t x = 0;
-        if (valid) {
-          const int xi = e >> sh;
-          const int ci = (e >> LP) & (nrej - 1);
-          c = nrej == 2 ? ci : rej0;
-          x = done_pos + xi;
-          const int j = e & (P - 1);
-          int f = -1;
-          if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)  // float pre-test of a double GS trial
-            f = c == 0 ? gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[0].f_px,
-                                       bk.c[0].f_inv, bk.c[0].f_am1, bk.c[0].f_band)
-                       : gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[1].f_px,
-                                       bk.c[1].f_inv, bk.c[1].f_am1, bk.c[1].f_band);
-          if (f >= 0) acc = f == 1;
-          else trial(c, x, j, acc);
-        }
-        const uint32_t bal = __ballot_sync(0xffffffffu, acc);
-        if (valid && (e % P) == 0)
-          pmask[c * kBetaRing + (int)(x % kBetaRing)] = (uint8_t)((bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1));
+    constexpr int LP = P == 8 ? 3 : 2;
+    const int sh = LP + nrej - 1;  // log2(nrej * P)
+    const int cnt = (int)(to - from) << sh;
+    for (int base = 0; base < cnt; base += T) {
+      const int e = base + t;
+      const bool valid = e < cnt;
+      bool acc = false;
+      int c = 0;
+      int64_t x = 0;
+      if (valid) {
+        const int xi = e >> sh;
+        const int ci = (e >> LP) & (nrej - 1);
+        c = nrej == 2 ? ci : rej0;
+        x = from + xi;
+        const int j = e & (P - 1);
+        int f = -1;
+        if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)  // float pre-test of a double GS trial
+          f = c == 0 ? gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[0].f_px,
+                                     bk.c[0].f_inv, bk.c[0].f_am1, bk.c[0].f_band)
+                     : gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[1].f_px,
+                                     bk.c[1].f_inv, bk.c[1].f_am1, bk.c[1].f_band);
+        if (f >= 0) acc = f == 1;
+        else trial(c, x, j, acc);
       }
+      const uint32_t bal = __ballot_sync(0xffffffffu, acc);
+      if (valid && (e % P) == 0)
+        pmask[c * kBetaRing + (int)(x & (kBetaRing - 1))] =
+            (uint8_t)((bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1));
     }
-    done_pos = max(done_pos, lim);
-    __syncthreads();
+  };
+  // block 0 and its masks (all threads); afterwards warps 1-4 make block b+1
+  // and its masks while thread 0 walks block b
+  mt_block(raw[2], raw[0], [&](int, const uint64_t*) {});
+  set_ring(0);
+  masks(0, kN - umax + 1, tid, kBetaThreads);
+  done_pos = kN - umax + 1;
+  int64_t nblk = 1;             // blocks generated
+  int64_t pk_avail = kN;        // packets generated
+  __syncthreads();
+  int64_t nb = 0;
+  for (;; ++nb) {
+    const bool gen = nb + 1 < max_blocks;
+    const int64_t lim_next = (nb + 2) * kN - umax + 1;
+    if (tid == 0 && gen && lim_next - s > kBetaRing) s_err = 1;  // masks would overwrite unwalked positions
+    bool first = true;
     // walk, then values, then outputs, until the evaluated positions are used
     // up (a walk step stops early when its record buffers fill)
     for (;;) {
+      if (first && gen && tid >= 32) {
+        // ---- warps 1-4: the next block (twist by 128 threads, named barrier
+        // 1) and its masks, while thread 0 walks
+        const int tt = tid - 32;
+        uint64_t(*old)[kN] = raw[nb % 3];
+        uint64_t(*nw)[kN] = raw[(nb + 1) % 3];
+#pragma unroll 1
+        for (int ph = 0; ph < 2; ++ph) {
+          for (int ii = tt; ii < kM; ii += kBetaThreads - 32) {
+            const int i = ph * kM + ii;
+#pragma unroll
+            for (int l = 0; l < kLanes; ++l) {
+              const uint64_t bb = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
+              const uint64_t cc2 = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
+              nw[l][i] = mt_twist(old[l][i], bb, cc2);
+            }
+          }
+          asm volatile("bar.sync 1, %0;" ::"r"(kBetaThreads - 32) : "memory");
+        }
+        set_ring(nb + 1);
+        masks(done_pos, lim_next, tt, kBetaThreads - 32);
+      }
       // ---- walk (thread 0): sources of the next output packets
       if (tid == 0) {
         s_ebase = E;
@@ -1638,8 +1675,8 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
         s_A0[0] = fc[0];
         s_A0[1] = fc[1];
         int nrec = 0, nf = 0, np[2] = {0, 0}, A[2] = {fc[0], fc[1]};
-        const int64_t pk_end = (nb + 1) * kN;  // packets generated so far
-        if (s < nb * kN - kN) s_err = 1;       // packets before s left the ring
+        const int64_t pk_end = pk_avail;       // packets generated so far
+        if (s < (nb - 1) * kN) s_err = 1;      // packets before s left the ring
         while (E < Npk) {
           if (nrec >= kBetaRec) {
             s_more = 1;
@@ -1728,6 +1765,17 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
         }
       }
       __syncthreads();
+      if (first) {  // block nb + 1 and its masks are ready
+        first = false;
+        if (gen) {
+          set_ring(nb + 1);
+          done_pos = lim_next;
+          nblk = nb + 2;
+          pk_avail = (nb + 2) * kN;
+        } else {
+          set_ring(nb);
+        }
+      }
       // ---- accepted lanes of the partial trials, listed by their FIFO slot
       const int np0 = s_np[0], np1 = s_np[1];
       const int a00 = s_A0[0], a01 = s_A0[1];
@@ -1789,7 +1837,7 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
       __syncthreads();
       if (!s_more || s_stop || s_err) break;
     }
-    if (s_stop || s_err) break;
+    if (s_stop || s_err || !gen) break;
   }
 
   // ---- state after the call
@@ -1800,13 +1848,26 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
   __syncthreads();
   const int64_t np = s_end;  // packets consumed
   if (np > 0) {
-    const int64_t nblk = min(nb + 1, max_blocks);  // blocks generated
+    const int64_t B = nblk - 1;          // newest block; windows hold B, B - 1, B - 2
     const int64_t lastb = (np - 1) / kN;
-    const int prv = cur == 0 ? 2 : cur - 1, prv2 = prv == 0 ? 2 : prv - 1;
-    const int64_t rr = np - lastb * kN;  // in [1, 312]
-    if (lastb == nblk - 1) store_window(st, raw[cur], raw[prv], (int)rr);
-    else if (lastb == nblk - 2) store_window(st, raw[prv], raw[prv2], (int)rr);
-    else if (tid == 0) atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+    const int rr = (int)(np - lastb * kN);  // in [1, 312]
+    if (lastb == B) {
+      store_window(st, raw[B % 3], raw[(B + 2) % 3], rr);
+    } else if (lastb == B - 1) {
+      store_window(st, raw[(B + 2) % 3], raw[(B + 1) % 3], rr);
+    } else if (lastb == B - 2 && B >= 2) {
+      // block B - 3 was overwritten by block B: recover it from block B - 2
+      // into block B's window (MT19937-64's twist inverts)
+      if (tid < kLanes) {
+        uint64_t* nwl = raw[(B + 1) % 3][tid];
+        uint64_t* odl = raw[B % 3][tid];
+        mt_untwist_block([&](int i) -> uint64_t& { return nwl[i]; }, [&](int i) -> uint64_t& { return odl[i]; });
+      }
+      __syncthreads();
+      store_window(st, raw[(B + 1) % 3], raw[B % 3], rr);
+    } else if (tid == 0) {
+      atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+    }
   }
   if (tid < 2 * 8) {
     const int c = tid / 8, j = tid % 8;

@@ -44,5 +44,41 @@ int main() {
     if (gr::mt_untemper64(gr::mt_temper64(s)) != s || gr::mt_temper64(gr::mt_untemper64(s)) != s) ++bad3;
   }
   std::printf("untemper mismatches %llu\n", bad3);
-  return bad != 0 || bad2 != 0 || bad3 != 0;
+  // untwisting a block: twist random blocks forward, then recover each
+  // previous block from the next one
+  unsigned long long bad4 = 0;
+  {
+    uint64_t st[4][312];
+    for (int b = 0; b < 4; ++b)
+      for (int i = 0; i < 312; ++i) {
+        s ^= s << 13;
+        s ^= s >> 7;
+        s ^= s << 17;
+        st[b][i] = s;
+      }
+    for (int rep = 0; rep < 200; ++rep) {
+      uint64_t old[312], nw[312], back[312];
+      for (int i = 0; i < 312; ++i) old[i] = st[rep % 4][(i + rep) % 312] ^ (uint64_t)rep * 0x9e3779b97f4a7c15ull;
+      auto f = [](uint64_t y) { return (y >> 1) ^ ((y & 1) ? 0xb5026f5aa96619e9ull : 0ull); };
+      for (int i = 0; i < 312; ++i) {
+        const uint64_t nxt = i + 1 < 312 ? old[i + 1] : nw[0];
+        const uint64_t y = (old[i] & 0x8000000000000000ull) | (nxt & 0x7fffffffffffffffull);
+        nw[i] = (i < 156 ? old[i + 156] : nw[i - 156]) ^ f(y);
+      }
+      // old[0]'s lower bits only matter through old[311] = old[155] ^ f(...):
+      // make the pair consistent, as any block produced by a twist is
+      const uint64_t y311 = (0ull) | (old[0] & 0x7fffffffffffffffull);
+      old[311] = old[155] ^ f(y311);
+      for (int i = 0; i < 312; ++i) {
+        const uint64_t nxt = i + 1 < 312 ? old[i + 1] : nw[0];
+        const uint64_t y = (old[i] & 0x8000000000000000ull) | (nxt & 0x7fffffffffffffffull);
+        nw[i] = (i < 156 ? old[i + 156] : nw[i - 156]) ^ f(y);
+      }
+      for (int i = 0; i < 312; ++i) back[i] = 0x5555555555555555ull;
+      gr::mt_untwist_block([&](int i) -> uint64_t& { return nw[i]; }, [&](int i) -> uint64_t& { return back[i]; });
+      for (int i = 0; i < 312; ++i) bad4 += back[i] != old[i];
+    }
+  }
+  std::printf("untwist mismatches %llu\n", bad4);
+  return bad != 0 || bad2 != 0 || bad3 != 0 || bad4 != 0;
 }

@@ -15,3 +15,4 @@ def test_exact_integer_forms(tmp_path):
     assert "mismatches 0 of 2^31" in r.stdout
     assert "one_minus_ur_d mismatches 0 of" in r.stdout
     assert "untemper mismatches 0" in r.stdout
+    assert "untwist mismatches 0" in r.stdout
