@@ -728,6 +728,10 @@ def run_case(args):
         out = torch.empty((2048, 2048), dtype=torch.float64, device="cuda")
         fn = lambda: er._lib.check(er._L.gr_sample(urng._h, er.ctypes.byref(d), er._ptr(out), out.numel(),
                                                    er._stream_ptr()))
+    elif name == "binomial20":
+        g = er.BinomialGen(20, 0.3)
+        out = torch.empty((2048, 2048), dtype=torch.int32, device="cuda")
+        fn = lambda: g.generate(2048, 2048, urng, out=out)
     elif name == "poisson4":
         g = er.PoissonGen(4.0)
         out = torch.empty((2048, 2048), dtype=torch.int32, device="cuda")
