@@ -33,6 +33,8 @@ __all__ = [
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
     "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen", "BernoulliGen",
     "GeometricGen", "FisherFGen", "UniformIntGen", "NegativeBinomialGen",
+    "Support", "support", "TruncGen", "TruncNormalGen", "truncated", "truncatedLike", "truncatedNormal",
+    "truncatedNormalLike",
     "sample_batched",
     "MvNormalGen", "WishartGen", "InvWishartGen", "DirichletGen", "MultinomialGen", "makeMvNormalGen",
     "makeMvNormalGenFromLt", "makeWishartGen", "makeWishartGenFromLt", "makeInvWishartGen",
@@ -447,6 +449,104 @@ def negativeBinomial(rows, cols, urng, trials=1, p=0.5, out=None, stream=None):
 
 def geometric(rows, cols, urng, p=0.5, out=None, stream=None):
     return _sample("GEOMETRIC", rows, cols, urng, torch.int32, p, out=out, stream=stream)
+
+
+# ---- truncated distributions (Dists/Truncated.h) ---------------------------
+_FINFO = {torch.float32: (-3.4028234663852886e38, 3.4028234663852886e38),
+          torch.float64: (-1.7976931348623157e308, 1.7976931348623157e308)}
+
+
+def _scalar(x, dtype):
+    """x rounded to the scalar type, as the reference's Support<Scalar> holds it."""
+    return float(torch.tensor(float(x), dtype=dtype).item())
+
+
+class Support:
+    """Support<Ty>{lower, upper} (Truncated.h:157-176)."""
+
+    def __init__(self, lower, upper):
+        self.lower = lower
+        self.upper = upper
+
+    def intersect(self, other):
+        return Support(self.lower if self.lower > other.lower else other.lower,
+                       self.upper if self.upper < other.upper else other.upper)
+
+
+def support(lower, upper):
+    """support(lower, upper) (Truncated.h:185-189)."""
+    return Support(lower, upper)
+
+
+def _trunc_args(base, sup):
+    """(base generator, support in its scalar type) after merging nested
+    TruncGens (TruncGen<TruncGen<B>>, Truncated.h:391-426)."""
+    dt = base.dtype
+    if sup is None:
+        sup = Support(*_FINFO[dt])
+    sup = Support(_scalar(sup.lower, dt), _scalar(sup.upper, dt))
+    while isinstance(base, TruncGen):
+        sup = base.support.intersect(sup)
+        base = base.base
+    return base, sup
+
+
+class TruncGen(_Gen):
+    """TruncGen<BaseGen>{base, support} (Truncated.h:202-263 and its
+    specialisations :342-964).  Bases with a closed-form CDF (normal, standard
+    normal, lognormal, exponential, Cauchy, extreme value, Weibull, the
+    uniform family) draw by inverse CDF; gamma, beta, Student t, chi-squared,
+    Fisher F and Bernoulli by CompressMask rejection over the base's packets
+    (single-stream engines; each call synchronises its stream).  The base's
+    caches start empty."""
+
+    def __init__(self, base, support=None):
+        base, sup = _trunc_args(base, support)
+        self.base = base
+        self.support = sup
+        self.dtype = base.dtype
+        self._desc, self._keep = base._desc, base._keep
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_gen_create_truncated(ctypes.byref(h), ctypes.byref(self._desc), sup.lower, sup.upper))
+        self._h = h
+
+    def getBase(self):
+        return self.base
+
+    def getSupport(self):
+        return self.support
+
+
+class TruncNormalGen(TruncGen):
+    """TruncNormalGen<T>(mean, stdev, support) (Truncated.h:276-332): inverse
+    CDF through erfinv, no rejection."""
+
+    def __init__(self, mean=0.0, stdev=1.0, support=None, dtype=torch.float32):
+        super().__init__(NormalGen(mean, stdev, dtype=dtype), support)
+
+
+def truncated(rows, cols, urng, baseGen, support, out=None, stream=None):
+    """truncated<Derived>(rows, cols, urng, baseGen, support) (Truncated.h:984-992)."""
+    base, sup = _trunc_args(baseGen, support)
+    o = _empty(rows, cols, base.dtype, out)
+    _lib.check(_L.gr_sample_truncated(urng._h, ctypes.byref(base._desc), sup.lower, sup.upper, _ptr(o),
+                                      rows * cols, _stream_ptr(stream)))
+    return o
+
+
+def truncatedLike(o, urng, baseGen, support, stream=None):
+    """truncatedLike(o, urng, baseGen, support) (Truncated.h:1008-1016)."""
+    return truncated(o.shape[0], o.shape[1], urng, baseGen, support, stream=stream)
+
+
+def truncatedNormal(rows, cols, urng, mean, stdev, support, dtype=torch.float32, out=None, stream=None):
+    """truncatedNormal<Derived>(rows, cols, urng, mean, stdev, support) (Truncated.h:1036-1045)."""
+    return truncated(rows, cols, urng, NormalGen(mean, stdev, dtype=dtype), support, out=out, stream=stream)
+
+
+def truncatedNormalLike(o, urng, mean, stdev, support, stream=None):
+    """truncatedNormalLike(o, urng, mean, stdev, support) (Truncated.h:1061-1070)."""
+    return truncatedNormal(o.shape[0], o.shape[1], urng, mean, stdev, support, dtype=o.dtype, stream=stream)
 
 
 # ---- vectorize-over-params, many sets in one launch ------------------------

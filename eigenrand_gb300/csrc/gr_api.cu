@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <random>
 #include <mutex>
@@ -107,6 +108,14 @@ struct gr_gen {
   int32_t* table = nullptr;  // prob + alias (or cdf)
   GenState* gst = nullptr;
   int gst_K = 0;
+  // TruncGen over a base without a closed-form inverse CDF (Truncated.h:
+  // 202-263): the base generator it holds, its support in the scalar type,
+  // the carried lanes of its CompressMask, and the accepted-lane counts seen
+  // so far (they size the next chunk of base packets)
+  gr_gen* trunc_base = nullptr;
+  GenSlot* trunc_carry = nullptr;
+  double trunc_lo = 0, trunc_hi = 0;
+  int64_t trunc_lanes = 0, trunc_acc = 0;
 };
 
 namespace gr {
@@ -753,6 +762,258 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
   return GR_OK;
 }
 
+// TruncGen's constructors (Truncated.h) in the scalar type T.  Bases with a
+// closed-form CDF become UniformRealGen(phi(lower), phi(upper)) followed by
+// the inverse CDF: TruncNormalGen (:293-305, also for NormalGen :353-358 and
+// StdNormalGen :793-798), lognormal (:565-575), exponential (:448-458),
+// Cauchy (:507-515), extreme value (:621-630), Weibull (:679-690); the
+// uniform family is a UniformRealGen over the intersected range (:741-751,
+// :840-845, :888-893, :936-941).  `reject` is set for every other base:
+// generic CompressMask rejection (:202-263).  std:: math in T, as the
+// reference calls it.
+template <typename T>
+gr_status trunc_setup(const gr_dist_desc& d, T lo, T hi, DistParams& p, bool& reject) {
+  reject = false;
+  if (!(lo < hi)) return fail(GR_ERR_INVALID, "truncation support needs lower < upper");
+  const T a = (T)d.a, b = (T)d.b;
+  T bias = 0, top = 0, c0 = 0, c1 = 0;
+  int kind = 0;
+  switch (d.kind) {
+    case GR_UNIFORM_REAL:
+    case GR_UNIFORM_REAL2:
+    case GR_BALANCED:
+    case GR_BALANCED2: {
+      // the base's bias and bias + slope
+      T ob = 0, os = 1;
+      if (d.kind == GR_BALANCED) ob = -1, os = 2;
+      if (d.kind == GR_UNIFORM_REAL2 || d.kind == GR_BALANCED2) ob = a, os = b - a;
+      const T mn = lo > ob ? lo : ob, mx = hi < ob + os ? hi : ob + os;
+      if (!(mn < mx)) return fail(GR_ERR_INVALID, "truncation support does not meet the base's range");
+      gr_dist_desc u{};
+      u.kind = GR_UNIFORM_REAL2;
+      u.dtype = d.dtype;
+      u.a = (double)mn;
+      u.b = (double)mx;
+      return make_params(u, p);
+    }
+    case GR_NORMAL_STD:
+    case GR_NORMAL:
+    case GR_LOGNORMAL: {
+      const T mean = d.kind == GR_NORMAL_STD ? (T)0 : a, sd = d.kind == GR_NORMAL_STD ? (T)1 : b;
+      if (!(sd > 0)) return fail(GR_ERR_INVALID, "truncated normal needs stdev > 0");
+      if (d.kind == GR_LOGNORMAL) {
+        lo = lo <= 0 ? std::numeric_limits<T>::lowest() : std::log(lo);
+        hi = std::log(hi);
+        if (!(lo < hi)) return fail(GR_ERR_INVALID, "truncation support needs lower < upper");
+      }
+      const T an = (lo - mean) / sd, bn = (hi - mean) / sd, k = (T)(1.0 / 1.4142135623730951);
+      bias = (T)0.5 * std::erfc(-an * k);
+      top = (T)0.5 * std::erfc(-bn * k);
+      c0 = sd;
+      c1 = mean;
+      kind = d.kind == GR_LOGNORMAL ? kTruncLognormalKind : kTruncNormalKind;
+      break;
+    }
+    case GR_EXPONENTIAL: {
+      const T el = lo < 0 ? (T)0 : lo;
+      bias = (T)1 - std::exp(-a * el);
+      top = (T)1 - std::exp(-a * hi);
+      c0 = (T)1 / a;
+      kind = kTruncExponentialKind;
+      break;
+    }
+    case GR_CAUCHY:
+      bias = (T)0.5 + std::atan((lo - a) / b) / (T)3.1415926535897932;
+      top = (T)0.5 + std::atan((hi - a) / b) / (T)3.1415926535897932;
+      c0 = a;
+      c1 = b;
+      kind = kTruncCauchyKind;
+      break;
+    case GR_EXTREME_VALUE:
+      bias = std::exp(-std::exp(-(lo - a) / b));
+      top = std::exp(-std::exp(-(hi - a) / b));
+      c0 = a;
+      c1 = b;
+      kind = kTruncExtremeKind;
+      break;
+    case GR_WEIBULL: {
+      const T el = lo < 0 ? (T)0 : lo;
+      bias = (T)1 - std::exp(-std::pow(el / b, a));
+      top = (T)1 - std::exp(-std::pow(hi / b, a));
+      c0 = (T)1 / a;
+      c1 = b;
+      kind = kTruncWeibullKind;
+      break;
+    }
+    case GR_GAMMA:
+    case GR_BETA:
+    case GR_STUDENT_T:
+    case GR_CHI_SQUARED:
+    case GR_FISHER_F:
+    case GR_BERNOULLI:
+      reject = true;
+      return GR_OK;
+    default:
+      return fail(GR_ERR_UNSUPPORTED, "truncation of this distribution kind is not implemented");
+  }
+  const T slope = top - bias;
+  std::memset(&p, 0, sizeof p);
+  p.kind = kind;
+  p.dtype = d.dtype;
+  p.fa = (float)slope;
+  p.fb = (float)bias;
+  p.fc = (float)c0;
+  p.fd = (float)c1;
+  p.da = (double)slope;
+  p.db = (double)bias;
+  p.dc = (double)c0;
+  p.dd = (double)c1;
+  return GR_OK;
+}
+
+// TruncGen<Base>::generate for the rejection form on a single-stream engine.
+// The base packets are drawn in chunks into HBM and filtered (gr_trunc.cu);
+// the host reads how many outputs each chunk gave.  When a chunk holds the
+// last wanted output at base packet k*, the engine and the base's caches go
+// back to their state before the chunk and the base draws exactly k* + 1
+// packets again, so both end where the reference's would.  A first call
+// draws a pilot chunk to learn the acceptance; later chunks aim just below
+// the expected need, so the redrawn tail stays small.  Synchronises the
+// stream once per chunk.
+gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s) {
+  const int dt = g->dp.dtype;
+  const int64_t P = dt == GR_F32 ? 8 : 4;
+  const size_t lb = dt == GR_F32 ? 4 : 8;
+  if (n % (size_t)P)
+    return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(P) + " (the reference packet width)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  if (e->K != 1) return fail(GR_ERR_UNSUPPORTED, "TruncGen rejection needs a single-stream engine");
+  gr_gen* b = g->trunc_base;
+  gr_status st = ensure_gen_state(b, 1);
+  if (st != GR_OK) return st;
+  if (!g->trunc_carry) {
+    GR_CUDA(cudaMalloc(&g->trunc_carry, sizeof(GenSlot)));
+    GR_CUDA(cudaMemset(g->trunc_carry, 0, sizeof(GenSlot)));
+  }
+  const int64_t need = (int64_t)(n / (size_t)P);
+  const int64_t mcap = kTruncChunkMax - 1;
+  // scratch, grown when a chunk needs more: candidates, FIFO, CTA sums,
+  // group slots, results, saved engine and base states
+  char* buf = nullptr;
+  int64_t have_m = 0;
+  auto layout = [&](int64_t m, size_t off[7]) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t r = o;
+      o += (bytes + 255) / 256 * 256;
+      return r;
+    };
+    off[0] = take((size_t)m * P * lb);
+    off[1] = take((size_t)(m + 1) * P * lb);
+    off[2] = take(sizeof(int64_t) * 2 * (size_t)((m + 255) / 256));
+    off[3] = take(sizeof(int64_t) * (size_t)(m + 1));
+    off[4] = take(sizeof(int64_t) * 8);
+    off[5] = take(sizeof(EngState));
+    off[6] = take(sizeof(GenState));
+    return o;
+  };
+  size_t off[7];
+  int64_t done = 0, drawn = 0;
+  int64_t res[6];
+  while (done < need) {
+    const int64_t rem = need - done;
+    const double q = g->trunc_lanes > 0 ? (double)g->trunc_acc / (double)g->trunc_lanes : 0.0;
+    int64_t M;
+    if (q <= 0) {
+      M = std::min<int64_t>(rem, 4096);
+    } else {
+      const double E = (double)rem / q;
+      M = E > 32768 ? (int64_t)(E * 0.98) : (int64_t)std::ceil(E * 1.25) + 64;
+    }
+    M = std::max<int64_t>(1, std::min(M, mcap));
+    drawn += M;
+    if (drawn > ((int64_t)1 << 40)) {
+      cudaFreeAsync(buf, s);
+      return fail(GR_ERR_REJECT_LIMIT, "TruncGen: the support holds almost none of the base distribution");
+    }
+    if (M > have_m) {
+      if (buf) cudaFreeAsync(buf, s);
+      buf = nullptr;
+      const int64_t m = std::min(mcap, std::max(M, have_m * 2));
+      GR_CUDA(cudaMallocAsync(&buf, layout(m, off), s));
+      have_m = m;
+    }
+    layout(have_m, off);
+    void* cand = buf + off[0];
+    int64_t* dres = reinterpret_cast<int64_t*>(buf + off[4]);
+    EngState* saved_e = reinterpret_cast<EngState*>(buf + off[5]);
+    GenState* saved_g = reinterpret_cast<GenState*>(buf + off[6]);
+    GR_CUDA(cudaMemcpyAsync(saved_e, e->st, sizeof(EngState), cudaMemcpyDeviceToDevice, s));
+    GR_CUDA(cudaMemcpyAsync(saved_g, b->gst, sizeof(GenState), cudaMemcpyDeviceToDevice, s));
+    st = run_call(e, b, b->dp, cand, (size_t)(M * P), s);
+    if (st != GR_OK) {
+      cudaFreeAsync(buf, s);
+      return st;
+    }
+    TruncFilterArgs a{};
+    a.cand = cand;
+    a.M = M;
+    a.lower = g->trunc_lo;
+    a.upper = g->trunc_hi;
+    a.carry = g->trunc_carry;
+    a.out = static_cast<char*>(out) + (size_t)done * P * lb;
+    a.cap = rem;
+    a.queue = buf + off[1];
+    a.blk = reinterpret_cast<int64_t*>(buf + off[2]);
+    a.grp = reinterpret_cast<int64_t*>(buf + off[3]);
+    a.res = dres;
+    cudaError_t err = launch_trunc_filter(dt, a, s);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(res, dres, sizeof res, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) {
+      cudaFreeAsync(buf, s);
+      return cuda_fail(err, "TruncGen filter");
+    }
+    g->trunc_lanes += M * P;
+    g->trunc_acc += res[2] * P + res[3];
+    if (res[1] < 0) {
+      done += res[0];
+      continue;
+    }
+    if (res[1] + 1 < M) {
+      // rewind to the chunk start and redraw only the base packets consumed
+      GR_CUDA(cudaMemcpyAsync(e->st, saved_e, sizeof(EngState), cudaMemcpyDeviceToDevice, s));
+      GR_CUDA(cudaMemcpyAsync(b->gst, saved_g, sizeof(GenState), cudaMemcpyDeviceToDevice, s));
+      st = run_call(e, b, b->dp, cand, (size_t)((res[1] + 1) * P), s);
+      if (st != GR_OK) {
+        cudaFreeAsync(buf, s);
+        return st;
+      }
+    }
+    done = need;
+  }
+  cudaFreeAsync(buf, s);
+  return GR_OK;
+}
+
+// TruncGen<Base>{base, Support(lower, upper)}: fills g (inverse-CDF forms in
+// g->dp; the rejection form with a base generator and carried lanes).
+gr_status make_truncated(gr_gen* g, const gr_dist_desc& base, double lower, double upper) {
+  if (base.dtype != GR_F32 && base.dtype != GR_F64)
+    return fail(GR_ERR_INVALID, "truncation needs a float or double generator");
+  bool reject = false;
+  gr_status st = base.dtype == GR_F32 ? trunc_setup<float>(base, (float)lower, (float)upper, g->dp, reject)
+                                      : trunc_setup<double>(base, lower, upper, g->dp, reject);
+  if (st != GR_OK || !reject) return st;
+  st = gr_gen_create(&g->trunc_base, &base);
+  if (st != GR_OK) return st;
+  g->dp = g->trunc_base->dp;
+  g->trunc_lo = base.dtype == GR_F32 ? (double)(float)lower : lower;
+  g->trunc_hi = base.dtype == GR_F32 ? (double)(float)upper : upper;
+  return GR_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -833,12 +1094,47 @@ gr_status gr_gen_destroy(gr_gen* g) {
   if (!g) return GR_OK;
   cudaFree(g->table);
   cudaFree(g->gst);
+  cudaFree(g->trunc_carry);
+  gr_gen_destroy(g->trunc_base);
   delete g;
   return GR_OK;
 }
 
+gr_status gr_gen_create_truncated(gr_gen** out, const gr_dist_desc* base, double lower, double upper) {
+  if (!out || !base) return fail(GR_ERR_INVALID, "NULL argument");
+  gr_gen* g = new gr_gen;
+  g->desc = *base;
+  g->desc.weights = nullptr;
+  const gr_status st = make_truncated(g, *base, lower, upper);
+  if (st != GR_OK) {
+    gr_gen_destroy(g);
+    return st;
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_sample_truncated(gr_engine* e, const gr_dist_desc* base, double lower, double upper, void* dev_out,
+                              size_t n, gr_stream_t stream) {
+  if (!e || !base) return fail(GR_ERR_INVALID, "NULL argument");
+  gr_gen tmp;
+  tmp.desc = *base;
+  gr_status st = make_truncated(&tmp, *base, lower, upper);
+  if (st == GR_OK) {
+    // the inverse-CDF forms keep no cache; the rejection form is synchronous
+    st = tmp.trunc_base ? gr_generate(&tmp, e, dev_out, n, stream)
+                        : run_call(e, nullptr, tmp.dp, dev_out, n, (cudaStream_t)stream);
+  }
+  cudaFree(tmp.trunc_carry);
+  gr_gen_destroy(tmp.trunc_base);
+  tmp.trunc_carry = nullptr;
+  tmp.trunc_base = nullptr;
+  return st;
+}
+
 gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_stream_t stream) {
   if (!g || !e) return fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (g->trunc_base) return run_trunc(e, g, dev_out, n, (cudaStream_t)stream);
   gr_status st = ensure_gen_state(g, e->K);
   if (st != GR_OK) return st;
   return run_call(e, g, g->dp, dev_out, n, (cudaStream_t)stream);

@@ -49,6 +49,15 @@ struct GenState {
 constexpr int kPrefixLen = kN + 130 * kM;
 constexpr int kRawKind = 100;  // internal kind id for the raw u64 stream
 constexpr int kBernoulliVKind = 101;  // BernoulliVGen<float>: per-element probability (DistParams::vparam)
+// Truncated.h inverse-CDF forms: u = UniformRealGen(phi(lower), phi(upper))
+// (slope fa/da, bias fb/db), then the base's inverse CDF with constants
+// fc/dc, fd/dd
+constexpr int kTruncNormalKind = 110;       // -sqrt2 erfinv(1 - 2u) * stdev(c) + mean(d)
+constexpr int kTruncLognormalKind = 111;    // exp of the above
+constexpr int kTruncExponentialKind = 112;  // -log(1 - u) * (1 / lambda)(c)
+constexpr int kTruncCauchyKind = 113;       // a(c) + b(d) tan(pi (u - 1/2))
+constexpr int kTruncExtremeKind = 114;      // a(c) - b(d) log(-log u)
+constexpr int kTruncWeibullKind = 115;      // b(d) exp(log(-log(1 - u)) (1 / a)(c))
 
 // Caches as they were when a segmented call started (written by the prefix
 // kernel, read by every segment so that the last segment may update the live

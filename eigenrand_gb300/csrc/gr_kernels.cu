@@ -168,6 +168,42 @@ __device__ __forceinline__ double ur_d(uint64_t x) {
   return u2d((x & 0xfffffffffffffull) | (1023ull << 52)) - 1.0;
 }
 
+// Truncated.h inverse-CDF forms, one lane: u is UniformRealGen(phi(lower),
+// phi(upper))'s value.  TruncNormalGen::packetOp (:322-331), lognormal
+// (:593-598), exponential (:477-484), Cauchy (:534-543), extreme value
+// (:649-656), Weibull (:709-718).
+template <int KIND>
+__device__ __forceinline__ float trunc32(float u, const DistParams& d) {
+  if (KIND == kTruncNormalKind || KIND == kTruncLognormalKind) {
+    const float x = ((float)-1.4142135623730951 * erfinvf_(1.0f - 2.0f * u)) * d.fc + d.fd;
+    return KIND == kTruncLognormalKind ? expf_(x) : x;
+  }
+  if (KIND == kTruncExponentialKind) return -logf_(1.0f - u) * d.fc;
+  if (KIND == kTruncCauchyKind) {
+    float s, c;
+    sincosf_((float)3.1415926535897932 * (u - 0.5f), s, c);
+    return d.fc + d.fd * (s / c);
+  }
+  if (KIND == kTruncExtremeKind) return d.fc - d.fd * logf_(-logf_(u));
+  return d.fd * expf_(logf_(-logf_(1.0f - u)) * d.fc);  // Weibull
+}
+
+template <int KIND>
+__device__ __forceinline__ double trunc64(double u, const DistParams& d) {
+  if (KIND == kTruncNormalKind || KIND == kTruncLognormalKind) {
+    const double x = (-1.4142135623730951 * erfinv_(1.0 - 2.0 * u)) * d.dc + d.dd;
+    return KIND == kTruncLognormalKind ? exp_(x) : x;
+  }
+  if (KIND == kTruncExponentialKind) return -log_(1.0 - u) * d.dc;
+  if (KIND == kTruncCauchyKind) {
+    double s, c;
+    sincos_(3.1415926535897932 * (u - 0.5), s, c);
+    return d.dc + d.dd * (s / c);
+  }
+  if (KIND == kTruncExtremeKind) return d.dc - d.dd * log_(-log_(u));
+  return d.dd * exp_(log_(-log_(1.0 - u)) * d.dc);
+}
+
 // float samples from one u32 word (one lane of a Packet8f), per kind.
 template <int KIND>
 __device__ __forceinline__ float tf32(uint32_t w, const DistParams& d) {
@@ -188,6 +224,7 @@ __device__ __forceinline__ float tf32(uint32_t w, const DistParams& d) {
   if (KIND == GR_EXTREME_VALUE) return d.fa - logf_(-logf_(ur_f(w) + 1.1920928955078125e-07f / 8)) * d.fb;
   // BernoulliGen<float>: the word of the lane, masked, compared signed
   if (KIND == GR_BERNOULLI) return ((int32_t)(w & 0x7fffffffu) < d.ia) ? 1.0f : 0.0f;
+  if (KIND >= kTruncNormalKind && KIND <= kTruncWeibullKind) return trunc32<KIND>(ur_f(w) * d.fa + d.fb, d);
   return 0.0f;
 }
 
@@ -216,6 +253,7 @@ __device__ __forceinline__ double tf64(uint64_t r, const DistParams& d) {
   // BernoulliGen<double>: the compare runs on the eight 32-bit words and the
   // blend reads each 64-bit element's sign, the compare of its high word
   if (KIND == GR_BERNOULLI) return ((int32_t)((uint32_t)(r >> 32) & 0x7fffffffu) < d.ia) ? 1.0 : 0.0;
+  if (KIND >= kTruncNormalKind && KIND <= kTruncWeibullKind) return trunc64<KIND>(ur_d(r) * d.da + d.db, d);
   return 0.0;
 }
 
@@ -614,6 +652,13 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
       return d.ia == 1;  // alpha == 1: beta * exponential
     case GR_BERNOULLI:
       return true;
+    case kTruncNormalKind:
+    case kTruncLognormalKind:
+    case kTruncExponentialKind:
+    case kTruncCauchyKind:
+    case kTruncExtremeKind:
+    case kTruncWeibullKind:
+      return dtype == GR_F32 || dtype == GR_F64;
     case kBernoulliVKind:
       return dtype == GR_F32;
     case GR_RANDBITS:
@@ -649,6 +694,12 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F32_CASE(GR_GAMMA)
       GR_F32_CASE(GR_BERNOULLI)
       GR_F32_CASE(kBernoulliVKind)
+      GR_F32_CASE(kTruncNormalKind)
+      GR_F32_CASE(kTruncLognormalKind)
+      GR_F32_CASE(kTruncExponentialKind)
+      GR_F32_CASE(kTruncCauchyKind)
+      GR_F32_CASE(kTruncExtremeKind)
+      GR_F32_CASE(kTruncWeibullKind)
       case GR_NORMAL_STD:
         return run_direct<M_N32, GR_NORMAL_STD>(p, d, snap, s);
       case GR_NORMAL:
@@ -669,6 +720,12 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F64_CASE(GR_EXTREME_VALUE)
       GR_F64_CASE(GR_GAMMA)
       GR_F64_CASE(GR_BERNOULLI)
+      GR_F64_CASE(kTruncNormalKind)
+      GR_F64_CASE(kTruncLognormalKind)
+      GR_F64_CASE(kTruncExponentialKind)
+      GR_F64_CASE(kTruncCauchyKind)
+      GR_F64_CASE(kTruncExtremeKind)
+      GR_F64_CASE(kTruncWeibullKind)
       case GR_BALANCED:
         return run_direct<M_W64, GR_BALANCED>(p, d, snap, s);
       case GR_BALANCED2:

@@ -106,6 +106,27 @@ cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, 
 // packets for the two GammaGens).
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s);
 
+// TruncGen's CompressMask filter over M base packets drawn into HBM
+// (gr_trunc.cu).  Writes up to `cap` output packets, updates the carried
+// lanes, and leaves in res: [0] packets emitted, [1] the base packet that
+// emitted the last wanted one (-1: the chunk ran out first), [2] full base
+// packets, [3] accepted lanes of partial base packets, [4] FIFO fill after
+// the stop packet (or the chunk), [5] carried lanes at the start.
+constexpr int64_t kTruncChunkMax = (int64_t)1 << 22;
+struct TruncFilterArgs {
+  const void* cand;  // M packets of P lanes (float bits P = 8, double bits P = 4)
+  int64_t M;
+  double lower, upper;  // the support, already in the scalar type
+  GenSlot* carry;       // rest_cnt + rest: TruncGen's carried lanes
+  void* out;            // output packets
+  int64_t cap;          // output packets wanted
+  void* queue;          // (M + 1) * P lanes
+  int64_t* blk;         // 2 * ceil(M / 256)
+  int64_t* grp;         // M + 1
+  int64_t* res;         // 6
+};
+cudaError_t launch_trunc_filter(int dtype, const TruncFilterArgs& a, cudaStream_t s);
+
 // Batched vectorize-over-params sets (gr_vop.cu).
 struct VopArgs {
   int64_t nsets;

@@ -15,6 +15,7 @@
 // sincos is EigenRand's own psincos (Cephes single-precision sin/cos with the
 // three-constant pi/4 reduction), EigenRand/MorePacketMath.h:297-491, and
 // lgamma_approx is EigenRand's plgamma_approx, MorePacketMath.h:158-170.
+// erfinv is Giles' approximation as EigenRand's perfinv evaluates it.
 #pragma once
 #include <cstdint>
 
@@ -208,6 +209,74 @@ __device__ __forceinline__ void sincos_(double x, double& s, double& c) {
   double o2 = yy + y2;
   s = u2d(d2u(o1) ^ sign_bit_sin);
   c = u2d(d2u(o2) ^ sign_bit_cos);
+}
+
+// Inverse error function: M. Giles, "Approximating the erfinv function" (GPU
+// Computing Gems, Jade Edition, 2011).  w = -log((1 - x)(1 + x)); erfinv(x) =
+// x * P(w - c) for small w, x * Q(sqrt(w) - c') for large w, with Giles'
+// published coefficients.  The evaluation follows EigenRand's packet perfinv
+// (MorePacketMath.h:499-535 float, :543-624 double): every product and sum
+// rounds on its own, and the region is picked by w < 5 (float) or w < 6.25,
+// w < 16 (double).  log is the library's own logf_/log_ above.
+static __constant__ float kErfinvFSmall[9] = {
+    2.81022636e-08f, 3.43273939e-07f, -3.5233877e-06f, -4.39150654e-06f, 0.00021858087f,
+    -0.00125372503f, -0.00417768164f, 0.246640727f, 1.50140941f};
+static __constant__ float kErfinvFLarge[9] = {
+    -0.000200214257f, 0.000100950558f, 0.00134934322f, -0.00367342844f, 0.00573950773f,
+    -0.0076224613f, 0.00943887047f, 1.00167406f, 2.83297682f};
+static __constant__ double kErfinvDSmall[23] = {
+    -3.6444120640178196996e-21, -1.685059138182016589e-19, 1.2858480715256400167e-18,
+    1.115787767802518096e-17, -1.333171662854620906e-16, 2.0972767875968561637e-17,
+    6.6376381343583238325e-15, -4.0545662729752068639e-14, -8.1519341976054721522e-14,
+    2.6335093153082322977e-12, -1.2975133253453532498e-11, -5.4154120542946279317e-11,
+    1.051212273321532285e-09, -4.1126339803469836976e-09, -2.9070369957882005086e-08,
+    4.2347877827932403518e-07, -1.3654692000834678645e-06, -1.3882523362786468719e-05,
+    0.0001867342080340571352, -0.00074070253416626697512, -0.0060336708714301490533,
+    0.24015818242558961693, 1.6536545626831027356};
+static __constant__ double kErfinvDMid[19] = {
+    2.2137376921775787049e-09, 9.0756561938885390979e-08, -2.7517406297064545428e-07,
+    1.8239629214389227755e-08, 1.5027403968909827627e-06, -4.013867526981545969e-06,
+    2.9234449089955446044e-06, 1.2475304481671778723e-05, -4.7318229009055733981e-05,
+    6.8284851459573175448e-05, 2.4031110387097893999e-05, -0.0003550375203628474796,
+    0.00095328937973738049703, -0.0016882755560235047313, 0.0024914420961078508066,
+    -0.0037512085075692412107, 0.005370914553590063617, 1.0052589676941592334,
+    3.0838856104922207635};
+static __constant__ double kErfinvDLarge[17] = {
+    -2.7109920616438573243e-11, -2.5556418169965252055e-10, 1.5076572693500548083e-09,
+    -3.7894654401267369937e-09, 7.6157012080783393804e-09, -1.4960026627149240478e-08,
+    2.9147953450901080826e-08, -6.7711997758452339498e-08, 2.2900482228026654717e-07,
+    -9.9298272942317002539e-07, 4.5260625972231537039e-06, -1.9681778105531670567e-05,
+    7.5995277030017761139e-05, -0.00021503011930044477347, -0.00013871931833623122026,
+    1.0103004648645343977, 4.8499064014085844221};
+
+template <int N>
+__device__ __forceinline__ float horner_f(const float (&c)[N], float t) {
+  float p = c[0];
+#pragma unroll
+  for (int i = 1; i < N; ++i) p = __fadd_rn(__fmul_rn(p, t), c[i]);
+  return p;
+}
+template <int N>
+__device__ __forceinline__ double horner_d(const double (&c)[N], double t) {
+  double p = c[0];
+#pragma unroll
+  for (int i = 1; i < N; ++i) p = __dadd_rn(__dmul_rn(p, t), c[i]);
+  return p;
+}
+
+__device__ __forceinline__ float erfinvf_(float x) {
+  const float w = -logf_((1.0f - x) * (1.0f + x));
+  const float p = w < 5.0f ? horner_f(kErfinvFSmall, w - 2.5f) : horner_f(kErfinvFLarge, __fsqrt_rn(w) - 3.0f);
+  return p * x;
+}
+
+__device__ __forceinline__ double erfinv_(double x) {
+  const double w = -log_((1.0 - x) * (1.0 + x));
+  double p;
+  if (w < 6.25) p = horner_d(kErfinvDSmall, w - 3.125);
+  else if (w < 16.0) p = horner_d(kErfinvDMid, __dsqrt_rn(w) - 3.25);
+  else p = horner_d(kErfinvDLarge, __dsqrt_rn(w) - 5.0);
+  return p * x;
 }
 
 __device__ __forceinline__ float lgamma_approxf_(float x) {

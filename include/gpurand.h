@@ -165,6 +165,29 @@ gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* batch, gr_stream_
 gr_status gr_sample_v(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, void* dev_out, size_t n,
                       gr_stream_t stream);
 
+/* ---- truncated distributions (EigenRand/Dists/Truncated.h) --------------
+ * TruncGen<Base>{base, Support(lower, upper)} (Truncated.h:202-263 and the
+ * specialisations :342-964); `base` describes the base generator as for
+ * gr_gen_create (a fresh one: its caches start empty), lower / upper are the
+ * support and are converted to the base's scalar type first (pass that type's
+ * lowest() / max() for an open side, as the reference's default does).
+ *   inverse CDF, no rejection: GR_NORMAL_STD, GR_NORMAL (TruncNormalGen,
+ *     :276-332), GR_LOGNORMAL, GR_EXPONENTIAL, GR_CAUCHY, GR_EXTREME_VALUE,
+ *     GR_WEIBULL, and the uniform family (GR_UNIFORM_REAL[2],
+ *     GR_BALANCED[2]: a UniformRealGen over the intersected range);
+ *   CompressMask rejection over the base's packets: GR_GAMMA, GR_BETA,
+ *     GR_STUDENT_T, GR_CHI_SQUARED, GR_FISHER_F, GR_BERNOULLI (float/double).
+ *     This form needs a single-stream engine and synchronises the stream
+ *     (it reads back how far each chunk of base packets got).
+ * Nesting (TruncGen<TruncGen<B>>, :391-426) is the intersection of the
+ * supports over the same base.  lower >= upper (or a support that misses the
+ * base's range) is GR_ERR_INVALID. */
+gr_status gr_gen_create_truncated(gr_gen** out, const gr_dist_desc* base, double lower, double upper);
+/* truncated(rows, cols, urng, base, support) / truncatedNormal(...)
+ * (Truncated.h:984-1045): a fresh TruncGen for one call. */
+gr_status gr_sample_truncated(gr_engine* e, const gr_dist_desc* base, double lower, double upper, void* dev_out,
+                              size_t n, gr_stream_t stream);
+
 /* ---- multivariate generators (EigenRand/MvDists) -------------------------
  * Each object mirrors one Mv*Gen instance: its parameters, the FP64 factor of
  * its covariance / scale matrix (computed on the GPU at creation), and the

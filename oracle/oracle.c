@@ -665,6 +665,277 @@ int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, v
 }
 
 /* ======================================================================
+ * Truncated family, Truncated.h.  A base with a closed-form CDF becomes
+ * UniformRealGen(phi(lower), phi(upper)) pushed through its inverse CDF; the
+ * constants are the constructors' own, in the scalar type, with the C
+ * library's erfc / exp / atan / pow / log as std:: calls them.  Every other
+ * base goes through TruncGen's CompressMask rejection over the base's own
+ * packets (:247-262), its carried lanes in g[3].
+ * ====================================================================== */
+enum { TR_UNIFORM, TR_NORMAL, TR_LOGNORMAL, TR_EXPONENTIAL, TR_CAUCHY, TR_EXTREME, TR_WEIBULL, TR_REJECT };
+
+typedef struct {
+  int form;
+  double bias, slope; /* UniformRealGen(phi_lower, phi_upper) */
+  double c0, c1;      /* the inverse CDF's constants */
+} or_trunc;
+
+/* The constructors of Truncated.h:293-305 (TruncNormalGen), :448-458
+ * (exponential), :507-515 (Cauchy), :565-575 (lognormal), :621-630 (extreme
+ * value), :679-690 (Weibull), :741-751, :840-845, :888-893, :936-941
+ * (uniform family), in float.  Returns 0, or 4 for an empty support. */
+static int trunc_setup_f(int dist, float a, float b, float lo, float hi, or_trunc* t) {
+  float bias = 0, top = 0, c0 = 0, c1 = 0;
+  if (!(lo < hi)) return 4;
+  switch (dist) {
+    case OR_UNIFORM:
+    case OR_BALANCED: {
+      const float ob = a, os = b - a; /* the base's bias and slope */
+      const float mn = lo > ob ? lo : ob, mx = hi < ob + os ? hi : ob + os;
+      if (!(mn < mx)) return 4;
+      t->form = TR_UNIFORM;
+      bias = mn;
+      top = mx;
+      break;
+    }
+    case OR_STDNORMAL:
+    case OR_NORMAL:
+    case OR_LOGNORMAL: {
+      const float mean = dist == OR_STDNORMAL ? 0.0f : a, sd = dist == OR_STDNORMAL ? 1.0f : b;
+      if (!(sd > 0)) return 4;
+      if (dist == OR_LOGNORMAL) {
+        lo = lo <= 0 ? -3.40282347e+38f : logf(lo);
+        hi = logf(hi);
+        if (!(lo < hi)) return 4;
+      }
+      const float an = (lo - mean) / sd, bn = (hi - mean) / sd, k = (float)(1.0 / 1.4142135623730951);
+      bias = 0.5f * erfcf(-an * k);
+      top = 0.5f * erfcf(-bn * k);
+      c0 = sd;
+      c1 = mean;
+      t->form = dist == OR_LOGNORMAL ? TR_LOGNORMAL : TR_NORMAL;
+      break;
+    }
+    case OR_EXPONENTIAL: {
+      const float el = lo < 0 ? 0.0f : lo;
+      bias = 1.0f - expf(-a * el);
+      top = 1.0f - expf(-a * hi);
+      c0 = 1.0f / a;
+      t->form = TR_EXPONENTIAL;
+      break;
+    }
+    case OR_CAUCHY:
+      bias = 0.5f + atanf((lo - a) / b) / (float)PI_D;
+      top = 0.5f + atanf((hi - a) / b) / (float)PI_D;
+      c0 = a;
+      c1 = b;
+      t->form = TR_CAUCHY;
+      break;
+    case OR_EXTREME:
+      bias = expf(-expf(-(lo - a) / b));
+      top = expf(-expf(-(hi - a) / b));
+      c0 = a;
+      c1 = b;
+      t->form = TR_EXTREME;
+      break;
+    case OR_WEIBULL: {
+      const float el = lo < 0 ? 0.0f : lo;
+      bias = 1.0f - expf(-powf(el / b, a));
+      top = 1.0f - expf(-powf(hi / b, a));
+      c0 = 1.0f / a;
+      c1 = b;
+      t->form = TR_WEIBULL;
+      break;
+    }
+    default:
+      t->form = TR_REJECT;
+      break;
+  }
+  t->bias = bias;
+  t->slope = (float)(top - bias);
+  t->c0 = c0;
+  t->c1 = c1;
+  return 0;
+}
+
+/* The same constructors in double. */
+static int trunc_setup_d(int dist, double a, double b, double lo, double hi, or_trunc* t) {
+  double bias = 0, top = 0, c0 = 0, c1 = 0;
+  if (!(lo < hi)) return 4;
+  switch (dist) {
+    case OR_UNIFORM:
+    case OR_BALANCED: {
+      const double ob = a, os = b - a;
+      const double mn = lo > ob ? lo : ob, mx = hi < ob + os ? hi : ob + os;
+      if (!(mn < mx)) return 4;
+      t->form = TR_UNIFORM;
+      bias = mn;
+      top = mx;
+      break;
+    }
+    case OR_STDNORMAL:
+    case OR_NORMAL:
+    case OR_LOGNORMAL: {
+      const double mean = dist == OR_STDNORMAL ? 0.0 : a, sd = dist == OR_STDNORMAL ? 1.0 : b;
+      if (!(sd > 0)) return 4;
+      if (dist == OR_LOGNORMAL) {
+        lo = lo <= 0 ? -1.7976931348623157e+308 : log(lo);
+        hi = log(hi);
+        if (!(lo < hi)) return 4;
+      }
+      const double an = (lo - mean) / sd, bn = (hi - mean) / sd, k = 1.0 / 1.4142135623730951;
+      bias = 0.5 * erfc(-an * k);
+      top = 0.5 * erfc(-bn * k);
+      c0 = sd;
+      c1 = mean;
+      t->form = dist == OR_LOGNORMAL ? TR_LOGNORMAL : TR_NORMAL;
+      break;
+    }
+    case OR_EXPONENTIAL: {
+      const double el = lo < 0 ? 0.0 : lo;
+      bias = 1.0 - exp(-a * el);
+      top = 1.0 - exp(-a * hi);
+      c0 = 1.0 / a;
+      t->form = TR_EXPONENTIAL;
+      break;
+    }
+    case OR_CAUCHY:
+      bias = 0.5 + atan((lo - a) / b) / PI_D;
+      top = 0.5 + atan((hi - a) / b) / PI_D;
+      c0 = a;
+      c1 = b;
+      t->form = TR_CAUCHY;
+      break;
+    case OR_EXTREME:
+      bias = exp(-exp(-(lo - a) / b));
+      top = exp(-exp(-(hi - a) / b));
+      c0 = a;
+      c1 = b;
+      t->form = TR_EXTREME;
+      break;
+    case OR_WEIBULL: {
+      const double el = lo < 0 ? 0.0 : lo;
+      bias = 1.0 - exp(-pow(el / b, a));
+      top = 1.0 - exp(-pow(hi / b, a));
+      c0 = 1.0 / a;
+      c1 = b;
+      t->form = TR_WEIBULL;
+      break;
+    }
+    default:
+      t->form = TR_REJECT;
+      break;
+  }
+  t->bias = bias;
+  t->slope = top - bias;
+  t->c0 = c0;
+  t->c1 = c1;
+  return 0;
+}
+
+/* One lane of an inverse-CDF form, u = UniformRealGen's value. */
+static float trunc_lane_f(const or_trunc* t, float u) {
+  const float c0 = (float)t->c0, c1 = (float)t->c1;
+  switch (t->form) {
+    case TR_NORMAL:
+    case TR_LOGNORMAL: { /* TruncNormalGen::packetOp, Truncated.h:322-331 */
+      const float z = (float)-1.4142135623730951 * or_erfinvf(1.0f - 2.0f * u);
+      const float x = z * c0 + c1;
+      return t->form == TR_LOGNORMAL ? or_expf(x) : x; /* :593-598 */
+    }
+    case TR_EXPONENTIAL: /* :477-484 */
+      return -or_logf(1.0f - u) * c0;
+    case TR_CAUCHY: { /* :534-543 */
+      float s, c;
+      or_sincosf((float)PI_D * (u - 0.5f), &s, &c);
+      return c0 + c1 * (s / c);
+    }
+    case TR_EXTREME: /* :649-656 */
+      return c0 - c1 * or_logf(-or_logf(u));
+    case TR_WEIBULL: /* :709-718 */
+      return c1 * or_expf(or_logf(-or_logf(1.0f - u)) * c0);
+    default:
+      return u;
+  }
+}
+
+static double trunc_lane_d(const or_trunc* t, double u) {
+  switch (t->form) {
+    case TR_NORMAL:
+    case TR_LOGNORMAL: {
+      const double z = -1.4142135623730951 * or_erfinv(1.0 - 2.0 * u);
+      const double x = z * t->c0 + t->c1;
+      return t->form == TR_LOGNORMAL ? or_exp(x) : x;
+    }
+    case TR_EXPONENTIAL:
+      return -or_log(1.0 - u) * t->c0;
+    case TR_CAUCHY: {
+      double s, c;
+      or_sincos(PI_D * (u - 0.5), &s, &c);
+      return t->c0 + t->c1 * (s / c);
+    }
+    case TR_EXTREME:
+      return t->c0 - t->c1 * or_log(-or_log(u));
+    case TR_WEIBULL:
+      return t->c1 * or_exp(or_log(-or_log(1.0 - u)) * t->c0);
+    default:
+      return u;
+  }
+}
+
+/* TruncGen<Base>{base, Support(lower, upper)}.generate: n samples.  `dist`,
+ * `a`, `b` describe the base as in or_gen_real (OR_UNIFORM / OR_BALANCED with
+ * the base's min and max).  g needs four slots: the base's caches in g[0..2]
+ * and TruncGen's carried lanes in g[3].  Returns 0, or 4 for an empty
+ * support / bad base parameter. */
+int or_gen_trunc(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, double lower, double upper,
+                 void* out, size_t n) {
+  const int dbl = dtype == 1, P = P_of(dbl);
+  if (n % (size_t)P) return 2;
+  if (e->L != 4) return 3;
+  or_trunc t;
+  const int rc = dbl ? trunc_setup_d(dist, a, b, lower, upper, &t)
+                     : trunc_setup_f(dist, (float)a, (float)b, (float)lower, (float)upper, &t);
+  if (rc) return rc;
+  float* of = (float*)out;
+  double* od = (double*)out;
+  or_gen* tg = g + 3;
+  for (size_t k = 0; k < n / (size_t)P; ++k) {
+    if (t.form == TR_REJECT) {
+      /* TruncGen::packetOp, Truncated.h:247-262 */
+      for (int it = 0;; ++it) {
+        if (it > (1 << 24)) return 5;
+        upk c;
+        int mask[8], full = 0;
+        const int r = or_gen_real(e, g, dist, dtype, a, b, dbl ? (void*)c.d : (void*)c.f, (size_t)P);
+        if (r) return r;
+        for (int j = 0; j < P; ++j) {
+          if (dbl) mask[j] = lower <= c.d[j] && c.d[j] <= upper;
+          else mask[j] = (float)lower <= c.f[j] && c.f[j] <= (float)upper;
+        }
+        tg->rest_cnt = compress_append(P, dbl, dbl ? (void*)c.d : (void*)c.f, mask, tg->rest, tg->rest_cnt, &full);
+        if (full) {
+          if (dbl) memcpy(od + k * 4, c.d, 32);
+          else memcpy(of + k * 8, c.f, 32);
+          break;
+        }
+      }
+      continue;
+    }
+    /* UniformRealGen::packetOp (Basic.h:627-635), then the form's map */
+    upk u;
+    ur_pk(e, dbl, &u);
+    if (dbl) {
+      for (int j = 0; j < 4; ++j) od[k * 4 + j] = trunc_lane_d(&t, u.d[j] * t.slope + t.bias);
+    } else {
+      const float sl = (float)t.slope, bi = (float)t.bias;
+      for (int j = 0; j < 8; ++j) of[k * 8 + j] = trunc_lane_f(&t, u.f[j] * sl + bi);
+    }
+  }
+  return 0;
+}
+
+/* ======================================================================
  * Integer generators.  int32 packets are Packet4i; their float internals are
  * Packet4f drawn through rng.half() (arch/AVX/RandUtils.h:28-31).
  * ====================================================================== */

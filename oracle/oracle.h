@@ -91,6 +91,9 @@ enum {
 };
 int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b,
                 void* out, size_t n);
+/* TruncGen<Base>{base, Support(lower, upper)} (Truncated.h); g: four slots */
+int or_gen_trunc(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, double lower, double upper,
+                 void* out, size_t n);
 
 /* int32 distributions */
 int or_gen_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out, size_t n);
@@ -135,9 +138,13 @@ void or_set_fp_math(int on);
 void or_sincosf(float x, float* s, float* c);
 void or_sincos(double x, double* s, double* c);
 float or_lgamma_approxf(float x);
+float or_erfinvf(float x);
+double or_erfinv(double x);
 double or_lgamma_approx(double x);
 void or_vec_logf(const float* x, float* y, size_t n);
 void or_vec_expf(const float* x, float* y, size_t n);
+void or_vec_erfinvf(const float* x, float* y, size_t n);
+void or_vec_erfinv(const double* x, double* y, size_t n);
 void or_vec_log(const double* x, double* y, size_t n);
 void or_vec_exp(const double* x, double* y, size_t n);
 void or_vec_sincosf(const float* x, float* s, float* c, size_t n);

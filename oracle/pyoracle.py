@@ -73,7 +73,10 @@ def lib():
         L.or_vop_set.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                  vp, sz]
         L.or_vop_set.restype = ctypes.c_int
-        for name in ("or_vec_logf", "or_vec_expf", "or_vec_log", "or_vec_exp"):
+        L.or_gen_trunc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, vp, sz]
+        L.or_gen_trunc.restype = ctypes.c_int
+        for name in ("or_vec_logf", "or_vec_expf", "or_vec_log", "or_vec_exp", "or_vec_erfinvf", "or_vec_erfinv"):
             getattr(L, name).argtypes = [vp, vp, sz]
         L.or_vec_sincosf.argtypes = [vp, vp, vp, sz]
         L.or_vec_sincos.argtypes = [vp, vp, vp, sz]
@@ -113,10 +116,11 @@ class Engine:
 
 
 class Gen:
-    """Generator caches (three slots, like a BetaGen with two GammaGens)."""
+    """Generator caches (four slots: a BetaGen with two GammaGens, and a
+    TruncGen's carried lanes over any of them)."""
 
     def __init__(self):
-        self.buf = np.zeros(3 * lib().or_gen_sizeof(), dtype=np.uint8)
+        self.buf = np.zeros(4 * lib().or_gen_sizeof(), dtype=np.uint8)
 
     @property
     def ptr(self):
@@ -172,6 +176,29 @@ def generate(eng, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0, weight
     if rc != 0:
         raise RuntimeError(f"oracle error {rc} for {kind}")
     return out
+
+
+def truncated(eng, gen, kind, n, lower, upper, dtype=np.float32, a=0.0, b=0.0):
+    """TruncGen<Base>{base, Support(lower, upper)} (Truncated.h): n samples.
+    kind names the base as in generate(); the uniform family takes the base's
+    own range in (a, b)."""
+    L = lib()
+    a, b = DEFAULT_AB.get(kind, (a, b))
+    out = np.empty(n, dtype=dtype)
+    dist = OR_BERNOULLI if kind == "BERNOULLI" else REAL[kind]
+    rc = L.or_gen_trunc(eng.h, gen.ptr, dist, 1 if dtype == np.float64 else 0, a, b, lower, upper, _p(out), n)
+    if rc != 0:
+        raise RuntimeError(f"oracle error {rc} for truncated {kind}")
+    return out
+
+
+def erfinv(x):
+    """The oracle's erfinv (Giles' approximation as EigenRand's perfinv evaluates it)."""
+    x = np.ascontiguousarray(x)
+    y = np.empty_like(x)
+    fn = lib().or_vec_erfinvf if x.dtype == np.float32 else lib().or_vec_erfinv
+    fn(_p(x), _p(y), x.size)
+    return y
 
 
 def multinomial(eng, gen, weights, trials, samples):

@@ -11,8 +11,9 @@ W5 = [1, 2, 3, 4, 5]
 CASES = {}
 
 
-def _add(name, kind, dtype, n, a=0.0, b=0.0, trials=0, weights=None, seed=1234):
-    CASES[name] = dict(kind=kind, dtype=dtype, n=n, a=a, b=b, trials=trials, weights=weights, seed=seed)
+def _add(name, kind, dtype, n, a=0.0, b=0.0, trials=0, weights=None, seed=1234, trunc=None):
+    CASES[name] = dict(kind=kind, dtype=dtype, n=n, a=a, b=b, trials=trials, weights=weights, seed=seed,
+                       trunc=trunc)
 
 
 for dt, tag, n in ((np.float32, "f32", 256), (np.float64, "f64", 128)):
@@ -50,6 +51,13 @@ _add("uniformInt_big", "UNIFORM_INT", np.int32, 256, -1000, 100000)
 _add("negbin_5_03", "NEGATIVE_BINOMIAL", np.int32, 256, 0.3, trials=5)
 _add("negbin_1_05", "NEGATIVE_BINOMIAL", np.int32, 256, 0.5, trials=1)
 _add("negbin_25_05", "NEGATIVE_BINOMIAL", np.int32, 256, 0.5, trials=25)
+# TruncGen<Base>{base, support(lower, upper)} (Truncated.h), seed 42 as in test.cpp:1094-1404
+for dt, tag, n in ((np.float32, "f32", 256), (np.float64, "f64", 128)):
+    _add(f"truncNormal_{tag}", "NORMAL", dt, n, 0.0, 1.0, seed=42, trunc=(-1.0, 1.0))
+    _add(f"truncExponential_{tag}", "EXPONENTIAL", dt, n, 1.0, seed=42, trunc=(0.5, 3.0))
+    _add(f"truncCauchy_{tag}", "CAUCHY", dt, n, 0.0, 1.0, seed=42, trunc=(-2.0, 2.0))
+    _add(f"truncWeibull_{tag}", "WEIBULL", dt, n, 2.0, 1.0, seed=42, trunc=(0.3, 1.5))
+    _add(f"truncGamma_{tag}", "GAMMA", dt, n, 2.0, 1.0, seed=42, trunc=(0.5, 5.0))
 
 
 def run_oracle(oracle, c):
@@ -57,6 +65,8 @@ def run_oracle(oracle, c):
     if c["kind"] == "RAW":
         return e.raw(c["n"] // 4)
     g = oracle.Gen()
+    if c["trunc"]:
+        return oracle.truncated(e, g, c["kind"], c["n"], c["trunc"][0], c["trunc"][1], c["dtype"], c["a"], c["b"])
     return oracle.generate(e, g, c["kind"], c["n"], c["dtype"], c["a"], c["b"], c["trials"], c["weights"])
 
 
@@ -68,6 +78,11 @@ def run_gpu(er, c):
     tdt = {np.float32: torch.float32, np.float64: torch.float64, np.int32: torch.int32}[c["dtype"]]
     d, keep = er._desc(c["kind"], tdt, c["a"], c["b"], c["trials"], c["weights"])
     o = torch.empty(c["n"], dtype=tdt, device="cuda")
+    if c["trunc"]:
+        er._lib.check(er._L.gr_sample_truncated(u._h, er.ctypes.byref(d), c["trunc"][0], c["trunc"][1], er._ptr(o),
+                                                c["n"], er._stream_ptr()))
+        torch.cuda.synchronize()
+        return o.cpu().numpy()
     er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), c["n"], er._stream_ptr()))
     torch.cuda.synchronize()
     return o.cpu().numpy()

@@ -240,3 +240,89 @@ def test_oracle_bernoulli_per_element(oracle):
     for k, pk in enumerate([0.05, 0.3, 0.5, 0.9]):
         assert abs(x[k].mean() - pk) < 5 * np.sqrt(pk * (1 - pk) / x.shape[1])
     assert not x[4].any()
+
+
+# ---------------------------------------------------------------- truncated family
+def test_oracle_erfinv_round_trip_and_accuracy(oracle):
+    """erf(erfinv(x)) ~= x to 1e-4 (float) / 1e-6 (double) at the reference's
+    points (test.cpp:1434-1454), and Giles' approximation within its
+    published accuracy over (-1, 1)."""
+    from scipy.special import erf, erfinv
+    pts = np.array([-0.9, -0.5, -0.1, 0.0, 0.1, 0.3, 0.5, 0.9])
+    for dt, tol, rel in ((np.float32, 1e-4, 4e-7), (np.float64, 1e-6, 2e-15)):
+        y = oracle.erfinv(pts.astype(dt)).astype(np.float64)
+        np.testing.assert_allclose(erf(y), pts.astype(dt), atol=tol)
+        xs = np.linspace(-1, 1, 400001)[1:-1].astype(dt)
+        got = oracle.erfinv(xs).astype(np.float64)
+        ref = erfinv(xs.astype(np.float64))
+        err = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+        assert err[ref != 0].max() < rel, err.max()
+
+
+def _trunc_mean(pdf, lo, hi):
+    from scipy import integrate
+    z = integrate.quad(pdf, lo, hi, limit=200)[0]
+    return integrate.quad(lambda x: x * pdf(x), lo, hi, limit=200)[0] / z
+
+
+TRUNC_MOMENT_CASES = [
+    ("NORMAL", 0.0, 1.0, -1.0, 2.0, lambda a, b: __import__("scipy.stats").stats.norm(a, b).pdf),
+    ("LOGNORMAL", 0.0, 1.0, 0.5, 3.0, lambda a, b: __import__("scipy.stats").stats.lognorm(b, scale=np.exp(a)).pdf),
+    ("EXPONENTIAL", 2.0, 0.0, 0.1, 1.0, lambda a, b: __import__("scipy.stats").stats.expon(scale=1 / a).pdf),
+    ("CAUCHY", 0.0, 1.0, -2.0, 2.0, lambda a, b: __import__("scipy.stats").stats.cauchy(a, b).pdf),
+    ("EXTREME_VALUE", 0.0, 1.0, -1.0, 2.0, lambda a, b: __import__("scipy.stats").stats.gumbel_r(a, b).pdf),
+    ("WEIBULL", 2.0, 1.0, 0.3, 1.5, lambda a, b: __import__("scipy.stats").stats.weibull_min(a, scale=b).pdf),
+    ("GAMMA", 2.0, 1.0, 0.5, 5.0, lambda a, b: __import__("scipy.stats").stats.gamma(a, scale=b).pdf),
+    ("BETA", 2.0, 3.0, 0.2, 0.6, lambda a, b: __import__("scipy.stats").stats.beta(a, b).pdf),
+    ("STUDENT_T", 5.0, 0.0, -1.0, 1.5, lambda a, b: __import__("scipy.stats").stats.t(a).pdf),
+    ("CHI_SQUARED", 3.0, 0.0, 1.0, 4.0, lambda a, b: __import__("scipy.stats").stats.chi2(a).pdf),
+    ("FISHER_F", 4.0, 6.0, 0.5, 2.0, lambda a, b: __import__("scipy.stats").stats.f(a, b).pdf),
+]
+
+
+@pytest.mark.parametrize("kind,a,b,lo,hi,pdf", TRUNC_MOMENT_CASES, ids=[c[0] for c in TRUNC_MOMENT_CASES])
+def test_oracle_truncated_moments(oracle, kind, a, b, lo, hi, pdf):
+    """TruncGen over each base: every value in the support and the mean of the
+    truncated density (numerical integral), float and double."""
+    for dt in (np.float32, np.float64):
+        x = oracle.truncated(oracle.Engine(42), oracle.Gen(), kind, 1 << 17, lo, hi, dt, a, b).astype(np.float64)
+        eps = 8 * float(np.finfo(dt).eps)
+        assert x.min() >= lo - eps * max(1, abs(lo)) and x.max() <= hi + eps * max(1, abs(hi))
+        m = _trunc_mean(pdf(a, b), lo, hi)
+        sd = x.std()
+        assert abs(x.mean() - m) < 5 * sd / np.sqrt(x.size), (kind, dt, x.mean(), m)
+
+
+def test_oracle_truncated_uniform_family_and_carry(oracle):
+    """The uniform family is UniformRealGen over the intersected range (the
+    same values as uniformReal(min, max)); the rejection form's carried lanes
+    make two calls equal one call of the summed size."""
+    for dt in (np.float32, np.float64):
+        x = oracle.truncated(oracle.Engine(5), oracle.Gen(), "UNIFORM_REAL2", 4096, 2.0, 8.0, dt, 0.0, 10.0)
+        y = oracle.generate(oracle.Engine(5), oracle.Gen(), "UNIFORM_REAL2", 4096, dt, 2.0, 8.0)
+        np.testing.assert_array_equal(x, y)
+        e1, g1 = oracle.Engine(9), oracle.Gen()
+        one = oracle.truncated(e1, g1, "GAMMA", 4096, 0.5, 5.0, dt, 2.0, 1.0)
+        e2, g2 = oracle.Engine(9), oracle.Gen()
+        two = np.concatenate([oracle.truncated(e2, g2, "GAMMA", n, 0.5, 5.0, dt, 2.0, 1.0) for n in (8, 4088)])
+        np.testing.assert_array_equal(one, two)
+
+
+def test_truncated_host_validation(gpulib):
+    """Host-side checks of gr_gen_create_truncated (no GPU work): empty or
+    inverted supports, non-positive stdev, integer bases; nested supports
+    intersect in the scalar type."""
+    er = gpulib
+    with pytest.raises(er.GrError):
+        er.TruncGen(er.NormalGen(0.0, 1.0), er.support(2.0, 1.0))
+    with pytest.raises(er.GrError):
+        er.TruncGen(er.UniformRealGen(0.0, 1.0), er.support(2.0, 3.0))
+    with pytest.raises(er.GrError):
+        er.TruncNormalGen(0.0, -1.0, er.support(0.0, 1.0))
+    with pytest.raises(er.GrError):
+        er.TruncGen(er.PoissonGen(3.0), er.support(0.0, 5.0))
+    t = er.TruncGen(er.TruncGen(er.GammaGen(2.0, 1.0), er.support(0.5, 5.0)), er.support(0.1, 0.7))
+    assert (t.support.lower, t.support.upper) == (0.5, float(np.float32(0.7)))
+    assert type(t.getBase()).__name__ == "GammaGen"
+    d = er.TruncGen(er.CauchyGen(0.0, 1.0))
+    assert d.support.upper == float(np.finfo(np.float32).max)
