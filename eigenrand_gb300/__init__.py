@@ -33,6 +33,8 @@ __all__ = [
     "LognormalGen", "ExponentialGen", "CauchyGen", "WeibullGen", "ExtremeValueGen", "GammaGen", "BetaGen",
     "StudentTGen", "ChiSquaredGen", "PoissonGen", "BinomialGen", "DiscreteGen", "RandbitsGen", "BernoulliGen",
     "GeometricGen", "FisherFGen", "UniformIntGen", "NegativeBinomialGen",
+    "UniformRealVGen", "BalancedVGen", "NormalVGen", "LognormalVGen", "ExponentialVGen", "StudentTVGen",
+    "WeibullVGen", "ExtremeValueVGen", "CauchyVGen", "BernoulliVGen",
     "Support", "support", "TruncGen", "TruncNormalGen", "truncated", "truncatedLike", "truncatedNormal",
     "truncatedNormalLike",
     "sample_batched",
@@ -345,45 +347,201 @@ class GeometricGen(_Gen):
         super().__init__(torch.int32, p)
 
 
+# ---- per-element generator classes (*VGen) ----------------------------------
+class _VGen:
+    """A *VGen object: generate(urng, a[, b]) draws one value per element of
+    the parameter tensors; NormalVGen / LognormalVGen keep their StdNormalGen
+    cache between calls."""
+
+    _kind = None
+    _two = True
+
+    def __init__(self, dtype=torch.float32):
+        self.dtype = dtype
+        self._desc, self._keep = _desc(self._kind, dtype)
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_gen_create(ctypes.byref(h), ctypes.byref(self._desc)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _L is not None:
+            _L.gr_gen_destroy(h)
+            self._h = None
+
+    def generate(self, urng, a, b=None, out=None, stream=None):
+        return _vform(self._kind, urng, a, b, two=self._two, gen=self, out=out, stream=stream)
+
+
+class UniformRealVGen(_VGen):
+    """UniformRealVGen<T> (Basic.h:638-666)."""
+    _kind = "UNIFORM_REAL2"
+
+
+class BalancedVGen(_VGen):
+    """BalancedVGen<T> (Basic.h:472-492)."""
+    _kind = "BALANCED2"
+
+
+class NormalVGen(_VGen):
+    """NormalVGen<T> (NormalExp.h:139-163)."""
+    _kind = "NORMAL"
+
+
+class LognormalVGen(_VGen):
+    """LognormalVGen<T> (NormalExp.h:213-236)."""
+    _kind = "LOGNORMAL"
+
+
+class ExponentialVGen(_VGen):
+    """ExponentialVGen<T> (NormalExp.h:402-427)."""
+    _kind = "EXPONENTIAL"
+    _two = False
+
+
+class StudentTVGen(_VGen):
+    """StudentTVGen<T> (NormalExp.h:305-343)."""
+    _kind = "STUDENT_T"
+    _two = False
+
+
+class WeibullVGen(_VGen):
+    """WeibullVGen<T> (NormalExp.h:659-686)."""
+    _kind = "WEIBULL"
+
+
+class ExtremeValueVGen(_VGen):
+    """ExtremeValueVGen<T> (NormalExp.h:736-765)."""
+    _kind = "EXTREME_VALUE"
+
+
+class CauchyVGen(_VGen):
+    """CauchyVGen<T> (NormalExp.h:859-889)."""
+    _kind = "CAUCHY"
+
+
+class BernoulliVGen(_VGen):
+    """BernoulliVGen<float> (Basic.h:711-747)."""
+    _kind = "BERNOULLI"
+    _two = False
+
+
 # ---- free functions (Dists/*.h tails) -----------------------------------
-def uniformReal(rows, cols, urng, min=None, max=None, dtype=torch.float32, out=None, stream=None):
+def _eigen_order(t, dtype):
+    """A parameter tensor on the device in Eigen's memory order (column-major
+    for 2-D), so that element i of memory is the reference's linear index i."""
+    t = t.to(device="cuda", dtype=dtype)
+    if t.dim() == 2:
+        return t.t().contiguous().t()
+    return t.contiguous()
+
+
+def _vform(kind, urng, a, b=None, two=True, gen=None, out=None, stream=None):
+    """The per-element forms: kind(urng, a, b) with a and / or b tensors of
+    the output's shape (*VGen, gr_sample_v2 / gr_generate_v)."""
+    ten = [x for x in (a, b) if torch.is_tensor(x)]
+    if not ten:
+        raise TypeError("the per-element form needs a parameter tensor")
+    dtype = ten[0].dtype if ten[0].dtype in (torch.float32, torch.float64) else torch.float32
+    pa = _eigen_order(a, dtype) if torch.is_tensor(a) else None
+    pb = _eigen_order(b, dtype) if torch.is_tensor(b) else None
+    if pa is not None and pb is not None and pa.shape != pb.shape:
+        raise ValueError("a and b must have the same shape")
+    ref = pa if pa is not None else pb
+    o = torch.empty_like(ref) if out is None else out
+    sa = 0.0 if pa is not None else float(a)
+    sb = 0.0 if pb is not None or not two else float(b)
+    vp = lambda t: _ptr(t) if t is not None else None
+    if gen is not None:
+        _lib.check(_L.gr_generate_v(gen._h, urng._h, vp(pa), vp(pb), _ptr(o), o.numel(), _stream_ptr(stream)))
+    else:
+        d, keep = _desc(kind, dtype, sa, sb)
+        _lib.check(_L.gr_sample_v2(urng._h, ctypes.byref(d), vp(pa), vp(pb), _ptr(o), o.numel(),
+                                   _stream_ptr(stream)))
+        del keep
+    return o
+
+
+def _is_v(args):
+    return bool(args) and isinstance(args[0], Vmt19937_64)
+
+
+def uniformReal(*args, min=None, max=None, dtype=torch.float32, out=None, stream=None):
+    """uniformReal(rows, cols, urng[, min, max]); uniformReal(urng, a, b) with
+    tensor bounds -> UniformRealVGen (Basic.h:1047-1092)."""
+    if _is_v(args):
+        return _vform("UNIFORM_REAL2", *args, out=out, stream=stream)
+    rows, cols, urng = args[:3]
+    if len(args) > 3:
+        min = args[3]
+    if len(args) > 4:
+        max = args[4]
     if min is None and max is None:
         return _sample("UNIFORM_REAL", rows, cols, urng, dtype, out=out, stream=stream)
     return _sample("UNIFORM_REAL2", rows, cols, urng, dtype, 0.0 if min is None else min,
                    1.0 if max is None else max, out=out, stream=stream)
 
 
-def balanced(rows, cols, urng, a=None, b=None, dtype=torch.float32, out=None, stream=None):
+def balanced(*args, a=None, b=None, dtype=torch.float32, out=None, stream=None):
+    """balanced(rows, cols, urng[, a, b]); balanced(urng, a, b) -> BalancedVGen (Basic.h:895-939)."""
+    if _is_v(args):
+        return _vform("BALANCED2", *args, out=out, stream=stream)
+    rows, cols, urng = args[:3]
+    if len(args) > 3:
+        a = args[3]
+    if len(args) > 4:
+        b = args[4]
     if a is None and b is None:
         return _sample("BALANCED", rows, cols, urng, dtype, out=out, stream=stream)
     return _sample("BALANCED2", rows, cols, urng, dtype, a, b, out=out, stream=stream)
 
 
-def normal(rows, cols, urng, mean=None, stdev=None, dtype=torch.float32, out=None, stream=None):
+def normal(*args, mean=None, stdev=None, dtype=torch.float32, out=None, stream=None):
+    """normal(rows, cols, urng[, mean, stdev]); normal(urng, mean, stdev) with
+    tensor operands -> NormalVGen (NormalExp.h:1296-1336)."""
+    if _is_v(args):
+        return _vform("NORMAL", *args, out=out, stream=stream)
+    rows, cols, urng = args[:3]
+    if len(args) > 3:
+        mean = args[3]
+    if len(args) > 4:
+        stdev = args[4]
     if mean is None and stdev is None:
         return _sample("NORMAL_STD", rows, cols, urng, dtype, out=out, stream=stream)
     return _sample("NORMAL", rows, cols, urng, dtype, 0.0 if mean is None else mean,
                    1.0 if stdev is None else stdev, out=out, stream=stream)
 
 
-def lognormal(rows, cols, urng, mean=0.0, stdev=1.0, dtype=torch.float32, out=None, stream=None):
-    return _sample("LOGNORMAL", rows, cols, urng, dtype, mean, stdev, out=out, stream=stream)
+def _two(kind, defaults):
+    def fn(*args, dtype=torch.float32, out=None, stream=None, **kw):
+        if _is_v(args):
+            return _vform(kind, *args, out=out, stream=stream)
+        rows, cols, urng = args[:3]
+        vals = list(args[3:]) + [kw.get(k, v) for k, v in list(defaults.items())[len(args) - 3:]]
+        return _sample(kind, rows, cols, urng, dtype, *vals[:2], out=out, stream=stream)
+    return fn
 
 
-def exponential(rows, cols, urng, lambda_=1.0, dtype=torch.float32, out=None, stream=None):
-    return _sample("EXPONENTIAL", rows, cols, urng, dtype, lambda_, out=out, stream=stream)
+def _one(kind, name, default):
+    def fn(*args, dtype=torch.float32, out=None, stream=None, **kw):
+        if _is_v(args):
+            return _vform(kind, args[0], args[1], two=False, out=out, stream=stream)
+        rows, cols, urng = args[:3]
+        v = args[3] if len(args) > 3 else kw.get(name, default)
+        return _sample(kind, rows, cols, urng, dtype, v, out=out, stream=stream)
+    return fn
 
 
-def cauchy(rows, cols, urng, a=0.0, b=1.0, dtype=torch.float32, out=None, stream=None):
-    return _sample("CAUCHY", rows, cols, urng, dtype, a, b, out=out, stream=stream)
-
-
-def weibull(rows, cols, urng, a=1.0, b=1.0, dtype=torch.float32, out=None, stream=None):
-    return _sample("WEIBULL", rows, cols, urng, dtype, a, b, out=out, stream=stream)
-
-
-def extremeValue(rows, cols, urng, a=0.0, b=1.0, dtype=torch.float32, out=None, stream=None):
-    return _sample("EXTREME_VALUE", rows, cols, urng, dtype, a, b, out=out, stream=stream)
+lognormal = _two("LOGNORMAL", {"mean": 0.0, "stdev": 1.0})
+lognormal.__doc__ = "lognormal(rows, cols, urng[, mean, stdev]); lognormal(urng, mean, stdev) -> LognormalVGen."
+exponential = _one("EXPONENTIAL", "lambda_", 1.0)
+exponential.__doc__ = "exponential(rows, cols, urng[, lambda]); exponential(urng, lambda) -> ExponentialVGen."
+cauchy = _two("CAUCHY", {"a": 0.0, "b": 1.0})
+cauchy.__doc__ = "cauchy(rows, cols, urng[, a, b]); cauchy(urng, a, b) -> CauchyVGen."
+weibull = _two("WEIBULL", {"a": 1.0, "b": 1.0})
+weibull.__doc__ = "weibull(rows, cols, urng[, a, b]); weibull(urng, a, b) -> WeibullVGen."
+extremeValue = _two("EXTREME_VALUE", {"a": 0.0, "b": 1.0})
+extremeValue.__doc__ = "extremeValue(rows, cols, urng[, a, b]); extremeValue(urng, a, b) -> ExtremeValueVGen."
 
 
 def gamma(rows, cols, urng, alpha=1.0, beta=1.0, dtype=torch.float32, out=None, stream=None):
@@ -394,8 +552,8 @@ def beta(rows, cols, urng, a=1.0, b=1.0, dtype=torch.float32, out=None, stream=N
     return _sample("BETA", rows, cols, urng, dtype, a, b, out=out, stream=stream)
 
 
-def studentT(rows, cols, urng, n=1.0, dtype=torch.float32, out=None, stream=None):
-    return _sample("STUDENT_T", rows, cols, urng, dtype, n, out=out, stream=stream)
+studentT = _one("STUDENT_T", "n", 1.0)
+studentT.__doc__ = "studentT(rows, cols, urng[, n]); studentT(urng, n) -> StudentTVGen (NormalExp.h:1512-1520)."
 
 
 def chiSquared(rows, cols, urng, n=1.0, dtype=torch.float32, out=None, stream=None):

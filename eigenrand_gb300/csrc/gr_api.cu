@@ -640,7 +640,8 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
   if (fam == Family::Direct) {
     // packets per slice, upper bound (caches can only reduce it)
     int opp = 8;
-    if (dp.kind == kRawKind || (dp.dtype == GR_F64 && dp.kind != GR_BALANCED && dp.kind != GR_BALANCED2)) opp = 4;
+    const int bk = dp.kind >= kVecBase ? dp.kind - kVecBase : dp.kind;
+    if (bk == kRawKind || (dp.dtype == GR_F64 && bk != GR_BALANCED && bk != GR_BALANCED2)) opp = 4;
     const int ppu = kind_packets_per_unit(dp.kind, dp.dtype);
     int64_t packets_max = (nk_max + opp - 1) / opp;
     if (ppu == 2) packets_max += packets_max & 1;
@@ -1268,16 +1269,76 @@ gr_status gr_sample(gr_engine* e, const gr_dist_desc* desc, void* dev_out, size_
 
 gr_status gr_sample_v(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, void* dev_out, size_t n,
                       gr_stream_t stream) {
-  if (!e || !desc || (n && (!dev_a || !dev_out))) return fail(GR_ERR_INVALID, "NULL argument");
-  if (desc->kind != GR_BERNOULLI || desc->dtype != GR_F32)
-    return fail(GR_ERR_UNSUPPORTED, "per-element parameters: BernoulliVGen<float> only");
-  if (((uintptr_t)dev_a | (uintptr_t)dev_out) % 16)
+  return gr_sample_v2(e, desc, dev_a, nullptr, dev_out, n, stream);
+}
+
+gr_status gr_sample_v2(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, const void* dev_b, void* dev_out,
+                       size_t n, gr_stream_t stream) {
+  if (!e || !desc) return fail(GR_ERR_INVALID, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  // a fresh *VGen: its StdNormalGen cache (normal, lognormal) starts empty
+  if (!e->scratch_gen) GR_CUDA(cudaMalloc(&e->scratch_gen, sizeof(GenState) * (size_t)e->K));
+  GR_CUDA(cudaMemsetAsync(e->scratch_gen, 0, sizeof(GenState) * (size_t)e->K, s));
+  gr_gen tmp;
+  tmp.desc = *desc;
+  tmp.gst = e->scratch_gen;
+  tmp.gst_K = e->K;
+  const gr_status st = gr_generate_v(&tmp, e, dev_a, dev_b, dev_out, n, stream);
+  tmp.gst = nullptr;
+  return st;
+}
+
+gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* dev_b, void* dev_out, size_t n,
+                        gr_stream_t stream) {
+  if (!g || !e || (n && !dev_out)) return fail(GR_ERR_INVALID, "NULL argument");
+  const gr_dist_desc& d = g->desc;
+  if (((uintptr_t)dev_a | (uintptr_t)dev_b | (uintptr_t)dev_out) % 16)
     return fail(GR_ERR_INVALID, "parameter and output arrays must be 16-byte aligned");
   DistParams dp{};
-  dp.kind = kBernoulliVKind;
-  dp.dtype = GR_F32;
+  if (d.kind == GR_BERNOULLI && d.dtype == GR_F32 && dev_a && !dev_b) {
+    dp.kind = kBernoulliVKind;
+    dp.dtype = GR_F32;
+    dp.vparam = dev_a;
+    return run_call(e, nullptr, dp, dev_out, n, (cudaStream_t)stream);
+  }
+  if (d.kind == GR_BERNOULLI)
+    return fail(GR_ERR_UNSUPPORTED,
+                "per-element bernoulli: BernoulliVGen<float> only (the double form goes through a cast the "
+                "reference leaves to Eigen's generic pcast)");
+  if (d.dtype != GR_F32 && d.dtype != GR_F64) return fail(GR_ERR_UNSUPPORTED, "per-element forms are float/double");
+  gr_status st = GR_OK;
+  switch (d.kind) {
+    case GR_UNIFORM_REAL2:
+    case GR_BALANCED2:
+    case GR_NORMAL:
+    case GR_LOGNORMAL:
+    case GR_WEIBULL:
+    case GR_EXTREME_VALUE:
+    case GR_CAUCHY:
+      break;
+    case GR_EXPONENTIAL:
+    case GR_STUDENT_T:
+      if (dev_b) return fail(GR_ERR_INVALID, "this per-element form takes one parameter array");
+      break;
+    default:
+      return fail(GR_ERR_UNSUPPORTED, "no per-element form for this distribution kind");
+  }
+  st = make_params(d, dp);
+  if (st != GR_OK) return st;
+  dp.flags = (dev_a ? kParamVecA : 0) | (dev_b ? kParamVecB : 0);
   dp.vparam = dev_a;
-  return run_call(e, nullptr, dp, dev_out, n, (cudaStream_t)stream);
+  dp.vparam2 = dev_b;
+  if (d.kind != GR_STUDENT_T) {
+    // direct kernels: kind kVecBase + K, scalar operands in fe/ff, de/df
+    dp.kind = kVecBase + d.kind;
+    dp.fe = (float)d.a;
+    dp.ff = (float)d.b;
+    dp.de = d.a;
+    dp.df = d.b;
+  }
+  st = ensure_gen_state(g, e->K);
+  if (st != GR_OK) return st;
+  return run_call(e, g, dp, dev_out, n, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -58,6 +58,10 @@ constexpr int kTruncExponentialKind = 112;  // -log(1 - u) * (1 / lambda)(c)
 constexpr int kTruncCauchyKind = 113;       // a(c) + b(d) tan(pi (u - 1/2))
 constexpr int kTruncExtremeKind = 114;      // a(c) - b(d) log(-log u)
 constexpr int kTruncWeibullKind = 115;      // b(d) exp(log(-log(1 - u)) (1 / a)(c))
+// Per-element forms (*VGen): kind kVecBase + K draws like K with parameters
+// a[i], b[i] of output element i (DistParams::vparam / vparam2 when the
+// kParamVecA / kParamVecB flag is set, else the scalars fe/ff, de/df)
+constexpr int kVecBase = 200;
 
 // Caches as they were when a segmented call started (written by the prefix
 // kernel, read by every segment so that the last segment may update the live

@@ -297,6 +297,79 @@ __device__ __forceinline__ double nscale64(double x, const DistParams& d) {
   return exp_(x * d.db + d.da);
 }
 
+// ---------------------------------------------------------------- per-element forms
+// The *VGen packetOp arguments of output element idx, mapped onto the
+// constants the scalar-parameter transform reads: UniformRealVGen and
+// BalancedVGen slope b - a, bias a (Basic.h:486-491, :660-665); NormalVGen and
+// LognormalVGen mean a, stdev b (NormalExp.h:155-162, :230-235);
+// ExponentialVGen lambda a (:420-426); WeibullVGen 1 / a and b (:679-685);
+// ExtremeValueVGen and CauchyVGen a, b (:757-764, :879-888).  Each is the
+// same packet arithmetic as the scalar generator with the lane's own values.
+template <int BK>
+__device__ __forceinline__ DistParams vparams32(const DistParams& d, int64_t idx) {
+  const float a = (d.flags & kParamVecA) ? __ldg(static_cast<const float*>(d.vparam) + idx) : d.fe;
+  const float b = (d.flags & kParamVecB) ? __ldg(static_cast<const float*>(d.vparam2) + idx) : d.ff;
+  DistParams e = d;
+  e.flags = 0;
+  if (BK == GR_UNIFORM_REAL2 || BK == GR_BALANCED2) {
+    e.fa = b - a;
+    e.fb = a;
+  } else if (BK == GR_WEIBULL) {
+    e.fa = 1.0f / a;
+    e.fb = b;
+  } else {
+    e.fa = a;
+    e.fb = b;
+  }
+  return e;
+}
+template <int BK>
+__device__ __forceinline__ DistParams vparams64(const DistParams& d, int64_t idx) {
+  const double a = (d.flags & kParamVecA) ? __ldg(static_cast<const double*>(d.vparam) + idx) : d.de;
+  const double b = (d.flags & kParamVecB) ? __ldg(static_cast<const double*>(d.vparam2) + idx) : d.df;
+  DistParams e = d;
+  e.flags = 0;
+  if (BK == GR_UNIFORM_REAL2 || BK == GR_BALANCED2) {
+    e.da = b - a;
+    e.db = a;
+  } else if (BK == GR_WEIBULL) {
+    e.da = 1.0 / a;
+    e.db = b;
+  } else {
+    e.da = a;
+    e.db = b;
+  }
+  return e;
+}
+
+// Transforms with the output element index: a per-element kind reads its
+// parameters there, the others ignore it.
+template <int KIND>
+__device__ __forceinline__ float tf32i(uint32_t w, const DistParams& d, int64_t idx) {
+  if constexpr (KIND >= kVecBase) return tf32<KIND - kVecBase>(w, vparams32<KIND - kVecBase>(d, idx));
+  else return tf32<KIND>(w, d);
+}
+template <int KIND>
+__device__ __forceinline__ double tf64i(uint64_t r, const DistParams& d, int64_t idx) {
+  if constexpr (KIND >= kVecBase) return tf64<KIND - kVecBase>(r, vparams64<KIND - kVecBase>(d, idx));
+  else return tf64<KIND>(r, d);
+}
+template <int KIND>
+__device__ __forceinline__ double tw64i(uint32_t w, const DistParams& d, int64_t idx) {
+  if constexpr (KIND >= kVecBase) return tw64<KIND - kVecBase>(w, vparams64<KIND - kVecBase>(d, idx));
+  else return tw64<KIND>(w, d);
+}
+template <int KIND>
+__device__ __forceinline__ float nscale32i(float x, const DistParams& d, int64_t idx) {
+  if constexpr (KIND >= kVecBase) return nscale32<KIND - kVecBase>(x, vparams32<KIND - kVecBase>(d, idx));
+  else return nscale32<KIND>(x, d);
+}
+template <int KIND>
+__device__ __forceinline__ double nscale64i(double x, const DistParams& d, int64_t idx) {
+  if constexpr (KIND >= kVecBase) return nscale64<KIND - kVecBase>(x, vparams64<KIND - kVecBase>(d, idx));
+  else return nscale64<KIND>(x, d);
+}
+
 // ---------------------------------------------------------------- direct kernel
 enum Mode { M_RAW, M_F32, M_F64, M_W32, M_W64, M_N32, M_N64 };
 
@@ -353,13 +426,13 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
   // --- prefix outputs served from the cache (segment 0 only)
   if (s == 0 && tid < Q0) {
     const int i = tid;
-    if (MODE == M_W64) reinterpret_cast<double*>(p.out)[off + i] = tw64<KIND>(cwords[i], d);
+    if (MODE == M_W64) reinterpret_cast<double*>(p.out)[off + i] = tw64i<KIND>(cwords[i], d, off + i);
     if (MODE == M_W32)
       reinterpret_cast<int32_t*>(p.out)[off + i] = kHalfKind ? tw32<KIND>(cwords[i], d) : (int32_t)cwords[i];
-    if (MODE == M_N32) reinterpret_cast<float*>(p.out)[off + i] = nscale32<KIND>(u2f(cwords[i]), d);
+    if (MODE == M_N32) reinterpret_cast<float*>(p.out)[off + i] = nscale32i<KIND>(u2f(cwords[i]), d, off + i);
     if (MODE == M_N64) {
       uint64_t b = (uint64_t)cwords[2 * i] | ((uint64_t)cwords[2 * i + 1] << 32);
-      reinterpret_cast<double*>(p.out)[off + i] = nscale64<KIND>(u2d(b), d);
+      reinterpret_cast<double*>(p.out)[off + i] = nscale64i<KIND>(u2d(b), d, off + i);
     }
   }
 
@@ -426,8 +499,8 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           } else {
 #pragma unroll
             for (int l = 0; l < kLanes; ++l) {
-              v[2 * l] = tf32<KIND>((uint32_t)pk[l], d);
-              v[2 * l + 1] = tf32<KIND>((uint32_t)(pk[l] >> 32), d);
+              v[2 * l] = tf32i<KIND>((uint32_t)pk[l], d, obase + pidx * 8 + 2 * l);
+              v[2 * l + 1] = tf32i<KIND>((uint32_t)(pk[l] >> 32), d, obase + pidx * 8 + 2 * l + 1);
             }
           }
           reinterpret_cast<float4*>(o)[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -438,7 +511,7 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           double* o = reinterpret_cast<double*>(p.out) + obase + pidx * 4;
           double v[4];
 #pragma unroll
-          for (int l = 0; l < kLanes; ++l) v[l] = tf64<KIND>(pk[l], d);
+          for (int l = 0; l < kLanes; ++l) v[l] = tf64i<KIND>(pk[l], d, obase + pidx * 4 + l);
           reinterpret_cast<double2*>(o)[0] = make_double2(v[0], v[1]);
           reinterpret_cast<double2*>(o)[1] = make_double2(v[2], v[3]);
         }
@@ -469,11 +542,13 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           } else {
             double v[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) v[q] = tw64<KIND>(wd[q], d);
+            for (int q = 0; q < 4; ++q) v[q] = tw64i<KIND>(wd[q], d, ob + q);
             double* o = reinterpret_cast<double*>(p.out) + ob;
             reinterpret_cast<double2*>(o)[0] = make_double2(v[0], v[1]);
             reinterpret_cast<double2*>(o)[1] = make_double2(v[2], v[3]);
             if (full) {
+#pragma unroll
+              for (int q = 4; q < 8; ++q) v[q] = tw64i<KIND>(wd[q], d, ob + q);
               reinterpret_cast<double2*>(o)[2] = make_double2(v[4], v[5]);
               reinterpret_cast<double2*>(o)[3] = make_double2(v[6], v[7]);
             } else {
@@ -513,12 +588,12 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           const int64_t ob = obase + unit * 16;
           float* o = reinterpret_cast<float*>(p.out) + ob;
           reinterpret_cast<float4*>(o + i0)[0] =
-              make_float4(nscale32<KIND>(sv[0], d), nscale32<KIND>(sv[1], d), nscale32<KIND>(sv[2], d),
-                          nscale32<KIND>(sv[3], d));
+              make_float4(nscale32i<KIND>(sv[0], d, ob + i0), nscale32i<KIND>(sv[1], d, ob + i0 + 1),
+                          nscale32i<KIND>(sv[2], d, ob + i0 + 2), nscale32i<KIND>(sv[3], d, ob + i0 + 3));
           if (ob + 16 <= oend) {
             reinterpret_cast<float4*>(o + 8 + i0)[0] =
-                make_float4(nscale32<KIND>(cv[0], d), nscale32<KIND>(cv[1], d), nscale32<KIND>(cv[2], d),
-                            nscale32<KIND>(cv[3], d));
+                make_float4(nscale32i<KIND>(cv[0], d, ob + 8 + i0), nscale32i<KIND>(cv[1], d, ob + 9 + i0),
+                            nscale32i<KIND>(cv[2], d, ob + 10 + i0), nscale32i<KIND>(cv[3], d, ob + 11 + i0));
           } else {
 #pragma unroll
             for (int q = 0; q < 4; ++q) gs->s[0].cache[i0 + q] = f2u(cv[q]);
@@ -549,10 +624,11 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           }
           const int64_t ob = obase + unit * 8;
           double* o = reinterpret_cast<double*>(p.out) + ob;
-          reinterpret_cast<double2*>(o + i0)[0] = make_double2(nscale64<KIND>(sv[0], d), nscale64<KIND>(sv[1], d));
+          reinterpret_cast<double2*>(o + i0)[0] =
+              make_double2(nscale64i<KIND>(sv[0], d, ob + i0), nscale64i<KIND>(sv[1], d, ob + i0 + 1));
           if (ob + 8 <= oend) {
             reinterpret_cast<double2*>(o + 4 + i0)[0] =
-                make_double2(nscale64<KIND>(cv[0], d), nscale64<KIND>(cv[1], d));
+                make_double2(nscale64i<KIND>(cv[0], d, ob + 4 + i0), nscale64i<KIND>(cv[1], d, ob + 5 + i0));
           } else {
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
@@ -629,6 +705,7 @@ int kind_granule(int kind, int dtype) {
 
 int kind_packets_per_unit(int kind, int dtype) {
   (void)dtype;
+  if (kind >= kVecBase) kind -= kVecBase;
   if (kind == GR_NORMAL_STD || kind == GR_NORMAL || kind == GR_LOGNORMAL) return 2;
   return 1;
 }
@@ -661,6 +738,15 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
       return dtype == GR_F32 || dtype == GR_F64;
     case kBernoulliVKind:
       return dtype == GR_F32;
+    case kVecBase + GR_UNIFORM_REAL2:
+    case kVecBase + GR_BALANCED2:
+    case kVecBase + GR_NORMAL:
+    case kVecBase + GR_LOGNORMAL:
+    case kVecBase + GR_EXPONENTIAL:
+    case kVecBase + GR_WEIBULL:
+    case kVecBase + GR_EXTREME_VALUE:
+    case kVecBase + GR_CAUCHY:
+      return dtype == GR_F32 || dtype == GR_F64;
     case GR_RANDBITS:
     case GR_DISCRETE:
     case GR_GEOMETRIC:
@@ -700,6 +786,16 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F32_CASE(kTruncCauchyKind)
       GR_F32_CASE(kTruncExtremeKind)
       GR_F32_CASE(kTruncWeibullKind)
+      GR_F32_CASE(kVecBase + GR_UNIFORM_REAL2)
+      GR_F32_CASE(kVecBase + GR_BALANCED2)
+      GR_F32_CASE(kVecBase + GR_EXPONENTIAL)
+      GR_F32_CASE(kVecBase + GR_WEIBULL)
+      GR_F32_CASE(kVecBase + GR_EXTREME_VALUE)
+      GR_F32_CASE(kVecBase + GR_CAUCHY)
+      case kVecBase + GR_NORMAL:
+        return run_direct<M_N32, kVecBase + GR_NORMAL>(p, d, snap, s);
+      case kVecBase + GR_LOGNORMAL:
+        return run_direct<M_N32, kVecBase + GR_LOGNORMAL>(p, d, snap, s);
       case GR_NORMAL_STD:
         return run_direct<M_N32, GR_NORMAL_STD>(p, d, snap, s);
       case GR_NORMAL:
@@ -726,6 +822,17 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
       GR_F64_CASE(kTruncCauchyKind)
       GR_F64_CASE(kTruncExtremeKind)
       GR_F64_CASE(kTruncWeibullKind)
+      GR_F64_CASE(kVecBase + GR_UNIFORM_REAL2)
+      GR_F64_CASE(kVecBase + GR_EXPONENTIAL)
+      GR_F64_CASE(kVecBase + GR_WEIBULL)
+      GR_F64_CASE(kVecBase + GR_EXTREME_VALUE)
+      GR_F64_CASE(kVecBase + GR_CAUCHY)
+      case kVecBase + GR_BALANCED2:
+        return run_direct<M_W64, kVecBase + GR_BALANCED2>(p, d, snap, s);
+      case kVecBase + GR_NORMAL:
+        return run_direct<M_N64, kVecBase + GR_NORMAL>(p, d, snap, s);
+      case kVecBase + GR_LOGNORMAL:
+        return run_direct<M_N64, kVecBase + GR_LOGNORMAL>(p, d, snap, s);
       case GR_BALANCED:
         return run_direct<M_W64, GR_BALANCED>(p, d, snap, s);
       case GR_BALANCED2:

@@ -24,6 +24,7 @@ struct DistParams {
   int32_t post;                            // output transform of a beta draw: 1 = FisherFGen (fh / dh = b/a)
   int32_t flags;                           // kParamUnit*: a divisor or scale that is exactly 1 in the scalar type
   const void* vparam;                      // per-element parameter array (device), aligned with the output
+  const void* vparam2;                     // second per-element parameter array (kParamVecB)
   const int32_t* prob;                     // alias table / cdf (device)
   const int32_t* alias;
 };
@@ -32,6 +33,9 @@ struct DistParams {
 // skips its division or multiplication without changing a bit.
 constexpr int32_t kParamUnitDiv = 1;    // ExponentialGen: lambda == 1
 constexpr int32_t kParamUnitScale = 2;  // GammaGen beta, WeibullGen b == 1
+// per-element forms: parameter a / b of element i is vparam[i] / vparam2[i]
+constexpr int32_t kParamVecA = 4;
+constexpr int32_t kParamVecB = 8;
 
 // Output transform of generators built on a BetaGen draw x (bits v):
 // FisherFGen writes (b/a) x / (1 - x), b/a in the scalar type

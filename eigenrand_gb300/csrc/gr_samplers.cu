@@ -122,7 +122,10 @@ __global__ void __launch_bounds__(160)
         } else if (KIND == GR_STUDENT_T) {
           const float u1 = 1.0f - ur_f(word(w0));
           const float u2 = ur_f(word(w0 + 8));
-          const float radius = sqrtf(d.fa * (expf_(logf_(u1) * d.fc) - 1.0f));
+          // StudentTVGen (NormalExp.h:327-342): n of the element, -2 / n per lane
+          const float nn = (d.flags & kParamVecA) ? __ldg(static_cast<const float*>(d.vparam) + o) : d.fa;
+          const float ex = (d.flags & kParamVecA) ? -2.0f / nn : d.fc;
+          const float radius = sqrtf(nn * (expf_(logf_(u1) * ex) - 1.0f));
           float sn, cs;
           sincosf_((float)(2 * 3.1415926535897932) * u2, sn, cs);
           reinterpret_cast<float*>(p.out)[o] = radius * sn;
@@ -137,7 +140,9 @@ __global__ void __launch_bounds__(160)
         } else if (KIND == GR_STUDENT_T) {
           const double u1 = one_minus_ur_d(rword(r0));
           const double u2 = ur_d(rword(r0 + 4));
-          const double radius = sqrt(d.da * (exp_(log_(u1) * d.dc) - 1.0));
+          const double nn = (d.flags & kParamVecA) ? __ldg(static_cast<const double*>(d.vparam) + o) : d.da;
+          const double ex = (d.flags & kParamVecA) ? -2.0 / nn : d.dc;
+          const double radius = sqrt(nn * (exp_(log_(u1) * ex) - 1.0));
           double sn, cs;
           sincos_((2 * 3.1415926535897932) * u2, sn, cs);
           reinterpret_cast<double*>(p.out)[o] = radius * sn;

@@ -155,15 +155,33 @@ typedef struct {
 gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* batch, gr_stream_t stream);
 
 /* ---- per-element parameters ---------------------------------------------
- * The reference's vectorized forms that take a parameter array of the
- * output's shape: out[i] drawn with parameter a[i] (device arrays of n
- * elements, 16-byte aligned).  Supported: GR_BERNOULLI with GR_F32 --
- * BernoulliVGen<float> (Basic.h:711-747, bernoulli(urng, ArrayXf p),
- * :1146-1153).  The double form goes through a packet cast the reference
- * leaves to Eigen's generic pcast, which cannot be pinned here: it returns
- * GR_ERR_UNSUPPORTED. */
+ * The reference's vectorized forms (*VGen, and the free functions that take
+ * parameter arrays of the output's shape): out[i] is drawn with parameters
+ * a[i], b[i].  dev_a / dev_b are device arrays of n elements of the output's
+ * type, 16-byte aligned; NULL takes desc->a / desc->b for every element (the
+ * overloads with one scalar operand).  The draws are the scalar generator's
+ * packet stream, so for every i the value equals that generator built with
+ * (a[i], b[i]) at the same stream position.
+ *   GR_UNIFORM_REAL2 (min, max)  UniformRealVGen     Basic.h:638-666
+ *   GR_BALANCED2 (a, b)          BalancedVGen        Basic.h:472-492
+ *   GR_NORMAL (mean, stdev)      NormalVGen          NormalExp.h:139-163
+ *   GR_LOGNORMAL (mean, stdev)   LognormalVGen       NormalExp.h:213-236
+ *   GR_EXPONENTIAL (lambda)      ExponentialVGen     NormalExp.h:402-427
+ *   GR_STUDENT_T (n)             StudentTVGen        NormalExp.h:305-343
+ *   GR_WEIBULL (a, b)            WeibullVGen         NormalExp.h:659-686
+ *   GR_EXTREME_VALUE (a, b)      ExtremeValueVGen    NormalExp.h:736-765
+ *   GR_CAUCHY (a, b)             CauchyVGen          NormalExp.h:859-889
+ *   GR_BERNOULLI, GR_F32 (p)     BernoulliVGen<float> Basic.h:711-747
+ * The double BernoulliVGen goes through a packet cast the reference leaves to
+ * Eigen's generic pcast, which cannot be pinned here: GR_ERR_UNSUPPORTED.
+ * gr_sample_v / gr_sample_v2 use a fresh generator (the free functions);
+ * gr_generate_v keeps g's caches between calls (NormalVGen's StdNormalGen). */
 gr_status gr_sample_v(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, void* dev_out, size_t n,
                       gr_stream_t stream);
+gr_status gr_sample_v2(gr_engine* e, const gr_dist_desc* desc, const void* dev_a, const void* dev_b, void* dev_out,
+                       size_t n, gr_stream_t stream);
+gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* dev_b, void* dev_out, size_t n,
+                        gr_stream_t stream);
 
 /* ---- truncated distributions (EigenRand/Dists/Truncated.h) --------------
  * TruncGen<Base>{base, Support(lower, upper)} (Truncated.h:202-263 and the

@@ -665,6 +665,109 @@ int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, v
 }
 
 /* ======================================================================
+ * Per-element forms (*VGen): the scalar generator's packet draws with the
+ * lane's own parameters a[i], b[i] (NULL array: the scalar sa / sb).
+ * UniformRealVGen Basic.h:660-665, BalancedVGen :486-491, NormalVGen
+ * NormalExp.h:155-162, LognormalVGen :230-235, StudentTVGen :327-342,
+ * ExponentialVGen :420-426, WeibullVGen :679-685, ExtremeValueVGen :757-764,
+ * CauchyVGen :879-888.  g holds NormalVGen's StdNormalGen cache.
+ * ====================================================================== */
+int or_gen_real_v(or_vmt* e, or_gen* g, int dist, int dtype, const void* av, const void* bv, double sa, double sb,
+                  void* out, size_t n) {
+  const int dbl = dtype == 1, P = P_of(dbl);
+  if (n % (size_t)P) return 2;
+  if (e->L != 4) return 3;
+  const float* af = (const float*)av;
+  const float* bf = (const float*)bv;
+  const double* ad = (const double*)av;
+  const double* bd = (const double*)bv;
+  for (size_t k = 0; k < n / (size_t)P; ++k) {
+    upk p, p2;
+    switch (dist) {
+      case OR_UNIFORM:
+      case OR_EXPONENTIAL:
+      case OR_WEIBULL:
+      case OR_CAUCHY:
+        ur_pk(e, dbl, &p);
+        break;
+      case OR_BALANCED:
+        z2o_pk(e, dbl, &p);
+        break;
+      case OR_NORMAL:
+      case OR_LOGNORMAL:
+        stdnormal_pk(e, g, dbl, &p);
+        break;
+      case OR_EXTREME:
+        nzur_pk(e, dbl, &p);
+        break;
+      case OR_STUDENT_T:
+        ur_pk(e, dbl, &p);
+        ur_pk(e, dbl, &p2);
+        break;
+      default:
+        return 1;
+    }
+    for (int j = 0; j < P; ++j) {
+      const size_t i = k * (size_t)P + (size_t)j;
+      if (dbl) {
+        const double a = av ? ad[i] : sa, b = bv ? bd[i] : sb, u = p.d[j];
+        double v;
+        switch (dist) {
+          case OR_UNIFORM:
+          case OR_BALANCED: v = u * (b - a) + a; break;
+          case OR_NORMAL: v = u * b + a; break;
+          case OR_LOGNORMAL: v = or_exp(u * b + a); break;
+          case OR_EXPONENTIAL: v = -(or_log(1.0 - u) / a); break;
+          case OR_WEIBULL: v = or_exp(or_log(-or_log(1.0 - u)) * (1.0 / a)) * b; break;
+          case OR_EXTREME: v = a - or_log(-or_log(u)) * b; break;
+          case OR_CAUCHY: {
+            double sn, cs;
+            or_sincos(PI_D * (u - 0.5), &sn, &cs);
+            v = a + b * (sn / cs);
+            break;
+          }
+          default: { /* OR_STUDENT_T, n = a */
+            const double r = sqrt(a * (or_exp(or_log(1.0 - u) * (-2.0 / a)) - 1));
+            double sn, cs;
+            or_sincos((2 * PI_D) * p2.d[j], &sn, &cs);
+            v = r * sn;
+            break;
+          }
+        }
+        ((double*)out)[i] = v;
+      } else {
+        const float a = av ? af[i] : (float)sa, b = bv ? bf[i] : (float)sb, u = p.f[j];
+        float v;
+        switch (dist) {
+          case OR_UNIFORM:
+          case OR_BALANCED: v = u * (b - a) + a; break;
+          case OR_NORMAL: v = u * b + a; break;
+          case OR_LOGNORMAL: v = or_expf(u * b + a); break;
+          case OR_EXPONENTIAL: v = -(or_logf(1.0f - u) / a); break;
+          case OR_WEIBULL: v = or_expf(or_logf(-or_logf(1.0f - u)) * (1.0f / a)) * b; break;
+          case OR_EXTREME: v = a - or_logf(-or_logf(u)) * b; break;
+          case OR_CAUCHY: {
+            float sn, cs;
+            or_sincosf((float)PI_D * (u - 0.5f), &sn, &cs);
+            v = a + b * (sn / cs);
+            break;
+          }
+          default: {
+            const float r = sqrtf(a * (or_expf(or_logf(1.0f - u) * (-2.0f / a)) - 1));
+            float sn, cs;
+            or_sincosf((float)(2 * PI_D) * p2.f[j], &sn, &cs);
+            v = r * sn;
+            break;
+          }
+        }
+        ((float*)out)[i] = v;
+      }
+    }
+  }
+  return 0;
+}
+
+/* ======================================================================
  * Truncated family, Truncated.h.  A base with a closed-form CDF becomes
  * UniformRealGen(phi(lower), phi(upper)) pushed through its inverse CDF; the
  * constants are the constructors' own, in the scalar type, with the C

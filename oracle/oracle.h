@@ -91,6 +91,9 @@ enum {
 };
 int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b,
                 void* out, size_t n);
+/* per-element forms (*VGen): parameters a[i] / b[i] (NULL: the scalars) */
+int or_gen_real_v(or_vmt* e, or_gen* g, int dist, int dtype, const void* av, const void* bv, double sa, double sb,
+                  void* out, size_t n);
 /* TruncGen<Base>{base, Support(lower, upper)} (Truncated.h); g: four slots */
 int or_gen_trunc(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, double lower, double upper,
                  void* out, size_t n);

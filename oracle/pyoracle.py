@@ -73,6 +73,9 @@ def lib():
         L.or_vop_set.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                  vp, sz]
         L.or_vop_set.restype = ctypes.c_int
+        L.or_gen_real_v.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_double,
+                                    vp, sz]
+        L.or_gen_real_v.restype = ctypes.c_int
         L.or_gen_trunc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, vp, sz]
         L.or_gen_trunc.restype = ctypes.c_int
@@ -175,6 +178,23 @@ def generate(eng, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0, weight
         raise ValueError(kind)
     if rc != 0:
         raise RuntimeError(f"oracle error {rc} for {kind}")
+    return out
+
+
+def generate_v(eng, gen, kind, a, b=None, dtype=np.float32):
+    """A per-element form (*VGen): a / b are arrays of the output's length in
+    Eigen's linear order, or scalars."""
+    L = lib()
+    arrs = [np.ascontiguousarray(x, dtype=dtype) if isinstance(x, np.ndarray) else None for x in (a, b)]
+    n = next(x.size for x in arrs if x is not None)
+    out = np.empty(n, dtype=dtype)
+    sa = 0.0 if arrs[0] is not None else float(a)
+    sb = 0.0 if arrs[1] is not None or b is None else float(b)
+    rc = L.or_gen_real_v(eng.h, gen.ptr, REAL[kind], 1 if dtype == np.float64 else 0,
+                         _p(arrs[0]) if arrs[0] is not None else None,
+                         _p(arrs[1]) if arrs[1] is not None else None, sa, sb, _p(out), n)
+    if rc != 0:
+        raise RuntimeError(f"oracle error {rc} for per-element {kind}")
     return out
 
 

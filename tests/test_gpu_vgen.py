@@ -1,0 +1,133 @@
+"""GPU parity of the per-element forms (*VGen: parameter arrays of the
+output's shape) against the CPU oracle, bit-exact, through the C ABI."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def er(gpulib):
+    return gpulib
+
+
+def assert_bits_equal(a, b, msg=""):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    ua = a.view(np.uint64 if a.itemsize == 8 else np.uint32)
+    ub = b.view(np.uint64 if b.itemsize == 8 else np.uint32)
+    bad = np.nonzero(ua != ub)[0]
+    assert bad.size == 0, f"{msg}: {bad.size} mismatches, first at {bad[:5]}: {a[bad[:5]]} vs {b[bad[:5]]}"
+
+
+def eigen_mem(t):
+    """Eigen linear order of a (rows, cols) tensor."""
+    torch.cuda.synchronize()
+    if t.dim() == 2:
+        t = t.t()
+    return t.contiguous().reshape(-1).cpu().numpy()
+
+
+# kind, python free function, parameter generators (a, b) as functions of (rng, n)
+def _pos(lo, hi):
+    return lambda r, n: r.uniform(lo, hi, n)
+
+
+VKINDS = [
+    ("UNIFORM_REAL2", "uniformReal", _pos(-3, 0), _pos(0.5, 4)),
+    ("BALANCED2", "balanced", _pos(-3, 0), _pos(0.5, 4)),
+    ("NORMAL", "normal", _pos(-2, 2), _pos(0.1, 3)),
+    ("LOGNORMAL", "lognormal", _pos(-1, 1), _pos(0.1, 1)),
+    ("EXPONENTIAL", "exponential", _pos(0.2, 5), None),
+    ("STUDENT_T", "studentT", _pos(0.5, 20), None),
+    ("WEIBULL", "weibull", _pos(0.5, 4), _pos(0.5, 3)),
+    ("EXTREME_VALUE", "extremeValue", _pos(-2, 2), _pos(0.2, 3)),
+    ("CAUCHY", "cauchy", _pos(-2, 2), _pos(0.2, 3)),
+]
+
+
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+@pytest.mark.parametrize("kind,fn,ga,gb", VKINDS, ids=[v[0] for v in VKINDS])
+def test_vgen_free_function_bit_exact(er, oracle, kind, fn, ga, gb, tdt):
+    """kind(urng, a, b): both operands arrays, one array and one scalar, a 2-D
+    (column-major) call, and a long call split into jump-ahead segments."""
+    npt = np.float32 if tdt == torch.float32 else np.float64
+    r = np.random.default_rng(3)
+    u = er.Vmt19937_64(42)
+    e = oracle.Engine(42)
+    f = getattr(er, fn)
+    for n in (64, 1 << 20, 8):
+        a = ga(r, n).astype(npt)
+        b = gb(r, n).astype(npt) if gb else None
+        got = f(u, torch.from_numpy(a), torch.from_numpy(b)) if gb else f(u, torch.from_numpy(a))
+        ref = oracle.generate_v(e, oracle.Gen(), kind, a, b, npt)
+        assert_bits_equal(eigen_mem(got), ref, f"{kind} {tdt} n={n}")
+    if gb:
+        a = ga(r, 4096).astype(npt)
+        got = f(u, torch.from_numpy(a), 1.5)
+        ref = oracle.generate_v(e, oracle.Gen(), kind, a, 1.5, npt)
+        assert_bits_equal(eigen_mem(got), ref, f"{kind} scalar b")
+        b = gb(r, 4096).astype(npt)
+        got = f(u, 0.25, torch.from_numpy(b))
+        ref = oracle.generate_v(e, oracle.Gen(), kind, 0.25, b, npt)
+        assert_bits_equal(eigen_mem(got), ref, f"{kind} scalar a")
+    A = ga(r, 32 * 48).astype(npt).reshape(32, 48)
+    B = gb(r, 32 * 48).astype(npt).reshape(32, 48) if gb else None
+    tA = torch.from_numpy(A)
+    got = f(u, tA, torch.from_numpy(B)) if gb else f(u, tA)
+    assert tuple(got.shape) == (32, 48)
+    ref = oracle.generate_v(e, oracle.Gen(), kind, A.T.reshape(-1), B.T.reshape(-1) if gb else None, npt)
+    assert_bits_equal(eigen_mem(got), ref, f"{kind} 2-D")
+
+
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+def test_vgen_objects_keep_their_cache(er, oracle, tdt):
+    """NormalVGen / LognormalVGen objects carry the StdNormalGen half-pair
+    between calls (odd packet counts), like the reference's generate()."""
+    npt = np.float32 if tdt == torch.float32 else np.float64
+    P = 8 if tdt == torch.float32 else 4
+    r = np.random.default_rng(5)
+    for cls, kind in ((er.NormalVGen, "NORMAL"), (er.LognormalVGen, "LOGNORMAL")):
+        u = er.Vmt19937_64(9)
+        e = oracle.Engine(9)
+        g = cls(dtype=tdt)
+        og = oracle.Gen()
+        for n in (P, 3 * P, (1 << 19) + P, 5 * P):
+            a = r.uniform(-1, 1, n).astype(npt)
+            b = r.uniform(0.2, 1, n).astype(npt)
+            got = g.generate(u, torch.from_numpy(a), torch.from_numpy(b))
+            ref = oracle.generate_v(e, og, kind, a, b, npt)
+            assert_bits_equal(eigen_mem(got), ref, f"{kind} object {tdt} n={n}")
+    g = er.ExponentialVGen(dtype=tdt)
+    u = er.Vmt19937_64(9)
+    a = r.uniform(0.5, 2, 4096).astype(npt)
+    ref = oracle.generate_v(oracle.Engine(9), oracle.Gen(), "EXPONENTIAL", a, None, npt)
+    assert_bits_equal(eigen_mem(g.generate(u, torch.from_numpy(a))), ref, "ExponentialVGen")
+
+
+def test_vgen_matches_scalar_generator_and_streams(er, oracle):
+    """Constant parameter arrays give the scalar generator's values; slices of
+    a multi-stream engine come from engines seed + 4k."""
+    u1, u2 = er.Vmt19937_64(77), er.Vmt19937_64(77)
+    x = er.cauchy(1024, 1, u1, 0.5, 2.0)
+    y = er.cauchy(u2, torch.full((1024,), 0.5), torch.full((1024,), 2.0))
+    assert_bits_equal(eigen_mem(x), eigen_mem(y), "cauchy scalar vs per-element")
+    K, per = 4, 8 * 1000
+    u = er.Vmt19937_64(1234, streams=K)
+    r = np.random.default_rng(1)
+    a = r.uniform(-1, 1, K * per).astype(np.float32)
+    b = r.uniform(0.5, 2, K * per).astype(np.float32)
+    got = eigen_mem(er.normal(u, torch.from_numpy(a), torch.from_numpy(b)))
+    for k in range(K):
+        sl = slice(k * per, (k + 1) * per)
+        ref = oracle.generate_v(oracle.Engine(1234 + 4 * k), oracle.Gen(), "NORMAL", a[sl], b[sl], np.float32)
+        assert_bits_equal(got[sl], ref, f"slice {k}")
+    with pytest.raises(er.GrError):
+        er._vform("GAMMA", er.Vmt19937_64(1), torch.ones(8), torch.ones(8))
+    with pytest.raises(er.GrError):
+        er.normal(er.Vmt19937_64(1), torch.ones(12), torch.ones(12))

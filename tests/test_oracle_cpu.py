@@ -326,3 +326,23 @@ def test_truncated_host_validation(gpulib):
     assert type(t.getBase()).__name__ == "GammaGen"
     d = er.TruncGen(er.CauchyGen(0.0, 1.0))
     assert d.support.upper == float(np.finfo(np.float32).max)
+
+
+def test_oracle_per_element_forms(oracle):
+    """*VGen restatement: constant parameter arrays reproduce the scalar
+    generators bit for bit, and per-element parameters give each element
+    its own distribution (means of exponential(lambda_i) * lambda_i)."""
+    for dt in (np.float32, np.float64):
+        n = 4096
+        for kind, a, b in (("UNIFORM_REAL2", -2.0, 3.0), ("BALANCED2", -3.0, 5.0), ("NORMAL", 2.0, 3.0),
+                           ("LOGNORMAL", 0.0, 1.0), ("EXPONENTIAL", 1.5, None), ("WEIBULL", 1.5, 2.0),
+                           ("EXTREME_VALUE", 0.0, 1.0), ("CAUCHY", 0.0, 1.0), ("STUDENT_T", 5.0, None)):
+            v = oracle.generate_v(oracle.Engine(3), oracle.Gen(), kind, np.full(n, a, dt),
+                                  None if b is None else np.full(n, b, dt), dt)
+            s = oracle.generate(oracle.Engine(3), oracle.Gen(), kind, n, dt, a, 0.0 if b is None else b)
+            np.testing.assert_array_equal(v, s, err_msg=f"{kind} {dt}")
+        lam = np.where(np.arange(1 << 16) % 2 == 0, 0.5, 4.0).astype(dt)
+        x = oracle.generate_v(oracle.Engine(8), oracle.Gen(), "EXPONENTIAL", lam, None, dt).astype(np.float64)
+        for L in (0.5, 4.0):
+            m = (x[lam == L] * L).mean()
+            assert abs(m - 1) < 0.03, (L, m)
