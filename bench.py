@@ -333,6 +333,7 @@ def run_ours(args, rank, world):
         del outs, host
         torch.cuda.empty_cache()
         res["workloads"] = {"batched_vop": bench_batched(er), "multivariate": bench_multivariate(er),
+                            "truncated_and_per_element": bench_next_rows(er),
                             "serving": bench_serving(er, seconds=args.serve_seconds)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
@@ -472,6 +473,42 @@ def bench_multivariate(er, streams=608):
                                      "alias_draws_g_s": round(n * trials / (ms / 1e3) / 1e9, 1),
                                      "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
     del out
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return res
+
+
+def bench_next_rows(er, streams=608):
+    """Truncated family and per-element forms at 4096x4096: inverse-CDF
+    TruncGen / TruncNormalGen and *VGen on the streams engine; TruncGen's
+    CompressMask rejection (gamma base) on one Vmt19937_64, the only engine
+    form it takes."""
+    import torch
+    N = 4096 * 4096
+    urng = er.Vmt19937_64(1234, streams=streams)
+    res = {}
+
+    def entry(ms, nbytes):
+        return {"ms": round(ms, 3), "gsamples_s": round(N / (ms / 1e3) / 1e9, 2),
+                "gbs": round(nbytes / (ms / 1e3) / 1e9, 1)}
+    for tdt, tag in ((torch.float32, "f32"), (torch.float64, "f64")):
+        es = 4 if tdt == torch.float32 else 8
+        out = torch.empty((4096, 4096), dtype=tdt, device="cuda")
+        tn = er.TruncNormalGen(0.0, 1.0, er.support(-1.0, 2.0), dtype=tdt)
+        res[f"truncNormal/{tag}"] = entry(_median_ms(lambda: tn.generate(4096, 4096, urng, out=out)), N * es)
+        te = er.TruncGen(er.ExponentialGen(1.0, dtype=tdt), er.support(0.5, 3.0))
+        res[f"truncExponential/{tag}"] = entry(_median_ms(lambda: te.generate(4096, 4096, urng, out=out)), N * es)
+        mean = torch.rand(N, dtype=tdt, device="cuda")
+        sd = torch.rand(N, dtype=tdt, device="cuda") + 0.5
+        res[f"normalV/{tag}"] = entry(_median_ms(lambda: er.normal(urng, mean, sd, out=out.view(-1))), 3 * N * es)
+        res[f"studentTV/{tag}"] = entry(_median_ms(lambda: er.studentT(urng, sd, out=out.view(-1))), 2 * N * es)
+        one = er.Vmt19937_64(1234)
+        tg = er.TruncGen(er.GammaGen(2.0, 1.0, dtype=tdt), er.support(0.5, 5.0))
+        tg.generate(4096, 4096, one, out=out)  # first call: pilot chunk learns the acceptance
+        res[f"truncGammaReject/{tag}"] = entry(_median_ms(lambda: tg.generate(4096, 4096, one, out=out)), N * es)
+        res[f"gamma2_single_stream/{tag}"] = entry(
+            _median_ms(lambda: er.gamma(4096, 4096, one, 2.0, 1.0, dtype=tdt, out=out)), N * es)
+        del out, mean, sd
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     return res

@@ -872,15 +872,53 @@ gr_status trunc_setup(const gr_dist_desc& d, T lo, T hi, DistParams& p, bool& re
   return GR_OK;
 }
 
+// Advances every stream of the engine by npackets raw packets without writing
+// them: k_direct's raw mode with no output, in jump-ahead segments like a
+// long call.
+gr_status advance_engine(gr_engine* e, uint64_t npackets, cudaStream_t s) {
+  if (npackets == 0) return GR_OK;
+  DistParams dp{};
+  dp.kind = kRawKind;
+  dp.dtype = GR_U64;
+  Plan p{};
+  p.eng = e->st;
+  p.K = e->K;
+  p.gran = 4;
+  p.gran_per_k = (int64_t)npackets;
+  p.gran_rem = 0;
+  p.out = nullptr;
+  int S;
+  int64_t J;
+  plan_segments(e, (int64_t)npackets, 1, S, J);
+  gr_status st = prepare_segments(e, p, S, J, 0, s);
+  if (st != GR_OK) return st;
+  const cudaError_t err = launch_direct(p, dp, e->snap, s);
+  if (err != cudaSuccess) return cuda_fail(err, "engine advance");
+  return GR_OK;
+}
+
+// Engine packets per base output packet when the base's consumption is
+// fixed (direct and staged kinds: GammaGen with integer alpha, StudentTGen,
+// BernoulliGen), else 0 (rejection and walk kinds).
+int64_t fixed_packets_per_packet(const DistParams& dp) {
+  const Family fam = family_of(dp);
+  if (fam == Family::Direct) return kind_packets_per_unit(dp.kind, dp.dtype);
+  if (fam == Family::Staged && dp.dtype != GR_I32) return dp.kind == GR_STUDENT_T ? 2 : dp.ib;
+  return 0;
+}
+
 // TruncGen<Base>::generate for the rejection form on a single-stream engine.
 // The base packets are drawn in chunks into HBM and filtered (gr_trunc.cu);
 // the host reads how many outputs each chunk gave.  When a chunk holds the
-// last wanted output at base packet k*, the engine and the base's caches go
-// back to their state before the chunk and the base draws exactly k* + 1
-// packets again, so both end where the reference's would.  A first call
-// draws a pilot chunk to learn the acceptance; later chunks aim just below
-// the expected need, so the redrawn tail stays small.  Synchronises the
-// stream once per chunk.
+// last wanted output at base packet k*, the engine goes back to its state at
+// the chunk start and moves to just after base packet k*: by a raw advance of
+// (k* + 1) * U packets when the base consumes a fixed U packets per packet,
+// else by drawing the k* + 1 base packets again (with the base's caches
+// restored too).  Chunk sizes come from the acceptance seen so far (a first
+// call draws a pilot chunk): a fixed-consumption base draws its expected need
+// plus four standard deviations, so one chunk almost always suffices; any
+// other base draws four standard deviations short, so the redrawn last chunk
+// is small.  Synchronises the stream once per chunk.
 gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s) {
   const int dt = g->dp.dtype;
   const int64_t P = dt == GR_F32 ? 8 : 4;
@@ -897,6 +935,7 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
     GR_CUDA(cudaMalloc(&g->trunc_carry, sizeof(GenSlot)));
     GR_CUDA(cudaMemset(g->trunc_carry, 0, sizeof(GenSlot)));
   }
+  const int64_t upk = fixed_packets_per_packet(b->dp);
   const int64_t need = (int64_t)(n / (size_t)P);
   const int64_t mcap = kTruncChunkMax - 1;
   // scratch, grown when a chunk needs more: candidates, FIFO, CTA sums,
@@ -919,6 +958,10 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
     off[6] = take(sizeof(GenState));
     return o;
   };
+  auto bail = [&](gr_status r) {
+    if (buf) cudaFreeAsync(buf, s);
+    return r;
+  };
   size_t off[7];
   int64_t done = 0, drawn = 0;
   int64_t res[6];
@@ -929,20 +972,22 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
     if (q <= 0) {
       M = std::min<int64_t>(rem, 4096);
     } else {
-      const double E = (double)rem / q;
-      M = E > 32768 ? (int64_t)(E * 0.98) : (int64_t)std::ceil(E * 1.25) + 64;
+      // packets for rem * P accepted lanes, and the spread of that count
+      const double lanes = (double)rem * (double)P, E = lanes / (q * (double)P);
+      const double sd = std::sqrt(lanes * std::max(1.0 - q, 0.0)) / (q * (double)P);
+      if (upk == 0 && E > 32768) M = (int64_t)(E - 4 * sd) - 16;
+      else M = (int64_t)std::ceil(E + 4 * sd) + 16;
     }
     M = std::max<int64_t>(1, std::min(M, mcap));
     drawn += M;
-    if (drawn > ((int64_t)1 << 40)) {
-      cudaFreeAsync(buf, s);
-      return fail(GR_ERR_REJECT_LIMIT, "TruncGen: the support holds almost none of the base distribution");
-    }
+    if (drawn > ((int64_t)1 << 40))
+      return bail(fail(GR_ERR_REJECT_LIMIT, "TruncGen: the support holds almost none of the base distribution"));
     if (M > have_m) {
       if (buf) cudaFreeAsync(buf, s);
       buf = nullptr;
       const int64_t m = std::min(mcap, std::max(M, have_m * 2));
-      GR_CUDA(cudaMallocAsync(&buf, layout(m, off), s));
+      const cudaError_t err = cudaMallocAsync(&buf, layout(m, off), s);
+      if (err != cudaSuccess) return cuda_fail(err, "TruncGen scratch");
       have_m = m;
     }
     layout(have_m, off);
@@ -950,13 +995,11 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
     int64_t* dres = reinterpret_cast<int64_t*>(buf + off[4]);
     EngState* saved_e = reinterpret_cast<EngState*>(buf + off[5]);
     GenState* saved_g = reinterpret_cast<GenState*>(buf + off[6]);
-    GR_CUDA(cudaMemcpyAsync(saved_e, e->st, sizeof(EngState), cudaMemcpyDeviceToDevice, s));
-    GR_CUDA(cudaMemcpyAsync(saved_g, b->gst, sizeof(GenState), cudaMemcpyDeviceToDevice, s));
+    cudaError_t err = cudaMemcpyAsync(saved_e, e->st, sizeof(EngState), cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(saved_g, b->gst, sizeof(GenState), cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) return bail(cuda_fail(err, "TruncGen state copy"));
     st = run_call(e, b, b->dp, cand, (size_t)(M * P), s);
-    if (st != GR_OK) {
-      cudaFreeAsync(buf, s);
-      return st;
-    }
+    if (st != GR_OK) return bail(st);
     TruncFilterArgs a{};
     a.cand = cand;
     a.M = M;
@@ -969,13 +1012,10 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
     a.blk = reinterpret_cast<int64_t*>(buf + off[2]);
     a.grp = reinterpret_cast<int64_t*>(buf + off[3]);
     a.res = dres;
-    cudaError_t err = launch_trunc_filter(dt, a, s);
+    err = launch_trunc_filter(dt, a, s);
     if (err == cudaSuccess) err = cudaMemcpyAsync(res, dres, sizeof res, cudaMemcpyDeviceToHost, s);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
-    if (err != cudaSuccess) {
-      cudaFreeAsync(buf, s);
-      return cuda_fail(err, "TruncGen filter");
-    }
+    if (err != cudaSuccess) return bail(cuda_fail(err, "TruncGen filter"));
     g->trunc_lanes += M * P;
     g->trunc_acc += res[2] * P + res[3];
     if (res[1] < 0) {
@@ -983,19 +1023,17 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
       continue;
     }
     if (res[1] + 1 < M) {
-      // rewind to the chunk start and redraw only the base packets consumed
-      GR_CUDA(cudaMemcpyAsync(e->st, saved_e, sizeof(EngState), cudaMemcpyDeviceToDevice, s));
-      GR_CUDA(cudaMemcpyAsync(b->gst, saved_g, sizeof(GenState), cudaMemcpyDeviceToDevice, s));
-      st = run_call(e, b, b->dp, cand, (size_t)((res[1] + 1) * P), s);
-      if (st != GR_OK) {
-        cudaFreeAsync(buf, s);
-        return st;
-      }
+      // back to the chunk start, then just past base packet k*
+      err = cudaMemcpyAsync(e->st, saved_e, sizeof(EngState), cudaMemcpyDeviceToDevice, s);
+      if (err == cudaSuccess) err = cudaMemcpyAsync(b->gst, saved_g, sizeof(GenState), cudaMemcpyDeviceToDevice, s);
+      if (err != cudaSuccess) return bail(cuda_fail(err, "TruncGen state copy"));
+      st = upk ? advance_engine(e, (uint64_t)((res[1] + 1) * upk), s)
+               : run_call(e, b, b->dp, cand, (size_t)((res[1] + 1) * P), s);
+      if (st != GR_OK) return bail(st);
     }
     done = need;
   }
-  cudaFreeAsync(buf, s);
-  return GR_OK;
+  return bail(GR_OK);
 }
 
 // TruncGen<Base>{base, Support(lower, upper)}: fills g (inverse-CDF forms in
@@ -1029,23 +1067,7 @@ gr_status gr_raw_u64(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stre
 
 gr_status gr_engine_discard(gr_engine* e, uint64_t npackets, gr_stream_t stream) {
   if (!e) return fail(GR_ERR_INVALID, "engine is NULL");
-  if (npackets == 0) return GR_OK;
-  DistParams dp{};
-  dp.kind = kRawKind;
-  dp.dtype = GR_U64;
-  Plan p{};
-  p.eng = e->st;
-  p.K = e->K;
-  p.S = 1;
-  p.J = (int64_t)npackets;
-  p.gran = 4;
-  p.gran_per_k = (int64_t)npackets;
-  p.gran_rem = 0;
-  p.out = nullptr;  // every engine advances npackets; nothing is written
-  // slice offsets are irrelevant without output; each engine gets npackets
-  cudaError_t err = launch_direct(p, dp, nullptr, (cudaStream_t)stream);
-  if (err != cudaSuccess) return cuda_fail(err, "discard kernel");
-  return GR_OK;
+  return advance_engine(e, npackets, (cudaStream_t)stream);
 }
 
 gr_status gr_gen_create(gr_gen** out, const gr_dist_desc* desc) {

@@ -94,6 +94,19 @@ def test_discard_matches_draws(er, oracle):
     assert_bits_equal(er.raw_u64(u, 4096).cpu().numpy().view(np.uint64), e.raw(1024), "discard")
 
 
+def test_long_discard_in_segments(er, oracle):
+    """discard(n) of millions of packets (jump-ahead segments), single and
+    multi-stream engines."""
+    for streams in (1, 3):
+        u = er.Vmt19937_64(13, streams=streams)
+        u.discard(3_000_017)
+        x = er.raw_u64(u, 4096 * streams).cpu().numpy().view(np.uint64)
+        for k in range(streams):
+            e = oracle.Engine(13 + 4 * k)
+            e.discard(3_000_017)
+            assert_bits_equal(x[k * 4096:(k + 1) * 4096], e.raw(1024), f"discard stream {k}")
+
+
 def test_streams_are_independent_engines(er, oracle):
     """streams=K: slice k comes from Vmt19937_64(seed + 4k)."""
     K, per = 8, 8 * 1000
