@@ -473,6 +473,16 @@ def bench_multivariate(er, streams=608):
                                      "alias_draws_g_s": round(n * trials / (ms / 1e3) / 1e9, 1),
                                      "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
     del out
+    # trials >= max(30 (K - 1), 100): the conditional-binomial path
+    K, trials, n = 10, 1000, 1_000_000
+    p = np.random.default_rng(99).dirichlet(np.ones(K))
+    mg = er.MultinomialGen(trials, p)
+    out = torch.empty((n, K), dtype=torch.int32, device="cuda").t()
+    ms = _median_ms(lambda: mg.generate(urng, n, out=out))
+    res["multinomial_k10_t1000_conditional"] = {"draws": n, "ms": round(ms, 3), "mdraws_s": round(n / ms / 1e3, 2),
+                                                "binomial_rows_g_s": round(n * (K - 1) / (ms / 1e3) / 1e9, 2),
+                                                "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
+    del out
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     return res

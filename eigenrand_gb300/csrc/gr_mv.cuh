@@ -71,6 +71,18 @@ struct MnArgs {
   int32_t* out;          // dim x samples, column-major
 };
 
+// MultinomialGen's conditional-binomial path (gr_mncond.cu): rows binomial
+// rows of p[row] over the engine's samples (granule 8), out dim x samples.
+struct McArgs {
+  const float* p;      // p of each drawn row, float (device)
+  int32_t rows;        // rows drawn: max(dim - 1, 1)
+  int32_t dim;
+  int32_t trials;
+  int32_t* out;        // dim x samples, column-major
+  int64_t max_blocks;  // engine blocks per engine before the status word is set
+};
+cudaError_t launch_mn_cond(const Plan& p, const McArgs& a, cudaStream_t s);
+
 cudaError_t launch_inverse_f64(double* A, double* W, int d, int32_t* status, cudaStream_t s);
 cudaError_t launch_chol_f64(double* A, int d, int32_t* status, cudaStream_t s);
 cudaError_t launch_jacobi_f64(double* A, double* V, double* L, int d, int32_t* status, cudaStream_t s);

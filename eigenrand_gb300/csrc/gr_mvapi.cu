@@ -33,6 +33,40 @@ gr_status mv_fail(gr_status s, const std::string& m) { return set_last_error(s, 
 int packet_width(int dtype) { return dtype == GR_F32 ? 8 : 4; }
 size_t elem_size(int dtype) { return dtype == GR_F32 ? sizeof(float) : sizeof(double); }
 
+// Eigen 3.4's sum() of a dynamic double vector compiled with AVX (packets of
+// 4, the LinearVectorizedTraversal redux): two packet accumulators over pairs
+// of packets, added, plus one more packet when the aligned part holds an odd
+// number of them; the packet reduced as (a0 + a2) + (a1 + a3); then the
+// remaining elements in order.  Below one packet it is a plain left-to-right
+// sum.  Eigen's storage is 32-byte aligned, so the aligned part starts at 0.
+// MultinomialGen normalises its weights by this sum.
+double eigen_sum_avx(const double* v, int n) {
+  constexpr int ps = 4;
+  const int as2 = (n / (2 * ps)) * (2 * ps), as = (n / ps) * ps;
+  if (as == 0) {
+    double r = v[0];
+    for (int i = 1; i < n; ++i) r = r + v[i];
+    return r;
+  }
+  double acc0[ps], acc1[ps];
+  for (int j = 0; j < ps; ++j) acc0[j] = v[j];
+  if (as > ps) {
+    for (int j = 0; j < ps; ++j) acc1[j] = v[ps + j];
+    for (int i = 2 * ps; i < as2; i += 2 * ps) {
+      for (int j = 0; j < ps; ++j) {
+        acc0[j] = acc0[j] + v[i + j];
+        acc1[j] = acc1[j] + v[i + ps + j];
+      }
+    }
+    for (int j = 0; j < ps; ++j) acc0[j] = acc0[j] + acc1[j];
+    if (as > as2)
+      for (int j = 0; j < ps; ++j) acc0[j] = acc0[j] + v[as2 + j];
+  }
+  double r = (acc0[0] + acc0[2]) + (acc0[1] + acc0[3]);
+  for (int i = as; i < n; ++i) r = r + v[i];
+  return r;
+}
+
 bool all_finite(const double* v, size_t n) {
   for (size_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
@@ -176,6 +210,10 @@ struct gr_dirichlet {
 
 struct gr_multinomial {
   int dim = 0, trials = 0;
+  // conditional-binomial path: p of each drawn row (device floats)
+  bool cond = false;
+  float* pdev = nullptr;
+  int rows = 0;
   int32_t* table = nullptr;  // prob (or CDF) then alias
   int32_t ncdf = 0;
   uint32_t bitmask = 0;
@@ -424,6 +462,7 @@ gr_status gr_dirichlet_sample(gr_dirichlet* g, gr_engine* e, void* dev_out, size
 // ---------------------------------------------------------------- MultinomialGen
 gr_status gr_multinomial_destroy(gr_multinomial* g) {
   if (!g) return GR_OK;
+  cudaFree(g->pdev);
   cudaFree(g->table);
   cudaFree(g->gst);
   delete g;
@@ -436,8 +475,35 @@ gr_status gr_multinomial_create(gr_multinomial** out, int32_t dim, int32_t trial
   if (trials < 0) return mv_fail(GR_ERR_INVALID, "trials must be >= 0");
   for (int i = 0; i < dim; ++i)
     if (!(weights[i] >= 0)) return mv_fail(GR_ERR_INVALID, "weights must be >= 0");
-  if ((int64_t)trials >= std::max<int64_t>(30 * (int64_t)(dim - 1), 100))
-    return mv_fail(GR_ERR_UNSUPPORTED, "the conditional-binomial multinomial path (trials >= max(30 (dim - 1), 100))");
+  if ((int64_t)trials >= std::max<int64_t>(30 * (int64_t)(dim - 1), 100)) {
+    // probs = weights / probs.sum() (Multinomial.h:41-49), then the p of
+    // each drawn row: probs[0], and probs[i] / rest_p with rest_p = 1 -
+    // probs[0] - ... - probs[i-1] in double, converted to float
+    const double sum = eigen_sum_avx(weights, dim);
+    std::vector<double> probs(weights, weights + dim);
+    for (double& q : probs) q = q / sum;
+    const int rows = std::max(dim - 1, 1);
+    std::vector<float> pr(rows);
+    double rest = 1 - probs[0];
+    pr[0] = (float)probs[0];
+    for (int i = 1; i < rows; ++i) {
+      pr[i] = (float)(probs[i] / rest);
+      rest -= probs[i];
+    }
+    gr_multinomial* g = new gr_multinomial;
+    g->dim = dim;
+    g->trials = trials;
+    g->cond = true;
+    g->rows = rows;
+    cudaError_t e = cudaMalloc(&g->pdev, sizeof(float) * rows);
+    if (e == cudaSuccess) e = cudaMemcpy(g->pdev, pr.data(), sizeof(float) * rows, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      gr_multinomial_destroy(g);
+      return mv_fail(GR_ERR_CUDA, std::string("multinomial p: ") + cudaGetErrorString(e));
+    }
+    *out = g;
+    return GR_OK;
+  }
   const MnLayout L = mn_layout(trials, 0);
   if (L.W0 > kMnMaxSampleWords || L.W1 > kMnMaxSampleWords)
     return mv_fail(GR_ERR_UNSUPPORTED, "multinomial: trials above 2400");
@@ -478,6 +544,31 @@ gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_ou
     return GR_OK;
   }
   const int K = gr_engine_streams(e);
+  if (g->cond) {
+    if (samples % 8)
+      return mv_fail(GR_ERR_INVALID, "the conditional-binomial multinomial path needs samples % 8 == 0 "
+                                     "(BinomialVGen<float> packets of 8 samples)");
+    const int64_t gran = (int64_t)(samples / 8);
+    Plan p{};
+    p.eng = engine_state_ptr(e);
+    p.K = K;
+    p.gran = 8;
+    p.gran_per_k = gran / K;
+    p.gran_rem = gran % K;
+    McArgs a{};
+    a.p = g->pdev;
+    a.rows = g->rows;
+    a.dim = g->dim;
+    a.trials = g->trials;
+    a.out = dev_out;
+    // Poisson loop about mean + 1 packets, tan rejection about 2.5 trials of
+    // two packets; the cap is far above either
+    const int64_t pk = (p.gran_per_k + 1) * (int64_t)g->rows;
+    a.max_blocks = (pk * 64) / kN + 64;
+    const cudaError_t err = launch_mn_cond(p, a, s);
+    if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("multinomial kernel: ") + cudaGetErrorString(err));
+    return GR_OK;
+  }
   if (g->gst_K != K) {  // DiscreteGen cache per engine stream
     cudaFree(g->gst);
     g->gst = nullptr;

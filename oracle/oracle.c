@@ -1555,11 +1555,11 @@ int or_gen_multinomial(or_vmt* e, or_gen* g, const or_discrete* d, int32_t trial
  * multiplicative Poisson loop; the others a tan-proposal rejection with a
  * per-lane accepted mask, iterating until every lane has a value.
  * ====================================================================== */
-int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out) {
-  float small_p[4], ptrials[4], mean[4], g1[4], sqrt_v[4], lsp[4], lsq[4], ne[4];
-  int valid[4], any_valid = 0, all_valid = 1;
-  float valid_res[4] = {0, 0, 0, 0};
-  for (int j = 0; j < 4; ++j) {
+static void binomial_v_lanes(or_vmt* e, int P, const int32_t* trials, const float* p, int32_t* out) {
+  float small_p[8], ptrials[8], mean[8], g1[8], sqrt_v[8], lsp[8], lsq[8], ne[8];
+  int valid[8], any_valid = 0, all_valid = 1;
+  float valid_res[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j < P; ++j) {
     small_p[j] = p[j] < 1.0f - p[j] ? p[j] : 1.0f - p[j]; /* pmin(p, 1 - p) */
     ptrials[j] = (float)trials[j];
     mean[j] = ptrials[j] * small_p[j];
@@ -1573,35 +1573,35 @@ int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32
     all_valid &= valid[j];
   }
   if (any_valid) {
-    int32_t res[4] = {0, 0, 0, 0};
-    float val[4] = {1, 1, 1, 1};
+    int32_t res[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float val[8] = {1, 1, 1, 1, 1, 1, 1, 1};
     for (;;) {
-      float u[4];
-      ur_f4(e, u);
-      int any = 0, c[4];
-      for (int j = 0; j < 4; ++j) {
+      float u[8];
+      if (P == 8) ur_f8(e, u); else ur_f4(e, u);
+      int any = 0, c[8];
+      for (int j = 0; j < P; ++j) {
         val[j] = val[j] * u[j];
         c[j] = (ne[j] < val[j]) && valid[j];
         any |= c[j];
       }
       if (!any) break;
-      for (int j = 0; j < 4; ++j) res[j] += c[j];
+      for (int j = 0; j < P; ++j) res[j] += c[j];
     }
-    for (int j = 0; j < 4; ++j) valid_res[j] = (float)res[j];
+    for (int j = 0; j < P; ++j) valid_res[j] = (float)res[j];
   }
   if (!all_valid) {
     for (;;) {
-      float u[4], u2[4], fres[4], ys[4];
-      ur_f4(e, u);
-      for (int j = 0; j < 4; ++j) {
+      float u[8], u2[8], fres[8], ys[8];
+      if (P == 8) ur_f8(e, u); else ur_f4(e, u);
+      for (int j = 0; j < P; ++j) {
         float s, c;
         or_sincosf((float)PI_D * u[j], &s, &c);
         ys[j] = s / c;
         fres[j] = truncf(sqrt_v[j] * ys[j] + mean[j]);
       }
-      ur_f4(e, u2);
+      if (P == 8) ur_f8(e, u2); else ur_f4(e, u2);
       int all = 1;
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < P; ++j) {
         float p1 = ((float)1.2 * sqrt_v[j]) * (1.0f + ys[j] * ys[j]);
         float t = (g1[j] - or_lgamma_approxf(fres[j] + 1.0f)) - or_lgamma_approxf((ptrials[j] + 1.0f) - fres[j]);
         t = t + fres[j] * lsp[j];
@@ -1615,7 +1615,79 @@ int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32
       if (all) break;
     }
   }
-  for (int j = 0; j < 4; ++j) out[j] = (p[j] == small_p[j]) ? (int32_t)valid_res[j] : trials[j] - (int32_t)valid_res[j];
+  for (int j = 0; j < P; ++j) out[j] = (p[j] == small_p[j]) ? (int32_t)valid_res[j] : trials[j] - (int32_t)valid_res[j];
+}
+
+int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out) {
+  binomial_v_lanes(e, 4, trials, p, out);
+  return 0;
+}
+
+/* Eigen 3.4's sum() of a dynamic double vector with AVX packets of 4 (the
+ * LinearVectorizedTraversal redux of Redux.h): two packet accumulators over
+ * pairs of packets, their sum, one more packet if the aligned part has an odd
+ * count, the packet reduced as (a0 + a2) + (a1 + a3), then the tail in order;
+ * below one packet, a plain left-to-right sum.  The vector's storage is
+ * 32-byte aligned, so the aligned part starts at 0. */
+double or_eigen_sum_avx(const double* v, int n) {
+  const int ps = 4, as2 = (n / (2 * ps)) * (2 * ps), as = (n / ps) * ps;
+  if (!as) {
+    double r = v[0];
+    for (int i = 1; i < n; ++i) r += v[i];
+    return r;
+  }
+  double p0[4], p1[4];
+  for (int j = 0; j < 4; ++j) p0[j] = v[j];
+  if (as > ps) {
+    for (int j = 0; j < 4; ++j) p1[j] = v[ps + j];
+    for (int i = 2 * ps; i < as2; i += 2 * ps)
+      for (int j = 0; j < 4; ++j) {
+        p0[j] = p0[j] + v[i + j];
+        p1[j] = p1[j] + v[i + ps + j];
+      }
+    for (int j = 0; j < 4; ++j) p0[j] = p0[j] + p1[j];
+    if (as > as2)
+      for (int j = 0; j < 4; ++j) p0[j] = p0[j] + v[as2 + j];
+  }
+  double r = (p0[0] + p0[2]) + (p0[1] + p0[3]);
+  for (int i = as; i < n; ++i) r = r + v[i];
+  return r;
+}
+
+/* MultinomialGen<int32_t>::generate(urng, samples) on its conditional-binomial
+ * path, trials >= max(30 (dim - 1), 100) (Multinomial.h:62-87): probs =
+ * weights / sum; row 0 is BinomialVGen<float> over every sample with p =
+ * probs[0] and the remaining trials per lane, then rows 1 .. dim-2 with p =
+ * probs[i] / rest_p (rest_p = 1 - probs[0] - ... in double, p converted to
+ * float), each row one packet of 8 samples after another; the last row is
+ * what remains.  out = dim x samples, column-major; samples % 8 == 0. */
+int or_gen_multinomial_cond(or_vmt* e, const double* w, int32_t dim, int32_t trials, int32_t* out,
+                            size_t samples) {
+  if (e->L != 4 || dim < 1 || samples % 8) return 2;
+  double* probs = (double*)malloc(sizeof(double) * (size_t)dim);
+  int32_t* r = (int32_t*)malloc(sizeof(int32_t) * (samples ? samples : 1));
+  const double sum = or_eigen_sum_avx(w, dim);
+  for (int i = 0; i < dim; ++i) probs[i] = w[i] / sum;
+  for (size_t q = 0; q < samples; ++q) r[q] = trials;
+  double rest = 0;
+  const int last = dim - 2 > 0 ? dim - 2 : 0;
+  for (int i = 0; i <= last; ++i) {
+    float pv = i == 0 ? (float)probs[0] : (float)(probs[i] / rest);
+    float pp[8];
+    for (int j = 0; j < 8; ++j) pp[j] = pv;
+    for (size_t k = 0; k < samples / 8; ++k) {
+      int32_t t[8];
+      binomial_v_lanes(e, 8, r + 8 * k, pp, t);
+      for (int j = 0; j < 8; ++j) {
+        if (i < dim - 1) out[(8 * k + j) * (size_t)dim + i] = t[j];
+        r[8 * k + j] -= t[j];
+      }
+    }
+    rest = i == 0 ? 1 - probs[0] : rest - probs[i];
+  }
+  for (size_t q = 0; q < samples; ++q) out[q * (size_t)dim + dim - 1] = r[q];
+  free(probs);
+  free(r);
   return 0;
 }
 

@@ -128,6 +128,10 @@ int or_gen_multinomial(or_vmt* e, or_gen* g, const or_discrete* d, int32_t trial
 
 /* vectorize-over-params */
 int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out);
+/* MultinomialGen, conditional-binomial path (trials >= max(30 (dim-1), 100)) */
+double or_eigen_sum_avx(const double* v, int n);
+int or_gen_multinomial_cond(or_vmt* e, const double* w, int32_t dim, int32_t trials, int32_t* out,
+                            size_t samples);
 int or_vop_set(uint64_t seed, int kind, double a, double b, int32_t trials, void* out, size_t count);
 
 /* ---- math (library's own log/exp; EigenRand psincos restated) ---------- */

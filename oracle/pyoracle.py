@@ -70,6 +70,10 @@ def lib():
         L.or_gen_discrete.restype = ctypes.c_int
         L.or_gen_multinomial.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
         L.or_gen_multinomial.restype = ctypes.c_int
+        L.or_gen_multinomial_cond.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
+        L.or_gen_multinomial_cond.restype = ctypes.c_int
+        L.or_eigen_sum_avx.argtypes = [vp, ctypes.c_int]
+        L.or_eigen_sum_avx.restype = ctypes.c_double
         L.or_vop_set.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                  vp, sz]
         L.or_vop_set.restype = ctypes.c_int
@@ -234,6 +238,24 @@ def multinomial(eng, gen, weights, trials, samples):
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return out
+
+
+def multinomial_cond(eng, weights, trials, samples):
+    """MultinomialGen<int32_t>(trials, weights).generate(urng, samples) on the
+    conditional-binomial path (Multinomial.h:62-87).  Returns (samples, dim)."""
+    L = lib()
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    out = np.empty((samples, len(w)), dtype=np.int32)
+    rc = L.or_gen_multinomial_cond(eng.h, _p(w), len(w), int(trials), _p(out), samples)
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return out
+
+
+def eigen_sum_avx(v):
+    """Eigen 3.4's vectorized sum() order for a double vector (AVX)."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    return lib().or_eigen_sum_avx(_p(v), len(v))
 
 
 def discrete_table(weights):

@@ -105,10 +105,38 @@ def test_multinomial_counts_chi2(er):
 
 
 def test_multinomial_errors(er):
-    with pytest.raises(er.GrError, match="UNSUPPORTED"):
-        er.MultinomialGen(100000, np.ones(10))  # conditional-binomial path
+    g = er.MultinomialGen(100000, np.ones(10))  # conditional-binomial path: packets of 8 samples
+    with pytest.raises(er.GrError, match="INVALID"):
+        g.generate(er.Vmt19937_64(1), 12)
     with pytest.raises(er.GrError, match="INVALID"):
         er.MultinomialGen(10, [1.0, -1.0, 2.0])
+
+
+@pytest.mark.parametrize("dim,trials", [(10, 1000), (2, 500), (1, 200), (5, 100000), (100, 5000), (7, 180)])
+def test_multinomial_conditional_path_bit_exact(er, oracle, dim, trials):
+    """trials >= max(30 (dim - 1), 100): BinomialVGen<float> row by row
+    (Multinomial.h:62-87), single-stream calls in a row (engine state carried)
+    and a multi-stream engine (slice k from engine seed + 4k)."""
+    w = np.random.default_rng(dim).uniform(0.0, 2.0, dim)
+    if dim > 3:
+        w[1] = 0.0
+    g = er.MultinomialGen(trials, w)
+    u = er.Vmt19937_64(77)
+    e = oracle.Engine(77)
+    for samples in (8, 4096, 24):
+        a = rows(g.generate(u, samples))
+        ref = oracle.multinomial_cond(e, w, trials, samples)
+        np.testing.assert_array_equal(a, ref)
+    np.testing.assert_array_equal(er.raw_u64(u, 64).cpu().numpy().view(np.uint64), e.raw(16))
+    K, samples = 3, 8 * 1001
+    a = rows(g.generate(er.Vmt19937_64(77, streams=K), samples))
+    gran, off = samples // 8, 0
+    for k in range(K):
+        n = 8 * (gran // K + (1 if k < gran % K else 0))
+        np.testing.assert_array_equal(a[off:off + n], oracle.multinomial_cond(oracle.Engine(77 + 4 * k), w, trials, n))
+        off += n
+    if dim > 1:
+        assert (a.sum(axis=1) == trials).all()
 
 
 # ------------------------------------------------------------------ MvNormal

@@ -69,3 +69,23 @@ def test_bartlett_layout():
     # draw 0: column 0 gets normals 1,2,3 (rows 1..3), column 1 gets 4,5, column 2 gets 6
     assert A[0, 1, 0] == 1 and A[0, 3, 0] == 3 and A[0, 2, 1] == 4 and A[0, 3, 2] == 6
     assert A[1, 1, 0] == 7 and np.all(np.diag(A[0]) == 2) and A[0, 0, 1] == 0
+
+
+def test_multinomial_conditional_oracle_moments(oracle):
+    """The conditional-binomial restatement: every sample sums to trials, and
+    the category totals fit the multinomial (chi-squared); a single category
+    gives 0, as the reference's last-row assignment overwrites row 0."""
+    import numpy as np
+    from scipy.stats import chi2
+    w = np.random.default_rng(4).uniform(0.1, 2.0, 12)
+    trials, samples = 1000, 8 * 2000
+    m = oracle.multinomial_cond(oracle.Engine(9), w, trials, samples)
+    assert (m.sum(axis=1) == trials).all() and m.min() >= 0
+    p = w / w.sum()
+    exp = p * trials * samples
+    stat = ((m.sum(axis=0) - exp) ** 2 / exp).sum()
+    assert chi2.sf(stat, len(w) - 1) > 1e-3, stat
+    assert (oracle.multinomial_cond(oracle.Engine(9), [2.0], 300, 16) == 0).all()
+    v = np.random.default_rng(2).uniform(size=13)
+    s = oracle.eigen_sum_avx(v)
+    assert abs(s - v.sum()) < 1e-14
