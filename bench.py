@@ -479,6 +479,19 @@ def bench_multivariate(er, streams=608):
     mg = er.MultinomialGen(trials, p)
     out = torch.empty((n, K), dtype=torch.int32, device="cuda").t()
     ms = _median_ms(lambda: mg.generate(urng, n, out=out))
+    # TruncMvNormalGen, the 9-dimensional case of the reference's tests, default
+    # burn-in (5 * dim sweeps, one scalar draw per component and chain)
+    c = np.zeros((9, 9))
+    c[0, 1], c[2, 7], c[3, 1] = 0.5, 0.5, 0.7
+    c[np.diag_indices(9)] = [1, 1.2, 1.4, 1.6, 1.8, 1.6, 1.4, 1.2, 1]
+    tg = er.TruncMvNormalGen([-1, 0, 1, 2, 3, 2, 1, 0, -1], c @ c.T,
+                             er.support([-4, -3, -2, -1, 0, -1, -2, -3, -4], [4, 5, 6, 7, 8, 7, 6, 5, 4]))
+    n = 100_000
+    out = torch.empty((n, 9), dtype=torch.float32, device="cuda").t()
+    ms = _median_ms(lambda: tg.generate(urng, n, out=out))
+    res["truncmvnormal_d9_n1e5"] = {"samples": n, "ms": round(ms, 3), "gibbs_steps_g_s":
+                                    round(n * 9 * 45 / (ms / 1e3) / 1e9, 2)}
+    del out
     res["multinomial_k10_t1000_conditional"] = {"draws": n, "ms": round(ms, 3), "mdraws_s": round(n / ms / 1e3, 2),
                                                 "binomial_rows_g_s": round(n * (K - 1) / (ms / 1e3) / 1e9, 2),
                                                 "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}

@@ -41,6 +41,7 @@ __all__ = [
     "MvNormalGen", "WishartGen", "InvWishartGen", "DirichletGen", "MultinomialGen", "makeMvNormalGen",
     "makeMvNormalGenFromLt", "makeWishartGen", "makeWishartGenFromLt", "makeInvWishartGen",
     "makeInvWishartGenFromIlt", "makeDirichletGen", "makeMultinomialGen",
+    "TruncMvNormalGen", "makeTruncMvNormalGen", "makeTruncMvNormalGenFromLt",
 ]
 
 _lib.load()
@@ -893,6 +894,41 @@ class MultinomialGen(_MvGen):
         o = out if out is not None else torch.empty((samples, self.dim), dtype=torch.int32, device="cuda").t()
         _lib.check(_L.gr_multinomial_sample(self._h, urng._h, _ptr(o), samples, _stream_ptr(stream)))
         return o
+
+
+class TruncMvNormalGen(_MvGen):
+    """Eigen::Rand::TruncMvNormalGen<T> (MvDists/TruncMvNormal.h:31-209):
+    TruncMvNormalGen(mean, cov, support(lower, upper), burn_in=0) or, with
+    lower_triangular=True, the covariance's factor.  generate(urng, samples)
+    -> (dim, samples) tensor; each column is a Gibbs chain of burn_in sweeps
+    (0 = 5 * dim)."""
+
+    _prefix = "gr_truncmvn"
+
+    def __init__(self, mean, cov, support, burn_in=0, lower_triangular=False, dtype=torch.float32):
+        m = _host_f64(mean)
+        self.dim = len(m)
+        self.dtype = dtype
+        c = _host_f64(cov, self.dim * self.dim)
+        lo = _host_f64(support.lower, self.dim)
+        hi = _host_f64(support.upper, self.dim)
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_truncmvn_create(ctypes.byref(h), _DT[dtype], self.dim, m, c,
+                                         1 if lower_triangular else 0, lo, hi, int(burn_in)))
+        self._finish(h)
+
+    def generate(self, urng, samples=1, out=None, stream=None):
+        o = out if out is not None else torch.empty((samples, self.dim), dtype=self.dtype, device="cuda").t()
+        _lib.check(_L.gr_truncmvn_sample(self._h, urng._h, _ptr(o), samples, _stream_ptr(stream)))
+        return o
+
+
+def makeTruncMvNormalGen(mean, cov, support, burn_in=0, dtype=torch.float32):
+    return TruncMvNormalGen(mean, cov, support, burn_in, dtype=dtype)
+
+
+def makeTruncMvNormalGenFromLt(mean, lt, support, burn_in=0, dtype=torch.float32):
+    return TruncMvNormalGen(mean, lt, support, burn_in, lower_triangular=True, dtype=dtype)
 
 
 def makeMvNormalGen(mean, cov, dtype=torch.float32):

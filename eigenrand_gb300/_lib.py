@@ -36,6 +36,7 @@ EXPORTS = [
     "gr_mvnormal_create", "gr_mvnormal_sample", "gr_mvnormal_destroy", "gr_wishart_create", "gr_wishart_sample",
     "gr_wishart_destroy", "gr_dirichlet_create", "gr_dirichlet_sample", "gr_dirichlet_destroy",
     "gr_multinomial_create", "gr_multinomial_sample", "gr_multinomial_destroy",
+    "gr_truncmvn_create", "gr_truncmvn_sample", "gr_truncmvn_destroy",
     "gr_server_create", "gr_server_set_mvnormal", "gr_server_submit", "gr_server_progress", "gr_server_read",
     "gr_server_release", "gr_server_pending", "gr_server_now", "gr_server_destroy",
 ]
@@ -152,6 +153,9 @@ def load(path=None):
         "gr_multinomial_create": (i32, [ctypes.POINTER(vp), i32, i32, vp]),
         "gr_multinomial_sample": (i32, [vp, vp, vp, sz, vp]),
         "gr_multinomial_destroy": (i32, [vp]),
+        "gr_truncmvn_create": (i32, [ctypes.POINTER(vp), i32, i32, vp, vp, i32, vp, vp, ctypes.c_int64]),
+        "gr_truncmvn_sample": (i32, [vp, vp, vp, sz, vp]),
+        "gr_truncmvn_destroy": (i32, [vp]),
         "gr_server_create": (i32, [ctypes.POINTER(vp), i32, vp, sz, i32]),
         "gr_server_set_mvnormal": (i32, [vp, i32, vp, vp]),
         "gr_server_submit": (i32, [vp, ctypes.POINTER(Request), ctypes.POINTER(u64)]),

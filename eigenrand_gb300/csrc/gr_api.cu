@@ -641,7 +641,8 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
     // packets per slice, upper bound (caches can only reduce it)
     int opp = 8;
     const int bk = dp.kind >= kVecBase ? dp.kind - kVecBase : dp.kind;
-    if (bk == kRawKind || (dp.dtype == GR_F64 && bk != GR_BALANCED && bk != GR_BALANCED2)) opp = 4;
+    if (bk == kRawKind || bk == kRawLane0Kind || (dp.dtype == GR_F64 && bk != GR_BALANCED && bk != GR_BALANCED2))
+      opp = 4;
     const int ppu = kind_packets_per_unit(dp.kind, dp.dtype);
     int64_t packets_max = (nk_max + opp - 1) / opp;
     if (ppu == 2) packets_max += packets_max & 1;
@@ -1431,6 +1432,33 @@ gr_status engine_reserve(gr_engine* e, int max_segments) {
     e->segwin_words = need;
   }
   if (!e->scratch_gen) GR_CUDA(cudaMalloc(&e->scratch_gen, sizeof(GenState) * (size_t)e->K));
+  return GR_OK;
+}
+
+}  // namespace gr
+
+namespace gr {
+
+gr_status draw_first_words(gr_engine* e, uint64_t* out, int64_t per_sample, int64_t samples, cudaStream_t s) {
+  if (per_sample <= 0 || samples <= 0) return GR_OK;
+  DistParams dp{};
+  dp.kind = kRawLane0Kind;
+  dp.dtype = GR_U64;
+  Plan p{};
+  p.eng = e->st;
+  p.K = e->K;
+  p.gran = (int32_t)(4 * per_sample);  // four (virtual) outputs per packet
+  p.gran_per_k = samples / e->K;
+  p.gran_rem = samples % e->K;
+  p.out = out;
+  const int64_t packets_max = (p.gran_per_k + (p.gran_rem ? 1 : 0)) * per_sample;
+  int S;
+  int64_t J;
+  plan_segments(e, packets_max, 1, S, J);
+  gr_status st = prepare_segments(e, p, S, J, 0, s);
+  if (st != GR_OK) return st;
+  const cudaError_t err = launch_direct(p, dp, e->snap, s);
+  if (err != cudaSuccess) return cuda_fail(err, "scalar draws");
   return GR_OK;
 }
 

@@ -49,6 +49,7 @@ struct GenState {
 constexpr int kPrefixLen = kN + 130 * kM;
 constexpr int kRawKind = 100;  // internal kind id for the raw u64 stream
 constexpr int kBernoulliVKind = 101;  // BernoulliVGen<float>: per-element probability (DistParams::vparam)
+constexpr int kRawLane0Kind = 102;   // lane 0 of every packet only (scalar draws: pfirst of rng()), u64 each
 // Truncated.h inverse-CDF forms: u = UniformRealGen(phi(lower), phi(upper))
 // (slope fa/da, bias fb/db), then the base's inverse CDF with constants
 // fc/dc, fd/dd

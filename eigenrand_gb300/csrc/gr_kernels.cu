@@ -371,11 +371,11 @@ __device__ __forceinline__ double nscale64i(double x, const DistParams& d, int64
 }
 
 // ---------------------------------------------------------------- direct kernel
-enum Mode { M_RAW, M_F32, M_F64, M_W32, M_W64, M_N32, M_N64 };
+enum Mode { M_RAW, M_F32, M_F64, M_W32, M_W64, M_N32, M_N64, M_RAW0 };
 
 template <int MODE>
 struct ModeInfo {
-  static constexpr int OPP = MODE == M_RAW ? 4 : MODE == M_F32 ? 8 : MODE == M_F64 ? 4 : MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : 8;
+  static constexpr int OPP = (MODE == M_RAW || MODE == M_RAW0) ? 4 : MODE == M_F32 ? 8 : MODE == M_F64 ? 4 : MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : 8;
   static constexpr bool kHalfCache = MODE == M_W64;  // randbits handled separately below
   static constexpr int kCacheOut = MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : (MODE == M_W32 || MODE == M_W64) ? 4 : 0;
 };
@@ -481,6 +481,10 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           reinterpret_cast<ulonglong2*>(o)[0] = make_ulonglong2(pk[0], pk[1]);
           reinterpret_cast<ulonglong2*>(o)[1] = make_ulonglong2(pk[2], pk[3]);
         }
+      } else if (MODE == M_RAW0) {
+        // a scalar draw takes the engine's whole packet and keeps its first
+        // element (StdUniformRealGen::operator(), Dists/Basic.h:533-540)
+        if (valid) reinterpret_cast<uint64_t*>(p.out)[obase / 4 + pidx] = pk[0];
       } else if (MODE == M_F32) {
         if (valid) {
           float* o = reinterpret_cast<float*>(p.out) + obase + pidx * 8;
@@ -698,7 +702,7 @@ cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, in
 }
 
 int kind_granule(int kind, int dtype) {
-  if (kind == kRawKind) return 4;
+  if (kind == kRawKind || kind == kRawLane0Kind) return 4;
   if (dtype == GR_F32) return 8;
   return 4;  // double packets and int32 packets hold 4 lanes
 }
@@ -713,6 +717,7 @@ int kind_packets_per_unit(int kind, int dtype) {
 bool kind_is_direct(int kind, int dtype, const DistParams& d) {
   switch (kind) {
     case kRawKind:
+    case kRawLane0Kind:
     case GR_UNIFORM_REAL:
     case GR_UNIFORM_REAL2:
     case GR_BALANCED:
@@ -767,6 +772,7 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
 
 cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s) {
   if (d.kind == kRawKind) return run_direct<M_RAW, kRawKind>(p, d, snap, s);
+  if (d.kind == kRawLane0Kind) return run_direct<M_RAW0, kRawLane0Kind>(p, d, snap, s);
   if (d.dtype == GR_F32) {
     switch (d.kind) {
       GR_F32_CASE(GR_UNIFORM_REAL)

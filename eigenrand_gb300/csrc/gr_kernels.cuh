@@ -155,5 +155,10 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d);
 // Host-side helpers shared by the C ABI translation units (gr_api.cu).
 EngState* engine_state_ptr(gr_engine* e);
 gr_status set_last_error(gr_status s, const std::string& msg);
+// Scalar draws on the packet engine (each takes a whole packet and keeps lane
+// 0): stream k of the engine owns samples [s0_k, s0_k + n_k) of `samples`,
+// split as any call splits them, and makes per_sample * n_k draws in stream
+// order into out[s0_k * per_sample ...].
+gr_status draw_first_words(gr_engine* e, uint64_t* out, int64_t per_sample, int64_t samples, cudaStream_t s);
 
 }  // namespace gr

@@ -83,6 +83,27 @@ struct McArgs {
 };
 cudaError_t launch_mn_cond(const Plan& p, const McArgs& a, cudaStream_t s);
 
+// TruncMvNormalGen's Gibbs chains (gr_tmvn.cu), one thread per chain, steps
+// [t0, t0 + tc) of sweep-major (sweep, component) order.  Arrays are device
+// arrays in the object's type.
+constexpr int kTmvMaxDim = 64;
+struct TmvArgs {
+  const void* H;         // precision matrix, column-major dim x dim
+  const void* mean;
+  const void* lo;
+  const void* hi;
+  const void* inv_diag;  // 1 / H_ii
+  const void* cond_sd;   // sqrt(1 / H_ii)
+  int32_t dim;
+  int32_t K;             // engine streams (chain slices as any call splits them)
+  int64_t samples;
+  int64_t t0, tc;
+  const uint64_t* draws; // stream k's draws of the run: s0_k * tc + (t - t0) * n_k + j
+  void* x;               // dim x samples, the chains' state and the result
+};
+cudaError_t launch_tmvn(int dtype, const TmvArgs& a, cudaStream_t s);
+cudaError_t launch_tmvn_init(int dtype, const void* init, void* x, int dim, int64_t samples, cudaStream_t s);
+
 cudaError_t launch_inverse_f64(double* A, double* W, int d, int32_t* status, cudaStream_t s);
 cudaError_t launch_chol_f64(double* A, int d, int32_t* status, cudaStream_t s);
 cudaError_t launch_jacobi_f64(double* A, double* V, double* L, int d, int32_t* status, cudaStream_t s);

@@ -67,6 +67,33 @@ double eigen_sum_avx(const double* v, int n) {
   return r;
 }
 
+// The constructor's per-dimension values in the scalar type T
+// (TruncMvNormal.h:76-91): H = L^-T L^-1 from the lower triangle of the
+// factor (computed in FP64, then rounded to T), 1 / H_ii, sqrt of that, and
+// clamp(mean, lower, upper).
+template <typename T>
+std::vector<T> tmvn_values(int d, const std::vector<double>& H, const double* mean, const double* lower,
+                           const double* upper) {
+  std::vector<T> v((size_t)d * d + 6 * (size_t)d);
+  T* Ht = v.data();
+  T* mu = Ht + (size_t)d * d;
+  T* lo = mu + d;
+  T* hi = lo + d;
+  T* idg = hi + d;
+  T* csd = idg + d;
+  T* init = csd + d;
+  for (size_t i = 0; i < (size_t)d * d; ++i) Ht[i] = (T)H[i];
+  for (int i = 0; i < d; ++i) {
+    mu[i] = (T)mean[i];
+    lo[i] = (T)lower[i];
+    hi[i] = (T)upper[i];
+    idg[i] = (T)1 / Ht[(size_t)i * d + i];
+    csd[i] = std::sqrt(idg[i]);
+    init[i] = std::max(lo[i], std::min(mu[i], hi[i]));
+  }
+  return v;
+}
+
 bool all_finite(const double* v, size_t n) {
   for (size_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
@@ -206,6 +233,14 @@ struct gr_dirichlet {
   int dim = 0, dtype = GR_F32;
   std::vector<gr_gen*> gammas;
   Scratch scratch;
+};
+
+struct gr_truncmvn {
+  int dim = 0, dtype = GR_F32;
+  int64_t burn_in = 0;
+  // device, the object's type: H (dim x dim), mean, lower, upper, 1/H_ii,
+  // sqrt(1/H_ii), initial state
+  void* buf = nullptr;
 };
 
 struct gr_multinomial {
@@ -457,6 +492,113 @@ gr_status gr_dirichlet_sample(gr_dirichlet* g, gr_engine* e, void* dev_out, size
   cudaError_t err = launch_dirichlet(rows, dev_out, g->dim, (int64_t)samples, g->dtype, (cudaStream_t)stream);
   if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("Dirichlet normalisation: ") + cudaGetErrorString(err));
   return GR_OK;
+}
+
+// ---------------------------------------------------------------- TruncMvNormalGen
+gr_status gr_truncmvn_destroy(gr_truncmvn* g) {
+  if (!g) return GR_OK;
+  cudaFree(g->buf);
+  delete g;
+  return GR_OK;
+}
+
+gr_status gr_truncmvn_create(gr_truncmvn** out, int32_t dtype, int32_t dim, const double* mean, const double* matrix,
+                             int32_t matrix_form, const double* lower, const double* upper, int64_t burn_in) {
+  if (!out || !mean || !matrix || !lower || !upper) return mv_fail(GR_ERR_INVALID, "NULL argument");
+  if (dtype != GR_F32 && dtype != GR_F64) return mv_fail(GR_ERR_INVALID, "TruncMvNormalGen needs a float or double type");
+  if (matrix_form != GR_MATRIX_FULL && matrix_form != GR_MATRIX_LOWER) return mv_fail(GR_ERR_INVALID, "bad matrix form");
+  if (dim < 1 || dim > kTmvMaxDim) return mv_fail(GR_ERR_UNSUPPORTED, "TruncMvNormalGen: 1 <= dim <= 64");
+  if (burn_in < 0) return mv_fail(GR_ERR_INVALID, "burn_in must be >= 0");
+  if (!all_finite(mean, dim) || !all_finite(matrix, (size_t)dim * dim))
+    return mv_fail(GR_ERR_INVALID, "non-finite mean or matrix");
+  for (int i = 0; i < dim; ++i) {
+    const bool ok = dtype == GR_F32 ? (float)lower[i] < (float)upper[i] : lower[i] < upper[i];
+    if (!ok) return mv_fail(GR_ERR_INVALID, "support needs lower[i] < upper[i]");
+  }
+  const size_t dd = (size_t)dim * dim;
+  double* Ldev = nullptr;
+  int tri = 1;
+  gr_status st = factor_f64(dim, matrix, matrix_form, false, &Ldev, &tri);
+  if (st != GR_OK) return st;
+  std::vector<double> L(dd);
+  cudaError_t e = cudaMemcpy(L.data(), Ldev, sizeof(double) * dd, cudaMemcpyDeviceToHost);
+  cudaFree(Ldev);
+  if (e != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("factor download: ") + cudaGetErrorString(e));
+  // inv = lower(L)^-1 by forward substitution, column by column; H = inv^T inv
+  std::vector<double> inv(dd, 0.0), H(dd, 0.0);
+  for (int c = 0; c < dim; ++c)
+    for (int r = c; r < dim; ++r) {
+      double v = r == c ? 1.0 : 0.0;
+      for (int k = c; k < r; ++k) v -= L[(size_t)k * dim + r] * inv[(size_t)c * dim + k];
+      inv[(size_t)c * dim + r] = v / L[(size_t)r * dim + r];
+    }
+  for (int j = 0; j < dim; ++j)
+    for (int i = 0; i < dim; ++i) {
+      double v = 0.0;
+      for (int k = std::max(i, j); k < dim; ++k) v += inv[(size_t)i * dim + k] * inv[(size_t)j * dim + k];
+      H[(size_t)j * dim + i] = v;
+    }
+  if (!all_finite(H.data(), dd)) return mv_fail(GR_ERR_NOT_PD, "the covariance factor is singular");
+  gr_truncmvn* g = new gr_truncmvn;
+  g->dim = dim;
+  g->dtype = dtype;
+  g->burn_in = burn_in == 0 ? 5 * (int64_t)dim : burn_in;
+  if (dtype == GR_F32) {
+    const std::vector<float> v = tmvn_values<float>(dim, H, mean, lower, upper);
+    e = cudaMalloc(&g->buf, sizeof(float) * v.size());
+    if (e == cudaSuccess) e = cudaMemcpy(g->buf, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice);
+  } else {
+    const std::vector<double> v = tmvn_values<double>(dim, H, mean, lower, upper);
+    e = cudaMalloc(&g->buf, sizeof(double) * v.size());
+    if (e == cudaSuccess) e = cudaMemcpy(g->buf, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    gr_truncmvn_destroy(g);
+    return mv_fail(GR_ERR_CUDA, std::string("TruncMvNormalGen set-up: ") + cudaGetErrorString(e));
+  }
+  *out = g;
+  return GR_OK;
+}
+
+gr_status gr_truncmvn_sample(gr_truncmvn* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (samples == 0) return GR_OK;
+  if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int d = g->dim;
+  const size_t es = elem_size(g->dtype);
+  const char* b = static_cast<const char*>(g->buf);
+  TmvArgs a{};
+  a.H = b;
+  a.mean = b + es * (size_t)d * d;
+  a.lo = b + es * ((size_t)d * d + d);
+  a.hi = b + es * ((size_t)d * d + 2 * d);
+  a.inv_diag = b + es * ((size_t)d * d + 3 * d);
+  a.cond_sd = b + es * ((size_t)d * d + 4 * d);
+  const void* init = b + es * ((size_t)d * d + 5 * d);
+  a.dim = d;
+  a.K = gr_engine_streams(e);
+  a.samples = (int64_t)samples;
+  a.x = dev_out;
+  MV_CUDA(launch_tmvn_init(g->dtype, init, dev_out, d, (int64_t)samples, s));
+  // the draws of up to 2^25 (step, chain) pairs at a time
+  const int64_t steps = g->burn_in * d;
+  const int64_t tc = std::max<int64_t>(1, std::min<int64_t>(steps, ((int64_t)1 << 25) / (int64_t)samples));
+  uint64_t* draws = nullptr;
+  MV_CUDA(cudaMallocAsync(&draws, sizeof(uint64_t) * (size_t)tc * samples, s));
+  gr_status st = GR_OK;
+  for (int64_t t0 = 0; t0 < steps && st == GR_OK; t0 += tc) {
+    const int64_t n = std::min(tc, steps - t0);
+    st = draw_first_words(e, draws, n, (int64_t)samples, s);
+    if (st != GR_OK) break;
+    a.t0 = t0;
+    a.tc = n;
+    a.draws = draws;
+    const cudaError_t err = launch_tmvn(g->dtype, a, s);
+    if (err != cudaSuccess) st = mv_fail(GR_ERR_CUDA, std::string("TruncMvNormal kernel: ") + cudaGetErrorString(err));
+  }
+  cudaFreeAsync(draws, s);
+  return st;
 }
 
 // ---------------------------------------------------------------- MultinomialGen

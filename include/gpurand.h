@@ -259,13 +259,28 @@ gr_status gr_dirichlet_destroy(gr_dirichlet* g);
 
 /* MultinomialGen<int32_t>(trials, weights) (Multinomial.h:25-118), weights
  * >= 0.  sample: dev_out = int32 dim x samples column-major, bit-exact with
- * the reference.  Implemented for trials < max(30 (dim - 1), 100) (the
- * reference's per-trial DiscreteGen path) with trials <= 2400; the
- * conditional-binomial path above that returns GR_ERR_UNSUPPORTED. */
+ * the reference.  trials < max(30 (dim - 1), 100): the per-trial DiscreteGen
+ * path (trials <= 2400); above: the conditional-binomial path
+ * (BinomialVGen<float> row by row), which needs samples % 8 == 0. */
 gr_status gr_multinomial_create(gr_multinomial** out, int32_t dim, int32_t trials, const double* weights);
 gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_out, size_t samples,
                                 gr_stream_t stream);
 gr_status gr_multinomial_destroy(gr_multinomial* g);
+
+/* TruncMvNormalGen<T>(mean, cov | lt, support(lower, upper), burn_in)
+ * (MvDists/TruncMvNormal.h:31-209): Gibbs chains, one per sample, through the
+ * precision matrix; burn_in sweeps (0 = 5 * dim).  The factor comes from
+ * get_lt (GR_MATRIX_FULL) or is the given lower triangle (GR_MATRIX_LOWER);
+ * the precision matrix is computed in FP64 and rounded to T.  dim <= 64,
+ * lower[i] < upper[i].  sample: dev_out = dim x samples column-major; the
+ * draws are the reference's scalar draws (one engine packet each).  Values
+ * match the reference within the rounding of erfc and of the dot products
+ * (tolerance stated in the tests), not bit for bit. */
+typedef struct gr_truncmvn gr_truncmvn;
+gr_status gr_truncmvn_create(gr_truncmvn** out, int32_t dtype, int32_t dim, const double* mean, const double* matrix,
+                             int32_t matrix_form, const double* lower, const double* upper, int64_t burn_in);
+gr_status gr_truncmvn_sample(gr_truncmvn* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream);
+gr_status gr_truncmvn_destroy(gr_truncmvn* g);
 
 /* ---- serving loop ----------------------------------------------------------
  * No counterpart in the reference (EigenRand is a library called in-process);

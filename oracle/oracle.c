@@ -1719,3 +1719,87 @@ int or_vop_set(uint64_t seed, int kind, double a, double b, int32_t trials, void
   or_vmt_free(e);
   return rc;
 }
+
+/* ======================================================================
+ * TruncMvNormalGen::generate(urng, samples), TruncMvNormal.h:171-209, with
+ * the precision matrix H given (column-major, FP64, rounded here to the
+ * scalar type).  Draws are StdUniformRealGen's scalar draws: one packet each,
+ * its first 32-bit word (float) or 64-bit lane (double) (Basic.h:533-540).
+ * out = dim x samples, column-major.
+ * ====================================================================== */
+int or_gen_truncmvn(or_vmt* e, int dtype, int dim, const double* H, const double* mean, const double* lower,
+                    const double* upper, int64_t burn_in, void* out, size_t samples) {
+  if (e->L != 4 || dim < 1 || dim > 64) return 2;
+  const int dbl = dtype == 1;
+  const int64_t sweeps = burn_in == 0 ? 5 * (int64_t)dim : burn_in;
+  const size_t n = (size_t)dim * samples;
+  if (dbl) {
+    double *x = (double*)out, *df = (double*)malloc(sizeof(double) * (n ? n : 1)), idg[64], csd[64];
+    for (int i = 0; i < dim; ++i) {
+      idg[i] = 1.0 / H[(size_t)i * dim + i];
+      csd[i] = sqrt(idg[i]);
+    }
+    for (size_t q = 0; q < samples; ++q)
+      for (int i = 0; i < dim; ++i) {
+        const double m = mean[i], lo = lower[i], hi = upper[i];
+        x[q * dim + i] = lo > (m < hi ? m : hi) ? lo : (m < hi ? m : hi);
+        df[q * dim + i] = x[q * dim + i] - m;
+      }
+    for (int64_t sw = 0; sw < sweeps; ++sw)
+      for (int i = 0; i < dim; ++i)
+        for (size_t q = 0; q < samples; ++q) {
+          double* xd = df + q * dim;
+          double h = H[i] * xd[0];
+          for (int j = 1; j < dim; ++j) h = h + H[(size_t)j * dim + i] * xd[j];
+          const double cm = mean[i] - idg[i] * (h - H[(size_t)i * dim + i] * xd[i]);
+          const double an = (lower[i] - cm) / csd[i], bn = (upper[i] - cm) / csd[i];
+          const double pa = 0.5 * erfc(-an * (1.0 / 1.4142135623730951));
+          const double pb = 0.5 * erfc(-bn * (1.0 / 1.4142135623730951));
+          uint64_t r[4];
+          vmt_packet(e, r);
+          const double u = pa + (pb - pa) * bit_ur_d(r[0]);
+          const double z = -1.4142135623730951 * or_erfinv(1.0 - 2.0 * u);
+          const double nx = z * csd[i] + cm;
+          xd[i] = nx - mean[i];
+          x[q * dim + i] = nx;
+        }
+    free(df);
+  } else {
+    float *x = (float*)out, *df = (float*)malloc(sizeof(float) * (n ? n : 1)), Hf[64 * 64], mf[64], lf[64], hf[64],
+          idg[64], csd[64];
+    for (int i = 0; i < dim * dim; ++i) Hf[i] = (float)H[i];
+    for (int i = 0; i < dim; ++i) {
+      mf[i] = (float)mean[i];
+      lf[i] = (float)lower[i];
+      hf[i] = (float)upper[i];
+      idg[i] = 1.0f / Hf[i * dim + i];
+      csd[i] = sqrtf(idg[i]);
+    }
+    for (size_t q = 0; q < samples; ++q)
+      for (int i = 0; i < dim; ++i) {
+        const float c = mf[i] < hf[i] ? mf[i] : hf[i];
+        x[q * dim + i] = lf[i] > c ? lf[i] : c;
+        df[q * dim + i] = x[q * dim + i] - mf[i];
+      }
+    const float rs2 = (float)(1.0 / 1.4142135623730951);
+    for (int64_t sw = 0; sw < sweeps; ++sw)
+      for (int i = 0; i < dim; ++i)
+        for (size_t q = 0; q < samples; ++q) {
+          float* xd = df + q * dim;
+          float h = Hf[i] * xd[0];
+          for (int j = 1; j < dim; ++j) h = h + Hf[j * dim + i] * xd[j];
+          const float cm = mf[i] - idg[i] * (h - Hf[i * dim + i] * xd[i]);
+          const float an = (lf[i] - cm) / csd[i], bn = (hf[i] - cm) / csd[i];
+          const float pa = 0.5f * erfcf(-an * rs2), pb = 0.5f * erfcf(-bn * rs2);
+          uint64_t r[4];
+          vmt_packet(e, r);
+          const float u = pa + (pb - pa) * bit_ur_f((uint32_t)r[0]);
+          const float z = (float)-1.4142135623730951 * or_erfinvf(1.0f - 2.0f * u);
+          const float nx = z * csd[i] + cm;
+          xd[i] = nx - mf[i];
+          x[q * dim + i] = nx;
+        }
+    free(df);
+  }
+  return 0;
+}

@@ -128,6 +128,9 @@ int or_gen_multinomial(or_vmt* e, or_gen* g, const or_discrete* d, int32_t trial
 
 /* vectorize-over-params */
 int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out);
+/* TruncMvNormalGen Gibbs chains with the precision matrix H (FP64, column-major) */
+int or_gen_truncmvn(or_vmt* e, int dtype, int dim, const double* H, const double* mean, const double* lower,
+                    const double* upper, int64_t burn_in, void* out, size_t samples);
 /* MultinomialGen, conditional-binomial path (trials >= max(30 (dim-1), 100)) */
 double or_eigen_sum_avx(const double* v, int n);
 int or_gen_multinomial_cond(or_vmt* e, const double* w, int32_t dim, int32_t trials, int32_t* out,

@@ -72,6 +72,8 @@ def lib():
         L.or_gen_multinomial.restype = ctypes.c_int
         L.or_gen_multinomial_cond.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
         L.or_gen_multinomial_cond.restype = ctypes.c_int
+        L.or_gen_truncmvn.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, ctypes.c_int64, vp, sz]
+        L.or_gen_truncmvn.restype = ctypes.c_int
         L.or_eigen_sum_avx.argtypes = [vp, ctypes.c_int]
         L.or_eigen_sum_avx.restype = ctypes.c_double
         L.or_vop_set.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
@@ -247,6 +249,30 @@ def multinomial_cond(eng, weights, trials, samples):
     w = np.ascontiguousarray(weights, dtype=np.float64)
     out = np.empty((samples, len(w)), dtype=np.int32)
     rc = L.or_gen_multinomial_cond(eng.h, _p(w), len(w), int(trials), _p(out), samples)
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return out
+
+
+def precision_from_lt(lt):
+    """H = L^-T L^-1 from the lower triangle of the factor, FP64."""
+    Lt = np.tril(np.asarray(lt, np.float64))
+    inv = np.linalg.solve(Lt, np.eye(len(Lt)))
+    return inv.T @ inv
+
+
+def truncmvn(eng, mean, cov, lower, upper, samples, burn_in=0, dtype=np.float32, lower_triangular=False):
+    """TruncMvNormalGen(mean, cov | lt, support(lower, upper), burn_in).generate(urng, samples)
+    (TruncMvNormal.h:171-209) with the factor of get_lt in FP64.  Returns (samples, dim)."""
+    L = lib()
+    lt = np.asarray(cov, np.float64) if lower_triangular else get_lt(cov)
+    H = np.ascontiguousarray(precision_from_lt(lt).T)  # column-major
+    m = np.ascontiguousarray(mean, np.float64)
+    lo = np.ascontiguousarray(lower, np.float64)
+    hi = np.ascontiguousarray(upper, np.float64)
+    out = np.empty((samples, len(m)), dtype=dtype)
+    rc = L.or_gen_truncmvn(eng.h, 1 if dtype == np.float64 else 0, len(m), _p(H), _p(m), _p(lo), _p(hi),
+                           int(burn_in), _p(out), samples)
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return out

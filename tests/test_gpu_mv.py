@@ -334,3 +334,72 @@ def test_dirichlet_moments(er):
     m = alpha / a0
     sd = np.sqrt(m * (1 - m) / (a0 + 1) / n)
     assert np.max(np.abs(x.mean(axis=0) - m) / sd) < 6
+
+
+# ------------------------------------------------------------------ TruncMvNormal
+TMVN_CASES = {
+    # test_mv.cpp:224-256 / :392-434 (truncMvNormal, truncMvNormalFromLt)
+    "basic": ([1, 2, 3], [[1.0, 0.3, 0.1], [0.3, 1.2, 0.2], [0.1, 0.2, 0.8]], [-1, 0, 1], [5, 5, 6], 0),
+    # :258-303 (truncMvNormalTight, 50 sweeps)
+    "tight": ([0, 0, 0], [[1.0, 0.5, 0.0], [0.5, 1.0, 0.5], [0.0, 0.5, 1.0]], [0.5] * 3, [1.5] * 3, 50),
+    # :305-353 (truncMvNormalOneSided)
+    "one_sided": ([0, 0, 0], [[1.0, 0.3, 0.0], [0.3, 1.0, 0.3], [0.0, 0.3, 1.0]], [0] * 3, [100] * 3, 0),
+}
+
+
+def _highdim_case():
+    """test_mv.cpp:355-390 (truncMvNormalHighDim)."""
+    c = np.zeros((9, 9))
+    c[0, 1], c[2, 7], c[3, 1] = 0.5, 0.5, 0.7
+    c[np.diag_indices(9)] = [1, 1.2, 1.4, 1.6, 1.8, 1.6, 1.4, 1.2, 1]
+    return ([-1, 0, 1, 2, 3, 2, 1, 0, -1], c @ c.T, [-4, -3, -2, -1, 0, -1, -2, -3, -4], [4, 5, 6, 7, 8, 7, 6, 5, 4], 0)
+
+
+TMVN_CASES["high_dim"] = _highdim_case()
+
+
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+@pytest.mark.parametrize("name", sorted(TMVN_CASES))
+def test_truncmvn_matches_oracle(er, oracle, name, tdt):
+    """Gibbs chains against the oracle on the same draws: every value within
+    the support, and within the rounding of erfc and of the dot products
+    (CUDA's erfc here, the C library's in the oracle: |diff| <= 1e-3 (1+|x|)
+    float, 1e-7 (1+|x|) double, median far below); consecutive calls carry the
+    engine; a multi-stream engine gives engine seed + 4k to slice k."""
+    mean, cov, lo, hi, burn = TMVN_CASES[name]
+    npt = NPD[tdt]
+    tol = 1e-3 if tdt == torch.float32 else 1e-7
+    g = er.TruncMvNormalGen(mean, cov, er.support(lo, hi), burn, dtype=tdt)
+    u = er.Vmt19937_64(42)
+    e = oracle.Engine(42)
+    for samples in (4096, 40):
+        x = rows(g.generate(u, samples)).astype(np.float64)
+        ref = oracle.truncmvn(e, mean, cov, lo, hi, samples, burn, npt).astype(np.float64)
+        err = np.abs(x - ref) / (1 + np.abs(ref))
+        assert err.max() <= tol and np.median(err) <= tol / 100, (err.max(), np.median(err))
+        slack = 1e-5 if tdt == torch.float32 else 1e-12
+        assert (x >= np.array(lo) - slack).all() and (x <= np.array(hi) + slack).all()
+    if name == "tight":
+        assert np.unique(x[:, 0]).size > 1
+    K, samples = 3, 1001
+    x = rows(g.generate(er.Vmt19937_64(7, streams=K), samples)).astype(np.float64)
+    off = 0
+    for k in range(K):
+        n = samples // K + (1 if k < samples % K else 0)
+        ref = oracle.truncmvn(oracle.Engine(7 + 4 * k), mean, cov, lo, hi, n, burn, npt).astype(np.float64)
+        assert (np.abs(x[off:off + n] - ref) / (1 + np.abs(ref))).max() <= tol
+        off += n
+
+
+def test_truncmvn_from_lt_and_errors(er, oracle):
+    """makeTruncMvNormalGenFromLt gives the covariance constructor's chains
+    (test_mv.cpp:392-434); bad supports and dimensions are refused."""
+    mean, cov, lo, hi, _ = TMVN_CASES["basic"]
+    lt = np.linalg.cholesky(np.asarray(cov))
+    a = rows(er.makeTruncMvNormalGenFromLt(mean, lt, er.support(lo, hi)).generate(er.Vmt19937_64(42), 2048))
+    b = rows(er.makeTruncMvNormalGen(mean, cov, er.support(lo, hi)).generate(er.Vmt19937_64(42), 2048))
+    assert np.abs(a - b).max() <= 1e-3 * (1 + np.abs(b).max())
+    with pytest.raises(er.GrError):
+        er.TruncMvNormalGen(mean, cov, er.support([0, 0, 5], [1, 1, 1]))
+    with pytest.raises(er.GrError):
+        er.TruncMvNormalGen(np.zeros(65), np.eye(65), er.support(-np.ones(65), np.ones(65)))

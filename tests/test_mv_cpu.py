@@ -89,3 +89,30 @@ def test_multinomial_conditional_oracle_moments(oracle):
     v = np.random.default_rng(2).uniform(size=13)
     s = oracle.eigen_sum_avx(v)
     assert abs(s - v.sum()) < 1e-14
+
+
+def test_truncmvn_oracle_bounds_and_symmetry(oracle):
+    """TruncMvNormalGen restatement: every chain inside the support, and the
+    one-sided case's symmetry E[X0] = E[X2] (test_mv.cpp:305-333); the mean
+    lies above the marginal truncated-normal mean there."""
+    import numpy as np
+    mean, lo, hi = [0, 0, 0], [0, 0, 0], [100, 100, 100]
+    cov = [[1.0, 0.3, 0.0], [0.3, 1.0, 0.3], [0.0, 0.3, 1.0]]
+    x = oracle.truncmvn(oracle.Engine(54321), mean, cov, lo, hi, 50000, burn_in=30, dtype=np.float64)
+    assert (x >= 0).all() and (x <= 100).all()
+    m = x.mean(axis=0)
+    assert abs(m[0] - m[2]) < 0.02, m
+    assert (m > np.sqrt(2 / np.pi) - 0.01).all(), m
+
+
+def test_truncmvn_host_validation(gpulib):
+    """Refused before any device work: inverted supports, dim above 64,
+    negative burn-in."""
+    import numpy as np
+    er = gpulib
+    with pytest.raises(er.GrError):
+        er.TruncMvNormalGen([0, 0], np.eye(2), er.support([1, 0], [0, 1]))
+    with pytest.raises(er.GrError):
+        er.TruncMvNormalGen(np.zeros(65), np.eye(65), er.support(-np.ones(65), np.ones(65)))
+    with pytest.raises(er.GrError):
+        er.TruncMvNormalGen([0, 0], np.eye(2), er.support([0, 0], [1, 1]), burn_in=-1)
