@@ -25,7 +25,7 @@ from . import _lib
 from ._lib import GrError, KINDS, F32, F64, I32, U64
 
 __all__ = [
-    "GrError", "Vmt19937_64", "raw_u64", "version",
+    "GrError", "Vmt19937_64", "mt19937_64", "P8_mt19937_64", "raw_u64", "version",
     "uniformReal", "balanced", "normal", "lognormal", "exponential", "cauchy", "weibull", "extremeValue",
     "gamma", "beta", "studentT", "chiSquared", "poisson", "binomial", "discrete", "randBits", "bernoulli",
     "geometric", "fisherF", "uniformInt", "negativeBinomial",
@@ -102,6 +102,41 @@ class Vmt19937_64:
         _lib.check(_L.gr_engine_sync(self._h, _stream_ptr(stream)))
 
 
+class _ScalarEngine:
+    """A scalar engine as the Urng (gr_sengine): its packets come from
+    RawbitsMaker<..., scalar_fullbit> over its 64-bit draws.  Fixed-draw
+    kinds only (the free functions and cacheless generator objects)."""
+
+    _kind = None
+
+    def __init__(self, seed=5489):
+        h = ctypes.c_void_p()
+        _lib.check(_L.gr_sengine_create(ctypes.byref(h), self._kind, ctypes.c_uint64(seed)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _L is not None:
+            _L.gr_sengine_destroy(h)
+            self._h = None
+
+    def raw(self, n, out=None, stream=None):
+        """operator()() n times; an int64 tensor of the uint64 bit patterns."""
+        o = out if out is not None else torch.empty(n, dtype=torch.int64, device="cuda")
+        _lib.check(_L.gr_sengine_raw_u64(self._h, _ptr(o), n, _stream_ptr(stream)))
+        return o
+
+
+class mt19937_64(_ScalarEngine):
+    """std::mt19937_64(seed) as EigenRand's Urng."""
+    _kind = 1
+
+
+class P8_mt19937_64(_ScalarEngine):
+    """Eigen::Rand::P8_mt19937_64(seed) (PacketRandomEngine.h:600-607)."""
+    _kind = 2
+
+
 def _empty(rows, cols, dtype, out):
     if out is not None:
         return out
@@ -159,6 +194,12 @@ class _Gen:
 
     def generate(self, rows, cols, urng, out=None, stream=None):
         o = _empty(rows, cols, self.dtype, out)
+        if isinstance(urng, _ScalarEngine):
+            if self._desc.kind in (KINDS["NORMAL_STD"], KINDS["NORMAL"], KINDS["LOGNORMAL"]):
+                raise GrError(3, "a generator object with a cache on a scalar engine; use the free function")
+            _lib.check(_L.gr_sengine_sample(urng._h, ctypes.byref(self._desc), _ptr(o), rows * cols,
+                                            _stream_ptr(stream)))
+            return o
         _lib.check(_L.gr_generate(self._h, urng._h, _ptr(o), rows * cols, _stream_ptr(stream)))
         return o
 
@@ -169,7 +210,8 @@ class _Gen:
 def _sample(kind, rows, cols, urng, dtype, a=0.0, b=0.0, trials=0, weights=None, out=None, stream=None):
     o = _empty(rows, cols, dtype, out)
     d, keep = _desc(kind, dtype, a, b, trials, weights)
-    _lib.check(_L.gr_sample(urng._h, ctypes.byref(d), _ptr(o), rows * cols, _stream_ptr(stream)))
+    fn = _L.gr_sengine_sample if isinstance(urng, _ScalarEngine) else _L.gr_sample
+    _lib.check(fn(urng._h, ctypes.byref(d), _ptr(o), rows * cols, _stream_ptr(stream)))
     del keep
     return o
 

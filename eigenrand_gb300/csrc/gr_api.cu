@@ -118,6 +118,20 @@ struct gr_gen {
   int64_t trunc_lanes = 0, trunc_acc = 0;
 };
 
+// A scalar engine as EigenRand's Urng.  std::mt19937_64(seed) is lane 0 of
+// Vmt19937_64(seed) (PacketRandomEngine.h:230-239 seeds lane l with seed +
+// l): a one-stream packet engine whose lane-0 words are the stream.
+// P8_mt19937_64(seed) (:600-607) hands out the four lanes of a packet of
+// Vmt19937_64(seed) and then of Vmt19937_64(seed + 4) in turn (:465-496): a
+// two-stream packet engine (streams seed + 4k) plus the eight lanes being
+// handed out and how many are gone.
+struct gr_sengine {
+  int kind = 0;
+  gr_engine* eng = nullptr;
+  uint64_t* pbuf = nullptr;  // P8: the current eight lanes (device)
+  int cnt = 8;               // P8: lanes of pbuf handed out (8: none left)
+};
+
 namespace gr {
 EngState* engine_state_ptr(gr_engine* e) { return e ? e->st : nullptr; }
 gr_status set_last_error(gr_status s, const std::string& msg) { return fail(s, msg); }
@@ -1463,3 +1477,131 @@ gr_status draw_first_words(gr_engine* e, uint64_t* out, int64_t per_sample, int6
 }
 
 }  // namespace gr
+
+// ---- scalar engines ------------------------------------------------------------
+namespace {
+
+__global__ void k_p8_words(const uint64_t* pbuf, int cnt, int64_t from_buf, const uint64_t* fresh, int64_t R,
+                           uint64_t* out, int64_t W) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= W) return;
+  if (i < from_buf) {
+    out[i] = pbuf[cnt + i];
+    return;
+  }
+  const int64_t q = i - from_buf, r = q / 8, j = q % 8;
+  out[i] = j < 4 ? fresh[4 * r + j] : fresh[4 * R + 4 * r + (j - 4)];
+}
+
+__global__ void k_p8_keep(uint64_t* pbuf, const uint64_t* fresh, int64_t R) {
+  const int j = threadIdx.x;
+  if (j < 8) pbuf[j] = j < 4 ? fresh[4 * (R - 1) + j] : fresh[4 * R + 4 * (R - 1) + (j - 4)];
+}
+
+// The next W 64-bit draws of the scalar engine into out (device).
+gr_status sengine_words(gr_sengine* se, uint64_t* out, int64_t W, cudaStream_t s) {
+  if (W <= 0) return GR_OK;
+  if (se->kind == GR_SCALAR_MT19937_64) {
+    for (int64_t done = 0; done < W;) {  // a call's granule counts outputs in int32
+      const int64_t c = std::min<int64_t>(W - done, (int64_t)1 << 28);
+      const gr_status st = draw_first_words(se->eng, out + done, c, 1, s);
+      if (st != GR_OK) return st;
+      done += c;
+    }
+    return GR_OK;
+  }
+  const int64_t from_buf = std::min<int64_t>(W, 8 - se->cnt), rest = W - from_buf;
+  const int64_t R = (rest + 7) / 8;  // new packets from each of the two engines
+  uint64_t* fresh = nullptr;
+  if (R > 0) {
+    GR_CUDA(cudaMallocAsync(&fresh, sizeof(uint64_t) * 8 * (size_t)R, s));
+    DistParams dp{};
+    dp.kind = kRawKind;
+    dp.dtype = GR_U64;
+    // two streams: stream 0's 4R words, then stream 1's
+    const gr_status st = run_call(se->eng, nullptr, dp, fresh, (size_t)(8 * R), s);
+    if (st != GR_OK) {
+      cudaFreeAsync(fresh, s);
+      return st;
+    }
+  }
+  k_p8_words<<<(unsigned)((W + 255) / 256), 256, 0, s>>>(se->pbuf, se->cnt, from_buf, fresh, R, out, W);
+  cudaError_t err = cudaGetLastError();
+  if (R > 0) {
+    if (err == cudaSuccess) {
+      k_p8_keep<<<1, 32, 0, s>>>(se->pbuf, fresh, R);
+      err = cudaGetLastError();
+    }
+    cudaFreeAsync(fresh, s);
+    se->cnt = (int)(rest - 8 * (R - 1));
+  } else {
+    se->cnt += (int)W;
+  }
+  if (err != cudaSuccess) return cuda_fail(err, "scalar engine words");
+  return GR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gr_status gr_sengine_create(gr_sengine** out, int32_t kind, uint64_t seed) {
+  if (!out) return fail(GR_ERR_INVALID, "NULL argument");
+  if (kind != GR_SCALAR_MT19937_64 && kind != GR_SCALAR_P8_MT19937_64)
+    return fail(GR_ERR_INVALID, "scalar engine kind: GR_SCALAR_MT19937_64 or GR_SCALAR_P8_MT19937_64");
+  gr_sengine* se = new gr_sengine;
+  se->kind = kind;
+  gr_status st = gr_engine_create(&se->eng, seed, 4, kind == GR_SCALAR_P8_MT19937_64 ? 2 : 1);
+  if (st == GR_OK && kind == GR_SCALAR_P8_MT19937_64 && cudaMalloc(&se->pbuf, sizeof(uint64_t) * 8) != cudaSuccess)
+    st = fail(GR_ERR_NOMEM, "scalar engine buffer");
+  if (st != GR_OK) {
+    gr_sengine_destroy(se);
+    return st;
+  }
+  *out = se;
+  return GR_OK;
+}
+
+gr_status gr_sengine_destroy(gr_sengine* se) {
+  if (!se) return GR_OK;
+  cudaFree(se->pbuf);
+  gr_engine_destroy(se->eng);
+  delete se;
+  return GR_OK;
+}
+
+gr_status gr_sengine_raw_u64(gr_sengine* se, uint64_t* dev_out, size_t n, gr_stream_t stream) {
+  if (!se || (n && !dev_out)) return fail(GR_ERR_INVALID, "NULL argument");
+  return sengine_words(se, dev_out, (int64_t)n, (cudaStream_t)stream);
+}
+
+gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream) {
+  if (!se || !desc) return fail(GR_ERR_INVALID, "NULL argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  DistParams dp{};
+  gr_status st = make_params(*desc, dp);
+  if (st != GR_OK) return st;
+  const int wpp = scalar_words_per_packet(dp.kind, dp.dtype);
+  if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
+    return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
+                                    "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
+                                    "randBits)");
+  const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
+  if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
+  if (n == 0) return GR_OK;
+  if (!dev_out) return fail(GR_ERR_INVALID, "output is NULL");
+  const int64_t npk = (int64_t)n / P;
+  const bool unit2 = dp.kind == GR_NORMAL_STD || dp.kind == GR_NORMAL || dp.kind == GR_LOGNORMAL;
+  const int64_t W = wpp * (unit2 ? 2 * ((npk + 1) / 2) : npk);  // a normal unit draws both packets
+  uint64_t* w = nullptr;
+  GR_CUDA(cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s));
+  st = sengine_words(se, w, W, s);
+  if (st == GR_OK) {
+    const cudaError_t err = launch_scalar_xform(w, dev_out, npk, dp, s);
+    if (err != cudaSuccess) st = cuda_fail(err, "scalar-engine sampling kernel");
+  }
+  cudaFreeAsync(w, s);
+  return st;
+}
+
+}  // extern "C"

@@ -863,4 +863,187 @@ cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* sn
   return cudaErrorNotSupported;
 }
 
+// ---------------------------------------------------------------- scalar engines
+// Samples drawn with a scalar engine as the Urng (std::mt19937_64,
+// P8_mt19937_64): the packets come from RawbitsMaker<Packet8i, Rng, uint64_t,
+// scalar_fullbit> (arch/AVX/RandUtils.h:59-144) and RawbitsMaker<Packet4i,
+// ...> (arch/SSE/RandUtils.h:22-65) over the engine's 64-bit words, with GCC's
+// right-to-left argument evaluation:
+//   S_F32U  uniform_real<Packet8f> = rawbits_34: 3 words (a, b, c) ->
+//           (c.lo, c.hi, b.lo, t0, b.hi, a.lo, a.hi, t1), t0 / t1 the top
+//           bytes of their half's three words (the third twice)
+//   S_F32R  rawbits (zero_to_one, BernoulliGen): 4 words in order, lo / hi
+//   S_F64   rawbits as 4 double lanes
+//   S_F64H  rawbits_half (zero_to_one<Packet4d>): 2 words -> 4 int32 words
+//   S_N32 / S_N64  StdNormalGen units of two uniform packets
+//   S_I32   Packet4i rawbits: 2 words -> 4 int32
+// Packet k of the call reads its words at w[k * wpp]; one thread per packet
+// (per unit for the normal kinds).
+enum SMode { S_F32U, S_F32R, S_F64, S_F64H, S_N32, S_N64, S_I32 };
+
+__device__ __forceinline__ void words34(const uint64_t* w, uint32_t* v8) {
+  const uint64_t a = w[0], b = w[1], c = w[2];
+  const uint32_t v[6] = {(uint32_t)c, (uint32_t)(c >> 32), (uint32_t)b, (uint32_t)(b >> 32), (uint32_t)a,
+                         (uint32_t)(a >> 32)};
+  v8[0] = v[0];
+  v8[1] = v[1];
+  v8[2] = v[2];
+  v8[3] = (v[0] >> 24) | ((v[1] >> 24) << 8) | ((v[2] >> 24) << 16) | ((v[2] >> 24) << 24);
+  v8[4] = v[3];
+  v8[5] = v[4];
+  v8[6] = v[5];
+  v8[7] = (v[3] >> 24) | ((v[4] >> 24) << 8) | ((v[5] >> 24) << 16) | ((v[5] >> 24) << 24);
+}
+
+template <int SM, int KIND>
+__global__ void __launch_bounds__(256) k_sxform(const uint64_t* w, void* out, int64_t npk, DistParams d) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (SM == S_N32 || SM == S_N64) {
+    constexpr int WPP = SM == S_N32 ? 3 : 4;
+    const int64_t u = t;
+    if (2 * u >= npk) return;
+    const uint64_t* w1 = w + 2 * u * WPP;
+    if (SM == S_N32) {
+      uint32_t a[8], b[8];
+      words34(w1, a);
+      words34(w1 + WPP, b);
+      float* o = reinterpret_cast<float*>(out) + 2 * u * 8;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float radius = sqrtf((float)-2 * logf_(1.0f - ur_f(a[q])));
+        float sn, cs;
+        sincosf_((float)(2 * 3.1415926535897932) * ur_f(b[q]), sn, cs);
+        o[q] = nscale32<KIND>(radius * sn, d);
+        if (2 * u + 1 < npk) o[8 + q] = nscale32<KIND>(radius * cs, d);
+      }
+    } else {
+      double* o = reinterpret_cast<double*>(out) + 2 * u * 4;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double radius = sqrt(-2.0 * log_(one_minus_ur_d(w1[q])));
+        double sn, cs;
+        sincos_((2 * 3.1415926535897932) * ur_d(w1[WPP + q]), sn, cs);
+        o[q] = nscale64<KIND>(radius * sn, d);
+        if (2 * u + 1 < npk) o[4 + q] = nscale64<KIND>(radius * cs, d);
+      }
+    }
+    return;
+  }
+  if (t >= npk) return;
+  if (SM == S_F32U || SM == S_F32R) {
+    uint32_t v[8];
+    if (SM == S_F32U) {
+      words34(w + 3 * t, v);
+    } else {
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        v[2 * l] = (uint32_t)w[4 * t + l];
+        v[2 * l + 1] = (uint32_t)(w[4 * t + l] >> 32);
+      }
+    }
+    float r[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) r[q] = tf32<KIND>(v[q], d);
+    float4* o = reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + 8 * t);
+    o[0] = make_float4(r[0], r[1], r[2], r[3]);
+    o[1] = make_float4(r[4], r[5], r[6], r[7]);
+  } else if (SM == S_F64) {
+    double r[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) r[l] = tf64<KIND>(w[4 * t + l], d);
+    double2* o = reinterpret_cast<double2*>(reinterpret_cast<double*>(out) + 4 * t);
+    o[0] = make_double2(r[0], r[1]);
+    o[1] = make_double2(r[2], r[3]);
+  } else if (SM == S_F64H) {
+    const uint64_t a = w[2 * t], b = w[2 * t + 1];
+    const uint32_t v[4] = {(uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32)};
+    double2* o = reinterpret_cast<double2*>(reinterpret_cast<double*>(out) + 4 * t);
+    o[0] = make_double2(tw64<KIND>(v[0], d), tw64<KIND>(v[1], d));
+    o[1] = make_double2(tw64<KIND>(v[2], d), tw64<KIND>(v[3], d));
+  } else {  // S_I32
+    const uint64_t a = w[2 * t], b = w[2 * t + 1];
+    int4* o = reinterpret_cast<int4*>(reinterpret_cast<int32_t*>(out) + 4 * t);
+    o[0] = make_int4(tw32<KIND>((uint32_t)a, d), tw32<KIND>((uint32_t)(a >> 32), d), tw32<KIND>((uint32_t)b, d),
+                     tw32<KIND>((uint32_t)(b >> 32), d));
+  }
+}
+
+template <int SM, int KIND>
+static cudaError_t run_sx(const uint64_t* w, void* out, int64_t npk, const DistParams& d, cudaStream_t s) {
+  const int64_t threads = (SM == S_N32 || SM == S_N64) ? (npk + 1) / 2 : npk;
+  k_sxform<SM, KIND><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(w, out, npk, d);
+  return cudaGetLastError();
+}
+
+int scalar_words_per_packet(int kind, int dtype) {
+  if (dtype == GR_I32) return kind == GR_RANDBITS ? 2 : 0;
+  const bool bal = kind == GR_BALANCED || kind == GR_BALANCED2;
+  switch (kind) {
+    case GR_UNIFORM_REAL:
+    case GR_UNIFORM_REAL2:
+    case GR_BALANCED:
+    case GR_BALANCED2:
+    case GR_NORMAL_STD:
+    case GR_NORMAL:
+    case GR_LOGNORMAL:
+    case GR_EXPONENTIAL:
+    case GR_CAUCHY:
+    case GR_WEIBULL:
+    case GR_EXTREME_VALUE:
+    case GR_GAMMA:
+    case GR_BERNOULLI:
+      if (dtype == GR_F32) return (bal || kind == GR_BERNOULLI) ? 4 : 3;
+      return bal ? 2 : 4;
+    default:
+      return 0;
+  }
+}
+
+#define GR_SX(SMODE, K) \
+  case K:               \
+    return run_sx<SMODE, K>(w, out, npk, d, s);
+
+cudaError_t launch_scalar_xform(const uint64_t* w, void* out, int64_t npk, const DistParams& d, cudaStream_t s) {
+  if (d.dtype == GR_I32) {
+    if (d.kind == GR_RANDBITS) return run_sx<S_I32, GR_RANDBITS>(w, out, npk, d, s);
+    return cudaErrorNotSupported;
+  }
+  if (d.dtype == GR_F32) {
+    switch (d.kind) {
+      GR_SX(S_F32U, GR_UNIFORM_REAL)
+      GR_SX(S_F32U, GR_UNIFORM_REAL2)
+      GR_SX(S_F32U, GR_EXPONENTIAL)
+      GR_SX(S_F32U, GR_CAUCHY)
+      GR_SX(S_F32U, GR_WEIBULL)
+      GR_SX(S_F32U, GR_EXTREME_VALUE)
+      GR_SX(S_F32U, GR_GAMMA)
+      GR_SX(S_F32R, GR_BALANCED)
+      GR_SX(S_F32R, GR_BALANCED2)
+      GR_SX(S_F32R, GR_BERNOULLI)
+      GR_SX(S_N32, GR_NORMAL_STD)
+      GR_SX(S_N32, GR_NORMAL)
+      GR_SX(S_N32, GR_LOGNORMAL)
+      default:
+        return cudaErrorNotSupported;
+    }
+  }
+  switch (d.kind) {
+    GR_SX(S_F64, GR_UNIFORM_REAL)
+    GR_SX(S_F64, GR_UNIFORM_REAL2)
+    GR_SX(S_F64, GR_EXPONENTIAL)
+    GR_SX(S_F64, GR_CAUCHY)
+    GR_SX(S_F64, GR_WEIBULL)
+    GR_SX(S_F64, GR_EXTREME_VALUE)
+    GR_SX(S_F64, GR_GAMMA)
+    GR_SX(S_F64, GR_BERNOULLI)
+    GR_SX(S_F64H, GR_BALANCED)
+    GR_SX(S_F64H, GR_BALANCED2)
+    GR_SX(S_N64, GR_NORMAL_STD)
+    GR_SX(S_N64, GR_NORMAL)
+    GR_SX(S_N64, GR_LOGNORMAL)
+    default:
+      return cudaErrorNotSupported;
+  }
+}
+
 }  // namespace gr

@@ -110,6 +110,13 @@ cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, 
 // packets for the two GammaGens).
 cudaError_t launch_walk(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s);
 
+// Samples drawn with a scalar engine as the Urng (gr_kernels.cu): npk output
+// packets from the engine's 64-bit words w (scalar_words_per_packet(kind,
+// dtype) words per packet, two packets per StdNormalGen unit).  0 words: the
+// kind has no scalar-engine form here.
+int scalar_words_per_packet(int kind, int dtype);
+cudaError_t launch_scalar_xform(const uint64_t* w, void* out, int64_t npk, const DistParams& d, cudaStream_t s);
+
 // TruncGen's CompressMask filter over M base packets drawn into HBM
 // (gr_trunc.cu).  Writes up to `cap` output packets, updates the carried
 // lanes, and leaves in res: [0] packets emitted, [1] the base packet that

@@ -183,6 +183,26 @@ gr_status gr_sample_v2(gr_engine* e, const gr_dist_desc* desc, const void* dev_a
 gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* dev_b, void* dev_out, size_t n,
                         gr_stream_t stream);
 
+/* ---- scalar engines as the Urng ------------------------------------------
+ * EigenRand also draws from scalar 64-bit engines (RandomEngineType::
+ * scalar_fullbit): std::mt19937_64 and P8_mt19937_64 (PacketRandomEngine.h:
+ * 430-516, 600-607; the engine of the reference's own tests).  Their packets
+ * are built by RawbitsMaker<..., scalar_fullbit> (arch/AVX/RandUtils.h:59-144,
+ * arch/SSE/RandUtils.h:22-65): 3 draws per float uniform packet (rawbits_34),
+ * 4 per double packet, 2 per half packet, in the order GCC evaluates the
+ * intrinsics' arguments (right to left).
+ *   gr_sengine_raw_u64: rng() n times.
+ *   gr_sengine_sample: a fresh generator of a fixed-draw kind (uniformReal,
+ *     balanced, normal, lognormal, exponential, cauchy, weibull,
+ *     extremeValue, gamma with alpha = 1, bernoulli; randBits for int32);
+ *     other kinds return GR_ERR_UNSUPPORTED. */
+typedef struct gr_sengine gr_sengine;
+typedef enum { GR_SCALAR_MT19937_64 = 1, GR_SCALAR_P8_MT19937_64 = 2 } gr_scalar_engine_kind;
+gr_status gr_sengine_create(gr_sengine** out, int32_t kind, uint64_t seed);
+gr_status gr_sengine_destroy(gr_sengine* e);
+gr_status gr_sengine_raw_u64(gr_sengine* e, uint64_t* dev_out, size_t n, gr_stream_t stream);
+gr_status gr_sengine_sample(gr_sengine* e, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream);
+
 /* ---- truncated distributions (EigenRand/Dists/Truncated.h) --------------
  * TruncGen<Base>{base, Support(lower, upper)} (Truncated.h:202-263 and the
  * specialisations :342-964); `base` describes the base generator as for

@@ -114,10 +114,74 @@ void or_vmt_window(const or_vmt* e, uint64_t* out) {
   for (int l = 0; l < e->L; ++l) mt_window(&e->lane[l], out + (size_t)l * MT_N);
 }
 
+/* ======================================================================
+ * Scalar engines as the Urng (RandomEngineType::scalar_fullbit): a
+ * std::mt19937_64, or P8_mt19937_64 = ParallelRandomEngineAdaptor over two
+ * Vmt19937_64(seed), (seed + 4) whose operator() returns the eight lanes of
+ * one packet of each in turn (PacketRandomEngine.h:430-516, 600-607).  While
+ * g_src is set, the packet primitives below draw through
+ * RawbitsMaker<Packet8i, Rng, uint64_t, scalar_fullbit> (arch/AVX/RandUtils.h:
+ * 59-144) instead of the packet engine:
+ *   rawbits      _mm256_set_epi64x(rng(), rng(), rng(), rng())
+ *   rawbits_half _mm_set_epi64x(rng(), rng())
+ *   rawbits_34   _mm256_setr_epi64x(rng(), rng(), rng(), 0), permuted
+ * with GCC's right-to-left argument evaluation (pinned with g++ 13 -mavx2:
+ * set_epi64x puts the k-th call in element k; setr_epi64x puts the first call
+ * in element 2 and the third in element 0).
+ * ====================================================================== */
+static or_seng* g_src = NULL;
+
+static uint64_t src_next(void) {
+  or_seng* s = g_src;
+  if (s->kind == OR_SENG_MT19937_64) return or_mt64_next(&s->mt);
+  if (s->cnt >= 8) {
+    vmt_packet(s->a, s->buf);
+    vmt_packet(s->b, s->buf + 4);
+    s->cnt = 0;
+  }
+  return s->buf[s->cnt++];
+}
+
+or_seng* or_seng_new(int kind, uint64_t seed) {
+  or_seng* s = (or_seng*)calloc(1, sizeof(or_seng));
+  s->kind = kind;
+  if (kind == OR_SENG_MT19937_64) {
+    or_mt64_seed(&s->mt, seed);
+  } else {
+    s->a = or_vmt_new(seed, 4);
+    s->b = or_vmt_new(seed + 4, 4);
+    s->cnt = 8;
+  }
+  return s;
+}
+
+void or_seng_free(or_seng* s) {
+  if (!s) return;
+  or_vmt_free(s->a);
+  or_vmt_free(s->b);
+  free(s);
+}
+
+void or_seng_raw(or_seng* s, uint64_t* out, size_t n) {
+  or_seng* prev = g_src;
+  g_src = s;
+  for (size_t i = 0; i < n; ++i) out[i] = src_next();
+  g_src = prev;
+}
+
+/* rawbits: four 64-bit draws, the k-th in element k */
+static void raw4(or_vmt* e, uint64_t* r) {
+  if (g_src) {
+    for (int l = 0; l < 4; ++l) r[l] = src_next();
+    return;
+  }
+  vmt_packet(e, r);
+}
+
 /* one engine packet viewed as 2L u32 words (Packet8i for L=4) */
 static void draw_full(or_vmt* e, uint32_t* w) {
   uint64_t r[OR_MAXL];
-  vmt_packet(e, r);
+  raw4(e, r);
   for (int l = 0; l < e->L; ++l) {
     w[2 * l] = (uint32_t)r[l];
     w[2 * l + 1] = (uint32_t)(r[l] >> 32);
@@ -127,6 +191,14 @@ static void draw_full(or_vmt* e, uint32_t* w) {
 /* MersenneTwister::half(), PacketRandomEngine.h:325-336: split_two gives the
  * low 128 bits now and caches the high 128 bits. */
 static void draw_half(or_vmt* e, uint32_t* w) {
+  if (g_src) { /* rawbits_half: two draws, the first in element 0 */
+    const uint64_t a = src_next(), b = src_next();
+    w[0] = (uint32_t)a;
+    w[1] = (uint32_t)(a >> 32);
+    w[2] = (uint32_t)b;
+    w[3] = (uint32_t)(b >> 32);
+    return;
+  }
   int hw = e->L; /* words in a half packet */
   if (e->half_valid) {
     e->half_valid = 0;
@@ -152,9 +224,30 @@ static inline double bit_ur_d(uint64_t x) {
   return u2d((x & 0xfffffffffffffull) | (1023ull << 52)) - 1.0;
 }
 
+/* rawbits_34 of a scalar engine: setr_epi64x(first, second, third) lands as
+ * elements (third, second, first); permutevar8x32 (0,1,2,7,3,4,5,7) and
+ * shuffle_epi8 (0..11, 3, 7, 11, 11) per 128-bit half give the words
+ * (c.lo, c.hi, b.lo, t0, b.hi, a.lo, a.hi, t1), a/b/c the first/second/third
+ * draw and t0 / t1 the top bytes of the half's three words (the third one
+ * twice) -- 3 draws for 8 floats, whose low 23 bits are all that is used. */
+static void draw_34(uint32_t* w) {
+  const uint64_t a = src_next(), b = src_next(), c = src_next();
+  const uint32_t v[6] = {(uint32_t)c, (uint32_t)(c >> 32), (uint32_t)b, (uint32_t)(b >> 32), (uint32_t)a,
+                         (uint32_t)(a >> 32)};
+  w[0] = v[0];
+  w[1] = v[1];
+  w[2] = v[2];
+  w[3] = (v[0] >> 24) | ((v[1] >> 24) << 8) | ((v[2] >> 24) << 16) | ((v[2] >> 24) << 24);
+  w[4] = v[3];
+  w[5] = v[4];
+  w[6] = v[5];
+  w[7] = (v[3] >> 24) | ((v[4] >> 24) << 8) | ((v[5] >> 24) << 16) | ((v[5] >> 24) << 24);
+}
+
 static void ur_f8(or_vmt* e, float* u) {
   uint32_t w[8];
-  draw_full(e, w);
+  if (g_src) draw_34(w); /* uniform_real<Packet8f> = bit_to_ur_float(rawbits_34) */
+  else draw_full(e, w);
   for (int j = 0; j < 8; ++j) u[j] = bit_ur_f(w[j]);
 }
 static void ur_f4(or_vmt* e, float* u) {
@@ -164,7 +257,7 @@ static void ur_f4(or_vmt* e, float* u) {
 }
 static void ur_d4(or_vmt* e, double* u) {
   uint64_t r[4];
-  vmt_packet(e, r);
+  raw4(e, r);
   for (int j = 0; j < 4; ++j) u[j] = bit_ur_d(r[j]);
 }
 
@@ -1802,4 +1895,27 @@ int or_gen_truncmvn(or_vmt* e, int dtype, int dim, const double* H, const double
     free(df);
   }
   return 0;
+}
+
+/* Any generator of or_gen_real drawn with a scalar engine as the Urng. */
+int or_sgen_real(or_seng* s, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n) {
+  or_vmt dummy;
+  memset(&dummy, 0, sizeof dummy);
+  dummy.L = 4;
+  or_seng* prev = g_src;
+  g_src = s;
+  const int rc = or_gen_real(&dummy, g, dist, dtype, a, b, out, n);
+  g_src = prev;
+  return rc;
+}
+
+int or_sgen_randbits(or_seng* s, int32_t* out, size_t n) {
+  or_vmt dummy;
+  memset(&dummy, 0, sizeof dummy);
+  dummy.L = 4;
+  or_seng* prev = g_src;
+  g_src = s;
+  const int rc = or_gen_randbits(&dummy, out, n);
+  g_src = prev;
+  return rc;
 }

@@ -60,6 +60,19 @@ void or_vmt_discard(or_vmt* e, uint64_t npackets);
  * state comparison: out[l*312 + i] */
 void or_vmt_window(const or_vmt* e, uint64_t* out);
 
+/* ---- scalar engines as the Urng: std::mt19937_64, P8_mt19937_64 --------- */
+enum { OR_SENG_MT19937_64 = 1, OR_SENG_P8_MT19937_64 = 2 };
+typedef struct {
+  int kind;
+  or_mt64 mt;        /* std::mt19937_64 */
+  or_vmt *a, *b;     /* P8: Vmt19937_64(seed), Vmt19937_64(seed + 4) */
+  uint64_t buf[8];   /* P8: the current eight lanes */
+  int cnt;           /* P8: lanes handed out of buf (8 = empty) */
+} or_seng;
+or_seng* or_seng_new(int kind, uint64_t seed);
+void or_seng_free(or_seng* s);
+void or_seng_raw(or_seng* s, uint64_t* out, size_t n);
+
 /* ---- generator state (caches that EigenRand keeps inside *Gen objects) --- */
 typedef struct {
   int valid;          /* StdNormalGen / DiscreteGen packet cache flag        */
@@ -94,6 +107,9 @@ int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b,
 /* per-element forms (*VGen): parameters a[i] / b[i] (NULL: the scalars) */
 int or_gen_real_v(or_vmt* e, or_gen* g, int dist, int dtype, const void* av, const void* bv, double sa, double sb,
                   void* out, size_t n);
+/* or_gen_real / or_gen_randbits with a scalar engine as the Urng */
+int or_sgen_real(or_seng* s, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n);
+int or_sgen_randbits(or_seng* s, int32_t* out, size_t n);
 /* TruncGen<Base>{base, Support(lower, upper)} (Truncated.h); g: four slots */
 int or_gen_trunc(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, double lower, double upper,
                  void* out, size_t n);

@@ -72,6 +72,14 @@ def lib():
         L.or_gen_multinomial.restype = ctypes.c_int
         L.or_gen_multinomial_cond.argtypes = [vp, vp, ctypes.c_int32, ctypes.c_int32, vp, sz]
         L.or_gen_multinomial_cond.restype = ctypes.c_int
+        L.or_seng_new.restype = vp
+        L.or_seng_new.argtypes = [ctypes.c_int, ctypes.c_uint64]
+        L.or_seng_free.argtypes = [vp]
+        L.or_seng_raw.argtypes = [vp, vp, sz]
+        L.or_sgen_real.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, sz]
+        L.or_sgen_real.restype = ctypes.c_int
+        L.or_sgen_randbits.argtypes = [vp, vp, sz]
+        L.or_sgen_randbits.restype = ctypes.c_int
         L.or_gen_truncmvn.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, ctypes.c_int64, vp, sz]
         L.or_gen_truncmvn.restype = ctypes.c_int
         L.or_eigen_sum_avx.argtypes = [vp, ctypes.c_int]
@@ -121,6 +129,41 @@ class Engine:
     def window(self):
         out = np.empty((self.lanes, 312), dtype=np.uint64)
         self.L.or_vmt_window(self.h, _p(out))
+        return out
+
+
+class ScalarEngine:
+    """A scalar engine as EigenRand's Urng: "mt19937_64" (std::mt19937_64) or
+    "p8" (P8_mt19937_64 over Vmt19937_64(seed), Vmt19937_64(seed + 4))."""
+
+    KINDS = {"mt19937_64": 1, "p8": 2}
+
+    def __init__(self, kind, seed):
+        self.L = lib()
+        self.h = self.L.or_seng_new(self.KINDS[kind], ctypes.c_uint64(seed))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.or_seng_free(self.h)
+            self.h = None
+
+    def raw(self, n):
+        out = np.empty(n, dtype=np.uint64)
+        self.L.or_seng_raw(self.h, _p(out), n)
+        return out
+
+    def generate(self, gen, kind, n, dtype=np.float32, a=0.0, b=0.0):
+        """Real kinds of generate() and RANDBITS, drawn through the scalar engine."""
+        if kind == "RANDBITS":
+            out = np.empty(n, dtype=np.int32)
+            rc = self.L.or_sgen_randbits(self.h, _p(out), n)
+        else:
+            a, b = DEFAULT_AB.get(kind, (a, b))
+            out = np.empty(n, dtype=dtype)
+            dist = OR_BERNOULLI if kind == "BERNOULLI" else REAL[kind]
+            rc = self.L.or_sgen_real(self.h, gen.ptr, dist, 1 if dtype == np.float64 else 0, a, b, _p(out), n)
+        if rc != 0:
+            raise RuntimeError(f"oracle error {rc} for {kind}")
         return out
 
 

@@ -1,0 +1,94 @@
+"""GPU parity of scalar engines as the Urng (std::mt19937_64, P8_mt19937_64)
+against the CPU oracle, bit-exact, through the C ABI."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def er(gpulib):
+    return gpulib
+
+
+def mem(t):
+    torch.cuda.synchronize()
+    if t.dim() == 2:
+        t = t.t()
+    return t.contiguous().reshape(-1).cpu().numpy()
+
+
+def assert_bits_equal(a, b, msg=""):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    ua = a.view(np.uint64 if a.itemsize == 8 else np.uint32)
+    ub = b.view(np.uint64 if b.itemsize == 8 else np.uint32)
+    bad = np.nonzero(ua != ub)[0]
+    assert bad.size == 0, f"{msg}: {bad.size} mismatches, first at {bad[:5]}: {a[bad[:5]]} vs {b[bad[:5]]}"
+
+
+ENGINES = [("mt19937_64", "mt19937_64"), ("p8", "P8_mt19937_64")]
+
+
+def test_mt19937_64_known_answer(er):
+    """std::mt19937_64's 10000th output for the default seed, drawn on the GPU."""
+    x = er.mt19937_64(5489).raw(10000).cpu().numpy().view(np.uint64)
+    assert int(x[-1]) == 9981545732273789042
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_raw_stream(er, oracle, okind, cls):
+    """rng() in calls of odd sizes (P8's eight-lane buffer carried between
+    calls) and a long one (jump-ahead segments)."""
+    u = getattr(er, cls)(42)
+    o = oracle.ScalarEngine(okind, 42)
+    for n in (3, 5, 13, 1 << 20, 8, 7, 100001):
+        assert_bits_equal(u.raw(n).cpu().numpy().view(np.uint64), o.raw(n), f"{cls} n={n}")
+
+
+KINDS = [("UNIFORM_REAL", 0, 0), ("UNIFORM_REAL2", -2.0, 3.0), ("BALANCED", 0, 0), ("BALANCED2", -3.0, 5.0),
+         ("NORMAL_STD", 0, 0), ("NORMAL", 2.0, 3.0), ("LOGNORMAL", 0.0, 1.0), ("EXPONENTIAL", 1.5, 0),
+         ("CAUCHY", 0.0, 1.0), ("WEIBULL", 1.5, 2.0), ("EXTREME_VALUE", 0.0, 1.0), ("GAMMA", 1.0, 2.0),
+         ("BERNOULLI", 0.3, 0)]
+
+
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+@pytest.mark.parametrize("kind,a,b", KINDS, ids=[k[0] for k in KINDS])
+@pytest.mark.parametrize("okind,cls", ENGINES, ids=["mt", "p8"])
+def test_scalar_engine_distributions(er, oracle, okind, cls, kind, a, b, tdt):
+    """Fixed-draw kinds through RawbitsMaker<..., scalar_fullbit>: 3 draws per
+    float uniform packet (rawbits_34), 4 per double or raw-bits packet, 2 per
+    half packet; consecutive free-function calls (fresh generators)."""
+    npt = np.float32 if tdt == torch.float32 else np.float64
+    P = 8 if tdt == torch.float32 else 4
+    u = getattr(er, cls)(1234)
+    o = oracle.ScalarEngine(okind, 1234)
+    for n in (P, 3 * P, 1 << 20, 5 * P):
+        d, keep = er._desc(kind, tdt, a, b)
+        out = torch.empty(n, dtype=tdt, device="cuda")
+        er._lib.check(er._L.gr_sengine_sample(u._h, er.ctypes.byref(d), er._ptr(out), n, er._stream_ptr()))
+        ref = o.generate(oracle.Gen(), kind, n, npt, a, b)
+        assert_bits_equal(mem(out), ref, f"{kind} {cls} {tdt} n={n}")
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES, ids=["mt", "p8"])
+def test_scalar_engine_randbits_and_mirror(er, oracle, okind, cls):
+    """RandbitsGen<int32_t> (Packet4i rawbits: 2 draws per packet), the Python
+    mirror's free functions on a scalar engine, and refused kinds."""
+    u = getattr(er, cls)(7)
+    o = oracle.ScalarEngine(okind, 7)
+    for n in (4, 12, 1 << 18):
+        assert_bits_equal(mem(er.randBits(n, 1, u)), o.generate(None, "RANDBITS", n), f"randbits n={n}")
+    x = mem(er.normal(64, 64, u, 1.0, 2.0))
+    assert_bits_equal(x, o.generate(oracle.Gen(), "NORMAL", 4096, np.float32, 1.0, 2.0), "normal mirror")
+    x = mem(er.ExponentialGen(2.0, dtype=torch.float64).generate(32, 32, u))
+    assert_bits_equal(x, o.generate(oracle.Gen(), "EXPONENTIAL", 1024, np.float64, 2.0), "object mirror")
+    with pytest.raises(er.GrError):
+        er.gamma(8, 1, u, 0.5, 1.0)
+    with pytest.raises(er.GrError):
+        er.NormalGen().generate(8, 1, u)
