@@ -88,11 +88,14 @@ def kernel_of(name):
 
 # DRAM bytes per sample of a sweep entry's kernel, from one ncu capture each
 # (dram__bytes_read.sum + dram__bytes_write.sum over the samples of the
-# launch; the capture command is in the named profiles/ summary), and the
-# FP64 pipe activity of FP64-bound kernels
+# launch; the capture command is in the named profiles/ summary), and what
+# binds the kernel when it is not HBM
 MEASURED = {
     "uniformReal/f32": {"dram_bytes_per_sample": 3.276, "profile": "profiles/k_direct_uniform_f32_8192sq.md"},
-    "beta/f64": {"dram_bytes_per_sample": None, "fp64_pipe_active": 0.469, "profile": "profiles/k_beta_f64_2048sq.md"},
+    "beta/f64": {"dram_bytes_per_sample": 5.17, "fp64_pipe_active": 0.166, "issue_active": 0.506,
+                 "note": "latency-bound: each CTA waits on its thread-0 walk over the accept masks; "
+                         "FP64 pipe 17%, ALU 39%, issue active 51% (not HBM, not FP64)",
+                 "profile": "profiles/k_beta_f64_2048sq.md"},
 }
 
 
@@ -105,9 +108,9 @@ def roofline_entry(name, pd, hbm_peak, peaks):
          "unit": "GB/s", "frac": round(pd["gbs"] / hbm_peak, 4),
          "traffic": round(bps * N) if bps else None,
          "peak_source": "measured" if peaks else "fallback"}
-    if m.get("fp64_pipe_active"):
-        e["fp64_pipe_active"] = m["fp64_pipe_active"]
-        e["note"] = "FP64-bound: the binding roof is the FP64 pipe, not HBM"
+    for key in ("fp64_pipe_active", "issue_active", "note"):
+        if m.get(key) is not None:
+            e[key] = m[key]
     if m.get("profile"):
         e["profile"] = m["profile"]
     return e
@@ -781,9 +784,10 @@ def run_case(args):
         side = 4096 if name.endswith("4096") else 2048  # 4096: the sweep's launch
         out = torch.empty((side, side), dtype=dt, device="cuda")
         fn = lambda: g.generate(side, side, urng, out=out)
-    elif name in ("weibull_f64", "exponential_f64", "gamma05_f64", "normal_f64"):  # 2048x2048 f64
+    elif name in ("weibull_f64", "exponential_f64", "gamma05_f64", "normal_f64", "cauchy_f64"):  # 2048x2048 f64
         kind = {"weibull_f64": ("WEIBULL", 1.5, 1.0), "exponential_f64": ("EXPONENTIAL", 1.0, 0.0),
-                "gamma05_f64": ("GAMMA", 0.5, 1.0), "normal_f64": ("NORMAL_STD", 0.0, 0.0)}[name]
+                "gamma05_f64": ("GAMMA", 0.5, 1.0), "normal_f64": ("NORMAL_STD", 0.0, 0.0),
+                "cauchy_f64": ("CAUCHY", 0.0, 1.0)}[name]
         d, keep = er._desc(kind[0], torch.float64, kind[1], kind[2])
         out = torch.empty((2048, 2048), dtype=torch.float64, device="cuda")
         fn = lambda: er._lib.check(er._L.gr_sample(urng._h, er.ctypes.byref(d), er._ptr(out), out.numel(),
