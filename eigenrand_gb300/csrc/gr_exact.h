@@ -95,7 +95,8 @@ GR_HD uint64_t mt_finv(uint64_t t) {
 }
 template <class NW, class OLD>
 GR_HD void mt_untwist_block(NW&& nw, OLD&& old) {
-  constexpr uint64_t U = 0x8000000000000000ull, L = 0x7fffffffffffffffull;
+  // MT19937-64 splits a word into its upper 33 and lower 31 bits
+  constexpr uint64_t U = 0xffffffff80000000ull, L = 0x000000007fffffffull;
   // upper half: y_i for i in [156, 312) from nw only
   for (int i = 156; i < 312; ++i) {
     const uint64_t y = mt_finv(nw(i) ^ nw(i - 156));

@@ -62,16 +62,16 @@ int main() {
       auto f = [](uint64_t y) { return (y >> 1) ^ ((y & 1) ? 0xb5026f5aa96619e9ull : 0ull); };
       for (int i = 0; i < 312; ++i) {
         const uint64_t nxt = i + 1 < 312 ? old[i + 1] : nw[0];
-        const uint64_t y = (old[i] & 0x8000000000000000ull) | (nxt & 0x7fffffffffffffffull);
+        const uint64_t y = (old[i] & 0xffffffff80000000ull) | (nxt & 0x000000007fffffffull);
         nw[i] = (i < 156 ? old[i + 156] : nw[i - 156]) ^ f(y);
       }
       // old[0]'s lower bits only matter through old[311] = old[155] ^ f(...):
       // make the pair consistent, as any block produced by a twist is
-      const uint64_t y311 = (0ull) | (old[0] & 0x7fffffffffffffffull);
+      const uint64_t y311 = (0ull) | (old[0] & 0x000000007fffffffull);
       old[311] = old[155] ^ f(y311);
       for (int i = 0; i < 312; ++i) {
         const uint64_t nxt = i + 1 < 312 ? old[i + 1] : nw[0];
-        const uint64_t y = (old[i] & 0x8000000000000000ull) | (nxt & 0x7fffffffffffffffull);
+        const uint64_t y = (old[i] & 0xffffffff80000000ull) | (nxt & 0x000000007fffffffull);
         nw[i] = (i < 156 ? old[i + 156] : nw[i - 156]) ^ f(y);
       }
       for (int i = 0; i < 312; ++i) back[i] = 0x5555555555555555ull;

@@ -360,23 +360,26 @@ def test_half_packet_cache_between_kinds(er, oracle):
         assert_bits_equal(mem(o), ref, f"{kind} n={n}")
 
 
+@pytest.mark.parametrize("ab", [(0.5, 2.0), (2.0, 1.0), (3.0, 1.5)])
 @pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
-def test_beta_walk_call_ends_everywhere(er, oracle, tdt):
+def test_beta_walk_call_ends_everywhere(er, oracle, tdt, ab):
     """Many BetaGen calls of random sizes on one engine: each call ends at a
     different point of the engine blocks it generated (including inside the
     oldest one resident, whose predecessor the kernel recovers by untwisting),
     and the engine continues exactly (checked by the next call and by a final
-    raw draw)."""
+    raw draw).  (2, 1) has no rejection component (the walk runs ahead of its
+    evaluated positions only by its record buffer); (3, 1.5) two tan-proposal
+    components."""
     P = 8 if tdt == torch.float32 else 4
     rng = np.random.default_rng(71)
     u = er.Vmt19937_64(33)
     e = oracle.Engine(33)
-    g = er.BetaGen(0.5, 2.0, dtype=tdt)
+    g = er.BetaGen(*ab, dtype=tdt)
     og = oracle.Gen()
     for _ in range(60):
         n = int(rng.integers(1, 700)) * P
-        ref = oracle.generate(e, og, "BETA", n, npdt(tdt), 0.5, 2.0)
-        assert_bits_equal(mem(g.generate(n, 1, u)), ref, f"beta {tdt} n={n}")
+        ref = oracle.generate(e, og, "BETA", n, npdt(tdt), *ab)
+        assert_bits_equal(mem(g.generate(n, 1, u)), ref, f"beta{ab} {tdt} n={n}")
     d, keep = er._desc("RANDBITS", torch.int32)
     o = torch.empty(16, dtype=torch.int32, device="cuda")
     er._lib.check(er._L.gr_sample(u._h, er.ctypes.byref(d), er._ptr(o), 16, er._stream_ptr()))
