@@ -535,6 +535,15 @@ def bench_next_rows(er, streams=608):
         res[f"gamma2_single_stream/{tag}"] = entry(
             _median_ms(lambda: er.gamma(4096, 4096, one, 2.0, 1.0, dtype=tdt, out=out)), N * es)
         del out, mean, sd
+    # binomialV: the reference's vectorize-over-params pattern (trials 20 / 50 /
+    # 100 by column, p 0.5 / 0.01 / 0.75 by row), 12 bytes per sample
+    idx = torch.arange(4096, device="cuda")
+    trials = torch.tensor([20, 50, 100], dtype=torch.int32, device="cuda")[idx % 3][None, :].expand(4096, 4096)
+    pr = torch.tensor([0.5, 0.01, 0.75], device="cuda")[idx % 3][:, None].expand(4096, 4096)
+    trials, pr = trials.t().contiguous().t(), pr.t().contiguous().t()
+    outi = torch.empty_like(trials)
+    res["binomialV/i32"] = entry(_median_ms(lambda: er.binomial(urng, trials, pr, out=outi)), 12 * N)
+    del trials, pr, outi
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     return res

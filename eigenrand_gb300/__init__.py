@@ -607,7 +607,31 @@ def poisson(rows, cols, urng, mean=1.0, out=None, stream=None):
     return _sample("POISSON", rows, cols, urng, torch.int32, mean, out=out, stream=stream)
 
 
-def binomial(rows, cols, urng, trials=1, p=0.5, out=None, stream=None):
+def binomial(*args, trials=1, p=0.5, out=None, stream=None):
+    """binomial(rows, cols, urng[, trials, p]) -> BinomialGen<int32_t>;
+    binomial(urng, trials, p) with an int32 trials tensor and / or a float p
+    tensor of the output's shape -> BinomialVGen<int32_t> (Discrete.h:1822-1898)."""
+    if _is_v(args):
+        urng, tr, pv = args[0], args[1], args[2]
+        ta = _eigen_order(tr, torch.int32) if torch.is_tensor(tr) else None
+        tb = _eigen_order(pv, torch.float32) if torch.is_tensor(pv) else None
+        if ta is None and tb is None:
+            raise TypeError("the per-element form needs a parameter tensor")
+        if ta is not None and tb is not None and ta.shape != tb.shape:
+            raise ValueError("trials and p must have the same shape")
+        ref = ta if ta is not None else tb
+        o = torch.empty_like(ref, dtype=torch.int32) if out is None else out
+        d, keep = _desc("BINOMIAL", torch.int32, 0.0 if tb is not None else float(pv),
+                        trials=0 if ta is not None else int(tr))
+        vp = lambda t: _ptr(t) if t is not None else None
+        _lib.check(_L.gr_sample_v2(urng._h, ctypes.byref(d), vp(ta), vp(tb), _ptr(o), o.numel(), _stream_ptr(stream)))
+        del keep
+        return o
+    rows, cols, urng = args[:3]
+    if len(args) > 3:
+        trials = args[3]
+    if len(args) > 4:
+        p = args[4]
     return _sample("BINOMIAL", rows, cols, urng, torch.int32, p, trials=trials, out=out, stream=stream)
 
 
@@ -624,7 +648,7 @@ def bernoulli(*args, p=0.5, dtype=torch.float32, out=None, stream=None):
     -> BernoulliVGen<float>, one probability per element (Basic.h:1105-1153)."""
     if args and isinstance(args[0], Vmt19937_64):
         urng, pv = args[0], args[1]
-        pv = pv.to(device="cuda", dtype=torch.float32).contiguous()
+        pv = _eigen_order(pv, torch.float32)
         o = torch.empty_like(pv) if out is None else out
         d, keep = _desc("BERNOULLI", torch.float32)
         _lib.check(_L.gr_sample_v(urng._h, ctypes.byref(d), _ptr(pv), _ptr(o), pv.numel(), _stream_ptr(stream)))

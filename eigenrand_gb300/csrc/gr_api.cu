@@ -1068,6 +1068,35 @@ gr_status make_truncated(gr_gen* g, const gr_dist_desc& base, double lower, doub
   return GR_OK;
 }
 
+// binomial(urng, trials, p) with int32 trials and float p arrays, or one of
+// them a scalar (Discrete.h:1822-1898): BinomialVGen<int32_t> on packets of 4.
+gr_status run_binom_v(gr_engine* e, const gr_dist_desc& d, const void* dev_a, const void* dev_b, void* out, size_t n,
+                      cudaStream_t s) {
+  if (d.dtype != GR_I32) return fail(GR_ERR_UNSUPPORTED, "per-element binomial: BinomialVGen<int32_t> only");
+  if (n % 4) return fail(GR_ERR_INVALID, "size must be a multiple of 4 (the reference packet width for this type)");
+  if (n == 0) return GR_OK;
+  Plan p{};
+  p.eng = e->st;
+  p.K = e->K;
+  p.gran = 4;
+  p.gran_per_k = (int64_t)(n / 4) / e->K;
+  p.gran_rem = (int64_t)(n / 4) % e->K;
+  p.out = out;
+  BinomVArgs a{};
+  a.trials = static_cast<const int32_t*>(dev_a);
+  a.p = static_cast<const float*>(dev_b);
+  a.trials0 = d.trials;
+  a.p0 = (float)d.a;
+  // half packets per output packet: the Poisson loop (mean < 1) draws about
+  // its largest count + 1, the tan rejection two per round until every lane
+  // has accepted
+  const int64_t npk = p.gran_per_k + (p.gran_rem ? 1 : 0);
+  a.max_blocks = (npk * 128) / (2 * kN) + 64;
+  const cudaError_t err = launch_binom_v(p, a, s);
+  if (err != cudaSuccess) return cuda_fail(err, "per-element binomial kernel");
+  return GR_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1342,6 +1371,7 @@ gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* 
     return fail(GR_ERR_UNSUPPORTED,
                 "per-element bernoulli: BernoulliVGen<float> only (the double form goes through a cast the "
                 "reference leaves to Eigen's generic pcast)");
+  if (d.kind == GR_BINOMIAL) return run_binom_v(e, d, dev_a, dev_b, dev_out, n, (cudaStream_t)stream);
   if (d.dtype != GR_F32 && d.dtype != GR_F64) return fail(GR_ERR_UNSUPPORTED, "per-element forms are float/double");
   gr_status st = GR_OK;
   switch (d.kind) {

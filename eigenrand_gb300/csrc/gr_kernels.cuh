@@ -138,6 +138,18 @@ struct TruncFilterArgs {
 };
 cudaError_t launch_trunc_filter(int dtype, const TruncFilterArgs& a, cudaStream_t s);
 
+// BinomialVGen<int32_t> with per-element (trials, p) (gr_binomv.cu): one warp
+// per stream, packets of 4 outputs on half-packet draws.  NULL arrays take
+// the scalar operands.
+struct BinomVArgs {
+  const int32_t* trials;
+  const float* p;
+  int32_t trials0;
+  float p0;
+  int64_t max_blocks;
+};
+cudaError_t launch_binom_v(const Plan& p, const BinomVArgs& a, cudaStream_t s);
+
 // Batched vectorize-over-params sets (gr_vop.cu).
 struct VopArgs {
   int64_t nsets;

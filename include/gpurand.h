@@ -172,6 +172,9 @@ gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* batch, gr_stream_
  *   GR_EXTREME_VALUE (a, b)      ExtremeValueVGen    NormalExp.h:736-765
  *   GR_CAUCHY (a, b)             CauchyVGen          NormalExp.h:859-889
  *   GR_BERNOULLI, GR_F32 (p)     BernoulliVGen<float> Basic.h:711-747
+ *   GR_BINOMIAL, GR_I32          BinomialVGen<int32_t> Discrete.h:1124-1192:
+ *     dev_a int32 trials (NULL: desc->trials), dev_b float p (NULL: (float)desc->a);
+ *     the binomial(urng, trials, p) overloads of Discrete.h:1822-1898
  * The double BernoulliVGen goes through a packet cast the reference leaves to
  * Eigen's generic pcast, which cannot be pinned here: GR_ERR_UNSUPPORTED.
  * gr_sample_v / gr_sample_v2 use a fresh generator (the free functions);

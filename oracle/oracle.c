@@ -1716,6 +1716,24 @@ int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32
   return 0;
 }
 
+/* binomial(urng, trials, p) (Discrete.h:1822-1898): BinomialVGen<int32_t>
+ * over n outputs (a multiple of 4) in packets of 4; a NULL array takes the
+ * scalar operand for every element. */
+int or_gen_binomial_v(or_vmt* e, const int32_t* trials, const float* p, int32_t trials0, float p0, int32_t* out,
+                      size_t n) {
+  if (n % 4) return 1;
+  for (size_t i = 0; i < n; i += 4) {
+    int32_t tr[4];
+    float pp[4];
+    for (int j = 0; j < 4; ++j) {
+      tr[j] = trials ? trials[i + j] : trials0;
+      pp[j] = p ? p[i + j] : p0;
+    }
+    binomial_v_lanes(e, 4, tr, pp, out + i);
+  }
+  return 0;
+}
+
 /* Eigen 3.4's sum() of a dynamic double vector with AVX packets of 4 (the
  * LinearVectorizedTraversal redux of Redux.h): two packet accumulators over
  * pairs of packets, their sum, one more packet if the aligned part has an odd

@@ -144,6 +144,8 @@ int or_gen_multinomial(or_vmt* e, or_gen* g, const or_discrete* d, int32_t trial
 
 /* vectorize-over-params */
 int or_binomial_v_packet(or_vmt* e, const int32_t* trials, const float* p, int32_t* out);
+int or_gen_binomial_v(or_vmt* e, const int32_t* trials, const float* p, int32_t trials0, float p0, int32_t* out,
+                      size_t n);
 /* TruncMvNormalGen Gibbs chains with the precision matrix H (FP64, column-major) */
 int or_gen_truncmvn(or_vmt* e, int dtype, int dim, const double* H, const double* mean, const double* lower,
                     const double* upper, int64_t burn_in, void* out, size_t samples);

@@ -90,6 +90,8 @@ def lib():
         L.or_gen_real_v.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_double, ctypes.c_double,
                                     vp, sz]
         L.or_gen_real_v.restype = ctypes.c_int
+        L.or_gen_binomial_v.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_float, vp, ctypes.c_size_t]
+        L.or_gen_binomial_v.restype = ctypes.c_int
         L.or_gen_trunc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, vp, sz]
         L.or_gen_trunc.restype = ctypes.c_int
@@ -280,6 +282,22 @@ def multinomial(eng, gen, weights, trials, samples):
     out = np.empty((samples, len(w)), dtype=np.int32)
     rc = L.or_gen_multinomial(eng.h, gen.ptr, d, int(trials), len(w), _p(out), samples)
     L.or_discrete_free(d)
+    if rc:
+        raise RuntimeError(f"oracle error {rc}")
+    return out
+
+
+def binomial_v(eng, trials, p):
+    """binomial(urng, trials, p) -> BinomialVGen<int32_t> (Discrete.h:1124-1192,
+    1822-1898): int32 trials and float p arrays in Eigen's linear order, or
+    one of them a scalar."""
+    L = lib()
+    ta = np.ascontiguousarray(trials, dtype=np.int32) if isinstance(trials, np.ndarray) else None
+    pa = np.ascontiguousarray(p, dtype=np.float32) if isinstance(p, np.ndarray) else None
+    n = (ta if ta is not None else pa).size
+    out = np.empty(n, dtype=np.int32)
+    rc = L.or_gen_binomial_v(eng.h, _p(ta) if ta is not None else None, _p(pa) if pa is not None else None,
+                             0 if ta is not None else int(trials), 0.0 if pa is not None else float(p), _p(out), n)
     if rc:
         raise RuntimeError(f"oracle error {rc}")
     return out

@@ -131,3 +131,60 @@ def test_vgen_matches_scalar_generator_and_streams(er, oracle):
         er._vform("GAMMA", er.Vmt19937_64(1), torch.ones(8), torch.ones(8))
     with pytest.raises(er.GrError):
         er.normal(er.Vmt19937_64(1), torch.ones(12), torch.ones(12))
+
+
+def _binom_params(r, n):
+    tr = r.choice(np.array([0, 1, 3, 20, 50, 100, 1000, 40000], np.int32), n)
+    p = r.choice(np.array([0.0, 0.01, 0.2, 0.5, 0.75, 0.99, 1.0], np.float32), n)
+    p = np.where(r.random(n) < 0.5, p, r.random(n).astype(np.float32))
+    return tr.astype(np.int32), p.astype(np.float32)
+
+
+def test_binomial_v_bit_exact(er, oracle):
+    """binomial(urng, trials, p) -> BinomialVGen<int32_t>: both operands
+    arrays, one scalar, a 2-D (column-major) call, and calls that continue
+    the same engine (the half-packet cache and the window carried between
+    calls, and into and out of the uniform-parameter BinomialGen)."""
+    r = np.random.default_rng(17)
+    u = er.Vmt19937_64(2024)
+    e = oracle.Engine(2024)
+    for n in (4, 64, 1 << 18, 12):
+        tr, p = _binom_params(r, n)
+        got = er.binomial(u, torch.from_numpy(tr), torch.from_numpy(p))
+        assert got.dtype == torch.int32
+        assert_bits_equal(eigen_mem(got), oracle.binomial_v(e, tr, p), f"binomialV n={n}")
+    tr, _ = _binom_params(r, 4096)
+    assert_bits_equal(eigen_mem(er.binomial(u, torch.from_numpy(tr), 0.5)), oracle.binomial_v(e, tr, 0.5),
+                      "scalar p")
+    _, p = _binom_params(r, 4096)
+    assert_bits_equal(eigen_mem(er.binomial(u, 50, torch.from_numpy(p))), oracle.binomial_v(e, 50, p), "scalar trials")
+    got = er.binomial(8, 6, u, 10, 0.3)
+    ref = oracle.generate(e, oracle.Gen(), "BINOMIAL", 48, np.int32, 0.3, 0.0, trials=10)
+    assert_bits_equal(eigen_mem(got), ref, "BinomialGen between per-element calls")
+    T = np.linspace(5, 50, 10).astype(np.int32).repeat(100).reshape(10, 100)
+    P = np.tile(np.linspace(0.1, 1.0, 10).astype(np.float32)[:, None], (1, 100))
+    got = er.binomial(u, torch.from_numpy(T), torch.from_numpy(P))
+    assert tuple(got.shape) == (10, 100)
+    ref = oracle.binomial_v(e, T.T.reshape(-1), P.T.reshape(-1))
+    assert_bits_equal(eigen_mem(got), ref, "2-D")
+
+
+def test_binomial_v_streams_and_errors(er, oracle):
+    """Slices of a multi-stream engine come from engines seed + 4k; constant
+    operands give the batched (VoP) binomial's values; sizes not a multiple
+    of 4 and mismatched shapes are rejected."""
+    K, per = 6, 4 * 333
+    u = er.Vmt19937_64(99, streams=K)
+    r = np.random.default_rng(4)
+    tr, p = _binom_params(r, K * per)
+    got = eigen_mem(er.binomial(u, torch.from_numpy(tr), torch.from_numpy(p)))
+    for k in range(K):
+        sl = slice(k * per, (k + 1) * per)
+        assert_bits_equal(got[sl], oracle.binomial_v(oracle.Engine(99 + 4 * k), tr[sl], p[sl]), f"slice {k}")
+    u1 = er.Vmt19937_64(321)
+    got = er.binomial(u1, torch.full((1000,), 25, dtype=torch.int32), 0.4)
+    assert_bits_equal(eigen_mem(got), oracle.vop_set(321, "BINOMIAL", 1000, 0.4, 1.0, 25), "VoP constant")
+    with pytest.raises(er.GrError):
+        er.binomial(er.Vmt19937_64(1), torch.ones(10, dtype=torch.int32), 0.5)
+    with pytest.raises(ValueError):
+        er.binomial(er.Vmt19937_64(1), torch.ones(8, dtype=torch.int32), torch.ones(12))
