@@ -6,9 +6,14 @@
 // with mean < 1, then a tan-proposal rejection until every lane has a value,
 // on float uniforms drawn as half packets (rng.half(), the engine's cached
 // upper half first).  A packet's consumption depends on its lanes, so each
-// engine's chain is sequential: one warp per engine, lanes 0-3 the packet
-// lanes deciding the loops by ballot; the warp twists its own blocks into
-// 624 half-packet draws each.  The engine window, its half cache and the
+// engine's chain is sequential: one warp per engine, every group of 4 lanes
+// holding the packet's 4 lanes and the loops decided by ballot; the warp
+// twists its own blocks into 624 half-packet draws each.  The warp's 8 lane
+// groups shorten the chain: they compute the parameter-only constants of 8
+// packets at once, and evaluate 8 rounds of the tan rejection at once on the
+// next 16 resident half packets (a lane keeps its first accepted round, the
+// packet ends with the round its last lane first accepts: the same draws and
+// values as round by round).  The engine window, its half cache and the
 // consumed count are written back at the end, as every engine call does.
 #include <cuda_runtime.h>
 
@@ -29,6 +34,27 @@ constexpr size_t kBvWarpBytes = (size_t)2 * kLanes * kN * 8 + (size_t)2 * kN * 1
 
 __device__ __forceinline__ float bv_ur(uint32_t x) { return u2f((x & 0x7fffffu) | (127u << 23)) - 1.0f; }
 
+// a lane's constants of BinomialVGen<int32_t>::packetOp
+struct BvLane {
+  float ptrials, mean, g1, sqrt_v, lsp, lsq;
+};
+
+// one round of the tan rejection on draws (u, u2): the proposal fres and
+// whether this lane accepts it
+__device__ __forceinline__ bool bv_trial(const BvLane& L, uint32_t w1, uint32_t w2, float& fres) {
+  float sn, cs;
+  sincosf_((float)3.1415926535897932 * bv_ur(w1), sn, cs);
+  const float ys = sn / cs;
+  fres = truncf(L.sqrt_v * ys + L.mean);
+  const float p1 = ((float)1.2 * L.sqrt_v) * (1.0f + ys * ys);
+  float t = (L.g1 - lgamma_approxf_(fres + 1.0f)) - lgamma_approxf_((L.ptrials + 1.0f) - fres);
+  t = t + fres * L.lsp;
+  t = t + (L.ptrials - fres) * L.lsq;
+  const float p2 = expf_(t);
+  const float u2 = bv_ur(w2);
+  return (0.0f <= fres) && (fres <= L.ptrials) && (u2 <= p1 * p2);
+}
+
 __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a) {
   extern __shared__ __align__(16) uint64_t bv_dyn[];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -43,7 +69,6 @@ __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a)
   const int64_t off = g0 * p.gran, n = ng * p.gran;
   if (n == 0) return;
   int32_t* out = static_cast<int32_t*>(p.out);
-  const float fpi = (float)3.1415926535897932;
 
   for (int i = lane; i < kLanes * kN; i += 32) raw[0][i / kN][i % kN] = st->win[i / kN][i % kN];
   __syncwarp();
@@ -55,7 +80,7 @@ __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a)
   auto next = [&]() -> uint32_t {
     if (pending) {
       pending = false;
-      return lane < 4 ? st->half_cache[lane] : 0u;
+      return st->half_cache[lane & 3];
     }
     if (h == 2 * kN) {
       if (nb >= a.max_blocks) {
@@ -93,58 +118,102 @@ __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a)
       ++nb;
       h = 0;
     }
-    const uint32_t v = lane < 4 ? hw[h][lane] : 0u;
+    const uint32_t v = hw[h][lane & 3];
     ++h;
     return v;
   };
   auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
 
-  for (int64_t e = 0; e < n / 4 && !abort; ++e) {
-    const int64_t i = off + e * 4 + (lane < 4 ? lane : 0);
-    const int32_t tr = lane < 4 ? (a.trials ? __ldg(a.trials + i) : a.trials0) : 0;
-    const float pv = lane < 4 ? (a.p ? __ldg(a.p + i) : a.p0) : 0.0f;
-    const float small_p = pv < 1.0f - pv ? pv : 1.0f - pv;  // pmin(p, 1 - p)
-    const float ptrials = (float)tr;
-    const float mean = ptrials * small_p;
-    const float g1 = lgamma_approxf_(ptrials + 1.0f);
-    const float sqrt_v = sqrtf((2.0f * mean) * (1.0f - small_p));
-    const float lsp = logf_(small_p), lsq = logf_(1.0f - small_p);
-    bool valid = mean < 1.0f;
-    float vres = 0.0f;
-    if (mask4(valid)) {
-      const float ne = expf_(-mean);
-      float val = 1.0f;
-      int32_t res = 0;
-      for (;;) {
-        val = val * bv_ur(next());
-        if (abort) break;
-        const bool c = (ne < val) && valid;
-        if (mask4(c) == 0) break;
-        res += c ? 1 : 0;
-      }
-      vres = (float)res;
+  const int64_t npk = n / 4;
+  const int jl = lane & 3;  // every group of 4 lanes holds the packet's 4 lanes
+  for (int64_t e0 = 0; e0 < npk && !abort; e0 += 8) {
+    // the parameter-only constants of packets e0 .. e0 + 7, group g = lane / 4
+    // computing those of packet e0 + g
+    int32_t trg = 0;
+    float pvg = 0.0f;
+    if (e0 + (lane >> 2) < npk) {
+      const int64_t i = off + (e0 + (lane >> 2)) * 4 + jl;
+      trg = a.trials ? __ldg(a.trials + i) : a.trials0;
+      pvg = a.p ? __ldg(a.p + i) : a.p0;
     }
-    if (mask4(valid) != 0xfu) {
-      for (;;) {
-        float sn, cs;
-        sincosf_(fpi * bv_ur(next()), sn, cs);
-        const float ys = sn / cs;
-        const float fres = truncf(sqrt_v * ys + mean);
-        const float p1 = ((float)1.2 * sqrt_v) * (1.0f + ys * ys);
-        float t = (g1 - lgamma_approxf_(fres + 1.0f)) - lgamma_approxf_((ptrials + 1.0f) - fres);
-        t = t + fres * lsp;
-        t = t + (ptrials - fres) * lsq;
-        const float p2 = expf_(t);
-        const float u2 = bv_ur(next());
-        if (abort) break;
-        const bool fv = (0.0f <= fres) && (fres <= ptrials) && (u2 <= p1 * p2);
-        if (fv && !valid) vres = fres;
-        valid = valid || fv;
-        if (mask4(valid) == 0xfu) break;
+    const float spg = pvg < 1.0f - pvg ? pvg : 1.0f - pvg;  // pmin(p, 1 - p)
+    const float meang = (float)trg * spg;
+    const float g1g = lgamma_approxf_((float)trg + 1.0f);
+    const float svg = sqrtf((2.0f * meang) * (1.0f - spg));
+    const float lspg = logf_(spg), lsqg = logf_(1.0f - spg);
+    const float neg = expf_(-meang);
+    const int kend = npk - e0 < 8 ? (int)(npk - e0) : 8;
+    for (int kk = 0; kk < kend && !abort; ++kk) {
+      const int64_t e = e0 + kk;
+      const int src = (kk << 2) | jl;
+      const int32_t tr = __shfl_sync(0xffffffffu, trg, src);
+      const float pv = __shfl_sync(0xffffffffu, pvg, src);
+      const float small_p = __shfl_sync(0xffffffffu, spg, src);
+      const float ptrials = (float)tr;
+      const float mean = __shfl_sync(0xffffffffu, meang, src);
+      const float g1 = __shfl_sync(0xffffffffu, g1g, src);
+      const float sqrt_v = __shfl_sync(0xffffffffu, svg, src);
+      const float lsp = __shfl_sync(0xffffffffu, lspg, src), lsq = __shfl_sync(0xffffffffu, lsqg, src);
+      const float ne = __shfl_sync(0xffffffffu, neg, src);
+      const int64_t i = off + e * 4 + jl;
+      bool valid = mean < 1.0f;
+      float vres = 0.0f;
+      if (mask4(valid)) {
+        float val = 1.0f;
+        int32_t res = 0;
+        for (;;) {
+          val = val * bv_ur(next());
+          if (abort) break;
+          const bool c = (ne < val) && valid;
+          if (mask4(c) == 0) break;
+          res += c ? 1 : 0;
+        }
+        vres = (float)res;
       }
+      if (mask4(valid) != 0xfu) {
+        const BvLane L{ptrials, mean, g1, sqrt_v, lsp, lsq};
+        for (;;) {
+          if (!pending && h + 16 <= 2 * kN) {
+            // rounds r .. r + 7 at once, group g = lane / 4 evaluating round
+            // r + g on half packets h + 2g, h + 2g + 1 of the resident block; a
+            // lane keeps its first accepted proposal and the packet ends with
+            // the round in which its last lane first accepts, as round by round
+            const int g = lane >> 2, j = lane & 3;
+            float fres;
+            const bool acc = bv_trial(L, hw[h + 2 * g][j], hw[h + 2 * g + 1][j], fres) && !valid;
+            const unsigned bal = __ballot_sync(0xffffffffu, acc);
+            unsigned mj = 0;
+  #pragma unroll
+            for (int q = 0; q < 8; ++q) mj |= ((bal >> (4 * q + j)) & 1u) << q;
+            const int first = mj ? __ffs(mj) - 1 : 8;
+            const float ffirst = __shfl_sync(0xffffffffu, fres, ((first & 7) << 2) | j);
+            int end = valid ? -1 : first;
+            end = max(end, __shfl_xor_sync(0xffffffffu, end, 1));
+            end = max(end, __shfl_xor_sync(0xffffffffu, end, 2));
+            if (!valid && first < 8) {
+              vres = ffirst;
+              valid = true;
+            }
+            if (end < 8) {
+              h += 2 * (end + 1);
+              break;
+            }
+            h += 16;
+            continue;
+          }
+          float fres;
+          const uint32_t w1 = next();
+          const uint32_t w2 = next();
+          if (abort) break;
+          const bool fv = bv_trial(L, w1, w2, fres);
+          if (fv && !valid) vres = fres;
+          valid = valid || fv;
+          if (mask4(valid) == 0xfu) break;
+        }
+      }
+      if (abort) break;
+      if (lane < 4) out[i] = (pv == small_p) ? cvtt_f32(vres) : tr - cvtt_f32(vres);
     }
-    if (abort) break;
-    if (lane < 4) out[i] = (pv == small_p) ? cvtt_f32(vres) : tr - cvtt_f32(vres);
   }
 
   // ---- state after the call (as k_negbin: the last draw's block, the
