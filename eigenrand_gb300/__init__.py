@@ -499,14 +499,14 @@ def _vform(kind, urng, a, b=None, two=True, gen=None, out=None, stream=None):
         _lib.check(_L.gr_generate_v(gen._h, urng._h, vp(pa), vp(pb), _ptr(o), o.numel(), _stream_ptr(stream)))
     else:
         d, keep = _desc(kind, dtype, sa, sb)
-        _lib.check(_L.gr_sample_v2(urng._h, ctypes.byref(d), vp(pa), vp(pb), _ptr(o), o.numel(),
-                                   _stream_ptr(stream)))
+        fn = _L.gr_sengine_sample_v2 if isinstance(urng, _ScalarEngine) else _L.gr_sample_v2
+        _lib.check(fn(urng._h, ctypes.byref(d), vp(pa), vp(pb), _ptr(o), o.numel(), _stream_ptr(stream)))
         del keep
     return o
 
 
 def _is_v(args):
-    return bool(args) and isinstance(args[0], Vmt19937_64)
+    return bool(args) and isinstance(args[0], (Vmt19937_64, _ScalarEngine))
 
 
 def uniformReal(*args, min=None, max=None, dtype=torch.float32, out=None, stream=None):
@@ -611,7 +611,7 @@ def binomial(*args, trials=1, p=0.5, out=None, stream=None):
     """binomial(rows, cols, urng[, trials, p]) -> BinomialGen<int32_t>;
     binomial(urng, trials, p) with an int32 trials tensor and / or a float p
     tensor of the output's shape -> BinomialVGen<int32_t> (Discrete.h:1822-1898)."""
-    if _is_v(args):
+    if args and isinstance(args[0], (Vmt19937_64, _ScalarEngine)):
         urng, tr, pv = args[0], args[1], args[2]
         ta = _eigen_order(tr, torch.int32) if torch.is_tensor(tr) else None
         tb = _eigen_order(pv, torch.float32) if torch.is_tensor(pv) else None
@@ -624,7 +624,8 @@ def binomial(*args, trials=1, p=0.5, out=None, stream=None):
         d, keep = _desc("BINOMIAL", torch.int32, 0.0 if tb is not None else float(pv),
                         trials=0 if ta is not None else int(tr))
         vp = lambda t: _ptr(t) if t is not None else None
-        _lib.check(_L.gr_sample_v2(urng._h, ctypes.byref(d), vp(ta), vp(tb), _ptr(o), o.numel(), _stream_ptr(stream)))
+        fn = _L.gr_sengine_sample_v2 if isinstance(urng, _ScalarEngine) else _L.gr_sample_v2
+        _lib.check(fn(urng._h, ctypes.byref(d), vp(ta), vp(tb), _ptr(o), o.numel(), _stream_ptr(stream)))
         del keep
         return o
     rows, cols, urng = args[:3]

@@ -33,7 +33,7 @@ EXPORTS = [
     "gr_gen_create", "gr_gen_destroy", "gr_generate", "gr_sample", "gr_sample_batched", "gr_last_error",
     "gr_version", "gr_raw_u64_noalloc", "gr_sample_v", "gr_gen_create_truncated", "gr_sample_truncated",
     "gr_sample_v2", "gr_generate_v",
-    "gr_sengine_create", "gr_sengine_destroy", "gr_sengine_raw_u64", "gr_sengine_sample",
+    "gr_sengine_create", "gr_sengine_destroy", "gr_sengine_raw_u64", "gr_sengine_sample", "gr_sengine_sample_v2",
     "gr_mvnormal_create", "gr_mvnormal_sample", "gr_mvnormal_destroy", "gr_wishart_create", "gr_wishart_sample",
     "gr_wishart_destroy", "gr_dirichlet_create", "gr_dirichlet_sample", "gr_dirichlet_destroy",
     "gr_multinomial_create", "gr_multinomial_sample", "gr_multinomial_destroy",
@@ -142,6 +142,7 @@ def load(path=None):
         "gr_sengine_destroy": (i32, [vp]),
         "gr_sengine_raw_u64": (i32, [vp, vp, sz, vp]),
         "gr_sengine_sample": (i32, [vp, ctypes.POINTER(DistDesc), vp, sz, vp]),
+        "gr_sengine_sample_v2": (i32, [vp, ctypes.POINTER(DistDesc), vp, vp, vp, sz, vp]),
         "gr_generate_v": (i32, [vp, vp, vp, vp, vp, sz, vp]),
         "gr_gen_create_truncated": (i32, [ctypes.POINTER(vp), ctypes.POINTER(DistDesc), ctypes.c_double,
                                           ctypes.c_double]),

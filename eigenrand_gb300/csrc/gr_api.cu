@@ -1571,6 +1571,77 @@ gr_status sengine_words(gr_sengine* se, uint64_t* out, int64_t W, cudaStream_t s
   return GR_OK;
 }
 
+// binomial(urng, trials, p) on a scalar engine: one chain, so chunks of the
+// engine's words are drawn into HBM from a saved engine state, a single warp
+// runs BinomialVGen<int32_t> over them until they run out, and the engine is
+// put back and advanced by exactly the words the completed packets used.
+gr_status sengine_binom_v(gr_sengine* se, const gr_dist_desc& d, const void* dev_a, const void* dev_b, void* out,
+                          size_t n, cudaStream_t s) {
+  if (d.dtype != GR_I32) return fail(GR_ERR_UNSUPPORTED, "per-element binomial: BinomialVGen<int32_t> only");
+  if (n % 4) return fail(GR_ERR_INVALID, "size must be a multiple of 4 (the reference packet width for this type)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  gr_engine* e = se->eng;
+  const int64_t npk = (int64_t)(n / 4);
+  constexpr int64_t kMaxWords = (int64_t)1 << 24;
+  EngState* saved = nullptr;
+  uint64_t *w = nullptr, *pb = nullptr;
+  int64_t* res = nullptr;
+  auto bail = [&](gr_status st) {
+    cudaFreeAsync(saved, s);
+    cudaFreeAsync(w, s);
+    cudaFreeAsync(pb, s);
+    cudaFreeAsync(res, s);
+    return st;
+  };
+  cudaError_t aerr = cudaMallocAsync(&saved, sizeof(EngState) * (size_t)e->K, s);
+  if (aerr == cudaSuccess) aerr = cudaMallocAsync(&pb, sizeof(uint64_t) * 8, s);
+  if (aerr == cudaSuccess) aerr = cudaMallocAsync(&res, sizeof(int64_t) * 2, s);
+  BinomVArgs a{};
+  a.trials0 = d.trials;
+  a.p0 = (float)d.a;
+  // about 10 half packets (20 words) per packet in common parameter ranges
+  int64_t W = std::min<int64_t>(kMaxWords, std::max<int64_t>(4096, 24 * npk));
+  if (aerr == cudaSuccess) aerr = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
+  if (aerr != cudaSuccess) return bail(cuda_fail(aerr, "per-element binomial scratch"));
+  for (int64_t done = 0; done < npk;) {
+    cudaError_t err = cudaMemcpyAsync(saved, e->st, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && se->pbuf)
+      err = cudaMemcpyAsync(pb, se->pbuf, sizeof(uint64_t) * 8, cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine state copy"));
+    const int cnt0 = se->cnt;
+    gr_status st = sengine_words(se, w, W, s);
+    if (st != GR_OK) return bail(st);
+    a.trials = dev_a ? static_cast<const int32_t*>(dev_a) + 4 * done : nullptr;
+    a.p = dev_b ? static_cast<const float*>(dev_b) + 4 * done : nullptr;
+    err = launch_binom_v_words(w, W, a, static_cast<int32_t*>(out) + 4 * done, npk - done, res, s);
+    int64_t hres[2] = {0, 0};
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hres, res, sizeof hres, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return bail(cuda_fail(err, "per-element binomial on a scalar engine"));
+    if (hres[0] == 0) {
+      if (W == kMaxWords) return bail(fail(GR_ERR_REJECT_LIMIT, "per-element binomial: a packet drew more than 2^24 words"));
+      W = std::min<int64_t>(kMaxWords, 2 * W);  // these words are drawn again below, more of them
+      cudaFreeAsync(w, s);
+      w = nullptr;
+      if (aerr == cudaSuccess) aerr = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
+  if (aerr != cudaSuccess) return bail(cuda_fail(aerr, "per-element binomial scratch"));
+    }
+    // back to the saved state, then forward by the words the packets used
+    err = cudaMemcpyAsync(e->st, saved, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && se->pbuf)
+      err = cudaMemcpyAsync(se->pbuf, pb, sizeof(uint64_t) * 8, cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine state copy"));
+    se->cnt = cnt0;
+    if (hres[1] > 0) {
+      st = sengine_words(se, w, hres[1], s);
+      if (st != GR_OK) return bail(st);
+    }
+    done += hres[0];
+  }
+  return bail(GR_OK);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1603,6 +1674,16 @@ gr_status gr_sengine_destroy(gr_sengine* se) {
 gr_status gr_sengine_raw_u64(gr_sengine* se, uint64_t* dev_out, size_t n, gr_stream_t stream) {
   if (!se || (n && !dev_out)) return fail(GR_ERR_INVALID, "NULL argument");
   return sengine_words(se, dev_out, (int64_t)n, (cudaStream_t)stream);
+}
+
+gr_status gr_sengine_sample_v2(gr_sengine* se, const gr_dist_desc* desc, const void* dev_a, const void* dev_b,
+                               void* dev_out, size_t n, gr_stream_t stream) {
+  if (!se || !desc) return fail(GR_ERR_INVALID, "NULL argument");
+  if (((uintptr_t)dev_a | (uintptr_t)dev_b | (uintptr_t)dev_out) % 16)
+    return fail(GR_ERR_INVALID, "parameter and output arrays must be 16-byte aligned");
+  if (desc->kind != GR_BINOMIAL)
+    return fail(GR_ERR_UNSUPPORTED, "scalar engines: the per-element form is built for binomial only");
+  return sengine_binom_v(se, *desc, dev_a, dev_b, dev_out, n, (cudaStream_t)stream);
 }
 
 gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream) {

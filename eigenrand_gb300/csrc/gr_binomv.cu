@@ -55,35 +55,26 @@ __device__ __forceinline__ bool bv_trial(const BvLane& L, uint32_t w1, uint32_t 
   return (0.0f <= fres) && (fres <= L.ptrials) && (u2 <= p1 * p2);
 }
 
-__global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a) {
-  extern __shared__ __align__(16) uint64_t bv_dyn[];
-  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int k = blockIdx.x * kBvWarps + wi;
-  if (k >= p.K) return;  // the whole warp
-  uint8_t* base = reinterpret_cast<uint8_t*>(bv_dyn) + (size_t)wi * kBvWarpBytes;
-  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(base);
-  uint32_t(*hw)[4] = reinterpret_cast<uint32_t(*)[4]>(base + (size_t)2 * kLanes * kN * 8);
-  EngState* st = p.eng + k;
-  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
-  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
-  const int64_t off = g0 * p.gran, n = ng * p.gran;
-  if (n == 0) return;
-  int32_t* out = static_cast<int32_t*>(p.out);
-
-  for (int i = lane; i < kLanes * kN; i += 32) raw[0][i / kN][i % kN] = st->win[i / kN][i % kN];
-  __syncwarp();
-
-  // draws: the engine's cached half first, then the halves of new blocks
-  bool pending = st->half_valid != 0, abort = false;
+// The draws of a Vmt19937_64 stream as half packets: the engine's cached
+// upper half first, then the 624 half packets of each block the warp twists
+// (two lane windows in shared memory, the newest block's halves beside them).
+struct BvEngineSrc {
+  uint64_t (*raw)[kLanes][kN];
+  uint32_t (*hw)[4];
+  EngState* st;
+  int64_t max_blocks;
+  int lane;
+  bool pending, abort = false;
   int h = 2 * kN, cur = 0;
   int64_t nb = 0;
-  auto next = [&]() -> uint32_t {
+
+  __device__ __forceinline__ uint32_t next() {
     if (pending) {
       pending = false;
       return st->half_cache[lane & 3];
     }
     if (h == 2 * kN) {
-      if (nb >= a.max_blocks) {
+      if (nb >= max_blocks) {
         abort = true;
         return 0u;
       }
@@ -118,15 +109,51 @@ __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a)
       ++nb;
       h = 0;
     }
-    const uint32_t v = hw[h][lane & 3];
-    ++h;
-    return v;
-  };
-  auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
+    return hw[h++][lane & 3];
+  }
+  // the next 16 half packets are resident (no cached half, no new block)
+  __device__ bool peek_ok() const { return !pending && h + 16 <= 2 * kN; }
+  __device__ uint32_t peek(int k) const { return hw[h + k][lane & 3]; }
+  __device__ void skip(int m) { h += m; }
+  __device__ void mark() {}
+};
 
-  const int64_t npk = n / 4;
+// The draws of a scalar engine (std::mt19937_64, P8_mt19937_64) as SSE
+// uniform packets: RawbitsMaker<Packet4i, Rng, uint64_t, scalar_fullbit>::
+// rawbits_34 (arch/SSE/RandUtils.h:36-55) takes two 64-bit draws, the first
+// in int32 lanes 0-1 (GCC evaluates _mm_set_epi64x's arguments right to left).
+struct BvWordsSrc {
+  const uint64_t* w;
+  int64_t nh;  // half packets available
+  int lane;
+  bool abort = false;
+  int64_t q = 0, q0 = 0;
+
+  __device__ uint32_t at(int64_t hh) const {
+    const uint64_t x = w[2 * hh + ((lane & 3) >> 1)];
+    return (lane & 1) ? (uint32_t)(x >> 32) : (uint32_t)x;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (q >= nh) {
+      abort = true;
+      return 0u;
+    }
+    return at(q++);
+  }
+  __device__ bool peek_ok() const { return q + 16 <= nh; }
+  __device__ uint32_t peek(int k) const { return at(q + k); }
+  __device__ void skip(int m) { q += m; }
+  __device__ void mark() { q0 = q; }
+};
+
+// npk packets of BinomialVGen<int32_t>::packetOp from src, outputs and
+// parameters at element off + 4e + lane.  Returns the packets completed
+// (fewer than npk when src ran out).
+template <class Src>
+__device__ __forceinline__ int64_t bv_chain(Src& src, const BinomVArgs& a, int64_t off, int64_t npk, int32_t* out, int lane) {
+  auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
   const int jl = lane & 3;  // every group of 4 lanes holds the packet's 4 lanes
-  for (int64_t e0 = 0; e0 < npk && !abort; e0 += 8) {
+  for (int64_t e0 = 0; e0 < npk; e0 += 8) {
     // the parameter-only constants of packets e0 .. e0 + 7, group g = lane / 4
     // computing those of packet e0 + g
     int32_t trg = 0;
@@ -143,50 +170,49 @@ __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a)
     const float lspg = logf_(spg), lsqg = logf_(1.0f - spg);
     const float neg = expf_(-meang);
     const int kend = npk - e0 < 8 ? (int)(npk - e0) : 8;
-    for (int kk = 0; kk < kend && !abort; ++kk) {
-      const int64_t e = e0 + kk;
-      const int src = (kk << 2) | jl;
-      const int32_t tr = __shfl_sync(0xffffffffu, trg, src);
-      const float pv = __shfl_sync(0xffffffffu, pvg, src);
-      const float small_p = __shfl_sync(0xffffffffu, spg, src);
+    for (int kk = 0; kk < kend; ++kk) {
+      src.mark();
+      const int srcl = (kk << 2) | jl;
+      const int32_t tr = __shfl_sync(0xffffffffu, trg, srcl);
+      const float pv = __shfl_sync(0xffffffffu, pvg, srcl);
+      const float small_p = __shfl_sync(0xffffffffu, spg, srcl);
       const float ptrials = (float)tr;
-      const float mean = __shfl_sync(0xffffffffu, meang, src);
-      const float g1 = __shfl_sync(0xffffffffu, g1g, src);
-      const float sqrt_v = __shfl_sync(0xffffffffu, svg, src);
-      const float lsp = __shfl_sync(0xffffffffu, lspg, src), lsq = __shfl_sync(0xffffffffu, lsqg, src);
-      const float ne = __shfl_sync(0xffffffffu, neg, src);
-      const int64_t i = off + e * 4 + jl;
+      const float mean = __shfl_sync(0xffffffffu, meang, srcl);
+      const float g1 = __shfl_sync(0xffffffffu, g1g, srcl);
+      const float sqrt_v = __shfl_sync(0xffffffffu, svg, srcl);
+      const float lsp = __shfl_sync(0xffffffffu, lspg, srcl), lsq = __shfl_sync(0xffffffffu, lsqg, srcl);
+      const float ne = __shfl_sync(0xffffffffu, neg, srcl);
       bool valid = mean < 1.0f;
       float vres = 0.0f;
       if (mask4(valid)) {
         float val = 1.0f;
         int32_t res = 0;
         for (;;) {
-          val = val * bv_ur(next());
-          if (abort) break;
+          val = val * bv_ur(src.next());
+          if (src.abort) break;
           const bool c = (ne < val) && valid;
           if (mask4(c) == 0) break;
           res += c ? 1 : 0;
         }
         vres = (float)res;
       }
-      if (mask4(valid) != 0xfu) {
+      if (!src.abort && mask4(valid) != 0xfu) {
         const BvLane L{ptrials, mean, g1, sqrt_v, lsp, lsq};
         for (;;) {
-          if (!pending && h + 16 <= 2 * kN) {
+          if (src.peek_ok()) {
             // rounds r .. r + 7 at once, group g = lane / 4 evaluating round
-            // r + g on half packets h + 2g, h + 2g + 1 of the resident block; a
-            // lane keeps its first accepted proposal and the packet ends with
-            // the round in which its last lane first accepts, as round by round
-            const int g = lane >> 2, j = lane & 3;
+            // r + g on half packets 2g, 2g + 1 ahead; a lane keeps its first
+            // accepted proposal and the packet ends with the round in which
+            // its last lane first accepts, as round by round
+            const int g = lane >> 2;
             float fres;
-            const bool acc = bv_trial(L, hw[h + 2 * g][j], hw[h + 2 * g + 1][j], fres) && !valid;
+            const bool acc = bv_trial(L, src.peek(2 * g), src.peek(2 * g + 1), fres) && !valid;
             const unsigned bal = __ballot_sync(0xffffffffu, acc);
             unsigned mj = 0;
-  #pragma unroll
-            for (int q = 0; q < 8; ++q) mj |= ((bal >> (4 * q + j)) & 1u) << q;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) mj |= ((bal >> (4 * q + jl)) & 1u) << q;
             const int first = mj ? __ffs(mj) - 1 : 8;
-            const float ffirst = __shfl_sync(0xffffffffu, fres, ((first & 7) << 2) | j);
+            const float ffirst = __shfl_sync(0xffffffffu, fres, ((first & 7) << 2) | jl);
             int end = valid ? -1 : first;
             end = max(end, __shfl_xor_sync(0xffffffffu, end, 1));
             end = max(end, __shfl_xor_sync(0xffffffffu, end, 2));
@@ -195,49 +221,83 @@ __global__ void __launch_bounds__(32 * kBvWarps) k_binom_v(Plan p, BinomVArgs a)
               valid = true;
             }
             if (end < 8) {
-              h += 2 * (end + 1);
+              src.skip(2 * (end + 1));
               break;
             }
-            h += 16;
+            src.skip(16);
             continue;
           }
           float fres;
-          const uint32_t w1 = next();
-          const uint32_t w2 = next();
-          if (abort) break;
+          const uint32_t w1 = src.next();
+          const uint32_t w2 = src.next();
+          if (src.abort) break;
           const bool fv = bv_trial(L, w1, w2, fres);
           if (fv && !valid) vres = fres;
           valid = valid || fv;
           if (mask4(valid) == 0xfu) break;
         }
       }
-      if (abort) break;
-      if (lane < 4) out[i] = (pv == small_p) ? cvtt_f32(vres) : tr - cvtt_f32(vres);
+      if (src.abort) return e0 + kk;
+      if (lane < 4) out[off + (e0 + kk) * 4 + jl] = (pv == small_p) ? cvtt_f32(vres) : tr - cvtt_f32(vres);
     }
   }
+  return npk;
+}
+
+__global__ void __launch_bounds__(32 * kBvWarps, 1) k_binom_v(Plan p, BinomVArgs a) {
+  extern __shared__ __align__(16) uint64_t bv_dyn[];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kBvWarps + wi;
+  if (k >= p.K) return;  // the whole warp
+  uint8_t* base = reinterpret_cast<uint8_t*>(bv_dyn) + (size_t)wi * kBvWarpBytes;
+  EngState* st = p.eng + k;
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  BvEngineSrc src{reinterpret_cast<uint64_t(*)[kLanes][kN]>(base),
+                  reinterpret_cast<uint32_t(*)[4]>(base + (size_t)2 * kLanes * kN * 8), st, a.max_blocks, lane,
+                  st->half_valid != 0};
+  for (int i = lane; i < kLanes * kN; i += 32) src.raw[0][i / kN][i % kN] = st->win[i / kN][i % kN];
+  __syncwarp();
+  bv_chain(src, a, off, n / 4, static_cast<int32_t*>(p.out), lane);
 
   // ---- state after the call (as k_negbin: the last draw's block, the
   // cached upper half when a packet was split)
-  if (abort) {
+  if (src.abort) {
     if (lane == 0) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
     return;
   }
-  if (nb > 0) {
+  const int h = src.h;
+  if (src.nb > 0) {
     const int last = h - 1;       // last half packet drawn from the newest block
     const int rr = last / 2 + 1;  // packets used of it
-    uint64_t(*lastb)[kN] = raw[cur];
-    uint64_t(*prevb)[kN] = raw[cur ^ 1];
+    uint64_t(*lastb)[kN] = src.raw[src.cur];
+    uint64_t(*prevb)[kN] = src.raw[src.cur ^ 1];
     for (int t = lane; t < kLanes * kN; t += 32) {
       const int l = t / kN, i = t % kN;
       st->win[l][i] = (i < kN - rr) ? prevb[l][rr + i] : lastb[l][i - (kN - rr)];
     }
-    if (lane < 4) st->half_cache[lane] = (last & 1) == 0 ? hw[last + 1][lane] : 0u;
+    if (lane < 4) st->half_cache[lane] = (last & 1) == 0 ? src.hw[last + 1][lane] : 0u;
     if (lane == 0) {
       st->half_valid = (last & 1) == 0 ? 1 : 0;
-      st->consumed += (uint64_t)((nb - 1) * kN + rr);
+      st->consumed += (uint64_t)((src.nb - 1) * kN + rr);
     }
-  } else if (lane == 0 && st->half_valid && n > 0) {
+  } else if (lane == 0 && st->half_valid) {
     st->half_valid = 0;  // only the cached half was drawn
+  }
+}
+
+// One scalar-engine chain over pre-drawn words: res[0] = packets completed,
+// res[1] = 64-bit words they consumed.
+__global__ void __launch_bounds__(32) k_binom_v_words(const uint64_t* w, int64_t nwords, BinomVArgs a, int32_t* out,
+                                                     int64_t npk, int64_t* res) {
+  const int lane = threadIdx.x & 31;
+  BvWordsSrc src{w, nwords / 2, lane};
+  const int64_t done = bv_chain(src, a, 0, npk, out, lane);
+  if (lane == 0) {
+    res[0] = done;
+    res[1] = 2 * (done < npk ? src.q0 : src.q);
   }
 }
 
@@ -255,6 +315,12 @@ cudaError_t launch_binom_v(const Plan& p, const BinomVArgs& a, cudaStream_t s) {
     attr[dev] = true;
   }
   k_binom_v<<<(p.K + kBvWarps - 1) / kBvWarps, 32 * kBvWarps, smem, s>>>(p, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_binom_v_words(const uint64_t* w, int64_t nwords, const BinomVArgs& a, int32_t* out, int64_t npk,
+                                 int64_t* res, cudaStream_t s) {
+  k_binom_v_words<<<1, 32, 0, s>>>(w, nwords, a, out, npk, res);
   return cudaGetLastError();
 }
 

@@ -149,6 +149,10 @@ struct BinomVArgs {
   int64_t max_blocks;
 };
 cudaError_t launch_binom_v(const Plan& p, const BinomVArgs& a, cudaStream_t s);
+// The same on a scalar engine's pre-drawn 64-bit words (one chain): res[0] =
+// packets completed, res[1] = words they consumed.
+cudaError_t launch_binom_v_words(const uint64_t* w, int64_t nwords, const BinomVArgs& a, int32_t* out, int64_t npk,
+                                 int64_t* res, cudaStream_t s);
 
 // Batched vectorize-over-params sets (gr_vop.cu).
 struct VopArgs {

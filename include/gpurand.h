@@ -205,6 +205,16 @@ gr_status gr_sengine_create(gr_sengine** out, int32_t kind, uint64_t seed);
 gr_status gr_sengine_destroy(gr_sengine* e);
 gr_status gr_sengine_raw_u64(gr_sengine* e, uint64_t* dev_out, size_t n, gr_stream_t stream);
 gr_status gr_sengine_sample(gr_sengine* e, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream);
+/* binomial(urng, trials, p) with a scalar engine as the Urng (BinomialVGen<
+ * int32_t>, Discrete.h:1124-1192,1822-1898): arguments as gr_sample_v2
+ * (desc->kind GR_BINOMIAL, GR_I32).  Each uniform packet takes two 64-bit
+ * draws (RawbitsMaker<Packet4i, Rng, uint64_t, scalar_fullbit>::rawbits_34,
+ * arch/SSE/RandUtils.h:36-55).  The engine is one chain, so the call runs as
+ * one warp over chunks of pre-drawn words and synchronises the stream once per
+ * chunk; afterwards the engine stands exactly past the words used.  Other
+ * kinds: GR_ERR_UNSUPPORTED. */
+gr_status gr_sengine_sample_v2(gr_sengine* e, const gr_dist_desc* desc, const void* dev_a, const void* dev_b,
+                               void* dev_out, size_t n, gr_stream_t stream);
 
 /* ---- truncated distributions (EigenRand/Dists/Truncated.h) --------------
  * TruncGen<Base>{base, Support(lower, upper)} (Truncated.h:202-263 and the

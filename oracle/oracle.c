@@ -1927,6 +1927,20 @@ int or_sgen_real(or_seng* s, or_gen* g, int dist, int dtype, double a, double b,
   return rc;
 }
 
+/* binomial(urng, trials, p) with a scalar engine as the Urng: BinomialVGen<
+ * int32_t> whose uniform packets take two draws each (draw_half). */
+int or_sgen_binomial_v(or_seng* s, const int32_t* trials, const float* p, int32_t trials0, float p0, int32_t* out,
+                       size_t n) {
+  or_vmt dummy;
+  memset(&dummy, 0, sizeof dummy);
+  dummy.L = 4;
+  or_seng* prev = g_src;
+  g_src = s;
+  const int rc = or_gen_binomial_v(&dummy, trials, p, trials0, p0, out, n);
+  g_src = prev;
+  return rc;
+}
+
 int or_sgen_randbits(or_seng* s, int32_t* out, size_t n) {
   or_vmt dummy;
   memset(&dummy, 0, sizeof dummy);

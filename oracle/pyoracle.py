@@ -92,6 +92,8 @@ def lib():
         L.or_gen_real_v.restype = ctypes.c_int
         L.or_gen_binomial_v.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_float, vp, ctypes.c_size_t]
         L.or_gen_binomial_v.restype = ctypes.c_int
+        L.or_sgen_binomial_v.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_float, vp, ctypes.c_size_t]
+        L.or_sgen_binomial_v.restype = ctypes.c_int
         L.or_gen_trunc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, vp, sz]
         L.or_gen_trunc.restype = ctypes.c_int
@@ -152,6 +154,19 @@ class ScalarEngine:
     def raw(self, n):
         out = np.empty(n, dtype=np.uint64)
         self.L.or_seng_raw(self.h, _p(out), n)
+        return out
+
+    def binomial_v(self, trials, p):
+        """binomial(urng, trials, p) (BinomialVGen<int32_t>) through the scalar engine."""
+        ta = np.ascontiguousarray(trials, dtype=np.int32) if isinstance(trials, np.ndarray) else None
+        pa = np.ascontiguousarray(p, dtype=np.float32) if isinstance(p, np.ndarray) else None
+        n = (ta if ta is not None else pa).size
+        out = np.empty(n, dtype=np.int32)
+        rc = self.L.or_sgen_binomial_v(self.h, _p(ta) if ta is not None else None, _p(pa) if pa is not None else None,
+                                       0 if ta is not None else int(trials), 0.0 if pa is not None else float(p),
+                                       _p(out), n)
+        if rc:
+            raise RuntimeError(f"oracle error {rc}")
         return out
 
     def generate(self, gen, kind, n, dtype=np.float32, a=0.0, b=0.0):

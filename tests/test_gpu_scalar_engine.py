@@ -92,3 +92,34 @@ def test_scalar_engine_randbits_and_mirror(er, oracle, okind, cls):
         er.gamma(8, 1, u, 0.5, 1.0)
     with pytest.raises(er.GrError):
         er.NormalGen().generate(8, 1, u)
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_binomial_v(er, oracle, okind, cls):
+    """binomial(urng, trials, p) with a scalar engine (the reference's own
+    binomialV test uses P8_mt19937_64{42}: test.cpp:470-490): its three
+    overloads on the test's shapes, a call large enough for several chunks of
+    pre-drawn words, and raw draws after each call (the engine stands exactly
+    past the words the packets used)."""
+    u = getattr(er, cls)(42)
+    o = oracle.ScalarEngine(okind, 42)
+    a = np.linspace(5, 50, 10).astype(np.int32)
+    b = np.linspace(0.1, 1.0, 10).astype(np.float32)
+    A = np.tile(a[:, None], (1, 100))
+    B = np.tile(b[:, None], (1, 100))
+    got = er.binomial(u, torch.from_numpy(A), 0.5)
+    assert_bits_equal(mem(got), o.binomial_v(A.T.reshape(-1), 0.5), "trials array, p 0.5")
+    got = er.binomial(u, 50, torch.from_numpy(B))
+    assert_bits_equal(mem(got), o.binomial_v(50, B.T.reshape(-1)), "trials 50, p array")
+    got = er.binomial(u, torch.from_numpy(A), torch.from_numpy(B))
+    assert_bits_equal(mem(got), o.binomial_v(A.T.reshape(-1), B.T.reshape(-1)), "both arrays")
+    assert_bits_equal(u.raw(5).cpu().numpy().view(np.uint64), o.raw(5), "raw after")
+    r = np.random.default_rng(8)
+    n = 4 * 30000
+    tr = r.choice(np.array([0, 3, 20, 100, 5000], np.int32), n)
+    p = r.random(n).astype(np.float32)
+    got = er.binomial(u, torch.from_numpy(tr), torch.from_numpy(p))
+    assert_bits_equal(mem(got), o.binomial_v(tr, p), "long call")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), "raw after the long call")
+    with pytest.raises(er.GrError):
+        er.normal(u, torch.ones(8), torch.ones(8))

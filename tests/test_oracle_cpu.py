@@ -387,3 +387,24 @@ def test_oracle_binomial_per_element(oracle):
     np.testing.assert_array_equal(y, np.where(edge_p == 1.0, edge_tr, 0))
     with pytest.raises(RuntimeError):
         oracle.binomial_v(oracle.Engine(2), np.ones(6, np.int32), 0.5)
+
+
+def test_oracle_binomial_per_element_scalar_engine(oracle):
+    """BinomialVGen<int32_t> on scalar engines: values inside [0, trials],
+    per-element means, and the engine consumption (two draws per uniform
+    packet): p = 0 lanes with mean 0 draw exactly one uniform packet each."""
+    for kind in ("mt19937_64", "p8"):
+        s = oracle.ScalarEngine(kind, 42)
+        n = 4 * 8192
+        tr = np.full(n, 40, np.int32)
+        p = np.where(np.arange(n) % 2 == 0, 0.25, 0.6).astype(np.float32)
+        x = s.binomial_v(tr, p)
+        assert (x >= 0).all() and (x <= 40).all()
+        for P in (0.25, 0.6):
+            m = x[p == np.float32(P)].mean()
+            assert abs(m - 40 * P) < 0.15, (kind, P, m)
+        s1, s2 = oracle.ScalarEngine(kind, 7), oracle.ScalarEngine(kind, 7)
+        z = s1.binomial_v(np.full(40, 9, np.int32), 0.0)
+        np.testing.assert_array_equal(z, 0)
+        s2.raw(2 * 10)
+        np.testing.assert_array_equal(s1.raw(4), s2.raw(4))
