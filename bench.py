@@ -482,6 +482,10 @@ def bench_multivariate(er, streams=608):
     mg = er.MultinomialGen(trials, p)
     out = torch.empty((n, K), dtype=torch.int32, device="cuda").t()
     ms = _median_ms(lambda: mg.generate(urng, n, out=out))
+    res["multinomial_k10_t1000_conditional"] = {"draws": n, "ms": round(ms, 3), "mdraws_s": round(n / ms / 1e3, 2),
+                                                "binomial_rows_g_s": round(n * (K - 1) / (ms / 1e3) / 1e9, 2),
+                                                "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
+    del out
     # TruncMvNormalGen, the 9-dimensional case of the reference's tests, default
     # burn-in (5 * dim sweeps, one scalar draw per component and chain)
     c = np.zeros((9, 9))
@@ -494,10 +498,6 @@ def bench_multivariate(er, streams=608):
     ms = _median_ms(lambda: tg.generate(urng, n, out=out))
     res["truncmvnormal_d9_n1e5"] = {"samples": n, "ms": round(ms, 3), "gibbs_steps_g_s":
                                     round(n * 9 * 45 / (ms / 1e3) / 1e9, 2)}
-    del out
-    res["multinomial_k10_t1000_conditional"] = {"draws": n, "ms": round(ms, 3), "mdraws_s": round(n / ms / 1e3, 2),
-                                                "binomial_rows_g_s": round(n * (K - 1) / (ms / 1e3) / 1e9, 2),
-                                                "gbs_out": round(4 * K * n / (ms / 1e3) / 1e9, 1)}
     del out
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
@@ -809,6 +809,26 @@ def run_case(args):
         g = er.PoissonGen(4.0)
         out = torch.empty((2048, 2048), dtype=torch.int32, device="cuda")
         fn = lambda: g.generate(2048, 2048, urng, out=out)
+    elif name == "binomial_v":  # per-element binomial, trials 20 / 50 / 100 by column, p 0.5 / 0.01 / 0.75 by row
+        idx = torch.arange(2048, device="cuda")
+        tr = torch.tensor([20, 50, 100], dtype=torch.int32, device="cuda")[idx % 3][None, :].expand(2048, 2048)
+        pr = torch.tensor([0.5, 0.01, 0.75], device="cuda")[idx % 3][:, None].expand(2048, 2048)
+        tr, pr = tr.t().contiguous().t(), pr.t().contiguous().t()
+        out = torch.empty_like(tr)
+        fn = lambda: er.binomial(urng, tr, pr, out=out)
+    elif name == "truncmvn_d9":  # TruncMvNormalGen, the reference tests' d = 9 case, 10^5 chains
+        c = np.zeros((9, 9))
+        c[0, 1], c[2, 7], c[3, 1] = 0.5, 0.5, 0.7
+        c[np.diag_indices(9)] = [1, 1.2, 1.4, 1.6, 1.8, 1.6, 1.4, 1.2, 1]
+        g = er.TruncMvNormalGen([-1, 0, 1, 2, 3, 2, 1, 0, -1], c @ c.T,
+                                er.support([-4, -3, -2, -1, 0, -1, -2, -3, -4], [4, 5, 6, 7, 8, 7, 6, 5, 4]))
+        out = torch.empty((100000, 9), dtype=torch.float32, device="cuda").t()
+        fn = lambda: g.generate(urng, 100000, out=out)
+    elif name == "multinomial_cond":  # conditional-binomial path, K = 10, trials = 1000
+        g = er.MultinomialGen(1000, np.random.default_rng(99).dirichlet(np.ones(10)))
+        n = 1 << 18
+        out = torch.empty((n, 10), dtype=torch.int32, device="cuda").t()
+        fn = lambda: g.generate(urng, n, out=out)
     elif name == "gamma_compat":
         u1 = er.Vmt19937_64(1234)
         g = er.GammaGen(0.5, 1.0)

@@ -28,9 +28,11 @@
 namespace gr {
 namespace {
 
-constexpr int kBvWarps = 4;  // engines per CTA
-// per warp: two lane windows, then the newest block's 624 half packets
-constexpr size_t kBvWarpBytes = (size_t)2 * kLanes * kN * 8 + (size_t)2 * kN * 16;
+constexpr int kBvWarps = 1;  // engines per CTA
+// per warp: two lane windows (the newest block and the one before)
+constexpr size_t kBvWarpBytes = (size_t)2 * kLanes * kN * 8;
+// with the newest block's 624 half packets stored tempered beside them
+constexpr size_t kBvWarpBytesBuf = kBvWarpBytes + (size_t)2 * kN * 16;
 
 __device__ __forceinline__ float bv_ur(uint32_t x) { return u2f((x & 0x7fffffu) | (127u << 23)) - 1.0f; }
 
@@ -57,7 +59,10 @@ __device__ __forceinline__ bool bv_trial(const BvLane& L, uint32_t w1, uint32_t 
 
 // The draws of a Vmt19937_64 stream as half packets: the engine's cached
 // upper half first, then the 624 half packets of each block the warp twists
-// (two lane windows in shared memory, the newest block's halves beside them).
+// (two lane windows in shared memory).  BUF: the newest block's half packets
+// are tempered once into a buffer (10 KB more shared memory, a shorter chain
+// per draw); otherwise each draw tempers its word as it is read.
+template <bool BUF>
 struct BvEngineSrc {
   uint64_t (*raw)[kLanes][kN];
   uint32_t (*hw)[4];
@@ -85,23 +90,25 @@ struct BvEngineSrc {
       for (int ph = 0; ph < 2; ++ph) {
         for (int ii = lane; ii < kM; ii += 32) {
           const int i = ph * kM + ii;
-          uint64_t pk[kLanes];
 #pragma unroll
           for (int l = 0; l < kLanes; ++l) {
             const uint64_t b = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
             const uint64_t c = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
-            const uint64_t v = mt_twist(old[l][i], b, c);
-            nw[l][i] = v;
-            pk[l] = mt_temper(v);
+            nw[l][i] = mt_twist(old[l][i], b, c);
           }
-          hw[2 * i][0] = (uint32_t)pk[0];
-          hw[2 * i][1] = (uint32_t)(pk[0] >> 32);
-          hw[2 * i][2] = (uint32_t)pk[1];
-          hw[2 * i][3] = (uint32_t)(pk[1] >> 32);
-          hw[2 * i + 1][0] = (uint32_t)pk[2];
-          hw[2 * i + 1][1] = (uint32_t)(pk[2] >> 32);
-          hw[2 * i + 1][2] = (uint32_t)pk[3];
-          hw[2 * i + 1][3] = (uint32_t)(pk[3] >> 32);
+          if (BUF) {
+            uint64_t pk[kLanes];
+#pragma unroll
+            for (int l = 0; l < kLanes; ++l) pk[l] = mt_temper(nw[l][i]);
+            hw[2 * i][0] = (uint32_t)pk[0];
+            hw[2 * i][1] = (uint32_t)(pk[0] >> 32);
+            hw[2 * i][2] = (uint32_t)pk[1];
+            hw[2 * i][3] = (uint32_t)(pk[1] >> 32);
+            hw[2 * i + 1][0] = (uint32_t)pk[2];
+            hw[2 * i + 1][1] = (uint32_t)(pk[2] >> 32);
+            hw[2 * i + 1][2] = (uint32_t)pk[3];
+            hw[2 * i + 1][3] = (uint32_t)(pk[3] >> 32);
+          }
         }
         __syncwarp();
       }
@@ -109,11 +116,18 @@ struct BvEngineSrc {
       ++nb;
       h = 0;
     }
-    return hw[h++][lane & 3];
+    return half(h++);
+  }
+  // word (lane & 3) of half packet hh of the newest block: packet hh / 2,
+  // its lanes 0-1 (hh even) or 2-3 (hh odd), low or high half of the lane
+  __device__ __forceinline__ uint32_t half(int hh) const {
+    if (BUF) return hw[hh][lane & 3];
+    const uint64_t t = mt_temper(raw[cur][2 * (hh & 1) + ((lane & 3) >> 1)][hh >> 1]);
+    return (lane & 1) ? (uint32_t)(t >> 32) : (uint32_t)t;
   }
   // the next 16 half packets are resident (no cached half, no new block)
   __device__ bool peek_ok() const { return !pending && h + 16 <= 2 * kN; }
-  __device__ uint32_t peek(int k) const { return hw[h + k][lane & 3]; }
+  __device__ uint32_t peek(int k) const { return half(h + k); }
   __device__ void skip(int m) { h += m; }
   __device__ void mark() {}
 };
@@ -244,20 +258,21 @@ __device__ __forceinline__ int64_t bv_chain(Src& src, const BinomVArgs& a, int64
   return npk;
 }
 
+template <bool BUF>
 __global__ void __launch_bounds__(32 * kBvWarps, 1) k_binom_v(Plan p, BinomVArgs a) {
   extern __shared__ __align__(16) uint64_t bv_dyn[];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * kBvWarps + wi;
   if (k >= p.K) return;  // the whole warp
-  uint8_t* base = reinterpret_cast<uint8_t*>(bv_dyn) + (size_t)wi * kBvWarpBytes;
+  uint8_t* base = reinterpret_cast<uint8_t*>(bv_dyn) + (size_t)wi * (BUF ? kBvWarpBytesBuf : kBvWarpBytes);
   EngState* st = p.eng + k;
   const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
   const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
   const int64_t off = g0 * p.gran, n = ng * p.gran;
   if (n == 0) return;
-  BvEngineSrc src{reinterpret_cast<uint64_t(*)[kLanes][kN]>(base),
-                  reinterpret_cast<uint32_t(*)[4]>(base + (size_t)2 * kLanes * kN * 8), st, a.max_blocks, lane,
-                  st->half_valid != 0};
+  BvEngineSrc<BUF> src{reinterpret_cast<uint64_t(*)[kLanes][kN]>(base),
+                       reinterpret_cast<uint32_t(*)[4]>(base + kBvWarpBytes), st, a.max_blocks, lane,
+                       st->half_valid != 0};
   for (int i = lane; i < kLanes * kN; i += 32) src.raw[0][i / kN][i % kN] = st->win[i / kN][i % kN];
   __syncwarp();
   bv_chain(src, a, off, n / 4, static_cast<int32_t*>(p.out), lane);
@@ -278,7 +293,7 @@ __global__ void __launch_bounds__(32 * kBvWarps, 1) k_binom_v(Plan p, BinomVArgs
       const int l = t / kN, i = t % kN;
       st->win[l][i] = (i < kN - rr) ? prevb[l][rr + i] : lastb[l][i - (kN - rr)];
     }
-    if (lane < 4) st->half_cache[lane] = (last & 1) == 0 ? src.hw[last + 1][lane] : 0u;
+    if (lane < 4) st->half_cache[lane] = (last & 1) == 0 ? src.half(last + 1) : 0u;
     if (lane == 0) {
       st->half_valid = (last & 1) == 0 ? 1 : 0;
       st->consumed += (uint64_t)((src.nb - 1) * kN + rr);
@@ -304,17 +319,28 @@ __global__ void __launch_bounds__(32) k_binom_v_words(const uint64_t* w, int64_t
 }  // namespace
 
 cudaError_t launch_binom_v(const Plan& p, const BinomVArgs& a, cudaStream_t s) {
-  constexpr size_t smem = kBvWarpBytes * kBvWarps;
   static bool attr[64] = {};
+  static int sms[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_binom_v, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_binom_v<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kBvWarpBytesBuf * kBvWarps));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_binom_v<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(kBvWarpBytes * kBvWarps));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  k_binom_v<<<(p.K + kBvWarps - 1) / kBvWarps, 32 * kBvWarps, smem, s>>>(p, a);
+  const unsigned grid = (unsigned)((p.K + kBvWarps - 1) / kBvWarps);
+  // the buffered form while every stream's CTA is resident at 30 KB (7 per
+  // SM); with more streams the 20 KB form fits 11 per SM
+  if ((int64_t)grid <= 7LL * sms[dev])
+    k_binom_v<true><<<grid, 32 * kBvWarps, kBvWarpBytesBuf * kBvWarps, s>>>(p, a);
+  else
+    k_binom_v<false><<<grid, 32 * kBvWarps, kBvWarpBytes * kBvWarps, s>>>(p, a);
   return cudaGetLastError();
 }
 

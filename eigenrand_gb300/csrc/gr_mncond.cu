@@ -27,20 +27,25 @@
 namespace gr {
 namespace {
 
-constexpr int kMcWarps = 4;  // engines per CTA
-// per warp: two lane windows, then the newest block's packets as 8 words each
-constexpr size_t kMcWarpBytes = (size_t)2 * kLanes * kN * 8 + (size_t)kN * 32;
+constexpr int kMcWarps = 1;  // engines per CTA
+// per warp: two lane windows (the newest block and the one before) ...
+constexpr size_t kMcWarpBytes = (size_t)2 * kLanes * kN * 8;
+// ... and, buffered, the newest block's packets tempered into 8 words each
+constexpr size_t kMcWarpBytesBuf = kMcWarpBytes + (size_t)kN * 32;
 
 __device__ __forceinline__ float ur_word(uint32_t x) { return u2f((x & 0x7fffffu) | (127u << 23)) - 1.0f; }
 
+// BUF: temper each new block once into a packet buffer (10 KB more shared
+// memory, a shorter chain per draw); otherwise temper the words as read.
+template <bool BUF>
 __global__ void __launch_bounds__(32 * kMcWarps) k_mn_cond(Plan p, McArgs a) {
   extern __shared__ __align__(16) uint64_t mc_dyn[];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * kMcWarps + wi;
   if (k >= p.K) return;  // the whole warp
-  uint8_t* base = reinterpret_cast<uint8_t*>(mc_dyn) + (size_t)wi * kMcWarpBytes;
+  uint8_t* base = reinterpret_cast<uint8_t*>(mc_dyn) + (size_t)wi * (BUF ? kMcWarpBytesBuf : kMcWarpBytes);
   uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(base);
-  uint32_t(*pw)[8] = reinterpret_cast<uint32_t(*)[8]>(base + (size_t)2 * kLanes * kN * 8);
+  uint32_t(*pw)[8] = reinterpret_cast<uint32_t(*)[8]>(base + kMcWarpBytes);
   EngState* st = p.eng + k;
   const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
   const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
@@ -75,11 +80,12 @@ __global__ void __launch_bounds__(32 * kMcWarps) k_mn_cond(Plan p, McArgs a) {
           for (int l = 0; l < kLanes; ++l) {
             const uint64_t b = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
             const uint64_t c = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
-            const uint64_t v = mt_twist(old[l][i], b, c);
-            nw[l][i] = v;
-            const uint64_t t = mt_temper(v);
-            pw[i][2 * l] = (uint32_t)t;
-            pw[i][2 * l + 1] = (uint32_t)(t >> 32);
+            nw[l][i] = mt_twist(old[l][i], b, c);
+            if (BUF) {
+              const uint64_t t = mt_temper(nw[l][i]);
+              pw[i][2 * l] = (uint32_t)t;
+              pw[i][2 * l + 1] = (uint32_t)(t >> 32);
+            }
           }
         }
         __syncwarp();
@@ -88,9 +94,16 @@ __global__ void __launch_bounds__(32 * kMcWarps) k_mn_cond(Plan p, McArgs a) {
       ++nb;
       h = 0;
     }
-    const uint32_t v = lane < 8 ? pw[h][lane] : 0u;
+    if (BUF) {
+      const uint32_t v = lane < 8 ? pw[h][lane] : 0u;
+      ++h;
+      return v;
+    }
+    // tempered as read: word j of packet h is the low (j even) or high half
+    // of lane j / 2
+    const uint64_t t = mt_temper(raw[cur][(lane & 7) >> 1][h]);
     ++h;
-    return v;
+    return lane < 8 ? ((lane & 1) ? (uint32_t)(t >> 32) : (uint32_t)t) : 0u;
   };
   auto mask8 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 8) & 0xffu; };
 
@@ -169,17 +182,28 @@ __global__ void __launch_bounds__(32 * kMcWarps) k_mn_cond(Plan p, McArgs a) {
 }  // namespace
 
 cudaError_t launch_mn_cond(const Plan& p, const McArgs& a, cudaStream_t s) {
-  constexpr size_t smem = kMcWarpBytes * kMcWarps;
   static bool attr[64] = {};
+  static int sms[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_mn_cond, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_mn_cond<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kMcWarpBytesBuf * kMcWarps));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_mn_cond<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(kMcWarpBytes * kMcWarps));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  k_mn_cond<<<(p.K + kMcWarps - 1) / kMcWarps, 32 * kMcWarps, smem, s>>>(p, a);
+  const unsigned grid = (unsigned)((p.K + kMcWarps - 1) / kMcWarps);
+  // buffered while every stream's CTA is resident at 30 KB (7 per SM); with
+  // more streams the 20 KB form fits 11 per SM
+  if ((int64_t)grid <= 7LL * sms[dev])
+    k_mn_cond<true><<<grid, 32 * kMcWarps, kMcWarpBytesBuf * kMcWarps, s>>>(p, a);
+  else
+    k_mn_cond<false><<<grid, 32 * kMcWarps, kMcWarpBytes * kMcWarps, s>>>(p, a);
   return cudaGetLastError();
 }
 

@@ -403,3 +403,23 @@ def test_truncmvn_from_lt_and_errors(er, oracle):
         er.TruncMvNormalGen(mean, cov, er.support([0, 0, 5], [1, 1, 1]))
     with pytest.raises(er.GrError):
         er.TruncMvNormalGen(np.zeros(65), np.eye(65), er.support(-np.ones(65), np.ones(65)))
+
+
+def test_multinomial_conditional_many_streams(er, oracle):
+    """More streams than 7 CTAs per SM take the kernel form that tempers each
+    word as it reads it (20 KB of shared memory per stream): every slice of
+    a 1500-stream engine, and the engines' next draws, against the oracle."""
+    w = np.random.default_rng(3).uniform(0.1, 2.0, 6)
+    g = er.MultinomialGen(500, w)
+    K = 1500
+    u = er.Vmt19937_64(91, streams=K)
+    samples = 8 * (2 * K + 7)
+    a = rows(g.generate(u, samples))
+    raw = er.raw_u64(u, 4 * K).cpu().numpy().view(np.uint64)
+    gran, off = samples // 8, 0
+    for k in range(K):
+        n = 8 * (gran // K + (1 if k < gran % K else 0))
+        e = oracle.Engine(91 + 4 * k)
+        np.testing.assert_array_equal(a[off:off + n], oracle.multinomial_cond(e, w, 500, n), err_msg=f"stream {k}")
+        np.testing.assert_array_equal(raw[4 * k:4 * k + 4], e.raw(1), err_msg=f"stream {k} after")
+        off += n

@@ -188,3 +188,21 @@ def test_binomial_v_streams_and_errors(er, oracle):
         er.binomial(er.Vmt19937_64(1), torch.ones(10, dtype=torch.int32), 0.5)
     with pytest.raises(ValueError):
         er.binomial(er.Vmt19937_64(1), torch.ones(8, dtype=torch.int32), torch.ones(12))
+
+
+def test_binomial_v_many_streams(er, oracle):
+    """More streams than 7 CTAs per SM take the kernel form that tempers each
+    half packet as it reads it: every slice of a 1500-stream engine, the
+    engines' half caches and windows (next draws), against the oracle."""
+    K, per = 1500, 4 * 7
+    u = er.Vmt19937_64(55, streams=K)
+    r = np.random.default_rng(12)
+    tr, p = _binom_params(r, K * per)
+    got = eigen_mem(er.binomial(u, torch.from_numpy(tr), torch.from_numpy(p)))
+    nxt = eigen_mem(er.binomial(u, 30, torch.full((4 * K,), 0.4)))
+    for k in range(K):
+        e = oracle.Engine(55 + 4 * k)
+        sl = slice(k * per, (k + 1) * per)
+        assert_bits_equal(got[sl], oracle.binomial_v(e, tr[sl], p[sl]), f"stream {k}")
+        assert_bits_equal(nxt[4 * k:4 * k + 4], oracle.binomial_v(e, 30, np.full(4, 0.4, np.float32)),
+                          f"stream {k} next")
