@@ -1571,18 +1571,15 @@ gr_status sengine_words(gr_sengine* se, uint64_t* out, int64_t W, cudaStream_t s
   return GR_OK;
 }
 
-// binomial(urng, trials, p) on a scalar engine: one chain, so chunks of the
-// engine's words are drawn into HBM from a saved engine state, a single warp
-// runs BinomialVGen<int32_t> over them until they run out, and the engine is
-// put back and advanced by exactly the words the completed packets used.
-gr_status sengine_binom_v(gr_sengine* se, const gr_dist_desc& d, const void* dev_a, const void* dev_b, void* out,
-                          size_t n, cudaStream_t s) {
-  if (d.dtype != GR_I32) return fail(GR_ERR_UNSUPPORTED, "per-element binomial: BinomialVGen<int32_t> only");
-  if (n % 4) return fail(GR_ERR_INVALID, "size must be a multiple of 4 (the reference packet width for this type)");
-  if (n == 0) return GR_OK;
-  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+// A one-chain sampler on a scalar engine: chunks of the engine's words are
+// drawn into HBM from a saved engine state, one warp runs the sampler over
+// them until they run out (launch(w, W, done, res) for the packets from
+// `done` on, res = {packets completed, words they used}), and the engine is
+// put back and advanced by exactly the words used.  wpp: words per packet
+// expected, for the first chunk's size.
+template <class Launch>
+gr_status sengine_chain(gr_sengine* se, int64_t npk, int64_t wpp, Launch&& launch, cudaStream_t s) {
   gr_engine* e = se->eng;
-  const int64_t npk = (int64_t)(n / 4);
   constexpr int64_t kMaxWords = (int64_t)1 << 24;
   EngState* saved = nullptr;
   uint64_t *w = nullptr, *pb = nullptr;
@@ -1594,52 +1591,93 @@ gr_status sengine_binom_v(gr_sengine* se, const gr_dist_desc& d, const void* dev
     cudaFreeAsync(res, s);
     return st;
   };
-  cudaError_t aerr = cudaMallocAsync(&saved, sizeof(EngState) * (size_t)e->K, s);
-  if (aerr == cudaSuccess) aerr = cudaMallocAsync(&pb, sizeof(uint64_t) * 8, s);
-  if (aerr == cudaSuccess) aerr = cudaMallocAsync(&res, sizeof(int64_t) * 2, s);
-  BinomVArgs a{};
-  a.trials0 = d.trials;
-  a.p0 = (float)d.a;
-  // about 10 half packets (20 words) per packet in common parameter ranges
-  int64_t W = std::min<int64_t>(kMaxWords, std::max<int64_t>(4096, 24 * npk));
-  if (aerr == cudaSuccess) aerr = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
-  if (aerr != cudaSuccess) return bail(cuda_fail(aerr, "per-element binomial scratch"));
+  int64_t W = std::min<int64_t>(kMaxWords, std::max<int64_t>(4096, wpp * npk + 64));
+  cudaError_t err = cudaMallocAsync(&saved, sizeof(EngState) * (size_t)e->K, s);
+  if (err == cudaSuccess) err = cudaMallocAsync(&pb, sizeof(uint64_t) * 8, s);
+  if (err == cudaSuccess) err = cudaMallocAsync(&res, sizeof(int64_t) * 2, s);
+  if (err == cudaSuccess) err = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
+  if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine chain scratch"));
   for (int64_t done = 0; done < npk;) {
-    cudaError_t err = cudaMemcpyAsync(saved, e->st, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
+    err = cudaMemcpyAsync(saved, e->st, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
     if (err == cudaSuccess && se->pbuf)
       err = cudaMemcpyAsync(pb, se->pbuf, sizeof(uint64_t) * 8, cudaMemcpyDeviceToDevice, s);
     if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine state copy"));
     const int cnt0 = se->cnt;
     gr_status st = sengine_words(se, w, W, s);
     if (st != GR_OK) return bail(st);
-    a.trials = dev_a ? static_cast<const int32_t*>(dev_a) + 4 * done : nullptr;
-    a.p = dev_b ? static_cast<const float*>(dev_b) + 4 * done : nullptr;
-    err = launch_binom_v_words(w, W, a, static_cast<int32_t*>(out) + 4 * done, npk - done, res, s);
+    err = launch(w, W, done, res);
     int64_t hres[2] = {0, 0};
     if (err == cudaSuccess) err = cudaMemcpyAsync(hres, res, sizeof hres, cudaMemcpyDeviceToHost, s);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
-    if (err != cudaSuccess) return bail(cuda_fail(err, "per-element binomial on a scalar engine"));
-    if (hres[0] == 0) {
-      if (W == kMaxWords) return bail(fail(GR_ERR_REJECT_LIMIT, "per-element binomial: a packet drew more than 2^24 words"));
-      W = std::min<int64_t>(kMaxWords, 2 * W);  // these words are drawn again below, more of them
-      cudaFreeAsync(w, s);
-      w = nullptr;
-      if (aerr == cudaSuccess) aerr = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
-  if (aerr != cudaSuccess) return bail(cuda_fail(aerr, "per-element binomial scratch"));
-    }
+    if (err != cudaSuccess) return bail(cuda_fail(err, "sampling on a scalar engine"));
     // back to the saved state, then forward by the words the packets used
     err = cudaMemcpyAsync(e->st, saved, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
     if (err == cudaSuccess && se->pbuf)
       err = cudaMemcpyAsync(se->pbuf, pb, sizeof(uint64_t) * 8, cudaMemcpyDeviceToDevice, s);
     if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine state copy"));
     se->cnt = cnt0;
-    if (hres[1] > 0) {
-      st = sengine_words(se, w, hres[1], s);
-      if (st != GR_OK) return bail(st);
+    if (hres[0] == 0) {  // one packet needs more words than the chunk: a larger chunk
+      if (W == kMaxWords) return bail(fail(GR_ERR_REJECT_LIMIT, "a packet drew more than 2^24 words"));
+      W = std::min<int64_t>(kMaxWords, 2 * W);
+      cudaFreeAsync(w, s);
+      w = nullptr;
+      err = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
+      if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine chain scratch"));
+      continue;
     }
+    st = sengine_words(se, w, hres[1], s);
+    if (st != GR_OK) return bail(st);
     done += hres[0];
   }
   return bail(GR_OK);
+}
+
+// binomial(urng, trials, p) on a scalar engine (BinomialVGen<int32_t>)
+gr_status sengine_binom_v(gr_sengine* se, const gr_dist_desc& d, const void* dev_a, const void* dev_b, void* out,
+                          size_t n, cudaStream_t s) {
+  if (d.dtype != GR_I32) return fail(GR_ERR_UNSUPPORTED, "per-element binomial: BinomialVGen<int32_t> only");
+  if (n % 4) return fail(GR_ERR_INVALID, "size must be a multiple of 4 (the reference packet width for this type)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  const int64_t npk = (int64_t)(n / 4);
+  BinomVArgs a{};
+  a.trials0 = d.trials;
+  a.p0 = (float)d.a;
+  // about 10 half packets (20 words) per packet in common parameter ranges
+  return sengine_chain(
+      se, npk, 24,
+      [&](const uint64_t* w, int64_t W, int64_t done, int64_t* res) {
+        a.trials = dev_a ? static_cast<const int32_t*>(dev_a) + 4 * done : nullptr;
+        a.p = dev_b ? static_cast<const float*>(dev_b) + 4 * done : nullptr;
+        return launch_binom_v_words(w, W, a, static_cast<int32_t*>(out) + 4 * done, npk - done, res, s);
+      },
+      s);
+}
+
+// PoissonGen / BinomialGen (int32) on a scalar engine: a fresh generator, so
+// CompressMask's carried lanes start empty and are dropped after the call
+gr_status sengine_int(gr_sengine* se, const DistParams& dp, void* out, size_t n, cudaStream_t s) {
+  if (n % 4) return fail(GR_ERR_INVALID, "size must be a multiple of 4 (the reference packet width for this type)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  const int64_t npk = (int64_t)(n / 4);
+  uint32_t* carry = nullptr;
+  GR_CUDA(cudaMallocAsync(&carry, sizeof(uint32_t) * 9, s));
+  cudaError_t err = cudaMemsetAsync(carry, 0, sizeof(uint32_t) * 9, s);
+  if (err != cudaSuccess) {
+    cudaFreeAsync(carry, s);
+    return cuda_fail(err, "scalar engine carry");
+  }
+  int64_t wpp = 24;
+  if (dp.kind == GR_BINOMIAL && dp.ia < 25) wpp = 2 * std::max(dp.ia, 0) + 2;
+  const gr_status st = sengine_chain(
+      se, npk, wpp,
+      [&](const uint64_t* w, int64_t W, int64_t done, int64_t* res) {
+        return launch_int_words(w, W, dp, static_cast<int32_t*>(out) + 4 * done, npk - done, res, carry, s);
+      },
+      s);
+  cudaFreeAsync(carry, s);
+  return st;
 }
 
 }  // namespace
@@ -1692,11 +1730,13 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
   DistParams dp{};
   gr_status st = make_params(*desc, dp);
   if (st != GR_OK) return st;
+  if (dp.dtype == GR_I32 && (dp.kind == GR_POISSON || dp.kind == GR_BINOMIAL))
+    return sengine_int(se, dp, dev_out, n, s);
   const int wpp = scalar_words_per_packet(dp.kind, dp.dtype);
   if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
     return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
-                                    "randBits)");
+                                    "randBits), poisson and binomial");
   const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
   if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
   if (n == 0) return GR_OK;

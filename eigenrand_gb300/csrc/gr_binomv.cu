@@ -316,7 +316,114 @@ __global__ void __launch_bounds__(32) k_binom_v_words(const uint64_t* w, int64_t
   }
 }
 
+// PoissonGen<int32_t> and BinomialGen<int32_t> (Discrete.h:855-905,
+// 990-1048) on a scalar engine's pre-drawn words, one chain: packets of 4 on
+// SSE uniform packets of two draws each.  Modes: BinomialGen with trials < 25
+// (one uniform packet per trial), the multiplicative Poisson loop (PoissonGen
+// mean < 12, BinomialGen mean < 1 through its PoissonGen member), and the tan
+// rejection through CompressMask (carried lanes in carry[0..3], their count in
+// carry[8], kept across chunks of one call).  res[0] = packets completed,
+// res[1] = words they consumed.
+__global__ void __launch_bounds__(32) k_int_words(const uint64_t* w, int64_t nwords, DistParams d, int32_t* out,
+                                                 int64_t npk, int64_t* res, uint32_t* carry) {
+  __shared__ uint32_t cb[8];
+  const int lane = threadIdx.x & 31;
+  BvWordsSrc src{w, nwords / 2, lane};
+  auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
+  const bool binom = d.kind == GR_BINOMIAL;
+  const int mode = (binom && d.ia < 25) ? 0 : (d.ic ? 1 : 2);
+  int fc = (int)carry[8];
+  if (lane < fc) cb[lane] = carry[lane];
+  __syncwarp();
+  // CompressMask::compress_append over lanes 0-3 (arch/AVX/PacketFilter.h:147-184)
+  auto compress = [&](uint32_t bits, bool acc, uint32_t& r) -> bool {
+    const unsigned m = mask4(acc);
+    if (m == 0xfu) {
+      r = bits;
+      return true;
+    }
+    if (lane < 4 && ((m >> lane) & 1u)) cb[fc + __popc(m & ((1u << lane) - 1))] = bits;
+    fc += __popc(m);
+    __syncwarp();
+    if (fc < 4) return false;
+    r = lane < 4 ? cb[lane] : 0u;
+    const uint32_t mv = lane < fc - 4 ? cb[4 + lane] : 0u;
+    __syncwarp();
+    if (lane < fc - 4) cb[lane] = mv;
+    fc -= 4;
+    __syncwarp();
+    return true;
+  };
+  const BvLane L{d.fh, d.fb, d.fg, d.fa, d.fc, d.fd};  // BinomialGen's tan constants
+  int64_t e = 0;
+  for (; e < npk; ++e) {
+    src.mark();
+    const int fc0 = fc;  // the carried lanes before this packet (at most 3)
+    const uint32_t cs = lane < fc ? cb[lane] : 0u;
+    int32_t r = 0;
+    if (mode == 0) {  // res = trials + sum of (p <= u ? -1 : 0) over trials uniform packets
+      r = d.ia;
+      for (int t = 0; t < d.ia; ++t) r += (d.fa <= bv_ur(src.next())) ? -1 : 0;
+    } else if (mode == 1) {
+      float val = 1.0f;
+      for (;;) {
+        val = val * bv_ur(src.next());
+        if (src.abort) break;
+        const bool c = d.fe < val;
+        if (mask4(c) == 0) break;
+        r += c ? 1 : 0;
+      }
+    } else {
+      for (;;) {
+        const uint32_t w1 = src.next();
+        const uint32_t w2 = src.next();
+        if (src.abort) break;
+        bool acc;
+        float fres;
+        if (binom) {
+          acc = bv_trial(L, w1, w2, fres);
+        } else {
+          float sn, cs2;
+          sincosf_((float)3.1415926535897932 * bv_ur(w1), sn, cs2);
+          const float yx = sn / cs2;
+          fres = truncf(d.fa * yx + d.fb);  // sqrt(2 mean) * yx + mean
+          const float p1 = (yx * yx + 1.0f) * 0.9f;
+          const float p2 = expf_((fres * d.fc - lgamma_approxf_(fres + 1.0f)) - d.fd);
+          acc = (0.0f <= fres) && (bv_ur(w2) <= p1 * p2);
+        }
+        uint32_t rb;
+        if (compress(f2u(fres), acc, rb)) {
+          r = cvtt_f32(u2f(rb));
+          break;
+        }
+      }
+    }
+    if (src.abort) {
+      __syncwarp();
+      fc = fc0;
+      if (lane < fc0) cb[lane] = cs;
+      __syncwarp();
+      break;
+    }
+    if (binom && mode != 0 && d.ib) r = d.ia - r;  // p > 1/2: trials - res (not the trials < 25 branch)
+    if (lane < 4) out[e * 4 + lane] = r;
+  }
+  __syncwarp();
+  if (lane < fc) carry[lane] = cb[lane];
+  if (lane == 0) {
+    carry[8] = (uint32_t)fc;
+    res[0] = e;
+    res[1] = 2 * (e < npk ? src.q0 : src.q);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_int_words(const uint64_t* w, int64_t nwords, const DistParams& d, int32_t* out, int64_t npk,
+                             int64_t* res, uint32_t* carry, cudaStream_t s) {
+  k_int_words<<<1, 32, 0, s>>>(w, nwords, d, out, npk, res, carry);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_binom_v(const Plan& p, const BinomVArgs& a, cudaStream_t s) {
   static bool attr[64] = {};

@@ -153,6 +153,10 @@ cudaError_t launch_binom_v(const Plan& p, const BinomVArgs& a, cudaStream_t s);
 // packets completed, res[1] = words they consumed.
 cudaError_t launch_binom_v_words(const uint64_t* w, int64_t nwords, const BinomVArgs& a, int32_t* out, int64_t npk,
                                  int64_t* res, cudaStream_t s);
+// PoissonGen / BinomialGen (int32) on a scalar engine's pre-drawn words (one
+// chain); carry: CompressMask's carried lanes [0..3] and their count [8].
+cudaError_t launch_int_words(const uint64_t* w, int64_t nwords, const DistParams& d, int32_t* out, int64_t npk,
+                             int64_t* res, uint32_t* carry, cudaStream_t s);
 
 // Batched vectorize-over-params sets (gr_vop.cu).
 struct VopArgs {

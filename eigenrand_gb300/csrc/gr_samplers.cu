@@ -2085,7 +2085,7 @@ static cudaError_t run_uniform_int(const Plan& p, const DistParams& d, int64_t m
 // lane per packet lane, decisions by ballot).
 // ===========================================================================
 namespace {
-constexpr int kNbWarps = 4;                                         // engines per CTA
+constexpr int kNbWarps = 1;  // engines per CTA (30 KB of shared memory each: 7 CTAs per SM)
 constexpr size_t kNbWarpBytes = (size_t)2 * kLanes * kN * 8 + (size_t)2 * kN * 16 + 64;  // windows, draws, carry
 }
 

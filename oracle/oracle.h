@@ -111,6 +111,7 @@ int or_gen_real_v(or_vmt* e, or_gen* g, int dist, int dtype, const void* av, con
 int or_sgen_real(or_seng* s, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n);
 int or_sgen_binomial_v(or_seng* s, const int32_t* trials, const float* p, int32_t trials0, float p0, int32_t* out,
                        size_t n);
+int or_sgen_int(or_seng* s, int kind, int32_t trials, double a, int32_t* out, size_t n);
 int or_sgen_randbits(or_seng* s, int32_t* out, size_t n);
 /* TruncGen<Base>{base, Support(lower, upper)} (Truncated.h); g: four slots */
 int or_gen_trunc(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, double lower, double upper,

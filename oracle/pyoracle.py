@@ -94,6 +94,8 @@ def lib():
         L.or_gen_binomial_v.restype = ctypes.c_int
         L.or_sgen_binomial_v.argtypes = [vp, vp, vp, ctypes.c_int32, ctypes.c_float, vp, ctypes.c_size_t]
         L.or_sgen_binomial_v.restype = ctypes.c_int
+        L.or_sgen_int.argtypes = [vp, ctypes.c_int, ctypes.c_int32, ctypes.c_double, vp, ctypes.c_size_t]
+        L.or_sgen_int.restype = ctypes.c_int
         L.or_gen_trunc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, vp, sz]
         L.or_gen_trunc.restype = ctypes.c_int
@@ -169,9 +171,13 @@ class ScalarEngine:
             raise RuntimeError(f"oracle error {rc}")
         return out
 
-    def generate(self, gen, kind, n, dtype=np.float32, a=0.0, b=0.0):
-        """Real kinds of generate() and RANDBITS, drawn through the scalar engine."""
-        if kind == "RANDBITS":
+    def generate(self, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0):
+        """Real kinds of generate(), RANDBITS, and the free functions poisson() /
+        binomial() (a fresh generator each call), drawn through the scalar engine."""
+        if kind in ("POISSON", "BINOMIAL"):
+            out = np.empty(n, dtype=np.int32)
+            rc = self.L.or_sgen_int(self.h, 0 if kind == "POISSON" else 1, int(trials), float(a), _p(out), n)
+        elif kind == "RANDBITS":
             out = np.empty(n, dtype=np.int32)
             rc = self.L.or_sgen_randbits(self.h, _p(out), n)
         else:

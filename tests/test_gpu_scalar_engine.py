@@ -123,3 +123,28 @@ def test_scalar_engine_binomial_v(er, oracle, okind, cls):
     assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), "raw after the long call")
     with pytest.raises(er.GrError):
         er.normal(u, torch.ones(8), torch.ones(8))
+
+
+INT_CASES = [("POISSON", 0.5, 0), ("POISSON", 4.0, 0), ("POISSON", 11.9, 0), ("POISSON", 12.0, 0),
+             ("POISSON", 100.0, 0), ("BINOMIAL", 0.3, 10), ("BINOMIAL", 0.8, 24), ("BINOMIAL", 0.005, 100),
+             ("BINOMIAL", 0.995, 100), ("BINOMIAL", 0.3, 100), ("BINOMIAL", 0.7, 1000), ("BINOMIAL", 0.5, 0)]
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_poisson_binomial(er, oracle, okind, cls):
+    """poisson() / binomial() (fresh PoissonGen / BinomialGen<int32_t>) with a
+    scalar engine: every branch (the trials < 25 sum, the multiplicative
+    loop, the tan rejection through CompressMask with lanes carried across
+    chunks of pre-drawn words, p > 1/2), calls of several sizes in a row, and
+    raw draws after them."""
+    u = getattr(er, cls)(2024)
+    o = oracle.ScalarEngine(okind, 2024)
+    for kind, a, trials in INT_CASES:
+        for rows, cols in ((4, 3), (256, 512)):
+            if kind == "POISSON":
+                got = er.poisson(rows, cols, u, a)
+            else:
+                got = er.binomial(rows, cols, u, trials, a)
+            ref = o.generate(None, kind, rows * cols, np.int32, a, trials=trials)
+            assert_bits_equal(mem(got), ref, f"{cls} {kind} {a} {trials} {rows}x{cols}")
+        assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after {kind} {a}")

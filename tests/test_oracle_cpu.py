@@ -408,3 +408,19 @@ def test_oracle_binomial_per_element_scalar_engine(oracle):
         np.testing.assert_array_equal(z, 0)
         s2.raw(2 * 10)
         np.testing.assert_array_equal(s1.raw(4), s2.raw(4))
+
+
+def test_oracle_poisson_binomial_scalar_engine(oracle):
+    """PoissonGen / BinomialGen<int32_t> with scalar engines as the Urng:
+    sample means of every branch, and the trials < 25 sum's consumption
+    (trials uniform packets of two draws per output packet)."""
+    for kind in ("mt19937_64", "p8"):
+        s = oracle.ScalarEngine(kind, 3)
+        for k, a, t, m in (("POISSON", 4.0, 0, 4.0), ("POISSON", 50.0, 0, 50.0), ("BINOMIAL", 0.3, 10, 3.0),
+                           ("BINOMIAL", 0.004, 100, 0.4), ("BINOMIAL", 0.7, 200, 140.0)):
+            x = s.generate(None, k, 4 * 8192, np.int32, a, trials=t).astype(np.float64)
+            assert abs(x.mean() - m) < 0.05 * m + 0.02, (kind, k, a, t, x.mean())
+        s1, s2 = oracle.ScalarEngine(kind, 9), oracle.ScalarEngine(kind, 9)
+        s1.generate(None, "BINOMIAL", 12, np.int32, 0.4, trials=5)
+        s2.raw(3 * 5 * 2)
+        np.testing.assert_array_equal(s1.raw(4), s2.raw(4))
