@@ -1654,6 +1654,129 @@ gr_status sengine_binom_v(gr_sengine* se, const gr_dist_desc& d, const void* dev
       s);
 }
 
+// GammaGen's rejection branches (GS for alpha < 1, the tan proposal) on a
+// scalar engine, a fresh generator (the free functions): chunks of trials are
+// drawn into HBM, every trial's candidate lanes evaluated at once (rejected
+// lanes NaN), and TruncGen's CompressMask filter, with an unbounded support,
+// emits the outputs in the reference's order.  A chunk that runs out leaves
+// the engine exactly past its words; the chunk that completes the call puts
+// the engine back and advances it past the trial that emitted the last
+// output.
+gr_status sengine_reject(gr_sengine* se, const DistParams& dp, int rk, void* out, size_t n, cudaStream_t s) {
+  const int dt = dp.dtype;
+  const int64_t P = dt == GR_F32 ? 8 : 4;
+  const size_t lb = dt == GR_F32 ? 4 : 8;
+  if (n % (size_t)P)
+    return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(P) + " (the reference packet width)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  gr_engine* e = se->eng;
+  // words per trial: packets per trial (GS 3, tan 2) of 3 (float) or 4 (double) draws
+  const int64_t wpt = (rk == 0 ? 3 : 2) * (dt == GR_F32 ? 3 : 4);
+  const int64_t need = (int64_t)(n / (size_t)P);
+  const int64_t mcap = kTruncChunkMax - 1;
+  const double q = reject_yield(rk, dp);
+  char* buf = nullptr;
+  int64_t have_m = 0;
+  auto layout = [&](int64_t m, size_t off[8]) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t r = o;
+      o += (bytes + 255) / 256 * 256;
+      return r;
+    };
+    off[0] = take((size_t)m * P * lb);                                  // candidates
+    off[1] = take((size_t)(m + 1) * P * lb);                            // FIFO
+    off[2] = take(sizeof(int64_t) * 2 * (size_t)((m + 255) / 256));     // CTA sums
+    off[3] = take(sizeof(int64_t) * (size_t)(m + 1));                   // group slots
+    off[4] = take(sizeof(int64_t) * 8);                                 // results
+    off[5] = take(sizeof(EngState) * (size_t)e->K + sizeof(uint64_t) * 8);  // saved engine
+    off[6] = take(sizeof(GenSlot));                                     // carried lanes
+    off[7] = take(sizeof(uint64_t) * (size_t)m * wpt);                  // words
+    return o;
+  };
+  auto bail = [&](gr_status r) {
+    if (buf) cudaFreeAsync(buf, s);
+    return r;
+  };
+  size_t off[8];
+  int64_t done = 0, drawn = 0;
+  int64_t res[6];
+  bool carry_clear = false;
+  while (done < need) {
+    const int64_t rem = need - done;
+    // trials for rem output packets: q P accepted lanes per trial, plus spread
+    const double E = (double)rem / q, sd = std::sqrt((double)rem * P * std::max(1.0 - q, 0.0)) / (q * P);
+    int64_t M = (int64_t)std::ceil(E + 4 * sd) + 16;
+    M = std::max<int64_t>(1, std::min(M, mcap));
+    drawn += M;
+    if (drawn > ((int64_t)1 << 40)) return bail(fail(GR_ERR_REJECT_LIMIT, "rejection: almost no trial accepts"));
+    if (M > have_m) {
+      // grow the scratch; the carried lanes move to the new buffer
+      char* nb = nullptr;
+      const int64_t m = std::min(mcap, std::max(M, have_m * 2));
+      size_t noff[8];
+      cudaError_t err = cudaMallocAsync(&nb, layout(m, noff), s);
+      if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine rejection scratch"));
+      if (buf && carry_clear)
+        err = cudaMemcpyAsync(nb + noff[6], buf + off[6], sizeof(GenSlot), cudaMemcpyDeviceToDevice, s);
+      else
+        err = cudaMemsetAsync(nb + noff[6], 0, sizeof(GenSlot), s);
+      if (buf) cudaFreeAsync(buf, s);
+      buf = nb;
+      carry_clear = true;
+      if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine rejection scratch"));
+      have_m = m;
+    }
+    layout(have_m, off);
+    void* cand = buf + off[0];
+    int64_t* dres = reinterpret_cast<int64_t*>(buf + off[4]);
+    EngState* saved = reinterpret_cast<EngState*>(buf + off[5]);
+    uint64_t* pb = reinterpret_cast<uint64_t*>(buf + off[5] + sizeof(EngState) * (size_t)e->K);
+    uint64_t* w = reinterpret_cast<uint64_t*>(buf + off[7]);
+    cudaError_t err = cudaMemcpyAsync(saved, e->st, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
+    if (err == cudaSuccess && se->pbuf)
+      err = cudaMemcpyAsync(pb, se->pbuf, sizeof(uint64_t) * 8, cudaMemcpyDeviceToDevice, s);
+    if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine state copy"));
+    const int cnt0 = se->cnt;
+    gr_status st = sengine_words(se, w, M * wpt, s);
+    if (st != GR_OK) return bail(st);
+    err = launch_sx_cand(rk, dt, w, M, dp, cand, s);
+    TruncFilterArgs a{};
+    a.cand = cand;
+    a.M = M;
+    a.lower = -INFINITY;
+    a.upper = INFINITY;
+    a.carry = reinterpret_cast<GenSlot*>(buf + off[6]);
+    a.out = static_cast<char*>(out) + (size_t)done * P * lb;
+    a.cap = rem;
+    a.queue = buf + off[1];
+    a.blk = reinterpret_cast<int64_t*>(buf + off[2]);
+    a.grp = reinterpret_cast<int64_t*>(buf + off[3]);
+    a.res = dres;
+    if (err == cudaSuccess) err = launch_trunc_filter(dt, a, s);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(res, dres, sizeof res, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine rejection"));
+    if (res[1] < 0) {
+      done += res[0];
+      continue;
+    }
+    if (res[1] + 1 < M) {
+      // back to the chunk start, then just past trial res[1]
+      err = cudaMemcpyAsync(e->st, saved, sizeof(EngState) * (size_t)e->K, cudaMemcpyDeviceToDevice, s);
+      if (err == cudaSuccess && se->pbuf)
+        err = cudaMemcpyAsync(se->pbuf, pb, sizeof(uint64_t) * 8, cudaMemcpyDeviceToDevice, s);
+      if (err != cudaSuccess) return bail(cuda_fail(err, "scalar engine state copy"));
+      se->cnt = cnt0;
+      st = sengine_words(se, w, (res[1] + 1) * wpt, s);
+      if (st != GR_OK) return bail(st);
+    }
+    done = need;
+  }
+  return bail(GR_OK);
+}
+
 // PoissonGen / BinomialGen (int32) on a scalar engine: a fresh generator, so
 // CompressMask's carried lanes start empty and are dropped after the call
 gr_status sengine_int(gr_sengine* se, const DistParams& dp, void* out, size_t n, cudaStream_t s) {
@@ -1732,11 +1855,13 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
   if (st != GR_OK) return st;
   if (dp.dtype == GR_I32 && (dp.kind == GR_POISSON || dp.kind == GR_BINOMIAL))
     return sengine_int(se, dp, dev_out, n, s);
+  if (dp.kind == GR_GAMMA && reject_code(dp) >= 0 && family_of(dp) == Family::Reject)
+    return sengine_reject(se, dp, reject_code(dp), dev_out, n, s);
   const int wpp = scalar_words_per_packet(dp.kind, dp.dtype);
   if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
     return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
-                                    "randBits), poisson and binomial");
+                                    "randBits), gamma, chiSquared, poisson and binomial");
   const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
   if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
   if (n == 0) return GR_OK;

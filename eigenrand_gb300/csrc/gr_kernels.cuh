@@ -155,6 +155,10 @@ cudaError_t launch_binom_v_words(const uint64_t* w, int64_t nwords, const BinomV
                                  int64_t* res, cudaStream_t s);
 // PoissonGen / BinomialGen (int32) on a scalar engine's pre-drawn words (one
 // chain); carry: CompressMask's carried lanes [0..3] and their count [8].
+// GammaGen's rejection trials (rk 0 GS, 1 tan; f32 / f64) on a scalar
+// engine's pre-drawn words: M trials' candidate lanes, rejected lanes NaN.
+cudaError_t launch_sx_cand(int rk, int dtype, const uint64_t* w, int64_t M, const DistParams& d, void* cand,
+                           cudaStream_t s);
 cudaError_t launch_int_words(const uint64_t* w, int64_t nwords, const DistParams& d, int32_t* out, int64_t npk,
                              int64_t* res, uint32_t* carry, cudaStream_t s);
 

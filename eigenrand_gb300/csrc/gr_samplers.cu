@@ -428,6 +428,57 @@ __device__ __forceinline__ bool rej_trial(const DistParams& d, int64_t t, int j,
         return acc;
 }
 
+// GammaGen's rejection trials drawn with a scalar engine (std::mt19937_64,
+// P8_mt19937_64) as the Urng: trial t's candidate lanes from pre-drawn 64-bit
+// words, a rejected lane written as NaN (accepted gamma candidates are never
+// NaN), for TruncGen's CompressMask filter with an unbounded support.  A float
+// uniform packet is RawbitsMaker<Packet8i, Rng, uint64_t, scalar_fullbit>::
+// rawbits_34 of three draws (arch/AVX/RandUtils.h:59-144: lanes c.lo, c.hi,
+// b.lo, top bytes, b.hi, a.lo, a.hi, top bytes, a the first draw); a double
+// packet is rawbits, four draws in order.
+template <int RK, int DT>
+__global__ void __launch_bounds__(256) k_sx_cand(const uint64_t* w, int64_t M, DistParams d, void* cand) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  const int64_t g = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (g >= M * P) return;
+  const int64_t t = g / P;
+  const int j = (int)(g % P);
+  auto word = [&](int64_t wi) -> uint32_t {
+    const uint64_t* q = w + 3 * (wi >> 3);
+    const uint32_t v[6] = {(uint32_t)q[2], (uint32_t)(q[2] >> 32), (uint32_t)q[1], (uint32_t)(q[1] >> 32),
+                           (uint32_t)q[0], (uint32_t)(q[0] >> 32)};
+    switch (wi & 7) {
+      case 0: return v[0];
+      case 1: return v[1];
+      case 2: return v[2];
+      case 3: return (v[0] >> 24) | ((v[1] >> 24) << 8) | ((v[2] >> 24) << 16) | ((v[2] >> 24) << 24);
+      case 4: return v[3];
+      case 5: return v[4];
+      case 6: return v[5];
+      default: return (v[3] >> 24) | ((v[4] >> 24) << 8) | ((v[5] >> 24) << 16) | ((v[5] >> 24) << 24);
+    }
+  };
+  auto rval = [&](int64_t r) -> uint64_t { return w[r]; };
+  uint64_t cb;
+  const bool acc = rej_trial<RK, DT>(d, t, j, word, rval, cb);
+  if (DT == SD_F32)
+    static_cast<uint32_t*>(cand)[g] = acc ? (uint32_t)cb : 0x7fc00000u;
+  else
+    static_cast<uint64_t*>(cand)[g] = acc ? cb : 0x7ff8000000000000ull;
+}
+
+cudaError_t launch_sx_cand(int rk, int dtype, const uint64_t* w, int64_t M, const DistParams& d, void* cand,
+                           cudaStream_t s) {
+  const int P = dtype == GR_F32 ? 8 : 4;
+  const unsigned blocks = (unsigned)((M * P + 255) / 256);
+  if (dtype == GR_F32 && rk == RK_GAMMA_GS) k_sx_cand<RK_GAMMA_GS, SD_F32><<<blocks, 256, 0, s>>>(w, M, d, cand);
+  else if (dtype == GR_F32 && rk == RK_GAMMA_TAN) k_sx_cand<RK_GAMMA_TAN, SD_F32><<<blocks, 256, 0, s>>>(w, M, d, cand);
+  else if (dtype == GR_F64 && rk == RK_GAMMA_GS) k_sx_cand<RK_GAMMA_GS, SD_F64><<<blocks, 256, 0, s>>>(w, M, d, cand);
+  else if (dtype == GR_F64 && rk == RK_GAMMA_TAN) k_sx_cand<RK_GAMMA_TAN, SD_F64><<<blocks, 256, 0, s>>>(w, M, d, cand);
+  else return cudaErrorNotSupported;
+  return cudaGetLastError();
+}
+
 template <int RK, int DT>  // DT: SD_F32 (P=8), SD_F64 (P=4), SD_I32H (P=4, float internals)
 __global__ void __maxnreg__(64) k_reject(Plan p, DistParams d, int64_t max_blocks) {
   constexpr int P = DT == SD_F32 ? 8 : 4;

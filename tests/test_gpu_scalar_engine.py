@@ -89,7 +89,7 @@ def test_scalar_engine_randbits_and_mirror(er, oracle, okind, cls):
     x = mem(er.ExponentialGen(2.0, dtype=torch.float64).generate(32, 32, u))
     assert_bits_equal(x, o.generate(oracle.Gen(), "EXPONENTIAL", 1024, np.float64, 2.0), "object mirror")
     with pytest.raises(er.GrError):
-        er.gamma(8, 1, u, 0.5, 1.0)
+        er.gamma(8, 1, u, 3.0, 1.0)  # integral alpha: not built for scalar engines
     with pytest.raises(er.GrError):
         er.NormalGen().generate(8, 1, u)
 
@@ -148,3 +148,39 @@ def test_scalar_engine_poisson_binomial(er, oracle, okind, cls):
             ref = o.generate(None, kind, rows * cols, np.int32, a, trials=trials)
             assert_bits_equal(mem(got), ref, f"{cls} {kind} {a} {trials} {rows}x{cols}")
         assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after {kind} {a}")
+
+
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_gamma_rejection(er, oracle, okind, cls, tdt):
+    """gamma() with a scalar engine on its rejection branches (GS for
+    alpha < 1, the tan proposal otherwise; a fresh GammaGen per call):
+    candidates of a chunk of trials evaluated at once, CompressMask order
+    through the filter, the engine left just past the trial that emitted the
+    last output; chiSquared on the same path."""
+    npt = np.float32 if tdt == torch.float32 else np.float64
+    u = getattr(er, cls)(31)
+    o = oracle.ScalarEngine(okind, 31)
+    for alpha, beta in ((0.2, 1.0), (0.5, 2.0), (0.93, 1.0), (1.5, 1.0), (2.5, 0.5), (7.3, 1.0)):
+        for rows, cols in ((8, 3), (384, 512)):
+            got = er.gamma(rows, cols, u, alpha, beta, dtype=tdt)
+            ref = o.generate(oracle.Gen(), "GAMMA", rows * cols, npt, alpha, beta)
+            assert_bits_equal(mem(got), ref, f"{cls} gamma({alpha}, {beta}) {tdt} {rows}x{cols}")
+        assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after gamma({alpha})")
+    got = er.chiSquared(64, 64, u, 3.0, dtype=tdt)
+    ref = o.generate(oracle.Gen(), "GAMMA", 64 * 64, npt, 1.5, 2.0)
+    assert_bits_equal(mem(got), ref, f"{cls} chiSquared(3)")
+    with pytest.raises(er.GrError):
+        er.gamma(8, 8, u, 2.0, 1.0, dtype=tdt)  # integral alpha: the product-of-uniforms form, not built here
+
+
+def test_scalar_engine_gamma_multichunk(er, oracle):
+    """A call needing more trials than one chunk holds: the first chunk runs
+    out with lanes carried into the next."""
+    u = er.mt19937_64(5)
+    o = oracle.ScalarEngine("mt19937_64", 5)
+    n = 8 * 4_700_000
+    got = er.gamma(n, 1, u, 0.5, 1.0)
+    ref = o.generate(oracle.Gen(), "GAMMA", n, np.float32, 0.5, 1.0)
+    assert_bits_equal(mem(got), ref, "gamma(0.5) multi-chunk")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), "raw after")
