@@ -1857,11 +1857,29 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
     return sengine_int(se, dp, dev_out, n, s);
   if (dp.kind == GR_GAMMA && reject_code(dp) >= 0 && family_of(dp) == Family::Reject)
     return sengine_reject(se, dp, reject_code(dp), dev_out, n, s);
+  if (dp.dtype != GR_I32 && family_of(dp) == Family::Staged && (dp.kind == GR_GAMMA || dp.kind == GR_STUDENT_T)) {
+    // a fixed run of U uniform packets per output packet: all words at once
+    const int U = dp.kind == GR_GAMMA ? dp.ib : 2;
+    const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
+    if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
+    if (n == 0) return GR_OK;
+    if (!dev_out) return fail(GR_ERR_INVALID, "output is NULL");
+    const int64_t npk = (int64_t)n / P, W = npk * U * (dp.dtype == GR_F32 ? 3 : 4);
+    uint64_t* w = nullptr;
+    GR_CUDA(cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s));
+    st = sengine_words(se, w, W, s);
+    if (st == GR_OK) {
+      const cudaError_t err = launch_sx_staged(w, dev_out, npk, dp, U, s);
+      if (err != cudaSuccess) st = cuda_fail(err, "scalar-engine sampling kernel");
+    }
+    cudaFreeAsync(w, s);
+    return st;
+  }
   const int wpp = scalar_words_per_packet(dp.kind, dp.dtype);
   if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
     return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
-                                    "randBits), gamma, chiSquared, poisson and binomial");
+                                    "randBits), gamma, chiSquared, studentT, poisson and binomial");
   const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
   if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
   if (n == 0) return GR_OK;

@@ -159,6 +159,10 @@ cudaError_t launch_binom_v_words(const uint64_t* w, int64_t nwords, const BinomV
 // engine's pre-drawn words: M trials' candidate lanes, rejected lanes NaN.
 cudaError_t launch_sx_cand(int rk, int dtype, const uint64_t* w, int64_t M, const DistParams& d, void* cand,
                            cudaStream_t s);
+// GammaGen with integral alpha < 20 (U = alpha uniform packets per output
+// packet) and StudentTGen (U = 2) on a scalar engine's pre-drawn words.
+cudaError_t launch_sx_staged(const uint64_t* w, void* out, int64_t npk, const DistParams& d, int U,
+                             cudaStream_t s);
 cudaError_t launch_int_words(const uint64_t* w, int64_t nwords, const DistParams& d, int32_t* out, int64_t npk,
                              int64_t* res, uint32_t* carry, cudaStream_t s);
 

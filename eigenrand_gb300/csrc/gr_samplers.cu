@@ -190,6 +190,80 @@ __global__ void __launch_bounds__(160)
   }
 }
 
+// The staged kinds drawn with a scalar engine as the Urng: output packet k
+// reads U uniform packets from pre-drawn 64-bit words, float packets as
+// rawbits_34 of three draws (c.lo, c.hi, b.lo, top bytes, b.hi, a.lo, a.hi,
+// top bytes; a the first draw), double packets as four draws in order; the
+// same per-lane arithmetic as k_staged.  One thread per output lane.
+template <int KIND, int DT>
+__global__ void __launch_bounds__(256) k_sx_staged(const uint64_t* w, void* out, int64_t npk, DistParams d, int U) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  const int64_t g = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (g >= npk * P) return;
+  const int64_t k = g / P;
+  const int j = (int)(g % P);
+  if (DT == SD_F32) {
+    // lane j of uniform packet t of output packet k
+    auto word = [&](int t) -> uint32_t {
+      const uint64_t* q = w + 3 * (k * U + t);
+      const uint32_t v[6] = {(uint32_t)q[2], (uint32_t)(q[2] >> 32), (uint32_t)q[1], (uint32_t)(q[1] >> 32),
+                             (uint32_t)q[0], (uint32_t)(q[0] >> 32)};
+      switch (j) {
+        case 0: return v[0];
+        case 1: return v[1];
+        case 2: return v[2];
+        case 3: return (v[0] >> 24) | ((v[1] >> 24) << 8) | ((v[2] >> 24) << 16) | ((v[2] >> 24) << 24);
+        case 4: return v[3];
+        case 5: return v[4];
+        case 6: return v[5];
+        default: return (v[3] >> 24) | ((v[4] >> 24) << 8) | ((v[5] >> 24) << 16) | ((v[5] >> 24) << 24);
+      }
+    };
+    if (KIND == GR_GAMMA) {
+      float y = ur_f(word(0)) + 1.1920928955078125e-07f / 8;
+      for (int t = 1; t < U; ++t) y = y * (ur_f(word(t)) + 1.1920928955078125e-07f / 8);
+      static_cast<float*>(out)[g] = -(d.fb * logf_(y));
+    } else {  // GR_STUDENT_T
+      const float u1 = 1.0f - ur_f(word(0));
+      const float u2 = ur_f(word(1));
+      const float radius = sqrtf(d.fa * (expf_(logf_(u1) * d.fc) - 1.0f));
+      float sn, cs;
+      sincosf_((float)(2 * 3.1415926535897932) * u2, sn, cs);
+      static_cast<float*>(out)[g] = radius * sn;
+    }
+  } else {
+    const uint64_t* q = w + 4 * k * U + j;
+    if (KIND == GR_GAMMA) {
+      double y = ur_d(q[0]) + 2.220446049250313e-16 / 8;
+      for (int t = 1; t < U; ++t) y = y * (ur_d(q[4 * t]) + 2.220446049250313e-16 / 8);
+      const double l = log_(y);
+      static_cast<double*>(out)[g] = (d.flags & kParamUnitScale) ? -l : -(d.db * l);
+    } else {  // GR_STUDENT_T
+      const double u1 = one_minus_ur_d(q[0]);
+      const double u2 = ur_d(q[4]);
+      const double radius = sqrt(d.da * (exp_(log_(u1) * d.dc) - 1.0));
+      double sn, cs;
+      sincos_((2 * 3.1415926535897932) * u2, sn, cs);
+      static_cast<double*>(out)[g] = radius * sn;
+    }
+  }
+}
+
+cudaError_t launch_sx_staged(const uint64_t* w, void* out, int64_t npk, const DistParams& d, int U,
+                             cudaStream_t s) {
+  const int P = d.dtype == GR_F32 ? 8 : 4;
+  const unsigned blocks = (unsigned)((npk * P + 255) / 256);
+  const bool gam = d.kind == GR_GAMMA;
+  if (d.dtype == GR_F32) {
+    if (gam) k_sx_staged<GR_GAMMA, SD_F32><<<blocks, 256, 0, s>>>(w, out, npk, d, U);
+    else k_sx_staged<GR_STUDENT_T, SD_F32><<<blocks, 256, 0, s>>>(w, out, npk, d, U);
+  } else {
+    if (gam) k_sx_staged<GR_GAMMA, SD_F64><<<blocks, 256, 0, s>>>(w, out, npk, d, U);
+    else k_sx_staged<GR_STUDENT_T, SD_F64><<<blocks, 256, 0, s>>>(w, out, npk, d, U);
+  }
+  return cudaGetLastError();
+}
+
 template <int KIND, int DT>
 static cudaError_t run_staged(const Plan& p, const DistParams& d, const CallSnap* snap, int U, int64_t Us,
                               int delta, cudaStream_t s) {

@@ -89,7 +89,7 @@ def test_scalar_engine_randbits_and_mirror(er, oracle, okind, cls):
     x = mem(er.ExponentialGen(2.0, dtype=torch.float64).generate(32, 32, u))
     assert_bits_equal(x, o.generate(oracle.Gen(), "EXPONENTIAL", 1024, np.float64, 2.0), "object mirror")
     with pytest.raises(er.GrError):
-        er.gamma(8, 1, u, 3.0, 1.0)  # integral alpha: not built for scalar engines
+        er.beta(8, 1, u, 0.5, 2.0)  # not built for scalar engines
     with pytest.raises(er.GrError):
         er.NormalGen().generate(8, 1, u)
 
@@ -170,8 +170,17 @@ def test_scalar_engine_gamma_rejection(er, oracle, okind, cls, tdt):
     got = er.chiSquared(64, 64, u, 3.0, dtype=tdt)
     ref = o.generate(oracle.Gen(), "GAMMA", 64 * 64, npt, 1.5, 2.0)
     assert_bits_equal(mem(got), ref, f"{cls} chiSquared(3)")
-    with pytest.raises(er.GrError):
-        er.gamma(8, 8, u, 2.0, 1.0, dtype=tdt)  # integral alpha: the product-of-uniforms form, not built here
+    # integral alpha < 20: the product of alpha uniforms, and studentT: two
+    # uniform packets per output packet
+    for alpha, beta in ((2.0, 1.0), (3.0, 0.5), (19.0, 1.0)):
+        got = er.gamma(64, 40, u, alpha, beta, dtype=tdt)
+        ref = o.generate(oracle.Gen(), "GAMMA", 64 * 40, npt, alpha, beta)
+        assert_bits_equal(mem(got), ref, f"{cls} gamma({alpha}, {beta}) {tdt}")
+    for nu in (1.0, 4.5):
+        got = er.studentT(96, 32, u, nu, dtype=tdt)
+        ref = o.generate(oracle.Gen(), "STUDENT_T", 96 * 32, npt, nu)
+        assert_bits_equal(mem(got), ref, f"{cls} studentT({nu}) {tdt}")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after the staged kinds")
 
 
 def test_scalar_engine_gamma_multichunk(er, oracle):
