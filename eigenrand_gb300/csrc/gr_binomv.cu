@@ -316,9 +316,9 @@ __global__ void __launch_bounds__(32) k_binom_v_words(const uint64_t* w, int64_t
   }
 }
 
-// PoissonGen<int32_t> and BinomialGen<int32_t> (Discrete.h:855-905,
-// 990-1048) on a scalar engine's pre-drawn words, one chain: packets of 4 on
-// SSE uniform packets of two draws each.  Modes: BinomialGen with trials < 25
+// PoissonGen<int32_t>, BinomialGen<int32_t> and UniformIntGen<int32_t>
+// (Discrete.h:855-905, 990-1048, 287-333) on a scalar engine's pre-drawn
+// words, one chain: packets of 4 on SSE packets of two draws each.  Modes: BinomialGen with trials < 25
 // (one uniform packet per trial), the multiplicative Poisson loop (PoissonGen
 // mean < 12, BinomialGen mean < 1 through its PoissonGen member), and the tan
 // rejection through CompressMask (carried lanes in carry[0..3], their count in
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(32) k_int_words(const uint64_t* w, int64_t nwo
   BvWordsSrc src{w, nwords / 2, lane};
   auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
   const bool binom = d.kind == GR_BINOMIAL;
-  const int mode = (binom && d.ia < 25) ? 0 : (d.ic ? 1 : 2);
+  const int mode = d.kind == GR_UNIFORM_INT ? 3 : ((binom && d.ia < 25) ? 0 : (d.ic ? 1 : 2));
   int fc = (int)carry[8];
   if (lane < fc) cb[lane] = carry[lane];
   __syncwarp();
@@ -372,6 +372,36 @@ __global__ void __launch_bounds__(32) k_int_words(const uint64_t* w, int64_t nwo
         const bool c = d.fe < val;
         if (mask4(c) == 0) break;
         r += c ? 1 : 0;
+      }
+    } else if (mode == 3) {
+      // UniformIntGen (Discrete.h:287-333): d.ia = pmin, d.ib = 0 constant /
+      // 1 masked bits / 2 rejection on slices of bitsize (d.ncdf) bits with
+      // plen (d.ic) compared as signed int32
+      if (d.ib == 0) {
+        r = d.ia;
+      } else {
+        uint32_t rx = src.next();
+        if (d.ib == 1) {
+          r = (int32_t)((rx & d.bitmask) + (uint32_t)d.ia);
+        } else {
+          int bitcnt = d.ncdf;
+          for (;;) {
+            if (src.abort) break;
+            const uint32_t cands = rx & d.bitmask;
+            uint32_t rb;
+            if (compress(cands, (int32_t)cands < d.ic, rb)) {
+              r = (int32_t)(rb + (uint32_t)d.ia);
+              break;
+            }
+            if (bitcnt + d.ncdf < 32) {
+              rx >>= d.ncdf;
+              bitcnt += d.ncdf;
+            } else {
+              rx = src.next();
+              bitcnt = d.ncdf;
+            }
+          }
+        }
       }
     } else {
       for (;;) {

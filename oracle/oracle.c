@@ -1941,9 +1941,9 @@ int or_sgen_binomial_v(or_seng* s, const int32_t* trials, const float* p, int32_
   return rc;
 }
 
-/* PoissonGen (kind 0) / BinomialGen (kind 1) <int32_t> with a scalar engine
- * as the Urng, a fresh generator (the free functions poisson() / binomial()):
- * every uniform packet takes two draws (draw_half). */
+/* PoissonGen (kind 0) / BinomialGen (kind 1) / UniformIntGen (kind 2, min a,
+ * max trials) <int32_t> with a scalar engine as the Urng, a fresh generator
+ * (the free functions): every packet takes two draws (draw_half). */
 int or_sgen_int(or_seng* s, int kind, int32_t trials, double a, int32_t* out, size_t n) {
   or_vmt dummy;
   memset(&dummy, 0, sizeof dummy);
@@ -1952,7 +1952,9 @@ int or_sgen_int(or_seng* s, int kind, int32_t trials, double a, int32_t* out, si
   memset(&g, 0, sizeof g);
   or_seng* prev = g_src;
   g_src = s;
-  const int rc = kind == 0 ? or_gen_poisson(&dummy, &g, a, out, n) : or_gen_binomial(&dummy, &g, trials, a, out, n);
+  const int rc = kind == 0   ? or_gen_poisson(&dummy, &g, a, out, n)
+                 : kind == 1 ? or_gen_binomial(&dummy, &g, trials, a, out, n)
+                             : or_gen_uniform_int(&dummy, &g, (int32_t)a, trials, out, n);
   g_src = prev;
   return rc;
 }

@@ -174,9 +174,11 @@ class ScalarEngine:
     def generate(self, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0):
         """Real kinds of generate(), RANDBITS, and the free functions poisson() /
         binomial() (a fresh generator each call), drawn through the scalar engine."""
-        if kind in ("POISSON", "BINOMIAL"):
+        if kind in ("POISSON", "BINOMIAL", "UNIFORM_INT"):
             out = np.empty(n, dtype=np.int32)
-            rc = self.L.or_sgen_int(self.h, 0 if kind == "POISSON" else 1, int(trials), float(a), _p(out), n)
+            k = {"POISSON": 0, "BINOMIAL": 1, "UNIFORM_INT": 2}[kind]
+            t = int(b) if kind == "UNIFORM_INT" else int(trials)  # UNIFORM_INT: a = min, b = max
+            rc = self.L.or_sgen_int(self.h, k, t, float(a), _p(out), n)
         elif kind == "RANDBITS":
             out = np.empty(n, dtype=np.int32)
             rc = self.L.or_sgen_randbits(self.h, _p(out), n)

@@ -193,3 +193,18 @@ def test_scalar_engine_gamma_multichunk(er, oracle):
     ref = o.generate(oracle.Gen(), "GAMMA", n, np.float32, 0.5, 1.0)
     assert_bits_equal(mem(got), ref, "gamma(0.5) multi-chunk")
     assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), "raw after")
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_uniform_int(er, oracle, okind, cls):
+    """uniformInt() (a fresh UniformIntGen<int32_t>) with a scalar engine:
+    constant, masked and rejection ranges (bit slices shifted out of one
+    draw, or a new draw per slice), and raw draws after the calls."""
+    u = getattr(er, cls)(77)
+    o = oracle.ScalarEngine(okind, 77)
+    for lo, hi in ((0, 9), (-5, 10), (3, 3), (0, 1000000), (0, 100), (-1000, 1000)):
+        for rows, cols in ((4, 5), (300, 200)):
+            got = er.uniformInt(rows, cols, u, lo, hi)
+            ref = o.generate(None, "UNIFORM_INT", rows * cols, np.int32, lo, hi)
+            assert_bits_equal(mem(got), ref, f"{cls} uniformInt({lo}, {hi}) {rows}x{cols}")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after")
