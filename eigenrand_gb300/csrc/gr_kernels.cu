@@ -976,7 +976,8 @@ static cudaError_t run_sx(const uint64_t* w, void* out, int64_t npk, const DistP
 }
 
 int scalar_words_per_packet(int kind, int dtype) {
-  if (dtype == GR_I32) return kind == GR_RANDBITS ? 2 : 0;
+  // int32 kinds on one SSE packet of two draws (rawbits / rawbits_34)
+  if (dtype == GR_I32) return (kind == GR_RANDBITS || kind == GR_BERNOULLI || kind == GR_GEOMETRIC) ? 2 : 0;
   const bool bal = kind == GR_BALANCED || kind == GR_BALANCED2;
   switch (kind) {
     case GR_UNIFORM_REAL:
@@ -1006,6 +1007,8 @@ int scalar_words_per_packet(int kind, int dtype) {
 cudaError_t launch_scalar_xform(const uint64_t* w, void* out, int64_t npk, const DistParams& d, cudaStream_t s) {
   if (d.dtype == GR_I32) {
     if (d.kind == GR_RANDBITS) return run_sx<S_I32, GR_RANDBITS>(w, out, npk, d, s);
+    if (d.kind == GR_BERNOULLI) return run_sx<S_I32, GR_BERNOULLI>(w, out, npk, d, s);
+    if (d.kind == GR_GEOMETRIC) return run_sx<S_I32, GR_GEOMETRIC>(w, out, npk, d, s);
     return cudaErrorNotSupported;
   }
   if (d.dtype == GR_F32) {

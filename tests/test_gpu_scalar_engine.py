@@ -208,3 +208,17 @@ def test_scalar_engine_uniform_int(er, oracle, okind, cls):
             ref = o.generate(None, "UNIFORM_INT", rows * cols, np.int32, lo, hi)
             assert_bits_equal(mem(got), ref, f"{cls} uniformInt({lo}, {hi}) {rows}x{cols}")
     assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after")
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_bernoulli_geometric_int(er, oracle, okind, cls):
+    """BernoulliGen<int32_t> and GeometricGen<int32_t> with a scalar engine:
+    one SSE packet of two draws per output packet."""
+    u = getattr(er, cls)(13)
+    o = oracle.ScalarEngine(okind, 13)
+    for p in (0.3, 0.9):
+        got = er.bernoulli(200, 40, u, p, dtype=torch.int32)
+        assert_bits_equal(mem(got), o.generate(None, "BERNOULLI", 8000, np.int32, p), f"{cls} bernoulli({p})")
+        got = er.geometric(200, 40, u, p)
+        assert_bits_equal(mem(got), o.generate(None, "GEOMETRIC", 8000, np.int32, p), f"{cls} geometric({p})")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after")
