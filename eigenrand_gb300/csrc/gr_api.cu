@@ -1850,8 +1850,53 @@ gr_status gr_sengine_sample_v2(gr_sengine* se, const gr_dist_desc* desc, const v
 gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream) {
   if (!se || !desc) return fail(GR_ERR_INVALID, "NULL argument");
   cudaStream_t s = (cudaStream_t)stream;
+  gr_status st = GR_OK;
+  if (desc->kind == GR_DISCRETE) {
+    // DiscreteGen<int32_t> (Discrete.h:443-480): one Packet8i of four draws
+    // gives two output packets; an odd last packet still draws all four, its
+    // upper half cached in the call's generator and dropped with it
+    if (n % 4) return fail(GR_ERR_INVALID, "size must be a multiple of 4 (the reference packet width for this type)");
+    if (n == 0) return GR_OK;
+    if (!dev_out) return fail(GR_ERR_INVALID, "output is NULL");
+    if (!desc->weights || desc->nweights <= 0) return fail(GR_ERR_INVALID, "discrete needs weights");
+    std::vector<double> wts(desc->weights, desc->weights + desc->nweights);
+    std::vector<int32_t> prob, alias;
+    int ncdf = 0;
+    uint32_t mask = 0;
+    st = build_discrete(wts, prob, alias, ncdf, mask);
+    if (st != GR_OK) return st;
+    const size_t np = prob.size();
+    std::vector<int32_t> both(prob);
+    both.insert(both.end(), alias.begin(), alias.end());
+    const int64_t npk = (int64_t)n / 4, W = 4 * ((npk + 1) / 2);
+    int32_t* table = nullptr;
+    uint64_t* w = nullptr;
+    GR_CUDA(cudaMallocAsync(&table, sizeof(int32_t) * (both.size() + 1), s));
+    cudaError_t err = cudaMemcpyAsync(table, both.data(), sizeof(int32_t) * both.size(), cudaMemcpyHostToDevice, s);
+    if (err == cudaSuccess) err = cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s);
+    if (err != cudaSuccess) {
+      cudaFreeAsync(table, s);
+      return cuda_fail(err, "scalar engine discrete table");
+    }
+    // the pageable source is staged before the copy call returns
+    DistParams dd{};
+    dd.kind = GR_DISCRETE;
+    dd.dtype = GR_I32;
+    dd.ncdf = ncdf;
+    dd.bitmask = mask;
+    dd.prob = table;
+    dd.alias = table + np;
+    st = sengine_words(se, w, W, s);
+    if (st == GR_OK) {
+      err = launch_scalar_xform(w, dev_out, npk, dd, s);
+      if (err != cudaSuccess) st = cuda_fail(err, "scalar-engine sampling kernel");
+    }
+    cudaFreeAsync(w, s);
+    cudaFreeAsync(table, s);
+    return st;
+  }
   DistParams dp{};
-  gr_status st = make_params(*desc, dp);
+  st = make_params(*desc, dp);
   if (st != GR_OK) return st;
   if (dp.dtype == GR_I32 && (dp.kind == GR_POISSON || dp.kind == GR_BINOMIAL || dp.kind == GR_UNIFORM_INT))
     return sengine_int(se, dp, dev_out, n, s);
@@ -1879,7 +1924,7 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
   if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
     return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
-                                    "randBits), gamma, chiSquared, studentT, poisson, binomial and uniformInt");
+                                    "randBits), gamma, chiSquared, studentT, poisson, binomial, uniformInt, geometric and discrete");
   const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
   if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
   if (n == 0) return GR_OK;

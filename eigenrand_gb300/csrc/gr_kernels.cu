@@ -1009,6 +1009,9 @@ cudaError_t launch_scalar_xform(const uint64_t* w, void* out, int64_t npk, const
     if (d.kind == GR_RANDBITS) return run_sx<S_I32, GR_RANDBITS>(w, out, npk, d, s);
     if (d.kind == GR_BERNOULLI) return run_sx<S_I32, GR_BERNOULLI>(w, out, npk, d, s);
     if (d.kind == GR_GEOMETRIC) return run_sx<S_I32, GR_GEOMETRIC>(w, out, npk, d, s);
+    // DiscreteGen: a Packet8i of four draws per two output packets, so packet
+    // t still reads draws 2t and 2t + 1
+    if (d.kind == GR_DISCRETE) return run_sx<S_I32, GR_DISCRETE>(w, out, npk, d, s);
     return cudaErrorNotSupported;
   }
   if (d.dtype == GR_F32) {

@@ -1962,6 +1962,21 @@ int or_sgen_int(or_seng* s, int kind, int32_t trials, double a, int32_t* out, si
   return rc;
 }
 
+/* DiscreteGen<int32_t> with a scalar engine as the Urng, a fresh generator
+ * (the free function discrete()): a Packet8i of four draws per two packets. */
+int or_sgen_discrete(or_seng* s, const or_discrete* d, int32_t* out, size_t n) {
+  or_vmt dummy;
+  memset(&dummy, 0, sizeof dummy);
+  dummy.L = 4;
+  or_gen g;
+  memset(&g, 0, sizeof g);
+  or_seng* prev = g_src;
+  g_src = s;
+  const int rc = or_gen_discrete(&dummy, &g, d, out, n);
+  g_src = prev;
+  return rc;
+}
+
 int or_sgen_randbits(or_seng* s, int32_t* out, size_t n) {
   or_vmt dummy;
   memset(&dummy, 0, sizeof dummy);

@@ -141,6 +141,7 @@ or_discrete* or_discrete_new(const double* w, int n);
 void or_discrete_free(or_discrete* d);
 int or_discrete_table(const or_discrete* d, int32_t* prob, int32_t* alias, int cap);
 int or_gen_discrete(or_vmt* e, or_gen* g, const or_discrete* d, int32_t* out, size_t n);
+int or_sgen_discrete(or_seng* s, const or_discrete* d, int32_t* out, size_t n);
 /* MultinomialGen<int32_t>(trials, w) per-trial path; out = dim x samples col-major */
 int or_gen_multinomial(or_vmt* e, or_gen* g, const or_discrete* d, int32_t trials, int32_t dim, int32_t* out,
                        size_t samples);

@@ -96,6 +96,8 @@ def lib():
         L.or_sgen_binomial_v.restype = ctypes.c_int
         L.or_sgen_int.argtypes = [vp, ctypes.c_int, ctypes.c_int32, ctypes.c_double, vp, ctypes.c_size_t]
         L.or_sgen_int.restype = ctypes.c_int
+        L.or_sgen_discrete.argtypes = [vp, vp, vp, ctypes.c_size_t]
+        L.or_sgen_discrete.restype = ctypes.c_int
         L.or_gen_trunc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, vp, sz]
         L.or_gen_trunc.restype = ctypes.c_int
@@ -156,6 +158,17 @@ class ScalarEngine:
     def raw(self, n):
         out = np.empty(n, dtype=np.uint64)
         self.L.or_seng_raw(self.h, _p(out), n)
+        return out
+
+    def discrete(self, weights, n):
+        """discrete() (a fresh DiscreteGen<int32_t>) through the scalar engine."""
+        w = np.asarray(weights, dtype=np.float64)
+        d = self.L.or_discrete_new(_p(w), len(w))
+        out = np.empty(n, dtype=np.int32)
+        rc = self.L.or_sgen_discrete(self.h, d, _p(out), n)
+        self.L.or_discrete_free(d)
+        if rc:
+            raise RuntimeError(f"oracle error {rc}")
         return out
 
     def binomial_v(self, trials, p):

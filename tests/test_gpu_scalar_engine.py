@@ -222,3 +222,19 @@ def test_scalar_engine_bernoulli_geometric_int(er, oracle, okind, cls):
         got = er.geometric(200, 40, u, p)
         assert_bits_equal(mem(got), o.generate(None, "GEOMETRIC", 8000, np.int32, p), f"{cls} geometric({p})")
     assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after")
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_discrete(er, oracle, okind, cls):
+    """discrete() (a fresh DiscreteGen<int32_t>) with a scalar engine: the CDF
+    (< 16 weights) and alias-table forms, even and odd packet counts (an odd
+    last packet draws a whole Packet8i), and raw draws after the calls."""
+    u = getattr(er, cls)(21)
+    o = oracle.ScalarEngine(okind, 21)
+    r = np.random.default_rng(2)
+    for nw in (5, 16, 100):
+        w = r.uniform(0.1, 2.0, nw)
+        for rows, cols in ((4, 3), (256, 130)):
+            got = er.discrete(rows, cols, u, w)
+            assert_bits_equal(mem(got), o.discrete(w, rows * cols), f"{cls} discrete({nw}) {rows}x{cols}")
+        assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after discrete({nw})")
