@@ -1898,7 +1898,8 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
   DistParams dp{};
   st = make_params(*desc, dp);
   if (st != GR_OK) return st;
-  if (dp.dtype == GR_I32 && (dp.kind == GR_POISSON || dp.kind == GR_BINOMIAL || dp.kind == GR_UNIFORM_INT))
+  if (dp.dtype == GR_I32 && (dp.kind == GR_POISSON || dp.kind == GR_BINOMIAL || dp.kind == GR_UNIFORM_INT ||
+                             dp.kind == GR_NEGATIVE_BINOMIAL))
     return sengine_int(se, dp, dev_out, n, s);
   if (dp.kind == GR_GAMMA && reject_code(dp) >= 0 && family_of(dp) == Family::Reject)
     return sengine_reject(se, dp, reject_code(dp), dev_out, n, s);
@@ -1924,7 +1925,8 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
   if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
     return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
-                                    "randBits), gamma, chiSquared, studentT, poisson, binomial, uniformInt, geometric and discrete");
+                                    "randBits), gamma, chiSquared, studentT, poisson, binomial, negativeBinomial, uniformInt, geometric "
+                                    "and discrete");
   const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
   if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
   if (n == 0) return GR_OK;

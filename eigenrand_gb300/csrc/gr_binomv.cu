@@ -316,8 +316,9 @@ __global__ void __launch_bounds__(32) k_binom_v_words(const uint64_t* w, int64_t
   }
 }
 
-// PoissonGen<int32_t>, BinomialGen<int32_t> and UniformIntGen<int32_t>
-// (Discrete.h:855-905, 990-1048, 287-333) on a scalar engine's pre-drawn
+// PoissonGen<int32_t>, BinomialGen<int32_t>, UniformIntGen<int32_t> and
+// NegativeBinomialGen<int32_t> (Discrete.h:855-905, 990-1048, 287-333,
+// GammaPoisson.h:55-110) on a scalar engine's pre-drawn
 // words, one chain: packets of 4 on SSE packets of two draws each.  Modes: BinomialGen with trials < 25
 // (one uniform packet per trial), the multiplicative Poisson loop (PoissonGen
 // mean < 12, BinomialGen mean < 1 through its PoissonGen member), and the tan
@@ -331,7 +332,9 @@ __global__ void __launch_bounds__(32) k_int_words(const uint64_t* w, int64_t nwo
   BvWordsSrc src{w, nwords / 2, lane};
   auto mask4 = [&](bool pr) -> unsigned { return __ballot_sync(0xffffffffu, pr && lane < 4) & 0xfu; };
   const bool binom = d.kind == GR_BINOMIAL;
-  const int mode = d.kind == GR_UNIFORM_INT ? 3 : ((binom && d.ia < 25) ? 0 : (d.ic ? 1 : 2));
+  const int mode = d.kind == GR_NEGATIVE_BINOMIAL ? 4
+                   : d.kind == GR_UNIFORM_INT     ? 3
+                                                  : ((binom && d.ia < 25) ? 0 : (d.ic ? 1 : 2));
   int fc = (int)carry[8];
   if (lane < fc) cb[lane] = carry[lane];
   __syncwarp();
@@ -399,6 +402,65 @@ __global__ void __launch_bounds__(32) k_int_words(const uint64_t* w, int64_t nwo
             } else {
               rx = src.next();
               bitcnt = d.ncdf;
+            }
+          }
+        }
+      }
+    } else if (mode == 4) {
+      // NegativeBinomialGen (GammaPoisson.h:55-110): a GammaGen<float>(trials,
+      // (1 - p) / p) packet (d.ic: 0 exponential, 1 product of d.ia uniforms,
+      // 2 tan rejection), then a Poisson draw per lane with that mean; both
+      // rejections append to the gamma's CompressMask cache
+      const float fpi = (float)3.1415926535897932, eps8 = 1.1920928955078125e-07f / 8;
+      float mean = 0.0f;
+      if (d.ic == 0) {
+        mean = d.fb * (-(logf_(1.0f - bv_ur(src.next())) / 1.0f));
+      } else if (d.ic == 1) {
+        float y = bv_ur(src.next()) + eps8;
+        for (int c = 1; c < d.ia; ++c) y = y * (bv_ur(src.next()) + eps8);
+        mean = -(d.fb * logf_(y));
+      } else {
+        for (;;) {
+          float ys, yc;
+          sincosf_(fpi * bv_ur(src.next()), ys, yc);
+          const float ux = bv_ur(src.next());
+          if (src.abort) break;
+          const float yx = ys / yc;
+          const float xx = d.fc * yx + d.fd;
+          const float ub = (yx * yx + 1.0f) * expf_(d.fd * logf_(xx / d.fd) - yx * d.fc);
+          uint32_t rb;
+          if (compress(f2u(d.fb * xx), (0.0f < xx) && (ux <= ub), rb)) {
+            mean = u2f(rb);
+            break;
+          }
+        }
+      }
+      if (!src.abort) {
+        const float pne = expf_(-mean);
+        if (mask4(12.0f < mean) == 0) {
+          float val = 1.0f;
+          for (;;) {
+            val = val * bv_ur(src.next());
+            if (src.abort) break;
+            const bool c = pne < val;
+            if (mask4(c) == 0) break;
+            r += c ? 1 : 0;
+          }
+        } else {
+          const float sq = sqrtf(2.0f * mean), lm = logf_(mean), g1 = mean * lm - lgamma_approxf_(mean + 1.0f);
+          for (;;) {
+            float s2, c2;
+            sincosf_(fpi * bv_ur(src.next()), s2, c2);
+            const float yx = s2 / c2;
+            const float fres = truncf(sq * yx + mean);
+            const float p1 = (yx * yx + 1.0f) * 0.9f;
+            const float u2 = bv_ur(src.next());
+            if (src.abort) break;
+            const float p2 = expf_((fres * lm - lgamma_approxf_(fres + 1.0f)) - g1);
+            uint32_t rb;
+            if (compress(f2u(fres), (0.0f <= fres) && (u2 <= p1 * p2), rb)) {
+              r = cvtt_f32(u2f(rb));
+              break;
             }
           }
         }

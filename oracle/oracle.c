@@ -1942,7 +1942,8 @@ int or_sgen_binomial_v(or_seng* s, const int32_t* trials, const float* p, int32_
 }
 
 /* PoissonGen (kind 0) / BinomialGen (kind 1) / UniformIntGen (kind 2, min a,
- * max trials) / BernoulliGen (kind 3) / GeometricGen (kind 4) <int32_t> with
+ * max trials) / BernoulliGen (kind 3) / GeometricGen (kind 4) /
+ * NegativeBinomialGen (kind 5, trials, p = a) <int32_t> with
  * a scalar engine as the Urng, a fresh generator
  * (the free functions): every packet takes two draws (draw_half). */
 int or_sgen_int(or_seng* s, int kind, int32_t trials, double a, int32_t* out, size_t n) {
@@ -1957,7 +1958,8 @@ int or_sgen_int(or_seng* s, int kind, int32_t trials, double a, int32_t* out, si
                  : kind == 1 ? or_gen_binomial(&dummy, &g, trials, a, out, n)
                  : kind == 2 ? or_gen_uniform_int(&dummy, &g, (int32_t)a, trials, out, n)
                  : kind == 3 ? or_gen_bernoulli_i32(&dummy, a, out, n)
-                             : or_gen_geometric(&dummy, a, out, n);
+                 : kind == 4 ? or_gen_geometric(&dummy, a, out, n)
+                             : or_gen_negative_binomial(&dummy, &g, trials, a, out, n);
   g_src = prev;
   return rc;
 }

@@ -187,9 +187,11 @@ class ScalarEngine:
     def generate(self, gen, kind, n, dtype=np.float32, a=0.0, b=0.0, trials=0):
         """Real kinds of generate(), RANDBITS, and the free functions poisson() /
         binomial() (a fresh generator each call), drawn through the scalar engine."""
-        if kind in ("POISSON", "BINOMIAL", "UNIFORM_INT") or (kind in ("BERNOULLI", "GEOMETRIC") and dtype == np.int32):
+        if kind in ("POISSON", "BINOMIAL", "UNIFORM_INT", "NEGATIVE_BINOMIAL") or (
+                kind in ("BERNOULLI", "GEOMETRIC") and dtype == np.int32):
             out = np.empty(n, dtype=np.int32)
-            k = {"POISSON": 0, "BINOMIAL": 1, "UNIFORM_INT": 2, "BERNOULLI": 3, "GEOMETRIC": 4}[kind]
+            k = {"POISSON": 0, "BINOMIAL": 1, "UNIFORM_INT": 2, "BERNOULLI": 3, "GEOMETRIC": 4,
+                 "NEGATIVE_BINOMIAL": 5}[kind]
             t = int(b) if kind == "UNIFORM_INT" else int(trials)  # UNIFORM_INT: a = min, b = max
             rc = self.L.or_sgen_int(self.h, k, t, float(a), _p(out), n)
         elif kind == "RANDBITS":

@@ -238,3 +238,19 @@ def test_scalar_engine_discrete(er, oracle, okind, cls):
             got = er.discrete(rows, cols, u, w)
             assert_bits_equal(mem(got), o.discrete(w, rows * cols), f"{cls} discrete({nw}) {rows}x{cols}")
         assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after discrete({nw})")
+
+
+@pytest.mark.parametrize("okind,cls", ENGINES)
+def test_scalar_engine_negative_binomial(er, oracle, okind, cls):
+    """negativeBinomial() (a fresh NegativeBinomialGen<int32_t>) with a scalar
+    engine: the gamma's exponential / product / tan forms, Poisson means below
+    and above 12 (the tan rejection sharing the gamma's CompressMask cache),
+    and raw draws after the calls."""
+    u = getattr(er, cls)(33)
+    o = oracle.ScalarEngine(okind, 33)
+    for trials, p in ((1, 0.3), (5, 0.5), (25, 0.8), (30, 0.1), (3, 0.05)):
+        for rows, cols in ((4, 3), (128, 96)):
+            got = er.negativeBinomial(rows, cols, u, trials, p)
+            ref = o.generate(None, "NEGATIVE_BINOMIAL", rows * cols, np.int32, p, trials=trials)
+            assert_bits_equal(mem(got), ref, f"{cls} negativeBinomial({trials}, {p}) {rows}x{cols}")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after")
