@@ -544,6 +544,15 @@ def bench_next_rows(er, streams=608):
     outi = torch.empty_like(trials)
     res["binomialV/i32"] = entry(_median_ms(lambda: er.binomial(urng, trials, pr, out=outi)), 12 * N)
     del trials, pr, outi
+    # gamma(0.5) with P8_mt19937_64 (the reference tests' engine) as the Urng:
+    # pre-drawn words, all trials evaluated at once, CompressMask filter
+    p8 = er.P8_mt19937_64(1234)
+    for tdt, tag in ((torch.float32, "f32"), (torch.float64, "f64")):
+        es = 4 if tdt == torch.float32 else 8
+        out = torch.empty((4096, 4096), dtype=tdt, device="cuda")
+        res[f"gamma0.5_P8_mt19937_64/{tag}"] = entry(
+            _median_ms(lambda: er.gamma(4096, 4096, p8, 0.5, 1.0, dtype=tdt, out=out)), N * es)
+        del out
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     return res
