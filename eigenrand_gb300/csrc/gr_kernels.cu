@@ -684,21 +684,38 @@ cudaError_t launch_prefix(const EngState* st, const GenState* gen, int K, uint64
   return cudaGetLastError();
 }
 
-cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, int S, uint64_t* segwin,
-                        cudaStream_t s) {
-  if (S <= 1) return cudaSuccess;
-  const size_t smem = (size_t)(kPrefixLen + kN) * sizeof(uint64_t);
+static constexpr size_t kJumpSmem = (size_t)(kPrefixLen + kN) * sizeof(uint64_t);
+
+// k_jump's dynamic shared-memory limit, set once per device.
+static cudaError_t jump_attr() {
   static bool attr[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_jump, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_jump, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJumpSmem);
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  k_jump<<<K * (S - 1) * kLanes, kJumpThreads, smem, s>>>(prefix, polys, S, segwin);
+  return cudaSuccess;
+}
+
+cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, int S, uint64_t* segwin,
+                        cudaStream_t s) {
+  if (S <= 1) return cudaSuccess;
+  cudaError_t e = jump_attr();
+  if (e != cudaSuccess) return e;
+  k_jump<<<K * (S - 1) * kLanes, kJumpThreads, kJumpSmem, s>>>(prefix, polys, S, segwin);
   return cudaGetLastError();
+}
+
+cudaError_t preload_raw_stream_kernels() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k_prefix);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_jump);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_direct<M_RAW, kRawKind>);
+  if (e == cudaSuccess) e = jump_attr();
+  return e;
 }
 
 int kind_granule(int kind, int dtype) {

@@ -72,6 +72,10 @@ cudaError_t launch_prefix(const EngState* st, const GenState* gen, int K, uint64
                           cudaStream_t s);
 cudaError_t launch_jump(const uint64_t* prefix, const uint64_t* polys, int K, int S, uint64_t* segwin,
                         cudaStream_t s);
+// Loads the code of k_prefix, k_jump and the raw-stream k_direct on the
+// current device and sets k_jump's shared-memory limit, so that later
+// launches of them load nothing.
+cudaError_t preload_raw_stream_kernels();
 // Fused engine + transform for kinds whose draws per output are fixed and
 // packet aligned.  Returns cudaErrorNotSupported for other kinds.
 cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s);

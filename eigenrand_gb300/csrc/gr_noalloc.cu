@@ -7,15 +7,19 @@
 // allocating behind its back.  Such a caller creates its engine once during
 // set-up, passes its own output buffer on every call, and this entry point
 // then allocates nothing: the jump-ahead scratch (lane prefixes, segment
-// windows, jump polynomials) lives in one file-scope __device__ array that
-// every GPU loading the library keeps until process exit.
+// windows) and every jump polynomial a call can need live in one file-scope
+// __device__ array that every GPU loading the library keeps until process
+// exit.
 //
 // Limits: engines created with streams = 1 only, n <= GR_NOALLOC_MAX_DRAWS,
-// at most kMaxSeg jump-ahead segments per call.  All calls share the array,
-// so calls that overlap on the GPU (different streams, different threads)
-// race on it and must be serialised by the caller.  The first call on a
-// device performs the one-time set-up (looking up the array's device address
-// and the kernel attributes); make that first call before any stream capture.
+// at most kMaxSeg jump-ahead segments per call (the allocating gr_raw_u64
+// splits a long call into up to 128).  All calls share the array, so calls
+// that overlap on the GPU (different streams, different threads) race on it
+// and must be serialised by the caller.  The first call on a device performs
+// the one-time set-up, with that device current: it looks up the array's
+// device address, loads the kernels' code, computes the jump polynomials for
+// every segment length a call can use and copies them into the array
+// (synchronously).  Make that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -34,30 +38,68 @@ using namespace gr;
 namespace {
 
 constexpr int kMaxSeg = 32;
+// Segment lengths are powers of two: J = 2^kLogJMin .. 2^kLogJMax packets.
+// The largest call (2^32 draws = 2^30 packets) in kMaxSeg segments needs
+// J = 2^25.
+constexpr int kLogJMin = 14;
+constexpr int kLogJMax = 25;
+constexpr int kJSets = kLogJMax - kLogJMin + 1;                             // 12
 constexpr size_t kPrefixWords = (size_t)kLanes * kPrefixLen;              // 82368
 constexpr size_t kSegWords = (size_t)(kMaxSeg - 1) * kLanes * kN;          // 38688
-constexpr size_t kPolyWordsAll = (size_t)(kMaxSeg - 1) * kPolyWords;       // 9672
+constexpr size_t kPolySetWords = (size_t)(kMaxSeg - 1) * kPolyWords;       // 9672 per J
+constexpr size_t kPolyWordsAll = (size_t)kJSets * kPolySetWords;           // 116064
 constexpr size_t kSnapWords = (sizeof(CallSnap) + 7) / 8 + 1;
 constexpr size_t kScratchWords = kPrefixWords + kSegWords + kPolyWordsAll + kSnapWords;
 
 }  // namespace
 
-// ~1.0 MiB per device, held until process exit.
+// ~1.9 MiB per device, held until process exit.
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kScratchWords];
 
 namespace {
 
 struct DevScratch {
   uint64_t* base = nullptr;  // device address of g_noalloc_scratch on this device
-  int64_t poly_J = -1;       // jump polynomials currently resident
-  int poly_count = 0;
 };
 
 std::mutex g_mu;
 std::map<int, DevScratch> g_dev;
-std::map<int64_t, std::vector<Poly>> g_host_polys;  // host cache, by segment length
+std::vector<Poly> g_host_polys;  // [kJSets][kMaxSeg - 1], computed once per process
 
 gr_status na_fail(gr_status s, const std::string& m) { return set_last_error(s, m); }
+
+// x^(i J) mod P(x) for every J = 2^kLogJMin .. 2^kLogJMax and i = 1 .. kMaxSeg - 1.
+gr_status host_polys() {
+  if (!g_host_polys.empty()) return GR_OK;
+  if (charpoly_terms().size() != 284)
+    return na_fail(GR_ERR_CUDA, "gr_raw_u64_noalloc: characteristic polynomial recovery failed");
+  std::vector<uint64_t> exps;
+  exps.reserve((size_t)kJSets * (kMaxSeg - 1));
+  for (int lj = kLogJMin; lj <= kLogJMax; ++lj)
+    for (int i = 1; i < kMaxSeg; ++i) exps.push_back((uint64_t)i << lj);
+  pow_x_mod_many(exps, g_host_polys);
+  return GR_OK;
+}
+
+// One-time set-up for the current device.
+gr_status setup_device(DevScratch& ds) {
+  void* p = nullptr;
+  cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (err != cudaSuccess)
+    return na_fail(GR_ERR_CUDA, std::string("gr_raw_u64_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(err));
+  err = preload_raw_stream_kernels();
+  if (err != cudaSuccess)
+    return na_fail(GR_ERR_CUDA, std::string("gr_raw_u64_noalloc: loading kernels: ") + cudaGetErrorString(err));
+  gr_status st = host_polys();
+  if (st != GR_OK) return st;
+  uint64_t* polys = (uint64_t*)p + kPrefixWords + kSegWords;
+  static_assert(sizeof(Poly) == kPolyWords * sizeof(uint64_t), "Poly is kPolyWords words");
+  err = cudaMemcpy(polys, g_host_polys.data(), sizeof(uint64_t) * kPolyWordsAll, cudaMemcpyHostToDevice);
+  if (err != cudaSuccess)
+    return na_fail(GR_ERR_CUDA, std::string("gr_raw_u64_noalloc: jump tables: ") + cudaGetErrorString(err));
+  ds.base = (uint64_t*)p;
+  return GR_OK;
+}
 
 }  // namespace
 
@@ -77,12 +119,8 @@ extern "C" gr_status gr_raw_u64_noalloc(gr_engine* e, uint64_t* dev_out, size_t 
   std::lock_guard<std::mutex> lk(g_mu);
   DevScratch& ds = g_dev[dev];
   if (!ds.base) {
-    // one-time set-up for this device, with this device current
-    void* p = nullptr;
-    cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (err != cudaSuccess)
-      return na_fail(GR_ERR_CUDA, std::string("gr_raw_u64_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(err));
-    ds.base = (uint64_t*)p;
+    gr_status st = setup_device(ds);
+    if (st != GR_OK) return st;
   }
   uint64_t* prefix = ds.base;
   uint64_t* segwin = prefix + kPrefixWords;
@@ -93,12 +131,14 @@ extern "C" gr_status gr_raw_u64_noalloc(gr_engine* e, uint64_t* dev_out, size_t 
   const int64_t packets = (int64_t)(n / kLanes);
   int S = 1;
   int64_t J = packets;
+  int lj = 0;
   if (packets >= ((int64_t)1 << 17)) {
-    int64_t j = (int64_t)1 << 14;
-    while (j * 128 < packets) j <<= 1;
-    while ((packets + j - 1) / j > kMaxSeg) j <<= 1;
-    J = j;
-    S = (int)((packets + j - 1) / j);
+    lj = kLogJMin;
+    while (((int64_t)128 << lj) < packets) ++lj;
+    while ((packets + ((int64_t)1 << lj) - 1) >> lj > kMaxSeg) ++lj;
+    if (lj > kLogJMax) return na_fail(GR_ERR_INVALID, "gr_raw_u64_noalloc: call too long for the jump tables");
+    J = (int64_t)1 << lj;
+    S = (int)((packets + J - 1) / J);
   }
   Plan p{};
   p.eng = engine_state_ptr(e);
@@ -111,24 +151,10 @@ extern "C" gr_status gr_raw_u64_noalloc(gr_engine* e, uint64_t* dev_out, size_t 
   p.gran_rem = 0;
   p.out = dev_out;
   if (S > 1) {
-    if (ds.poly_J != J || ds.poly_count < S - 1) {
-      auto& hp = g_host_polys[J];
-      if ((int)hp.size() < kMaxSeg - 1) {
-        if (charpoly_terms().size() != 284)
-          return na_fail(GR_ERR_CUDA, "gr_raw_u64_noalloc: characteristic polynomial recovery failed");
-        std::vector<uint64_t> exps(kMaxSeg - 1);
-        for (int i = 0; i < kMaxSeg - 1; ++i) exps[i] = (uint64_t)(i + 1) * (uint64_t)J;
-        pow_x_mod_many(exps, hp);
-      }
-      // pageable source: staged before cudaMemcpyAsync returns
-      cudaError_t err = cudaMemcpyAsync(polys, hp.data(), sizeof(uint64_t) * kPolyWordsAll, cudaMemcpyHostToDevice, s);
-      if (err != cudaSuccess)
-        return na_fail(GR_ERR_CUDA, std::string("gr_raw_u64_noalloc: poly upload: ") + cudaGetErrorString(err));
-      ds.poly_J = J;
-      ds.poly_count = kMaxSeg - 1;
-    }
+    // the tables for this J: x^(i J) mod P for i = 1 .. kMaxSeg - 1
+    const uint64_t* pj = polys + (size_t)(lj - kLogJMin) * kPolySetWords;
     cudaError_t err = launch_prefix(p.eng, nullptr, 1, prefix, snap, s);
-    if (err == cudaSuccess) err = launch_jump(prefix, polys, 1, S, segwin, s);
+    if (err == cudaSuccess) err = launch_jump(prefix, pj, 1, S, segwin, s);
     if (err != cudaSuccess)
       return na_fail(GR_ERR_CUDA, std::string("gr_raw_u64_noalloc: jump-ahead: ") + cudaGetErrorString(err));
     p.segwin = segwin;
