@@ -72,9 +72,19 @@ def elem_bytes(tag):
     return {"f32": 4, "f64": 8, "i32": 4}[tag]
 
 
-def kernel_of(name):
-    """Sampling kernel of a sweep entry (streams mode: one launch per call)."""
+def kernel_of(name, compat=False):
+    """Sampling kernel of a sweep entry (streams mode: one launch per call;
+    compat: the single-engine kernels)."""
     base, tag = name.split("/")
+    if compat:
+        if base == "beta":
+            return f"k_beta<{'float' if tag == 'f32' else 'double'}> (one CTA)"
+        if base == "poisson4":
+            return "k_poisson (one CTA)"
+        if base in ("gamma0.5", "poisson100"):
+            return "k_rs_count/scan/write/gather/finish (segmented rejection)"
+        return "k_prefix + k_jump + " + ("k_staged" if base in ("gamma5", "binomial20") else "k_direct") + \
+            " (jump-ahead segments)"
     if base == "beta":
         return f"k_beta<{'float' if tag == 'f32' else 'double'}>"
     if base in ("gamma0.5", "poisson100"):
@@ -99,12 +109,14 @@ MEASURED = {
 }
 
 
-def roofline_entry(name, pd, hbm_peak, peaks):
+def roofline_entry(name, pd, hbm_peak, peaks, measured=True):
     """Roofline of one sweep entry's kernel: algorithmic bytes (the output,
-    4 or 8 B per sample, 2^24 samples per launch) / its graph-replay time."""
-    m = MEASURED.get(name, {})
+    4 or 8 B per sample, 2^24 samples per launch) / its graph-replay time.
+    measured=False: the ncu figures (captured on the 608-stream engine) do
+    not apply."""
+    m = MEASURED.get(name, {}) if measured else {}
     bps = m.get("dram_bytes_per_sample")
-    e = {"kernel": f"{kernel_of(name)} ({name})", "bound": "hbm", "achieved": pd["gbs"], "peak": hbm_peak,
+    e = {"kernel": f"{kernel_of(name, compat=not measured)} ({name})", "bound": "hbm", "achieved": pd["gbs"], "peak": hbm_peak,
          "unit": "GB/s", "frac": round(pd["gbs"] / hbm_peak, 4),
          "traffic": round(bps * N) if bps else None,
          "peak_source": "measured" if peaks else "fallback"}
@@ -173,6 +185,95 @@ def load_peaks():
 
 
 # --------------------------------------------------------------------------- ours
+class Sweep:
+    """The 26 calls of the sweep on one engine: one generator object per
+    distribution (the reference benchmark's "/gen" form, reused across steps;
+    4096^2 is a whole number of packets, so no cache carries between calls and
+    the values equal the free functions'), one output buffer per call."""
+
+    def __init__(self, er, urng, items):
+        import torch
+        self.er, self.urng, self.items = er, urng, items
+        tdt = {"f32": torch.float32, "f64": torch.float64, "i32": torch.int32}
+        self.outs = [torch.empty(N, dtype=tdt[t], device="cuda") for (_, _, t, *_r) in items]
+        self.gens = []
+        for (name, kind, t, a, b, tr, w) in items:
+            d, keep = er._desc(kind, tdt[t], a, b, tr, w)
+            h = ctypes.c_void_p()
+            er._lib.check(er._L.gr_gen_create(ctypes.byref(h), ctypes.byref(d)))
+            self.gens.append(h)
+
+    def close(self):
+        for h in self.gens:
+            self.er._L.gr_gen_destroy(h)
+        self.gens = []
+        self.outs = []
+
+    def one(self, i, s=None):
+        import torch
+        sp = ctypes.c_void_p((s or torch.cuda.current_stream()).cuda_stream)
+        self.er._lib.check(self.er._L.gr_generate(self.gens[i], self.urng._h,
+                                                  ctypes.c_void_p(self.outs[i].data_ptr()), N, sp))
+
+    def step(self):
+        for i in range(len(self.items)):
+            self.one(i)
+
+    def per_call_ms(self, R):
+        """Device time of each call: R calls captured in a CUDA graph, replayed
+        between CUDA events (no host launch gaps in the interval); median of 3."""
+        import torch
+        stream = torch.cuda.current_stream()
+        per = {}
+        for i, it in enumerate(self.items):
+            g = torch.cuda.CUDAGraph()
+            cs = torch.cuda.Stream()
+            cs.wait_stream(stream)
+            with torch.cuda.stream(cs):
+                self.one(i, cs)  # warm on the capture stream
+                cs.synchronize()
+                with torch.cuda.graph(g, stream=cs):
+                    for _ in range(R):
+                        self.one(i, cs)
+            stream.wait_stream(cs)
+            torch.cuda.synchronize()
+            for rep in range(3):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                g.replay()
+                e1.record(stream)
+                e1.synchronize()
+                per.setdefault(it[0], []).append(e0.elapsed_time(e1) / R)
+            del g
+        torch.cuda.synchronize()
+        return {k: statistics.median(v) for k, v in per.items()}
+
+    def timed_steps(self, steps):
+        """ms for `steps` whole sweeps between CUDA events on the launching stream."""
+        import torch
+        stream = torch.cuda.current_stream()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            self.step()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1)
+
+
+def per_dist_table(items, per, hbm_peak):
+    out = {}
+    for name, kind, t, *_r in items:
+        m = per[name]
+        gb = N * elem_bytes(t) / 1e9
+        out[name] = {"ms": round(m, 4), "gsamples_s": round(N / (m / 1e3) / 1e9, 3),
+                     "gbs": round(gb / (m / 1e3), 1), "hbm_frac": round(gb / (m / 1e3) / hbm_peak, 3)}
+    return out
+
+
 def run_ours(args, rank, world):
     import torch
     import eigenrand_gb300 as er
@@ -186,31 +287,8 @@ def run_ours(args, rank, world):
     seed = 1234 + rank * 4 * 1000003  # replicas draw disjoint engines
     urng = er.Vmt19937_64(seed, streams=streams)
     items = sweep_items()
-    tdt = {"f32": torch.float32, "f64": torch.float64, "i32": torch.int32}
-    outs = [torch.empty(N, dtype=tdt[t], device="cuda") for (_, _, t, *_r) in items]
-    descs = []
-    for (name, kind, t, a, b, tr, w) in items:
-        d, keep = er._desc(kind, tdt[t], a, b, tr, w)
-        descs.append((d, keep))
-    L = er._L
-    # one generator object per distribution, reused across steps (the
-    # reference benchmark's "/gen" form); 4096^2 is a whole number of packets,
-    # so no cache carries between calls and the values equal the free functions'
-    gens = []
-    for (d, keep) in descs:
-        h = ctypes.c_void_p()
-        er._lib.check(L.gr_gen_create(ctypes.byref(h), ctypes.byref(d)))
-        gens.append(h)
-
-    def one(i, s=None):
-        sp = ctypes.c_void_p((s or torch.cuda.current_stream()).cuda_stream)
-        er._lib.check(L.gr_generate(gens[i], urng._h, ctypes.c_void_p(outs[i].data_ptr()), N, sp))
-
+    sw = Sweep(er, urng, items)
     stream = torch.cuda.current_stream()
-
-    def step():
-        for i in range(len(items)):
-            one(i)
 
     def barrier():
         if world > 1:
@@ -218,49 +296,17 @@ def run_ours(args, rank, world):
             dist.barrier()
 
     for _ in range(args.warmup):
-        step()
+        sw.step()
     torch.cuda.synchronize()
-    # per-distribution device time: R calls captured in a CUDA graph, replayed
-    # between CUDA events (no host launch gaps in the interval)
-    per = {}
-    R = 8 if args.mode == "streams" else 1
-    for i, it in enumerate(items):
-        g = torch.cuda.CUDAGraph()
-        cs = torch.cuda.Stream()
-        cs.wait_stream(stream)
-        with torch.cuda.stream(cs):
-            one(i, cs)  # warm on the capture stream
-            cs.synchronize()
-            with torch.cuda.graph(g, stream=cs):
-                for _ in range(R):
-                    one(i, cs)
-        stream.wait_stream(cs)
-        torch.cuda.synchronize()
-        for rep in range(3):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            g.replay()
-            e1.record(stream)
-            e1.synchronize()
-            per.setdefault(it[0], []).append(e0.elapsed_time(e1) / R)
-        del g
-    torch.cuda.synchronize()
+    per = sw.per_call_ms(8 if streams > 1 else 1)
 
     clocks = ClockSampler(dev)
     barrier()
     torch.cuda.synchronize()
     clocks.start()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for _ in range(args.steps):
-        step()
-    t1.record(stream)
-    torch.cuda.synchronize()
+    ms = sw.timed_steps(args.steps)
     barrier()
     clk = clocks.stop()
-    ms = t0.elapsed_time(t1)
     if world > 1:
         import torch.distributed as dist
         tt = torch.tensor([ms], device="cuda")
@@ -271,11 +317,11 @@ def run_ours(args, rank, world):
 
     # e2e: the same sweep through the public API into host memory (pinned),
     # D2H copy of every result inside the timed region
+    outs = sw.outs
     host = [torch.empty(N, dtype=o.dtype, pin_memory=True) for o in outs]
-    for _ in range(1):
-        for i in range(len(items)):
-            one(i)
-            host[i].copy_(outs[i], non_blocking=True)
+    for i in range(len(items)):
+        sw.one(i)
+        host[i].copy_(outs[i], non_blocking=True)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -283,29 +329,29 @@ def run_ours(args, rank, world):
     e0.record(stream)
     for _ in range(args.steps):
         for i in range(len(items)):
-            one(i)
+            sw.one(i)
             host[i].copy_(outs[i], non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     d2h = sum(o.numel() * o.element_size() for o in outs)
+    del host
 
     peaks = load_peaks()
     hbm_peak = peaks["hbm_gbs"] if peaks else 6800.0
-    per_dist = {}
-    best_name, best_ms = None, -1.0
-    for name, kind, t, *_r in items:
-        m = statistics.median(per[name])
-        gb = N * elem_bytes(t) / 1e9
-        per_dist[name] = {"ms": round(m, 4), "gsamples_s": round(N / (m / 1e3) / 1e9, 3),
-                          "gbs": round(gb / (m / 1e3), 1), "hbm_frac": round(gb / (m / 1e3) / hbm_peak, 3)}
-        if m > best_ms:
-            best_ms, best_name = m, name
+    per_dist = per_dist_table(items, per, hbm_peak)
     # roofline of the dominant kernel (the slowest call of the step) and of
     # the HBM-write-bound uniform float kernel
-    dom = per_dist[best_name]
-    uf = per_dist["uniformReal/f32"]
+    best_name = max(per, key=per.get)
     launches_per_call = 1 if streams > 1 else 3
+    if streams > 1:
+        workload = (f"univariate sweep 4096x4096 per call, 26 calls (11 kinds f32 + f64, 4 int32 kinds); "
+                    f"engine: {streams} independent Vmt19937_64(1234 + 4k) streams (one per engine, the "
+                    f"reference's one-engine-per-thread usage), each filling a contiguous slice of every call; "
+                    f"the single-engine Vmt19937_64(1234) sweep is timed under 'compat'")
+    else:
+        workload = ("univariate sweep 4096x4096 per call, 26 calls; engine: one Vmt19937_64(1234) carried "
+                    "across the sweep (the reference stream, bit-exact)")
     res = {
         "metric": "Gsamples/s (univariate sweep, 4096x4096 per distribution)",
         "value": round(value, 3),
@@ -319,28 +365,58 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32+f64+i32",
         "data": "synthetic (engine seeded 1234)",
-        "config": {"workload": "univariate sweep 4096x4096, one Vmt19937_64(1234) carried across the sweep",
+        "config": {"workload": workload,
                    "engine_mode": args.mode, "engine_streams": streams,
                    "distributions": [it[0] for it in items],
                    "l2": "distinct output buffer per distribution; 2.4 GB written per step > 129 MB L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "per_dist": per_dist,
-        "roofline": roofline_entry(best_name, dom, hbm_peak, peaks),
-        "roofline_hbm_kernel": roofline_entry("uniformReal/f32", uf, hbm_peak, peaks),
+        "roofline": roofline_entry(best_name, per_dist[best_name], hbm_peak, peaks),
+        "roofline_hbm_kernel": roofline_entry("uniformReal/f32", per_dist["uniformReal/f32"], hbm_peak, peaks),
         "e2e": {"value": round(samples_per_step * args.steps * world / (e2e_ms / 1e3) / 1e9, 3),
                 "unit": "Gsamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_per_call * len(items) * args.steps,
         "clocks": clk,
     }
+    sw.close()
+    del sw, outs
+    torch.cuda.empty_cache()
+    if streams > 1 and not args.no_compat:
+        res["compat"] = bench_compat(er, items, hbm_peak, peaks, steps=max(3, min(args.steps, 10)))
     if not args.no_extras:
-        del outs, host
-        torch.cuda.empty_cache()
         res["workloads"] = {"batched_vop": bench_batched(er), "multivariate": bench_multivariate(er),
                             "truncated_and_per_element": bench_next_rows(er),
                             "serving": bench_serving(er, seconds=args.serve_seconds)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
     return res
+
+
+def bench_compat(er, items, hbm_peak, peaks, steps=5, warmup=3):
+    """The sweep on ONE Vmt19937_64(1234) carried across all 26 calls: the
+    single reference stream, bit-exact with the reference run as written.
+    Long calls run as jump-ahead segments (closed forms) or segmented
+    rejection; the data-dependent walks run on one CTA."""
+    import torch
+    urng = er.Vmt19937_64(1234)
+    sw = Sweep(er, urng, items)
+    for _ in range(warmup):
+        sw.step()
+    torch.cuda.synchronize()
+    per = sw.per_call_ms(1)
+    ms = sw.timed_steps(steps)
+    value = N * len(items) * steps / (ms / 1e3) / 1e9
+    per_dist = per_dist_table(items, per, hbm_peak)
+    best = max(per, key=per.get)
+    sw.close()
+    torch.cuda.empty_cache()
+    return {"workload": "univariate sweep 4096x4096 per call, 26 calls, one Vmt19937_64(1234) carried across "
+                        "the sweep (the reference benchmark's engine use, benchmark/benchmark.cpp:15-20)",
+            "value": round(value, 3), "unit": "Gsamples/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": round(ms / steps, 4), "per_dist": per_dist,
+            "roofline": roofline_entry(best, per_dist[best], hbm_peak, peaks, measured=False),
+            "roofline_hbm_kernel": roofline_entry("uniformReal/f32", per_dist["uniformReal/f32"], hbm_peak, peaks,
+                                                  measured=False)}
 
 
 # --------------------------------------------------------------------------- other workloads
@@ -689,6 +765,23 @@ def bench_serving(er, seconds=6.0, rates=(2000.0, 500.0), nclients=256, budget=4
 
 
 # --------------------------------------------------------------------------- reference arm
+def host_cpu():
+    """ISA and model of the host cores that run the CPU baseline."""
+    import platform
+    info = {"isa": platform.machine(), "model": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                info["model"] = v.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    info["code"] = ("scalar C restatement of the reference's packet algorithms (oracle/), -O2, no SIMD "
+                    "intrinsics: the reference's AVX2 / NEON packet code needs Eigen, which is absent")
+    return info
+
+
 def cpu_run(per_dist_samples, threads=1):
     """The reference's CPU path over a bounded sample of the sweep.  The
     reference needs Eigen, which is absent, so this runs its restatement
@@ -728,6 +821,7 @@ def cpu_baseline(seconds=15.0):
     n = int(n0 * max(1.0, seconds / max(t0, 1e-3)))
     s, t = cpu_run(n, threads)
     return {"value": round(s / t / 1e9, 5), "unit": "Gsamples/s", "cores": threads, "kind": "port",
+            "cpu": host_cpu(),
             "sample": f"{s // len(sweep_items())} samples per distribution x {len(sweep_items())} distributions "
                       f"({t:.1f} s), {threads} threads each with its own Vmt19937_64(1234+4k); the reference needs "
                       "Eigen (absent), so its plain-C restatement in oracle/ runs, with the C library's FP64 "
@@ -757,6 +851,7 @@ def run_reference(args, rank, world):
                                    "distribution per thread per step", "threads": threads},
             "impl": "reference",
             "cpu_baseline": {"value": round(v, 5), "unit": "Gsamples/s", "cores": threads, "kind": "port",
+                             "cpu": host_cpu(),
                              "sample": f"2^16 samples per distribution per thread per step, {threads} threads, "
                                        "one Vmt19937_64(1234+4k) per thread; the reference needs Eigen (absent), "
                                        "so its restatement in oracle/ runs"},
@@ -862,6 +957,7 @@ def main():
     ap.add_argument("--case", default=None,
                     help="run one named small workload instead (uniform_f32, uniform_f32_big, mvnormal_dD, multinomial, wishart_d32, "
                          "beta_f32, beta_f64, poisson4, gamma_compat), for profiler captures")
+    ap.add_argument("--no-compat", action="store_true", help="skip the single-engine sweep (the 'compat' key)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, multivariate and serving workloads (extra keys of the JSON line)")
     args = ap.parse_args()
