@@ -104,7 +104,9 @@ gr_status gr_engine_seed(gr_engine* e, uint64_t seed, gr_stream_t stream);
 size_t gr_engine_state_size(const gr_engine* e);
 gr_status gr_engine_save(const gr_engine* e, void* host_buf, size_t size, gr_stream_t stream);
 gr_status gr_engine_restore(gr_engine* e, const void* host_buf, size_t size, gr_stream_t stream);
-/* MersenneTwister::discard(num) (:317-323) — num packets, O(num). */
+/* MersenneTwister::discard(num) (:317-323) — num packets.  Long discards
+ * jump ahead (x^num mod the characteristic polynomial applied to the lane
+ * windows), so the cost does not grow with num. */
 gr_status gr_engine_discard(gr_engine* e, uint64_t npackets, gr_stream_t stream);
 /* Waits for the engine's stream work and folds device error words. */
 gr_status gr_engine_sync(gr_engine* e, gr_stream_t stream);
@@ -377,11 +379,15 @@ const char* gr_version(void);
  * for example a plugin whose host framework owns all device memory, or a
  * thread with a real-time budget.  The engine is created once at set-up
  * (streams = 1 only); the call then allocates nothing: its jump-ahead scratch
- * is a file-scope __device__ array of about 1 MiB that every GPU loading the
+ * and the jump polynomials of every segment length it can use are a
+ * file-scope __device__ array of about 1.9 MiB that every GPU loading the
  * library keeps until process exit.  n <= GR_NOALLOC_MAX_DRAWS, else
- * GR_ERR_INVALID.  Calls share that array, so calls that overlap on the GPU
- * race and must be serialised by the caller.  The first call on a device
- * performs one-time set-up; make it before any stream capture. */
+ * GR_ERR_INVALID; a call runs as at most 32 jump-ahead segments.  Calls share
+ * that array, so calls that overlap on the GPU race and must be serialised by
+ * the caller.  The first call on a device performs one-time set-up with that
+ * device current (the array's address, the kernels' code, the jump
+ * polynomials computed on the host and copied in synchronously); make it
+ * before any stream capture. */
 #define GR_NOALLOC_MAX_DRAWS 4294967296ull
 gr_status gr_raw_u64_noalloc(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stream);
 
