@@ -99,6 +99,7 @@ struct gr_engine {
   size_t segwin_words = 0;
   CallSnap* snap = nullptr;
   GenState* scratch_gen = nullptr;  // caches of temporary generators (gr_sample)
+  uint64_t* tailw = nullptr;        // draws of a call's partial last packet
 };
 
 struct gr_gen {
@@ -173,6 +174,7 @@ gr_status gr_engine_destroy(gr_engine* e) {
   cudaFree(e->segwin);
   cudaFree(e->snap);
   cudaFree(e->scratch_gen);
+  cudaFree(e->tailw);
   delete e;
   return GR_OK;
 }
@@ -625,7 +627,98 @@ double reject_yield(int rk, const DistParams& d) {
   return q;
 }
 
+// Expected half packets one PoissonGen packetOp consumes (the longest of
+// its four lanes' multiplicative loops, threshold fe = exp(-mean) in float),
+// estimated once per threshold on the host from 4096 simulated packets.  Used
+// only to plan how many segments a long call covers; the result does not
+// depend on it.
+// The engine blocks a rejection or walk kernel may generate in one call
+// (its iteration cap).  GR_MAX_BLOCKS (tests) lowers the cap so that a call
+// runs into it: the kernel stops, records GR_DEV_REJECT_LIMIT in the engine's
+// status word and returns, and gr_engine_sync reports GR_ERR_REJECT_LIMIT.
+int64_t block_cap(int64_t planned) {
+  const char* v = std::getenv("GR_MAX_BLOCKS");
+  if (!v) return planned;
+  const long long c = std::atoll(v);
+  return c > 0 ? std::min<int64_t>(planned, (int64_t)c) : planned;
+}
+
+double poisson_step_halves(float fe) {
+  static std::mutex mu;
+  static std::map<float, double> cache;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(fe);
+    if (it != cache.end()) return it->second;
+  }
+  std::mt19937_64 rng(0x5eed);
+  auto u = [&]() { return (float)((double)(rng() >> 40) * (1.0 / 16777216.0)); };
+  const int N = 4096;
+  double tot = 0;
+  for (int i = 0; i < N; ++i) {
+    int L = 0;
+    for (int j = 0; j < 4; ++j) {
+      float v = 1.0f;
+      int it = 0;
+      do {
+        v *= u();
+        ++it;
+      } while (fe < v && it < 64);
+      L = std::max(L, it);
+    }
+    tot += L;
+  }
+  const double m = tot / N;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[fe] = m;
+  return m;
+}
+
+gr_status run_packets(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream);
+
+// The n % P elements after the last whole packet of a call: the scalar
+// operator(), one engine packet each, drawn from the last stream (whose slice
+// they extend), its first 64-bit lane transformed by launch_tail.
+gr_status run_tail(gr_engine* e, const DistParams& dp, void* out, int r, cudaStream_t stream) {
+  if (!e->tailw) GR_CUDA(cudaMalloc(&e->tailw, sizeof(uint64_t) * 8));
+  DistParams rp{};
+  rp.kind = kRawLane0Kind;
+  rp.dtype = GR_U64;
+  Plan p{};
+  p.eng = e->st + (e->K - 1);
+  p.K = 1;
+  p.S = 1;
+  p.J = r;
+  p.gran = 4;  // four (virtual) outputs per packet: one draw
+  p.gran_per_k = r;
+  p.out = e->tailw;
+  cudaError_t err = launch_direct(p, rp, nullptr, stream);
+  if (err == cudaSuccess) err = launch_tail(e->tailw, out, r, dp, true, stream);
+  if (err != cudaSuccess) return cuda_fail(err, "scalar tail");
+  return GR_OK;
+}
+
 gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream) {
+  const int gran = kind_granule(dp.kind, dp.dtype);
+  const int r = (int)(n % (size_t)gran);
+  if (r == 0) return run_packets(e, g, dp, out, n, stream);
+  if (!kind_has_exact_tail(dp.kind, dp.dtype)) {
+    return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(gran) +
+                                    " (the reference packet width for this type); a partial last packet is "
+                                    "supported for uniformReal, balanced, bernoulli and randBits, whose scalar "
+                                    "form is exact");
+  }
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  const size_t whole = n - (size_t)r;
+  if (whole) {
+    gr_status st = run_packets(e, g, dp, out, whole, stream);
+    if (st != GR_OK) return st;
+  }
+  const size_t es = dp.dtype == GR_F64 ? 8 : 4;
+  return run_tail(e, dp, static_cast<char*>(out) + whole * es, r, stream);
+}
+
+gr_status run_packets(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream) {
   const int gran = kind_granule(dp.kind, dp.dtype);
   if (n % (size_t)gran) {
     return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(gran) +
@@ -676,7 +769,7 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
     const int rk = reject_code(dp);
     const int64_t wt = rk == 0 ? 24 : (rk >= 3 ? 8 : 16);  // words per trial
     const int64_t npk = nk_max / P;
-    const int64_t max_blocks = ((16 * npk + 4096) * wt) / (kN * 8) + 64;
+    const int64_t max_blocks = block_cap(((16 * npk + 4096) * wt) / (kN * 8) + 64);
     if (e->K < 16 && npk >= ((int64_t)1 << 12)) {
       // long call on few engines: jump-ahead segments over the trial stream
       const double q = reject_yield(rk, dp);
@@ -737,7 +830,38 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
       wd.fe = dp.kind == GR_POISSON ? (float)std::exp(-dp.da) : dp.fe;
       wd.ia = dp.kind == GR_BINOMIAL ? dp.ia : 0;
       wd.ic = dp.kind == GR_BINOMIAL ? dp.ib : 0;
-      max_blocks = (npk * 64) / (2 * kN) + 64;
+      max_blocks = block_cap((npk * 64) / (2 * kN) + 64);
+      if (e->K < 16 && npk >= ((int64_t)1 << 14)) {
+        // long call on few engines: the step chain over jump-ahead segments
+        const int64_t J = (int64_t)1 << 15;
+        const double hl = poisson_step_halves(wd.fe);
+        // GR_WALK_PLAN_SCALE (tests) scales the planned packets: below 1 the
+        // last segment runs on past its plan, above 1 the call ends in an
+        // earlier segment; the result is the same
+        const char* sc = std::getenv("GR_WALK_PLAN_SCALE");
+        const double scale = sc ? std::max(0.0, std::atof(sc)) : 1.0;
+        const int64_t need = (int64_t)std::ceil((double)npk * hl * 0.5 * 1.03 * scale) + 64;
+        const int S = (int)std::max<int64_t>(2, (need + J - 1) / J);
+        gr_status st = prepare_segments(e, p, S, J, 0, stream);
+        if (st != GR_OK) return st;
+        PwArgs a{};
+        a.J = J;
+        a.snap = e->snap;
+        a.words_per_seg = (2 * J + 1) / 32 + 2;
+        a.max_blocks = max_blocks;
+        const size_t KS = (size_t)e->K * S;
+        const size_t bytes = KS * (4 * 4 + kPwEntries * 2 * 4 + 3 * 8 + (size_t)a.words_per_seg * 4);
+        char* buf = nullptr;
+        GR_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, stream));
+        a.plan = reinterpret_cast<int64_t*>(buf);
+        a.info = reinterpret_cast<int32_t*>(buf + KS * 3 * 8);
+        a.ent = a.info + KS * 4;
+        a.bits = reinterpret_cast<uint32_t*>(a.ent + KS * kPwEntries * 2);
+        cudaError_t err = launch_poisson_segmented(p, wd, a, stream);
+        cudaFreeAsync(buf, stream);
+        if (err != cudaSuccess) return cuda_fail(err, "segmented Poisson kernels");
+        return GR_OK;
+      }
     } else {
       const bool f32 = dp.dtype == GR_F32;
       wd.ia = gamma_branch(dp.da, f32);
@@ -746,6 +870,7 @@ gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, siz
       wd.fb = (float)dp.db;
       max_blocks = (npk * 64) / kN + 64;
     }
+    max_blocks = block_cap(max_blocks);
     cudaError_t err = launch_walk(p, wd, max_blocks, stream);
     if (err != cudaSuccess) return cuda_fail(err, "walk sampling kernel");
     return GR_OK;
@@ -1927,19 +2052,29 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
                                     "randBits), gamma, chiSquared, studentT, poisson, binomial, negativeBinomial, uniformInt, geometric "
                                     "and discrete");
-  const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
-  if (n % (size_t)P) return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width");
+  const int64_t P = kind_granule(dp.kind, dp.dtype);
+  // a partial last packet: the scalar operator(), one draw per element (the
+  // kinds whose scalar form is exact bit arithmetic)
+  const int64_t r = (int64_t)(n % (size_t)P);
+  if (r && !kind_has_exact_tail(dp.kind, dp.dtype))
+    return fail(GR_ERR_INVALID, "size must be a multiple of the reference packet width; a partial last packet is "
+                                "supported for uniformReal, balanced, bernoulli and randBits");
   if (n == 0) return GR_OK;
   if (!dev_out) return fail(GR_ERR_INVALID, "output is NULL");
   const int64_t npk = (int64_t)n / P;
   const bool unit2 = dp.kind == GR_NORMAL_STD || dp.kind == GR_NORMAL || dp.kind == GR_LOGNORMAL;
   const int64_t W = wpp * (unit2 ? 2 * ((npk + 1) / 2) : npk);  // a normal unit draws both packets
   uint64_t* w = nullptr;
-  GR_CUDA(cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)W, s));
-  st = sengine_words(se, w, W, s);
-  if (st == GR_OK) {
+  GR_CUDA(cudaMallocAsync(&w, sizeof(uint64_t) * (size_t)(W + r), s));
+  st = sengine_words(se, w, W + r, s);
+  if (st == GR_OK && npk) {
     const cudaError_t err = launch_scalar_xform(w, dev_out, npk, dp, s);
     if (err != cudaSuccess) st = cuda_fail(err, "scalar-engine sampling kernel");
+  }
+  if (st == GR_OK && r) {
+    const size_t es = dp.dtype == GR_F64 ? 8 : 4;
+    const cudaError_t err = launch_tail(w + W, static_cast<char*>(dev_out) + (size_t)npk * P * es, (int)r, dp, false, s);
+    if (err != cudaSuccess) st = cuda_fail(err, "scalar-engine tail");
   }
   cudaFreeAsync(w, s);
   return st;

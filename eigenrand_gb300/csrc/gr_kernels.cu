@@ -718,6 +718,83 @@ cudaError_t preload_raw_stream_kernels() {
   return e;
 }
 
+// ---------------------------------------------------------------- scalar tails
+// A size that is not a whole number of packets ends with n % P elements made
+// by the generator's scalar operator() (Eigen's linear vectorised assignment
+// loop: packets up to the last whole one, then scalars).  Each takes one draw:
+// the first 64-bit lane of an engine packet (pfirst of the packet), or one
+// draw of a scalar engine.  Exact bit arithmetic for these kinds:
+// randBits (Basic.h:386-391), balanced (:416-420), balanced(a, b)
+// (:456-460), uniformReal (:533-540, ExtractFirstUint :345-371),
+// uniformReal(min, max) (:620-624), bernoulli (:689-693).
+bool kind_has_exact_tail(int kind, int dtype) {
+  switch (kind) {
+    case GR_UNIFORM_REAL:
+    case GR_UNIFORM_REAL2:
+    case GR_BALANCED:
+    case GR_BALANCED2:
+      return dtype == GR_F32 || dtype == GR_F64;
+    case GR_BERNOULLI:
+      return true;
+    case GR_RANDBITS:
+      return dtype == GR_I32;
+    default:
+      return false;
+  }
+}
+
+__global__ void k_tail(const uint64_t* w, void* out, int n, DistParams d, int packet_engine) {
+  const int i = threadIdx.x;
+  if (i >= n) return;
+  const uint64_t r = w[i];
+  const uint32_t lo = (uint32_t)r;
+  // pfirst of an engine packet is its first 32-bit word; of a scalar engine's
+  // draw, the whole 64-bit value
+  const uint64_t first = packet_engine ? (uint64_t)(int64_t)(int32_t)lo : r;
+  const bool f64 = d.dtype == GR_F64;
+  switch (d.kind) {
+    case GR_UNIFORM_REAL:
+      // ExtractFirstUint: the first 32-bit word (float), the first 64-bit lane (double)
+      if (f64) reinterpret_cast<double*>(out)[i] = ur_d(r);
+      else reinterpret_cast<float*>(out)[i] = ur_f(lo);
+      break;
+    case GR_UNIFORM_REAL2:  // bias + to_ur(pfirst(rng())) * slope
+      if (f64) reinterpret_cast<double*>(out)[i] = d.db + ur_d(first) * d.da;
+      else reinterpret_cast<float*>(out)[i] = d.fb + ur_f(lo) * d.fa;
+      break;
+    case GR_BALANCED:
+    case GR_BALANCED2: {
+      const uint32_t k = lo & 0x7fffffffu;
+      if (f64) {
+        const double z = div_2p31m1(k);
+        reinterpret_cast<double*>(out)[i] = d.kind == GR_BALANCED ? z * 2.0 - 1.0 : z * d.da + d.db;
+      } else {
+        const float z = (float)(int32_t)k / (float)0x7FFFFFFF;
+        reinterpret_cast<float*>(out)[i] = d.kind == GR_BALANCED ? z * 2.0f - 1.0f : z * d.fa + d.fb;
+      }
+      break;
+    }
+    case GR_BERNOULLI: {
+      const int v = ((int32_t)(lo & 0x7fffffffu) < d.ia) ? 1 : 0;
+      if (d.dtype == GR_I32) reinterpret_cast<int32_t*>(out)[i] = v;
+      else if (f64) reinterpret_cast<double*>(out)[i] = v;
+      else reinterpret_cast<float*>(out)[i] = (float)v;
+      break;
+    }
+    case GR_RANDBITS:
+      reinterpret_cast<int32_t*>(out)[i] = (int32_t)lo;
+      break;
+    default:
+      break;
+  }
+}
+
+cudaError_t launch_tail(const uint64_t* w, void* out, int n, const DistParams& d, bool packet_engine, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_tail<<<1, 32, 0, s>>>(w, out, n, d, packet_engine ? 1 : 0);
+  return cudaGetLastError();
+}
+
 int kind_granule(int kind, int dtype) {
   if (kind == kRawKind || kind == kRawLane0Kind) return 4;
   if (dtype == GR_F32) return 8;

@@ -108,6 +108,23 @@ struct RsArgs {
 cudaError_t launch_reject_segmented(const Plan& p, const DistParams& d, int rk, const CallSnap* snap, const RsArgs& a,
                                     int64_t gather_n, cudaStream_t s);
 
+// PoissonGen (mean < 12) / BinomialGen (mean < 1) on few engines over S
+// jump-ahead segments of J packets per engine (gr_samplers.cu): a scan per
+// segment, a plan per engine, a write per segment.  Scratch per engine and
+// segment; bits: words_per_seg bitmap words per segment.
+constexpr int kPwEntries = 64;  // entry offsets into a segment (the step look-ahead)
+struct PwArgs {
+  int64_t J;                // packets per segment
+  const CallSnap* snap;     // caches at call start, per engine
+  int32_t* info;            // [K*S][4]: exit offset, steps, every entry merged, unused
+  int32_t* ent;             // [K*S][kPwEntries][2]: steps, exit offset
+  int64_t* plan;            // [K*S][3]: entry offset, first output packet, steps
+  uint32_t* bits;           // [K*S][words_per_seg]
+  int64_t words_per_seg;
+  int64_t max_blocks;       // blocks the last segment of an engine may run to
+};
+cudaError_t launch_poisson_segmented(const Plan& p, const DistParams& d, const PwArgs& a, cudaStream_t s);
+
 // Data-dependent consumption (gr_samplers.cu), one CTA per stream: k_poisson
 // for PoissonGen mean < 12 and BinomialGen mean < 1 (int32), k_beta for
 // BetaGen with a or b >= 1 (f32/f64; d.ia / d.ib hold (gamma branch << 8) |
@@ -187,6 +204,12 @@ cudaError_t launch_vop(int kind, int threads, const VopArgs& va, cudaStream_t s)
 
 // Outputs per granule: the smallest output count a call (or a stream slice)
 // may have for the kind.  Packets per unit: 2 for the Box-Muller kinds.
+// The scalar operator() tail of a size that is not a whole number of packets
+// (gr_kernels.cu): kinds whose scalar form is exact bit arithmetic on one
+// draw, and the kernel that applies it to n < P draws w (engine packets'
+// first 64-bit lanes, or a scalar engine's draws).
+bool kind_has_exact_tail(int kind, int dtype);
+cudaError_t launch_tail(const uint64_t* w, void* out, int n, const DistParams& d, bool packet_engine, cudaStream_t s);
 int kind_granule(int kind, int dtype);
 int kind_packets_per_unit(int kind, int dtype);
 bool kind_is_direct(int kind, int dtype, const DistParams& d);

@@ -1451,6 +1451,356 @@ static cudaError_t run_poisson(const Plan& p, const DistParams& d, int64_t max_b
 }
 
 // ===========================================================================
+// PoissonGen (mean < 12) and BinomialGen (mean < 1) on few engines over
+// jump-ahead segments.  The steps x -> x + L(x) of one engine form a chain
+// that a single CTA would have to follow from start to end; here segment s of
+// engine k (fresh packets [sJ, (s+1)J)) runs on its own CTA, in three
+// launches:
+//   scan   follows a speculative chain from the segment's first position,
+//          marking its step starts in a bitmap, and the chains from each of
+//          the other kPwEntries - 1 positions where the true chain can enter
+//          the segment (the previous segment's last step overshoots its end
+//          by less than kPoisLook) until they meet the marked chain; records,
+//          per entry offset, the steps the chain takes in the segment and the
+//          offset at which it leaves it;
+//   plan   (one CTA per engine) chains the entry offsets from segment to
+//          segment and turns the step counts into output offsets;
+//   write  follows its segment's true chain and writes its steps at their
+//          offsets; the segment holding the call's last step leaves the
+//          engine state, and an engine's last segment runs on past its end
+//          when the planned segments hold too few steps.
+// A step depends only on its start position, so two chains that meet share
+// every later step: the outputs equal the single-CTA walk's, bit for bit.
+// ===========================================================================
+template <int MODE>  // 0 scan, 1 write
+__global__ void __launch_bounds__(kPoisThreads) k_pw(Plan p, DistParams d, PwArgs a) {
+  extern __shared__ __align__(16) uint64_t pois_dyn[];
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(pois_dyn);
+  float(*uf)[kN][8] = reinterpret_cast<float(*)[kN][8]>(pois_dyn + 3 * kLanes * kN);
+  uint32_t* pos = reinterpret_cast<uint32_t*>(pois_dyn + 3 * kLanes * kN + kN * 8);
+  uint16_t* rec = reinterpret_cast<uint16_t*>(pos + kPoisRing);
+  __shared__ int s_nrec, s_stop, s_err, s_walkers, s_cnt0;
+  __shared__ int64_t s_ebase, s_end, s_x0;
+  __shared__ float4 s_cache;
+  const int S = p.S;
+  const int k = blockIdx.x / S, sg = blockIdx.x % S;
+  const int tid = threadIdx.x;
+  EngState* st = p.eng + k;
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  const int64_t Npk = n / 4;
+  const int c = a.snap[k].half_valid ? 1 : 0;  // position 0 is the engine's cached half packet
+  const int c0w = 4 * c;
+  const int64_t pk0 = (int64_t)sg * a.J;  // first fresh packet of the segment
+  const int64_t seg_lo = sg == 0 ? 0 : 2 * pk0 + c;
+  const int64_t seg_hi = 2 * (pk0 + a.J) + c;
+  const bool lastseg = sg == S - 1;
+  const size_t sidx = (size_t)k * S + sg;
+  int64_t start = seg_lo, O = 0, nsteps = INT64_MAX;
+  if (MODE == 1) {
+    start = seg_lo + a.plan[sidx * 3 + 0];
+    O = a.plan[sidx * 3 + 1];
+    if (!lastseg) nsteps = a.plan[sidx * 3 + 2];
+    if (O >= Npk) return;  // the call ends in an earlier segment
+  }
+  // lane windows: segment 0 from the call-start copy, the others from the jumps
+  if (sg == 0) load_window(raw[0], p.prefix + (size_t)k * kLanes * kPrefixLen, kPrefixLen);
+  else load_window(raw[0], p.segwin + ((size_t)k * (S - 1) + (sg - 1)) * kLanes * kN, kN);
+  if (tid == 0) {
+    s_err = 0;
+    s_stop = 0;
+    s_walkers = (MODE == 0 && sg > 0) ? kPwEntries - 1 : 0;
+    const uint32_t* hc = a.snap[k].half_cache;
+    s_cache = make_float4(ur_f(hc[0]), ur_f(hc[1]), ur_f(hc[2]), ur_f(hc[3]));
+  }
+  __syncthreads();
+  uint32_t* bits = a.bits + sidx * (size_t)a.words_per_seg;
+  const int64_t max_blocks = lastseg ? a.max_blocks : (2 * a.J + 4 * kPoisLook) / (2 * kN) + 3;
+  // chain of thread 0 (the speculative chain, or the true one); scan-mode
+  // walkers: thread t in [1, kPwEntries) follows the chain entering at seg_lo + t
+  int64_t x0 = start, E = 0;
+  int32_t cnt0 = 0;
+  int64_t bw = -1;  // bitmap word held by thread 0
+  uint32_t bv = 0;
+  int64_t xt = seg_lo + tid, mt = 0;
+  int32_t nt = 0;
+  int wstate = (MODE == 0 && sg > 0 && tid >= 1 && tid < kPwEntries) ? 1 : 0;  // 1 active, 2 met, 3 left
+  int64_t done_pos = start;
+  int cur = 0;
+  int64_t nb = 0;
+  for (; nb < max_blocks; ++nb) {
+    const int slot = (int)(nb & 1);
+    const int nxt = cur == 2 ? 0 : cur + 1;
+    mt_block(raw[cur], raw[nxt], [&](int i, const uint64_t* pk) {
+#pragma unroll
+      for (int l = 0; l < kLanes; ++l) {
+        uf[slot][i][2 * l] = ur_f((uint32_t)pk[l]);
+        uf[slot][i][2 * l + 1] = ur_f((uint32_t)(pk[l] >> 32));
+      }
+    });
+    cur = nxt;
+    const int64_t lim = c + 2 * pk0 + 2 * (nb + 1) * kN - kPoisLook;
+    if (tid == 0 && lim - x0 > kPoisRing) s_err = 1;  // positions still needed would leave the ring
+    // ---- steps of the new start positions (as in k_poisson)
+    for (int64_t x = done_pos + tid; x < lim; x += kPoisThreads) {
+      const bool cached = 4 * x < c0w;
+      int w = (int)(4 * (x - c - 2 * pk0) - 8 * nb * (int64_t)kN);
+      float val[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+      int kk[4] = {0, 0, 0, 0};
+      int L = 0;
+      bool any = true;
+      for (int it = 0; it < kPoisLook && any; ++it, w += 4) {
+        float4 u;
+        if (it == 0 && cached) {
+          u = s_cache;
+        } else {
+          int pkk = w >> 3, sl = slot;
+          if (pkk < 0) {
+            pkk += kN;
+            sl ^= 1;
+          }
+          u = *reinterpret_cast<const float4*>(&uf[sl][pkk][w & 7]);
+        }
+        const float uu[4] = {u.x, u.y, u.z, u.w};
+        any = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          val[j] = val[j] * uu[j];
+          const bool cc = d.fe < val[j];
+          kk[j] += cc ? 1 : 0;
+          any |= cc;
+        }
+        L = it + 1;
+      }
+      if (any) atomicOr(&s_err, 1);
+      pos[(int)(x & (kPoisRing - 1))] =
+          ((uint32_t)L << 24) | (uint32_t)kk[0] | ((uint32_t)kk[1] << 6) | ((uint32_t)kk[2] << 12) | ((uint32_t)kk[3] << 18);
+    }
+    done_pos = max(done_pos, lim);
+    __syncthreads();
+    if (MODE == 0) {
+      // ---- the speculative chain (thread 0), its step starts marked
+      if (tid == 0) {
+        while (x0 < done_pos && x0 < seg_hi) {
+          const int64_t r = x0 - seg_lo;
+          if ((r >> 5) != bw) {
+            if (bw >= 0) bits[bw] = bv;
+            for (int64_t q = bw + 1; q < (r >> 5); ++q) bits[q] = 0u;
+            bw = r >> 5;
+            bv = 0;
+          }
+          bv |= 1u << (r & 31);
+          ++cnt0;
+          x0 += pos[(int)(x0 & (kPoisRing - 1))] >> 24;
+        }
+        if (bw >= 0) bits[bw] = bv;
+        s_x0 = x0;
+        if (x0 >= seg_hi && s_walkers == 0) s_stop = 1;
+      }
+      __syncthreads();
+      // ---- walkers: until they meet the marked chain or leave the segment
+      if (wstate == 1) {
+        const int64_t xs = s_x0;
+        while (xt < done_pos) {
+          if (xt >= seg_hi) {
+            wstate = 3;
+            break;
+          }
+          const int64_t r = xt - seg_lo;
+          if (xt == xs || (xt < xs && ((bits[r >> 5] >> (r & 31)) & 1u))) {
+            wstate = 2;
+            mt = xt;
+            break;
+          }
+          ++nt;
+          xt += pos[(int)(xt & (kPoisRing - 1))] >> 24;
+        }
+        if (wstate != 1) atomicSub(&s_walkers, 1);
+      }
+      __syncthreads();
+      if (tid == 0 && s_x0 >= seg_hi && s_walkers == 0) s_stop = 1;
+      __syncthreads();
+    } else {
+      // ---- the true chain (thread 0), as k_poisson's walk
+      if (tid == 0) {
+        s_ebase = E;
+        int nrec = 0;
+        const int64_t want = min(nsteps, Npk - O);
+        while (x0 < done_pos && E < want && nrec < kPoisRec) {
+          const int ri = (int)(x0 & (kPoisRing - 1));
+          rec[nrec++] = (uint16_t)ri;
+          x0 += pos[ri] >> 24;
+          ++E;
+        }
+        s_nrec = nrec;
+        if (E >= want) {
+          s_stop = (O + E >= Npk) ? 1 : 2;  // 1: the call ends here
+          s_end = x0;
+        }
+      }
+      __syncthreads();
+      const int nrec = s_nrec;
+      const int64_t e_first = O + s_ebase;
+      for (int e = tid; e < nrec * 4; e += kPoisThreads) {
+        const int i = e >> 2, j = e & 3;
+        int32_t v = (int32_t)((pos[rec[i]] >> (6 * j)) & 63);
+        if (d.ic) v = d.ia - v;  // BinomialGen: trials - res when p > 1/2
+        reinterpret_cast<int32_t*>(p.out)[off + (e_first + i) * 4 + j] = v;
+      }
+      __syncthreads();
+    }
+    if (s_stop || s_err) break;
+  }
+  if (MODE == 0) {
+    if (tid == 0 && (!s_stop || s_err)) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+    const int64_t xs = s_x0;
+    if (tid == 0) {
+      s_cnt0 = cnt0;  // the chain's steps, for the walkers' counts below
+      int32_t* info = a.info + sidx * 4;
+      info[0] = (int32_t)(xs - seg_hi);
+      info[1] = cnt0;
+      info[2] = 1;  // every entry met the chain (cleared below otherwise)
+      int32_t* en = a.ent + sidx * kPwEntries * 2;
+      en[0] = cnt0;
+      en[1] = (int32_t)(xs - seg_hi);
+    }
+    __syncthreads();
+    if (wstate == 2) {
+      // steps of the marked chain before the meeting point
+      const int64_t r = mt - seg_lo;
+      int32_t rank = 0;
+      for (int64_t q = 0; q < (r >> 5); ++q) rank += __popc(bits[q]);
+      rank += __popc(bits[r >> 5] & ((1u << (r & 31)) - 1u));
+      int32_t* en = a.ent + (sidx * kPwEntries + tid) * 2;
+      en[0] = nt + s_cnt0 - rank;
+      en[1] = (int32_t)(xs - seg_hi);
+    } else if (wstate == 3 || wstate == 1) {
+      int32_t* en = a.ent + (sidx * kPwEntries + tid) * 2;
+      en[0] = nt;
+      en[1] = (int32_t)(xt - seg_hi);
+      a.info[sidx * 4 + 2] = 0;
+    }
+    return;
+  }
+  // ---- write mode: the engine state, from the segment that ends the call
+  if (tid == 0 && (s_stop == 0 || s_err)) {
+    // an engine's last segment ran out of blocks, or a step was too long
+    atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+  }
+  __syncthreads();
+  if (s_stop != 1) return;
+  const int64_t fresh = s_end - c;    // half packets drawn fresh, from the call start
+  const int64_t np = (fresh + 1) / 2;  // packets consumed
+  const int64_t lp = np - pk0;          // ... of this segment's blocks
+  const int prv = cur == 0 ? 2 : cur - 1, prv2 = prv == 0 ? 2 : prv - 1;
+  const int64_t nblk = min(nb + 1, max_blocks);
+  if (lp > 0) {
+    const int64_t lastb = (lp - 1) / kN;
+    const int64_t rr = lp - lastb * kN;
+    if (lastb == nblk - 1) store_window(st, raw[cur], raw[prv], (int)rr);
+    else if (lastb == nblk - 2) store_window(st, raw[prv], raw[prv2], (int)rr);
+    else if (tid == 0) atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+  } else if (tid == 0) {
+    atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+  }
+  if (tid == 0) {
+    if (fresh & 1) {  // the last packet's upper half stays in the engine's half cache
+      const int64_t pl = lp - 1;
+      const int buf = (pl / kN == nblk - 1) ? cur : prv;
+      const uint64_t aa = mt_temper(raw[buf][2][pl % kN]), bb = mt_temper(raw[buf][3][pl % kN]);
+      st->half_cache[0] = (uint32_t)aa;
+      st->half_cache[1] = (uint32_t)(aa >> 32);
+      st->half_cache[2] = (uint32_t)bb;
+      st->half_cache[3] = (uint32_t)(bb >> 32);
+      st->half_valid = 1;
+    } else {
+      st->half_valid = 0;
+    }
+    st->consumed += (uint64_t)max(np, (int64_t)0);
+  }
+}
+
+// One CTA per engine: entry offsets chained from segment to segment, output
+// offsets from the step counts.
+__global__ void __launch_bounds__(1024) k_pw_plan(Plan p, PwArgs a) {
+  __shared__ int32_t s_tot[32];
+  __shared__ int64_t s_carry;
+  const int S = p.S, k = blockIdx.x, tid = threadIdx.x;
+  const size_t base = (size_t)k * S;
+  // entry offsets: known where the previous segment's entries all met
+  for (int sg = tid; sg < S; sg += blockDim.x) {
+    int64_t dv = -1;
+    if (sg == 0) dv = 0;
+    else if (a.info[(base + sg - 1) * 4 + 2]) dv = a.info[(base + sg - 1) * 4 + 0];
+    a.plan[(base + sg) * 3 + 0] = dv;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int sg = 1; sg < S; ++sg) {
+      if (a.plan[(base + sg) * 3 + 0] >= 0) continue;
+      const int64_t dp = a.plan[(base + sg - 1) * 3 + 0];
+      a.plan[(base + sg) * 3 + 0] = a.ent[((base + sg - 1) * kPwEntries + dp) * 2 + 1];
+    }
+    s_carry = 0;
+  }
+  __syncthreads();
+  // steps per segment, then their exclusive prefix sums
+  for (int b0 = 0; b0 < S; b0 += blockDim.x) {
+    const int sg = b0 + tid;
+    int32_t v = 0;
+    if (sg < S) {
+      int64_t dv = a.plan[(base + sg) * 3 + 0];
+      if (dv < 0 || dv >= kPwEntries) dv = 0;  // unreachable: offsets stay below kPoisLook
+      v = a.ent[((base + sg) * kPwEntries + dv) * 2 + 0];
+    }
+    // block-wide inclusive scan of v
+    int32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((tid & 31) >= o) x += y;
+    }
+    if ((tid & 31) == 31) s_tot[tid >> 5] = x;
+    __syncthreads();
+    if (tid < 32) {
+      int32_t t = s_tot[tid];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if (tid >= o) t += y;
+      }
+      s_tot[tid] = t;
+    }
+    __syncthreads();
+    const int64_t incl = s_carry + x + ((tid >> 5) ? s_tot[(tid >> 5) - 1] : 0);
+    if (sg < S) {
+      a.plan[(base + sg) * 3 + 1] = incl - v;
+      a.plan[(base + sg) * 3 + 2] = v;
+    }
+    __syncthreads();
+    if (tid == blockDim.x - 1) s_carry = incl;
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_poisson_segmented(const Plan& p, const DistParams& d, const PwArgs& a, cudaStream_t s) {
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k_pw<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPoisSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pw<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPoisSmem);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  k_pw<0><<<p.K * p.S, kPoisThreads, kPoisSmem, s>>>(p, d, a);
+  k_pw_plan<<<p.K, 1024, 0, s>>>(p, a);
+  k_pw<1><<<p.K * p.S, kPoisThreads, kPoisSmem, s>>>(p, d, a);
+  return cudaGetLastError();
+}
+
+// ===========================================================================
 // k_beta: BetaGen with a >= 1 or b >= 1 (NormalExp.h:970-975).  Each output
 // packet draws one packet from GammaGen(a), then one from GammaGen(b); a
 // component is closed form (alpha == 1: 1 packet; integer alpha < 20: alpha

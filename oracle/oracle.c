@@ -598,10 +598,73 @@ static void beta_pk(or_vmt* e, or_gen* g, or_gen* g2, or_gen* g3, int dbl, doubl
   *pp = p;
 }
 
+/* The scalar operator() that fills the elements after the last whole packet
+ * of a call (Eigen's linear vectorised assignment loop: packets, then scalars
+ * for the remainder).  One draw per element: pfirst of the engine's packet,
+ * or one draw of a scalar engine.  pfirst of a Packet8i is its first 32-bit
+ * word; ExtractFirstUint<double> (Basic.h:345-371) stores the packet and takes
+ * its first 64-bit element; pfirst of a scalar engine's uint64_t draw is the
+ * draw.  dtype: 0 float, 1 double, 2 int32.
+ *   randBits          pfirst(rng())                         Basic.h:386-391
+ *   balanced          ((T)((int32)pfirst & 0x7FFFFFFF) / 0x7FFFFFFF) * 2 - 1   :416-420
+ *   balanced(a, b)    ... * slope + bias                     :456-460
+ *   uniformReal       to_ur(ExtractFirstUint<T>(rng()))     :533-540
+ *   uniformReal(a, b) bias + to_ur(pfirst(rng())) * slope    :620-624
+ *   bernoulli         ((uint32)pfirst & 0x7FFFFFFF) < p ? 1 : 0   :689-693 */
+static void scalar_tail(or_vmt* e, int dist, int dtype, double a, double b, void* out, size_t n) {
+  for (size_t i = 0; i < n; ++i) {
+    uint64_t r;
+    int packet = 0;
+    if (g_src) {
+      r = src_next();
+    } else {
+      uint64_t pk[OR_MAXL];
+      vmt_packet(e, pk);
+      r = pk[0];
+      packet = 1;
+    }
+    const uint32_t lo = (uint32_t)r;
+    /* pfirst converted to uint64_t: a packet's first int32 word, sign-extended */
+    const uint64_t first = packet ? (uint64_t)(int64_t)(int32_t)lo : r;
+    if (dist == OR_UNIFORM) {
+      const int std_form = a == 0 && b == 1;
+      if (dtype == 1) {
+        const double u = bit_ur_d(std_form ? r : first);
+        ((double*)out)[i] = std_form ? u : a + u * (b - a);
+      } else {
+        const float fa = (float)a, fb = (float)b;
+        const float u = bit_ur_f(lo);
+        ((float*)out)[i] = std_form ? u : fa + u * (fb - fa);
+      }
+    } else if (dist == OR_BALANCED) {
+      const int std_form = a == -1 && b == 1;
+      const int32_t k = (int32_t)(lo & 0x7FFFFFFFu);
+      if (dtype == 1) {
+        const double z = (double)k / 2147483647.0;
+        ((double*)out)[i] = std_form ? z * 2 - 1 : z * (b - a) + a;
+      } else {
+        const float fa = (float)a, fb = (float)b;
+        const float z = (float)k / (float)0x7FFFFFFF;
+        ((float*)out)[i] = std_form ? z * 2 - 1 : z * (fb - fa) + fa;
+      }
+    } else if (dist == OR_BERNOULLI) {
+      const uint32_t pt = (uint32_t)(a * 2147483648.0);
+      const int v = ((lo & 0x7FFFFFFFu) < pt) ? 1 : 0;
+      if (dtype == 2) ((int32_t*)out)[i] = v;
+      else if (dtype == 1) ((double*)out)[i] = v;
+      else ((float*)out)[i] = (float)v;
+    } else { /* randBits */
+      ((int32_t*)out)[i] = (int32_t)lo;
+    }
+  }
+}
+
 int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n) {
   int dbl = dtype == 1;
   int P = P_of(dbl);
-  if (n % (size_t)P) return 2;
+  /* a partial last packet: the scalar operator() (kinds whose scalar form is exact) */
+  const size_t tail = n % (size_t)P;
+  if (tail && dist != OR_UNIFORM && dist != OR_BALANCED && dist != OR_BERNOULLI) return 2;
   if (e->L != 4) return 3; /* AVX2 profile only */
   float* of = (float*)out;
   double* od = (double*)out;
@@ -753,6 +816,10 @@ int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, v
     }
     if (dbl) memcpy(od + k * 4, p.d, 32);
     else memcpy(of + k * 8, p.f, 32);
+  }
+  if (tail) {
+    const size_t at = n - tail;
+    scalar_tail(e, dist, dbl, a, b, dbl ? (void*)(od + at) : (void*)(of + at), tail);
   }
   return 0;
 }
@@ -1260,12 +1327,13 @@ int or_gen_binomial(or_vmt* e, or_gen* g, int32_t trials, double p, int32_t* out
 /* RandbitsGen::packetOp<Packet4i>: RawbitsMaker<Packet4i,..>::rawbits =
  * rng.half(), Basic.h:393-399, arch/AVX/RandUtils.h:23-26 */
 int or_gen_randbits(or_vmt* e, int32_t* out, size_t n) {
-  if (n % 4 || e->L != 4) return 2;
+  if (e->L != 4) return 2;
   for (size_t k = 0; k < n / 4; ++k) {
     uint32_t w[4];
     draw_half(e, w);
     memcpy(out + 4 * k, w, 16);
   }
+  if (n % 4) scalar_tail(e, -1, 2, 0, 0, out + n / 4 * 4, n % 4);
   return 0;
 }
 
@@ -1273,13 +1341,14 @@ int or_gen_randbits(or_vmt* e, int32_t* out, size_t n) {
  * Packet4i = rng.half() (arch/AVX/RandUtils.h:23-26), (w & 0x7FFFFFFF)
  * compared signed with (int32)(uint32)(p * 2^31) (so p = 1 gives 0) */
 int or_gen_bernoulli_i32(or_vmt* e, double p, int32_t* out, size_t n) {
-  if (n % 4 || e->L != 4) return 2;
+  if (e->L != 4) return 2;
   const int32_t pt = (int32_t)(uint32_t)(p * 2147483648.0);
   for (size_t k = 0; k < n / 4; ++k) {
     uint32_t w[4];
     draw_half(e, w);
     for (int j = 0; j < 4; ++j) out[4 * k + j] = ((int32_t)(w[j] & 0x7fffffffu) < pt) ? 1 : 0;
   }
+  if (n % 4) scalar_tail(e, OR_BERNOULLI, 2, p, 0, out + n / 4 * 4, n % 4);
   return 0;
 }
 

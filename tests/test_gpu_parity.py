@@ -273,6 +273,36 @@ def test_walk_int_kinds_bit_exact(er, oracle, kind, a, t):
     assert_bits_equal(mem(o), oracle.generate(e, oracle.Gen(), "RANDBITS", 8, np.int32), "randbits after")
 
 
+@pytest.mark.parametrize("scale", [1.0, 0.5, 3.0])
+@pytest.mark.parametrize("kind,a,t", [("POISSON", 4.0, 0), ("POISSON", 11.5, 0), ("BINOMIAL", 0.004, 100),
+                                      ("BINOMIAL", 0.996, 200)])
+def test_walk_segmented_single_engine(er, oracle, monkeypatch, kind, a, t, scale):
+    """Long PoissonGen / BinomialGen (mean < 1) calls on one engine run as
+    jump-ahead segments (scan, plan, write).  Odd sizes leave the engine's
+    half cache set; a plan scale below 1 makes the last segment run on past
+    its plan, above 1 ends the call in an earlier segment."""
+    monkeypatch.setenv("GR_WALK_PLAN_SCALE", str(scale))
+    u = er.Vmt19937_64(77)
+    e = oracle.Engine(77)
+    g = er._Gen(torch.int32, a, 0.0, trials=t, kind=kind)
+    og = oracle.Gen()
+    for n in (4, (1 << 18) + 4, 1 << 20, 12, (1 << 16) + 4, 1 << 21):
+        got = mem(g.generate(n, 1, u))
+        ref = oracle.generate(e, og, kind, n, np.int32, a, 0.0, t)
+        assert_bits_equal(got, ref, f"{kind}({a},{t}) n={n} scale={scale}")
+    u.sync()
+    assert_bits_equal(er.raw_u64(u, 64).cpu().numpy().view(np.uint64), e.raw(16), "engine after segmented walk")
+
+
+def test_walk_segmented_three_streams(er, oracle):
+    K, per = 3, 4 * 300001
+    u = er.Vmt19937_64(88, streams=K)
+    x = mem(er.poisson(K * per, 1, u, 3.5))
+    for k in range(K):
+        ref = oracle.generate(oracle.Engine(88 + 4 * k), oracle.Gen(), "POISSON", per, np.int32, 3.5)
+        assert_bits_equal(x[k * per:(k + 1) * per], ref, f"poisson3.5 slice {k}")
+
+
 @pytest.mark.parametrize("a,b", [(0.5, 2.0), (2.0, 0.5), (1.0, 3.0), (2.5, 4.0), (0.3, 1.0), (22.0, 1.5)])
 @pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
 def test_beta_general_bit_exact(er, oracle, a, b, tdt):
@@ -552,9 +582,14 @@ def test_discrete_gen_cache(er, oracle, weights):
 
 # ---------------------------------------------------------------- errors
 def test_size_not_multiple_of_packet_is_rejected(er):
+    """A partial last packet goes through the generator's scalar operator();
+    kinds whose scalar form is not exact bit arithmetic refuse it (the
+    exact ones are in test_gpu_tail.py)."""
     u = er.Vmt19937_64(1)
     with pytest.raises(er.GrError):
-        er.uniformReal(5, 3, u)
+        er.normal(5, 3, u)
+    with pytest.raises(er.GrError):
+        er.gamma(3, 3, u, 0.5, 1.0)
 
 
 def test_nan_weight_sum_is_rejected(er):

@@ -424,3 +424,28 @@ def test_oracle_poisson_binomial_scalar_engine(oracle):
         s1.generate(None, "BINOMIAL", 12, np.int32, 0.4, trials=5)
         s2.raw(3 * 5 * 2)
         np.testing.assert_array_equal(s1.raw(4), s2.raw(4))
+
+
+def test_oracle_scalar_tail_from_raw_stream(oracle):
+    """The oracle's scalar operator() tail, restated from the raw stream in
+    numpy: after whole packets, each tail element takes one engine packet
+    and uses its first 32-bit word (balanced, uniformReal(min, max) float),
+    its first 64-bit lane (uniformReal double), or the first word
+    sign-extended to 64 bits (uniformReal(min, max) double: pfirst's int
+    converted to uint64_t)."""
+    import numpy as np
+    raw = oracle.Engine(42).raw(1 + 3)  # one whole packet, then three tail draws
+    lane0 = raw.reshape(-1, 4)[1:, 0]
+    lo = (lane0 & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    got = oracle.generate(oracle.Engine(42), oracle.Gen(), "BALANCED", 8 + 3, np.float32)
+    ref = (lo & np.uint32(0x7FFFFFFF)).astype(np.int32).astype(np.float32) / np.float32(2147483648.0) * 2 - 1
+    assert np.array_equal(got[8:].view(np.uint32), ref.astype(np.float32).view(np.uint32))
+    got = oracle.generate(oracle.Engine(42), oracle.Gen(), "UNIFORM_REAL", 4 + 3, np.float64)
+    raw = oracle.Engine(42).raw(1 + 3)
+    lane0 = raw.reshape(-1, 4)[1:, 0]
+    ref = ((lane0 & np.uint64(0xFFFFFFFFFFFFF)) | np.uint64(1023 << 52)).view(np.float64) - 1.0
+    assert np.array_equal(got[4:], ref)
+    got = oracle.generate(oracle.Engine(42), oracle.Gen(), "UNIFORM_REAL2", 4 + 3, np.float64, 0.5, 2.0)
+    sext = lo.astype(np.int32).astype(np.int64).view(np.uint64)
+    u = ((sext & np.uint64(0xFFFFFFFFFFFFF)) | np.uint64(1023 << 52)).view(np.float64) - 1.0
+    assert np.array_equal(got[4:], 0.5 + u * 1.5)
