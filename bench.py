@@ -316,21 +316,37 @@ def run_ours(args, rank, world):
     value = samples_per_step * args.steps * world / (ms / 1e3) / 1e9
 
     # e2e: the same sweep through the public API into host memory (pinned),
-    # D2H copy of every result inside the timed region
+    # D2H copy of every result inside the timed region.  The copies run on a
+    # second stream, each after its call's event, so call i + 1 samples while
+    # call i's result travels to the host; before a call rewrites a buffer it
+    # waits for the previous step's copy out of it.
     outs = sw.outs
     host = [torch.empty(N, dtype=o.dtype, pin_memory=True) for o in outs]
-    for i in range(len(items)):
-        sw.one(i)
-        host[i].copy_(outs[i], non_blocking=True)
+    cstream = torch.cuda.Stream()
+    done = [torch.cuda.Event() for _ in outs]
+    copied = [torch.cuda.Event() for _ in outs]
+
+    def e2e_step():
+        for i in range(len(items)):
+            stream.wait_event(copied[i])
+            sw.one(i)
+            done[i].record(stream)
+            cstream.wait_event(done[i])
+            with torch.cuda.stream(cstream):
+                host[i].copy_(outs[i], non_blocking=True)
+            copied[i].record(cstream)
+
+    for ev in copied:
+        ev.record(cstream)
+    e2e_step()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier()
     e0.record(stream)
     for _ in range(args.steps):
-        for i in range(len(items)):
-            sw.one(i)
-            host[i].copy_(outs[i], non_blocking=True)
+        e2e_step()
+    stream.wait_stream(cstream)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
