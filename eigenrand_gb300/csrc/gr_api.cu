@@ -90,6 +90,7 @@ gr_status get_jump_polys(int dev, int64_t J, int delta, int need, const uint64_t
 
 struct gr_engine {
   int K = 1;
+  int lanes = 4;  // 4: AVX2 profile (Packet8i); 2: SSE / NEON profile (Packet4i)
   int device = 0;
   uint64_t seed = 0;
   EngState* st = nullptr;
@@ -135,6 +136,11 @@ struct gr_sengine {
 
 namespace gr {
 EngState* engine_state_ptr(gr_engine* e) { return e ? e->st : nullptr; }
+gr_status need_four_lanes(const gr_engine* e, const char* what) {
+  if (e && e->lanes != kLanes)
+    return set_last_error(GR_ERR_UNSUPPORTED, std::string(what) + ": needs the 4-lane Vmt19937_64 (AVX2 profile)");
+  return GR_OK;
+}
 gr_status set_last_error(gr_status s, const std::string& msg) { return fail(s, msg); }
 }  // namespace gr
 
@@ -145,10 +151,12 @@ const char* gr_version(void) { return "gpurand 0.1 (sm_103a; EigenRand 0.6.0 AVX
 
 gr_status gr_engine_create(gr_engine** out, uint64_t seed, int32_t lanes, int32_t streams) {
   if (!out) return fail(GR_ERR_INVALID, "out is NULL");
-  if (lanes != kLanes) return fail(GR_ERR_UNSUPPORTED, "only the 4-lane Vmt19937_64 (AVX2 profile) is implemented");
+  if (lanes != kLanes && lanes != 2)
+    return fail(GR_ERR_UNSUPPORTED, "lanes must be 4 (AVX2 Vmt19937_64) or 2 (SSE / NEON Vmt19937_64)");
   if (streams < 1 || streams > (1 << 20)) return fail(GR_ERR_INVALID, "streams must be in [1, 2^20]");
   gr_engine* e = new gr_engine;
   e->K = streams;
+  e->lanes = lanes;
   e->seed = seed;
   cudaGetDevice(&e->device);
   cudaError_t err = cudaMalloc(&e->st, sizeof(EngState) * (size_t)streams);
@@ -217,6 +225,7 @@ gr_status gr_engine_sync(gr_engine* e, gr_stream_t stream) {
   if (any) {
     GR_CUDA(cudaMemset2D(&e->st[0].status, sizeof(EngState), 0, sizeof(int32_t), (size_t)e->K));
     if (any & GR_DEV_REJECT_LIMIT) return fail(GR_ERR_REJECT_LIMIT, "a rejection loop hit its iteration cap");
+    if (any & GR_DEV_MMA_TIMEOUT) return fail(GR_ERR_CUDA, "a tensor-core kernel timed out waiting for its products");
     return fail(GR_ERR_INVALID, "device reported invalid input");
   }
   return GR_OK;
@@ -698,7 +707,48 @@ gr_status run_tail(gr_engine* e, const DistParams& dp, void* out, int r, cudaStr
   return GR_OK;
 }
 
+// The 2-lane Vmt19937_64 (SSE / NEON profile, Pmt19937_64<Packet4i>,
+// PacketRandomEngine.h:585-588): lanes seed, seed + 1, a packet of two 64-bit
+// lanes per draw, a Packet4f (4 floats) or Packet2d (2 doubles) per packet.
+// Its lanes are the first two of the 4-lane engine with the same seed, so
+// the kernels run the 4-lane engine and use lanes 0 and 1.  Served: the raw
+// stream and the kinds whose packetOp transforms each 32-bit word (float) or
+// 64-bit lane (double) on its own, whose values do not depend on the packet
+// width.
+gr_status run_two_lane(gr_engine* e, const DistParams& dp0, void* out, size_t n, cudaStream_t stream) {
+  if (!kind_two_lane(dp0.kind, dp0.dtype) || (dp0.kind == GR_GAMMA && dp0.ia != 1))
+    return fail(GR_ERR_UNSUPPORTED, "2-lane Vmt19937_64: the raw stream, uniformReal, exponential, cauchy, weibull, "
+                                    "extremeValue and gamma(alpha = 1) in float and double, balanced and "
+                                    "bernoulli in float");
+  const int opp = (dp0.kind == kRawKind || dp0.dtype == GR_F64) ? 2 : 4;
+  if (n % (size_t)opp)
+    return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(opp) +
+                                    " (the 2-lane packet width for this type)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  DistParams dp = dp0;
+  dp.flags |= kParamTwoLane;
+  const int64_t granules = (int64_t)(n / (size_t)opp);
+  Plan p{};
+  p.eng = e->st;
+  p.K = e->K;
+  p.gran = opp;
+  p.gran_per_k = granules / e->K;
+  p.gran_rem = granules % e->K;
+  p.out = out;
+  const int64_t packets_max = p.gran_per_k + (p.gran_rem ? 1 : 0);
+  int S;
+  int64_t J;
+  plan_segments(e, packets_max, 1, S, J);
+  gr_status st = prepare_segments(e, p, S, J, 0, stream);
+  if (st != GR_OK) return st;
+  cudaError_t err = launch_direct(p, dp, e->snap, stream);
+  if (err != cudaSuccess) return cuda_fail(err, "2-lane sampling kernel");
+  return GR_OK;
+}
+
 gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream) {
+  if (e->lanes == 2) return run_two_lane(e, dp, out, n, stream);
   const int gran = kind_granule(dp.kind, dp.dtype);
   const int r = (int)(n % (size_t)gran);
   if (r == 0) return run_packets(e, g, dp, out, n, stream);
@@ -1326,7 +1376,10 @@ gr_status gr_sample_truncated(gr_engine* e, const gr_dist_desc* base, double low
 
 gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_stream_t stream) {
   if (!g || !e) return fail(GR_ERR_INVALID, "NULL generator or engine");
-  if (g->trunc_base) return run_trunc(e, g, dev_out, n, (cudaStream_t)stream);
+  if (g->trunc_base) {
+    if (need_four_lanes(e, "truncated rejection") != GR_OK) return GR_ERR_UNSUPPORTED;
+    return run_trunc(e, g, dev_out, n, (cudaStream_t)stream);
+  }
   gr_status st = ensure_gen_state(g, e->K);
   if (st != GR_OK) return st;
   return run_call(e, g, g->dp, dev_out, n, (cudaStream_t)stream);
@@ -1482,6 +1535,7 @@ gr_status gr_sample_v2(gr_engine* e, const gr_dist_desc* desc, const void* dev_a
 gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* dev_b, void* dev_out, size_t n,
                         gr_stream_t stream) {
   if (!g || !e || (n && !dev_out)) return fail(GR_ERR_INVALID, "NULL argument");
+  if (need_four_lanes(e, "per-element parameters") != GR_OK) return GR_ERR_UNSUPPORTED;
   const gr_dist_desc& d = g->desc;
   if (((uintptr_t)dev_a | (uintptr_t)dev_b | (uintptr_t)dev_out) % 16)
     return fail(GR_ERR_INVALID, "parameter and output arrays must be 16-byte aligned");
@@ -1610,6 +1664,7 @@ namespace gr {
 
 gr_status draw_first_words(gr_engine* e, uint64_t* out, int64_t per_sample, int64_t samples, cudaStream_t s) {
   if (per_sample <= 0 || samples <= 0) return GR_OK;
+  if (need_four_lanes(e, "scalar draws") != GR_OK) return GR_ERR_UNSUPPORTED;
   DistParams dp{};
   dp.kind = kRawLane0Kind;
   dp.dtype = GR_U64;

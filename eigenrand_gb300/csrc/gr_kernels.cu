@@ -371,11 +371,16 @@ __device__ __forceinline__ double nscale64i(double x, const DistParams& d, int64
 }
 
 // ---------------------------------------------------------------- direct kernel
-enum Mode { M_RAW, M_F32, M_F64, M_W32, M_W64, M_N32, M_N64, M_RAW0 };
+// M_RAW2 / M_F32H / M_F64H: the 2-lane Vmt19937_64 (SSE / NEON profile,
+// Pmt19937_64<Packet4i>): its packets are the first two lanes of the 4-lane
+// engine with the same seed, a Packet4f (4 floats) or Packet2d (2 doubles)
+// per packet; the other two lanes are made and left unused.
+enum Mode { M_RAW, M_F32, M_F64, M_W32, M_W64, M_N32, M_N64, M_RAW0, M_RAW2, M_F32H, M_F64H };
 
 template <int MODE>
 struct ModeInfo {
-  static constexpr int OPP = (MODE == M_RAW || MODE == M_RAW0) ? 4 : MODE == M_F32 ? 8 : MODE == M_F64 ? 4 : MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : 8;
+  static constexpr int OPP = (MODE == M_RAW || MODE == M_RAW0) ? 4 : MODE == M_F32 ? 8 : MODE == M_F64 ? 4 : MODE == M_N32 ? 8 : MODE == M_N64 ? 4
+                           : MODE == M_RAW2 ? 2 : MODE == M_F32H ? 4 : MODE == M_F64H ? 2 : 8;
   static constexpr bool kHalfCache = MODE == M_W64;  // randbits handled separately below
   static constexpr int kCacheOut = MODE == M_N32 ? 8 : MODE == M_N64 ? 4 : (MODE == M_W32 || MODE == M_W64) ? 4 : 0;
 };
@@ -480,6 +485,24 @@ __global__ void __maxnreg__(64) k_direct(Plan p, DistParams d, const CallSnap* s
           uint64_t* o = reinterpret_cast<uint64_t*>(p.out) + obase + pidx * 4;
           reinterpret_cast<ulonglong2*>(o)[0] = make_ulonglong2(pk[0], pk[1]);
           reinterpret_cast<ulonglong2*>(o)[1] = make_ulonglong2(pk[2], pk[3]);
+        }
+      } else if (MODE == M_RAW2) {
+        if (valid && p.out)
+          reinterpret_cast<ulonglong2*>(reinterpret_cast<uint64_t*>(p.out) + obase + pidx * 2)[0] =
+              make_ulonglong2(pk[0], pk[1]);
+      } else if (MODE == M_F32H) {
+        if (valid) {
+          float* o = reinterpret_cast<float*>(p.out) + obase + pidx * 4;
+          const int64_t ib = obase + pidx * 4;
+          reinterpret_cast<float4*>(o)[0] =
+              make_float4(tf32i<KIND>((uint32_t)pk[0], d, ib), tf32i<KIND>((uint32_t)(pk[0] >> 32), d, ib + 1),
+                          tf32i<KIND>((uint32_t)pk[1], d, ib + 2), tf32i<KIND>((uint32_t)(pk[1] >> 32), d, ib + 3));
+        }
+      } else if (MODE == M_F64H) {
+        if (valid) {
+          double* o = reinterpret_cast<double*>(p.out) + obase + pidx * 2;
+          const int64_t ib = obase + pidx * 2;
+          reinterpret_cast<double2*>(o)[0] = make_double2(tf64i<KIND>(pk[0], d, ib), tf64i<KIND>(pk[1], d, ib + 1));
         }
       } else if (MODE == M_RAW0) {
         // a scalar draw takes the engine's whole packet and keeps its first
@@ -864,7 +887,67 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d) {
   case K:              \
     return run_direct<M_F64, K>(p, d, snap, s);
 
+bool kind_two_lane(int kind, int dtype) {
+  if (kind == kRawKind) return true;
+  switch (kind) {
+    case GR_UNIFORM_REAL:
+    case GR_UNIFORM_REAL2:
+    case GR_EXPONENTIAL:
+    case GR_CAUCHY:
+    case GR_WEIBULL:
+    case GR_EXTREME_VALUE:
+    case GR_GAMMA:  // alpha == 1 (the caller checks)
+      return dtype == GR_F32 || dtype == GR_F64;
+    case GR_BALANCED:
+    case GR_BALANCED2:
+    case GR_BERNOULLI:
+      return dtype == GR_F32;
+    default:
+      return false;
+  }
+}
+
+#define GR_F32H_CASE(K) \
+  case K:               \
+    return run_direct<M_F32H, K>(p, d, snap, s);
+#define GR_F64H_CASE(K) \
+  case K:               \
+    return run_direct<M_F64H, K>(p, d, snap, s);
+
 cudaError_t launch_direct(const Plan& p, const DistParams& d, const CallSnap* snap, cudaStream_t s) {
+  if (d.flags & kParamTwoLane) {
+    if (d.kind == kRawKind) return run_direct<M_RAW2, kRawKind>(p, d, snap, s);
+    if (d.dtype == GR_F32) {
+      switch (d.kind) {
+        GR_F32H_CASE(GR_UNIFORM_REAL)
+        GR_F32H_CASE(GR_UNIFORM_REAL2)
+        GR_F32H_CASE(GR_BALANCED)
+        GR_F32H_CASE(GR_BALANCED2)
+        GR_F32H_CASE(GR_EXPONENTIAL)
+        GR_F32H_CASE(GR_CAUCHY)
+        GR_F32H_CASE(GR_WEIBULL)
+        GR_F32H_CASE(GR_EXTREME_VALUE)
+        GR_F32H_CASE(GR_GAMMA)
+        GR_F32H_CASE(GR_BERNOULLI)
+        default:
+          return cudaErrorNotSupported;
+      }
+    }
+    if (d.dtype == GR_F64) {
+      switch (d.kind) {
+        GR_F64H_CASE(GR_UNIFORM_REAL)
+        GR_F64H_CASE(GR_UNIFORM_REAL2)
+        GR_F64H_CASE(GR_EXPONENTIAL)
+        GR_F64H_CASE(GR_CAUCHY)
+        GR_F64H_CASE(GR_WEIBULL)
+        GR_F64H_CASE(GR_EXTREME_VALUE)
+        GR_F64H_CASE(GR_GAMMA)
+        default:
+          return cudaErrorNotSupported;
+      }
+    }
+    return cudaErrorNotSupported;
+  }
   if (d.kind == kRawKind) return run_direct<M_RAW, kRawKind>(p, d, snap, s);
   if (d.kind == kRawLane0Kind) return run_direct<M_RAW0, kRawLane0Kind>(p, d, snap, s);
   if (d.dtype == GR_F32) {

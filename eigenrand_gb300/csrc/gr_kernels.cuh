@@ -36,6 +36,9 @@ constexpr int32_t kParamUnitScale = 2;  // GammaGen beta, WeibullGen b == 1
 // per-element forms: parameter a / b of element i is vparam[i] / vparam2[i]
 constexpr int32_t kParamVecA = 4;
 constexpr int32_t kParamVecB = 8;
+// the 2-lane Vmt19937_64 (SSE / NEON profile): Packet4f / Packet2d outputs
+// from the first two lanes of each packet (launch_direct only)
+constexpr int32_t kParamTwoLane = 16;
 
 // Output transform of generators built on a BetaGen draw x (bits v):
 // FisherFGen writes (b/a) x / (1 - x), b/a in the scalar type
@@ -209,6 +212,10 @@ cudaError_t launch_vop(int kind, int threads, const VopArgs& va, cudaStream_t s)
 // draw, and the kernel that applies it to n < P draws w (engine packets'
 // first 64-bit lanes, or a scalar engine's draws).
 bool kind_has_exact_tail(int kind, int dtype);
+// Kinds the 2-lane Vmt19937_64 profile serves: the raw stream and the
+// transforms of one 32-bit word (float) or one 64-bit lane (double) per
+// output, whose values do not depend on the packet width.
+bool kind_two_lane(int kind, int dtype);
 cudaError_t launch_tail(const uint64_t* w, void* out, int n, const DistParams& d, bool packet_engine, cudaStream_t s);
 int kind_granule(int kind, int dtype);
 int kind_packets_per_unit(int kind, int dtype);
@@ -216,6 +223,10 @@ bool kind_is_direct(int kind, int dtype, const DistParams& d);
 
 // Host-side helpers shared by the C ABI translation units (gr_api.cu).
 EngState* engine_state_ptr(gr_engine* e);
+// GR_ERR_UNSUPPORTED (with the error text set) unless e is a 4-lane engine:
+// the entry points other than the raw stream and the per-word kinds serve the
+// AVX2 profile only.
+gr_status need_four_lanes(const gr_engine* e, const char* what);
 gr_status set_last_error(gr_status s, const std::string& msg);
 // Scalar draws on the packet engine (each takes a whole packet and keeps lane
 // 0): stream k of the engine owns samples [s0_k, s0_k + n_k) of `samples`,

@@ -92,7 +92,14 @@ typedef struct gr_gen gr_gen;
 
 /* ---- engines ------------------------------------------------------------
  * Replaces Eigen::Rand::Vmt19937_64 (PacketRandomEngine.h:585-599, the
- * MersenneTwister class :196-415).  lanes must be 4 (the AVX2 packet engine).
+ * MersenneTwister class :196-415).  lanes = 4: the AVX2 packet engine
+ * (Pmt19937_64<Packet8i>).  lanes = 2: the SSE / NEON engine
+ * (Pmt19937_64<Packet4i>, :585-588), lanes seed and seed + 1, a Packet4f or
+ * Packet2d per packet; it serves the raw stream and the kinds whose packetOp
+ * transforms each 32-bit word (float) or 64-bit lane (double) on its own
+ * (uniformReal, exponential, cauchy, weibull, extremeValue, gamma with
+ * alpha = 1; balanced and bernoulli in float), other calls return
+ * GR_ERR_UNSUPPORTED.
  * streams = 1 gives one Vmt19937_64(seed); streams = K > 1 gives K engines
  * seeded seed + 4k (the reference's one-engine-per-thread usage). */
 gr_status gr_engine_create(gr_engine** out, uint64_t seed, int32_t lanes, int32_t streams);
@@ -113,8 +120,8 @@ gr_status gr_engine_sync(gr_engine* e, gr_stream_t stream);
 int32_t gr_engine_streams(const gr_engine* e);
 
 /* Raw stream: makeUniversalRng<uint64_t>(Vmt19937_64) operator()
- * (PacketRandomEngine.h:468-475, 577-583).  n must be a multiple of 4 per
- * stream slice. */
+ * (PacketRandomEngine.h:468-475, 577-583).  n must be a multiple of 4 (2 for
+ * a 2-lane engine). */
 gr_status gr_raw_u64(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stream);
 
 /* ---- generators ---------------------------------------------------------
@@ -123,7 +130,13 @@ gr_status gr_raw_u64(gr_engine* e, uint64_t* dev_out, size_t n, gr_stream_t stre
  * Weights / parameters are copied at creation. */
 gr_status gr_gen_create(gr_gen** out, const gr_dist_desc* desc);
 gr_status gr_gen_destroy(gr_gen* g);
-/* *Gen::generate(rows, cols, urng) with n = rows * cols, column-major. */
+/* *Gen::generate(rows, cols, urng) with n = rows * cols, column-major.  A
+ * size that is not a whole number of packets ends with the generator's scalar
+ * operator(), one engine packet per remaining element, drawn from the last
+ * stream (Eigen's linear vectorised assignment loop); served for
+ * uniformReal, balanced, bernoulli and randBits, whose scalar forms are exact
+ * (Basic.h:386-391, 416-420, 456-460, 533-540, 620-624, 689-693), else
+ * GR_ERR_INVALID. */
 gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_stream_t stream);
 /* Free-function form (Eigen::Rand::normal(rows, cols, urng, ...)): a fresh
  * generator for one call. */

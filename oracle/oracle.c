@@ -659,8 +659,87 @@ static void scalar_tail(or_vmt* e, int dist, int dtype, double a, double b, void
   }
 }
 
+/* The SSE / NEON profile: Vmt19937_64 = Pmt19937_64<Packet4i>, two lanes
+ * (PacketRandomEngine.h:585-588); a Packet4f takes the engine packet's four
+ * 32-bit words, a Packet2d its two 64-bit lanes.  The kinds whose packetOp
+ * transforms each word (float) or lane (double) on its own: the same per-lane
+ * arithmetic as the AVX2 profile (uniformReal Basic.h:584-590, 638-645;
+ * balanced RandUtils.h:36-45 with arch/SSE's float zero_to_one; exponential
+ * NormalExp.h:391-398; cauchy :844-855; weibull :648-655; extremeValue
+ * :724-732; gamma with alpha = 1, its exponential branch; bernoulli
+ * Basic.h:695-707).  Other kinds: 3. */
+static int gen_real_sse(or_vmt* e, int dist, int dbl, double a, double b, void* out, size_t n) {
+  const size_t P = dbl ? 2 : 4;
+  if (n % P) return 2;
+  const int supported = dist == OR_UNIFORM || dist == OR_EXPONENTIAL || dist == OR_CAUCHY || dist == OR_WEIBULL ||
+                        dist == OR_EXTREME || (!dbl && (dist == OR_BALANCED || dist == OR_BERNOULLI));
+  if (!supported) return 3;
+  float* of = (float*)out;
+  double* od = (double*)out;
+  for (size_t k = 0; k < n / P; ++k) {
+    uint64_t r[2];
+    vmt_packet(e, r);
+    for (size_t j = 0; j < P; ++j) {
+      if (dbl) {
+        const double u = bit_ur_d(r[j]);
+        double v;
+        switch (dist) {
+          case OR_UNIFORM: v = (a == 0 && b == 1) ? u : u * (b - a) + a; break;
+          case OR_EXPONENTIAL: v = -(or_log(1.0 - u) / a); break;
+          case OR_CAUCHY: {
+            double sn, cs;
+            or_sincos(PI_D * (u - 0.5), &sn, &cs);
+            v = a + b * (sn / cs);
+            break;
+          }
+          case OR_WEIBULL: v = or_exp(or_log(-or_log(1.0 - u)) * (1 / a)) * b; break;
+          default: v = a - or_log(-or_log(u + 2.220446049250313e-16 / 8)) * b; break; /* extreme value */
+        }
+        od[k * P + j] = v;
+      } else {
+        const uint32_t w = (j & 1) ? (uint32_t)(r[j >> 1] >> 32) : (uint32_t)r[j >> 1];
+        const float u = bit_ur_f(w), fa = (float)a, fb = (float)b;
+        float v;
+        switch (dist) {
+          case OR_UNIFORM: v = (a == 0 && b == 1) ? u : u * (fb - fa) + fa; break;
+          case OR_BALANCED: {
+            const float z = (float)(int32_t)(w & 0x7fffffffu) / (float)0x7FFFFFFF;
+            v = (a == -1 && b == 1) ? z * 2.0f - 1.0f : z * (fb - fa) + fa;
+            break;
+          }
+          case OR_EXPONENTIAL: v = -(or_logf(1.0f - u) / fa); break;
+          case OR_CAUCHY: {
+            float sn, cs;
+            or_sincosf((float)PI_D * (u - 0.5f), &sn, &cs);
+            v = fa + fb * (sn / cs);
+            break;
+          }
+          case OR_WEIBULL: v = or_expf(or_logf(-or_logf(1.0f - u)) * (1 / fa)) * fb; break;
+          case OR_BERNOULLI: v = ((int32_t)(w & 0x7fffffffu) < (int32_t)(uint32_t)(a * 2147483648.0)) ? 1.0f : 0.0f; break;
+          default: v = fa - or_logf(-or_logf(u + 1.1920928955078125e-07f / 8)) * fb; break; /* extreme value */
+        }
+        of[k * P + j] = v;
+      }
+    }
+  }
+  return 0;
+}
+
 int or_gen_real(or_vmt* e, or_gen* g, int dist, int dtype, double a, double b, void* out, size_t n) {
   int dbl = dtype == 1;
+  if (e->L == 2 && !g_src) {
+    /* gamma with alpha = 1 is its exponential branch times beta */
+    if (dist == OR_GAMMA && a == 1.0) {
+      const int rc = gen_real_sse(e, OR_EXPONENTIAL, dbl, 1.0, 0.0, out, n);
+      if (rc == 0 && b != 1.0)
+        for (size_t i = 0; i < n; ++i) {
+          if (dbl) ((double*)out)[i] = b * ((double*)out)[i];
+          else ((float*)out)[i] = (float)b * ((float*)out)[i];
+        }
+      return rc;
+    }
+    return gen_real_sse(e, dist, dbl, a, b, out, n);
+  }
   int P = P_of(dbl);
   /* a partial last packet: the scalar operator() (kinds whose scalar form is exact) */
   const size_t tail = n % (size_t)P;

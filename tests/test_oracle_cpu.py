@@ -449,3 +449,21 @@ def test_oracle_scalar_tail_from_raw_stream(oracle):
     sext = lo.astype(np.int32).astype(np.int64).view(np.uint64)
     u = ((sext & np.uint64(0xFFFFFFFFFFFFF)) | np.uint64(1023 << 52)).view(np.float64) - 1.0
     assert np.array_equal(got[4:], 0.5 + u * 1.5)
+
+
+def test_two_lane_profile_restated_from_the_raw_stream(oracle):
+    """The SSE / NEON Vmt19937_64 (two lanes): its packets are the first two
+    lanes of the 4-lane engine with the same seed (lane l is
+    std::mt19937_64(seed + l) in both), and a Packet4f takes the packet's
+    four 32-bit words in order."""
+    import numpy as np
+    two = oracle.Engine(321, lanes=2).raw(1000).reshape(-1, 2)
+    four = oracle.Engine(321).raw(1000).reshape(-1, 4)
+    assert np.array_equal(two, four[:, :2])
+    got = oracle.generate(oracle.Engine(321, lanes=2), oracle.Gen(), "UNIFORM_REAL", 4000, np.float32)
+    words = two.reshape(-1).view(np.uint32)
+    ref = ((words & np.uint32(0x7FFFFF)) | np.uint32(0x3F800000)).view(np.float32) - np.float32(1)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    got = oracle.generate(oracle.Engine(321, lanes=2), oracle.Gen(), "UNIFORM_REAL", 2000, np.float64)
+    ref = ((two.reshape(-1) & np.uint64(0xFFFFFFFFFFFFF)) | np.uint64(1023 << 52)).view(np.float64) - 1.0
+    assert np.array_equal(got, ref)
