@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-ffp-contract=off"]
 SOURCES = ["gr_kernels.cu", "gr_samplers.cu", "gr_vop.cu", "gr_mv.cu", "gr_api.cu", "gr_mvapi.cu", "gr_serve.cu",
-           "gr_noalloc.cu", "gr_trunc.cu", "gr_mncond.cu", "gr_tmvn.cu", "gr_binomv.cu",
+           "gr_noalloc.cu", "gr_trunc.cu", "gr_umma.cu", "gr_mncond.cu", "gr_tmvn.cu", "gr_binomv.cu",
            "gr_poly.cpp"]
 HEADERS = ["gr_exact.h", "gr_internal.h", "gr_kernels.cuh", "gr_math.cuh", "gr_math_tables.h", "gr_mt.cuh", "gr_mv.cuh", "gr_admit.h", "gr_poly.h"]
 

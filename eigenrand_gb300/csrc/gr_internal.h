@@ -77,6 +77,7 @@ struct CallSnap {
 enum DevStatus : int32_t {
   GR_DEV_REJECT_LIMIT = 1,  // a rejection loop hit its iteration cap
   GR_DEV_BAD_INPUT = 2,
+  GR_DEV_MMA_TIMEOUT = 8,   // a tensor-core kernel gave up waiting for its products
 };
 
 }  // namespace gr

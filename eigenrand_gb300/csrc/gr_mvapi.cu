@@ -215,6 +215,7 @@ struct gr_mvnormal {
   int dim = 0, dtype = GR_F32, tri = 1;
   double* L64 = nullptr;
   float* Lf = nullptr;  // packed float fragments (float objects)
+  float* Lu = nullptr;  // the factor as the tcgen05 B operand (float objects, dim <= kUmmaMaxDim)
   void* mean = nullptr;
   gr_gen* normal = nullptr;
 };
@@ -277,6 +278,11 @@ gr_status mvnormal_clone(const gr_mvnormal* src, gr_mvnormal** out) {
     e = cudaMalloc(&g->Lf, sizeof(float) * (size_t)nfr * 128);
     if (e == cudaSuccess) e = cudaMemcpy(g->Lf, src->Lf, sizeof(float) * (size_t)nfr * 128, cudaMemcpyDeviceToDevice);
   }
+  if (e == cudaSuccess && src->Lu) {
+    const size_t nu = (size_t)umma_chunks(src->dim) * 2 * umma_padded_dim(src->dim) * 32;
+    e = cudaMalloc(&g->Lu, sizeof(float) * nu);
+    if (e == cudaSuccess) e = cudaMemcpy(g->Lu, src->Lu, sizeof(float) * nu, cudaMemcpyDeviceToDevice);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&g->mean, es * src->dim);
   if (e == cudaSuccess) e = cudaMemcpy(g->mean, src->mean, es * src->dim, cudaMemcpyDeviceToDevice);
   gr_status st = e == cudaSuccess ? GR_OK : mv_fail(GR_ERR_CUDA, std::string("MvNormalGen copy: ") + cudaGetErrorString(e));
@@ -298,6 +304,7 @@ gr_status gr_mvnormal_destroy(gr_mvnormal* g) {
   if (!g) return GR_OK;
   cudaFree(g->L64);
   cudaFree(g->Lf);
+  cudaFree(g->Lu);
   cudaFree(g->mean);
   gr_gen_destroy(g->normal);
   delete g;
@@ -326,6 +333,11 @@ gr_status gr_mvnormal_create(gr_mvnormal** out, int32_t dtype, int32_t dim, cons
       const int64_t nfr = g->tri ? mv_tri_frags(MT, KS) : (int64_t)MT * KS;
       e = cudaMalloc(&g->Lf, sizeof(float) * (size_t)nfr * 128);
       if (e == cudaSuccess) e = launch_pack_lt(g->L64, g->Lf, dim, g->tri, nullptr);
+      if (e == cudaSuccess && dim <= kUmmaMaxDim) {
+        const size_t nu = (size_t)umma_chunks(dim) * 2 * umma_padded_dim(dim) * 32;
+        e = cudaMalloc(&g->Lu, sizeof(float) * nu);
+        if (e == cudaSuccess) e = launch_prep_lt_umma(g->L64, g->Lu, dim, nullptr);
+      }
       std::vector<float> mf(mean, mean + dim);
       if (e == cudaSuccess) e = cudaMalloc(&g->mean, sizeof(float) * dim);
       if (e == cudaSuccess) e = cudaMemcpy(g->mean, mf.data(), sizeof(float) * dim, cudaMemcpyHostToDevice);
@@ -346,6 +358,7 @@ gr_status gr_mvnormal_create(gr_mvnormal** out, int32_t dtype, int32_t dim, cons
 }
 
 gr_status gr_mvnormal_sample(gr_mvnormal* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (need_four_lanes(e, "MvNormalGen") != GR_OK) return GR_ERR_UNSUPPORTED;
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
@@ -356,10 +369,14 @@ gr_status gr_mvnormal_sample(gr_mvnormal* g, gr_engine* e, void* dev_out, size_t
   // Z = StdNormalGen draws (dim x samples), then X = L Z + mean in place
   gr_status st = gr_generate(g->normal, e, dev_out, n, stream);
   if (st != GR_OK) return st;
-  cudaError_t err = g->dtype == GR_F32
-                        ? launch_mvn(g->Lf, g->tri, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples, s)
-                        : launch_mvn_f64(g->L64, g->tri, (const double*)g->mean, (double*)dev_out, g->dim,
-                                         (int64_t)samples, s);
+  cudaError_t err;
+  if (g->dtype == GR_F32 && g->Lu)
+    err = launch_mvn_umma(g->Lu, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples,
+                          &engine_state_ptr(e)->status, s);
+  else if (g->dtype == GR_F32)
+    err = launch_mvn(g->Lf, g->tri, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples, s);
+  else
+    err = launch_mvn_f64(g->L64, g->tri, (const double*)g->mean, (double*)dev_out, g->dim, (int64_t)samples, s);
   if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("MvNormal product: ") + cudaGetErrorString(err));
   return GR_OK;
 }
@@ -416,6 +433,7 @@ gr_status gr_wishart_create(gr_wishart** out, int32_t dtype, int32_t dim, int64_
 }
 
 gr_status gr_wishart_sample(gr_wishart* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (need_four_lanes(e, "WishartGen") != GR_OK) return GR_ERR_UNSUPPORTED;
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
@@ -477,6 +495,7 @@ gr_status gr_dirichlet_create(gr_dirichlet** out, int32_t dtype, int32_t dim, co
 }
 
 gr_status gr_dirichlet_sample(gr_dirichlet* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (need_four_lanes(e, "DirichletGen") != GR_OK) return GR_ERR_UNSUPPORTED;
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
@@ -561,6 +580,7 @@ gr_status gr_truncmvn_create(gr_truncmvn** out, int32_t dtype, int32_t dim, cons
 }
 
 gr_status gr_truncmvn_sample(gr_truncmvn* g, gr_engine* e, void* dev_out, size_t samples, gr_stream_t stream) {
+  if (need_four_lanes(e, "TruncMvNormalGen") != GR_OK) return GR_ERR_UNSUPPORTED;
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
@@ -677,6 +697,7 @@ gr_status gr_multinomial_create(gr_multinomial** out, int32_t dim, int32_t trial
 
 gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_out, size_t samples,
                                 gr_stream_t stream) {
+  if (need_four_lanes(e, "MultinomialGen") != GR_OK) return GR_ERR_UNSUPPORTED;
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");

@@ -161,6 +161,16 @@ def test_mvnormal_f32_vs_fp64_oracle(er, oracle, d):
     assert err <= 1e-5
 
 
+@pytest.mark.parametrize("d,n", [(5, 776), (33, 136), (100, 1002), (200, 257), (256, 300)])
+def test_mvnormal_f32_tensor_memory_shapes(er, oracle, d, n):
+    """The tcgen05 product (dim <= 256) at shapes that pad every dimension:
+    dim not a multiple of 4, 16 or 32 (scalar loads, zero-padded N and K) and
+    sample counts that leave a partial 128-sample tile."""
+    err = mvn_case(er, oracle, d, n, torch.float32, seed=d)
+    print(f"MvNormal d={d} n={n} float: max error / (|L||Z| + |mean|) = {err:.3g}")
+    assert err <= 1e-5
+
+
 @pytest.mark.parametrize("d", [3, 16, 64])
 def test_mvnormal_f64_vs_fp64_oracle(er, oracle, d):
     err = mvn_case(er, oracle, d, 400, torch.float64)
