@@ -748,6 +748,8 @@ gr_status run_two_lane(gr_engine* e, const DistParams& dp0, void* out, size_t n,
 }
 
 gr_status run_call(gr_engine* e, gr_gen* g, const DistParams& dp, void* out, size_t n, cudaStream_t stream) {
+  // the kernels store whole packets with 16-byte vector stores
+  if (n && ((uintptr_t)out % 16)) return fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   if (e->lanes == 2) return run_two_lane(e, dp, out, n, stream);
   const int gran = kind_granule(dp.kind, dp.dtype);
   const int r = (int)(n % (size_t)gran);
@@ -1376,6 +1378,7 @@ gr_status gr_sample_truncated(gr_engine* e, const gr_dist_desc* base, double low
 
 gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_stream_t stream) {
   if (!g || !e) return fail(GR_ERR_INVALID, "NULL generator or engine");
+  if (n && ((uintptr_t)dev_out % 16)) return fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   if (g->trunc_base) {
     if (need_four_lanes(e, "truncated rejection") != GR_OK) return GR_ERR_UNSUPPORTED;
     return run_trunc(e, g, dev_out, n, (cudaStream_t)stream);
@@ -1412,6 +1415,7 @@ gr_status gr_sample_batched(gr_engine* e, const gr_batch_desc* bd, gr_stream_t s
   if (!bd->a || !bd->counts || !bd->offsets || !bd->out || (bd->kind == GR_GAMMA && !bd->b) ||
       (bd->kind == GR_BINOMIAL_V && !bd->trials))
     return fail(GR_ERR_INVALID, "missing device array in gr_batch_desc");
+  if ((uintptr_t)bd->out % 16) return fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
   VopArgs va{};
   va.nsets = bd->nsets;
@@ -2014,6 +2018,7 @@ gr_status gr_sengine_destroy(gr_sengine* se) {
 
 gr_status gr_sengine_raw_u64(gr_sengine* se, uint64_t* dev_out, size_t n, gr_stream_t stream) {
   if (!se || (n && !dev_out)) return fail(GR_ERR_INVALID, "NULL argument");
+  if (n && ((uintptr_t)dev_out % 16)) return fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   return sengine_words(se, dev_out, (int64_t)n, (cudaStream_t)stream);
 }
 
@@ -2029,6 +2034,7 @@ gr_status gr_sengine_sample_v2(gr_sengine* se, const gr_dist_desc* desc, const v
 
 gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_out, size_t n, gr_stream_t stream) {
   if (!se || !desc) return fail(GR_ERR_INVALID, "NULL argument");
+  if (n && ((uintptr_t)dev_out % 16)) return fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
   gr_status st = GR_OK;
   if (desc->kind == GR_DISCRETE) {

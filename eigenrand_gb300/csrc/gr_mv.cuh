@@ -111,13 +111,17 @@ cudaError_t launch_pack_lt(const double* L, float* out, int d, int tri, cudaStre
 cudaError_t launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
 cudaError_t launch_mvn(const float* Lf, int tri, const float* mean, float* X, int d, int64_t n, cudaStream_t s);
 // X = L Z + mean (float) with tcgen05.mma (gr_umma.cu), dim <= kUmmaMaxDim:
-// the factor prepared once by launch_prep_lt_umma into umma_chunks(d) * 2 *
-// umma_padded_dim(d) * 32 floats; device errors go to *status.
+// the factor prepared once by launch_prep_lt_umma into umma_prep_floats(d,
+// tri) floats (tri: L lower triangular, its zero blocks left out);
+// umma_usable says whether a call can take this path (dim a multiple of 4,
+// X 16-byte aligned, fewer than 2^31 samples); device errors go to *status.
 constexpr int kUmmaMaxDim = 256;
 int umma_padded_dim(int d);
 int umma_chunks(int d);
-cudaError_t launch_prep_lt_umma(const double* L, float* out, int d, cudaStream_t s);
-cudaError_t launch_mvn_umma(const float* Lp, const float* mean, float* X, int d, int64_t n, int32_t* status,
+size_t umma_prep_floats(int d, int tri);
+bool umma_usable(int d, const void* X, int64_t n);
+cudaError_t launch_prep_lt_umma(const double* L, float* out, int d, int tri, cudaStream_t s);
+cudaError_t launch_mvn_umma(const float* Lp, int tri, const float* mean, float* X, int d, int64_t n, int32_t* status,
                             cudaStream_t s);
 cudaError_t launch_mvn_f64(const double* L, int tri, const double* mean, double* X, int d, int64_t n, cudaStream_t s);
 size_t wishart_smem(int d, int dtype);

@@ -7,6 +7,8 @@
 // assembly kernels of gr_mv.cu.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -279,7 +281,7 @@ gr_status mvnormal_clone(const gr_mvnormal* src, gr_mvnormal** out) {
     if (e == cudaSuccess) e = cudaMemcpy(g->Lf, src->Lf, sizeof(float) * (size_t)nfr * 128, cudaMemcpyDeviceToDevice);
   }
   if (e == cudaSuccess && src->Lu) {
-    const size_t nu = (size_t)umma_chunks(src->dim) * 2 * umma_padded_dim(src->dim) * 32;
+    const size_t nu = umma_prep_floats(src->dim, src->tri);
     e = cudaMalloc(&g->Lu, sizeof(float) * nu);
     if (e == cudaSuccess) e = cudaMemcpy(g->Lu, src->Lu, sizeof(float) * nu, cudaMemcpyDeviceToDevice);
   }
@@ -326,6 +328,10 @@ gr_status gr_mvnormal_create(gr_mvnormal** out, int32_t dtype, int32_t dim, cons
   g->dim = dim;
   g->dtype = dtype;
   gr_status st = factor_f64(dim, matrix, matrix_form, false, &g->L64, &g->tri);
+  // test hook: GR_MVN_FULL_FORM=1 treats a triangular factor as a full matrix
+  // (the products then run over every block, as for the eigen form)
+  if (const char* ff = std::getenv("GR_MVN_FULL_FORM"))
+    if (ff[0] == '1') g->tri = 0;
   if (st == GR_OK) {
     cudaError_t e = cudaSuccess;
     if (dtype == GR_F32) {
@@ -334,9 +340,9 @@ gr_status gr_mvnormal_create(gr_mvnormal** out, int32_t dtype, int32_t dim, cons
       e = cudaMalloc(&g->Lf, sizeof(float) * (size_t)nfr * 128);
       if (e == cudaSuccess) e = launch_pack_lt(g->L64, g->Lf, dim, g->tri, nullptr);
       if (e == cudaSuccess && dim <= kUmmaMaxDim) {
-        const size_t nu = (size_t)umma_chunks(dim) * 2 * umma_padded_dim(dim) * 32;
+        const size_t nu = umma_prep_floats(dim, g->tri);
         e = cudaMalloc(&g->Lu, sizeof(float) * nu);
-        if (e == cudaSuccess) e = launch_prep_lt_umma(g->L64, g->Lu, dim, nullptr);
+        if (e == cudaSuccess) e = launch_prep_lt_umma(g->L64, g->Lu, dim, g->tri, nullptr);
       }
       std::vector<float> mf(mean, mean + dim);
       if (e == cudaSuccess) e = cudaMalloc(&g->mean, sizeof(float) * dim);
@@ -370,8 +376,8 @@ gr_status gr_mvnormal_sample(gr_mvnormal* g, gr_engine* e, void* dev_out, size_t
   gr_status st = gr_generate(g->normal, e, dev_out, n, stream);
   if (st != GR_OK) return st;
   cudaError_t err;
-  if (g->dtype == GR_F32 && g->Lu)
-    err = launch_mvn_umma(g->Lu, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples,
+  if (g->dtype == GR_F32 && g->Lu && umma_usable(g->dim, dev_out, (int64_t)samples))
+    err = launch_mvn_umma(g->Lu, g->tri, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples,
                           &engine_state_ptr(e)->status, s);
   else if (g->dtype == GR_F32)
     err = launch_mvn(g->Lf, g->tri, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples, s);
@@ -437,6 +443,7 @@ gr_status gr_wishart_sample(gr_wishart* g, gr_engine* e, void* dev_out, size_t s
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  if ((uintptr_t)dev_out % 16) return mv_fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   const int d = g->dim;
   const size_t P = (size_t)packet_width(g->dtype);
   const size_t nnorm = samples * (size_t)d * (size_t)(d - 1) / 2;
@@ -499,6 +506,7 @@ gr_status gr_dirichlet_sample(gr_dirichlet* g, gr_engine* e, void* dev_out, size
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  if ((uintptr_t)dev_out % 16) return mv_fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   if (samples % (size_t)packet_width(g->dtype)) return mv_fail(GR_ERR_INVALID, "samples must be a multiple of the packet width");
   const size_t es = elem_size(g->dtype);
   gr_status st = g->scratch.need((size_t)g->dim * samples * es);
@@ -584,6 +592,7 @@ gr_status gr_truncmvn_sample(gr_truncmvn* g, gr_engine* e, void* dev_out, size_t
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  if ((uintptr_t)dev_out % 16) return mv_fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
   const int d = g->dim;
   const size_t es = elem_size(g->dtype);
@@ -701,6 +710,7 @@ gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_ou
   if (!g || !e) return mv_fail(GR_ERR_INVALID, "NULL generator or engine");
   if (samples == 0) return GR_OK;
   if (!dev_out) return mv_fail(GR_ERR_INVALID, "output is NULL");
+  if ((uintptr_t)dev_out % 16) return mv_fail(GR_ERR_INVALID, "output array must be 16-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
   if (g->trials == 0) {  // no draws: every count is 0
     MV_CUDA(cudaMemsetAsync(dev_out, 0, sizeof(int32_t) * (size_t)g->dim * samples, s));

@@ -109,6 +109,7 @@ extern "C" gr_status gr_raw_u64_noalloc(gr_engine* e, uint64_t* dev_out, size_t 
     return na_fail(GR_ERR_UNSUPPORTED, "gr_raw_u64_noalloc: only engines created with streams = 1");
   if (need_four_lanes(e, "gr_raw_u64_noalloc") != GR_OK) return GR_ERR_UNSUPPORTED;
   if (n % kLanes) return na_fail(GR_ERR_INVALID, "gr_raw_u64_noalloc: n must be a multiple of 4");
+  if ((uintptr_t)dev_out % 16) return na_fail(GR_ERR_INVALID, "gr_raw_u64_noalloc: output must be 16-byte aligned");
   if (n > (size_t)GR_NOALLOC_MAX_DRAWS)
     return na_fail(GR_ERR_INVALID, "gr_raw_u64_noalloc: n exceeds GR_NOALLOC_MAX_DRAWS (2^32 draws); "
                                    "split the call");

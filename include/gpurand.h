@@ -11,6 +11,11 @@
  * Engines and generators are externally synchronised: use one stream per
  * engine, as EigenRand requires one engine per thread.
  *
+ * Every device output array must be 16-byte aligned (cudaMalloc and the
+ * caching allocators of the usual frameworks return such pointers): the
+ * kernels write whole packets with 16-byte stores.  A misaligned output
+ * returns GR_ERR_INVALID before anything is launched.
+ *
  * Stream semantics (bit-exact with the reference, AVX2 + Eigen 3.4 profile):
  *   - lane l of a Vmt19937_64 seeded s is std::mt19937_64(s + l), l < 4;
  *   - raw u64 stream R[4k + l] = lane_l[k]  (packet k = 4 lanes);

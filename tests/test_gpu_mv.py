@@ -161,14 +161,52 @@ def test_mvnormal_f32_vs_fp64_oracle(er, oracle, d):
     assert err <= 1e-5
 
 
-@pytest.mark.parametrize("d,n", [(5, 776), (33, 136), (100, 1002), (200, 257), (256, 300)])
+@pytest.mark.parametrize("d,n", [(4, 776), (36, 136), (100, 1002), (132, 258), (200, 257), (256, 300),
+                                 (5, 776), (33, 136)])
 def test_mvnormal_f32_tensor_memory_shapes(er, oracle, d, n):
-    """The tcgen05 product (dim <= 256) at shapes that pad every dimension:
-    dim not a multiple of 4, 16 or 32 (scalar loads, zero-padded N and K) and
-    sample counts that leave a partial 128-sample tile."""
+    """The tcgen05 product (dim a multiple of 4, <= 256) at shapes that pad
+    every dimension: zero-padded N (dim to a multiple of 16) and K (to 32),
+    one and two 128-column passes, the factor resident in shared memory
+    (dim <= 160) or streamed per slice (200, 256), and sample counts that
+    leave a partial 128-sample tile.  dim 5 and 33 take the mma.sync form."""
     err = mvn_case(er, oracle, d, n, torch.float32, seed=d)
     print(f"MvNormal d={d} n={n} float: max error / (|L||Z| + |mean|) = {err:.3g}")
     assert err <= 1e-5
+
+
+@pytest.mark.parametrize("d,n", [(20, 300), (64, 500), (128, 260), (136, 300), (256, 200)])
+def test_mvnormal_f32_full_form_products(er, oracle, d, n, monkeypatch):
+    """The full-matrix form of the products (every block of L, as for the
+    eigen-form factor of a singular covariance), forced on a Cholesky factor
+    with the GR_MVN_FULL_FORM test hook so that the FP64 check still holds."""
+    monkeypatch.setenv("GR_MVN_FULL_FORM", "1")
+    err = mvn_case(er, oracle, d, n, torch.float32, seed=d + 1)
+    assert err <= 1e-5
+
+
+def test_mvnormal_f32_many_tiles_per_cta(er, oracle):
+    """More tiles than twice the SM count: every ring (raw slots, A stages,
+    both accumulators) wraps many times."""
+    d, n = 64, 152 * 128 * 5 + 77
+    err = mvn_case(er, oracle, d, n, torch.float32, seed=3)
+    assert err <= 1e-5
+
+
+def test_misaligned_outputs_refused(er):
+    """A device output that is not 16-byte aligned is refused on the host
+    (GR_ERR_INVALID) before anything is launched."""
+    import ctypes
+    buf = torch.zeros(4096 + 4, dtype=torch.float32, device="cuda")
+    bad = ctypes.c_void_p(buf.data_ptr() + 4)
+    u = er.Vmt19937_64(1)
+    d, keep = er._desc("NORMAL_STD", torch.float32)
+    assert er._L.gr_sample(u._h, ctypes.byref(d), bad, 64, er._stream_ptr()) == 1
+    assert "aligned" in er._L.gr_last_error().decode()
+    assert er._L.gr_raw_u64(u._h, bad, 64, er._stream_ptr()) == 1
+    g = er.MvNormalGen(np.zeros(4), np.eye(4))
+    assert er._L.gr_mvnormal_sample(g._h, u._h, bad, 16, er._stream_ptr()) == 1
+    torch.cuda.synchronize()
+    assert float(buf.abs().sum()) == 0.0  # nothing was written
 
 
 @pytest.mark.parametrize("d", [3, 16, 64])
