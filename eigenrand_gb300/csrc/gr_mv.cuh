@@ -116,6 +116,7 @@ cudaError_t launch_mvn(const float* Lf, int tri, const float* mean, float* X, in
 // umma_usable says whether a call can take this path (dim a multiple of 4,
 // X 16-byte aligned, fewer than 2^31 samples); device errors go to *status.
 constexpr int kUmmaMaxDim = 256;
+constexpr int kUmmaAutoMinDim = 20;  // smallest dim the tcgen05 product is used for by default
 int umma_padded_dim(int d);
 int umma_chunks(int d);
 size_t umma_prep_floats(int d, int tri);

@@ -376,7 +376,14 @@ gr_status gr_mvnormal_sample(gr_mvnormal* g, gr_engine* e, void* dev_out, size_t
   gr_status st = gr_generate(g->normal, e, dev_out, n, stream);
   if (st != GR_OK) return st;
   cudaError_t err;
-  if (g->dtype == GR_F32 && g->Lu && umma_usable(g->dim, dev_out, (int64_t)samples))
+  // the tcgen05 product from kUmmaAutoMinDim up (below it the mma.sync form
+  // is as fast); test hook GR_MVN_PRODUCT=tcgen05 | mma_sync picks one form
+  bool umma = g->dim >= kUmmaAutoMinDim;
+  if (const char* pv = std::getenv("GR_MVN_PRODUCT")) {
+    if (std::strcmp(pv, "tcgen05") == 0) umma = true;
+    if (std::strcmp(pv, "mma_sync") == 0) umma = false;
+  }
+  if (g->dtype == GR_F32 && g->Lu && umma && umma_usable(g->dim, dev_out, (int64_t)samples))
     err = launch_mvn_umma(g->Lu, g->tri, (const float*)g->mean, (float*)dev_out, g->dim, (int64_t)samples,
                           &engine_state_ptr(e)->status, s);
   else if (g->dtype == GR_F32)

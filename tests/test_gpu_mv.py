@@ -163,15 +163,26 @@ def test_mvnormal_f32_vs_fp64_oracle(er, oracle, d):
 
 @pytest.mark.parametrize("d,n", [(4, 776), (36, 136), (100, 1002), (132, 258), (200, 257), (256, 300),
                                  (5, 776), (33, 136)])
-def test_mvnormal_f32_tensor_memory_shapes(er, oracle, d, n):
-    """The tcgen05 product (dim a multiple of 4, <= 256) at shapes that pad
-    every dimension: zero-padded N (dim to a multiple of 16) and K (to 32),
-    one and two 128-column passes, the factor resident in shared memory
-    (dim <= 160) or streamed per slice (200, 256), and sample counts that
-    leave a partial 128-sample tile.  dim 5 and 33 take the mma.sync form."""
+def test_mvnormal_f32_tensor_memory_shapes(er, oracle, d, n, monkeypatch):
+    """The tcgen05 product (dim a multiple of 4, <= 256; forced with the
+    GR_MVN_PRODUCT test hook below the default threshold) at shapes that pad
+    every dimension: zero-padded N (dim to a multiple of 16) and K (to 32,
+    all-zero K steps left out), one and two 128-column passes, the factor
+    resident in shared memory (dim <= 160) or streamed per slice (200, 256),
+    and sample counts that leave a partial 128-sample tile.  dim 5 and 33
+    take the mma.sync form."""
+    monkeypatch.setenv("GR_MVN_PRODUCT", "tcgen05")
     err = mvn_case(er, oracle, d, n, torch.float32, seed=d)
     print(f"MvNormal d={d} n={n} float: max error / (|L||Z| + |mean|) = {err:.3g}")
     assert err <= 1e-5
+
+
+@pytest.mark.parametrize("d", [16, 64, 256])
+def test_mvnormal_f32_mma_sync_form(er, oracle, d, monkeypatch):
+    """The mma.sync form of the product (the default below dim 20, and for
+    dims that are not a multiple of 4), forced at dims that default to tcgen05."""
+    monkeypatch.setenv("GR_MVN_PRODUCT", "mma_sync")
+    assert mvn_case(er, oracle, d, 520, torch.float32, seed=d + 2) <= 1e-5
 
 
 @pytest.mark.parametrize("d,n", [(20, 300), (64, 500), (128, 260), (136, 300), (256, 200)])
