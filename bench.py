@@ -517,14 +517,14 @@ def bench_batched(er, nsets=1_000_000, percall_sets=2048):
 
 
 def bench_multivariate(er, streams=608):
-    """MvNormal d in {16, 64, 256} (N = 10^6), Wishart d=32 df=40 (10^5 draws),
+    """MvNormal d in {16, 64, 128, 256} (N = 10^6), Wishart d=32 df=40 (10^5 draws),
     Dirichlet K=64 (10^6), Multinomial K=100 trials=1000 (10^6); float32."""
     import numpy as np
     import torch
     urng = er.Vmt19937_64(99, streams=streams)
     res = {}
     N = 1_000_000
-    for d in (16, 64, 256):
+    for d in (16, 64, 128, 256):
         rng = np.random.default_rng(99)
         A = rng.standard_normal((d, d))
         cov = A @ A.T + d * np.eye(d)
@@ -892,7 +892,7 @@ def run_case(args):
         rng = np.random.default_rng(99)
         A = rng.standard_normal((d, d))
         g = er.MvNormalGen(rng.standard_normal(d), A @ A.T + d * np.eye(d))
-        n = (1 << 26) // (4 * d)  # 64 MiB of output: above L2 with the normals
+        n = (1 << 28) // (4 * d)  # 256 MiB of output, twice the L2
         out = torch.empty((n, d), dtype=torch.float32, device="cuda").t()
         fn = lambda: g.generate(urng, n, out=out)
     elif name == "multinomial":
