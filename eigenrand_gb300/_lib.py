@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libgpurand.so")
 GR_OK = 0
 STATUS_NAMES = {
     0: "GR_OK", 1: "GR_ERR_INVALID", 2: "GR_ERR_CUDA", 3: "GR_ERR_UNSUPPORTED", 4: "GR_ERR_NOMEM",
-    5: "GR_ERR_REJECT_LIMIT", 6: "GR_ERR_NOT_PD", 7: "GR_ERR_NAN_WEIGHT",
+    5: "GR_ERR_REJECT_LIMIT", 6: "GR_ERR_NOT_PD", 7: "GR_ERR_NAN_WEIGHT", 8: "GR_ERR_CANCELLED",
 }
 
 # gr_dtype
@@ -39,7 +39,8 @@ EXPORTS = [
     "gr_multinomial_create", "gr_multinomial_sample", "gr_multinomial_destroy",
     "gr_truncmvn_create", "gr_truncmvn_sample", "gr_truncmvn_destroy",
     "gr_server_create", "gr_server_set_mvnormal", "gr_server_submit", "gr_server_progress", "gr_server_read",
-    "gr_server_release", "gr_server_pending", "gr_server_now", "gr_server_destroy",
+    "gr_server_release", "gr_server_cancel", "gr_server_cancel_client", "gr_server_fail_allocs", "gr_server_pending",
+    "gr_server_now", "gr_server_destroy",
 ]
 
 GR_SERVE_MVNORMAL = 64
@@ -168,6 +169,9 @@ def load(path=None):
         "gr_server_progress": (i32, [vp, vp, sz, ctypes.POINTER(sz)]),
         "gr_server_read": (i32, [vp, u64, vp, sz]),
         "gr_server_release": (i32, [vp, u64]),
+        "gr_server_cancel": (i32, [vp, u64]),
+        "gr_server_cancel_client": (i32, [vp, i32]),
+        "gr_server_fail_allocs": (i32, [vp, i32]),
         "gr_server_pending": (i32, [vp, ctypes.POINTER(sz), ctypes.POINTER(sz), ctypes.POINTER(sz)]),
         "gr_server_now": (ctypes.c_double, []),
         "gr_server_destroy": (i32, [vp]),

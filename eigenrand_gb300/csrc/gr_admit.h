@@ -60,6 +60,16 @@ class Admission {
     return out;
   }
 
+  // drops a queued (not yet admitted) request; false if it is not queued
+  bool cancel(uint64_t ticket) {
+    for (auto it = queue_.begin(); it != queue_.end(); ++it)
+      if (it->ticket == ticket) {
+        queue_.erase(it);
+        return true;
+      }
+    return false;
+  }
+
   // the request's GPU work is done: its slot and its client are free again
   void finish(int client) {
     busy_[client] = 0;

@@ -7,6 +7,7 @@
 // stream-ordered memory pool reserved for the server.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <deque>
@@ -40,9 +41,12 @@ struct ServeReq {
   uint64_t gen = 0;   // scalars generated (count rounded up)
   uint64_t units = 0; // value passed to the sampling call (samples for MvNormal)
   size_t bytes = 0;
+  size_t charged = 0;  // bytes held in the admission budget (from admission to release)
   void* dev_out = nullptr;
   int slot = -1;
   int state = kQueued;
+  bool cancelled = false;  // running when cancelled: freed and reported as such on completion
+  bool reported = false;
   gr_status status = GR_OK;
   double admitted = 0, completed = 0;
 };
@@ -71,6 +75,7 @@ struct gr_server {
   std::deque<uint64_t> done;  // finished, not yet reported
   uint64_t next_ticket = 1;
   size_t held = 0;
+  int fail_allocs = 0;  // test hook: allocations left to fail
 };
 
 extern "C" {
@@ -219,6 +224,16 @@ gr_status gr_server_progress(gr_server* s, gr_completion* done, size_t cap, size
     q.completed = gr_server_now();
     q.state = kDone;
     if (e != cudaSuccess) q.status = sfail(GR_ERR_CUDA, std::string("request: ") + cudaGetErrorString(e));
+    if (q.cancelled) {  // its work is done: the result goes straight back
+      q.status = GR_ERR_CANCELLED;
+      if (q.dev_out) {
+        cudaFreeAsync(q.dev_out, s->rel);
+        q.dev_out = nullptr;
+        s->held -= q.bytes;
+      }
+      s->adm->release(q.charged);
+      q.charged = 0;
+    }
     s->slot_ticket[i] = 0;
     s->free_slots.push_back((int)i);
     s->adm->finish(q.r.client);
@@ -233,8 +248,13 @@ gr_status gr_server_progress(gr_server* s, gr_completion* done, size_t cap, size
     cudaStream_t st = s->streams[slot];
     q.slot = slot;
     q.admitted = now;
+    q.charged = q.bytes;
     gr_status rs = GR_OK;
-    if (cudaMallocFromPoolAsync(&q.dev_out, q.bytes, s->pool, st) != cudaSuccess) {
+    if (s->fail_allocs > 0) {
+      --s->fail_allocs;
+      q.dev_out = nullptr;
+      rs = sfail(GR_ERR_NOMEM, "device memory pool exhausted (test hook)");
+    } else if (cudaMallocFromPoolAsync(&q.dev_out, q.bytes, s->pool, st) != cudaSuccess) {
       cudaGetLastError();
       q.dev_out = nullptr;
       rs = sfail(GR_ERR_NOMEM, "device memory pool exhausted");
@@ -270,7 +290,8 @@ gr_status gr_server_progress(gr_server* s, gr_completion* done, size_t cap, size
   // report
   size_t n = 0;
   while (n < cap && !s->done.empty() && done) {
-    const ServeReq& q = s->reqs[s->done.front()];
+    ServeReq& q = s->reqs[s->done.front()];
+    q.reported = true;
     gr_completion& c = done[n++];
     c.ticket = q.ticket;
     c.status = q.status;
@@ -307,8 +328,61 @@ gr_status gr_server_release(gr_server* s, uint64_t ticket) {
     SV_CUDA(cudaFreeAsync(q.dev_out, s->rel));
     s->held -= q.bytes;
   }
-  s->adm->release(q.bytes);
+  s->adm->release(q.charged);
   s->reqs.erase(it);
+  return GR_OK;
+}
+
+gr_status gr_server_cancel(gr_server* s, uint64_t ticket) {
+  if (!s) return sfail(GR_ERR_INVALID, "server is NULL");
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return sfail(GR_ERR_INVALID, "no such ticket");
+  ServeReq& q = it->second;
+  if (q.state == kQueued) {
+    // never admitted: nothing ran and nothing is held
+    s->adm->cancel(ticket);
+    q.state = kDone;
+    q.status = GR_ERR_CANCELLED;
+    q.completed = gr_server_now();
+    s->done.push_back(ticket);
+    return GR_OK;
+  }
+  if (q.state == kRunning) {
+    q.cancelled = true;
+    return GR_OK;
+  }
+  if (q.reported) return sfail(GR_ERR_INVALID, "the request was already reported (release it)");
+  // finished, not reported yet: its result goes back now, the report says cancelled
+  if (q.dev_out) {
+    SV_CUDA(cudaFreeAsync(q.dev_out, s->rel));
+    q.dev_out = nullptr;
+    s->held -= q.bytes;
+  }
+  s->adm->release(q.charged);
+  q.charged = 0;
+  q.status = GR_ERR_CANCELLED;
+  return GR_OK;
+}
+
+gr_status gr_server_cancel_client(gr_server* s, int32_t client) {
+  if (!s) return sfail(GR_ERR_INVALID, "server is NULL");
+  if (client < 0 || client >= s->nclients) return sfail(GR_ERR_INVALID, "no such client");
+  std::vector<uint64_t> mine;
+  for (const auto& kv : s->reqs)
+    if (kv.second.r.client == client && !kv.second.reported && !kv.second.cancelled &&
+        kv.second.status != GR_ERR_CANCELLED)
+      mine.push_back(kv.first);
+  std::sort(mine.begin(), mine.end());  // (admission only runs in gr_server_progress: any order would do)
+  for (uint64_t t : mine) {
+    const gr_status st = gr_server_cancel(s, t);
+    if (st != GR_OK) return st;
+  }
+  return GR_OK;
+}
+
+gr_status gr_server_fail_allocs(gr_server* s, int32_t n) {
+  if (!s || n < 0) return sfail(GR_ERR_INVALID, "bad argument");
+  s->fail_allocs = n;
   return GR_OK;
 }
 

@@ -87,6 +87,20 @@ class Server:
         _lib.check(_L.gr_server_release(self._h, ticket))
         self._dtype.pop(ticket, None)
 
+    def cancel(self, ticket):
+        """Cancel a request not reported yet: queued ones never run, running ones
+        finish on the GPU and are freed; reported later with status
+        GR_ERR_CANCELLED and ended by release() like any other."""
+        _lib.check(_L.gr_server_cancel(self._h, ticket))
+
+    def cancel_client(self, client):
+        """Cancel every unreported request of a client (a client that went away)."""
+        _lib.check(_L.gr_server_cancel_client(self._h, client))
+
+    def fail_allocs(self, n):
+        """Test hook: the next n result allocations fail (GR_ERR_NOMEM completions)."""
+        _lib.check(_L.gr_server_fail_allocs(self._h, n))
+
     def pending(self):
         q, r, b = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
         _lib.check(_L.gr_server_pending(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(b)))

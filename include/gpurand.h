@@ -48,7 +48,8 @@ typedef enum {
   GR_ERR_NOMEM = 4,        /* device allocation failed */
   GR_ERR_REJECT_LIMIT = 5, /* a rejection loop hit its iteration cap (device word) */
   GR_ERR_NOT_PD = 6,       /* covariance / scale matrix not positive definite */
-  GR_ERR_NAN_WEIGHT = 7    /* non-finite weight sum (AliasMethod, Discrete.h:88) */
+  GR_ERR_NAN_WEIGHT = 7,   /* non-finite weight sum (AliasMethod, Discrete.h:88) */
+  GR_ERR_CANCELLED = 8     /* a served request was cancelled (gr_server_cancel) */
 } gr_status;
 
 typedef enum { GR_F32 = 0, GR_F64 = 1, GR_I32 = 2, GR_U64 = 3 } gr_dtype;
@@ -381,8 +382,24 @@ gr_status gr_server_submit(gr_server* s, const gr_request* r, uint64_t* ticket);
 gr_status gr_server_progress(gr_server* s, gr_completion* done, size_t cap, size_t* ndone);
 /* copies a finished result to host memory (synchronous) */
 gr_status gr_server_read(gr_server* s, uint64_t ticket, void* host_dst, size_t bytes);
-/* gives a finished result's memory back to the budget */
+/* ends a reported request (any status): gives its memory back to the budget */
 gr_status gr_server_release(gr_server* s, uint64_t ticket);
+/* Cancels a request that has not been reported yet.  Queued: it is dropped
+ * and nothing runs, so the client's engine is not advanced (the client's
+ * later results equal its call sequence without it).  Running: the GPU work
+ * completes (its draws are consumed, as in the call sequence with it) and the
+ * result is freed when it does.  Either way the request is then reported by
+ * gr_server_progress with status GR_ERR_CANCELLED and no result, and is ended
+ * by gr_server_release like any other.  GR_ERR_INVALID if the ticket is
+ * unknown or its completion was already reported. */
+gr_status gr_server_cancel(gr_server* s, uint64_t ticket);
+/* gr_server_cancel for every unreported request of a client (a client that
+ * went away); its finished, reported results still need gr_server_release */
+gr_status gr_server_cancel_client(gr_server* s, int32_t client);
+/* test hook: the next n result allocations fail as if the server's memory
+ * pool were exhausted (those requests complete with GR_ERR_NOMEM, nothing
+ * runs for them and the client's engine is not advanced) */
+gr_status gr_server_fail_allocs(gr_server* s, int32_t n);
 gr_status gr_server_pending(const gr_server* s, size_t* queued, size_t* running, size_t* bytes_held);
 double gr_server_now(void);
 gr_status gr_server_destroy(gr_server* s);

@@ -88,6 +88,26 @@ int main() {
     CHECK(!a.submit(AdmitReq{2, 5, 1, 0.0}));
     CHECK(a.queued() == 0);
   }
+  {  // cancel: a queued request leaves the queue and is never admitted; the
+     // client's later request then goes ahead; admitted ones are not queued
+    Admission a(2, 100, 4, 1.0);
+    a.submit(AdmitReq{1, 0, 10, 0.0});
+    a.submit(AdmitReq{2, 0, 20, 0.0});
+    a.submit(AdmitReq{3, 0, 30, 0.0});
+    a.submit(AdmitReq{4, 1, 10, 0.0});
+    CHECK(a.cancel(2));
+    CHECK(!a.cancel(2));   // already gone
+    CHECK(!a.cancel(99));  // unknown
+    CHECK(a.queued() == 3);
+    auto t = tickets(a.admit(0.0));
+    CHECK(t.size() == 2 && t[0] == 1 && t[1] == 4);
+    CHECK(!a.cancel(1));  // running: not in the queue
+    CHECK(a.used() == 20);
+    a.finish(0);
+    t = tickets(a.admit(0.0));
+    CHECK(t.size() == 1 && t[0] == 3);
+    CHECK(a.used() == 50 && a.queued() == 0);
+  }
   if (fails) return 1;
   std::printf("admission checks passed\n");
   return 0;
