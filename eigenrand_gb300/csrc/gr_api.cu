@@ -1961,6 +1961,57 @@ gr_status sengine_reject(gr_sengine* se, const DistParams& dp, int rk, void* out
   return bail(GR_OK);
 }
 
+// BetaGen / FisherFGen on a scalar engine, a fresh generator (the free
+// functions): the chain of k_sx_beta over chunks of the engine's words, the
+// carried lanes of GammaGen(a), GammaGen(b) and the beta's own loop starting
+// empty and dropped after the call
+gr_status sengine_beta(gr_sengine* se, const DistParams& dp, void* out, size_t n, cudaStream_t s) {
+  const int64_t P = dp.dtype == GR_F32 ? 8 : 4;
+  if (n % (size_t)P)
+    return fail(GR_ERR_INVALID, "size must be a multiple of " + std::to_string(P) + " (the reference packet width)");
+  if (n == 0) return GR_OK;
+  if (!out) return fail(GR_ERR_INVALID, "output is NULL");
+  const int64_t npk = (int64_t)(n / (size_t)P);
+  const size_t es = dp.dtype == GR_F32 ? 4 : 8;
+  SxBetaArgs a{};
+  a.beta = dp;
+  if (!dp.ic) {  // GammaGen(a), GammaGen(b) with the parameters in the scalar type (NormalExp.h:914-917)
+    for (int c = 0; c < 2; ++c) {
+      gr_dist_desc gd{};
+      gd.kind = GR_GAMMA;
+      gd.dtype = dp.dtype;
+      gd.a = dp.dtype == GR_F32 ? (double)(c == 0 ? dp.fa : dp.fb) : (c == 0 ? dp.da : dp.db);
+      gd.b = 1.0;
+      const gr_status st = make_params(gd, a.g[c]);
+      if (st != GR_OK) return st;
+    }
+  }
+  char* buf = nullptr;
+  const size_t carry_bytes = sizeof(uint64_t) * 3 * 2 * (size_t)P;
+  GR_CUDA(cudaMallocAsync(&buf, carry_bytes + 64, s));
+  a.carry = reinterpret_cast<uint64_t*>(buf);
+  a.cnt = reinterpret_cast<int32_t*>(buf + carry_bytes);
+  a.res = reinterpret_cast<int64_t*>(buf + carry_bytes + 32);
+  cudaError_t err = cudaMemsetAsync(buf, 0, carry_bytes + 64, s);
+  if (err != cudaSuccess) {
+    cudaFreeAsync(buf, s);
+    return cuda_fail(err, "scalar engine carry");
+  }
+  // words per output packet: about two uniform packets per gamma, or per
+  // trial of the a, b < 1 loop, of 3 (float) or 4 (double) draws
+  const gr_status st = sengine_chain(
+      se, npk, dp.dtype == GR_F32 ? 24 : 32,
+      [&](const uint64_t* w, int64_t W, int64_t done, int64_t* res) {
+        a.out = static_cast<char*>(out) + (size_t)done * P * es;
+        a.npk = npk - done;
+        a.res = res;
+        return launch_sx_beta(w, W, a, dp.dtype, s);
+      },
+      s);
+  cudaFreeAsync(buf, s);
+  return st;
+}
+
 // PoissonGen / BinomialGen (int32) on a scalar engine: a fresh generator, so
 // CompressMask's carried lanes start empty and are dropped after the call
 gr_status sengine_int(gr_sengine* se, const DistParams& dp, void* out, size_t n, cudaStream_t s) {
@@ -2089,6 +2140,7 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
     return sengine_int(se, dp, dev_out, n, s);
   if (dp.kind == GR_GAMMA && reject_code(dp) >= 0 && family_of(dp) == Family::Reject)
     return sengine_reject(se, dp, reject_code(dp), dev_out, n, s);
+  if (dp.kind == GR_BETA && dp.dtype != GR_I32) return sengine_beta(se, dp, dev_out, n, s);
   if (dp.dtype != GR_I32 && family_of(dp) == Family::Staged && (dp.kind == GR_GAMMA || dp.kind == GR_STUDENT_T)) {
     // a fixed run of U uniform packets per output packet: all words at once
     const int U = dp.kind == GR_GAMMA ? dp.ib : 2;
@@ -2111,8 +2163,8 @@ gr_status gr_sengine_sample(gr_sengine* se, const gr_dist_desc* desc, void* dev_
   if (wpp == 0 || (dp.kind == GR_GAMMA && dp.ia != 1))
     return fail(GR_ERR_UNSUPPORTED, "scalar engines: the fixed-draw kinds only (uniformReal, balanced, normal, "
                                     "lognormal, exponential, cauchy, weibull, extremeValue, gamma(1), bernoulli, "
-                                    "randBits), gamma, chiSquared, studentT, poisson, binomial, negativeBinomial, uniformInt, geometric "
-                                    "and discrete");
+                                    "randBits), gamma, chiSquared, studentT, beta, fisherF, poisson, binomial, "
+                                    "negativeBinomial, uniformInt, geometric and discrete");
   const int64_t P = kind_granule(dp.kind, dp.dtype);
   // a partial last packet: the scalar operator(), one draw per element (the
   // kinds whose scalar form is exact bit arithmetic)

@@ -185,6 +185,20 @@ cudaError_t launch_sx_cand(int rk, int dtype, const uint64_t* w, int64_t M, cons
                            cudaStream_t s);
 // GammaGen with integral alpha < 20 (U = alpha uniform packets per output
 // packet) and StudentTGen (U = 2) on a scalar engine's pre-drawn words.
+// BetaGen / FisherFGen on a scalar engine (gr_samplers.cu, k_sx_beta): one
+// warp over a chunk of W pre-drawn words; carry: 3 x (2 P) carried lanes and
+// cnt: 3 counts (GammaGen(a), GammaGen(b), the beta's own), device, updated;
+// res: packets completed, draws they used.
+struct SxBetaArgs {
+  DistParams beta;  // the BetaGen's parameters (ic: a < 1 and b < 1; post: FisherF map)
+  DistParams g[2];  // GammaGen(a), GammaGen(b) in the scalar type (general branch)
+  void* out;
+  int64_t npk;
+  uint64_t* carry;
+  int32_t* cnt;
+  int64_t* res;
+};
+cudaError_t launch_sx_beta(const uint64_t* w, int64_t W, const SxBetaArgs& a, int dtype, cudaStream_t s);
 cudaError_t launch_sx_staged(const uint64_t* w, void* out, int64_t npk, const DistParams& d, int U,
                              cudaStream_t s);
 cudaError_t launch_int_words(const uint64_t* w, int64_t nwords, const DistParams& d, int32_t* out, int64_t npk,

@@ -553,6 +553,188 @@ cudaError_t launch_sx_cand(int rk, int dtype, const uint64_t* w, int64_t M, cons
   return cudaGetLastError();
 }
 
+// BetaGen / FisherFGen drawn with a scalar engine (std::mt19937_64,
+// P8_mt19937_64) as the Urng, a fresh generator (the free functions;
+// NormalExp.h:949-976, 1016-1021).  The draws are a chain: in the general
+// branch every output packet is GammaGen(a)'s packetOp then GammaGen(b)'s,
+// each a CompressMask loop with its own carried lanes when it rejects, so
+// one warp walks it over a chunk of pre-drawn 64-bit words, lane j computing
+// packet lane j with the same per-lane expressions as the packet engine's
+// kernels (rej_trial; the exponential for alpha = 1; the product of alpha
+// uniforms for an integral alpha < 20).  The a, b < 1 branch is the beta's
+// own CompressMask loop over pairs of uniform packets; its mask is carried
+// explicitly (an accepted lane may be 0/0).  A float uniform packet is three
+// draws (rawbits_34), a double packet four.  The carried lanes are
+// snapshotted at every completed output packet: the launch reports the
+// packets it completed and the draws they used, and leaves the carried
+// lanes as of that point, so the next chunk continues exactly there.
+template <int DT>
+__global__ void __launch_bounds__(32) k_sx_beta(const uint64_t* w, int64_t W, SxBetaArgs a) {
+  constexpr int P = DT == SD_F32 ? 8 : 4;
+  constexpr int64_t DPK = DT == SD_F32 ? 3 : 4;  // draws per uniform packet
+  constexpr unsigned kFull = (1u << P) - 1u;
+  const int lane = threadIdx.x;
+  __shared__ uint64_t cache[3][2 * P], snap[3][2 * P];
+  __shared__ int s_cnt[3], s_snap[3];
+  for (int c = 0; c < 3; ++c) {
+    if (lane < 2 * P) cache[c][lane] = snap[c][lane] = a.carry[c * 2 * P + lane];
+    if (lane == 0) s_cnt[c] = s_snap[c] = a.cnt[c];
+  }
+  __syncwarp();
+  int64_t pos = 0, used = 0, done = 0;  // draws consumed; by completed packets; packets completed
+
+  // lane wi & 7 of float uniform packet wi >> 3 at draw offset pos (rawbits_34
+  // of three draws a, b, c: c.lo, c.hi, b.lo, top bytes, b.hi, a.lo, a.hi, top bytes)
+  auto word = [&](int64_t wi) -> uint32_t {
+    const uint64_t* q = w + pos + 3 * (wi >> 3);
+    const uint32_t v[6] = {(uint32_t)q[2], (uint32_t)(q[2] >> 32), (uint32_t)q[1], (uint32_t)(q[1] >> 32),
+                           (uint32_t)q[0], (uint32_t)(q[0] >> 32)};
+    switch (wi & 7) {
+      case 0: return v[0];
+      case 1: return v[1];
+      case 2: return v[2];
+      case 3: return (v[0] >> 24) | ((v[1] >> 24) << 8) | ((v[2] >> 24) << 16) | ((v[2] >> 24) << 24);
+      case 4: return v[3];
+      case 5: return v[4];
+      case 6: return v[5];
+      default: return (v[3] >> 24) | ((v[4] >> 24) << 8) | ((v[5] >> 24) << 16) | ((v[5] >> 24) << 24);
+    }
+  };
+  // lane r & 3 of double uniform packet r >> 2 at draw offset pos (rawbits: four draws in order)
+  auto rval = [&](int64_t r) -> uint64_t { return w[pos + r]; };
+
+  // CompressMask::compress_append over lanes 0 .. P-1 into carried set c
+  // (arch/AVX/PacketFilter.h:147-184): a full packet is returned as it is;
+  // otherwise the accepted lanes join the carried ones and the first P leave
+  auto compress = [&](int c, uint64_t bits, bool acc, uint64_t& res) -> bool {
+    const unsigned m = __ballot_sync(0xffffffffu, acc && lane < P) & kFull;
+    if (m == kFull) {
+      res = bits;
+      return true;
+    }
+    int fc = s_cnt[c];
+    if (lane < P && ((m >> lane) & 1u)) cache[c][fc + __popc(m & ((1u << lane) - 1u))] = bits;
+    fc += __popc(m);
+    __syncwarp();
+    if (fc < P) {
+      if (lane == 0) s_cnt[c] = fc;
+      __syncwarp();
+      return false;
+    }
+    res = lane < P ? cache[c][lane] : 0;
+    const uint64_t mv = lane < fc - P ? cache[c][P + lane] : 0;
+    __syncwarp();
+    if (lane < fc - P) cache[c][lane] = mv;
+    if (lane == 0) s_cnt[c] = fc - P;
+    __syncwarp();
+    return true;
+  };
+
+  // GammaGen(alpha)'s packetOp for component c (0: a, 1: b); false when the
+  // chunk runs out first
+  auto gamma_packet = [&](int c, uint64_t& v) -> bool {
+    const DistParams& g = a.g[c];
+    if (g.ic) {  // alpha < 1: GS rejection, three uniform packets per trial
+      for (;;) {
+        if (pos + 3 * DPK > W) return false;
+        uint64_t cb = 0;
+        const bool acc = lane < P && rej_trial<RK_GAMMA_GS, DT>(g, 0, lane, word, rval, cb);
+        pos += 3 * DPK;
+        if (compress(c, cb, acc, v)) return true;
+      }
+    }
+    if (g.ia) {  // alpha == 1: beta * ExponentialGen
+      if (pos + DPK > W) return false;
+      if (lane < P) {
+        if (DT == SD_F32) {
+          v = f2u(g.fb * (-(logf_(1.0f - ur_f(word(lane))) / 1.0f)));
+        } else {
+          const double l = -(log_(one_minus_ur_d(rval(lane))) / 1.0);
+          v = d2u((g.flags & kParamUnitScale) ? l : g.db * l);
+        }
+      }
+      pos += DPK;
+      return true;
+    }
+    if (g.ib >= 2) {  // integral alpha < 20: product of alpha nonzero uniforms
+      if (pos + g.ib * DPK > W) return false;
+      if (lane < P) {
+        if (DT == SD_F32) {
+          float y = ur_f(word(lane)) + 1.1920928955078125e-07f / 8;
+          for (int t = 1; t < g.ib; ++t) y = y * (ur_f(word(8 * t + lane)) + 1.1920928955078125e-07f / 8);
+          v = f2u(-(g.fb * logf_(y)));
+        } else {
+          double y = ur_d(rval(lane)) + 2.220446049250313e-16 / 8;
+          for (int t = 1; t < g.ib; ++t) y = y * (ur_d(rval(4 * t + lane)) + 2.220446049250313e-16 / 8);
+          const double l = log_(y);
+          v = d2u((g.flags & kParamUnitScale) ? -l : -(g.db * l));
+        }
+      }
+      pos += g.ib * DPK;
+      return true;
+    }
+    for (;;) {  // the tan proposal, two uniform packets per trial
+      if (pos + 2 * DPK > W) return false;
+      uint64_t cb = 0;
+      const bool acc = lane < P && rej_trial<RK_GAMMA_TAN, DT>(g, 0, lane, word, rval, cb);
+      pos += 2 * DPK;
+      if (compress(c, cb, acc, v)) return true;
+    }
+  };
+
+  while (done < a.npk) {
+    uint64_t v = 0;
+    bool ok = true;
+    if (a.beta.ic) {  // a < 1 and b < 1: the beta's own rejection loop
+      for (;;) {
+        if (pos + 2 * DPK > W) {
+          ok = false;
+          break;
+        }
+        uint64_t cb = 0;
+        const bool acc = lane < P && rej_trial<RK_BETA_SMALL, DT>(a.beta, 0, lane, word, rval, cb);
+        pos += 2 * DPK;
+        if (compress(2, cb, acc, v)) break;
+      }
+    } else {
+      uint64_t p1 = 0, p2 = 0;
+      ok = gamma_packet(0, p1) && gamma_packet(1, p2);
+      if (ok) {
+        if (DT == SD_F32) v = f2u(u2f((uint32_t)p1) / (u2f((uint32_t)p1) + u2f((uint32_t)p2)));
+        else v = d2u(u2d(p1) / (u2d(p1) + u2d(p2)));
+      }
+    }
+    if (!ok) break;
+    v = beta_post<DT == SD_F64>(v, a.beta);
+    if (lane < P) {
+      if (DT == SD_F32) static_cast<uint32_t*>(a.out)[done * P + lane] = (uint32_t)v;
+      else static_cast<uint64_t*>(a.out)[done * P + lane] = v;
+    }
+    ++done;
+    used = pos;
+    for (int c = 0; c < 3; ++c) {
+      if (lane < 2 * P) snap[c][lane] = cache[c][lane];
+      if (lane == 0) s_snap[c] = s_cnt[c];
+    }
+    __syncwarp();
+  }
+  // the carried lanes as of the last completed packet
+  for (int c = 0; c < 3; ++c) {
+    if (lane < 2 * P) a.carry[c * 2 * P + lane] = snap[c][lane];
+    if (lane == 0) a.cnt[c] = s_snap[c];
+  }
+  if (lane == 0) {
+    a.res[0] = done;
+    a.res[1] = used;
+  }
+}
+
+cudaError_t launch_sx_beta(const uint64_t* w, int64_t W, const SxBetaArgs& a, int dtype, cudaStream_t s) {
+  if (dtype == GR_F32) k_sx_beta<SD_F32><<<1, 32, 0, s>>>(w, W, a);
+  else k_sx_beta<SD_F64><<<1, 32, 0, s>>>(w, W, a);
+  return cudaGetLastError();
+}
+
 template <int RK, int DT>  // DT: SD_F32 (P=8), SD_F64 (P=4), SD_I32H (P=4, float internals)
 __global__ void __maxnreg__(64) k_reject(Plan p, DistParams d, int64_t max_blocks) {
   constexpr int P = DT == SD_F32 ? 8 : 4;

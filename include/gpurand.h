@@ -216,13 +216,13 @@ gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* 
  * 4 per double packet, 2 per half packet, in the order GCC evaluates the
  * intrinsics' arguments (right to left).
  *   gr_sengine_raw_u64: rng() n times.
- *   gr_sengine_sample: a fresh generator (the free functions) of uniformReal,
- *     balanced, normal, lognormal, exponential, cauchy, weibull,
- *     extremeValue, gamma, chiSquared, studentT, bernoulli; for int32
- *     randBits, bernoulli, geometric, discrete, uniformInt, poisson,
- *     binomial and negativeBinomial.  The data-dependent kinds run their single chain over chunks
- *     of pre-drawn words and synchronise the stream once per chunk.  Other
- *     kinds (beta, fisherF) return GR_ERR_UNSUPPORTED. */
+ *   gr_sengine_sample: a fresh generator (the free functions) of every
+ *     univariate kind: uniformReal, balanced, normal, lognormal, exponential,
+ *     cauchy, weibull, extremeValue, gamma, chiSquared, studentT, beta,
+ *     fisherF, bernoulli; for int32 randBits, bernoulli, geometric,
+ *     discrete, uniformInt, poisson, binomial and negativeBinomial.  The
+ *     data-dependent kinds run their single chain over chunks of pre-drawn
+ *     words and synchronise the stream once per chunk. */
 typedef struct gr_sengine gr_sengine;
 typedef enum { GR_SCALAR_MT19937_64 = 1, GR_SCALAR_P8_MT19937_64 = 2 } gr_scalar_engine_kind;
 gr_status gr_sengine_create(gr_sengine** out, int32_t kind, uint64_t seed);

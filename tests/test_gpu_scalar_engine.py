@@ -89,8 +89,6 @@ def test_scalar_engine_randbits_and_mirror(er, oracle, okind, cls):
     x = mem(er.ExponentialGen(2.0, dtype=torch.float64).generate(32, 32, u))
     assert_bits_equal(x, o.generate(oracle.Gen(), "EXPONENTIAL", 1024, np.float64, 2.0), "object mirror")
     with pytest.raises(er.GrError):
-        er.beta(8, 1, u, 0.5, 2.0)  # not built for scalar engines
-    with pytest.raises(er.GrError):
         er.NormalGen().generate(8, 1, u)
 
 
@@ -181,6 +179,45 @@ def test_scalar_engine_gamma_rejection(er, oracle, okind, cls, tdt):
         ref = o.generate(oracle.Gen(), "STUDENT_T", 96 * 32, npt, nu)
         assert_bits_equal(mem(got), ref, f"{cls} studentT({nu}) {tdt}")
     assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after the staged kinds")
+
+
+BETAS = [(0.5, 0.7), (0.2, 0.9), (0.5, 2.0), (2.5, 3.5), (1.0, 2.5), (2.0, 3.0), (0.3, 1.0), (7.3, 0.8)]
+
+
+@pytest.mark.parametrize("tdt", [torch.float32, torch.float64])
+@pytest.mark.parametrize("okind,cls", ENGINES, ids=["mt", "p8"])
+def test_scalar_engine_beta_fisherf(er, oracle, okind, cls, tdt):
+    """beta() and fisherF() with a scalar engine (a fresh BetaGen per call):
+    the a, b < 1 rejection loop, and the general branch's GammaGen(a) then
+    GammaGen(b) per output packet on every gamma branch (GS, alpha = 1,
+    integral alpha, the tan proposal), each with its own carried lanes; the
+    engine continues exactly after each call."""
+    npt = np.float32 if tdt == torch.float32 else np.float64
+    u = getattr(er, cls)(41)
+    o = oracle.ScalarEngine(okind, 41)
+    for a, b in BETAS:
+        for rows, cols in ((8, 1), (256, 96)):
+            got = er.beta(rows, cols, u, a, b, dtype=tdt)
+            ref = o.generate(oracle.Gen(), "BETA", rows * cols, npt, a, b)
+            assert_bits_equal(mem(got), ref, f"{cls} beta({a}, {b}) {tdt} {rows}x{cols}")
+        assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after beta({a}, {b})")
+    for m, n in ((1.0, 1.5), (5.0, 2.0), (10.0, 12.0)):
+        got = er.fisherF(128, 64, u, m, n, dtype=tdt)
+        ref = o.generate(oracle.Gen(), "FISHER_F", 128 * 64, npt, m, n)
+        assert_bits_equal(mem(got), ref, f"{cls} fisherF({m}, {n}) {tdt}")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), f"{cls} raw after fisherF")
+
+
+def test_scalar_engine_beta_multichunk(er, oracle):
+    """Calls whose chain outruns its first chunk of words: the carried lanes
+    of both gammas (and of the a, b < 1 loop) continue into the next chunk."""
+    u = er.mt19937_64(6)
+    o = oracle.ScalarEngine("mt19937_64", 6)
+    for a, b, n in ((0.9, 0.8, 8 * 1_500_000), (0.4, 2.5, 8 * 1_000_000)):  # > 2^24 words each
+        got = er.beta(n, 1, u, a, b)
+        ref = o.generate(oracle.Gen(), "BETA", n, np.float32, a, b)
+        assert_bits_equal(mem(got), ref, f"beta({a}, {b}) multi-chunk")
+    assert_bits_equal(u.raw(3).cpu().numpy().view(np.uint64), o.raw(3), "raw after")
 
 
 def test_scalar_engine_gamma_multichunk(er, oracle):
