@@ -117,6 +117,12 @@ cudaError_t launch_mvn(const float* Lf, int tri, const float* mean, float* X, in
 // X 16-byte aligned, fewer than 2^31 samples); device errors go to *status.
 constexpr int kUmmaMaxDim = 256;
 constexpr int kUmmaAutoMinDim = 20;  // smallest dim the tcgen05 product is used for by default
+// WishartGen<float> (not inverse) Bartlett products T = L A, W = T T^T on
+// tcgen05 (gr_umma.cu), dims up to kWishUmmaMaxDim; device errors go to *status
+constexpr int kWishUmmaMaxDim = 64;
+bool wishart_umma_usable(int d, int dtype, int inverse);
+cudaError_t launch_wishart_umma(const float* normals, const float* chis, const float* chol, float* out, int d,
+                                int64_t samples, int32_t* status, cudaStream_t s);
 int umma_padded_dim(int d);
 int umma_chunks(int d);
 size_t umma_prep_floats(int d, int tri);

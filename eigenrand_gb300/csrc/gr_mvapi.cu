@@ -470,8 +470,16 @@ gr_status gr_wishart_sample(gr_wishart* g, gr_engine* e, void* dev_out, size_t s
     st = gr_generate(g->chis[i], e, chis + (size_t)i * samples * es, samples, stream);
     if (st != GR_OK) return st;
   }
-  cudaError_t err = launch_wishart(normals, chis, g->chol, dev_out, d, (int64_t)samples, g->inverse, g->dtype,
-                                   (cudaStream_t)stream);
+  // the tcgen05 products for float WishartGen up to dim 64; test hook
+  // GR_WISHART_PRODUCT=mma_sync picks the mma.sync form
+  bool umma = wishart_umma_usable(d, g->dtype, g->inverse);
+  if (const char* pv = std::getenv("GR_WISHART_PRODUCT"))
+    if (std::strcmp(pv, "mma_sync") == 0) umma = false;
+  cudaError_t err = umma ? launch_wishart_umma((const float*)normals, (const float*)chis, (const float*)g->chol,
+                                               (float*)dev_out, d, (int64_t)samples, &engine_state_ptr(e)->status,
+                                               (cudaStream_t)stream)
+                         : launch_wishart(normals, chis, g->chol, dev_out, d, (int64_t)samples, g->inverse, g->dtype,
+                                          (cudaStream_t)stream);
   if (err != cudaSuccess) return mv_fail(GR_ERR_CUDA, std::string("Wishart products: ") + cudaGetErrorString(err));
   return GR_OK;
 }

@@ -80,6 +80,10 @@ constexpr uint32_t kItemFirst = 1, kItemLast = 2;       // first / last item of 
 // byte offset 128 (the K-adjacent core matrix), stride byte offset 1024 (the
 // next 8-row group), version 1; the start address (>> 4) is added in.
 constexpr uint64_t kDescConst = ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46);
+// the same with another stride byte offset (8-row group pitch)
+__host__ __device__ constexpr uint64_t kDescConstW(uint32_t sbo) {
+  return ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -658,6 +662,316 @@ __global__ void __launch_bounds__(kThreads, 1) k_mvn_umma(const __grid_constant_
     asm volatile("tcgen05.fence::after_thread_sync;");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
   }
+}
+
+// ============================================================================
+// WishartGen<float> (not inverse) Bartlett products on tcgen05, dims up to 64
+// (MvNormal.h:236-277): per draw j, A_j = strictly-lower normals (column by
+// column) + diagonal sqrt(chi^2(df - i)), T_j = L A_j, W_j = T_j T_j^T.
+// Draws are stacked along M: a tile holds G = 128 / p draws, p the dim
+// rounded up to a power of two (16, 32 or 64), 128 threads, lane (g, i) =
+// thread g p + i.
+//   1. lane (g, i) writes column i of A_g (its tf32 high and low parts) into
+//      tensor memory: row (g, i) of the stacked A^T;
+//   2. T^T = A^T L^T: tcgen05.mma, A from tensor memory, B = L (rows of L,
+//      K-major, high and low parts resident in shared memory); accumulator
+//      row (g, i), column r = T_g[r][i];
+//   3. the accumulator is read back (tcgen05.ld) and written transposed into
+//      shared memory as S[(g, r)][i] = T_g[r][i], split into tf32 parts,
+//      K-major canonical layout;
+//   4. S S^T: one M = 128, N = 128 product whose diagonal p x p blocks are
+//      the draws' W_g (the cross blocks are not used);
+//   5. lane (g, r) reads its draw's block of row (g, r) and stores W_g's
+//      column-major elements (coalesced along r).
+// 3xTF32 with FP32 accumulation in both products, as the mma.sync form.
+namespace {
+
+__device__ __forceinline__ void mma_tf32_ss(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_tf32_ts1(uint32_t dtmem, uint32_t atmem, uint64_t b, uint32_t idesc,
+                                             uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "r"(atmem), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit1(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+constexpr int kWishUThreads = 128;
+
+// Wait for an MMA commit by polling mbarrier.test_wait (non-blocking) from
+// lane 0 of each warp; bounded like mbar_wait.
+__device__ __forceinline__ bool wish_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int32_t* status) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    uint32_t done = 0;
+    unsigned long long t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+      asm volatile(
+          "{\n\t.reg .pred p;\n\t"
+          "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}\n"
+          : "=r"(done)
+          : "r"(smem_u32(bar)), "r"(parity)
+          : "memory");
+      if (done) break;
+      if ((it & 255) == 0) {
+        if (it == 0) t0 = gtimer();
+        if (*abort) {
+          ok = 0;
+          break;
+        }
+        if (gtimer() - t0 > kWaitNs) {
+          *abort = 1;
+          atomicOr(status, (int)GR_DEV_MMA_TIMEOUT);
+          ok = 0;
+          break;
+        }
+      }
+    }
+  }
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kWishUThreads)
+    k_wishart_umma(const float* __restrict__ normals, const float* __restrict__ chis, const float* __restrict__ chol,
+                   float* __restrict__ out, int d, int dp, int64_t samples, int32_t* status) {
+  extern __shared__ __align__(1024) unsigned char wu_dyn[];
+  unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)wu_dyn + 1023) & ~(uintptr_t)1023);
+  float* Bhi = reinterpret_cast<float*>(base);  // L: dp rows x dp k
+  float* Blo = Bhi + dp * dp;
+  float* Xhi = Blo + dp * dp;  // A^T of the tile (128 rows x dp k), then S (stacked T)
+  float* Xlo = Xhi + 128 * dp;
+  float* stage0 = Xlo + 128 * dp;  // the tile's normals (G draws, contiguous in HBM), double buffered
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int G = 128 / dp;
+  const uint32_t SBO = (uint32_t)dp * 32;  // bytes between 8-row groups: dp/4 core matrices of 128 bytes
+  auto koff = [&](int row, int k) -> uint32_t {
+    return ((uint32_t)(row >> 3) * SBO + (uint32_t)(k >> 2) * 128u + (uint32_t)(row & 7) * 16u + (uint32_t)(k & 3) * 4u) >> 2;
+  };
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                 "r"(128u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  // the factor's rows: B[r][k] = L[r][k] (chol column-major), zero outside d x d
+  for (int t = tid; t < dp * dp; t += kWishUThreads) {
+    const int r = t / dp, k = t % dp;
+    const float x = (r < d && k < d) ? chol[(size_t)k * d + r] : 0.0f;
+    float hi, lo;
+    split_tf32(x, hi, lo);
+    Bhi[koff(r, k)] = hi;
+    Blo[koff(r, k)] = lo;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = s_tmem;
+  const uint32_t lane_addr = (uint32_t)(32 * warp) << 16;
+  // tensor memory (128 columns): S S^T; T^T lives in its first dp columns
+  // until the second product overwrites them
+  const int g = tid / dp, i = tid % dp;
+  const int64_t nper = (int64_t)d * (d - 1) / 2;
+  const int64_t ntiles = (samples + G - 1) / G;
+  const uint32_t idesc1 = umma_idesc_tf32(128, dp), idesc2 = umma_idesc_tf32(128, 128);
+  const uint64_t dsc = kDescConstW(SBO);
+  const uint64_t bh = dsc | (uint64_t)(smem_u32(Bhi) >> 4), bl = dsc | (uint64_t)(smem_u32(Blo) >> 4);
+  const uint64_t xh = dsc | (uint64_t)(smem_u32(Xhi) >> 4), xl = dsc | (uint64_t)(smem_u32(Xlo) >> 4);
+  const int stage_len = (G * (int)nper + 3) & ~3;
+  float* stages[2] = {stage0, stage0 + stage_len};
+  // a tile's normals into a stage buffer with cp.async (4-byte copies: the
+  // tile's start need not be 16-byte aligned); lands while the previous tile
+  // is processed
+  auto prefetch = [&](int64_t t, float* dst) {
+    if (t < ntiles) {
+      const int64_t j0 = t * G, nd = (samples - j0 < G ? samples - j0 : G);
+      const int cnt = (int)(nd * nper);
+      const float* src = normals + j0 * nper;
+      for (int q = tid; q < cnt; q += kWishUThreads)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst + q)), "l"(src + q) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  prefetch(blockIdx.x, stages[0]);
+  int sb = 0;
+  uint32_t phase = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles && !s_abort; tile += gridDim.x) {
+    const int64_t j = tile * G + g;
+    const bool jok = j < samples;
+    const float diag = (jok && i < d) ? sqrtf(chis[(int64_t)i * samples + j]) : 0.0f;
+    // ---- 1. this tile's normals (prefetched), the next tile's on their way,
+    // then row (g, i) of the stacked A^T = column i of A_g, tf32 parts, into
+    // shared memory
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    prefetch(tile + gridDim.x, stages[sb ^ 1]);
+    const float* stage = stages[sb];
+    sb ^= 1;
+    const int nb = g * (int)nper + i * (d - 1) - i * (i - 1) / 2;  // its normals start here in the stage
+    for (int k0 = 0; k0 < dp; k0 += 4) {
+      float4 h, l;
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = k0 + q;
+        v[q] = 0.0f;
+        if (jok && i < d && k < d) {
+          if (k > i) v[q] = stage[nb + (k - i - 1)];
+          else if (k == i) v[q] = diag;
+        }
+      }
+      split_tf32(v[0], h.x, l.x);
+      split_tf32(v[1], h.y, l.y);
+      split_tf32(v[2], h.z, l.z);
+      split_tf32(v[3], h.w, l.w);
+      *reinterpret_cast<float4*>(Xhi + koff(tid, k0)) = h;
+      *reinterpret_cast<float4*>(Xlo + koff(tid, k0)) = l;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    // ---- 2. T^T = A^T L^T
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      for (int ks = 0; ks < dp / 8; ++ks) {
+        const uint64_t o = 16u * (uint64_t)ks;
+        mma_tf32_ss(tmem, xl + o, bh + o, idesc1, ks > 0 ? 1u : 0u);
+        mma_tf32_ss(tmem, xh + o, bl + o, idesc1, 1u);
+        mma_tf32_ss(tmem, xh + o, bh + o, idesc1, 1u);
+      }
+      commit1(&bar);
+    }
+    if (!wish_wait(&bar, phase, &s_abort, status)) break;
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // ---- 3. S[(g, r)][i] = T_g[r][i], split, over A^T (consumed)
+    for (int c0 = 0; c0 < dp; c0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + lane_addr + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float hf, lf;
+        split_tf32(__uint_as_float(r[q]), hf, lf);
+        const uint32_t o = koff(g * dp + c0 + q, i);
+        Xhi[o] = hf;
+        Xlo[o] = lf;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    // ---- 4. S S^T (the diagonal p x p blocks are the draws' W)
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      for (int ks = 0; ks < dp / 8; ++ks) {
+        const uint64_t o = 16u * (uint64_t)ks;
+        mma_tf32_ss(tmem, xl + o, xh + o, idesc2, ks > 0 ? 1u : 0u);
+        mma_tf32_ss(tmem, xh + o, xl + o, idesc2, 1u);
+        mma_tf32_ss(tmem, xh + o, xh + o, idesc2, 1u);
+      }
+      commit1(&bar);
+    }
+    if (!wish_wait(&bar, phase, &s_abort, status)) break;
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // ---- 5. lane (g, r): row (g, r) of its draw's block, W_g[r][s] at column g p + s
+    {
+      const int r = i;
+      const int c0 = dp >= 32 ? (32 * warp / dp) * dp : 32 * warp;  // the warp's first column (warp-uniform)
+      const int width = dp >= 32 ? dp : 32;
+      float* o = out + j * (int64_t)d * d;
+      for (int cc = 0; cc < width; cc += 16) {
+        uint32_t v[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(tmem + lane_addr + (uint32_t)(c0 + cc)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int sc = c0 + cc + q - g * dp;  // column within the draw's block
+          if (jok && r < d && sc >= 0 && sc < d) o[(int64_t)sc * d + r] = __uint_as_float(v[q]);
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+  }
+  // copies and products in flight finish before the CTA leaves
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (tid == 0) {
+    commit1(&bar);
+    mbar_wait(&bar, phase, &s_abort, status);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u));
+  }
+}
+
+bool wishart_umma_usable(int d, int dtype, int inverse) {
+  return dtype == GR_F32 && !inverse && d >= 1 && d <= kWishUmmaMaxDim;
+}
+
+cudaError_t launch_wishart_umma(const float* normals, const float* chis, const float* chol, float* out, int d,
+                                int64_t samples, int32_t* status, cudaStream_t s) {
+  if (d < 1 || d > kWishUmmaMaxDim || samples <= 0) return samples == 0 ? cudaSuccess : cudaErrorInvalidValue;
+  int dp = 16;
+  while (dp < d) dp <<= 1;
+  const int G = 128 / dp;
+  // 128 tensor-memory columns per CTA: four CTAs per SM; shared memory is
+  // sized so that no more than four are resident (a fifth would wait in
+  // tcgen05.alloc), fewer where a CTA needs more
+  const size_t stage_len = ((size_t)G * d * (d - 1) / 2 + 3) & ~(size_t)3;
+  size_t smem = 1024 + (size_t)(2 * dp * dp + 2 * 128 * dp + 2 * stage_len) * sizeof(float);
+  if (smem < 52 * 1024) smem = 52 * 1024;
+  int dev = 0, sms = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem + 4096 > (size_t)optin) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_wishart_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_wishart_umma, kWishUThreads, smem);
+  if (per < 1) per = 1;
+  if (per > 4) per = 4;
+  const int64_t tiles = (samples + G - 1) / G;
+  const int64_t cap = (int64_t)sms * per;
+  const int64_t grid = tiles < cap ? tiles : cap;
+  k_wishart_umma<<<(unsigned)grid, kWishUThreads, smem, s>>>(normals, chis, chol, out, d, dp, samples, status);
+  return cudaGetLastError();
 }
 
 int umma_padded_dim(int d) { return (d + 15) / 16 * 16; }

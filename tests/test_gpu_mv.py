@@ -333,6 +333,25 @@ def test_wishart_f32_vs_fp64_oracle(er, oracle, d, df, n):
     assert err <= 1e-5
 
 
+@pytest.mark.parametrize("d,df,n", [(1, 3, 16), (3, 5, 40), (16, 20, 24), (17, 20, 40), (33, 40, 40), (64, 70, 24),
+                                    (32, 40, 152 * 4 * 3 + 8)])
+def test_wishart_f32_tensor_memory_shapes(er, oracle, d, df, n):
+    """The tcgen05 Bartlett products (float, dim <= 64): draws stacked 8 / 4 /
+    2 to a 128-row tile for padded dims 16 / 32 / 64, partial last tiles,
+    zero-padded rows and columns, and more tiles than SMs."""
+    err = wishart_case(er, oracle, d, df, n, torch.float32)
+    print(f"Wishart d={d} n={n} float (tcgen05): max |W - W64| / max |W64| = {err:.3g}")
+    assert err <= 1e-5
+
+
+@pytest.mark.parametrize("d,df,n", [(4, 6, 64), (32, 40, 64)])
+def test_wishart_f32_mma_sync_form(er, oracle, d, df, n, monkeypatch):
+    """The mma.sync products (InvWishart, dims above 64), forced with the
+    GR_WISHART_PRODUCT test hook at dims that default to tcgen05."""
+    monkeypatch.setenv("GR_WISHART_PRODUCT", "mma_sync")
+    assert wishart_case(er, oracle, d, df, n, torch.float32) <= 1e-5
+
+
 @pytest.mark.parametrize("d,df,n", [(4, 6, 64), (32, 40, 32)])
 def test_invwishart_f32_vs_fp64_oracle(er, oracle, d, df, n):
     err = wishart_case(er, oracle, d, df, n, torch.float32, inverse=True)
