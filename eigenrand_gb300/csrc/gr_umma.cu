@@ -962,9 +962,23 @@ cudaError_t launch_wishart_umma(const float* normals, const float* chis, const f
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (smem + 4096 > (size_t)optin) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_wishart_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // all of the SM's unified L1 / shared memory as shared memory, so that
+  // several CTAs fit
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_wishart_umma, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
-  int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_wishart_umma, kWishUThreads, smem);
+  // resident CTAs per SM from the SM's shared memory (the occupancy API
+  // answers 1 for this kernel whatever the size, while the SM holds three at
+  // dim 32); tensor memory (512 columns, 128 per CTA) caps it at four
+  int sm_smem = 0, reserved = 0;
+  cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, k_wishart_umma);
+  if (e != cudaSuccess) return e;
+  const size_t per_cta = smem + fa.sharedSizeBytes + (size_t)reserved;
+  int per = (int)((size_t)sm_smem / per_cta);
   if (per < 1) per = 1;
   if (per > 4) per = 4;
   const int64_t tiles = (samples + G - 1) / G;
