@@ -12,6 +12,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 #include <type_traits>
 
 #include "../../include/gpurand.h"
@@ -2074,12 +2076,12 @@ BetaComp beta_component(int branch, float af, double ad) {
 // component at packet position x, lane j.  ACC: also decide acceptance (the
 // rejection types); without it only the candidate is computed, for lanes
 // already known to be accepted (the same expressions, so the same bits).
-template <int DT, bool ACC, class WF, class RF>
-__device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j, WF&& word, RF&& rval, bool& acc) {
+// Uf(q) / Ud(q): the uniform of lane j of packet x + q.
+template <int DT, bool ACC, class UFF, class UDF>
+__device__ __forceinline__ uint64_t beta_comp_u(const BetaComp g, const int type, UFF&& Uf, UDF&& Ud, bool& acc) {
   acc = true;
-  const int type = g.type, U = g.U;
+  const int U = g.U;
   if (DT == SD_F32) {
-    auto Uf = [&](int q) { return ur_f(word((x + q) * 8 + j)); };
     if (type == 0) return f2u(1.0f * (-(logf_(1.0f - Uf(0)) / 1.0f)));
     if (type == 1) {
       float y = Uf(0) + 1.1920928955078125e-07f / 8;
@@ -2110,7 +2112,6 @@ __device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j
     }
     return f2u(1.0f * xx);
   } else {
-    auto Ud = [&](int q) { return ur_d(rval((x + q) * 4 + j)); };
     if (type == 0) return d2u(1.0 * (-(log_(1.0 - Ud(0)) / 1.0)));
     if (type == 1) {
       double y = Ud(0) + 2.220446049250313e-16 / 8;
@@ -2141,6 +2142,13 @@ __device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j
     }
     return d2u(1.0 * xx);
   }
+}
+
+template <int DT, bool ACC, class WF, class RF>
+__device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j, WF&& word, RF&& rval, bool& acc) {
+  return beta_comp_u<DT, ACC>(
+      g, g.type, [&](int q) { return ur_f(word((x + q) * 8 + j)); }, [&](int q) { return ur_d(rval((x + q) * 4 + j)); },
+      acc);
 }
 
 }  // namespace
@@ -2550,6 +2558,467 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
   }
 }
 
+// ===========================================================================
+// k_beta_chase: the BetaGen walk with the reference automaton on a warp of
+// its own, one step ahead of the workers.
+//   chase  (warp 0) follows the automaton over the accept masks: per trial
+//          of a rejection component one mask read, its popcount and two
+//          compares.  Per step it records the source of every output packet
+//          (closed-form position, full-trial value slot or FIFO offset) and,
+//          for every accepted lane of a consumed partial trial, its FIFO slot
+//          (position and lane, written by the warp's first P lanes at once),
+//          into one of two buffers.
+//   work   (warps 1-5) take the previous step's buffer: the full-trial values
+//          of the rejection component, the accepted partial lanes and the
+//          positional values of the other component as one task list;
+//          p1 / (p1 + p2) per output lane; the carried lanes to the front of
+//          the lane buffer; then they twist the next engine block and
+//          evaluate its accept masks.
+// The chase of step t reads only masks; the workers of step t - 1 read the
+// raw ring (blocks t - 2 .. t) before they overwrite block t - 2 with block
+// t + 1, so the step's packets must start at block t - 2 or later (checked;
+// a record longer than two blocks ends the call with the iteration-cap
+// status).  Buffers hold more than one block's worth of records, partial
+// lanes and FIFO lanes, so a chase that fell behind catches up.
+// TY0 / TY1: the components' sampler types when known at compile time (the
+// kernel then carries only their code), else -1.
+// ===========================================================================
+namespace {
+
+constexpr int kBcThreads = 192;
+constexpr int kBcWork = kBcThreads - 32;
+constexpr int kBcRec = 160;         // output packets per step (a block holds at most 156)
+constexpr int kBcFifo = 112;        // FIFO outputs per component per step (at most 104 per block)
+constexpr int kBcFull = 112;        // full-trial outputs of the buffered component per step
+constexpr int kBcFullTag = 16384;   // record source >= this: full-trial value slot
+
+template <int DT>
+__host__ __device__ constexpr int bc_lb() {  // lane buffer per component: carried + one step's FIFO lanes
+  return 16 + kBcFifo * beta_lanes<DT>();
+}
+
+struct BcStep {
+  int64_t base, e0;  // first packet of the step (sources are relative to it), first output packet
+  int nrec, nf, fs[2], A[2], f[2];
+};
+
+template <int DT>
+__host__ __device__ constexpr size_t bc_smem_bytes() {
+  return (size_t)3 * kLanes * kN * 8 +                                                   // raw windows
+         ((size_t)2 * bc_lb<DT>() + (size_t)(kBcFull + kBcRec) * beta_lanes<DT>()) *     // lane buffers, full-
+             (DT == SD_F64 ? 8 : 4) +                                                    //   trial and positional values
+         (size_t)2 * kBcRec * 2 * 2 +                                                    // records
+         (size_t)2 * kBcFull * 2 +                                                       // full-trial positions
+         (size_t)2 * 2 * bc_lb<DT>() * 2 +                                               // partial-lane tasks
+         (size_t)2 * kBetaRing;                                                          // masks per position
+}
+
+}  // namespace
+
+template <int DT, int TY0, int TY1>  // DT: SD_F32 or SD_F64
+__global__ void __maxnreg__(80) k_beta_chase(Plan p, BetaConsts bk, int64_t max_blocks) {
+  constexpr int P = beta_lanes<DT>();
+  constexpr int LB = bc_lb<DT>();
+  constexpr unsigned FULL = 0xffffffffu;
+  using V = typename std::conditional<DT == SD_F64, uint64_t, uint32_t>::type;
+  extern __shared__ __align__(16) uint64_t bc_dyn[];
+  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(bc_dyn);
+  V* lanebuf = reinterpret_cast<V*>(bc_dyn + 3 * kLanes * kN);          // [2][LB]
+  V* fullval = lanebuf + 2 * LB;                                         // [kBcFull][P]
+  V* posval = fullval + kBcFull * P;                                     // [kBcRec][P]
+  int16_t* rec = reinterpret_cast<int16_t*>(posval + kBcRec * P);        // [2][kBcRec][2]
+  int16_t* fpos = rec + 2 * kBcRec * 2;                                  // [2][kBcFull]
+  uint16_t* ptask = reinterpret_cast<uint16_t*>(fpos + 2 * kBcFull);     // [2][2][LB]
+  uint8_t* pmask = reinterpret_cast<uint8_t*>(ptask + 2 * 2 * LB);       // [2][kBetaRing]
+  __shared__ BcStep s_step[2];
+  __shared__ int s_done, s_err, s_fc[2];
+  __shared__ int64_t s_end;
+
+  const int k = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  EngState* st = p.eng + k;
+  GenState* gs = p.gen + k;
+  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
+  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
+  const int64_t off = g0 * p.gran, n = ng * p.gran;
+  if (n == 0) return;
+  const int64_t Npk = n / P;
+
+  const int type0 = TY0 >= 0 ? TY0 : bk.c[0].type, type1 = TY1 >= 0 ? TY1 : bk.c[1].type;
+  const int U0 = bk.c[0].U, U1 = bk.c[1].U;
+  const bool post = bk.post == 1;
+  const int umax = max(max(U0, U1), 3);
+  // bc: the rejection component whose full-trial values get a slot; ob: the
+  // component whose positional values are computed with them
+  const int bc = type0 >= 2 ? 0 : (type1 >= 2 ? 1 : -1);
+  const int ob = bc == 0 ? 1 : (bc == 1 ? 0 : 1);
+  load_window(raw[2], &st->win[0][0], kN);  // block -1; block b lives in window b mod 3
+  // carried lanes of the two GammaGens (generator slots 1 and 2)
+  if (tid < 2 * 8) {
+    const int c = tid / 8, j = tid % 8;
+    const GenSlot& g = gs->s[1 + c];
+    if (j < g.rest_cnt)
+      lanebuf[c * LB + j] = (V)(DT == SD_F64 ? ((uint64_t)g.rest[2 * j] | ((uint64_t)g.rest[2 * j + 1] << 32))
+                                             : (uint64_t)g.rest[j]);
+  }
+  if (tid == 0) {
+    s_err = 0;
+    s_done = 0;
+  }
+  __syncthreads();
+  // The newest three raw blocks are the ring of packets; words are tempered
+  // where they are read.  Each thread keeps its own view of the newest block.
+  int64_t ring_new = 0;
+  int wb0 = 0, wb1 = 2, wb2 = 1;
+  auto set_ring = [&](int64_t B) {
+    ring_new = B * kN;
+    wb0 = (int)(B % 3);
+    wb1 = (int)((B + 2) % 3);
+    wb2 = (int)((B + 1) % 3);
+  };
+  auto tword = [&](int64_t rel, int l) -> uint64_t {
+    int dd = (int)(rel - ring_new);
+    int w = wb0;
+    if (dd < 0) {
+      dd += kN;
+      w = wb1;
+      if (dd < 0) {
+        dd += kN;
+        w = wb2;
+      }
+    }
+    if ((unsigned)dd >= (unsigned)kN) dd = 0;  // outside the ring: never read past the buffers
+    return mt_temper(raw[w][l][dd]);
+  };
+  auto word = [&](int64_t w) -> uint32_t {
+    const uint64_t v = tword(w >> 3, (int)((w & 7) >> 1));
+    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
+  };
+  auto rval = [&](int64_t r) -> uint64_t { return tword(r >> 2, (int)(r & 3)); };
+  // value of an accepted trial lane or a closed-form draw; double GS lanes
+  // use the branch threshold in integer form
+  auto value = [&](int c, int64_t x, int j) -> uint64_t {
+    bool acc;
+    auto uf = [&](int q) { return ur_f(word((x + q) * 8 + j)); };
+    auto ud = [&](int q) { return ur_d(rval((x + q) * 4 + j)); };
+    if (c == 0) {
+      if (DT == SD_F64 && type0 == 2)
+        return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[0].tpx, bk.c[0].d_inv));
+      return beta_comp_u<DT, false>(bk.c[0], type0, uf, ud, acc);
+    }
+    if (DT == SD_F64 && type1 == 2)
+      return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[1].tpx, bk.c[1].d_inv));
+    return beta_comp_u<DT, false>(bk.c[1], type1, uf, ud, acc);
+  };
+  const int nrej = (type0 >= 2 ? 1 : 0) + (type1 >= 2 ? 1 : 0);
+  const int rej0 = type0 >= 2 ? 0 : 1;
+  // accept masks of the rejection components at positions [from, to), by
+  // threads t = 0 .. T-1 of whole warps.  Each group of P threads (one per
+  // lane) walks a run of consecutive positions and slides a window of the
+  // lane's three tempered words along it (one word fetched per position);
+  // a ballot per step gives the masks of the warp's 32 / P runs.
+  auto masks = [&](int64_t from, int64_t to, int t, int T) {
+    if (nrej == 0 || to <= from) return;
+    constexpr int G = 32 / P;
+    const int runs = (T >> 5) * G;
+    const int L = ((int)(to - from) + runs - 1) / runs;
+    const int r = (t >> 5) * G + (t & 31) / P, j = t & (P - 1);
+    const int lw = DT == SD_F64 ? j : (j >> 1);  // the lane's 64-bit word
+    const int64_t x0 = from + (int64_t)r * L;
+    for (int ci = 0; ci < nrej; ++ci) {
+      const int c = nrej == 2 ? ci : rej0;
+      const int ty = c == 0 ? type0 : type1;
+      uint64_t w0 = 0, w1 = tword(x0, lw), w2 = tword(x0 + 1, lw);
+      for (int i = 0; i < L; ++i) {
+        const int64_t x = x0 + i;
+        const bool valid = x < to;
+        w0 = w1;
+        w1 = w2;
+        w2 = tword(x + 2, lw);
+        bool acc = false;
+        if (valid) {
+          int f = -1;
+          if (DT == SD_F64 && ty == 2)  // float pre-test of a double GS trial
+            f = c == 0 ? gs_filter_f64(w0, w1, w2, bk.c[0].f_px, bk.c[0].f_inv, bk.c[0].f_am1, bk.c[0].f_band)
+                       : gs_filter_f64(w0, w1, w2, bk.c[1].f_px, bk.c[1].f_inv, bk.c[1].f_am1, bk.c[1].f_band);
+          if (f >= 0) {
+            acc = f == 1;
+          } else {
+            auto uf = [&](int q) {
+              const uint64_t v = q == 0 ? w0 : (q == 1 ? w1 : w2);
+              return ur_f((j & 1) ? (uint32_t)(v >> 32) : (uint32_t)v);
+            };
+            auto ud = [&](int q) { return ur_d(q == 0 ? w0 : (q == 1 ? w1 : w2)); };
+            if (c == 0) beta_comp_u<DT, true>(bk.c[0], type0, uf, ud, acc);
+            else beta_comp_u<DT, true>(bk.c[1], type1, uf, ud, acc);
+          }
+        }
+        const uint32_t bal = __ballot_sync(FULL, acc);
+        if (valid && j == 0)
+          pmask[c * kBetaRing + (int)(x & (kBetaRing - 1))] =
+              (uint8_t)((bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1));
+      }
+    }
+  };
+  // block 0 and its masks (all threads)
+  mt_block(raw[2], raw[0], [&](int, const uint64_t*) {});
+  set_ring(0);
+  masks(0, kN - umax + 1, tid, kBcThreads);
+  __syncthreads();
+
+  // chase state (warp 0, the same in every lane)
+  int64_t cx = 0, cE = 0;
+  int cf[2] = {0, 0};
+  if (warp == 0) {
+    cf[0] = gs->s[1].rest_cnt;
+    cf[1] = gs->s[2].rest_cnt;
+  }
+  int64_t B = 0;  // newest block generated
+  bool done = false;
+  for (int64_t t = 0;; ++t) {
+    const bool gen = !done && t + 1 < max_blocks;
+    const int64_t M = (t + 1) * kN - umax + 1;  // positions with masks
+    if (warp == 0) {
+      if (!done) {
+        // ---- chase step t into buffer t mod 2
+        const int q = (int)(t & 1);
+        const int64_t pk_lim = (t + 1) * kN;  // packets generated
+        int16_t* rq = rec + q * kBcRec * 2;
+        int16_t* fq = fpos + q * kBcFull;
+        uint16_t* tq = ptask + q * 2 * LB;
+        const int64_t base = cx, e0 = cE;
+        const int fs0 = cf[0], fs1 = cf[1];
+        int nrec = 0, nf = 0, A[2] = {cf[0], cf[1]};
+        const bool lag = cx < (t - 1) * kN;
+        const int Mr = (int)(M - base), bm = (int)(base & (kBetaRing - 1));
+        if (!lag) {
+          while (cE < Npk && nrec < kBcRec) {
+            const int64_t xs = cx;
+            const int cf0 = cf[0], cf1 = cf[1], A0 = A[0], A1 = A[1], nfs = nf;
+            // one component of record nrec: 0 done, 1 a buffer is full,
+            // 2 positions not evaluated or packets not generated yet
+            auto visit = [&](auto cc) -> int {
+              constexpr int c = decltype(cc)::value;
+              const int ty = c == 0 ? type0 : type1, U = c == 0 ? U0 : U1;
+              if (ty <= 1) {
+                if (cx + U > pk_lim) return 2;
+                if (lane == 0) rq[nrec * 2 + c] = (int16_t)(cx - base);
+                cx += U;
+                return 0;
+              }
+              const int fsc = c == 0 ? fs0 : fs1;
+              int acc = 0;
+              int xr = (int)(cx - base);  // trial position relative to the step
+              for (;;) {
+                if (xr >= Mr) return 2;
+                const uint32_t m = pmask[c * kBetaRing + ((bm + xr) & (kBetaRing - 1))];
+                const int cn = __popc(m);
+                if (cn == P) {  // a full trial ends the visit; the partial lanes stay carried
+                  if (c == bc) {
+                    if (nf >= kBcFull) return 1;
+                    if (lane == 0) {
+                      fq[nf] = (int16_t)xr;
+                      rq[nrec * 2 + c] = (int16_t)(kBcFullTag + nf);
+                    }
+                    ++nf;
+                  } else if (lane == 0) {
+                    rq[nrec * 2 + c] = (int16_t)xr;
+                  }
+                  cf[c] += acc;
+                  break;
+                }
+                if (A[c] + acc + cn > LB) return 1;
+                // FIFO slots of the trial's accepted lanes
+                if (lane < P && ((m >> lane) & 1u))
+                  tq[c * LB + A[c] + acc - fsc + __popc(m & ((1u << lane) - 1u))] = (uint16_t)((xr << 3) | lane);
+                acc += cn;
+                if (cf[c] + acc >= P) {  // the carry fills: its oldest P lanes are the output
+                  if (lane == 0) rq[nrec * 2 + c] = (int16_t)(-(1 + (A[c] - cf[c])));
+                  cf[c] += acc - P;
+                  break;
+                }
+                xr += U;
+              }
+              A[c] += acc;
+              cx = base + xr + U;
+              return 0;
+            };
+            int r = visit(std::integral_constant<int, 0>{});
+            if (!r) r = visit(std::integral_constant<int, 1>{});
+            if (r) {
+              cx = xs;
+              cf[0] = cf0;
+              cf[1] = cf1;
+              A[0] = A0;
+              A[1] = A1;
+              nf = nfs;
+              break;
+            }
+            ++nrec;
+            ++cE;
+          }
+        }
+        if (lane == 0) {
+          BcStep& S = s_step[q];
+          S.base = base;
+          S.e0 = e0;
+          S.nrec = nrec;
+          S.nf = nf;
+          S.fs[0] = fs0;
+          S.fs[1] = fs1;
+          S.A[0] = A[0];
+          S.A[1] = A[1];
+          S.f[0] = cf[0];
+          S.f[1] = cf[1];
+          if (lag) s_err = 1;
+          if (cE >= Npk) {
+            s_done = 1;
+            s_end = cx;
+          }
+        }
+      }
+    } else {
+      const int tt = tid - 32;
+      if (t >= 1 && s_step[(t - 1) & 1].nrec > 0) {
+        // ---- step t - 1: values and outputs
+        const int q = (int)((t - 1) & 1);
+        const BcStep& S = s_step[q];
+        const int nrec = S.nrec, nf = S.nf;
+        const int fs0 = S.fs[0], fs1 = S.fs[1];
+        const int64_t base = S.base;
+        const int16_t* rq = rec + q * kBcRec * 2;
+        const uint16_t* tq = ptask + q * 2 * LB;
+        set_ring(t);
+        // one task list, one lane per thread: full trials of the buffered
+        // component, the accepted partial-trial lanes, positional values of
+        // the other component
+        const int t0 = nf * P, tp0 = S.A[0] - fs0, tp1 = S.A[1] - fs1;
+        const int t1 = t0 + tp0 + tp1;
+        for (int u = tt; u < t1 + nrec * P; u += kBcWork) {
+          if (u < t0) {
+            const int i = u / P, j = u % P;
+            fullval[i * P + j] = (V)value(bc, base + fpos[q * kBcFull + i], j);
+          } else if (u < t1) {
+            const int c = u < t0 + tp0 ? 0 : 1;
+            const int qq = c == 0 ? u - t0 : u - t0 - tp0;
+            const int tk = tq[c * LB + qq];
+            lanebuf[c * LB + (c == 0 ? fs0 : fs1) + qq] = (V)value(c, base + (tk >> 3), tk & 7);
+          } else {
+            const int i = (u - t1) / P, j = (u - t1) % P;
+            const int src = rq[i * 2 + ob];
+            if (src >= 0 && src < kBcFullTag) posval[i * P + j] = (V)value(ob, base + src, j);
+          }
+        }
+        asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
+        // output packets
+        const int64_t e0 = S.e0;
+        for (int u = tt; u < nrec * P; u += kBcWork) {
+          const int i = u / P, j = u % P;
+          uint64_t v[2];
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const int src = rq[i * 2 + c];
+            if (src < 0) v[c] = (uint64_t)lanebuf[c * LB + (-src - 1) + j];
+            else if (src >= kBcFullTag) v[c] = (uint64_t)fullval[(src - kBcFullTag) * P + j];
+            else if (c == ob) v[c] = (uint64_t)posval[i * P + j];
+            else v[c] = value(c, base + src, j);  // both components closed form
+          }
+          if (DT == SD_F32) {
+            const float p1 = u2f((uint32_t)v[0]), p2 = u2f((uint32_t)v[1]);
+            const float x = p1 / (p1 + p2);
+            reinterpret_cast<float*>(p.out)[off + (e0 + i) * P + j] = post ? (bk.fpost * x) / (1.0f - x) : x;
+          } else {
+            const double p1 = u2d(v[0]), p2 = u2d(v[1]);
+            const double x = p1 / (p1 + p2);
+            reinterpret_cast<double*>(p.out)[off + (e0 + i) * P + j] = post ? (bk.dpost * x) / (1.0 - x) : x;
+          }
+        }
+        // lanes still carried move to the front of each lane buffer
+        V carry = 0;
+        const int cc = tt / 8, cj = tt % 8;
+        const bool mover = tt < 16 && cj < S.f[cc];
+        if (mover) carry = lanebuf[cc * LB + S.A[cc] - S.f[cc] + cj];
+        asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
+        if (mover) lanebuf[cc * LB + cj] = carry;
+      }
+      if (gen) {
+        // ---- block t + 1 and its masks.  Word i < 156 of the new block needs
+        // only the old block; word 156 + i needs new word i, which the same
+        // thread made (word 311 needs new word 0: recomputed), so the twist
+        // needs no barrier of its own
+        uint64_t(*old)[kN] = raw[t % 3];
+        uint64_t(*nw)[kN] = raw[(t + 1) % 3];
+        for (int i = tt; i < kM; i += kBcWork) {
+#pragma unroll
+          for (int l = 0; l < kLanes; ++l) {
+            const uint64_t lo = mt_twist(old[l][i], old[l][i + 1], old[l][i + kM]);
+            const uint64_t n0 = i == kM - 1 ? mt_twist(old[l][0], old[l][1], old[l][kM]) : 0;
+            const uint64_t hi = mt_twist(old[l][i + kM], i == kM - 1 ? n0 : old[l][i + kM + 1], lo);
+            nw[l][i] = lo;
+            nw[l][i + kM] = hi;
+          }
+        }
+        asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
+        set_ring(t + 1);
+        masks(M, M + kN, tt, kBcWork);
+      }
+    }
+    __syncthreads();
+    if (done || s_err) break;
+    done = s_done != 0;
+    if (gen) B = t + 1;
+    if (!done && !gen) break;  // no block left for the chase: the iteration cap
+  }
+
+  // ---- state after the call
+  if (tid == 0) {
+    if (!s_done) s_end = cx;
+    if (!s_done || s_err) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
+    s_fc[0] = cf[0];
+    s_fc[1] = cf[1];
+  }
+  __syncthreads();
+  const int64_t np = s_end;  // packets consumed
+  if (np > 0) {
+    const int64_t lastb = (np - 1) / kN;
+    const int rr = (int)(np - lastb * kN);  // in [1, 312]
+    if (lastb == B) {
+      store_window(st, raw[B % 3], raw[(B + 2) % 3], rr);
+    } else if (lastb == B - 1) {
+      store_window(st, raw[(B + 2) % 3], raw[(B + 1) % 3], rr);
+    } else if (lastb == B - 2 && B >= 2) {
+      // block B - 3 was overwritten by block B: recover it from block B - 2
+      // into block B's window (MT19937-64's twist inverts)
+      if (tid < kLanes) {
+        uint64_t* nwl = raw[(B + 1) % 3][tid];
+        uint64_t* odl = raw[B % 3][tid];
+        mt_untwist_block([&](int i) -> uint64_t& { return nwl[i]; }, [&](int i) -> uint64_t& { return odl[i]; });
+      }
+      __syncthreads();
+      store_window(st, raw[(B + 1) % 3], raw[B % 3], rr);
+    } else if (tid == 0) {
+      atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
+    }
+  }
+  if (tid < 2 * 8) {
+    const int c = tid / 8, j = tid % 8;
+    GenSlot& g = gs->s[1 + c];
+    const uint64_t v = j < s_fc[c] ? (uint64_t)lanebuf[c * LB + j] : 0;
+    if (DT == SD_F64) {
+      g.rest[2 * j] = (uint32_t)v;
+      g.rest[2 * j + 1] = (uint32_t)(v >> 32);
+    } else {
+      g.rest[j] = (uint32_t)v;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    gs->s[1].rest_cnt = s_fc[0];
+    gs->s[2].rest_cnt = s_fc[1];
+    st->consumed += (uint64_t)max(np, (int64_t)0);
+  }
+}
+
 template <int DT>
 static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_blocks, cudaStream_t s) {
   BetaConsts bk;
@@ -2558,17 +3027,28 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
   bk.post = d.post;
   bk.fpost = d.fh;
   bk.dpost = d.dh;
-  constexpr size_t smem = beta_smem_bytes<DT>();
   static bool attr[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  constexpr size_t smem = beta_smem_bytes<DT>(), smem2 = bc_smem_bytes<DT>();
   if (!attr[dev]) {
     cudaError_t e = cudaFuncSetAttribute(k_beta<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_beta_chase<DT, -1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_beta_chase<DT, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_beta_chase<DT, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  k_beta<DT><<<p.K, kBetaThreads, smem, s>>>(p, bk, max_blocks);
+  const char* fv = std::getenv("GR_BETA_FORM");
+  const int t0 = bk.c[0].type, t1 = bk.c[1].type;
+  if (fv && std::strcmp(fv, "walk") == 0) k_beta<DT><<<p.K, kBetaThreads, smem, s>>>(p, bk, max_blocks);
+  else if (t0 == 2 && t1 == 1) k_beta_chase<DT, 2, 1><<<p.K, kBcThreads, smem2, s>>>(p, bk, max_blocks);
+  else if (t0 == 1 && t1 == 2) k_beta_chase<DT, 1, 2><<<p.K, kBcThreads, smem2, s>>>(p, bk, max_blocks);
+  else k_beta_chase<DT, -1, -1><<<p.K, kBcThreads, smem2, s>>>(p, bk, max_blocks);
   return cudaGetLastError();
 }
 
