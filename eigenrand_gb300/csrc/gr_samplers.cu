@@ -2710,6 +2710,44 @@ __global__ void __maxnreg__(80) k_beta_chase(Plan p, BetaConsts bk, int64_t max_
       return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[1].tpx, bk.c[1].d_inv));
     return beta_comp_u<DT, false>(bk.c[1], type1, uf, ud, acc);
   };
+  // The GS + integral-alpha pairs: the value of either component is one log
+  // (of the GS trial's vx, or of the product of the integral draw's
+  // uniforms), then an exp for GS lanes below the branch threshold; every
+  // lane of a warp shares the log whichever component it computes.
+  constexpr bool kFused = (TY0 == 2 && TY1 == 1) || (TY0 == 1 && TY1 == 2);
+  constexpr int gc = TY0 == 2 ? 0 : 1;  // the GS component of a fused pair
+  auto value_task = [&](int c, int64_t x, int j) -> uint64_t {
+    if (!kFused) return value(c, x, j);
+    const BetaComp& g = c == 0 ? bk.c[0] : bk.c[1];
+    const bool gsv = c == gc;
+    if (DT == SD_F64) {
+      constexpr double e = 2.220446049250313e-16 / 8;
+      const uint64_t b0 = rval(x * 4 + j), b1 = rval((x + 1) * 4 + j);
+      double arg = ur_d(b1) + e;
+      if (!gsv) {
+        double y = ur_d(b0) + e;
+        y = y * arg;
+        for (int q = 2; q < g.U; ++q) y = y * (ur_d(rval((x + q) * 4 + j)) + e);
+        arg = y;
+      }
+      const double l = log_(arg);
+      if (!gsv) return d2u(-(1.0 * l));
+      return d2u(1.0 * (((b0 & 0xfffffffffffffull) < g.tpx) ? exp_(g.d_inv * l) : 1.0 - l));
+    } else {
+      constexpr float e = 1.1920928955078125e-07f / 8;
+      const float u0 = ur_f(word(x * 8 + j)), u1 = ur_f(word((x + 1) * 8 + j));
+      float arg = u1 + e;
+      if (!gsv) {
+        float y = u0 + e;
+        y = y * arg;
+        for (int q = 2; q < g.U; ++q) y = y * (ur_f(word((x + q) * 8 + j)) + e);
+        arg = y;
+      }
+      const float l = logf_(arg);
+      if (!gsv) return f2u(-(1.0f * l));
+      return f2u(1.0f * ((u0 < g.f_px) ? expf_(g.f_inv * l) : 1.0f - l));
+    }
+  };
   const int nrej = (type0 >= 2 ? 1 : 0) + (type1 >= 2 ? 1 : 0);
   const int rej0 = type0 >= 2 ? 0 : 1;
   // accept masks of the rejection components at positions [from, to), by
@@ -2895,19 +2933,29 @@ __global__ void __maxnreg__(80) k_beta_chase(Plan p, BetaConsts bk, int64_t max_
         const int t0 = nf * P, tp0 = S.A[0] - fs0, tp1 = S.A[1] - fs1;
         const int t1 = t0 + tp0 + tp1;
         for (int u = tt; u < t1 + nrec * P; u += kBcWork) {
+          int c, j, rel;
+          V* dst;
           if (u < t0) {
-            const int i = u / P, j = u % P;
-            fullval[i * P + j] = (V)value(bc, base + fpos[q * kBcFull + i], j);
+            const int i = u / P;
+            j = u % P;
+            c = bc;
+            rel = fpos[q * kBcFull + i];
+            dst = fullval + i * P + j;
           } else if (u < t1) {
-            const int c = u < t0 + tp0 ? 0 : 1;
+            c = u < t0 + tp0 ? 0 : 1;
             const int qq = c == 0 ? u - t0 : u - t0 - tp0;
             const int tk = tq[c * LB + qq];
-            lanebuf[c * LB + (c == 0 ? fs0 : fs1) + qq] = (V)value(c, base + (tk >> 3), tk & 7);
+            j = tk & 7;
+            rel = tk >> 3;
+            dst = lanebuf + c * LB + (c == 0 ? fs0 : fs1) + qq;
           } else {
-            const int i = (u - t1) / P, j = (u - t1) % P;
-            const int src = rq[i * 2 + ob];
-            if (src >= 0 && src < kBcFullTag) posval[i * P + j] = (V)value(ob, base + src, j);
+            const int i = (u - t1) / P;
+            j = (u - t1) % P;
+            c = ob;
+            rel = rq[i * 2 + ob];
+            dst = (rel >= 0 && rel < kBcFullTag) ? posval + i * P + j : nullptr;
           }
+          if (dst) *dst = (V)value_task(c, base + rel, j);
         }
         asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
         // output packets
