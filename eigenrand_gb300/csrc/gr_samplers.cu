@@ -358,14 +358,9 @@ __device__ __forceinline__ int gs_filter_f64(uint64_t bux, uint64_t bvx, uint64_
   const float vx = __uint2float_rn((uint32_t)(mv >> 20)) * 0x1p-32f;
   const float ux2 = __uint2float_rn((uint32_t)((bux2 & M) >> 20)) * 0x1p-32f;
   const float lv = logf_(vx);
-  float qx;
-  if (ux < pxf) {
-    const float xx = expf_(inv_a * lv);
-    qx = expf_(-xx);
-  } else {
-    const float xx = 1.0f - lv;
-    qx = expf_(logf_(xx) * am1);
-  }
+  const bool c = ux < pxf;
+  const float e1 = expf_(c ? inv_a * lv : logf_(1.0f - lv) * am1);  // one exp for both branches
+  const float qx = c ? expf_(-e1) : e1;
   if (ux2 < qx * (1.0f - band)) return 1;
   if (ux2 > qx * (1.0f + band)) return 0;
   return -1;
@@ -398,16 +393,14 @@ __device__ __forceinline__ bool rej_trial(const DistParams& d, int64_t t, int j,
       const float ux2 = ur_f(word(w0 + 16 + j));
       // the reference evaluates both branches and blends (NormalExp.h:543-553);
       // evaluating only the selected one gives the same bits
+      // branch c: xx = exp(lv / alpha), bound exp(-xx); else xx = 1 - lv,
+      // bound exp(log(xx) (alpha - 1)).  One exp serves both branches, so a
+      // warp with lanes in both runs three transcendentals after lv, not four
       const float lv = logf_(vx);
       const bool c = ux < d.fe;  // px
-      float xx, qx;
-      if (c) {
-        xx = expf_(d.fc * lv);  // (1/alpha) * log(vx)
-        qx = expf_(-xx);
-      } else {
-        xx = 1.0f - lv;
-        qx = expf_(logf_(xx) * d.fd);  // alpha - 1
-      }
+      const float e1 = expf_(c ? d.fc * lv : logf_(1.0f - lv) * d.fd);  // 1/alpha, alpha - 1
+      const float xx = c ? e1 : 1.0f - lv;
+      const float qx = c ? expf_(-e1) : e1;
       cbits = f2u(d.fb * xx);
       acc = ux2 < qx;
     } else if (RK == RK_GAMMA_TAN) {
@@ -2091,15 +2084,11 @@ __device__ __forceinline__ uint64_t beta_comp_u(const BetaComp g, const int type
     if (type == 2) {
       const float ux = Uf(0), vx = Uf(1) + 1.1920928955078125e-07f / 8;
       const float lv = logf_(vx);
-      float xx;
-      if (ux < g.f_px) {
-        xx = expf_(g.f_inv * lv);
-        if (ACC) acc = Uf(2) < expf_(-xx);
-      } else {
-        xx = 1.0f - lv;
-        if (ACC) acc = Uf(2) < expf_(logf_(xx) * g.f_am1);
-      }
-      return f2u(1.0f * xx);
+      const bool c = ux < g.f_px;
+      if (!ACC) return f2u(1.0f * (c ? expf_(g.f_inv * lv) : 1.0f - lv));
+      const float e1 = expf_(c ? g.f_inv * lv : logf_(1.0f - lv) * g.f_am1);  // one exp for both branches
+      acc = Uf(2) < (c ? expf_(-e1) : e1);
+      return f2u(1.0f * (c ? e1 : 1.0f - lv));
     }
     const float a1 = g.f_am1, sq = g.f_sq;
     float ys, yc;
