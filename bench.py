@@ -78,7 +78,7 @@ def kernel_of(name, compat=False):
     base, tag = name.split("/")
     if compat:
         if base == "beta":
-            return f"k_beta<{'float' if tag == 'f32' else 'double'}> (one CTA)"
+            return f"k_beta<{'float' if tag == 'f32' else 'double'}, GS, integral> (one CTA)"
         if base == "poisson4":
             return "k_poisson (one CTA)"
         if base in ("gamma0.5", "poisson100"):
@@ -86,7 +86,7 @@ def kernel_of(name, compat=False):
         return "k_prefix + k_jump + " + ("k_staged" if base in ("gamma5", "binomial20") else "k_direct") + \
             " (jump-ahead segments)"
     if base == "beta":
-        return f"k_beta<{'float' if tag == 'f32' else 'double'}>"
+        return f"k_beta<{'float' if tag == 'f32' else 'double'}, GS, integral>"
     if base in ("gamma0.5", "poisson100"):
         return "k_reject"
     if base in ("gamma5", "binomial20"):
@@ -102,9 +102,9 @@ def kernel_of(name, compat=False):
 # binds the kernel when it is not HBM
 MEASURED = {
     "uniformReal/f32": {"dram_bytes_per_sample": 3.276, "profile": "profiles/k_direct_uniform_f32_8192sq.md"},
-    "beta/f64": {"dram_bytes_per_sample": 5.17, "fp64_pipe_active": 0.166, "issue_active": 0.506,
-                 "note": "latency-bound: each CTA waits on its thread-0 walk over the accept masks; "
-                         "FP64 pipe 17%, ALU 39%, issue active 51% (not HBM, not FP64)",
+    "beta/f64": {"dram_bytes_per_sample": 5.19, "fp64_pipe_active": 0.270, "issue_active": 0.633,
+                 "note": "issue-bound on the integer double log / exp of the masks and values (the walk "
+                         "runs on its own warp): issue active 63%, ALU 52%, FP64 pipe 27% (not HBM)",
                  "profile": "profiles/k_beta_f64_2048sq.md"},
 }
 

@@ -12,8 +12,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
-#include <cstdlib>
-#include <cstring>
 #include <type_traits>
 
 #include "../../include/gpurand.h"
@@ -1983,49 +1981,19 @@ cudaError_t launch_poisson_segmented(const Plan& p, const DistParams& d, const P
 // component is closed form (alpha == 1: 1 packet; integer alpha < 20: alpha
 // packets) or a rejection sampler (GS trials of 3 packets, tan trials of 2)
 // with its own CompressMask carry.
-// The ring of packets is the newest two raw engine blocks in shared memory,
-// tempered where read (no tempered copy), so four CTAs fit on an SM and all
-// engines run in one wave.  Per block of 312 packets:
-//   masks  every start position of a rejection component gets its P-lane
-//          accept mask (all threads; ballot per P lanes);
-//   walk   thread 0 follows the reference automaton over the masks only:
-//          output packet sources (closed form / full trial at x, or FIFO
-//          packet at a lane offset) and the partial trials it consumed;
-//   values the accepted lanes of the consumed partial trials are listed by
-//          FIFO slot; then one thread per lane, with no idle lanes, computes
-//          them into the lane buffer and the full-trial lanes of the
-//          rejection component into a value buffer (a value-only evaluation:
-//          acceptance is already known);
-//   write  p1 / (p1 + p2) per output lane, the other component computed in
-//          place; lanes still carried move to the front of the lane buffer.
+// The ring of packets is the newest three raw engine blocks in shared
+// memory, tempered where read (no tempered copy), so four CTAs fit on an SM
+// and all engines run in one wave.  Every start position of a rejection
+// component gets its P-lane accept mask ahead of the walk; the walk over
+// the masks and the value work run on separate warps (the kernel below).
 // ===========================================================================
 namespace {
 
-constexpr int kBetaThreads = 160;
-constexpr int kBetaRing = 1024;             // positions whose masks are kept (a power of two)
-constexpr int kBetaRec = 160;               // output packets per walk step
-constexpr int kBetaPT = 128;                // partial trials per component per walk step
+constexpr int kBetaRing = 1024;  // positions whose accept masks are kept (a power of two)
 
 template <int DT>
 __host__ __device__ constexpr int beta_lanes() {
   return DT == SD_F64 ? 4 : 8;
-}
-template <int DT>
-__host__ __device__ constexpr int beta_lb() {  // lane buffer per component: carried lanes + partial-trial lanes
-  return 8 + kBetaPT * beta_lanes<DT>();
-}
-
-template <int DT>
-__host__ __device__ constexpr size_t beta_smem_bytes() {
-  return (size_t)3 * kLanes * kN * 8 +                                             // raw windows
-         (size_t)kBetaRec * 2 * 8 +                                                // rec
-         (size_t)2 * kBetaPT * 8 +                                                 // partial trial positions
-         ((size_t)2 * beta_lb<DT>() + (size_t)kBetaRec * beta_lanes<DT>()) *       // lane buffers, values of
-             (DT == SD_F64 ? 8 : 4) +                                              //   full trials
-         (size_t)2 * kBetaPT * 4 * 2 +                                             // lane offsets, masks
-         (size_t)kBetaRec * 2 +                                                    // full-trial records
-         (size_t)2 * kBetaPT * beta_lanes<DT>() * 2 +                              // partial-lane tasks
-         (size_t)2 * kBetaRing;                                                    // masks per position
 }
 
 // Constants of one GammaGen component of a BetaGen, computed on the host
@@ -2142,414 +2110,9 @@ __device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j
 
 }  // namespace
 
-template <int DT>  // SD_F32 or SD_F64
-__global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks) {
-  constexpr int P = beta_lanes<DT>();
-  constexpr int LB = beta_lb<DT>();
-  using V = typename std::conditional<DT == SD_F64, uint64_t, uint32_t>::type;
-  extern __shared__ __align__(16) uint64_t beta_dyn[];
-  uint64_t(*raw)[kLanes][kN] = reinterpret_cast<uint64_t(*)[kLanes][kN]>(beta_dyn);
-  int64_t* rec = reinterpret_cast<int64_t*>(beta_dyn + 3 * kLanes * kN);   // [kBetaRec][2]
-  int64_t* ptx = rec + kBetaRec * 2;                                         // [2][kBetaPT]
-  V* lanebuf = reinterpret_cast<V*>(ptx + 2 * kBetaPT);                      // [2][LB]
-  V* fullval = lanebuf + 2 * LB;                                             // [kBetaRec][P]
-  int32_t* pA = reinterpret_cast<int32_t*>(fullval + kBetaRec * P);          // [2][kBetaPT]
-  uint32_t* pm = reinterpret_cast<uint32_t*>(pA + 2 * kBetaPT);              // [2][kBetaPT]
-  uint16_t* fr = reinterpret_cast<uint16_t*>(pm + 2 * kBetaPT);              // [kBetaRec]
-  uint16_t* ptask = fr + kBetaRec;                                           // [2][kBetaPT * P]
-  uint8_t* pmask = reinterpret_cast<uint8_t*>(ptask + 2 * kBetaPT * P);      // [2][kBetaRing]
-  __shared__ int s_nrec, s_nf, s_np[2], s_fc[2], s_A[2], s_A0[2];
-  __shared__ int s_stop, s_err, s_more;
-  __shared__ int64_t s_ebase, s_end;
-
-  const int k = blockIdx.x;
-  const int tid = threadIdx.x;
-  EngState* st = p.eng + k;
-  GenState* gs = p.gen + k;
-  const int64_t g0 = (int64_t)k * p.gran_per_k + min((int64_t)k, p.gran_rem);
-  const int64_t ng = p.gran_per_k + ((int64_t)k < p.gran_rem ? 1 : 0);
-  const int64_t off = g0 * p.gran, n = ng * p.gran;
-  if (n == 0) return;
-  const int64_t Npk = n / P;
-
-  const int type0 = bk.c[0].type, U0 = bk.c[0].U, type1 = bk.c[1].type, U1 = bk.c[1].U;
-  const bool post = bk.post == 1;
-  const int umax = max(max(U0, U1), 3);
-  // the component whose full-trial values are computed ahead of the outputs
-  // (a rejection one); the other is computed where its output is written
-  const int bc = type0 >= 2 ? 0 : (type1 >= 2 ? 1 : -1);
-  load_window(raw[2], &st->win[0][0], kN);  // block -1; block b lives in window b mod 3
-  // carried lanes of the two GammaGens (generator slots 1 and 2)
-  if (tid < 2 * 8) {
-    const int c = tid / 8, j = tid % 8;
-    const GenSlot& g = gs->s[1 + c];
-    if (j < g.rest_cnt)
-      lanebuf[c * LB + j] = (V)(DT == SD_F64 ? ((uint64_t)g.rest[2 * j] | ((uint64_t)g.rest[2 * j + 1] << 32))
-                                             : (uint64_t)g.rest[j]);
-  }
-  if (tid == 0) {
-    s_err = 0;
-    s_stop = 0;
-    s_fc[0] = gs->s[1].rest_cnt;
-    s_fc[1] = gs->s[2].rest_cnt;
-  }
-  __syncthreads();
-  // The newest three raw blocks are the ring of packets; words are tempered
-  // where they are read.  Each thread keeps its own view of the newest block.
-  int64_t ring_new = 0;         // first packet of the newest block
-  int wb0 = 0, wb1 = 2, wb2 = 1;  // windows of the newest block and the two before
-  auto set_ring = [&](int64_t B) {
-    ring_new = B * kN;
-    wb0 = (int)(B % 3);
-    wb1 = (int)((B + 2) % 3);
-    wb2 = (int)((B + 1) % 3);
-  };
-  auto tword = [&](int64_t rel, int l) -> uint64_t {
-    int dd = (int)(rel - ring_new);
-    int w = wb0;
-    if (dd < 0) {
-      dd += kN;
-      w = wb1;
-      if (dd < 0) {
-        dd += kN;
-        w = wb2;
-      }
-    }
-    if ((unsigned)dd >= (unsigned)kN) dd = 0;  // outside the ring: never read past the buffers
-    return mt_temper(raw[w][l][dd]);
-  };
-  auto word = [&](int64_t w) -> uint32_t {
-    const uint64_t v = tword(w >> 3, (int)((w & 7) >> 1));
-    return (w & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
-  };
-  auto rval = [&](int64_t r) -> uint64_t { return tword(r >> 2, (int)(r & 3)); };
-  auto trial = [&](int c, int64_t x, int j, bool& acc) -> uint64_t {
-    return c == 0 ? beta_comp<DT, true>(bk.c[0], x, j, word, rval, acc)
-                  : beta_comp<DT, true>(bk.c[1], x, j, word, rval, acc);
-  };
-  // value of an accepted trial lane or a closed-form draw; double GS lanes
-  // use the branch threshold in integer form
-  auto value = [&](int c, int64_t x, int j) -> uint64_t {
-    bool acc;
-    if (c == 0) {
-      if (DT == SD_F64 && type0 == 2)
-        return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[0].tpx, bk.c[0].d_inv));
-      return beta_comp<DT, false>(bk.c[0], x, j, word, rval, acc);
-    }
-    if (DT == SD_F64 && type1 == 2)
-      return d2u(1.0 * gs_value_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), bk.c[1].tpx, bk.c[1].d_inv));
-    return beta_comp<DT, false>(bk.c[1], x, j, word, rval, acc);
-  };
-  // rejection components evaluated at every position
-  const int nrej = (type0 >= 2 ? 1 : 0) + (type1 >= 2 ? 1 : 0);
-  const int rej0 = type0 >= 2 ? 0 : 1;  // first rejection component
-
-  int64_t s = 0, E = 0, done_pos = 0;  // walk state (thread 0 reads / writes s and E)
-  int sr = 0;                           // s mod kBetaRing
-  int fc[2] = {0, 0};
-  if (tid == 0) {
-    fc[0] = s_fc[0];
-    fc[1] = s_fc[1];
-  }
-  // accept masks of the rejection components at positions [from, to), by
-  // threads t = 0 .. T-1 of whole warps
-  auto masks = [&](int64_t from, int64_t to, int t, int T) {
-    if (nrej == 0) return;
-    // (32-bit index arithmetic with shifts: a 64-bit division by a runtime
-    // value would run on the FP64 pipe)
-    constexpr int LP = P == 8 ? 3 : 2;
-    const int sh = LP + nrej - 1;  // log2(nrej * P)
-    const int cnt = (int)(to - from) << sh;
-    for (int base = 0; base < cnt; base += T) {
-      const int e = base + t;
-      const bool valid = e < cnt;
-      bool acc = false;
-      int c = 0;
-      int64_t x = 0;
-      if (valid) {
-        const int xi = e >> sh;
-        const int ci = (e >> LP) & (nrej - 1);
-        c = nrej == 2 ? ci : rej0;
-        x = from + xi;
-        const int j = e & (P - 1);
-        int f = -1;
-        if (DT == SD_F64 && (c == 0 ? type0 : type1) == 2)  // float pre-test of a double GS trial
-          f = c == 0 ? gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[0].f_px,
-                                     bk.c[0].f_inv, bk.c[0].f_am1, bk.c[0].f_band)
-                     : gs_filter_f64(rval(x * 4 + j), rval((x + 1) * 4 + j), rval((x + 2) * 4 + j), bk.c[1].f_px,
-                                     bk.c[1].f_inv, bk.c[1].f_am1, bk.c[1].f_band);
-        if (f >= 0) acc = f == 1;
-        else trial(c, x, j, acc);
-      }
-      const uint32_t bal = __ballot_sync(0xffffffffu, acc);
-      if (valid && (e % P) == 0)
-        pmask[c * kBetaRing + (int)(x & (kBetaRing - 1))] =
-            (uint8_t)((bal >> (threadIdx.x & 31 & ~(P - 1))) & ((1u << P) - 1));
-    }
-  };
-  // block 0 and its masks (all threads); afterwards warps 1-4 make block b+1
-  // and its masks while thread 0 walks block b
-  mt_block(raw[2], raw[0], [&](int, const uint64_t*) {});
-  set_ring(0);
-  masks(0, kN - umax + 1, tid, kBetaThreads);
-  done_pos = kN - umax + 1;
-  int64_t nblk = 1;             // blocks generated
-  int64_t pk_avail = kN;        // packets generated
-  __syncthreads();
-  int64_t nb = 0;
-  for (;; ++nb) {
-    const bool gen = nb + 1 < max_blocks;
-    const int64_t lim_next = (nb + 2) * kN - umax + 1;
-    if (tid == 0 && gen && lim_next - s > kBetaRing) s_err = 1;  // masks would overwrite unwalked positions
-    bool first = true;
-    // walk, then values, then outputs, until the evaluated positions are used
-    // up (a walk step stops early when its record buffers fill)
-    for (;;) {
-      if (first && gen && tid >= 32) {
-        // ---- warps 1-4: the next block (twist by 128 threads, named barrier
-        // 1) and its masks, while thread 0 walks
-        const int tt = tid - 32;
-        uint64_t(*old)[kN] = raw[nb % 3];
-        uint64_t(*nw)[kN] = raw[(nb + 1) % 3];
-#pragma unroll 1
-        for (int ph = 0; ph < 2; ++ph) {
-          for (int ii = tt; ii < kM; ii += kBetaThreads - 32) {
-            const int i = ph * kM + ii;
-#pragma unroll
-            for (int l = 0; l < kLanes; ++l) {
-              const uint64_t bb = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
-              const uint64_t cc2 = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
-              nw[l][i] = mt_twist(old[l][i], bb, cc2);
-            }
-          }
-          asm volatile("bar.sync 1, %0;" ::"r"(kBetaThreads - 32) : "memory");
-        }
-        set_ring(nb + 1);
-        masks(done_pos, lim_next, tt, kBetaThreads - 32);
-      }
-      // ---- walk (thread 0): sources of the next output packets
-      if (tid == 0) {
-        s_ebase = E;
-        s_more = 0;
-        s_A0[0] = fc[0];
-        s_A0[1] = fc[1];
-        int nrec = 0, nf = 0, np[2] = {0, 0}, A[2] = {fc[0], fc[1]};
-        const int64_t pk_end = pk_avail;       // packets generated so far
-        if (s < (nb - 1) * kN) s_err = 1;      // packets before s left the ring
-        while (E < Npk) {
-          if (nrec >= kBetaRec) {
-            s_more = 1;
-            break;
-          }
-          int64_t x = s;
-          int xr = sr;  // x mod kBetaRing, advanced with x
-          bool full_bc = false;
-          auto adv = [&](int U) {
-            x += U;
-            xr += U;
-            if (xr >= kBetaRing) xr -= kBetaRing;
-          };
-          // one component of output record nrec: 0 done, 1 partial-trial
-          // buffer full, 2 positions not evaluated yet (component index a
-          // compile-time constant, so the walk state stays in registers)
-          auto step = [&](auto cc) -> int {
-            constexpr int c = decltype(cc)::value;
-            const int ty = c == 0 ? type0 : type1, U = c == 0 ? U0 : U1;
-            if (ty <= 1) {
-              if (x + U > pk_end) return 2;
-              rec[nrec * 2 + c] = x;
-              adv(U);
-              return 0;
-            }
-            for (;;) {
-              if (x >= done_pos) return 2;
-              if (np[c] >= kBetaPT) return 1;
-              const uint32_t m = pmask[c * kBetaRing + xr];
-              const int cn = __popc(m);
-              if (cn == P) {
-                rec[nrec * 2 + c] = x;
-                if (c == bc) full_bc = true;
-                adv(U);
-                return 0;
-              }
-              ptx[c * kBetaPT + np[c]] = x;
-              pA[c * kBetaPT + np[c]] = A[c];
-              pm[c * kBetaPT + np[c]] = m;
-              ++np[c];
-              A[c] += cn;
-              fc[c] += cn;
-              adv(U);
-              if (fc[c] >= P) {
-                rec[nrec * 2 + c] = -(int64_t)(1 + (A[c] - fc[c]));
-                fc[c] -= P;
-                return 0;
-              }
-            }
-          };
-          // a record that does not fit rolls back: it waits for the next
-          // step (buffer full) or the next block (positions not evaluated)
-          const int np0 = np[0], np1 = np[1], a0 = A[0], a1 = A[1], f0 = fc[0], f1 = fc[1];
-          int stall = step(std::integral_constant<int, 0>{});
-          if (!stall) stall = step(std::integral_constant<int, 1>{});
-          if (stall) {
-            np[0] = np0;
-            np[1] = np1;
-            A[0] = a0;
-            A[1] = a1;
-            fc[0] = f0;
-            fc[1] = f1;
-            if (stall == 1) {
-              if (nrec == 0) s_err = 1;  // one record needs more partial trials than the buffer holds
-              else s_more = 1;
-            }
-            break;
-          }
-          if (full_bc) fr[nf++] = (uint16_t)nrec;
-          ++nrec;
-          s = x;
-          sr = xr;
-          ++E;
-        }
-        s_nrec = nrec;
-        s_nf = nf;
-        s_np[0] = np[0];
-        s_np[1] = np[1];
-        s_A[0] = A[0];
-        s_A[1] = A[1];
-        s_fc[0] = fc[0];
-        s_fc[1] = fc[1];
-        if (E >= Npk) {
-          s_stop = 1;
-          s_end = s;
-        }
-      }
-      __syncthreads();
-      if (first) {  // block nb + 1 and its masks are ready
-        first = false;
-        if (gen) {
-          set_ring(nb + 1);
-          done_pos = lim_next;
-          nblk = nb + 2;
-          pk_avail = (nb + 2) * kN;
-        } else {
-          set_ring(nb);
-        }
-      }
-      // ---- accepted lanes of the partial trials, listed by their FIFO slot
-      const int np0 = s_np[0], np1 = s_np[1];
-      const int a00 = s_A0[0], a01 = s_A0[1];
-      for (int e = tid; e < (np0 + np1) * P; e += kBetaThreads) {
-        const int c = e < np0 * P ? 0 : 1;
-        const int kk = (c == 0 ? e : e - np0 * P) / P, j = e % P;
-        const uint32_t m = pm[c * kBetaPT + kk];
-        if ((m >> j) & 1u)
-          ptask[c * kBetaPT * P + pA[c * kBetaPT + kk] - (c == 0 ? a00 : a01) + __popc(m & ((1u << j) - 1))] =
-              (uint16_t)(kk * 8 + j);
-      }
-      __syncthreads();
-      // ---- values, one lane per thread with no idle lanes: full trials of
-      // the buffered component, then the accepted partial-trial lanes
-      const int t0 = s_nf * P, tp0 = s_A[0] - a00, tp1 = s_A[1] - a01;
-      for (int t = tid; t < t0 + tp0 + tp1; t += kBetaThreads) {
-        if (t < t0) {
-          const int i = fr[t / P], j = t % P;
-          fullval[i * P + j] = (V)value(bc, rec[i * 2 + bc], j);
-        } else {
-          const int c = t < t0 + tp0 ? 0 : 1;
-          const int q = c == 0 ? t - t0 : t - t0 - tp0;
-          const int tk = ptask[c * kBetaPT * P + q];
-          lanebuf[c * LB + (c == 0 ? a00 : a01) + q] = (V)value(c, ptx[c * kBetaPT + (tk >> 3)], tk & 7);
-        }
-      }
-      __syncthreads();
-      // ---- output packets
-      const int nrec = s_nrec;
-      const int64_t e_first = s_ebase;
-      for (int e = tid; e < nrec * P; e += kBetaThreads) {
-        const int i = e / P, j = e % P;
-        uint64_t v[2];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          const int64_t src = rec[i * 2 + c];
-          if (src < 0) v[c] = (uint64_t)lanebuf[c * LB + (int)(-src - 1) + j];
-          else if (c == bc) v[c] = (uint64_t)fullval[i * P + j];
-          else v[c] = value(c, src, j);
-        }
-        if (DT == SD_F32) {
-          const float p1 = u2f((uint32_t)v[0]), p2 = u2f((uint32_t)v[1]);
-          const float x = p1 / (p1 + p2);
-          reinterpret_cast<float*>(p.out)[off + (e_first + i) * P + j] = post ? (bk.fpost * x) / (1.0f - x) : x;
-        } else {
-          const double p1 = u2d(v[0]), p2 = u2d(v[1]);
-          const double x = p1 / (p1 + p2);
-          reinterpret_cast<double*>(p.out)[off + (e_first + i) * P + j] = post ? (bk.dpost * x) / (1.0 - x) : x;
-        }
-      }
-      __syncthreads();
-      // ---- lanes still carried move to the front of each lane buffer
-      V carry = 0;
-      const int cc = tid / 8, cj = tid % 8;
-      const bool mover = tid < 16 && cj < s_fc[cc];
-      if (mover) carry = lanebuf[cc * LB + s_A[cc] - s_fc[cc] + cj];
-      __syncthreads();
-      if (mover) lanebuf[cc * LB + cj] = carry;
-      __syncthreads();
-      if (!s_more || s_stop || s_err) break;
-    }
-    if (s_stop || s_err || !gen) break;
-  }
-
-  // ---- state after the call
-  if (tid == 0) {
-    if (!s_stop) s_end = s;
-    if (!s_stop || s_err) atomicOr(&st->status, (int)GR_DEV_REJECT_LIMIT);
-  }
-  __syncthreads();
-  const int64_t np = s_end;  // packets consumed
-  if (np > 0) {
-    const int64_t B = nblk - 1;          // newest block; windows hold B, B - 1, B - 2
-    const int64_t lastb = (np - 1) / kN;
-    const int rr = (int)(np - lastb * kN);  // in [1, 312]
-    if (lastb == B) {
-      store_window(st, raw[B % 3], raw[(B + 2) % 3], rr);
-    } else if (lastb == B - 1) {
-      store_window(st, raw[(B + 2) % 3], raw[(B + 1) % 3], rr);
-    } else if (lastb == B - 2 && B >= 2) {
-      // block B - 3 was overwritten by block B: recover it from block B - 2
-      // into block B's window (MT19937-64's twist inverts)
-      if (tid < kLanes) {
-        uint64_t* nwl = raw[(B + 1) % 3][tid];
-        uint64_t* odl = raw[B % 3][tid];
-        mt_untwist_block([&](int i) -> uint64_t& { return nwl[i]; }, [&](int i) -> uint64_t& { return odl[i]; });
-      }
-      __syncthreads();
-      store_window(st, raw[(B + 1) % 3], raw[B % 3], rr);
-    } else if (tid == 0) {
-      atomicOr(&st->status, (int)GR_DEV_BAD_INPUT);
-    }
-  }
-  if (tid < 2 * 8) {
-    const int c = tid / 8, j = tid % 8;
-    GenSlot& g = gs->s[1 + c];
-    const uint64_t v = j < s_fc[c] ? (uint64_t)lanebuf[c * LB + j] : 0;
-    if (DT == SD_F64) {
-      g.rest[2 * j] = (uint32_t)v;
-      g.rest[2 * j + 1] = (uint32_t)(v >> 32);
-    } else {
-      g.rest[j] = (uint32_t)v;
-    }
-  }
-  __syncthreads();
-  if (tid == 0) {
-    gs->s[1].rest_cnt = s_fc[0];
-    gs->s[2].rest_cnt = s_fc[1];
-    st->consumed += (uint64_t)max(np, (int64_t)0);
-  }
-}
-
 // ===========================================================================
-// k_beta_chase: the BetaGen walk with the reference automaton on a warp of
-// its own, one step ahead of the workers.
+// k_beta: the walk with the reference automaton on a warp of its own, one
+// step ahead of the workers.
 //   chase  (warp 0) follows the automaton over the accept masks: per trial
 //          of a rejection component one mask read, its popcount and two
 //          compares.  Per step it records the source of every output packet
@@ -2605,7 +2168,7 @@ __host__ __device__ constexpr size_t bc_smem_bytes() {
 }  // namespace
 
 template <int DT, int TY0, int TY1>  // DT: SD_F32 or SD_F64
-__global__ void __maxnreg__(80) k_beta_chase(Plan p, BetaConsts bk, int64_t max_blocks) {
+__global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks) {
   constexpr int P = beta_lanes<DT>();
   constexpr int LB = bc_lb<DT>();
   constexpr unsigned FULL = 0xffffffffu;
@@ -3068,24 +2631,22 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  constexpr size_t smem = beta_smem_bytes<DT>(), smem2 = bc_smem_bytes<DT>();
+  constexpr size_t smem = bc_smem_bytes<DT>();
   if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_beta<DT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_beta<DT, -1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_beta_chase<DT, -1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+      e = cudaFuncSetAttribute(k_beta<DT, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_beta_chase<DT, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_beta_chase<DT, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+      e = cudaFuncSetAttribute(k_beta<DT, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  const char* fv = std::getenv("GR_BETA_FORM");
+  // the GS + integral-alpha pairs (beta(a < 1, integer b) and the mirror)
+  // have kernels of their own
   const int t0 = bk.c[0].type, t1 = bk.c[1].type;
-  if (fv && std::strcmp(fv, "walk") == 0) k_beta<DT><<<p.K, kBetaThreads, smem, s>>>(p, bk, max_blocks);
-  else if (t0 == 2 && t1 == 1) k_beta_chase<DT, 2, 1><<<p.K, kBcThreads, smem2, s>>>(p, bk, max_blocks);
-  else if (t0 == 1 && t1 == 2) k_beta_chase<DT, 1, 2><<<p.K, kBcThreads, smem2, s>>>(p, bk, max_blocks);
-  else k_beta_chase<DT, -1, -1><<<p.K, kBcThreads, smem2, s>>>(p, bk, max_blocks);
+  if (t0 == 2 && t1 == 1) k_beta<DT, 2, 1><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
+  else if (t0 == 1 && t1 == 2) k_beta<DT, 1, 2><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
+  else k_beta<DT, -1, -1><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
   return cudaGetLastError();
 }
 
