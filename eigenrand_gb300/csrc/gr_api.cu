@@ -485,12 +485,14 @@ gr_status build_discrete(const std::vector<double>& w, std::vector<int32_t>& pro
   return GR_OK;
 }
 
-gr_status ensure_gen_state(gr_gen* g, int K) {
+// Zeroed on the call's stream: a plain cudaMemset runs on the legacy stream,
+// which streams created non-blocking (the serving loop's) do not wait for.
+gr_status ensure_gen_state(gr_gen* g, int K, cudaStream_t s) {
   if (g->gst && g->gst_K == K) return GR_OK;
   cudaFree(g->gst);
   g->gst = nullptr;
   GR_CUDA(cudaMalloc(&g->gst, sizeof(GenState) * (size_t)K));
-  GR_CUDA(cudaMemset(g->gst, 0, sizeof(GenState) * (size_t)K));
+  GR_CUDA(cudaMemsetAsync(g->gst, 0, sizeof(GenState) * (size_t)K, s));
   g->gst_K = K;
   return GR_OK;
 }
@@ -1121,11 +1123,11 @@ gr_status run_trunc(gr_engine* e, gr_gen* g, void* out, size_t n, cudaStream_t s
   if (!out) return fail(GR_ERR_INVALID, "output is NULL");
   if (e->K != 1) return fail(GR_ERR_UNSUPPORTED, "TruncGen rejection needs a single-stream engine");
   gr_gen* b = g->trunc_base;
-  gr_status st = ensure_gen_state(b, 1);
+  gr_status st = ensure_gen_state(b, 1, s);
   if (st != GR_OK) return st;
   if (!g->trunc_carry) {
     GR_CUDA(cudaMalloc(&g->trunc_carry, sizeof(GenSlot)));
-    GR_CUDA(cudaMemset(g->trunc_carry, 0, sizeof(GenSlot)));
+    GR_CUDA(cudaMemsetAsync(g->trunc_carry, 0, sizeof(GenSlot), s));
   }
   const int64_t upk = fixed_packets_per_packet(b->dp);
   const int64_t need = (int64_t)(n / (size_t)P);
@@ -1383,7 +1385,7 @@ gr_status gr_generate(gr_gen* g, gr_engine* e, void* dev_out, size_t n, gr_strea
     if (need_four_lanes(e, "truncated rejection") != GR_OK) return GR_ERR_UNSUPPORTED;
     return run_trunc(e, g, dev_out, n, (cudaStream_t)stream);
   }
-  gr_status st = ensure_gen_state(g, e->K);
+  gr_status st = ensure_gen_state(g, e->K, (cudaStream_t)stream);
   if (st != GR_OK) return st;
   return run_call(e, g, g->dp, dev_out, n, (cudaStream_t)stream);
 }
@@ -1586,7 +1588,7 @@ gr_status gr_generate_v(gr_gen* g, gr_engine* e, const void* dev_a, const void* 
     dp.de = d.a;
     dp.df = d.b;
   }
-  st = ensure_gen_state(g, e->K);
+  st = ensure_gen_state(g, e->K, (cudaStream_t)stream);
   if (st != GR_OK) return st;
   return run_call(e, g, dp, dev_out, n, (cudaStream_t)stream);
 }

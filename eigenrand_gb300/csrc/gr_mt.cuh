@@ -30,29 +30,33 @@ __device__ __forceinline__ double ur_d(uint64_t x) {
 }
 
 // One block (312 packets) of a 4-lane engine, computed by a CTA of >= 156
-// threads: new[l][i] from old[l][*] in two phases of 156 independent words.
+// threads: thread t makes new words t and t + 156.  Word t + 156 needs new
+// word t (kept in a register) and, for word 311, new word 0 (recomputed from
+// the old block), so the halves need no barrier between them.
 // per_packet(i, pk) runs on the thread that produced packet i of the block
 // (pk = the 4 tempered lane words).  Ends with a CTA barrier.
 template <class F>
 __device__ __forceinline__ void mt_block(uint64_t (*old)[kN], uint64_t (*nw)[kN], F&& per_packet) {
   const int tid = threadIdx.x;
+  if (tid < kM) {
+    uint64_t lo[kLanes];
 #pragma unroll 1
-  for (int ph = 0; ph < 2; ++ph) {
-    if (tid < kM) {
+    for (int ph = 0; ph < 2; ++ph) {
       const int i = ph * kM + tid;
       uint64_t pk[kLanes];
 #pragma unroll
       for (int l = 0; l < kLanes; ++l) {
-        uint64_t b = (i + 1 < kN) ? old[l][i + 1] : nw[l][0];
-        uint64_t c = (ph == 0) ? old[l][i + kM] : nw[l][i - kM];
-        uint64_t v = mt_twist(old[l][i], b, c);
+        const uint64_t b = (i + 1 < kN) ? old[l][i + 1] : mt_twist(old[l][0], old[l][1], old[l][kM]);
+        const uint64_t c = (ph == 0) ? old[l][i + kM] : lo[l];
+        const uint64_t v = mt_twist(old[l][i], b, c);
         nw[l][i] = v;
+        if (ph == 0) lo[l] = v;
         pk[l] = mt_temper(v);
       }
       per_packet(i, pk);
     }
-    __syncthreads();
   }
+  __syncthreads();
 }
 
 // Packet `rel` of the two-block ring tp (blocks go to slots 0, 1, 0, ... in

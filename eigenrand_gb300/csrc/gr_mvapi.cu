@@ -287,6 +287,9 @@ gr_status mvnormal_clone(const gr_mvnormal* src, gr_mvnormal** out) {
   }
   if (e == cudaSuccess) e = cudaMalloc(&g->mean, es * src->dim);
   if (e == cudaSuccess) e = cudaMemcpy(g->mean, src->mean, es * src->dim, cudaMemcpyDeviceToDevice);
+  // device-to-device copies return before they finish, and the clone's
+  // users launch on streams that do not wait for the legacy stream
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
   gr_status st = e == cudaSuccess ? GR_OK : mv_fail(GR_ERR_CUDA, std::string("MvNormalGen copy: ") + cudaGetErrorString(e));
   if (st == GR_OK) st = make_gen(&g->normal, GR_NORMAL_STD, g->dtype, 0.0);
   if (st != GR_OK) {
@@ -762,7 +765,7 @@ gr_status gr_multinomial_sample(gr_multinomial* g, gr_engine* e, int32_t* dev_ou
     g->gst = nullptr;
     g->gst_K = 0;
     MV_CUDA(cudaMalloc(&g->gst, sizeof(GenState) * (size_t)K));
-    MV_CUDA(cudaMemset(g->gst, 0, sizeof(GenState) * (size_t)K));
+    MV_CUDA(cudaMemsetAsync(g->gst, 0, sizeof(GenState) * (size_t)K, s));
     g->gst_K = K;
   }
   MnArgs a{};
