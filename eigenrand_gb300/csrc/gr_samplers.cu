@@ -2034,10 +2034,11 @@ BetaComp beta_component(int branch, float af, double ad) {
 }
 
 // Value (closed form) or candidate (rejection trial) of one GammaGen
-// component at packet position x, lane j.  ACC: also decide acceptance (the
-// rejection types); without it only the candidate is computed, for lanes
-// already known to be accepted (the same expressions, so the same bits).
-// Uf(q) / Ud(q): the uniform of lane j of packet x + q.
+// component of sampler type `type` at one lane: Uf(q) / Ud(q) give the
+// lane's uniform in the q-th packet of the draw.  ACC: also decide
+// acceptance (the rejection types); without it only the candidate is
+// computed, for lanes already known to be accepted (the same expressions,
+// so the same bits).
 template <int DT, bool ACC, class UFF, class UDF>
 __device__ __forceinline__ uint64_t beta_comp_u(const BetaComp g, const int type, UFF&& Uf, UDF&& Ud, bool& acc) {
   acc = true;
@@ -2099,13 +2100,6 @@ __device__ __forceinline__ uint64_t beta_comp_u(const BetaComp g, const int type
     }
     return d2u(1.0 * xx);
   }
-}
-
-template <int DT, bool ACC, class WF, class RF>
-__device__ __forceinline__ uint64_t beta_comp(const BetaComp g, int64_t x, int j, WF&& word, RF&& rval, bool& acc) {
-  return beta_comp_u<DT, ACC>(
-      g, g.type, [&](int q) { return ur_f(word((x + q) * 8 + j)); }, [&](int q) { return ur_d(rval((x + q) * 4 + j)); },
-      acc);
 }
 
 }  // namespace
