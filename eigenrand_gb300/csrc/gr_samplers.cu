@@ -2131,8 +2131,9 @@ __device__ __forceinline__ uint64_t beta_comp_u(const BetaComp g, const int type
 // ===========================================================================
 namespace {
 
-constexpr int kBcThreads = 192;
-constexpr int kBcWork = kBcThreads - 32;
+constexpr int kBcThreads = 192;       // four CTAs per SM
+constexpr int kBcThreadsAlone = 512;  // one CTA per SM (no more engines than SMs): fifteen worker warps
+constexpr uint16_t kBcTabNone = 0xffffu;  // visit-table entry not known yet
 constexpr int kBcRec = 160;         // output packets per step (a block holds at most 156)
 constexpr int kBcFifo = 112;        // FIFO outputs per component per step (at most 104 per block)
 constexpr int kBcFull = 112;        // full-trial outputs of the buffered component per step
@@ -2148,9 +2149,10 @@ struct BcStep {
   int nrec, nf, fs[2], A[2], f[2];
 };
 
-template <int DT>
+template <int DT, bool TAB>
 __host__ __device__ constexpr size_t bc_smem_bytes() {
-  return (size_t)3 * kLanes * kN * 8 +                                                   // raw windows
+  return (TAB ? (size_t)kBetaRing * beta_lanes<DT>() * 2 + (size_t)2 * kBcRec * 6 : 0) +  // visit table, record starts
+         (size_t)3 * kLanes * kN * 8 +                                                   // raw windows
          ((size_t)2 * bc_lb<DT>() + (size_t)(kBcFull + kBcRec) * beta_lanes<DT>()) *     // lane buffers, full-
              (DT == SD_F64 ? 8 : 4) +                                                    //   trial and positional values
          (size_t)2 * kBcRec * 2 * 2 +                                                    // records
@@ -2161,8 +2163,17 @@ __host__ __device__ constexpr size_t bc_smem_bytes() {
 
 }  // namespace
 
-template <int DT, int TY0, int TY1>  // DT: SD_F32 or SD_F64
+// ALONE: one CTA per SM.  For the GS + integral-alpha pairs it also keeps a
+// visit table: for every position and carry, where the GS visit starting
+// there ends, whether on a full trial, and the lanes its partial trials
+// accept.  The chase then reads one entry per record, and the workers
+// expand each record's partial trials into FIFO slots themselves.
+template <int DT, int TY0, int TY1, bool ALONE>  // DT: SD_F32 or SD_F64
 __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks) {
+  constexpr int NT = ALONE ? kBcThreadsAlone : kBcThreads;
+  constexpr int kBcWork = NT - 32;
+  constexpr bool kFusedPair = (TY0 == 2 && TY1 == 1) || (TY0 == 1 && TY1 == 2);
+  constexpr bool TAB = ALONE && kFusedPair;
   constexpr int P = beta_lanes<DT>();
   constexpr int LB = bc_lb<DT>();
   constexpr unsigned FULL = 0xffffffffu;
@@ -2176,9 +2187,14 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
   int16_t* fpos = rec + 2 * kBcRec * 2;                                  // [2][kBcFull]
   uint16_t* ptask = reinterpret_cast<uint16_t*>(fpos + 2 * kBcFull);     // [2][2][LB]
   uint8_t* pmask = reinterpret_cast<uint8_t*>(ptask + 2 * 2 * LB);       // [2][kBetaRing]
+  uint16_t* vtab = reinterpret_cast<uint16_t*>(pmask + 2 * kBetaRing);    // [kBetaRing][P] (TAB)
+  int16_t* rxs = reinterpret_cast<int16_t*>(vtab + (TAB ? kBetaRing * P : 0));  // [2][kBcRec] visit starts (TAB)
+  uint16_t* ras = reinterpret_cast<uint16_t*>(rxs + (TAB ? 2 * kBcRec : 0));    // [2][kBcRec] FIFO tail at the start
+  uint16_t* rfs = ras + (TAB ? 2 * kBcRec : 0);                                 // [2][kBcRec] carry at the start
   __shared__ BcStep s_step[2];
   __shared__ int s_done, s_err, s_fc[2];
   __shared__ int64_t s_end;
+  __shared__ unsigned long long s_inv[2];  // TAB: first position whose table entry is still unknown
 
   const int k = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -2344,10 +2360,47 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
       }
     }
   };
+  // TAB: visit-table entries of positions [from, to) (masks known below
+  // `to`), by threads t = 0 .. T-1; an entry whose visit runs past `to` stays
+  // unknown and its position is noted in *inv
+  constexpr int gcomp = TY0 == 2 ? 0 : 1;  // the GS component of a fused pair
+  auto build_table = [&](int64_t from, int64_t to, int t, int T, unsigned long long* inv) {
+    if (!TAB || to <= from) return;
+    const int U = gcomp == 0 ? U0 : U1;
+    const int cnt = (int)(to - from) * P;
+    for (int u = t; u < cnt; u += T) {
+      const int64_t x = from + u / P;
+      const int f = u % P;
+      uint16_t e = kBcTabNone;
+      int acc = 0;
+      for (int d = 0; d < 1024 - U; d += U) {
+        const int64_t xr = x + d;
+        if (xr >= to) break;
+        const uint32_t m = pmask[gcomp * kBetaRing + (int)(xr & (kBetaRing - 1))];
+        const int cn = __popc(m);
+        if (cn == P) {
+          e = (uint16_t)(d | (1 << 10) | (acc << 11));
+          break;
+        }
+        acc += cn;
+        if (f + acc >= P) {
+          e = (uint16_t)(d | (acc << 11));
+          break;
+        }
+      }
+      vtab[(int)(x & (kBetaRing - 1)) * P + f] = e;
+      if (e == kBcTabNone) atomicMin(inv, (unsigned long long)x);
+    }
+  };
   // block 0 and its masks (all threads)
   mt_block(raw[2], raw[0], [&](int, const uint64_t*) {});
   set_ring(0);
-  masks(0, kN - umax + 1, tid, kBcThreads);
+  masks(0, kN - umax + 1, tid, NT);
+  if (TAB) {
+    if (tid == 0) s_inv[0] = (unsigned long long)(kN - umax + 1);
+    __syncthreads();
+    build_table(0, kN - umax + 1, tid, NT, &s_inv[0]);
+  }
   __syncthreads();
 
   // chase state (warp 0, the same in every lane)
@@ -2370,6 +2423,9 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
         int16_t* rq = rec + q * kBcRec * 2;
         int16_t* fq = fpos + q * kBcFull;
         uint16_t* tq = ptask + q * 2 * LB;
+        int16_t* xq = rxs + q * kBcRec;
+        uint16_t* aq = ras + q * kBcRec;
+        uint16_t* fsq = rfs + q * kBcRec;
         const int64_t base = cx, e0 = cE;
         const int fs0 = cf[0], fs1 = cf[1];
         int nrec = 0, nf = 0, A[2] = {cf[0], cf[1]};
@@ -2393,6 +2449,40 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
               const int fsc = c == 0 ? fs0 : fs1;
               int acc = 0;
               int xr = (int)(cx - base);  // trial position relative to the step
+              if (TAB) {
+                // one table entry: the visit's end, its kind and the lanes its
+                // partial trials accept; the workers place those lanes
+                if (xr >= Mr) return 2;
+                const uint32_t e = vtab[((bm + xr) & (kBetaRing - 1)) * P + cf[c]];
+                if (e == kBcTabNone) return 2;
+                acc = (int)(e >> 11);
+                if (A[c] + acc > LB) return 1;
+                const int xe = xr + (int)(e & 1023u);
+                if (lane == 0) {
+                  xq[nrec] = (int16_t)xr;
+                  aq[nrec] = (uint16_t)A[c];
+                  fsq[nrec] = (uint16_t)cf[c];
+                }
+                if (e & (1u << 10)) {
+                  if (c == bc) {
+                    if (nf >= kBcFull) return 1;
+                    if (lane == 0) {
+                      fq[nf] = (int16_t)xe;
+                      rq[nrec * 2 + c] = (int16_t)(kBcFullTag + nf);
+                    }
+                    ++nf;
+                  } else if (lane == 0) {
+                    rq[nrec * 2 + c] = (int16_t)xe;
+                  }
+                  cf[c] += acc;
+                } else {
+                  if (lane == 0) rq[nrec * 2 + c] = (int16_t)(-(1 + (A[c] - cf[c])));
+                  cf[c] += acc - P;
+                }
+                A[c] += acc;
+                cx = base + xe + U;
+                return 0;
+              }
               for (;;) {
                 if (xr >= Mr) return 2;
                 const uint32_t m = pmask[c * kBetaRing + ((bm + xr) & (kBetaRing - 1))];
@@ -2471,8 +2561,31 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
         const int fs0 = S.fs[0], fs1 = S.fs[1];
         const int64_t base = S.base;
         const int16_t* rq = rec + q * kBcRec * 2;
-        const uint16_t* tq = ptask + q * 2 * LB;
+        uint16_t* tq = ptask + q * 2 * LB;
         set_ring(t);
+        if (TAB) {
+          // the accepted lanes of each record's partial trials at their FIFO
+          // slots (the visit walked again from its start)
+          const int U = gcomp == 0 ? U0 : U1;
+          const int bmq = (int)(base & (kBetaRing - 1));
+          const int fsg = gcomp == 0 ? fs0 : fs1;
+          for (int i = tt; i < nrec; i += kBcWork) {
+            int xr = rxs[q * kBcRec + i], run = 0;
+            const int a0 = ras[q * kBcRec + i] - fsg, f0 = rfs[q * kBcRec + i];
+            for (int d = 0; d < 1024; d += U, xr += U) {
+              const uint32_t m = pmask[gcomp * kBetaRing + ((bmq + xr) & (kBetaRing - 1))];
+              const int cn = __popc(m);
+              if (cn == P) break;
+              for (uint32_t mm = m; mm; mm &= mm - 1) {
+                const int j = __ffs(mm) - 1;
+                tq[gcomp * LB + a0 + run + __popc(m & ((1u << j) - 1u))] = (uint16_t)((xr << 3) | j);
+              }
+              run += cn;
+              if (f0 + run >= P) break;
+            }
+          }
+          asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
+        }
         // one task list, one lane per thread: full trials of the buffered
         // component, the accepted partial-trial lanes, positional values of
         // the other component
@@ -2555,6 +2668,17 @@ __global__ void __maxnreg__(80) k_beta(Plan p, BetaConsts bk, int64_t max_blocks
         asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
         set_ring(t + 1);
         masks(M, M + kN, tt, kBcWork);
+        if (TAB) {
+          // entries still unknown from the last build and the new positions;
+          // positions below (t - 1) * kN are behind any chase that has not
+          // failed, so their entries are never read again
+          const int q1 = (int)((t + 1) & 1);
+          if (tt == 0) s_inv[q1] = (unsigned long long)(M + kN);
+          asm volatile("bar.sync 1, %0;" ::"r"(kBcWork) : "memory");
+          int64_t from = (int64_t)min(s_inv[t & 1], (unsigned long long)M);
+          from = max(from, (t - 1) * (int64_t)kN);
+          build_table(from, M + kN, tt, kBcWork, &s_inv[q1]);
+        }
       }
     }
     __syncthreads();
@@ -2622,25 +2746,40 @@ static cudaError_t run_beta(const Plan& p, const DistParams& d, int64_t max_bloc
   bk.fpost = d.fh;
   bk.dpost = d.dh;
   static bool attr[64] = {};
+  static int sms[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  constexpr size_t smem = bc_smem_bytes<DT>();
+  constexpr size_t smem = bc_smem_bytes<DT, false>(), smem_t = bc_smem_bytes<DT, true>();
   if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k_beta<DT, -1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_beta<DT, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e = cudaFuncSetAttribute(k_beta<DT, -1, -1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_beta<DT, 1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e = cudaFuncSetAttribute(k_beta<DT, 2, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_beta<DT, 1, 2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_beta<DT, 2, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_beta<DT, 1, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t);
     if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
   // the GS + integral-alpha pairs (beta(a < 1, integer b) and the mirror)
-  // have kernels of their own
+  // have kernels of their own; with no more engines than SMs each engine's
+  // CTA has an SM to itself and runs the visit-table form
   const int t0 = bk.c[0].type, t1 = bk.c[1].type;
-  if (t0 == 2 && t1 == 1) k_beta<DT, 2, 1><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
-  else if (t0 == 1 && t1 == 2) k_beta<DT, 1, 2><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
-  else k_beta<DT, -1, -1><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
+  const bool alone = p.K <= sms[dev];
+  if (t0 == 2 && t1 == 1) {
+    if (alone) k_beta<DT, 2, 1, true><<<p.K, kBcThreadsAlone, smem_t, s>>>(p, bk, max_blocks);
+    else k_beta<DT, 2, 1, false><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
+  } else if (t0 == 1 && t1 == 2) {
+    if (alone) k_beta<DT, 1, 2, true><<<p.K, kBcThreadsAlone, smem_t, s>>>(p, bk, max_blocks);
+    else k_beta<DT, 1, 2, false><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
+  } else {
+    k_beta<DT, -1, -1, false><<<p.K, kBcThreads, smem, s>>>(p, bk, max_blocks);
+  }
   return cudaGetLastError();
 }
 
