@@ -78,7 +78,7 @@ def kernel_of(name, compat=False):
     base, tag = name.split("/")
     if compat:
         if base == "beta":
-            return f"k_beta<{'float' if tag == 'f32' else 'double'}, GS, integral> (one CTA)"
+            return f"k_beta<{'float' if tag == 'f32' else 'double'}, GS, integral> (one CTA, visit table)"
         if base == "poisson4":
             return "k_poisson (one CTA)"
         if base in ("gamma0.5", "poisson100"):
