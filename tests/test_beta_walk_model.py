@@ -7,19 +7,21 @@ packet from GammaGen(a), then one from GammaGen(b); a GS component
 packet and leaves the carried lanes alone; otherwise the accepted lanes are
 appended to the carry, and once it holds P lanes its oldest P are the output.
 
-k_beta resolves that automaton from accept masks evaluated ahead of the walk,
-and for single-engine calls through a visit table: per position x and carry
-f, where the GS visit starting there ends, whether on a full trial, and how
-many lanes its partial trials accept.  The chase reads one entry per output
-packet and records the visit's start, carry and FIFO tail; the workers walk
-each visit again one step later to place its accepted lanes.  The kernel keeps
+k_beta resolves that automaton from accept masks evaluated ahead of the walk.
+On engines that share an SM the chase walks trial by trial and writes the
+FIFO slots itself.  For single-engine calls it reads a visit table: per
+position x and carry f, where the GS visit starting there ends, whether on a
+full trial, and how many lanes its partial trials accept; the chase reads one
+entry per output packet and records the visit's start, carry and FIFO tail,
+and the workers walk each visit again one step later to place its accepted
+lanes.  The kernel keeps
 masks and table entries in 1024-slot rings, evaluates masks one engine block
 (312 packets) at a time, leaves an entry unknown while its visit runs past the
 evaluated masks, rebuilds unknown entries with the next block's masks (the
 chase may read an entry while it is rebuilt), and never looks further back
 than two blocks.  This model follows those steps and checks every output
 packet's sources, the FIFO lane order, the final position and carry against a
-direct restatement of the automaton, on random masks.
+direct restatement of the automaton, on random masks, for both forms.
 """
 import random
 
@@ -184,8 +186,89 @@ def table_pipeline(mask_at, P, ug, uc, order, f0, npk, rng, rec_cap=160, fifo_ca
     return out, carry, cx, cf
 
 
-@pytest.mark.parametrize("seed", range(12))
-def test_visit_table_pipeline_equals_automaton(seed):
+def trial_pipeline(mask_at, P, ug, uc, order, f0, npk, rec_cap=160, fifo_cap=112):
+    """The k_beta steps on engines that share an SM: the chase walks trial by
+    trial over the masks (positions below the evaluated limit only) and writes
+    each accepted partial lane's FIFO slot itself; a record that does not fit
+    rolls back to the next step; the workers read the slots one step later."""
+    lb = 16 + fifo_cap * P
+    umax = max(ug, uc, 3)
+    pmask = [0] * RING
+
+    def M_of(t):
+        return (t + 1) * KN - umax + 1
+
+    for x in range(M_of(0)):
+        pmask[x % RING] = mask_at(x)
+    cx, cf, ce, done = 0, f0, 0, False
+    steps, out, carry = {}, [], [("carried", i) for i in range(f0)]
+    t = 0
+    while True:
+        M, pk_lim = M_of(t), (t + 1) * KN
+        if not done:
+            assert cx >= (t - 1) * KN, "the chase fell more than two blocks behind"
+            base, fs, A, recs, slots = cx, cf, cf, [], {}
+            while ce < npk and len(recs) < rec_cap:
+                saved = (cx, cf, A, dict(slots))
+                rec, ok = [], True
+                for c in order:
+                    if c == "closed":
+                        if cx + uc > pk_lim:
+                            ok = False
+                            break
+                        rec.append(("pos", cx))
+                        cx += uc
+                        continue
+                    acc, xr, end = 0, cx, None
+                    while end is None:
+                        if xr >= M:
+                            break
+                        m = pmask[xr % RING]
+                        cn = popc(m)
+                        if cn == P:
+                            end = ("full", xr)
+                            cf += acc
+                            break
+                        if A + acc + cn > lb:
+                            break
+                        for j in range(P):
+                            if m >> j & 1:
+                                slots[A + acc - fs + popc(m & ((1 << j) - 1))] = (xr, j)
+                        acc += cn
+                        if cf + acc >= P:
+                            end = ("fifo", A - cf)
+                            cf += acc - P
+                            break
+                        xr += ug
+                    if end is None:
+                        ok = False
+                        break
+                    rec.append(end)
+                    A += acc
+                    cx = xr + ug
+                if not ok:
+                    cx, cf, A, slots = saved
+                    break
+                recs.append(tuple(rec))
+                ce += 1
+            steps[t] = (fs, A, cf, recs, slots)
+            finished = ce >= npk
+        if t >= 1 and steps.get(t - 1) and steps[t - 1][3]:
+            fs, a_end, f_end, recs, slots = steps[t - 1]
+            lanes = carry + [slots[i] for i in range(a_end - fs)]
+            for rec in recs:
+                out.append(tuple(("fifo", tuple(lanes[i[1]:i[1] + P])) if i[0] == "fifo" else i for i in rec))
+            carry = lanes[a_end - f_end:a_end]
+        if done:
+            break
+        for x in range(M, M + KN):
+            pmask[x % RING] = mask_at(x)
+        done = finished
+        t += 1
+    return out, carry, cx, cf
+
+
+def _case(seed):
     rng = random.Random(seed)
     P = rng.choice([4, 8])  # double and float packets
     uc = rng.choice([2, 3, 7, 19])  # integral alpha of the closed-form component
@@ -203,6 +286,20 @@ def test_visit_table_pipeline_equals_automaton(seed):
     ref, fifo, rx, rf = automaton(mask_at, P, 3, uc, order, f0, npk)
     lanes = [("carried", i) for i in range(f0)] + fifo
     want = [tuple(("fifo", tuple(lanes[i[1]:i[1] + P])) if i[0] == "fifo" else i for i in rec) for rec in ref]
+    return mask_at, P, uc, order, f0, npk, want, (rx, rf)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_trial_chase_pipeline_equals_automaton(seed):
+    mask_at, P, uc, order, f0, npk, want, end = _case(seed)
+    got, _, gx, gf = trial_pipeline(mask_at, P, 3, uc, order, f0, npk)
+    assert got == want
+    assert (gx, gf) == end
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_visit_table_pipeline_equals_automaton(seed):
+    mask_at, P, uc, order, f0, npk, want, end = _case(seed)
     got, _, gx, gf = table_pipeline(mask_at, P, 3, uc, order, f0, npk, random.Random(seed + 100))
     assert got == want
-    assert (gx, gf) == (rx, rf)
+    assert (gx, gf) == end
